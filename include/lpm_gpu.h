@@ -1,0 +1,126 @@
+/*
+ * lpm_gpu.h -- C ABI of the GB300 direct-sum library (liblpm_gpu.so).
+ *
+ * Drop-in replacements for the all-pairs direct sums of lpm-v2 that build each RK4
+ * stage's right-hand side.  Every entry point takes plain host pointers and sizes,
+ * copies to the GPU, runs the hand-written sm_103a kernels and copies the results back
+ * before returning (synchronous, like the Fortran routines they replace).  A Fortran
+ * caller binds them through iso_c_binding.
+ *
+ * Conventions shared by every entry point
+ *  - Arrays are contiguous, length n, in particle order (Fortran 1-based array base
+ *    pointers pass straight through).
+ *  - active[j] is 1 for active (panel-centre) particles and 0 for passive (vertex)
+ *    particles: the Fortran logical(klog) mask converted once with merge(1,0,mask).
+ *  - i_begin/i_end are 1-based and inclusive, the MPISetup indexStart/indexEnd of the
+ *    calling rank (src/MPISetup.f90:132-146).  Only outputs i_begin..i_end are written;
+ *    other entries are left untouched, as the reference leaves them for MPI_BCAST.
+ *  - mode selects the arithmetic:
+ *      LPM_MODE_FP64  : FP64, the reference expression association with no fused
+ *                       multiply-add, sources swept in ascending index order: results are
+ *                       bit-identical to the Fortran loop built without FMA contraction.
+ *      LPM_MODE_FP32C : pair arithmetic in FP32 with hi/lo positions, chord-form
+ *                       denominators, per-tile compensated (TwoSum) accumulation and an
+ *                       FP64 cross-tile reduction (velocity relative error <= 1e-6).
+ *    OR-ing LPM_FLAG_CHECK_FINITE makes the call fail with LPM_ERR_NONFINITE when an
+ *    output is NaN or Inf.
+ *  - Return value: LPM_OK (0) or a negative LPM_ERR_* code; lpm_last_error_string()
+ *    describes the last failure of the calling thread.  Nothing is thrown across the ABI.
+ */
+#ifndef LPM_GPU_H
+#define LPM_GPU_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  LPM_OK = 0,
+  LPM_ERR_ARG = -1,       /* bad argument (null pointer, n <= 0, bad range or mode) */
+  LPM_ERR_CUDA = -2,      /* a CUDA runtime call failed */
+  LPM_ERR_TIMEOUT = -3,   /* a bounded device-side wait gave up */
+  LPM_ERR_NONFINITE = -4, /* LPM_FLAG_CHECK_FINITE found a NaN/Inf output */
+  LPM_ERR_ALLOC = -5,     /* device or host allocation failed */
+  LPM_ERR_NO_DEVICE = -6, /* no usable CUDA device */
+  LPM_ERR_STATE = -7      /* handle used in a wrong state */
+};
+
+enum { LPM_MODE_FP64 = 0, LPM_MODE_FP32C = 1 };
+#define LPM_MODE_MASK 0xff
+#define LPM_FLAG_CHECK_FINITE 0x100
+
+/* PSE kernel selector */
+enum {
+  LPM_PSE_K8_GEODESIC = 0, /* bivariateLaplacianKernel8 of the great-circle distance */
+  LPM_PSE_GAUSS_CHORD = 1, /* second-order Gaussian, 4 exp(-r^2)/pi, chord distance    */
+  LPM_PSE_K8_CHORD = 2     /* bivariateLaplacianKernel8 of the chord distance          */
+};
+
+const char* lpm_last_error_string(void);
+/* Library version string and the compiled GPU architecture. */
+const char* lpm_version(void);
+
+/* ------------------------------------------------------------------ direct sums */
+
+/* Replaces BVESphereVelocity (src/SphereBVESolver.f90:377-430):
+ *   u_i = sum_{j != i, active} (x_i x x_j) * (-zeta_j A_j) / (4 pi a (a^2 - x_i.x_j))
+ * for i in [i_begin, i_end].  zeta is the RELATIVE vorticity.  rotationRate is not an
+ * argument because the reference sum never reads it. */
+int lpm_bve_velocity(int64_t n, const double* x, const double* y, const double* z,
+                     const double* zeta, const double* area, const int32_t* active,
+                     double radius, int64_t i_begin, int64_t i_end, double* u, double* v,
+                     double* w, int mode);
+
+/* Replaces setVelocityFromVorticity (src/SphereBVE.f90:489-531): the same sum with the
+ * denominator associated as a^2 - sum(x_i*x_j).  In LPM_MODE_FP32C it is identical to
+ * lpm_bve_velocity. */
+int lpm_bve_set_velocity_from_vorticity(int64_t n, const double* x, const double* y,
+                                        const double* z, const double* zeta,
+                                        const double* area, const int32_t* active,
+                                        double radius, int64_t i_begin, int64_t i_end,
+                                        double* u, double* v, double* w, int mode);
+
+/* Replaces planarIncompressibleVelocity (src/PlaneIncompressibleSolver.f90:278-316):
+ *   u_i = -sum omega_j A_j (y_i-y_j) / (2 pi (r^2 + delta^2)),
+ *   v_i = +sum omega_j A_j (x_i-x_j) / (2 pi (r^2 + delta^2)),  j != i, active.
+ * delta = 0 is the reference's singular kernel. */
+int lpm_plane_velocity(int64_t n, const double* x, const double* y, const double* omega,
+                       const double* area, const int32_t* active, double delta,
+                       int64_t i_begin, int64_t i_end, double* u, double* v, int mode);
+
+/* Replaces PSESphereLaplacianAtParticles (src/PSEDirectSum.f90:502-535) with
+ * kernel = LPM_PSE_K8_GEODESIC, and the Gaussian chord-distance variant with
+ * LPM_PSE_GAUSS_CHORD:
+ *   lap_i = eps^-4 sum_{j active} (f_j - f_i) A_j K(d_ij / eps)
+ * radius is the sphere radius used by the great-circle distance. */
+int lpm_pse_sphere_laplacian(int64_t n, const double* x, const double* y, const double* z,
+                             const double* f, const double* area, const int32_t* active,
+                             double eps, double radius, int kernel, int64_t i_begin,
+                             int64_t i_end, double* lap, int mode);
+
+/* Replaces PSEPlaneLaplacianAtParticles (src/PSEDirectSum.f90:467-500): K8 of the planar
+ * distance (kernel = LPM_PSE_K8_CHORD) or the Gaussian (LPM_PSE_GAUSS_CHORD). */
+int lpm_pse_plane_laplacian(int64_t n, const double* x, const double* y, const double* f,
+                            const double* area, const int32_t* active, double eps,
+                            int kernel, int64_t i_begin, int64_t i_end, double* lap,
+                            int mode);
+
+/* Replaces SetStreamFunctionsOnMesh (src/SphereBVE.f90:445-485): psi = sum G zeta A with
+ * G = -log(a^2 - x_i.x_j)/(4 pi), for the relative and absolute vorticity. */
+int lpm_bve_stream_functions(int64_t n, const double* x, const double* y, const double* z,
+                             const double* relvort, const double* absvort,
+                             const double* area, const int32_t* active, double radius,
+                             int64_t i_begin, int64_t i_end, double* psi_rel,
+                             double* psi_abs, int mode);
+
+/* Replaces SetStreamFunctionOnMesh (src/PlanarIncompressible.f90:470-505):
+ * psi = sum log(|x_i - x_j|)/(2 pi) omega_j A_j. */
+int lpm_plane_stream_function(int64_t n, const double* x, const double* y,
+                              const double* omega, const double* area,
+                              const int32_t* active, int64_t i_begin, int64_t i_end,
+                              double* psi, int mode);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

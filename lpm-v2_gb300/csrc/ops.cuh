@@ -1,0 +1,382 @@
+// ops.cuh -- pair operators of the direct sums, FP64 (reference association) and FP32C.
+//
+// Each FP32C operator defines
+//   Rec     : the source record staged through shared memory (16-byte multiple)
+//   Tgt     : the per-target register state
+//   NC      : number of accumulated components
+//   load_target(p, i) and interact(tgt, rec, acc[NC])
+// and a matching prep functor (in sums.cu) builds Rec from the particle arrays.  Each FP64
+// operator restates one Fortran loop body with explicit round-to-nearest intrinsics so
+// that nvcc cannot fuse a multiply into an add: every intermediate rounds exactly where
+// the Fortran rounds it.
+#pragma once
+
+#include "lpm_common.cuh"
+
+namespace lpm {
+
+// hi/lo split of a double: hi = fl32(v), lo = fl32(v - hi); hi + lo carries ~48 bits.
+__device__ __forceinline__ void split2(double v, float& hi, float& lo) {
+  hi = __double2float_rn(v);
+  lo = __double2float_rn(v - static_cast<double>(hi));
+}
+
+// difference of two hi/lo numbers: (ah - bh) + (al - bl).  For nearby values ah - bh is
+// exact (Sterbenz), so near pairs keep ~48-bit differences.
+__device__ __forceinline__ float diff2(float ah, float al, float bh, float bl) {
+  return __fadd_rn(__fsub_rn(ah, bh), __fsub_rn(al, bl));
+}
+
+// ============================================================ sphere BVE velocity
+// Reference: BVESphereVelocity, src/SphereBVESolver.f90:395-420.
+//
+// FP32C form.  With unit-scaled positions p = x/a, d = p_i - p_j and c = |p|^2 - 1,
+//   a^2 - x_i.x_j = a^2 (|d|^2 - c_i - c_j) / 2      (exact identity, no cancellation)
+//   x_i x x_j     = a^2 (d x p_i)
+// so u_i = [ sum_j S_j d / (|d|^2 - c_i - c_j) ] x p_i with S_j = -zeta_j A_j / (2 pi a).
+// The cross product leaves the sum: per pair 17 FP32 operations + 1 MUFU.RCP.
+struct BveF32 {
+  static constexpr int NC = 3;
+  struct __align__(16) Rec {
+    float4 a;  // p_hi.x, p_hi.y, p_hi.z, -c
+    float4 b;  // S, p_lo.x, p_lo.y, p_lo.z
+  };
+  struct Tgt {
+    float xh, yh, zh, xl, yl, zl, nc;
+  };
+  struct Params {
+    const double *x, *y, *z;
+    double inv_a;
+  };
+  // -c_i is offset by 2^-100 so that a self pair (d = 0) on an exactly normalised particle
+  // gives a finite weight times d = 0 instead of inf * 0.  |c| is either 0 or >= 2^-54, so
+  // the offset never changes a nonzero c.
+  __device__ static Tgt load_target(const Params& p, int64_t i) {
+    Tgt t;
+    const double px = p.x[i] * p.inv_a, py = p.y[i] * p.inv_a, pz = p.z[i] * p.inv_a;
+    split2(px, t.xh, t.xl);
+    split2(py, t.yh, t.yl);
+    split2(pz, t.zh, t.zl);
+    const double c = fma(px, px, fma(py, py, fma(pz, pz, -1.0)));
+    t.nc = __double2float_rn(-c) + 7.888609052210118e-31f;  // + 2^-100
+    return t;
+  }
+  __device__ static __forceinline__ void interact(const Tgt& t, const Rec& r, float (&acc)[3]) {
+    const float dx = diff2(t.xh, t.xl, r.a.x, r.b.y);
+    const float dy = diff2(t.yh, t.yl, r.a.y, r.b.z);
+    const float dz = diff2(t.zh, t.zl, r.a.z, r.b.w);
+    float q = __fadd_rn(t.nc, r.a.w);
+    q = __fmaf_rn(dx, dx, q);
+    q = __fmaf_rn(dy, dy, q);
+    q = __fmaf_rn(dz, dz, q);
+    const float wgt = __fmul_rn(r.b.x, rcp_approx(q));
+    acc[0] = __fmaf_rn(wgt, dx, acc[0]);
+    acc[1] = __fmaf_rn(wgt, dy, acc[1]);
+    acc[2] = __fmaf_rn(wgt, dz, acc[2]);
+  }
+};
+
+// FP64 source record shared by the sphere sums: position, q = zeta*A (or f and A for PSE)
+struct __align__(16) Rec64 {
+  double x, y, z, q;
+  double r;       // second scalar (area for PSE, absolute vorticity for the stream function)
+  long long idx;  // particle index (self-interaction test)
+};
+
+struct BveF64Params {
+  const double *x, *y, *z;
+  double a2, kden;  // a*a and fl(fl(4 pi) a)
+  double *u, *v, *w;
+};
+
+// ASSOC 0: ((a^2 - xi xj) - yi yj) - zi zj   (SphereBVESolver.f90:403-404)
+// ASSOC 1: a^2 - ((xi xj + yi yj) + zi zj)   (SphereBVE.f90:509, sum(xi*xj))
+template <int ASSOC>
+struct BveF64 {
+  struct Tgt {
+    double x, y, z;
+  };
+  struct Acc {
+    double u, v, w;
+  };
+  __device__ static Tgt load(const BveF64Params& p, int64_t i) { return Tgt{p.x[i], p.y[i], p.z[i]}; }
+  __device__ static __forceinline__ void interact(const BveF64Params& p, const Tgt& t,
+                                                  const Rec64& r, Acc& a) {
+    double den;
+    if (ASSOC == 0) {
+      den = __dsub_rn(__dsub_rn(__dsub_rn(p.a2, __dmul_rn(t.x, r.x)), __dmul_rn(t.y, r.y)),
+                      __dmul_rn(t.z, r.z));
+    } else {
+      den = __dsub_rn(p.a2, __dadd_rn(__dadd_rn(__dmul_rn(t.x, r.x), __dmul_rn(t.y, r.y)),
+                                      __dmul_rn(t.z, r.z)));
+    }
+    const double s = -__ddiv_rn(r.q, __dmul_rn(p.kden, den));
+    a.u = __dadd_rn(a.u, __dmul_rn(__dsub_rn(__dmul_rn(t.y, r.z), __dmul_rn(t.z, r.y)), s));
+    a.v = __dadd_rn(a.v, __dmul_rn(__dsub_rn(__dmul_rn(t.z, r.x), __dmul_rn(t.x, r.z)), s));
+    a.w = __dadd_rn(a.w, __dmul_rn(__dsub_rn(__dmul_rn(t.x, r.y), __dmul_rn(t.y, r.x)), s));
+  }
+  __device__ static void store(const BveF64Params& p, int64_t i, int64_t il, const Acc& a) {
+    p.u[il] = a.u;
+    p.v[il] = a.v;
+    p.w[il] = a.w;
+  }
+  static constexpr bool kSkipSelf = true;
+};
+
+// ============================================================ planar velocity
+// Reference: planarIncompressibleVelocity, src/PlaneIncompressibleSolver.f90:291-308.
+// FP32C: U = sum S d_y / (r^2 + delta^2), V = sum S d_x / (r^2 + delta^2), S = omega A/(2 pi);
+// u = -U, v = V.  delta^2 carries a 2^-100 offset so a self pair gives 0 * finite.
+struct PlaneF32 {
+  static constexpr int NC = 2;
+  struct __align__(16) Rec {
+    float4 a;  // x_hi, y_hi, x_lo, y_lo
+    float4 b;  // S, 0, 0, 0
+  };
+  struct Tgt {
+    float xh, yh, xl, yl, d2;
+  };
+  struct Params {
+    const double *x, *y;
+    float d2;  // delta^2 + 2^-100
+  };
+  __device__ static Tgt load_target(const Params& p, int64_t i) {
+    Tgt t;
+    split2(p.x[i], t.xh, t.xl);
+    split2(p.y[i], t.yh, t.yl);
+    t.d2 = p.d2;
+    return t;
+  }
+  __device__ static __forceinline__ void interact(const Tgt& t, const Rec& r, float (&acc)[2]) {
+    const float dx = diff2(t.xh, t.xl, r.a.x, r.a.z);
+    const float dy = diff2(t.yh, t.yl, r.a.y, r.a.w);
+    float q = __fmaf_rn(dx, dx, t.d2);
+    q = __fmaf_rn(dy, dy, q);
+    const float wgt = __fmul_rn(r.b.x, rcp_approx(q));
+    acc[0] = __fmaf_rn(wgt, dy, acc[0]);
+    acc[1] = __fmaf_rn(wgt, dx, acc[1]);
+  }
+};
+
+struct __align__(16) RecPlane64 {
+  double x, y, q;
+  long long idx;
+};
+
+struct PlaneF64Params {
+  const double *x, *y;
+  double two_pi, d2;
+  double *u, *v;
+};
+
+struct PlaneF64 {
+  struct Tgt {
+    double x, y;
+  };
+  struct Acc {
+    double u, v;
+  };
+  __device__ static Tgt load(const PlaneF64Params& p, int64_t i) { return Tgt{p.x[i], p.y[i]}; }
+  __device__ static __forceinline__ void interact(const PlaneF64Params& p, const Tgt& t,
+                                                  const RecPlane64& r, Acc& a) {
+    const double dx = __dsub_rn(t.x, r.x);
+    const double dy = __dsub_rn(t.y, r.y);
+    const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), p.d2);
+    const double s = __ddiv_rn(r.q, __dmul_rn(p.two_pi, r2));
+    a.u = __dsub_rn(a.u, __dmul_rn(dy, s));
+    a.v = __dadd_rn(a.v, __dmul_rn(dx, s));
+  }
+  __device__ static void store(const PlaneF64Params& p, int64_t i, int64_t il, const Acc& a) {
+    p.u[il] = a.u;
+    p.v[il] = a.v;
+  }
+  static constexpr bool kSkipSelf = true;
+};
+
+// ============================================================ PSE Laplacian
+// Reference: PSESphereLaplacianAtParticles / PSEPlaneLaplacianAtParticles,
+// src/PSEDirectSum.f90:467-535, kernel bivariateLaplacianKernel8 (:622-627).
+// KIND 0: K8 of the great-circle distance (SphereDistance, SphereGeometry.f90:107-125)
+// KIND 1: Gaussian 4 exp(-r^2)/pi of the chord distance
+// KIND 2: K8 of the chord distance (ChordDistance, SphereGeometry.f90:67-73)
+enum { kPseK8Geodesic = 0, kPseGaussChord = 1, kPseK8Chord = 2 };
+
+// FP32C form: positions scaled by 1/R and split hi/lo, f split hi/lo; per pair
+//   acc += (f_j - f_i) A_j P(r^2) exp(-r^2)
+// with the constant factor (1/pi or 4/pi, times eps^-4) applied once in the FP64 finish.
+// The great-circle angle is atan2(|d x p_i|, p_i.p_j) with p_i.p_j = (|p_i|^2+|p_j|^2-|d|^2)/2,
+// both free of cancellation for near pairs.
+template <int KIND>
+struct PseF32 {
+  static constexpr int NC = 1;
+  struct __align__(16) Rec {
+    float4 a;  // p_hi.x, p_hi.y, p_hi.z, f_hi
+    float4 b;  // p_lo.x, p_lo.y, p_lo.z, f_lo
+    float4 c;  // A, |p|^2, 0, 0
+  };
+  struct Tgt {
+    float xh, yh, zh, xl, yl, zl, fh, fl, n2, ks;
+  };
+  struct Params {
+    const double *x, *y, *z, *f;
+    double inv_r;  // 1/R (1 for the plane)
+    float ks;      // R/eps: r = theta R/eps (geodesic) or |d| R/eps (chord)
+  };
+  __device__ static Tgt load_target(const Params& p, int64_t i) {
+    Tgt t;
+    const double px = p.x[i] * p.inv_r, py = p.y[i] * p.inv_r;
+    const double pz = p.z ? p.z[i] * p.inv_r : 0.0;
+    split2(px, t.xh, t.xl);
+    split2(py, t.yh, t.yl);
+    split2(pz, t.zh, t.zl);
+    split2(p.f[i], t.fh, t.fl);
+    t.n2 = __double2float_rn(fma(px, px, fma(py, py, pz * pz)));
+    t.ks = p.ks;
+    return t;
+  }
+  __device__ static __forceinline__ void interact(const Tgt& t, const Rec& r, float (&acc)[1]) {
+    const float dx = diff2(t.xh, t.xl, r.a.x, r.b.x);
+    const float dy = diff2(t.yh, t.yl, r.a.y, r.b.y);
+    const float dz = diff2(t.zh, t.zl, r.a.z, r.b.z);
+    const float df = diff2(r.a.w, r.b.w, t.fh, t.fl);  // f_j - f_i
+    const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+    float r2;
+    if (KIND == kPseK8Geodesic) {
+      const float cx = __fmaf_rn(dy, t.zh, -__fmul_rn(dz, t.yh));
+      const float cy = __fmaf_rn(dz, t.xh, -__fmul_rn(dx, t.zh));
+      const float cz = __fmaf_rn(dx, t.yh, -__fmul_rn(dy, t.xh));
+      const float cn = sqrtf(__fmaf_rn(cz, cz, __fmaf_rn(cy, cy, __fmul_rn(cx, cx))));
+      const float dot = 0.5f * ((t.n2 + r.c.y) - d2);
+      const float rr = atan2f(cn, dot) * t.ks;
+      r2 = rr * rr;
+    } else {
+      r2 = d2 * (t.ks * t.ks);
+    }
+    float k = expf(-r2);
+    if (KIND != kPseGaussChord) {
+      const float poly =
+          __fmaf_rn(__fmaf_rn(__fmaf_rn(-0.6666666666666666f, r2, 10.0f), r2, -40.0f), r2, 40.0f);
+      k = poly * k;
+    }
+    acc[0] = __fmaf_rn(df, r.c.x * k, acc[0]);
+  }
+};
+
+// FP64 K8, bivariateLaplacianKernel8 with gfortran's integer-power chain
+// (r^2 = r r, r^4 = r^2 r^2, r^6 = r^3 r^3 with r^3 = r r^2).
+__device__ __forceinline__ double k8_f64(double r) {
+  const double r2 = __dmul_rn(r, r);
+  const double r3 = __dmul_rn(r, r2);
+  const double r4 = __dmul_rn(r2, r2);
+  const double r6 = __dmul_rn(r3, r3);
+  const double poly = __dsub_rn(__dadd_rn(__dsub_rn(40.0, __dmul_rn(40.0, r2)), __dmul_rn(10.0, r4)),
+                                __ddiv_rn(__dmul_rn(2.0, r6), 3.0));
+  return __ddiv_rn(__dmul_rn(poly, exp(-__dmul_rn(r, r))), 3.1415926535897932384626433832795027975);
+}
+
+struct PseF64Params {
+  const double *x, *y, *z, *f;
+  double eps, eps2, scale, radius;
+  double* lap;
+};
+
+template <int KIND>
+struct PseF64 {
+  struct Tgt {
+    double x, y, z, f;
+  };
+  struct Acc {
+    double l;
+  };
+  __device__ static Tgt load(const PseF64Params& p, int64_t i) {
+    return Tgt{p.x[i], p.y[i], p.z ? p.z[i] : 0.0, p.f[i]};
+  }
+  __device__ static __forceinline__ void interact(const PseF64Params& p, const Tgt& t,
+                                                  const Rec64& r, Acc& a) {
+    double k;
+    if (KIND == kPseK8Geodesic) {
+      const double c1 = __dsub_rn(__dmul_rn(t.y, r.z), __dmul_rn(r.y, t.z));
+      const double c2 = __dsub_rn(__dmul_rn(r.x, t.z), __dmul_rn(t.x, r.z));
+      const double c3 = __dsub_rn(__dmul_rn(t.x, r.y), __dmul_rn(r.x, t.y));
+      const double cn = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(c1, c1), __dmul_rn(c2, c2)), __dmul_rn(c3, c3)));
+      const double dp = __dadd_rn(__dadd_rn(__dmul_rn(t.x, r.x), __dmul_rn(t.y, r.y)), __dmul_rn(t.z, r.z));
+      const double kin = __ddiv_rn(__dmul_rn(atan2(cn, dp), p.radius), p.eps);
+      k = k8_f64(kin);
+    } else {
+      const double d1 = __dsub_rn(r.x, t.x), d2 = __dsub_rn(r.y, t.y), d3 = __dsub_rn(r.z, t.z);
+      const double kin = __ddiv_rn(
+          __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(d1, d1), __dmul_rn(d2, d2)), __dmul_rn(d3, d3))), p.eps);
+      if (KIND == kPseGaussChord) {
+        k = __ddiv_rn(__dmul_rn(4.0, exp(-__dmul_rn(kin, kin))), 3.1415926535897932384626433832795027975);
+      } else {
+        k = k8_f64(kin);
+      }
+    }
+    a.l = __dadd_rn(a.l, __dmul_rn(__ddiv_rn(__dmul_rn(__dsub_rn(r.q, t.f), k), p.eps2), r.r));
+  }
+  __device__ static void store(const PseF64Params& p, int64_t i, int64_t il, const Acc& a) {
+    p.lap[il] = __dmul_rn(a.l, p.scale);
+  }
+  static constexpr bool kSkipSelf = false;
+};
+
+// ============================================================ stream functions (FP64)
+// SetStreamFunctionsOnMesh, src/SphereBVE.f90:445-485 and SetStreamFunctionOnMesh,
+// src/PlanarIncompressible.f90:470-505.  Both skip j = i.
+struct __align__(16) RecStream64 {
+  double x, y, z, qr, qa, area;
+  long long idx;
+  long long pad;
+};
+
+struct StreamF64Params {
+  const double *x, *y, *z;
+  double a2, four_pi, two_pi;
+  double *psi_rel, *psi_abs;
+};
+
+// G = -log(a^2 - sum(xi*xj)) / (4 pi); psi_rel += (G zeta_rel) A, psi_abs += (G zeta_abs) A
+struct SphereStreamF64 {
+  struct Tgt {
+    double x, y, z;
+  };
+  struct Acc {
+    double r, a;
+  };
+  __device__ static Tgt load(const StreamF64Params& p, int64_t i) { return Tgt{p.x[i], p.y[i], p.z[i]}; }
+  __device__ static __forceinline__ void interact(const StreamF64Params& p, const Tgt& t,
+                                                  const RecStream64& r, Acc& a) {
+    const double dot = __dadd_rn(__dadd_rn(__dmul_rn(t.x, r.x), __dmul_rn(t.y, r.y)), __dmul_rn(t.z, r.z));
+    const double g = -__ddiv_rn(log(__dsub_rn(p.a2, dot)), p.four_pi);
+    a.r = __dadd_rn(a.r, __dmul_rn(__dmul_rn(g, r.qr), r.area));
+    a.a = __dadd_rn(a.a, __dmul_rn(__dmul_rn(g, r.qa), r.area));
+  }
+  __device__ static void store(const StreamF64Params& p, int64_t i, int64_t il, const Acc& a) {
+    p.psi_rel[il] = a.r;
+    p.psi_abs[il] = a.a;
+  }
+  static constexpr bool kSkipSelf = true;
+};
+
+// G = log(sqrt((xi-xj)^2 + (yi-yj)^2)) / (2 pi); psi += (G omega) A
+struct PlaneStreamF64 {
+  struct Tgt {
+    double x, y, z;
+  };
+  struct Acc {
+    double r;
+  };
+  __device__ static Tgt load(const StreamF64Params& p, int64_t i) { return Tgt{p.x[i], p.y[i], 0.0}; }
+  __device__ static __forceinline__ void interact(const StreamF64Params& p, const Tgt& t,
+                                                  const RecStream64& r, Acc& a) {
+    const double dx = __dsub_rn(t.x, r.x), dy = __dsub_rn(t.y, r.y);
+    const double g = __ddiv_rn(log(__dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)))), p.two_pi);
+    a.r = __dadd_rn(a.r, __dmul_rn(__dmul_rn(g, r.qr), r.area));
+  }
+  __device__ static void store(const StreamF64Params& p, int64_t i, int64_t il, const Acc& a) {
+    p.psi_rel[il] = a.r;
+  }
+  static constexpr bool kSkipSelf = true;
+};
+
+}  // namespace lpm

@@ -1,0 +1,698 @@
+// sums.cu -- direct-sum kernels (prep, sweep, finish), their launchers and the host-buffer
+// C-ABI entry points lpm_bve_velocity, lpm_plane_velocity, lpm_pse_*_laplacian and the
+// stream functions.
+#include <cmath>
+#include <vector>
+
+#include "engine.cuh"
+#include "ops.cuh"
+#include "sums.cuh"
+
+namespace lpm {
+
+namespace {
+
+constexpr double kPi = 3.1415926535897932384626433832795027975;
+
+// FP32C sweep shapes (threads per CTA, targets per thread, tile, min CTAs per SM)
+constexpr int kBveThreads = 128, kBveTpt = 4, kBveTile = 256, kBveMinB = 4;
+constexpr int kPlaneThreads = 128, kPlaneTpt = 4, kPlaneTile = 256, kPlaneMinB = 4;
+constexpr int kPseThreads = 128, kPseTpt = 2, kPseTile = 128, kPseMinB = 4;
+// FP64 sequential sweep shape
+constexpr int k64Threads = 128, k64Tile = 128;
+
+// ------------------------------------------------------------------ FP64 sequential sweep
+// One thread per target, sources in ascending particle order, one accumulator: the same
+// summation order as the Fortran j loop, hence bit-identical sums.
+template <class Op, class Rec, class P>
+__global__ void __launch_bounds__(k64Threads) seq_fp64_kernel(P p, const Rec* __restrict__ src,
+                                                              int64_t ns, int64_t ib, int64_t nt,
+                                                              int* status) {
+  __shared__ __align__(128) Rec stage[2][k64Tile];
+  __shared__ __align__(8) uint64_t bars[2];
+  const int64_t il = static_cast<int64_t>(blockIdx.x) * k64Threads + threadIdx.x;
+  const bool valid = il < nt;
+  const int64_t i = ib + (valid ? il : nt - 1);
+  const typename Op::Tgt t = Op::load(p, i);
+  typename Op::Acc acc{};
+  const int64_t n_tiles = ceil_div(ns, k64Tile);
+  int64_t tile = 0;
+  staged_sweep<Rec, k64Tile>(src, 0, n_tiles, stage[0], stage[1], bars, status,
+                             [&](const Rec* tl) {
+                               const int64_t j0 = tile * k64Tile;
+                               const int cnt = static_cast<int>(ns - j0 < k64Tile ? ns - j0 : k64Tile);
+                               for (int j = 0; j < cnt; ++j) {
+                                 const Rec& r = tl[j];
+                                 if (Op::kSkipSelf && r.idx == i) continue;
+                                 Op::interact(p, t, r, acc);
+                               }
+                               ++tile;
+                             });
+  if (valid) Op::store(p, i, il, acc);
+}
+
+// ------------------------------------------------------------------ prep kernels
+// Gather the active particles (src_idx) into source records; records ns..npad-1 are inert.
+
+__global__ void prep_rec64_kernel(const double* x, const double* y, const double* z,
+                                  const double* s1, const double* area, const int32_t* idx,
+                                  int64_t ns, int pse, Rec64* out) {
+  const int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= ns) return;
+  const int64_t j = idx[k];
+  Rec64 r;
+  r.x = x[j];
+  r.y = y[j];
+  r.z = z ? z[j] : 0.0;
+  if (pse) {
+    r.q = s1[j];  // f_j
+    r.r = area[j];
+  } else {
+    r.q = __dmul_rn(s1[j], area[j]);  // zeta_j * A_j, the first product of the Fortran term
+    r.r = 0.0;
+  }
+  r.idx = j;
+  out[k] = r;
+}
+
+__global__ void prep_plane64_kernel(const double* x, const double* y, const double* omega,
+                                    const double* area, const int32_t* idx, int64_t ns,
+                                    RecPlane64* out) {
+  const int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= ns) return;
+  const int64_t j = idx[k];
+  RecPlane64 r;
+  r.x = x[j];
+  r.y = y[j];
+  r.q = __dmul_rn(omega[j], area[j]);
+  r.idx = j;
+  out[k] = r;
+}
+
+__global__ void prep_stream64_kernel(const double* x, const double* y, const double* z,
+                                     const double* qr, const double* qa, const double* area,
+                                     const int32_t* idx, int64_t ns, RecStream64* out) {
+  const int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= ns) return;
+  const int64_t j = idx[k];
+  RecStream64 r;
+  r.x = x[j];
+  r.y = y[j];
+  r.z = z ? z[j] : 0.0;
+  r.qr = qr[j];
+  r.qa = qa ? qa[j] : 0.0;
+  r.area = area[j];
+  r.idx = j;
+  r.pad = 0;
+  out[k] = r;
+}
+
+// S_j = -zeta_j A_j / (2 pi a); position scaled by 1/a and split hi/lo; -c_j = 1 - |p_j|^2
+__global__ void prep_bve32_kernel(const double* x, const double* y, const double* z,
+                                  const double* zeta, const double* area, const int32_t* idx,
+                                  int64_t ns, int64_t npad, double inv_a, double s_scale,
+                                  BveF32::Rec* out) {
+  const int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= npad) return;
+  BveF32::Rec r;
+  if (k < ns) {
+    const int64_t j = idx[k];
+    const double px = x[j] * inv_a, py = y[j] * inv_a, pz = z[j] * inv_a;
+    float h, l;
+    split2(px, h, l);
+    r.a.x = h;
+    r.b.y = l;
+    split2(py, h, l);
+    r.a.y = h;
+    r.b.z = l;
+    split2(pz, h, l);
+    r.a.z = h;
+    r.b.w = l;
+    r.a.w = __double2float_rn(-fma(px, px, fma(py, py, fma(pz, pz, -1.0))));
+    r.b.x = __double2float_rn(zeta[j] * area[j] * s_scale);
+  } else {
+    // inert: at the origin with zero strength (q = |p_i|^2 - c_i = 1 > 0, weight 0)
+    r.a = make_float4(0.f, 0.f, 0.f, 0.f);
+    r.b = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  out[k] = r;
+}
+
+__global__ void prep_plane32_kernel(const double* x, const double* y, const double* omega,
+                                    const double* area, const int32_t* idx, int64_t ns,
+                                    int64_t npad, double s_scale, PlaneF32::Rec* out) {
+  const int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= npad) return;
+  PlaneF32::Rec r;
+  if (k < ns) {
+    const int64_t j = idx[k];
+    float h, l;
+    split2(x[j], h, l);
+    r.a.x = h;
+    r.a.z = l;
+    split2(y[j], h, l);
+    r.a.y = h;
+    r.a.w = l;
+    r.b = make_float4(__double2float_rn(omega[j] * area[j] * s_scale), 0.f, 0.f, 0.f);
+  } else {
+    r.a = make_float4(0.f, 0.f, 0.f, 0.f);
+    r.b = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  out[k] = r;
+}
+
+template <int KIND>
+__global__ void prep_pse32_kernel(const double* x, const double* y, const double* z,
+                                  const double* f, const double* area, const int32_t* idx,
+                                  int64_t ns, int64_t npad, double inv_r,
+                                  typename PseF32<KIND>::Rec* out) {
+  const int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= npad) return;
+  typename PseF32<KIND>::Rec r;
+  if (k < ns) {
+    const int64_t j = idx[k];
+    const double px = x[j] * inv_r, py = y[j] * inv_r, pz = z ? z[j] * inv_r : 0.0;
+    float h, l;
+    split2(px, h, l);
+    r.a.x = h;
+    r.b.x = l;
+    split2(py, h, l);
+    r.a.y = h;
+    r.b.y = l;
+    split2(pz, h, l);
+    r.a.z = h;
+    r.b.z = l;
+    split2(f[j], h, l);
+    r.a.w = h;
+    r.b.w = l;
+    r.c = make_float4(__double2float_rn(area[j]), __double2float_rn(fma(px, px, fma(py, py, pz * pz))),
+                      0.f, 0.f);
+  } else {
+    r.a = make_float4(0.f, 0.f, 0.f, 0.f);
+    r.b = make_float4(0.f, 0.f, 0.f, 0.f);
+    r.c = make_float4(0.f, 0.f, 0.f, 0.f);  // zero area: contributes nothing
+  }
+  out[k] = r;
+}
+
+// ------------------------------------------------------------------ finish kernels
+// Fixed-order FP64 reduction over the split-K chunks, then the per-target epilogue.
+
+__global__ void finish_bve_kernel(const double* partial, int64_t nsplit, int64_t nt, int64_t ib,
+                                  const double* x, const double* y, const double* z, double inv_a,
+                                  double* u, double* v, double* w) {
+  const int64_t il = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (il >= nt) return;
+  double d0 = 0.0, d1 = 0.0, d2 = 0.0;
+  for (int64_t c = 0; c < nsplit; ++c) {
+    d0 += partial[(c * 3 + 0) * nt + il];
+    d1 += partial[(c * 3 + 1) * nt + il];
+    d2 += partial[(c * 3 + 2) * nt + il];
+  }
+  const int64_t i = ib + il;
+  const double px = x[i] * inv_a, py = y[i] * inv_a, pz = z[i] * inv_a;
+  u[il] = d1 * pz - d2 * py;
+  v[il] = d2 * px - d0 * pz;
+  w[il] = d0 * py - d1 * px;
+}
+
+__global__ void finish_plane_kernel(const double* partial, int64_t nsplit, int64_t nt, double* u,
+                                    double* v) {
+  const int64_t il = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (il >= nt) return;
+  double su = 0.0, sv = 0.0;
+  for (int64_t c = 0; c < nsplit; ++c) {
+    su += partial[(c * 2 + 0) * nt + il];
+    sv += partial[(c * 2 + 1) * nt + il];
+  }
+  u[il] = -su;
+  v[il] = sv;
+}
+
+__global__ void finish_scalar_kernel(const double* partial, int64_t nsplit, int64_t nt,
+                                     double scale, double* out) {
+  const int64_t il = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (il >= nt) return;
+  double s = 0.0;
+  for (int64_t c = 0; c < nsplit; ++c) s += partial[c * nt + il];
+  out[il] = s * scale;
+}
+
+template <class Op, int THREADS, int TPT, int TILE, int MINB>
+void launch_sweep(const SumJob& job, const SumPlan& plan, const typename Op::Params& p) {
+  SweepArgs<Op> a;
+  a.p = p;
+  a.src = static_cast<const typename Op::Rec*>(job.src_buf);
+  a.n_tiles = plan.n_tiles;
+  a.tiles_per_chunk = plan.tiles_per_chunk;
+  a.ib = job.ib;
+  a.nt = job.nt;
+  a.partial = job.partial;
+  a.status = job.status;
+  const dim3 grid(static_cast<unsigned>(ceil_div(job.nt, THREADS * TPT)), static_cast<unsigned>(plan.nsplit));
+  sweep_fp32c_kernel<Op, THREADS, TPT, TILE, MINB><<<grid, THREADS, 0, job.stream>>>(a);
+}
+
+int tile_of(int kind, int mode) {
+  if (mode == LPM_MODE_FP64) return k64Tile;
+  switch (kind) {
+    case kSumBve:
+    case kSumBveMesh:
+      return kBveTile;
+    case kSumPlane:
+      return kPlaneTile;
+    default:
+      return kPseTile;
+  }
+}
+
+size_t rec_bytes(int kind, int mode) {
+  if (mode == LPM_MODE_FP64) {
+    if (kind == kSumPlane) return sizeof(RecPlane64);
+    if (kind == kSumSphereStream || kind == kSumPlaneStream) return sizeof(RecStream64);
+    return sizeof(Rec64);
+  }
+  switch (kind) {
+    case kSumBve:
+    case kSumBveMesh:
+      return sizeof(BveF32::Rec);
+    case kSumPlane:
+      return sizeof(PlaneF32::Rec);
+    default:
+      return sizeof(PseF32<0>::Rec);
+  }
+}
+
+int comps_of(int kind) {
+  switch (kind) {
+    case kSumBve:
+    case kSumBveMesh:
+      return 3;
+    case kSumPlane:
+      return 2;
+    default:
+      return 1;
+  }
+}
+
+int targets_per_cta(int kind) {
+  switch (kind) {
+    case kSumBve:
+    case kSumBveMesh:
+      return kBveThreads * kBveTpt;
+    case kSumPlane:
+      return kPlaneThreads * kPlaneTpt;
+    default:
+      return kPseThreads * kPseTpt;
+  }
+}
+
+}  // namespace
+
+int kernels_per_sum(int mode) { return mode == LPM_MODE_FP64 ? 2 : 3; }
+
+SumPlan plan_sum(int kind, int mode, int64_t ns, int64_t nt, int sm_count) {
+  SumPlan pl;
+  const int tile = tile_of(kind, mode);
+  pl.n_tiles = ceil_div(ns > 0 ? ns : 1, tile);
+  pl.src_bytes = static_cast<size_t>(pl.n_tiles) * tile * rec_bytes(kind, mode);
+  if (mode == LPM_MODE_FP64) {
+    pl.nsplit = 1;
+    pl.tiles_per_chunk = pl.n_tiles;
+    pl.partial_bytes = 0;
+    return pl;
+  }
+  // Split the source range until the grid covers about two waves of resident CTAs.
+  const int64_t tblocks = ceil_div(nt, targets_per_cta(kind));
+  const int64_t want = static_cast<int64_t>(sm_count > 0 ? sm_count : 152) * 4 * 2;
+  int64_t nsplit = ceil_div(want, tblocks);
+  if (nsplit < 1) nsplit = 1;
+  if (nsplit > pl.n_tiles) nsplit = pl.n_tiles;
+  if (nsplit > 65535) nsplit = 65535;
+  pl.tiles_per_chunk = ceil_div(pl.n_tiles, nsplit);
+  pl.nsplit = ceil_div(pl.n_tiles, pl.tiles_per_chunk);
+  pl.partial_bytes = static_cast<size_t>(pl.nsplit) * comps_of(kind) * nt * sizeof(double);
+  return pl;
+}
+
+int launch_sum(const SumJob& job, const SumPlan& plan) {
+  const int pb = 256;
+  const unsigned prep_grid_ns = static_cast<unsigned>(ceil_div(job.ns > 0 ? job.ns : 1, pb));
+  const unsigned fin_grid = static_cast<unsigned>(ceil_div(job.nt, pb));
+  const int tile = tile_of(job.kind, job.mode);
+  const int64_t npad = plan.n_tiles * tile;
+  const unsigned prep_grid_pad = static_cast<unsigned>(ceil_div(npad, pb));
+
+  if (job.mode == LPM_MODE_FP64) {
+    const unsigned g = static_cast<unsigned>(ceil_div(job.nt, k64Threads));
+    switch (job.kind) {
+      case kSumBve:
+      case kSumBveMesh: {
+        prep_rec64_kernel<<<prep_grid_ns, pb, 0, job.stream>>>(job.x, job.y, job.z, job.s1, job.area,
+                                                               job.src_idx, job.ns, 0,
+                                                               static_cast<Rec64*>(job.src_buf));
+        BveF64Params p{job.x, job.y, job.z, job.radius * job.radius, (4.0 * kPi) * job.radius,
+                       job.out0, job.out1, job.out2};
+        if (job.kind == kSumBve) {
+          seq_fp64_kernel<BveF64<0>, Rec64><<<g, k64Threads, 0, job.stream>>>(
+              p, static_cast<const Rec64*>(job.src_buf), job.ns, job.ib, job.nt, job.status);
+        } else {
+          seq_fp64_kernel<BveF64<1>, Rec64><<<g, k64Threads, 0, job.stream>>>(
+              p, static_cast<const Rec64*>(job.src_buf), job.ns, job.ib, job.nt, job.status);
+        }
+        break;
+      }
+      case kSumPlane: {
+        prep_plane64_kernel<<<prep_grid_ns, pb, 0, job.stream>>>(job.x, job.y, job.s1, job.area, job.src_idx,
+                                                                 job.ns, static_cast<RecPlane64*>(job.src_buf));
+        PlaneF64Params p{job.x, job.y, 2.0 * kPi, job.delta * job.delta, job.out0, job.out1};
+        seq_fp64_kernel<PlaneF64, RecPlane64><<<g, k64Threads, 0, job.stream>>>(
+            p, static_cast<const RecPlane64*>(job.src_buf), job.ns, job.ib, job.nt, job.status);
+        break;
+      }
+      case kSumPseK8Geo:
+      case kSumPseGaussChord:
+      case kSumPseK8Chord: {
+        prep_rec64_kernel<<<prep_grid_ns, pb, 0, job.stream>>>(job.x, job.y, job.z, job.s1, job.area,
+                                                               job.src_idx, job.ns, 1,
+                                                               static_cast<Rec64*>(job.src_buf));
+        const double eps2 = job.eps * job.eps;
+        PseF64Params p{job.x, job.y, job.z, job.s1, job.eps, eps2, 1.0 / eps2, job.radius, job.out0};
+        const Rec64* src = static_cast<const Rec64*>(job.src_buf);
+        if (job.kind == kSumPseK8Geo) {
+          seq_fp64_kernel<PseF64<kPseK8Geodesic>, Rec64><<<g, k64Threads, 0, job.stream>>>(
+              p, src, job.ns, job.ib, job.nt, job.status);
+        } else if (job.kind == kSumPseGaussChord) {
+          seq_fp64_kernel<PseF64<kPseGaussChord>, Rec64><<<g, k64Threads, 0, job.stream>>>(
+              p, src, job.ns, job.ib, job.nt, job.status);
+        } else {
+          seq_fp64_kernel<PseF64<kPseK8Chord>, Rec64><<<g, k64Threads, 0, job.stream>>>(
+              p, src, job.ns, job.ib, job.nt, job.status);
+        }
+        break;
+      }
+      case kSumSphereStream:
+      case kSumPlaneStream: {
+        prep_stream64_kernel<<<prep_grid_ns, pb, 0, job.stream>>>(job.x, job.y, job.z, job.s1, job.s2,
+                                                                  job.area, job.src_idx, job.ns,
+                                                                  static_cast<RecStream64*>(job.src_buf));
+        StreamF64Params p{job.x, job.y, job.z, job.radius * job.radius, 4.0 * kPi, 2.0 * kPi, job.out0, job.out1};
+        const RecStream64* src = static_cast<const RecStream64*>(job.src_buf);
+        if (job.kind == kSumSphereStream) {
+          seq_fp64_kernel<SphereStreamF64, RecStream64><<<g, k64Threads, 0, job.stream>>>(
+              p, src, job.ns, job.ib, job.nt, job.status);
+        } else {
+          seq_fp64_kernel<PlaneStreamF64, RecStream64><<<g, k64Threads, 0, job.stream>>>(
+              p, src, job.ns, job.ib, job.nt, job.status);
+        }
+        break;
+      }
+      default:
+        return set_error(LPM_ERR_ARG, "unknown sum kind %d", job.kind);
+    }
+    LPM_CUDA_TRY(cudaGetLastError());
+    return LPM_OK;
+  }
+
+  // ---------------- FP32C
+  switch (job.kind) {
+    case kSumBve:
+    case kSumBveMesh: {
+      const double inv_a = 1.0 / job.radius;
+      prep_bve32_kernel<<<prep_grid_pad, pb, 0, job.stream>>>(
+          job.x, job.y, job.z, job.s1, job.area, job.src_idx, job.ns, npad, inv_a,
+          -1.0 / (2.0 * kPi * job.radius), static_cast<BveF32::Rec*>(job.src_buf));
+      BveF32::Params p{job.x, job.y, job.z, inv_a};
+      launch_sweep<BveF32, kBveThreads, kBveTpt, kBveTile, kBveMinB>(job, plan, p);
+      finish_bve_kernel<<<fin_grid, pb, 0, job.stream>>>(job.partial, plan.nsplit, job.nt, job.ib, job.x,
+                                                         job.y, job.z, inv_a, job.out0, job.out1, job.out2);
+      break;
+    }
+    case kSumPlane: {
+      prep_plane32_kernel<<<prep_grid_pad, pb, 0, job.stream>>>(job.x, job.y, job.s1, job.area, job.src_idx,
+                                                                job.ns, npad, 1.0 / (2.0 * kPi),
+                                                                static_cast<PlaneF32::Rec*>(job.src_buf));
+      PlaneF32::Params p{job.x, job.y, static_cast<float>(job.delta * job.delta) + 7.888609052210118e-31f};
+      launch_sweep<PlaneF32, kPlaneThreads, kPlaneTpt, kPlaneTile, kPlaneMinB>(job, plan, p);
+      finish_plane_kernel<<<fin_grid, pb, 0, job.stream>>>(job.partial, plan.nsplit, job.nt, job.out0,
+                                                           job.out1);
+      break;
+    }
+    case kSumPseK8Geo:
+    case kSumPseGaussChord:
+    case kSumPseK8Chord: {
+      const bool sphere = job.kind != kSumPseK8Chord;
+      const double inv_r = sphere ? 1.0 / job.radius : 1.0;
+      const double rscale = sphere ? job.radius : 1.0;
+      const float ks = static_cast<float>(rscale / job.eps);
+      const double e4 = (job.eps * job.eps) * (job.eps * job.eps);
+      const double cscale = (job.kind == kSumPseGaussChord ? 4.0 : 1.0) / kPi / e4;
+      if (job.kind == kSumPseK8Geo) {
+        using Op = PseF32<kPseK8Geodesic>;
+        prep_pse32_kernel<kPseK8Geodesic><<<prep_grid_pad, pb, 0, job.stream>>>(
+            job.x, job.y, job.z, job.s1, job.area, job.src_idx, job.ns, npad, inv_r,
+            static_cast<Op::Rec*>(job.src_buf));
+        launch_sweep<Op, kPseThreads, kPseTpt, kPseTile, kPseMinB>(job, plan,
+                                                                   Op::Params{job.x, job.y, job.z, job.s1, inv_r, ks});
+      } else if (job.kind == kSumPseGaussChord) {
+        using Op = PseF32<kPseGaussChord>;
+        prep_pse32_kernel<kPseGaussChord><<<prep_grid_pad, pb, 0, job.stream>>>(
+            job.x, job.y, job.z, job.s1, job.area, job.src_idx, job.ns, npad, inv_r,
+            static_cast<Op::Rec*>(job.src_buf));
+        launch_sweep<Op, kPseThreads, kPseTpt, kPseTile, kPseMinB>(job, plan,
+                                                                   Op::Params{job.x, job.y, job.z, job.s1, inv_r, ks});
+      } else {
+        using Op = PseF32<kPseK8Chord>;
+        prep_pse32_kernel<kPseK8Chord><<<prep_grid_pad, pb, 0, job.stream>>>(
+            job.x, job.y, job.z, job.s1, job.area, job.src_idx, job.ns, npad, inv_r,
+            static_cast<Op::Rec*>(job.src_buf));
+        launch_sweep<Op, kPseThreads, kPseTpt, kPseTile, kPseMinB>(job, plan,
+                                                                   Op::Params{job.x, job.y, job.z, job.s1, inv_r, ks});
+      }
+      finish_scalar_kernel<<<fin_grid, pb, 0, job.stream>>>(job.partial, plan.nsplit, job.nt, cscale, job.out0);
+      break;
+    }
+    default:
+      return set_error(LPM_ERR_ARG, "sum kind %d has no FP32C form", job.kind);
+  }
+  LPM_CUDA_TRY(cudaGetLastError());
+  return LPM_OK;
+}
+
+// ------------------------------------------------------------------ host-buffer entry points
+
+namespace {
+
+struct HostArgs {
+  int kind;
+  int64_t n;
+  const double *x, *y, *z, *s1, *s2, *area;
+  const int32_t* active;
+  double radius, delta, eps;
+  int64_t i_begin, i_end;  // 1-based inclusive
+  double *out0, *out1, *out2;
+  int mode;
+};
+
+int check_common(const HostArgs& a, int nout) {
+  if (a.n <= 0) return set_error(LPM_ERR_ARG, "n must be positive (got %lld)", (long long)a.n);
+  if (!a.x || !a.y || !a.s1 || !a.area || !a.active)
+    return set_error(LPM_ERR_ARG, "null input array");
+  if (!a.out0 || (nout > 1 && !a.out1) || (nout > 2 && !a.out2))
+    return set_error(LPM_ERR_ARG, "null output array");
+  if (a.i_begin < 1 || a.i_end > a.n || a.i_begin > a.i_end)
+    return set_error(LPM_ERR_ARG, "target range [%lld, %lld] is not inside [1, %lld]", (long long)a.i_begin,
+                     (long long)a.i_end, (long long)a.n);
+  const int prec = a.mode & LPM_MODE_MASK;
+  if (prec != LPM_MODE_FP64 && prec != LPM_MODE_FP32C)
+    return set_error(LPM_ERR_ARG, "unknown precision mode %d", prec);
+  if ((a.mode & ~(LPM_MODE_MASK | LPM_FLAG_CHECK_FINITE)) != 0)
+    return set_error(LPM_ERR_ARG, "unknown mode flags 0x%x", a.mode);
+  return LPM_OK;
+}
+
+int run_host(const HostArgs& a, int nout) {
+  Context* ctx = nullptr;
+  LPM_TRY(get_context(&ctx));
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  clear_error();
+  const int prec = a.mode & LPM_MODE_MASK;
+  const int64_t n = a.n;
+  const int64_t ib = a.i_begin - 1;
+  const int64_t nt = a.i_end - a.i_begin + 1;
+
+  std::vector<int32_t> idx;
+  idx.reserve(static_cast<size_t>(n));
+  for (int64_t j = 0; j < n; ++j)
+    if (a.active[j]) idx.push_back(static_cast<int32_t>(j));
+  const int64_t ns = static_cast<int64_t>(idx.size());
+
+  const bool has_z = a.z != nullptr;
+  const bool has_s2 = a.s2 != nullptr;
+  const int narr = 4 + (has_z ? 1 : 0) + (has_s2 ? 1 : 0);  // x, y, s1, area (+z, +s2)
+  void* p_in = nullptr;
+  LPM_TRY(workspace(ctx, kWsTargets, static_cast<size_t>(narr) * n * sizeof(double), &p_in));
+  double* d = static_cast<double*>(p_in);
+  double* dx = d;
+  double* dy = d + n;
+  double* ds1 = d + 2 * n;
+  double* darea = d + 3 * n;
+  double* dz = has_z ? d + 4 * n : nullptr;
+  double* ds2 = has_s2 ? d + (4 + (has_z ? 1 : 0)) * n : nullptr;
+  const size_t nb = static_cast<size_t>(n) * sizeof(double);
+  cudaStream_t s = ctx->stream;
+  LPM_CUDA_TRY(cudaMemcpyAsync(dx, a.x, nb, cudaMemcpyHostToDevice, s));
+  LPM_CUDA_TRY(cudaMemcpyAsync(dy, a.y, nb, cudaMemcpyHostToDevice, s));
+  LPM_CUDA_TRY(cudaMemcpyAsync(ds1, a.s1, nb, cudaMemcpyHostToDevice, s));
+  LPM_CUDA_TRY(cudaMemcpyAsync(darea, a.area, nb, cudaMemcpyHostToDevice, s));
+  if (has_z) LPM_CUDA_TRY(cudaMemcpyAsync(dz, a.z, nb, cudaMemcpyHostToDevice, s));
+  if (has_s2) LPM_CUDA_TRY(cudaMemcpyAsync(ds2, a.s2, nb, cudaMemcpyHostToDevice, s));
+
+  void* p_out = nullptr;
+  LPM_TRY(workspace(ctx, kWsOutput, static_cast<size_t>(nout) * nt * sizeof(double), &p_out));
+  double* dout = static_cast<double*>(p_out);
+
+  if (ns == 0) {
+    LPM_CUDA_TRY(cudaMemsetAsync(dout, 0, static_cast<size_t>(nout) * nt * sizeof(double), s));
+  } else {
+    void* p_idx = nullptr;
+    LPM_TRY(workspace(ctx, kWsActive, static_cast<size_t>(ns) * sizeof(int32_t), &p_idx));
+    LPM_CUDA_TRY(cudaMemcpyAsync(p_idx, idx.data(), static_cast<size_t>(ns) * sizeof(int32_t),
+                                 cudaMemcpyHostToDevice, s));
+    const SumPlan plan = plan_sum(a.kind, prec, ns, nt, ctx->sm_count);
+    SumJob job;
+    job.kind = a.kind;
+    job.mode = prec;
+    job.n = n;
+    job.x = dx;
+    job.y = dy;
+    job.z = dz;
+    job.s1 = ds1;
+    job.s2 = ds2;
+    job.area = darea;
+    job.src_idx = static_cast<const int32_t*>(p_idx);
+    job.ns = ns;
+    job.radius = a.radius;
+    job.delta = a.delta;
+    job.eps = a.eps;
+    job.ib = ib;
+    job.nt = nt;
+    job.out0 = dout;
+    job.out1 = nout > 1 ? dout + nt : nullptr;
+    job.out2 = nout > 2 ? dout + 2 * nt : nullptr;
+    LPM_TRY(workspace(ctx, kWsSources, plan.src_bytes, &job.src_buf));
+    if (plan.partial_bytes) {
+      void* pp = nullptr;
+      LPM_TRY(workspace(ctx, kWsPartial, plan.partial_bytes, &pp));
+      job.partial = static_cast<double*>(pp);
+    }
+    job.status = ctx->d_status;
+    job.stream = s;
+    LPM_TRY(launch_sum(job, plan));
+  }
+  double* outs[3] = {a.out0, a.out1, a.out2};
+  for (int c = 0; c < nout; ++c) {
+    LPM_CUDA_TRY(cudaMemcpyAsync(outs[c] + ib, dout + c * nt, static_cast<size_t>(nt) * sizeof(double),
+                                 cudaMemcpyDeviceToHost, s));
+  }
+  LPM_TRY(sync_and_check(ctx, "direct sum"));
+  if (a.mode & LPM_FLAG_CHECK_FINITE) {
+    for (int c = 0; c < nout; ++c) {
+      for (int64_t i = ib; i < ib + nt; ++i) {
+        if (!std::isfinite(outs[c][i])) {
+          return set_error(LPM_ERR_NONFINITE, "non-finite output %d at particle %lld", c, (long long)(i + 1));
+        }
+      }
+    }
+  }
+  return LPM_OK;
+}
+
+}  // namespace
+}  // namespace lpm
+
+using lpm::HostArgs;
+
+extern "C" int lpm_bve_velocity(int64_t n, const double* x, const double* y, const double* z,
+                                const double* zeta, const double* area, const int32_t* active,
+                                double radius, int64_t i_begin, int64_t i_end, double* u, double* v,
+                                double* w, int mode) {
+  HostArgs a{lpm::kSumBve, n, x, y, z, zeta, nullptr, area, active, radius, 0.0, 0.0, i_begin, i_end, u, v, w, mode};
+  LPM_TRY(lpm::check_common(a, 3));
+  if (!z) return lpm::set_error(LPM_ERR_ARG, "null z array");
+  if (!(radius > 0.0)) return lpm::set_error(LPM_ERR_ARG, "radius must be positive");
+  return lpm::run_host(a, 3);
+}
+
+extern "C" int lpm_bve_set_velocity_from_vorticity(int64_t n, const double* x, const double* y,
+                                                   const double* z, const double* zeta, const double* area,
+                                                   const int32_t* active, double radius, int64_t i_begin,
+                                                   int64_t i_end, double* u, double* v, double* w, int mode) {
+  HostArgs a{lpm::kSumBveMesh, n, x, y, z, zeta, nullptr, area, active, radius, 0.0, 0.0, i_begin, i_end, u, v, w, mode};
+  LPM_TRY(lpm::check_common(a, 3));
+  if (!z) return lpm::set_error(LPM_ERR_ARG, "null z array");
+  if (!(radius > 0.0)) return lpm::set_error(LPM_ERR_ARG, "radius must be positive");
+  return lpm::run_host(a, 3);
+}
+
+extern "C" int lpm_plane_velocity(int64_t n, const double* x, const double* y, const double* omega,
+                                  const double* area, const int32_t* active, double delta, int64_t i_begin,
+                                  int64_t i_end, double* u, double* v, int mode) {
+  HostArgs a{lpm::kSumPlane, n, x, y, nullptr, omega, nullptr, area, active, 1.0, delta, 0.0, i_begin, i_end, u, v, nullptr, mode};
+  LPM_TRY(lpm::check_common(a, 2));
+  if (!(delta >= 0.0)) return lpm::set_error(LPM_ERR_ARG, "delta must be >= 0");
+  return lpm::run_host(a, 2);
+}
+
+extern "C" int lpm_pse_sphere_laplacian(int64_t n, const double* x, const double* y, const double* z,
+                                        const double* f, const double* area, const int32_t* active, double eps,
+                                        double radius, int kernel, int64_t i_begin, int64_t i_end, double* lap,
+                                        int mode) {
+  int kind;
+  if (kernel == LPM_PSE_K8_GEODESIC) kind = lpm::kSumPseK8Geo;
+  else if (kernel == LPM_PSE_GAUSS_CHORD) kind = lpm::kSumPseGaussChord;
+  else return lpm::set_error(LPM_ERR_ARG, "unknown sphere PSE kernel %d", kernel);
+  HostArgs a{kind, n, x, y, z, f, nullptr, area, active, radius, 0.0, eps, i_begin, i_end, lap, nullptr, nullptr, mode};
+  LPM_TRY(lpm::check_common(a, 1));
+  if (!z) return lpm::set_error(LPM_ERR_ARG, "null z array");
+  if (!(eps > 0.0) || !(radius > 0.0)) return lpm::set_error(LPM_ERR_ARG, "eps and radius must be positive");
+  return lpm::run_host(a, 1);
+}
+
+extern "C" int lpm_pse_plane_laplacian(int64_t n, const double* x, const double* y, const double* f,
+                                       const double* area, const int32_t* active, double eps, int kernel,
+                                       int64_t i_begin, int64_t i_end, double* lap, int mode) {
+  int kind;
+  if (kernel == LPM_PSE_K8_CHORD) kind = lpm::kSumPseK8Chord;
+  else if (kernel == LPM_PSE_GAUSS_CHORD) kind = lpm::kSumPseGaussChord;
+  else return lpm::set_error(LPM_ERR_ARG, "unknown plane PSE kernel %d", kernel);
+  HostArgs a{kind, n, x, y, nullptr, f, nullptr, area, active, 1.0, 0.0, eps, i_begin, i_end, lap, nullptr, nullptr, mode};
+  LPM_TRY(lpm::check_common(a, 1));
+  if (!(eps > 0.0)) return lpm::set_error(LPM_ERR_ARG, "eps must be positive");
+  return lpm::run_host(a, 1);
+}
+
+extern "C" int lpm_bve_stream_functions(int64_t n, const double* x, const double* y, const double* z,
+                                        const double* relvort, const double* absvort, const double* area,
+                                        const int32_t* active, double radius, int64_t i_begin, int64_t i_end,
+                                        double* psi_rel, double* psi_abs, int mode) {
+  HostArgs a{lpm::kSumSphereStream, n, x, y, z, relvort, absvort, area, active, radius, 0.0, 0.0,
+             i_begin, i_end, psi_rel, psi_abs, nullptr, mode};
+  LPM_TRY(lpm::check_common(a, 2));
+  if (!z || !absvort) return lpm::set_error(LPM_ERR_ARG, "null z or absvort array");
+  if (!(radius > 0.0)) return lpm::set_error(LPM_ERR_ARG, "radius must be positive");
+  if ((mode & LPM_MODE_MASK) != LPM_MODE_FP64)
+    return lpm::set_error(LPM_ERR_ARG, "the stream functions are computed in LPM_MODE_FP64 only");
+  return lpm::run_host(a, 2);
+}
+
+extern "C" int lpm_plane_stream_function(int64_t n, const double* x, const double* y, const double* omega,
+                                         const double* area, const int32_t* active, int64_t i_begin,
+                                         int64_t i_end, double* psi, int mode) {
+  HostArgs a{lpm::kSumPlaneStream, n, x, y, nullptr, omega, nullptr, area, active, 1.0, 0.0, 0.0,
+             i_begin, i_end, psi, nullptr, nullptr, mode};
+  LPM_TRY(lpm::check_common(a, 1));
+  if ((mode & LPM_MODE_MASK) != LPM_MODE_FP64)
+    return lpm::set_error(LPM_ERR_ARG, "the stream function is computed in LPM_MODE_FP64 only");
+  return lpm::run_host(a, 1);
+}

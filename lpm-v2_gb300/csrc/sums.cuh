@@ -1,0 +1,65 @@
+// sums.cuh -- device-level launchers of the direct sums (shared by the host-buffer entry
+// points and the device-resident solvers).  All pointers are device pointers; nothing here
+// allocates, so the launches can be captured into CUDA graphs.
+#pragma once
+
+#include "lpm_common.cuh"
+
+namespace lpm {
+
+// Scratch layout of one direct-sum launch: compacted source records, then the split-K
+// partial sums (FP32C only).
+struct SumPlan {
+  int64_t n_tiles = 0;       // source tiles (ns padded to a tile multiple)
+  int64_t tiles_per_chunk = 0;
+  int64_t nsplit = 1;        // split-K chunks (gridDim.y)
+  size_t src_bytes = 0;      // bytes of the padded source-record array
+  size_t partial_bytes = 0;  // bytes of the FP64 partial sums
+};
+
+enum SumKind : int {
+  kSumBve = 0,        // sphere BVE velocity, BVESphereVelocity association
+  kSumBveMesh,        // sphere BVE velocity, setVelocityFromVorticity association
+  kSumPlane,          // planar Biot-Savart velocity
+  kSumPseK8Geo,       // PSE Laplacian, K8 + great-circle distance
+  kSumPseGaussChord,  // PSE Laplacian, Gaussian + chord distance
+  kSumPseK8Chord,     // PSE Laplacian, K8 + chord distance (plane)
+  kSumSphereStream,   // sphere stream functions (FP64 only)
+  kSumPlaneStream     // planar stream function (FP64 only)
+};
+
+// Inputs of one direct sum over particles [0, n): sources are the ns particles listed (in
+// ascending order) by src_idx; targets are particles ib .. ib+nt-1.
+struct SumJob {
+  int kind = kSumBve;
+  int mode = LPM_MODE_FP64;  // LPM_MODE_FP64 or LPM_MODE_FP32C
+  int64_t n = 0;
+  const double *x = nullptr, *y = nullptr, *z = nullptr;
+  const double* s1 = nullptr;  // zeta (BVE), omega (plane), f (PSE), relvort (stream)
+  const double* s2 = nullptr;  // absvort (sphere stream), unused otherwise
+  const double* area = nullptr;
+  const int32_t* src_idx = nullptr;
+  int64_t ns = 0;
+  double radius = 1.0;  // sphere radius (BVE, PSE, stream)
+  double delta = 0.0;   // planar regularisation
+  double eps = 1.0;     // PSE radius
+  int64_t ib = 0, nt = 0;
+  double* out0 = nullptr;  // u / lap / psi_rel   (length nt)
+  double* out1 = nullptr;  // v / psi_abs
+  double* out2 = nullptr;  // w
+  // scratch (sizes from plan_sum)
+  void* src_buf = nullptr;
+  double* partial = nullptr;
+  int* status = nullptr;
+  cudaStream_t stream = nullptr;
+};
+
+// Decides tiles and split-K for a job on a device with sm_count SMs.
+SumPlan plan_sum(int kind, int mode, int64_t ns, int64_t nt, int sm_count);
+// Enqueues prep + sweep (+ finish) on job.stream.
+int launch_sum(const SumJob& job, const SumPlan& plan);
+
+// Velocity-sum kernels launched by launch_sum for a job (for launch counting).
+int kernels_per_sum(int mode);
+
+}  // namespace lpm

@@ -1,0 +1,430 @@
+"""Python binding of liblpm_gpu.so (the GB300 direct-sum library) through its C ABI.
+
+The functions mirror the lpm-v2 routines they replace -- same names (snake_case), same
+argument meaning, 1-based inclusive target ranges -- so a test reads like the reference's
+own code.  Every call goes through the C ABI declared in include/lpm_gpu.h; there is no
+CPU fallback: if the library cannot be loaded, or a call fails, LpmError is raised.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from pathlib import Path
+
+import numpy as np
+
+PKG_DIR = Path(__file__).resolve().parent
+LIB_PATH = PKG_DIR / "liblpm_gpu.so"
+
+MODE_FP64 = 0
+MODE_FP32C = 1
+FLAG_CHECK_FINITE = 0x100
+PSE_K8_GEODESIC = 0
+PSE_GAUSS_CHORD = 1
+PSE_K8_CHORD = 2
+
+QUAD_RECT_SEED = 202
+ICOS_TRI_SPHERE_SEED = 205
+CUBED_SPHERE_SEED = 206
+
+ERRORS = {
+    0: "LPM_OK",
+    -1: "LPM_ERR_ARG",
+    -2: "LPM_ERR_CUDA",
+    -3: "LPM_ERR_TIMEOUT",
+    -4: "LPM_ERR_NONFINITE",
+    -5: "LPM_ERR_ALLOC",
+    -6: "LPM_ERR_NO_DEVICE",
+    -7: "LPM_ERR_STATE",
+}
+
+
+class LpmError(RuntimeError):
+    """A liblpm_gpu call returned a negative status."""
+
+    def __init__(self, code: int, message: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {message}")
+        self.code = code
+
+
+_D = ctypes.POINTER(ctypes.c_double)
+_I = ctypes.POINTER(ctypes.c_int32)
+_L = ctypes.POINTER(ctypes.c_int64)
+_i64 = ctypes.c_int64
+_dbl = ctypes.c_double
+_int = ctypes.c_int
+_vp = ctypes.c_void_p
+_pvp = ctypes.POINTER(ctypes.c_void_p)
+
+# name -> argtypes (restype int unless listed in _RESTYPES)
+_SIGNATURES = {
+    "lpm_last_error_string": [],
+    "lpm_version": [],
+    "lpm_bve_velocity": [_i64, _D, _D, _D, _D, _D, _I, _dbl, _i64, _i64, _D, _D, _D, _int],
+    "lpm_bve_set_velocity_from_vorticity": [_i64, _D, _D, _D, _D, _D, _I, _dbl, _i64, _i64, _D, _D, _D, _int],
+    "lpm_plane_velocity": [_i64, _D, _D, _D, _D, _I, _dbl, _i64, _i64, _D, _D, _int],
+    "lpm_pse_sphere_laplacian": [_i64, _D, _D, _D, _D, _D, _I, _dbl, _dbl, _int, _i64, _i64, _D, _int],
+    "lpm_pse_plane_laplacian": [_i64, _D, _D, _D, _D, _I, _dbl, _int, _i64, _i64, _D, _int],
+    "lpm_bve_stream_functions": [_i64, _D, _D, _D, _D, _D, _D, _I, _dbl, _i64, _i64, _D, _D, _int],
+    "lpm_plane_stream_function": [_i64, _D, _D, _D, _D, _I, _i64, _i64, _D, _int],
+    "lpm_bve_solver_create": [_pvp, _i64, _D, _D, _D, _D, _D, _I, _D, _D, _D, _dbl, _dbl, _int],
+    "lpm_bve_timestep": [_vp, _dbl, _int, _int],
+    "lpm_bve_get_state": [_vp, _D, _D, _D, _D, _D, _D, _D],
+    "lpm_bve_set_state": [_vp, _D, _D, _D, _D, _D, _D, _D],
+    "lpm_bve_diagnostics": [_vp, _D, _D, _D],
+    "lpm_bve_kernel_timing": [_vp, _D, _L],
+    "lpm_bve_solver_destroy": [_vp],
+    "lpm_plane_solver_create": [_pvp, _i64, _D, _D, _D, _D, _I, _D, _D, _dbl, _int],
+    "lpm_plane_timestep": [_vp, _dbl, _int],
+    "lpm_plane_get_state": [_vp, _D, _D, _D, _D],
+    "lpm_plane_diagnostics": [_vp, _D, _D, _D],
+    "lpm_plane_solver_destroy": [_vp],
+    "lpm_ensemble_create": [_pvp, _int, _L, _D, _D, _D, _D, _D, _I, _D, _D, _int],
+    "lpm_ensemble_timestep": [_vp, _dbl, _int],
+    "lpm_ensemble_velocity": [_vp],
+    "lpm_ensemble_get_state": [_vp, _D, _D, _D, _D, _D, _D, _D],
+    "lpm_ensemble_kernel_timing": [_vp, _D, _L],
+    "lpm_ensemble_destroy": [_vp],
+    "lpm_mesh_create": [_pvp, _int, _int, _dbl],
+    "lpm_mesh_destroy": [_vp],
+    "lpm_mesh_n_particles": [_vp],
+    "lpm_mesh_n_active": [_vp],
+    "lpm_mesh_n_faces": [_vp],
+    "lpm_mesh_n_edges": [_vp],
+    "lpm_mesh_n_leaf_edges": [_vp],
+    "lpm_mesh_is_spherical": [_vp],
+    "lpm_mesh_get_particles": [_vp, _D, _D, _D, _D, _I],
+    "lpm_mesh_max_edge_length": [_vp],
+    "lpm_mesh_avg_edge_length": [_vp],
+}
+_RESTYPES = {
+    "lpm_last_error_string": ctypes.c_char_p,
+    "lpm_version": ctypes.c_char_p,
+    "lpm_mesh_destroy": None,
+    "lpm_mesh_n_particles": _i64,
+    "lpm_mesh_n_active": _i64,
+    "lpm_mesh_n_faces": _i64,
+    "lpm_mesh_n_edges": _i64,
+    "lpm_mesh_n_leaf_edges": _i64,
+    "lpm_mesh_max_edge_length": _dbl,
+    "lpm_mesh_avg_edge_length": _dbl,
+}
+
+_LIB = None
+
+
+def lib() -> ctypes.CDLL:
+    """Loads liblpm_gpu.so (built by build.py).  Raises if it is missing: no fallback."""
+    global _LIB
+    if _LIB is None:
+        path = Path(os.environ.get("LPM_GPU_LIB", LIB_PATH))
+        if not path.exists():
+            raise LpmError(-6, f"{path} is missing: build it with __graft_entry__.build() (no CPU fallback)")
+        L = ctypes.CDLL(str(path))
+        for name, args in _SIGNATURES.items():
+            fn = getattr(L, name, None)
+            if fn is None:
+                continue
+            fn.argtypes = args
+            fn.restype = _RESTYPES.get(name, ctypes.c_int)
+        _LIB = L
+    return _LIB
+
+
+def version() -> str:
+    return lib().lpm_version().decode()
+
+
+def _check(rc: int) -> None:
+    if rc != 0:
+        msg = lib().lpm_last_error_string().decode(errors="replace")
+        raise LpmError(rc, msg)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _i32(a):
+    return np.ascontiguousarray(np.asarray(a).astype(np.int32, copy=False))
+
+
+def _dp(a):
+    return None if a is None else a.ctypes.data_as(_D)
+
+
+def _ip(a):
+    return a.ctypes.data_as(_I)
+
+
+def _mode(mode) -> int:
+    if isinstance(mode, str):
+        return {"fp64": MODE_FP64, "fp32c": MODE_FP32C}[mode.lower()]
+    return int(mode)
+
+
+def _range(n, i_begin, i_end):
+    ib = 1 if i_begin is None else int(i_begin)
+    ie = n if i_end is None else int(i_end)
+    return ib, ie
+
+
+# ------------------------------------------------------------------ direct sums
+def bve_sphere_velocity(x, y, z, rel_vort, area, active_mask, sphere_radius=1.0, i_begin=None, i_end=None,
+                        mode="fp64", out=None):
+    """BVESphereVelocity (src/SphereBVESolver.f90:377).  Returns (u, v, w) of length n; only
+    entries i_begin..i_end (1-based, inclusive) are written."""
+    x, y, z, rel_vort, area = (_f64(a) for a in (x, y, z, rel_vort, area))
+    act = _i32(active_mask)
+    n = x.size
+    ib, ie = _range(n, i_begin, i_end)
+    u, v, w = out if out is not None else (np.zeros(n), np.zeros(n), np.zeros(n))
+    _check(lib().lpm_bve_velocity(n, _dp(x), _dp(y), _dp(z), _dp(rel_vort), _dp(area), _ip(act),
+                                  float(sphere_radius), ib, ie, _dp(u), _dp(v), _dp(w), _mode(mode)))
+    return u, v, w
+
+
+def set_velocity_from_vorticity(x, y, z, rel_vort, area, active_mask, sphere_radius=1.0, i_begin=None,
+                                i_end=None, mode="fp64"):
+    """setVelocityFromVorticity (src/SphereBVE.f90:489)."""
+    x, y, z, rel_vort, area = (_f64(a) for a in (x, y, z, rel_vort, area))
+    act = _i32(active_mask)
+    n = x.size
+    ib, ie = _range(n, i_begin, i_end)
+    u, v, w = np.zeros(n), np.zeros(n), np.zeros(n)
+    _check(lib().lpm_bve_set_velocity_from_vorticity(n, _dp(x), _dp(y), _dp(z), _dp(rel_vort), _dp(area),
+                                                     _ip(act), float(sphere_radius), ib, ie, _dp(u), _dp(v),
+                                                     _dp(w), _mode(mode)))
+    return u, v, w
+
+
+def planar_incompressible_velocity(x, y, vort, area, active_mask, delta=0.0, i_begin=None, i_end=None,
+                                   mode="fp64"):
+    """planarIncompressibleVelocity (src/PlaneIncompressibleSolver.f90:278); delta = 0 is the
+    reference kernel."""
+    x, y, vort, area = (_f64(a) for a in (x, y, vort, area))
+    act = _i32(active_mask)
+    n = x.size
+    ib, ie = _range(n, i_begin, i_end)
+    u, v = np.zeros(n), np.zeros(n)
+    _check(lib().lpm_plane_velocity(n, _dp(x), _dp(y), _dp(vort), _dp(area), _ip(act), float(delta), ib, ie,
+                                    _dp(u), _dp(v), _mode(mode)))
+    return u, v
+
+
+def pse_sphere_laplacian_at_particles(x, y, z, f, area, active_mask, eps, sphere_radius=1.0,
+                                      kernel=PSE_K8_GEODESIC, i_begin=None, i_end=None, mode="fp64"):
+    """PSESphereLaplacianAtParticles (src/PSEDirectSum.f90:502)."""
+    x, y, z, f, area = (_f64(a) for a in (x, y, z, f, area))
+    act = _i32(active_mask)
+    n = x.size
+    ib, ie = _range(n, i_begin, i_end)
+    lap = np.zeros(n)
+    _check(lib().lpm_pse_sphere_laplacian(n, _dp(x), _dp(y), _dp(z), _dp(f), _dp(area), _ip(act), float(eps),
+                                          float(sphere_radius), int(kernel), ib, ie, _dp(lap), _mode(mode)))
+    return lap
+
+
+def pse_plane_laplacian_at_particles(x, y, f, area, active_mask, eps, kernel=PSE_K8_CHORD, i_begin=None,
+                                     i_end=None, mode="fp64"):
+    """PSEPlaneLaplacianAtParticles (src/PSEDirectSum.f90:467)."""
+    x, y, f, area = (_f64(a) for a in (x, y, f, area))
+    act = _i32(active_mask)
+    n = x.size
+    ib, ie = _range(n, i_begin, i_end)
+    lap = np.zeros(n)
+    _check(lib().lpm_pse_plane_laplacian(n, _dp(x), _dp(y), _dp(f), _dp(area), _ip(act), float(eps), int(kernel),
+                                         ib, ie, _dp(lap), _mode(mode)))
+    return lap
+
+
+def set_stream_functions_on_mesh(x, y, z, rel_vort, abs_vort, area, active_mask, sphere_radius=1.0, i_begin=None,
+                                 i_end=None, mode="fp64"):
+    """SetStreamFunctionsOnMesh (src/SphereBVE.f90:445).  Returns (psi_rel, psi_abs)."""
+    x, y, z, rel_vort, abs_vort, area = (_f64(a) for a in (x, y, z, rel_vort, abs_vort, area))
+    act = _i32(active_mask)
+    n = x.size
+    ib, ie = _range(n, i_begin, i_end)
+    pr, pa = np.zeros(n), np.zeros(n)
+    _check(lib().lpm_bve_stream_functions(n, _dp(x), _dp(y), _dp(z), _dp(rel_vort), _dp(abs_vort), _dp(area),
+                                          _ip(act), float(sphere_radius), ib, ie, _dp(pr), _dp(pa), _mode(mode)))
+    return pr, pa
+
+
+def set_stream_function_on_mesh(x, y, vort, area, active_mask, i_begin=None, i_end=None, mode="fp64"):
+    """SetStreamFunctionOnMesh (src/PlanarIncompressible.f90:470)."""
+    x, y, vort, area = (_f64(a) for a in (x, y, vort, area))
+    act = _i32(active_mask)
+    n = x.size
+    ib, ie = _range(n, i_begin, i_end)
+    p = np.zeros(n)
+    _check(lib().lpm_plane_stream_function(n, _dp(x), _dp(y), _dp(vort), _dp(area), _ip(act), ib, ie, _dp(p),
+                                           _mode(mode)))
+    return p
+
+
+# ------------------------------------------------------------------ solvers
+class BVESolver:
+    """Device-resident BVESolver (src/SphereBVESolver.f90:38-353)."""
+
+    def __init__(self, x, y, z, rel_vort, area, active_mask, radius=1.0, rotation_rate=0.0, u=None, v=None, w=None,
+                 mode="fp64"):
+        arrs = [_f64(a) for a in (x, y, z, rel_vort, area)]
+        self.n = arrs[0].size
+        self._keep = arrs
+        act = _i32(active_mask)
+        uvw = [None if a is None else _f64(a) for a in (u, v, w)]
+        h = ctypes.c_void_p()
+        _check(lib().lpm_bve_solver_create(ctypes.byref(h), self.n, *(_dp(a) for a in arrs), _ip(act),
+                                           *(_dp(a) for a in uvw), float(radius), float(rotation_rate), _mode(mode)))
+        self._h = h
+
+    def timestep(self, dt, n_steps=1, renormalize=False):
+        _check(lib().lpm_bve_timestep(self._h, float(dt), int(n_steps), 1 if renormalize else 0))
+
+    def get_state(self):
+        out = [np.empty(self.n) for _ in range(7)]
+        _check(lib().lpm_bve_get_state(self._h, *(_dp(a) for a in out)))
+        return dict(zip(("x", "y", "z", "rel_vort", "u", "v", "w"), out))
+
+    def set_state(self, x, y, z, rel_vort, u, v, w):
+        arrs = [_f64(a) for a in (x, y, z, rel_vort, u, v, w)]
+        _check(lib().lpm_bve_set_state(self._h, *(_dp(a) for a in arrs)))
+
+    def diagnostics(self):
+        ke, en, ci = _dbl(), _dbl(), _dbl()
+        _check(lib().lpm_bve_diagnostics(self._h, ctypes.byref(ke), ctypes.byref(en), ctypes.byref(ci)))
+        return {"kinetic_energy": ke.value, "enstrophy": en.value, "circulation": ci.value}
+
+    def kernel_timing(self):
+        ms, n = _dbl(), _i64()
+        _check(lib().lpm_bve_kernel_timing(self._h, ctypes.byref(ms), ctypes.byref(n)))
+        return ms.value, n.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().lpm_bve_solver_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class PlaneSolver:
+    """Device-resident PlaneSolver (src/PlaneIncompressibleSolver.f90:103-259)."""
+
+    def __init__(self, x, y, vort, area, active_mask, u=None, v=None, delta=0.0, mode="fp64"):
+        arrs = [_f64(a) for a in (x, y, vort, area)]
+        self.n = arrs[0].size
+        self._keep = arrs
+        act = _i32(active_mask)
+        uv = [None if a is None else _f64(a) for a in (u, v)]
+        h = ctypes.c_void_p()
+        _check(lib().lpm_plane_solver_create(ctypes.byref(h), self.n, *(_dp(a) for a in arrs), _ip(act),
+                                             *(_dp(a) for a in uv), float(delta), _mode(mode)))
+        self._h = h
+
+    def timestep(self, dt, n_steps=1):
+        _check(lib().lpm_plane_timestep(self._h, float(dt), int(n_steps)))
+
+    def get_state(self):
+        out = [np.empty(self.n) for _ in range(4)]
+        _check(lib().lpm_plane_get_state(self._h, *(_dp(a) for a in out)))
+        return dict(zip(("x", "y", "u", "v"), out))
+
+    def diagnostics(self):
+        ke, en, ci = _dbl(), _dbl(), _dbl()
+        _check(lib().lpm_plane_diagnostics(self._h, ctypes.byref(ke), ctypes.byref(en), ctypes.byref(ci)))
+        return {"kinetic_energy": ke.value, "enstrophy": en.value, "circulation": ci.value}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().lpm_plane_solver_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Ensemble:
+    """Batched independent sphere-BVE instances (one persistent launch per RK4 stage)."""
+
+    def __init__(self, instances, mode="fp32c"):
+        """instances: list of dicts with x, y, z, rel_vort, area, active, radius, rotation_rate."""
+        self.sizes = [int(np.asarray(d["x"]).size) for d in instances]
+        offs = np.zeros(len(instances) + 1, dtype=np.int64)
+        offs[1:] = np.cumsum(self.sizes)
+        self.offsets = offs
+        cat = {k: _f64(np.concatenate([np.asarray(d[k], dtype=np.float64) for d in instances]))
+               for k in ("x", "y", "z", "rel_vort", "area")}
+        act = _i32(np.concatenate([np.asarray(d["active"]) for d in instances]))
+        radius = _f64([d.get("radius", 1.0) for d in instances])
+        rot = _f64([d.get("rotation_rate", 0.0) for d in instances])
+        self._keep = (cat, act, radius, rot)
+        h = ctypes.c_void_p()
+        _check(lib().lpm_ensemble_create(ctypes.byref(h), len(instances), offs.ctypes.data_as(_L), _dp(cat["x"]),
+                                         _dp(cat["y"]), _dp(cat["z"]), _dp(cat["rel_vort"]), _dp(cat["area"]),
+                                         _ip(act), _dp(radius), _dp(rot), _mode(mode)))
+        self._h = h
+        self.n = int(offs[-1])
+
+    def timestep(self, dt, n_steps=1):
+        _check(lib().lpm_ensemble_timestep(self._h, float(dt), int(n_steps)))
+
+    def velocity(self):
+        _check(lib().lpm_ensemble_velocity(self._h))
+
+    def get_state(self):
+        out = [np.empty(self.n) for _ in range(7)]
+        _check(lib().lpm_ensemble_get_state(self._h, *(_dp(a) for a in out)))
+        return dict(zip(("x", "y", "z", "rel_vort", "u", "v", "w"), out))
+
+    def kernel_timing(self):
+        ms, n = _dbl(), _i64()
+        _check(lib().lpm_ensemble_kernel_timing(self._h, ctypes.byref(ms), ctypes.byref(n)))
+        return ms.value, n.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().lpm_ensemble_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ------------------------------------------------------------------ meshes
+class PolyMesh2d:
+    """Uniformly refined lpm-v2 mesh (New(PolyMesh2d, seed, initNest, ...), src/PolyMesh2d.f90:135)."""
+
+    def __init__(self, mesh_seed: int, init_nest: int, amp_factor: float = 1.0):
+        h = ctypes.c_void_p()
+        _check(lib().lpm_mesh_create(ctypes.byref(h), int(mesh_seed), int(init_nest), float(amp_factor)))
+        self._h = h
+        L = lib()
+        self.n = int(L.lpm_mesh_n_particles(h))
+        self.spherical = bool(L.lpm_mesh_is_spherical(h))
+        self.x = np.empty(self.n)
+        self.y = np.empty(self.n)
+        self.z = np.zeros(self.n)
+        self.area = np.empty(self.n)
+        self.active = np.empty(self.n, dtype=np.int32)
+        _check(L.lpm_mesh_get_particles(h, _dp(self.x), _dp(self.y), _dp(self.z) if self.spherical else None,
+                                        _dp(self.area), _ip(self.active)))
+        self.n_active = int(L.lpm_mesh_n_active(h))
+        self.n_faces = int(L.lpm_mesh_n_faces(h))
+        self.n_edges = int(L.lpm_mesh_n_edges(h))
+        self.n_leaf_edges = int(L.lpm_mesh_n_leaf_edges(h))
+        self.max_edge_length = float(L.lpm_mesh_max_edge_length(h))
+        self.avg_edge_length = float(L.lpm_mesh_avg_edge_length(h))
+        L.lpm_mesh_destroy(h)
+        self._h = None

@@ -1,0 +1,346 @@
+/*
+ * lpm_oracle.c -- CPU restatement of the lpm-v2 direct sums (TEST INFRASTRUCTURE ONLY).
+ *
+ * The checker for the CUDA library: the tests compare the GPU results against these
+ * loops, and the benchmark's CPU-baseline leg times them on the host cores.  Nothing in
+ * the shipped library calls this file.  See lpm_oracle.h for what pins each routine.
+ *
+ * Build: -O3 -fopenmp -ffp-contract=off (no fused multiply-add, so every product and
+ * sum is rounded exactly where the Fortran source rounds it).
+ */
+#include "lpm_oracle.h"
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* NumberKindsModule PI, src/TypeDefs.f90:31 */
+static const double PI = 3.1415926535897932384626433832795027975;
+
+static int pick_threads(int nthreads)
+{
+#ifdef _OPENMP
+  return nthreads > 0 ? nthreads : omp_get_max_threads();
+#else
+  (void)nthreads;
+  return 1;
+#endif
+}
+
+/*
+ * BVESphereVelocity, src/SphereBVESolver.f90:377-430 (assoc = SOLVER) and
+ * setVelocityFromVorticity, src/SphereBVE.f90:489-531 (assoc = MESH).
+ * j runs 1..i-1 then i+1..N (:401-419), i.e. ascending j skipping i; inactive j skipped.
+ *   strength = -zeta_j A_j / (4 pi a (a^2 - x_i.x_j))
+ *   u_i += (y_i z_j - z_i y_j) strength  etc.
+ */
+void lpmo_bve_velocity(int64_t n, const double* x, const double* y, const double* z,
+                       const double* zeta, const double* area, const int32_t* active,
+                       double radius, int assoc, int64_t ib, int64_t ie,
+                       double* u, double* v, double* w, int nthreads)
+{
+  const double four_pi = 4.0 * PI; /* gfortran folds 4.0_kreal*PI at compile time */
+  const double kden = four_pi * radius;
+  const double a2 = radius * radius;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(pick_threads(nthreads))
+  for (int64_t i = ib; i < ie; ++i) {
+    const double xi = x[i], yi = y[i], zi = z[i];
+    double ui = 0.0, vi = 0.0, wi = 0.0;
+    for (int64_t j = 0; j < n; ++j) {
+      if (j == i || !active[j]) continue;
+      double den;
+      if (assoc == LPMO_ASSOC_SOLVER) {
+        den = ((a2 - xi * x[j]) - yi * y[j]) - zi * z[j];
+      } else {
+        den = a2 - ((xi * x[j] + yi * y[j]) + zi * z[j]);
+      }
+      const double strength = -((zeta[j] * area[j]) / (kden * den));
+      ui = ui + (yi * z[j] - zi * y[j]) * strength;
+      vi = vi + (zi * x[j] - xi * z[j]) * strength;
+      wi = wi + (xi * y[j] - yi * x[j]) * strength;
+    }
+    u[i] = ui;
+    v[i] = vi;
+    w[i] = wi;
+  }
+}
+
+/*
+ * planarIncompressibleVelocity, src/PlaneIncompressibleSolver.f90:278-316.
+ *   strength = omega_j A_j / (2 pi ((x_i-x_j)^2 + (y_i-y_j)^2 [+ delta^2]))
+ *   u_i -= (y_i - y_j) strength ; v_i += (x_i - x_j) strength
+ * delta = 0 is the reference (singular) kernel; adding +0.0 leaves every rounding as is.
+ */
+void lpmo_plane_velocity(int64_t n, const double* x, const double* y,
+                         const double* omega, const double* area, const int32_t* active,
+                         double delta, int64_t ib, int64_t ie,
+                         double* u, double* v, int nthreads)
+{
+  const double two_pi = 2.0 * PI;
+  const double d2 = delta * delta;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(pick_threads(nthreads))
+  for (int64_t i = ib; i < ie; ++i) {
+    const double xi = x[i], yi = y[i];
+    double ui = 0.0, vi = 0.0;
+    for (int64_t j = 0; j < n; ++j) {
+      if (j == i || !active[j]) continue;
+      const double dx = xi - x[j];
+      const double dy = yi - y[j];
+      const double r2 = (dx * dx + dy * dy) + d2;
+      const double strength = (omega[j] * area[j]) / (two_pi * r2);
+      ui = ui - dy * strength;
+      vi = vi + dx * strength;
+    }
+    u[i] = ui;
+    v[i] = vi;
+  }
+}
+
+/* bivariateLaplacianKernel8, src/PSEDirectSum.f90:622-627.  gfortran expands r**k with
+ * its integer-power multiplication chain: r^2 = r*r, r^4 = r^2*r^2, r^6 = r^3*r^3 with
+ * r^3 = r*r^2. */
+double lpmo_k8(double r)
+{
+  const double r2 = r * r;
+  const double r3 = r * r2;
+  const double r4 = r2 * r2;
+  const double r6 = r3 * r3;
+  return (((40.0 - 40.0 * r2) + 10.0 * r4) - (2.0 * r6) / 3.0) * exp(-(r * r)) / PI;
+}
+
+/* SphereDistance (vector form), src/SphereGeometry.f90:107-125, SphereRadius = radius */
+static double sphere_distance(double ax, double ay, double az, double bx, double by,
+                              double bz, double radius)
+{
+  const double c1 = ay * bz - by * az;
+  const double c2 = bx * az - ax * bz;
+  const double c3 = ax * by - bx * ay;
+  const double cn = sqrt((c1 * c1 + c2 * c2) + c3 * c3);
+  const double dp = (ax * bx + ay * by) + az * bz;
+  return atan2(cn, dp) * radius;
+}
+
+/* ChordDistance, src/SphereGeometry.f90:67-73: sqrt(sum((b-a)*(b-a))) */
+static double chord_distance(double ax, double ay, double az, double bx, double by, double bz)
+{
+  const double d1 = bx - ax, d2 = by - ay, d3 = bz - az;
+  return sqrt((d1 * d1 + d2 * d2) + d3 * d3);
+}
+
+/*
+ * PSESphereLaplacianAtParticles, src/PSEDirectSum.f90:502-535 (kernel K8_GEODESIC) and
+ * PSEPlaneLaplacianAtParticles, :467-500 (kernel K8_CHORD).  j runs over all active
+ * particles including j = i (that term is 0).  Per pair:
+ *   lap_i += (f_j - f_i) * K8(d/eps) / eps**2 * A_j
+ * and the finished field is multiplied by 1/eps**2 (:534).
+ * GAUSS_CHORD uses eta(r) = 4 exp(-r^2)/pi in place of K8 with the chord distance: the
+ * second-order Gaussian PSE Laplacian (the factor 4 makes (1/eps^2) sum (f_j-f_i)
+ * eta(|x_i-x_j|/eps)/eps^2 A_j consistent with the Laplacian).
+ */
+void lpmo_pse_laplacian(int64_t n, const double* x, const double* y, const double* z,
+                        const double* f, const double* area, const int32_t* active,
+                        double eps, double radius, int kernel, int64_t ib, int64_t ie,
+                        double* lap, int nthreads)
+{
+  const double eps2 = eps * eps; /* eps**2 */
+  const double scale = 1.0 / eps2;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(pick_threads(nthreads))
+  for (int64_t i = ib; i < ie; ++i) {
+    const double xi = x[i], yi = y[i], zi = z ? z[i] : 0.0;
+    double li = 0.0;
+    for (int64_t j = 0; j < n; ++j) {
+      if (!active[j]) continue;
+      const double xj = x[j], yj = y[j], zj = z ? z[j] : 0.0;
+      double k;
+      if (kernel == LPMO_PSE_K8_GEODESIC) {
+        const double kin = sphere_distance(xi, yi, zi, xj, yj, zj, radius) / eps;
+        k = lpmo_k8(kin);
+      } else if (kernel == LPMO_PSE_K8_CHORD) {
+        const double kin = chord_distance(xi, yi, zi, xj, yj, zj) / eps;
+        k = lpmo_k8(kin);
+      } else {
+        const double kin = chord_distance(xi, yi, zi, xj, yj, zj) / eps;
+        k = 4.0 * exp(-(kin * kin)) / PI;
+      }
+      li = li + (((f[j] - f[i]) * k) / eps2) * area[j];
+    }
+    lap[i] = li * scale; /* MultiplyFieldByScalar(scalarLap, 1/eps**2) */
+  }
+}
+
+/*
+ * SetStreamFunctionsOnMesh, src/SphereBVE.f90:445-485: G = -log(a^2 - sum(xi*xj))/(4 pi),
+ * psi_rel += G zeta_rel_j A_j, psi_abs += G zeta_abs_j A_j, j != i, active j.
+ */
+void lpmo_bve_stream(int64_t n, const double* x, const double* y, const double* z,
+                     const double* relvort, const double* absvort, const double* area,
+                     const int32_t* active, double radius, int64_t ib, int64_t ie,
+                     double* psi_rel, double* psi_abs, int nthreads)
+{
+  const double four_pi = 4.0 * PI;
+  const double a2 = radius * radius;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(pick_threads(nthreads))
+  for (int64_t i = ib; i < ie; ++i) {
+    const double xi = x[i], yi = y[i], zi = z[i];
+    double pr = 0.0, pa = 0.0;
+    for (int64_t j = 0; j < n; ++j) {
+      if (j == i || !active[j]) continue;
+      const double g = -log(a2 - ((xi * x[j] + yi * y[j]) + zi * z[j])) / four_pi;
+      pr = pr + (g * relvort[j]) * area[j];
+      pa = pa + (g * absvort[j]) * area[j];
+    }
+    psi_rel[i] = pr;
+    psi_abs[i] = pa;
+  }
+}
+
+/* SetStreamFunctionOnMesh, src/PlanarIncompressible.f90:470-505:
+ * G = log(sqrt((xi-xj)^2 + (yi-yj)^2)) / (2 pi). */
+void lpmo_plane_stream(int64_t n, const double* x, const double* y,
+                       const double* omega, const double* area, const int32_t* active,
+                       int64_t ib, int64_t ie, double* psi, int nthreads)
+{
+  const double two_pi = 2.0 * PI;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(pick_threads(nthreads))
+  for (int64_t i = ib; i < ie; ++i) {
+    const double xi = x[i], yi = y[i];
+    double p = 0.0;
+    for (int64_t j = 0; j < n; ++j) {
+      if (j == i || !active[j]) continue;
+      const double dx = xi - x[j], dy = yi - y[j];
+      const double g = log(sqrt(dx * dx + dy * dy)) / two_pi;
+      p = p + (g * omega[j]) * area[j];
+    }
+    psi[i] = p;
+  }
+}
+
+/*
+ * timestepPrivate, src/SphereBVESolver.f90:219-353, without the stream-function call
+ * at :352 (its result is not part of the RK4 state).
+ */
+void lpmo_bve_timestep(int64_t n, double* x, double* y, double* z, double* zeta,
+                       const double* area, const int32_t* active, double* u, double* v,
+                       double* w, double radius, double omega, double dt, int nsteps,
+                       int nthreads)
+{
+  const size_t bytes = (size_t)n * sizeof(double);
+  double* buf = (double*)malloc(bytes * 20);
+  double *x1 = buf, *y1 = buf + n, *z1 = buf + 2 * n, *q1 = buf + 3 * n;
+  double *x2 = buf + 4 * n, *y2 = buf + 5 * n, *z2 = buf + 6 * n, *q2 = buf + 7 * n;
+  double *x3 = buf + 8 * n, *y3 = buf + 9 * n, *z3 = buf + 10 * n, *q3 = buf + 11 * n;
+  double *x4 = buf + 12 * n, *y4 = buf + 13 * n, *z4 = buf + 14 * n, *q4 = buf + 15 * n;
+  double *xin = buf + 16 * n, *yin = buf + 17 * n, *zin = buf + 18 * n, *qin = buf + 19 * n;
+  for (int s = 0; s < nsteps; ++s) {
+    /* stage 1 (:238-244): k1 = dt * u_prev */
+    for (int64_t i = 0; i < n; ++i) {
+      x1[i] = dt * u[i];
+      y1[i] = dt * v[i];
+      z1[i] = dt * w[i];
+      q1[i] = -((((dt * 2.0) * omega) * w[i]) / radius);
+    }
+    /* stages 2-4 (:249-313) */
+    double* ks[3][4] = {{x1, y1, z1, q1}, {x2, y2, z2, q2}, {x3, y3, z3, q3}};
+    double* kout[3][4] = {{x2, y2, z2, q2}, {x3, y3, z3, q3}, {x4, y4, z4, q4}};
+    for (int st = 0; st < 3; ++st) {
+      double** kp = ks[st];
+      double** ko = kout[st];
+      for (int64_t i = 0; i < n; ++i) {
+        if (st < 2) {
+          xin[i] = x[i] + 0.5 * kp[0][i];
+          yin[i] = y[i] + 0.5 * kp[1][i];
+          zin[i] = z[i] + 0.5 * kp[2][i];
+          qin[i] = zeta[i] + 0.5 * kp[3][i];
+        } else {
+          xin[i] = x[i] + kp[0][i];
+          yin[i] = y[i] + kp[1][i];
+          zin[i] = z[i] + kp[2][i];
+          qin[i] = zeta[i] + kp[3][i];
+        }
+      }
+      lpmo_bve_velocity(n, xin, yin, zin, qin, area, active, radius, LPMO_ASSOC_SOLVER, 0, n,
+                        ko[0], ko[1], ko[2], nthreads);
+      for (int64_t i = 0; i < n; ++i) {
+        ko[3][i] = -((((dt * 2.0) * omega) * ko[2][i]) / radius);
+        ko[0][i] = dt * ko[0][i];
+        ko[1][i] = dt * ko[1][i];
+        ko[2][i] = dt * ko[2][i];
+      }
+    }
+    /* RK4 update (:319-329) */
+    for (int64_t i = 0; i < n; ++i) {
+      x[i] = (((x[i] + x1[i] / 6.0) + x2[i] / 3.0) + x3[i] / 3.0) + x4[i] / 6.0;
+      y[i] = (((y[i] + y1[i] / 6.0) + y2[i] / 3.0) + y3[i] / 3.0) + y4[i] / 6.0;
+      z[i] = (((z[i] + z1[i] / 6.0) + z2[i] / 3.0) + z3[i] / 3.0) + z4[i] / 6.0;
+      zeta[i] = (((zeta[i] + q1[i] / 6.0) + q2[i] / 3.0) + q3[i] / 3.0) + q4[i] / 6.0;
+    }
+    /* velocity at the new positions (:345-350) */
+    lpmo_bve_velocity(n, x, y, z, zeta, area, active, radius, LPMO_ASSOC_SOLVER, 0, n, u, v,
+                      w, nthreads);
+  }
+  free(buf);
+}
+
+/* timestepPrivate, src/PlaneIncompressibleSolver.f90:171-259 (without the stream function). */
+void lpmo_plane_timestep(int64_t n, double* x, double* y, const double* omega,
+                         const double* area, const int32_t* active, double* u, double* v,
+                         double delta, double dt, int nsteps, int nthreads)
+{
+  const size_t bytes = (size_t)n * sizeof(double);
+  double* buf = (double*)malloc(bytes * 10);
+  double *x1 = buf, *y1 = buf + n, *x2 = buf + 2 * n, *y2 = buf + 3 * n;
+  double *x3 = buf + 4 * n, *y3 = buf + 5 * n, *x4 = buf + 6 * n, *y4 = buf + 7 * n;
+  double *xin = buf + 8 * n, *yin = buf + 9 * n;
+  for (int s = 0; s < nsteps; ++s) {
+    for (int64_t i = 0; i < n; ++i) {
+      x1[i] = dt * u[i];
+      y1[i] = dt * v[i];
+    }
+    double* kp[3][2] = {{x1, y1}, {x2, y2}, {x3, y3}};
+    double* ko[3][2] = {{x2, y2}, {x3, y3}, {x4, y4}};
+    for (int st = 0; st < 3; ++st) {
+      for (int64_t i = 0; i < n; ++i) {
+        if (st < 2) {
+          xin[i] = x[i] + 0.5 * kp[st][0][i];
+          yin[i] = y[i] + 0.5 * kp[st][1][i];
+        } else {
+          xin[i] = x[i] + kp[st][0][i];
+          yin[i] = y[i] + kp[st][1][i];
+        }
+      }
+      lpmo_plane_velocity(n, xin, yin, omega, area, active, delta, 0, n, ko[st][0], ko[st][1],
+                          nthreads);
+      for (int64_t i = 0; i < n; ++i) {
+        ko[st][0][i] = dt * ko[st][0][i];
+        ko[st][1][i] = dt * ko[st][1][i];
+      }
+    }
+    for (int64_t i = 0; i < n; ++i) {
+      x[i] = (((x[i] + x1[i] / 6.0) + x2[i] / 3.0) + x3[i] / 3.0) + x4[i] / 6.0;
+      y[i] = (((y[i] + y1[i] / 6.0) + y2[i] / 3.0) + y3[i] / 3.0) + y4[i] / 6.0;
+    }
+    lpmo_plane_velocity(n, x, y, omega, area, active, delta, 0, n, u, v, nthreads);
+  }
+  free(buf);
+}
+
+/* TotalKE / TotalEnstrophy, src/SphereBVE.f90:410-441; circulation = sum zeta A over
+ * active particles (SetGaussConst numerator, examples/BVESingleGaussianVortex.f90:350). */
+void lpmo_bve_diagnostics(int64_t n, const double* u, const double* v, const double* w,
+                          const double* zeta, const double* area, const int32_t* active,
+                          double* ke, double* enstrophy, double* circulation)
+{
+  double k = 0.0, e = 0.0, c = 0.0;
+  for (int64_t i = 0; i < n; ++i) {
+    if (!active[i]) continue;
+    const double m2 = (u[i] * u[i] + v[i] * v[i]) + (w ? w[i] * w[i] : 0.0);
+    k = k + m2 * area[i];
+    e = e + (zeta[i] * zeta[i]) * area[i];
+    c = c + zeta[i] * area[i];
+  }
+  *ke = 0.5 * k;
+  *enstrophy = 0.5 * e;
+  *circulation = c;
+}

@@ -1,0 +1,165 @@
+"""ctypes wrapper of the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Only the test suite, the smoke check and the benchmark's CPU-baseline leg use this module.
+It restates the reference Fortran loops in FP64 (see lpm_oracle.h for the citations and
+for what pins each routine); the shipped library never imports it.
+"""
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+import numpy as np
+
+from . import build as _build  # noqa: F401  (package-relative when imported as oracle.oracle)
+
+_LIB = None
+
+ASSOC_SOLVER = 0
+ASSOC_MESH = 1
+PSE_K8_GEODESIC = 0
+PSE_GAUSS_CHORD = 1
+PSE_K8_CHORD = 2
+
+_D = ctypes.POINTER(ctypes.c_double)
+_I = ctypes.POINTER(ctypes.c_int32)
+_i64 = ctypes.c_int64
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        path = _build.build()
+        L = ctypes.CDLL(str(path))
+        L.lpmo_bve_velocity.argtypes = [_i64, _D, _D, _D, _D, _D, _I, ctypes.c_double, ctypes.c_int,
+                                        _i64, _i64, _D, _D, _D, ctypes.c_int]
+        L.lpmo_plane_velocity.argtypes = [_i64, _D, _D, _D, _D, _I, ctypes.c_double, _i64, _i64, _D, _D,
+                                          ctypes.c_int]
+        L.lpmo_pse_laplacian.argtypes = [_i64, _D, _D, _D, _D, _D, _I, ctypes.c_double, ctypes.c_double,
+                                         ctypes.c_int, _i64, _i64, _D, ctypes.c_int]
+        L.lpmo_bve_stream.argtypes = [_i64, _D, _D, _D, _D, _D, _D, _I, ctypes.c_double, _i64, _i64, _D, _D,
+                                      ctypes.c_int]
+        L.lpmo_plane_stream.argtypes = [_i64, _D, _D, _D, _D, _I, _i64, _i64, _D, ctypes.c_int]
+        L.lpmo_bve_timestep.argtypes = [_i64, _D, _D, _D, _D, _D, _I, _D, _D, _D, ctypes.c_double,
+                                        ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int]
+        L.lpmo_plane_timestep.argtypes = [_i64, _D, _D, _D, _D, _I, _D, _D, ctypes.c_double, ctypes.c_double,
+                                          ctypes.c_int, ctypes.c_int]
+        L.lpmo_bve_diagnostics.argtypes = [_i64, _D, _D, _D, _D, _D, _I, _D, _D, _D]
+        L.lpmo_k8.argtypes = [ctypes.c_double]
+        L.lpmo_k8.restype = ctypes.c_double
+        _LIB = L
+    return _LIB
+
+
+def _d(a):
+    if a is None:
+        return None
+    return a.ctypes.data_as(_D)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _range(n, ib, ie):
+    ib = 0 if ib is None else int(ib)
+    ie = n if ie is None else int(ie)
+    return ib, ie
+
+
+def bve_velocity(x, y, z, zeta, area, active, radius=1.0, assoc=ASSOC_SOLVER, ib=None, ie=None, threads=0):
+    """BVESphereVelocity / setVelocityFromVorticity for targets [ib, ie) (0-based)."""
+    x, y, z, zeta, area = (_f64(a) for a in (x, y, z, zeta, area))
+    active = _i32(active)
+    n = x.size
+    ib, ie = _range(n, ib, ie)
+    u = np.zeros(n)
+    v = np.zeros(n)
+    w = np.zeros(n)
+    lib().lpmo_bve_velocity(n, _d(x), _d(y), _d(z), _d(zeta), _d(area), active.ctypes.data_as(_I), radius,
+                            assoc, ib, ie, _d(u), _d(v), _d(w), threads)
+    return u[ib:ie], v[ib:ie], w[ib:ie]
+
+
+def plane_velocity(x, y, omega, area, active, delta=0.0, ib=None, ie=None, threads=0):
+    x, y, omega, area, active = _f64(x), _f64(y), _f64(omega), _f64(area), _i32(active)
+    n = x.size
+    ib, ie = _range(n, ib, ie)
+    u = np.zeros(n)
+    v = np.zeros(n)
+    lib().lpmo_plane_velocity(n, _d(x), _d(y), _d(omega), _d(area), active.ctypes.data_as(_I), delta, ib, ie,
+                              _d(u), _d(v), threads)
+    return u[ib:ie], v[ib:ie]
+
+
+def pse_laplacian(x, y, z, f, area, active, eps, radius=1.0, kernel=PSE_K8_GEODESIC, ib=None, ie=None,
+                  threads=0):
+    x, y, f, area, active = _f64(x), _f64(y), _f64(f), _f64(area), _i32(active)
+    z = None if z is None else _f64(z)
+    n = x.size
+    ib, ie = _range(n, ib, ie)
+    lap = np.zeros(n)
+    lib().lpmo_pse_laplacian(n, _d(x), _d(y), _d(z), _d(f), _d(area), active.ctypes.data_as(_I), eps, radius,
+                             kernel, ib, ie, _d(lap), threads)
+    return lap[ib:ie]
+
+
+def bve_stream(x, y, z, relvort, absvort, area, active, radius=1.0, ib=None, ie=None, threads=0):
+    x, y, z, relvort, absvort, area, active = (_f64(x), _f64(y), _f64(z), _f64(relvort), _f64(absvort),
+                                               _f64(area), _i32(active))
+    n = x.size
+    ib, ie = _range(n, ib, ie)
+    pr = np.zeros(n)
+    pa = np.zeros(n)
+    lib().lpmo_bve_stream(n, _d(x), _d(y), _d(z), _d(relvort), _d(absvort), _d(area), active.ctypes.data_as(_I),
+                          radius, ib, ie, _d(pr), _d(pa), threads)
+    return pr[ib:ie], pa[ib:ie]
+
+
+def plane_stream(x, y, omega, area, active, ib=None, ie=None, threads=0):
+    x, y, omega, area, active = _f64(x), _f64(y), _f64(omega), _f64(area), _i32(active)
+    n = x.size
+    ib, ie = _range(n, ib, ie)
+    p = np.zeros(n)
+    lib().lpmo_plane_stream(n, _d(x), _d(y), _d(omega), _d(area), active.ctypes.data_as(_I), ib, ie, _d(p),
+                            threads)
+    return p[ib:ie]
+
+
+def bve_timestep(x, y, z, zeta, area, active, u, v, w, radius, omega, dt, nsteps, threads=0):
+    """Advances copies of the state; returns (x, y, z, zeta, u, v, w)."""
+    x, y, z, zeta, u, v, w = (_f64(a).copy() for a in (x, y, z, zeta, u, v, w))
+    area, active = _f64(area), _i32(active)
+    lib().lpmo_bve_timestep(x.size, _d(x), _d(y), _d(z), _d(zeta), _d(area), active.ctypes.data_as(_I), _d(u),
+                            _d(v), _d(w), radius, omega, dt, nsteps, threads)
+    return x, y, z, zeta, u, v, w
+
+
+def plane_timestep(x, y, omega, area, active, u, v, delta, dt, nsteps, threads=0):
+    x, y, u, v = (_f64(a).copy() for a in (x, y, u, v))
+    omega, area, active = _f64(omega), _f64(area), _i32(active)
+    lib().lpmo_plane_timestep(x.size, _d(x), _d(y), _d(omega), _d(area), active.ctypes.data_as(_I), _d(u),
+                              _d(v), delta, dt, nsteps, threads)
+    return x, y, u, v
+
+
+def bve_diagnostics(u, v, w, zeta, area, active):
+    u, v, zeta, area, active = _f64(u), _f64(v), _f64(zeta), _f64(area), _i32(active)
+    w = None if w is None else _f64(w)
+    ke = ctypes.c_double()
+    en = ctypes.c_double()
+    ci = ctypes.c_double()
+    lib().lpmo_bve_diagnostics(u.size, _d(u), _d(v), _d(w), _d(zeta), _d(area), active.ctypes.data_as(_I),
+                               ctypes.byref(ke), ctypes.byref(en), ctypes.byref(ci))
+    return ke.value, en.value, ci.value
+
+
+def k8(r: float) -> float:
+    return lib().lpmo_k8(r)
+
+
+LIB_PATH: Path = _build.LIB_PATH

@@ -1,0 +1,218 @@
+"""GPU parity tests of the direct sums through the C ABI (liblpm_gpu.so).
+
+FP64 mode restates the reference loops with the reference association and source order, so
+the BVE and planar sums must be bit-identical to the oracle.  The PSE and stream-function
+sums call exp/atan2/log, whose CUDA and C-library implementations may differ by an ulp:
+those are checked to 1e-12 relative to max|result|.  FP32C mode is checked to the velocity
+relative L-infinity error bound 1e-6 (relative to max|u| over the targets).
+"""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+FP32C_TOL = 1e-6
+
+
+@pytest.fixture(scope="module")
+def lg(built_lib):
+    return built_lib
+
+
+@pytest.fixture(scope="module")
+def wl(built_lib):
+    import workloads
+    return workloads
+
+
+def rel_linf(got, ref):
+    got = np.stack(got) if isinstance(got, (tuple, list)) else got
+    ref = np.stack(ref) if isinstance(ref, (tuple, list)) else ref
+    return np.abs(got - ref).max() / np.abs(ref).max()
+
+
+# ------------------------------------------------------------------ golden fixtures
+def test_golden_bve_fp64_bit_exact(lg):
+    g = np.load(GOLDEN / "bve_icos2.npz")
+    u, v, w = lg.bve_sphere_velocity(g["x"], g["y"], g["z"], g["zeta"], g["area"], g["active"], 1.0)
+    assert np.array_equal(u, g["u"]) and np.array_equal(v, g["v"]) and np.array_equal(w, g["w"])
+    u, v, w = lg.set_velocity_from_vorticity(g["x"], g["y"], g["z"], g["zeta"], g["area"], g["active"], 1.0)
+    assert np.array_equal(u, g["um"]) and np.array_equal(v, g["vm"]) and np.array_equal(w, g["wm"])
+    u, v, w = lg.bve_sphere_velocity(g["xo"], g["yo"], g["zo"], g["zeta"], g["area"], g["active"], 1.0)
+    assert np.array_equal(u, g["uo"]) and np.array_equal(v, g["vo"]) and np.array_equal(w, g["wo"])
+
+
+def test_golden_bve_fp32c(lg):
+    g = np.load(GOLDEN / "bve_icos2.npz")
+    got = lg.bve_sphere_velocity(g["x"], g["y"], g["z"], g["zeta"], g["area"], g["active"], 1.0, mode="fp32c")
+    assert rel_linf(got, (g["u"], g["v"], g["w"])) <= FP32C_TOL
+    got = lg.bve_sphere_velocity(g["xo"], g["yo"], g["zo"], g["zeta"], g["area"], g["active"], 1.0, mode="fp32c")
+    assert rel_linf(got, (g["uo"], g["vo"], g["wo"])) <= FP32C_TOL
+
+
+def test_golden_plane(lg):
+    g = np.load(GOLDEN / "plane_quad3.npz")
+    u, v = lg.planar_incompressible_velocity(g["x"], g["y"], g["omega"], g["area"], g["active"], 0.0)
+    assert np.array_equal(u, g["u0"]) and np.array_equal(v, g["v0"])
+    u, v = lg.planar_incompressible_velocity(g["x"], g["y"], g["omega"], g["area"], g["active"], 0.02)
+    assert np.array_equal(u, g["u2"]) and np.array_equal(v, g["v2"])
+    got = lg.planar_incompressible_velocity(g["x"], g["y"], g["omega"], g["area"], g["active"], 0.02, mode="fp32c")
+    assert rel_linf(got, (g["u2"], g["v2"])) <= FP32C_TOL
+    got = lg.planar_incompressible_velocity(g["x"], g["y"], g["omega"], g["area"], g["active"], 0.0, mode="fp32c")
+    assert rel_linf(got, (g["u0"], g["v0"])) <= FP32C_TOL
+
+
+def test_golden_pse(lg):
+    g = np.load(GOLDEN / "pse_small.npz")
+    lk = lg.pse_sphere_laplacian_at_particles(g["x"], g["y"], g["z"], g["f"], g["area"], g["active"],
+                                              float(g["eps_k8"]), 1.0, lg.PSE_K8_GEODESIC)
+    assert rel_linf(lk, g["lap_k8"]) <= 1e-12
+    lgs = lg.pse_sphere_laplacian_at_particles(g["x"], g["y"], g["z"], g["f"], g["area"], g["active"],
+                                               float(g["eps_g"]), 1.0, lg.PSE_GAUSS_CHORD)
+    assert rel_linf(lgs, g["lap_gauss"]) <= 1e-12
+    lp = lg.pse_plane_laplacian_at_particles(g["px"], g["py"], g["pf"], g["parea"], g["pactive"], float(g["peps"]),
+                                             lg.PSE_K8_CHORD)
+    assert rel_linf(lp, g["plap"]) <= 1e-12
+
+
+def test_golden_stream(lg):
+    g = np.load(GOLDEN / "bve_icos2.npz")
+    pr, pa = lg.set_stream_functions_on_mesh(g["x"], g["y"], g["z"], g["zeta"], g["absvort"], g["area"],
+                                             g["active"], 1.0)
+    assert rel_linf(pr, g["psi_rel"]) <= 1e-12 and rel_linf(pa, g["psi_abs"]) <= 1e-12
+    gp = np.load(GOLDEN / "plane_quad3.npz")
+    ps = lg.set_stream_function_on_mesh(gp["x"], gp["y"], gp["omega"], gp["area"], gp["active"])
+    assert rel_linf(ps, gp["psi"]) <= 1e-12
+
+
+# ------------------------------------------------------------------ oracle parity at larger sizes
+@pytest.mark.parametrize("nest", [3, 4])
+def test_bve_fp64_bit_exact_vs_oracle(lg, wl, oracle_mod, nest):
+    c = wl.config_gauss_vortex_icos(nest)
+    args = (c["x"], c["y"], c["z"], c["zeta"], c["area"], c["active"])
+    ref = oracle_mod.bve_velocity(*args)
+    got = lg.bve_sphere_velocity(*args, 1.0)
+    for a, b in zip(got, ref):
+        assert np.array_equal(a, b)
+
+
+def test_bve_fp32c_vs_oracle_rh54(lg, wl, oracle_mod):
+    c = wl.config_rh54_icos(5, seed=3)
+    args = (c["x"], c["y"], c["z"], c["zeta"], c["area"], c["active"])
+    ref = oracle_mod.bve_velocity(*args)
+    got = lg.bve_sphere_velocity(*args, 1.0, mode="fp32c")
+    assert rel_linf(got, ref) <= FP32C_TOL
+
+
+def test_bve_rank_block_range(lg, wl, oracle_mod):
+    """i_begin/i_end (1-based, inclusive) write only the rank's block, as MPISetup splits it."""
+    c = wl.config_gauss_vortex_icos(3)
+    args = (c["x"], c["y"], c["z"], c["zeta"], c["area"], c["active"])
+    n = c["x"].size
+    ref = oracle_mod.bve_velocity(*args)
+    chunk = n // 3
+    for r in range(3):
+        ib, ie = r * chunk + 1, (n if r == 2 else (r + 1) * chunk)
+        sentinel = [np.full(n, 7.0) for _ in range(3)]
+        got = lg.bve_sphere_velocity(*args, 1.0, i_begin=ib, i_end=ie, out=sentinel)
+        for a, b in zip(got, ref):
+            assert np.array_equal(a[ib - 1:ie], b[ib - 1:ie])
+            assert np.all(a[:ib - 1] == 7.0) and np.all(a[ie:] == 7.0)
+        got32 = lg.bve_sphere_velocity(*args, 1.0, i_begin=ib, i_end=ie, mode="fp32c")
+        assert rel_linf([g[ib - 1:ie] for g in got32], [b[ib - 1:ie] for b in ref]) <= FP32C_TOL
+
+
+@pytest.mark.parametrize("n", [1, 2, 33, 257, 1000])
+def test_bve_ragged_sizes(lg, oracle_mod, n):
+    """Odd sizes, not multiples of the tile or the CTA width; random activity pattern."""
+    rng = np.random.default_rng(n)
+    p = rng.normal(size=(3, n))
+    p /= np.linalg.norm(p, axis=0)
+    zeta = rng.normal(size=n)
+    area = rng.uniform(0.5, 1.5, size=n) * 4 * np.pi / n
+    act = (rng.random(n) < 0.7).astype(np.int32)
+    ref = oracle_mod.bve_velocity(p[0], p[1], p[2], zeta, area, act)
+    got = lg.bve_sphere_velocity(p[0], p[1], p[2], zeta, area, act, 1.0)
+    for a, b in zip(got, ref):
+        assert np.array_equal(a, b)
+    if np.abs(np.stack(ref)).max() > 0:
+        got32 = lg.bve_sphere_velocity(p[0], p[1], p[2], zeta, area, act, 1.0, mode="fp32c")
+        assert rel_linf(got32, ref) <= FP32C_TOL
+
+
+def test_bve_no_active_sources(lg):
+    n = 10
+    p = np.eye(3)[:, [0, 1, 2, 0, 1, 2, 0, 1, 2, 0]] * 1.0
+    p[:, 3:] += 0.1
+    z = np.zeros(n)
+    for mode in ("fp64", "fp32c"):
+        u, v, w = lg.bve_sphere_velocity(p[0], p[1], p[2], np.ones(n), np.ones(n), np.zeros(n, np.int32), 1.0,
+                                         mode=mode)
+        assert np.array_equal(u, z) and np.array_equal(v, z) and np.array_equal(w, z)
+
+
+def test_bve_radius_scaling(lg, wl, oracle_mod):
+    """A sphere of radius a != 1 (the Earth-radius case of the drivers)."""
+    c = wl.config_gauss_vortex_icos(3)
+    a = 6.37122e6
+    args = (c["x"] * a, c["y"] * a, c["z"] * a, c["zeta"] * 1e-5, c["area"] * a * a, c["active"])
+    ref = oracle_mod.bve_velocity(*args, radius=a)
+    got = lg.bve_sphere_velocity(*args, a)
+    for g_, r_ in zip(got, ref):
+        assert np.array_equal(g_, r_)
+    assert rel_linf(lg.bve_sphere_velocity(*args, a, mode="fp32c"), ref) <= FP32C_TOL
+
+
+@pytest.mark.parametrize("delta", [0.0, 0.02])
+def test_plane_vs_oracle(lg, wl, oracle_mod, delta):
+    c = wl.config_colliding_dipoles(5)
+    args = (c["x"], c["y"], c["omega"], c["area"], c["active"])
+    ref = oracle_mod.plane_velocity(*args, delta)
+    got = lg.planar_incompressible_velocity(*args, delta)
+    for a, b in zip(got, ref):
+        assert np.array_equal(a, b)
+    assert rel_linf(lg.planar_incompressible_velocity(*args, delta, mode="fp32c"), ref) <= FP32C_TOL
+
+
+def test_pse_reference_thresholds_on_gpu(lg, wl):
+    """The reference regression test's thresholds hold for the GPU Laplacian (both modes)."""
+    m = lg.PolyMesh2d(205, 3, 1.0)
+    eps = m.max_edge_length ** 0.6
+    f = wl.y54(m.x, m.y, m.z)
+    exact = -30.0 * f
+    for mode in ("fp64", "fp32c"):
+        lap = lg.pse_sphere_laplacian_at_particles(m.x, m.y, m.z, f, m.area, m.active, eps, mode=mode)
+        err = np.abs(lap - exact)
+        assert err.max() / np.abs(exact).max() <= 0.0175
+        blk = slice(0, m.n // 4)
+        act = m.active[blk].astype(bool)
+        l2 = np.sum(err[blk][act] ** 2 * m.area[blk][act]) / np.sum(exact[blk][act] ** 2 * m.area[blk][act])
+        assert l2 <= 1.18e-4
+        lc = lg.pse_sphere_laplacian_at_particles(m.x, m.y, m.z, np.full(m.n, 2.0), m.area, m.active, eps, mode=mode)
+        assert np.abs(lc).max() <= 1e-10
+
+
+@pytest.mark.parametrize("kernel", [0, 1])
+def test_pse_vs_oracle(lg, wl, oracle_mod, kernel):
+    c = wl.config_pse_cubed(4)
+    eps = c["eps_k8"] if kernel == 0 else c["eps_gauss"]
+    args = (c["x"], c["y"], c["z"], c["f"], c["area"], c["active"], eps)
+    ref = oracle_mod.pse_laplacian(*args, 1.0, kernel)
+    got = lg.pse_sphere_laplacian_at_particles(*args, 1.0, kernel)
+    assert rel_linf(got, ref) <= 1e-12
+    got32 = lg.pse_sphere_laplacian_at_particles(*args, 1.0, kernel, mode="fp32c")
+    assert rel_linf(got32, ref) <= 1e-4
+
+
+def test_check_finite_flag(lg):
+    n = 4
+    x = np.array([1.0, 0.0, 0.0, np.nan])
+    y = np.array([0.0, 1.0, 0.0, 0.0])
+    z = np.array([0.0, 0.0, 1.0, 0.0])
+    act = np.ones(n, np.int32)
+    with pytest.raises(lg.LpmError) as e:
+        lg.bve_sphere_velocity(x, y, z, np.ones(n), np.ones(n), act, 1.0, mode=lg.MODE_FP64 | lg.FLAG_CHECK_FINITE)
+    assert e.value.code == -4
