@@ -1,0 +1,362 @@
+#!/usr/bin/env python3
+"""Benchmark of the sphere-BVE direct-sum hot path on GB300.
+
+Workload (the configuration the headline metric is quoted on): icosahedral mesh nest 8,
+1,966,082 targets and 1,310,720 active sources, relative vorticity = Rossby-Haurwitz wave 4
+plus a Gaussian vortex at a seeded random centre (mean removed), Omega = 2 pi.  One step is
+one classical RK4 step = 4 velocity sums (2.577e12 interactions each) plus the FP64 stage
+combinations, replayed from one CUDA graph, in LPM_MODE_FP32C, with the stage positions
+projected onto the sphere (at this resolution the unprojected stage positions of the
+reference scheme leave the sphere by more than the nearest-neighbour gap a^2 - x.x_j, and
+the Biot-Savart denominator changes sign).
+
+Metric: Ginteractions/s (interactions = N_targets * N_sources - self pairs per sum).
+  value : device time of the K steps with the state resident in HBM (CUDA events on the
+          solver's stream, L2 flushed with a 256 MB write between steps, outside the events)
+  e2e   : the same steps through the C ABI with the state copied from pinned host memory
+          before and back after every step (lpm_bve_set_state / lpm_bve_timestep /
+          lpm_bve_get_state), timed with CUDA events on the same stream
+  roofline: the velocity-sum kernels against the measured FP32 FMA peak (24 flops/pair)
+  cpu_baseline: the CPU oracle (the reference loop restated in C, OpenMP over targets) on
+          a bounded sample of targets against all sources
+
+--impl reference times the reference's CPU implementation of the path (the C restatement
+in oracle/, all host threads) on the same workload, each step a bounded target sample.
+Under torchrun (N > 1) every rank runs an independent replica on its own GPU (the path has
+no exchange step on one node's replicas), and value = all ranks' interactions / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(ROOT / "lpm-v2_gb300"))
+
+METRIC = "BVE direct-sum Ginteractions/s, FP32-comp vs FP64 on GB300 at <=1e-6 rel err"
+UNIT = "Ginteractions/s"
+FLOPS_PER_INTERACTION = 24  # dot 5, a^2-dot 1, x4pi a 1, zeta A/den 2, cross 9, accumulate 6
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse_args():
+    p = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--nest", type=int, default=8, help="icosahedral refinement level (8 = the metric's size)")
+    p.add_argument("--dt", type=float, default=0.01)
+    p.add_argument("--accuracy-targets", type=int, default=8192)
+    p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline sample budget")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def workload(nest: int):
+    import workloads as wl
+    c = wl.config_rh54_icos(nest, seed=0)
+    n = c["x"].size
+    ns = int(c["active"].sum())
+    per_sum = n * ns - ns
+    return c, n, ns, per_sum
+
+
+def workload_name(nest, n, ns):
+    return (f"sphere BVE RK4 step, icosahedral nest {nest} ({n} targets, {ns} sources), "
+            f"RH4 + Gaussian vortex, 4 velocity sums per step in one CUDA graph")
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi samples (200 ms) during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_id: str):
+        self.gpu_id = gpu_id
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", self.gpu_id], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def gpu_id_for(torch, dev: int) -> str:
+    try:
+        u = str(torch.cuda.get_device_properties(dev).uuid)
+        return u if u.startswith("GPU-") else f"GPU-{u}"
+    except Exception:
+        return str(dev)
+
+
+# ------------------------------------------------------------------ CPU sides
+def cpu_sample_rate(c, n, ns, budget_s: float):
+    """Times the oracle's BVE sum on a contiguous block of targets against all sources,
+    scaled so the sample takes about budget_s seconds.  Returns (Ginter/s, cores, desc)."""
+    from oracle import oracle as orc
+    args = (c["x"], c["y"], c["z"], c["zeta"], c["area"], c["active"])
+    start = n // 3
+    probe = 64
+    t0 = time.perf_counter()
+    orc.bve_velocity(*args, ib=start, ie=start + probe)
+    dt = max(time.perf_counter() - t0, 1e-6)
+    m = int(min(n - start, max(probe, probe * budget_s / dt)))
+    t0 = time.perf_counter()
+    orc.bve_velocity(*args, ib=start, ie=start + m)
+    el = time.perf_counter() - t0
+    act = int(c["active"][start:start + m].sum())
+    inter = m * ns - act
+    cores = os.cpu_count() or 1
+    desc = (f"oracle BVE sum (OpenMP, {cores} threads), targets {start + 1}..{start + m} of {n} against all "
+            f"{ns} sources ({inter:.3e} interactions, {el:.1f} s)")
+    return inter / el / 1e9, cores, desc, m
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    c, n, ns, per_sum = workload(args.nest)
+    from oracle import oracle as orc
+    # one step = the oracle sum over a fixed block of targets, sized to ~4 s
+    rate, cores, desc, m = cpu_sample_rate(c, n, ns, 4.0)
+    a = (c["x"], c["y"], c["z"], c["zeta"], c["area"], c["active"])
+    start = n // 3
+    for _ in range(args.warmup):
+        orc.bve_velocity(*a, ib=start, ie=start + m)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        orc.bve_velocity(*a, ib=start, ie=start + m)
+        times.append(time.perf_counter() - t0)
+    inter = m * ns - int(c["active"][start:start + m].sum())
+    value = inter * args.steps / sum(times) / 1e9
+    sample = (f"each step: the oracle BVE sum for targets {start + 1}..{start + m} against all {ns} sources "
+              f"({inter:.3e} interactions)")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": workload_name(args.nest, n, ns), "n_targets": n, "n_sources": ns,
+                   "interactions_per_sum": per_sum, "l2": "n/a (CPU)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------------ GPU side
+def run_ours(args):
+    import ctypes
+    import torch
+    import lpm_gpu as lg
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    c, n, ns, per_sum = workload(args.nest)
+    peak = lg.measure_fp32_peak(300.0)
+    stream = torch.cuda.Stream()
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    solver = lg.BVESolver(c["x"], c["y"], c["z"], c["zeta"], c["area"], c["active"], c["radius"], c["omega"],
+                          mode="fp32c")
+    solver.set_stream(stream.cuda_stream)
+    diag0 = solver.diagnostics()
+
+    for _ in range(args.warmup):
+        solver.timestep(args.dt, 1, renormalize=True)
+
+    # ---------------- timed region (state resident in HBM)
+    sampler = ClockSampler(gpu_id_for(torch, local))
+    sampler.start()
+    time.sleep(0.5)
+    k_ms0, k_n0 = solver.kernel_timing()
+    barrier()
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            flush.zero_()
+            starts[k].record(stream)
+            solver.timestep(args.dt, 1, renormalize=True)
+            ends[k].record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clocks = sampler.stop()
+    k_ms1, k_n1 = solver.kernel_timing()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = sum(step_ms)
+    if dist is not None:
+        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    inter_step = 4 * per_sum
+    value = world * inter_step * args.steps / (total_ms * 1e-3) / 1e9
+
+    # velocity-sum kernels: events around each sum inside the graph
+    sums = 4 * args.steps
+    sum_ms = (k_ms1 - k_ms0) / sums
+    achieved_tflops = FLOPS_PER_INTERACTION * per_sum / (sum_ms * 1e-3) / 1e12
+
+    # ---------------- accuracy of the FP32C velocity at the final state vs the FP64 sum
+    st = solver.get_state()
+    rng = np.random.default_rng(1)
+    m = min(args.accuracy_targets, n)
+    ib = int(rng.integers(0, n - m + 1)) + 1
+    u64 = lg.bve_sphere_velocity(st["x"], st["y"], st["z"], st["rel_vort"], c["area"], c["active"], c["radius"],
+                                 i_begin=ib, i_end=ib + m - 1, mode="fp64")
+    ref = np.stack([a[ib - 1:ib - 1 + m] for a in u64])
+    got = np.stack([st[k][ib - 1:ib - 1 + m] for k in ("u", "v", "w")])
+    rel_linf = float(np.abs(got - ref).max() / np.abs(ref).max())
+    rel_l2 = float(np.sqrt(np.sum((got - ref) ** 2) / np.sum(ref ** 2)))
+    diag1 = solver.diagnostics()
+
+    # ---------------- end to end through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        L = lg.lib()
+        host = {k: torch.from_numpy(np.ascontiguousarray(st[k])).pin_memory()
+                for k in ("x", "y", "z", "rel_vort", "u", "v", "w")}
+        ptrs = [ctypes.cast(host[k].data_ptr(), ctypes.POINTER(ctypes.c_double))
+                for k in ("x", "y", "z", "rel_vort", "u", "v", "w")]
+        es = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        ee = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        barrier()
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            for k in range(args.steps):
+                flush.zero_()
+                es[k].record(stream)
+                lg._check(L.lpm_bve_set_state(solver._h, *ptrs))
+                lg._check(L.lpm_bve_timestep(solver._h, args.dt, 1, 1))
+                lg._check(L.lpm_bve_get_state(solver._h, *ptrs))
+                ee[k].record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        e_ms = sum(s.elapsed_time(e) for s, e in zip(es, ee))
+        if dist is not None:
+            t = torch.tensor([e_ms], device="cuda", dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e_ms = float(t.item())
+        nbytes = 7 * n * 8
+        e2e = {"value": world * inter_step * args.steps / (e_ms * 1e-3) / 1e9, "unit": UNIT,
+               "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+               "path": "lpm_bve_set_state + lpm_bve_timestep + lpm_bve_get_state, pinned host buffers"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline and world == 1:
+        rate, cores, desc, _ = cpu_sample_rate(c, n, ns, args.cpu_seconds)
+        cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc}
+
+    solver.close()
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": workload_name(args.nest, n, ns), "n_targets": n, "n_sources": ns,
+                       "interactions_per_sum": per_sum, "sums_per_step": 4, "mode": "LPM_MODE_FP32C",
+                       "renormalize": "stage inputs and new positions projected onto the sphere",
+                       "dt": args.dt, "l2": "flushed between steps (256 MB write, outside the timed events)",
+                       "parallelism": f"replicas x{world}"},
+            "clocks": clocks,
+            "gpu_launches": (k_n1 - k_n0) + 4 * args.steps,
+            "roofline": {"bound": "fp32", "achieved": achieved_tflops, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved_tflops / peak, "traffic": None,
+                         "kernel": "sweep_fp32c_kernel<BveF32> (+prep, finish) per velocity sum",
+                         "ms_per_launch": sum_ms, "flops_per_interaction": FLOPS_PER_INTERACTION,
+                         "peak_source": "measured in-process FFMA loop (lpm_measure_fp32_peak)"},
+            "accuracy": {"velocity_rel_linf_vs_fp64": rel_linf, "velocity_rel_l2_vs_fp64": rel_l2,
+                         "targets": f"{ib}..{ib + m - 1}",
+                         "circulation_drift": diag1["circulation"] - diag0["circulation"],
+                         "ke_rel_drift": (diag1["kinetic_energy"] - diag0["kinetic_energy"]) / diag0["kinetic_energy"],
+                         "steps_advanced": args.warmup + args.steps},
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+            "step_ms": step_ms,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

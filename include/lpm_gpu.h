@@ -120,6 +120,83 @@ int lpm_plane_stream_function(int64_t n, const double* x, const double* y,
                               const int32_t* active, int64_t i_begin, int64_t i_end,
                               double* psi, int mode);
 
+/* ------------------------------------------------------------------ RK4 solvers */
+
+/* Device-resident BVESolver (src/SphereBVESolver.f90:38-353).  create copies the state
+ * (New(BVESolver, sphere)); u/v/w are the velocity at the initial positions (the stage-1
+ * reuse of the reference) -- pass NULL to have them computed with setVelocityFromVorticity.
+ * timestep advances n_steps classical RK4 steps without returning to the host; the four
+ * velocity sums of each step are replayed from one captured CUDA graph.  renormalize != 0
+ * projects positions back onto the sphere after each step (an extension; the reference
+ * does not renormalise). */
+typedef struct lpm_bve_solver lpm_bve_solver;
+int lpm_bve_solver_create(lpm_bve_solver** solver, int64_t n, const double* x,
+                          const double* y, const double* z, const double* relvort,
+                          const double* area, const int32_t* active, const double* u,
+                          const double* v, const double* w, double radius,
+                          double rotation_rate, int mode);
+int lpm_bve_timestep(lpm_bve_solver* solver, double dt, int n_steps, int renormalize);
+int lpm_bve_get_state(lpm_bve_solver* solver, double* x, double* y, double* z,
+                      double* relvort, double* u, double* v, double* w);
+int lpm_bve_set_state(lpm_bve_solver* solver, const double* x, const double* y,
+                      const double* z, const double* relvort, const double* u,
+                      const double* v, const double* w);
+/* KE = 1/2 sum |u|^2 A, enstrophy = 1/2 sum zeta^2 A, circulation = sum zeta A over
+ * active particles (src/SphereBVE.f90:410-441). */
+int lpm_bve_diagnostics(lpm_bve_solver* solver, double* kinetic_energy, double* enstrophy,
+                        double* circulation);
+/* Accumulated device time of the velocity-sum kernels launched by lpm_bve_timestep,
+ * measured with CUDA events on the solver's stream, and the number of such launches. */
+int lpm_bve_kernel_timing(lpm_bve_solver* solver, double* total_ms, int64_t* launches);
+/* Makes the solver enqueue its work on `stream` (a cudaStream_t of the caller's context;
+ * NULL restores the solver's own stream), so the caller can time it with events. */
+int lpm_bve_solver_set_stream(lpm_bve_solver* solver, void* stream);
+/* enable != 0 (the default): lpm_bve_timestep synchronises after every step to accumulate
+ * the kernel timing; 0: steps are replayed back to back with one synchronisation at the end. */
+int lpm_bve_solver_set_timing(lpm_bve_solver* solver, int enable);
+int lpm_bve_solver_destroy(lpm_bve_solver* solver);
+
+/* Device-resident PlaneSolver (src/PlaneIncompressibleSolver.f90:103-259). */
+typedef struct lpm_plane_solver lpm_plane_solver;
+int lpm_plane_solver_create(lpm_plane_solver** solver, int64_t n, const double* x,
+                            const double* y, const double* omega, const double* area,
+                            const int32_t* active, const double* u, const double* v,
+                            double delta, int mode);
+int lpm_plane_timestep(lpm_plane_solver* solver, double dt, int n_steps);
+int lpm_plane_get_state(lpm_plane_solver* solver, double* x, double* y, double* u,
+                        double* v);
+int lpm_plane_diagnostics(lpm_plane_solver* solver, double* kinetic_energy,
+                          double* enstrophy, double* circulation);
+int lpm_plane_solver_destroy(lpm_plane_solver* solver);
+
+/* ------------------------------------------------------------------ ensembles */
+
+/* Many independent sphere-BVE instances of uneven size advanced together.  Instance k
+ * owns particles offsets[k] .. offsets[k+1]-1 of the concatenated arrays.  Each RK4 stage
+ * of all instances is one persistent launch over a flattened (instance, target block,
+ * source range) work queue; the steps are replayed from a captured CUDA graph.  mode must
+ * be LPM_MODE_FP32C or LPM_MODE_FP64 (FP64 runs the bit-exact sweep instance by instance).
+ * renormalize has the meaning of lpm_bve_timestep's. */
+typedef struct lpm_ensemble lpm_ensemble;
+int lpm_ensemble_create(lpm_ensemble** ens, int n_instances, const int64_t* offsets,
+                        const double* x, const double* y, const double* z,
+                        const double* relvort, const double* area, const int32_t* active,
+                        const double* radius, const double* rotation_rate, int mode);
+int lpm_ensemble_timestep(lpm_ensemble* ens, double dt, int n_steps, int renormalize);
+/* One velocity evaluation of every instance at the current state. */
+int lpm_ensemble_velocity(lpm_ensemble* ens);
+int lpm_ensemble_get_state(lpm_ensemble* ens, double* x, double* y, double* z,
+                           double* relvort, double* u, double* v, double* w);
+int lpm_ensemble_kernel_timing(lpm_ensemble* ens, double* total_ms, int64_t* launches);
+int lpm_ensemble_destroy(lpm_ensemble* ens);
+
+/* ------------------------------------------------------------------ calibration */
+
+/* Runs a fused multiply-add throughput loop on every SM for about `ms_target` ms and
+ * returns the achieved FP32 rate in TFLOP/s (2 flops per FMA): the measured CUDA-core peak
+ * that the direct-sum kernels are reported against. */
+int lpm_measure_fp32_peak(double ms_target, double* tflops);
+
 #ifdef __cplusplus
 }
 #endif

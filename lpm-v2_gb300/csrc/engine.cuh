@@ -13,35 +13,40 @@
 
 namespace lpm {
 
-// Two-stage TMA pipeline over tiles [tile0, tile0 + ntl) of `src`.  body(const Rec* tile)
-// is called once per tile by every thread of the block.  Returns false on a timeout.
-template <class Rec, int TILE, class Body>
-__device__ __forceinline__ bool staged_sweep(const Rec* __restrict__ src, int64_t tile0,
-                                             int64_t ntl, Rec* stage0, Rec* stage1,
-                                             uint64_t* bars, int* status, Body&& body) {
-  constexpr uint32_t kBytes = TILE * sizeof(Rec);
-  static_assert(kBytes % 16 == 0, "tile bytes must be a multiple of 16");
+// Initialises the two stage barriers of a TMA pipeline (once per CTA).
+__device__ __forceinline__ void pipe_init(uint64_t* bars) {
   if (threadIdx.x == 0) {
     mbar_init(&bars[0], 1);
     mbar_init(&bars[1], 1);
     fence_mbar_init();
   }
   __syncthreads();
+}
+
+// Two-stage TMA pipeline over tiles [tile0, tile0 + ntl) of `src`.  body(const Rec* tile)
+// is called once per tile by every thread of the block.  `g` counts the tiles this CTA has
+// pushed through the pipeline so far (identical in every thread): tile g uses stage g & 1
+// and completes phase (g >> 1) & 1 of that stage's barrier, so one CTA can run many sweeps
+// (a persistent kernel) on barriers initialised once.  Returns false on a timeout.
+template <class Rec, int TILE, class Body>
+__device__ __forceinline__ bool staged_sweep(const Rec* __restrict__ src, int64_t tile0,
+                                             int64_t ntl, Rec* stage0, Rec* stage1,
+                                             uint64_t* bars, uint32_t& g, int* status, Body&& body) {
+  constexpr uint32_t kBytes = TILE * sizeof(Rec);
+  static_assert(kBytes % 16 == 0, "tile bytes must be a multiple of 16");
   if (threadIdx.x == 0) {
-    if (ntl > 0) {
-      mbar_arrive_expect_tx(&bars[0], kBytes);
-      tma_load_1d(stage0, src + tile0 * TILE, kBytes, &bars[0]);
-    }
-    if (ntl > 1) {
-      mbar_arrive_expect_tx(&bars[1], kBytes);
-      tma_load_1d(stage1, src + (tile0 + 1) * TILE, kBytes, &bars[1]);
+    for (int64_t k = 0; k < ntl && k < 2; ++k) {
+      const uint32_t gk = g + static_cast<uint32_t>(k);
+      mbar_arrive_expect_tx(&bars[gk & 1u], kBytes);
+      tma_load_1d((gk & 1u) ? stage1 : stage0, src + (tile0 + k) * TILE, kBytes, &bars[gk & 1u]);
     }
   }
   bool ok = true;
   int64_t k = 0;
   for (; k < ntl; ++k) {
-    const int s = static_cast<int>(k & 1);
-    const uint32_t phase = static_cast<uint32_t>((k >> 1) & 1);
+    const uint32_t gk = g + static_cast<uint32_t>(k);
+    const int s = static_cast<int>(gk & 1u);
+    const uint32_t phase = (gk >> 1) & 1u;
     const bool mine = mbar_wait_bounded(&bars[s], phase, status);
     if (!__syncthreads_and(mine)) {
       ok = false;
@@ -55,12 +60,13 @@ __device__ __forceinline__ bool staged_sweep(const Rec* __restrict__ src, int64_
     }
   }
   if (!ok && threadIdx.x == 0) {
-    // let copies that are still in flight land before the CTA exits (bounded again)
+    // let copies that are still in flight land before the CTA moves on (bounded again)
     for (int64_t kk = k; kk < ntl && kk < k + 2; ++kk) {
-      const int s = static_cast<int>(kk & 1);
-      mbar_wait_bounded(&bars[s], static_cast<uint32_t>((kk >> 1) & 1), status);
+      const uint32_t gk = g + static_cast<uint32_t>(kk);
+      mbar_wait_bounded(&bars[gk & 1u], (gk >> 1) & 1u, status);
     }
   }
+  g += static_cast<uint32_t>(ntl);
   return ok;
 }
 
@@ -108,7 +114,9 @@ __global__ void __launch_bounds__(THREADS, MINB) sweep_fp32c_kernel(SweepArgs<Op
     }
   }
 
-  staged_sweep<Rec, TILE>(a.src, tile0, ntl, stage[0], stage[1], bars, a.status,
+  pipe_init(bars);
+  uint32_t g = 0;
+  staged_sweep<Rec, TILE>(a.src, tile0, ntl, stage[0], stage[1], bars, g, a.status,
                           [&](const Rec* tile) {
                             float acc[TPT][NC];
 #pragma unroll

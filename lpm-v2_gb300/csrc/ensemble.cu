@@ -1,0 +1,630 @@
+// ensemble.cu -- many independent sphere-BVE instances of uneven size, advanced together.
+//
+// Layout in HBM: the instances' particle arrays are concatenated (instance k owns
+// particles off[k] .. off[k+1]-1); each instance's active sources are compacted into its
+// own tile-padded range of one packed source-record array.
+//
+// Work decomposition: each velocity evaluation of all instances is a flattened list of
+// work items (instance, block of 512 targets, range of source tiles).  Source ranges are cut
+// so that items cost about the same, and the items are sorted by decreasing cost.  One
+// persistent launch (a few CTAs per SM) pulls items from an atomic queue; each item writes
+// its own FP64 partial slot, and a finish kernel reduces the slots of a target block in a
+// fixed order, so the result does not depend on which CTA ran which item.  With the four
+// RK4 stage kernels, one step of all instances is 9 launches, captured in one CUDA graph.
+//
+// FP64 mode (parity) runs the bit-exact sequential sweep per instance instead.
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+#include <vector>
+
+#include "bve_x2.cuh"
+#include "lpm_common.cuh"
+#include "solver.cuh"
+#include "sums.cuh"
+
+namespace lpm {
+namespace {
+
+constexpr int kThreads = 128, kTpt = 4, kTile = 256, kMinB = 4;
+constexpr int kTB = kThreads * kTpt;  // targets per block (work item)
+constexpr double kPi = 3.1415926535897932384626433832795027975;
+constexpr int kStage = 256;
+
+struct Item {
+  int inst;
+  int nt;         // targets in this item (<= kTB)
+  long long t0;   // first target (global particle index)
+  long long tile0;  // first source tile (global tile index)
+  int ntiles;
+  int pad;
+  long long slot;  // partial slot (item id in block order)
+};
+
+struct EnsArgs {
+  const Item* items;
+  const int* queue;
+  int n_items;
+  int* head;
+  const BveX2::Rec* src;
+  const double *x, *y, *z;
+  const double* inv_a;  // per instance
+  double* partial;      // [slot][3][kTB]
+  int* status;
+};
+
+__global__ void __launch_bounds__(kThreads, kMinB) ensemble_sweep_kernel(EnsArgs a) {
+  constexpr int NP = kTpt / 2;
+  using Rec = BveX2::Rec;
+  __shared__ __align__(128) Rec stage[2][kTile];
+  __shared__ __align__(8) uint64_t bars[2];
+  __shared__ int s_item;
+  pipe_init(bars);
+  uint32_t g = 0;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(a.head, 1);
+    __syncthreads();
+    const int q = s_item;
+    __syncthreads();
+    if (q >= a.n_items) break;
+    const Item it = a.items[a.queue[q]];
+    const BveF32::Params prm{a.x, a.y, a.z, a.inv_a[it.inst]};
+    BveX2::Pair pr[NP];
+    float2 hx[NP], hy[NP], hz[NP], lx[NP], ly[NP], lz[NP];
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+      int l0 = (2 * p) * kThreads + threadIdx.x, l1 = (2 * p + 1) * kThreads + threadIdx.x;
+      if (l0 >= it.nt) l0 = it.nt - 1;
+      if (l1 >= it.nt) l1 = it.nt - 1;
+      const BveF32::Tgt t0 = BveF32::load_target(prm, it.t0 + l0);
+      const BveF32::Tgt t1 = BveF32::load_target(prm, it.t0 + l1);
+      pr[p].xh = make_float2(t0.xh, t1.xh);
+      pr[p].yh = make_float2(t0.yh, t1.yh);
+      pr[p].zh = make_float2(t0.zh, t1.zh);
+      pr[p].xl = make_float2(t0.xl, t1.xl);
+      pr[p].yl = make_float2(t0.yl, t1.yl);
+      pr[p].zl = make_float2(t0.zl, t1.zl);
+      pr[p].nc = make_float2(t0.nc, t1.nc);
+      hx[p] = hy[p] = hz[p] = lx[p] = ly[p] = lz[p] = make_float2(0.f, 0.f);
+    }
+    const bool ok = staged_sweep<Rec, kTile>(a.src, it.tile0, it.ntiles, stage[0], stage[1], bars, g, a.status,
+                                             [&](const Rec* tile) {
+      float2 ax[NP], ay[NP], az[NP];
+#pragma unroll
+      for (int p = 0; p < NP; ++p) ax[p] = ay[p] = az[p] = make_float2(0.f, 0.f);
+#pragma unroll 2
+      for (int j = 0; j < kTile; ++j) {
+        const float4 ra = tile[j].a, rb = tile[j].b, rc = tile[j].c, rd = tile[j].d;
+        const float2 nxh = lo2(ra), nyh = hi2(ra), nzh = lo2(rb), nxl = hi2(rb), nyl = lo2(rc), nzl = hi2(rc);
+        const float2 ncj = lo2(rd), s2 = hi2(rd);
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+          const float2 dx = __fadd2_rn(__fadd2_rn(pr[p].xh, nxh), __fadd2_rn(pr[p].xl, nxl));
+          const float2 dy = __fadd2_rn(__fadd2_rn(pr[p].yh, nyh), __fadd2_rn(pr[p].yl, nyl));
+          const float2 dz = __fadd2_rn(__fadd2_rn(pr[p].zh, nzh), __fadd2_rn(pr[p].zl, nzl));
+          float2 qq = __fadd2_rn(pr[p].nc, ncj);
+          qq = __ffma2_rn(dx, dx, qq);
+          qq = __ffma2_rn(dy, dy, qq);
+          qq = __ffma2_rn(dz, dz, qq);
+          const float2 inv = make_float2(rcp_approx(qq.x), rcp_approx(qq.y));
+          const float2 wgt = __fmul2_rn(s2, inv);
+          ax[p] = __ffma2_rn(wgt, dx, ax[p]);
+          ay[p] = __ffma2_rn(wgt, dy, ay[p]);
+          az[p] = __ffma2_rn(wgt, dz, az[p]);
+        }
+      }
+#pragma unroll
+      for (int p = 0; p < NP; ++p) {
+        comp_add(hx[p].x, lx[p].x, ax[p].x);
+        comp_add(hx[p].y, lx[p].y, ax[p].y);
+        comp_add(hy[p].x, ly[p].x, ay[p].x);
+        comp_add(hy[p].y, ly[p].y, ay[p].y);
+        comp_add(hz[p].x, lz[p].x, az[p].x);
+        comp_add(hz[p].y, lz[p].y, az[p].y);
+      }
+    });
+    if (!ok) break;
+    double* slot = a.partial + it.slot * 3 * kTB;
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int l = (2 * p + h) * kThreads + threadIdx.x;
+        if (l < it.nt) {
+          slot[0 * kTB + l] = static_cast<double>(h ? hx[p].y : hx[p].x) + static_cast<double>(h ? lx[p].y : lx[p].x);
+          slot[1 * kTB + l] = static_cast<double>(h ? hy[p].y : hy[p].x) + static_cast<double>(h ? ly[p].y : ly[p].x);
+          slot[2 * kTB + l] = static_cast<double>(h ? hz[p].y : hz[p].x) + static_cast<double>(h ? lz[p].y : lz[p].x);
+        }
+      }
+    }
+  }
+}
+
+// Packed source records of all instances: record r holds particle src_gidx[r] (inert if < 0).
+__global__ void ensemble_prep_kernel(int64_t nrec, const int32_t* src_gidx, const int32_t* pinst,
+                                     const double* x, const double* y, const double* z, const double* zeta,
+                                     const double* area, const double* radius, BveX2::Rec* out) {
+  const int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (r >= nrec) return;
+  const int32_t j = src_gidx[r];
+  BveX2::Rec rec;
+  if (j >= 0) {
+    const double a = radius[pinst[j]];
+    const double inv_a = 1.0 / a;
+    const double px = x[j] * inv_a, py = y[j] * inv_a, pz = z[j] * inv_a;
+    float xh, xl, yh, yl, zh, zl;
+    split2(px, xh, xl);
+    split2(py, yh, yl);
+    split2(pz, zh, zl);
+    const float nc = __double2float_rn(-fma(px, px, fma(py, py, fma(pz, pz, -1.0))));
+    const float s = __double2float_rn(zeta[j] * area[j] * (-1.0 / (2.0 * kPi * a)));
+    rec.a = make_float4(-xh, -xh, -yh, -yh);
+    rec.b = make_float4(-zh, -zh, -xl, -xl);
+    rec.c = make_float4(-yl, -yl, -zl, -zl);
+    rec.d = make_float4(nc, nc, s, s);
+  } else {
+    rec.a = rec.b = rec.c = rec.d = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  out[r] = rec;
+}
+
+// Per target: fixed-order FP64 sum of its block's item slots, then u = D x p.
+__global__ void ensemble_finish_kernel(int64_t n, const int32_t* pinst, const int64_t* off,
+                                       const int32_t* blk_off, const int32_t* blk_first, const int32_t* blk_cnt,
+                                       const double* partial, const double* x, const double* y, const double* z,
+                                       const double* inv_a, double* u, double* v, double* w) {
+  const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int k = pinst[i];
+  const int64_t local = i - off[k];
+  const int b = blk_off[k] + static_cast<int>(local / kTB);
+  const int l = static_cast<int>(local % kTB);
+  double d0 = 0.0, d1 = 0.0, d2 = 0.0;
+  for (int c = 0; c < blk_cnt[b]; ++c) {
+    const double* slot = partial + static_cast<int64_t>(blk_first[b] + c) * 3 * kTB;
+    d0 += slot[l];
+    d1 += slot[kTB + l];
+    d2 += slot[2 * kTB + l];
+  }
+  const double ia = inv_a[k];
+  const double px = x[i] * ia, py = y[i] * ia, pz = z[i] * ia;
+  u[i] = d1 * pz - d2 * py;
+  v[i] = d2 * px - d0 * pz;
+  w[i] = d0 * py - d1 * px;
+}
+
+__device__ __forceinline__ void project_to(double a, double& x, double& y, double& z) {
+  const double s = a / sqrt(x * x + y * y + z * z);
+  x *= s;
+  y *= s;
+  z *= s;
+}
+
+// RK4 stages of timestepPrivate (SphereBVESolver.f90:238-329) with per-instance radius and
+// rotation rate; the arithmetic and its order are those of the single-instance solver.
+__global__ void ensemble_stage_kernel(int64_t n, int which, int renorm, double dt, const int32_t* pinst,
+                                      const double* radius, const double* omega, double* x, double* y, double* z,
+                                      double* q, const double* us, const double* vs, const double* ws, double* ax,
+                                      double* ay, double* az, double* aq, double* xin, double* yin, double* zin,
+                                      double* qin) {
+  const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int k = pinst[i];
+  const double a = radius[k];
+  const double two_dt_omega = __dmul_rn(__dmul_rn(dt, 2.0), omega[k]);
+  const double kq = -__ddiv_rn(__dmul_rn(two_dt_omega, ws[i]), a);
+  const double kx = __dmul_rn(dt, us[i]);
+  const double ky = __dmul_rn(dt, vs[i]);
+  const double kz = __dmul_rn(dt, ws[i]);
+  double px, py, pz;
+  if (which == 0) {  // stage 1: k1 from the stored velocity
+    ax[i] = __dadd_rn(x[i], __ddiv_rn(kx, 6.0));
+    ay[i] = __dadd_rn(y[i], __ddiv_rn(ky, 6.0));
+    az[i] = __dadd_rn(z[i], __ddiv_rn(kz, 6.0));
+    aq[i] = __dadd_rn(q[i], __ddiv_rn(kq, 6.0));
+  } else if (which < 3) {
+    ax[i] = __dadd_rn(ax[i], __ddiv_rn(kx, 3.0));
+    ay[i] = __dadd_rn(ay[i], __ddiv_rn(ky, 3.0));
+    az[i] = __dadd_rn(az[i], __ddiv_rn(kz, 3.0));
+    aq[i] = __dadd_rn(aq[i], __ddiv_rn(kq, 3.0));
+  }
+  if (which < 2) {
+    px = __dadd_rn(x[i], __dmul_rn(0.5, kx));
+    py = __dadd_rn(y[i], __dmul_rn(0.5, ky));
+    pz = __dadd_rn(z[i], __dmul_rn(0.5, kz));
+    qin[i] = __dadd_rn(q[i], __dmul_rn(0.5, kq));
+  } else if (which == 2) {
+    px = __dadd_rn(x[i], kx);
+    py = __dadd_rn(y[i], ky);
+    pz = __dadd_rn(z[i], kz);
+    qin[i] = __dadd_rn(q[i], kq);
+  } else {
+    px = __dadd_rn(ax[i], __ddiv_rn(kx, 6.0));
+    py = __dadd_rn(ay[i], __ddiv_rn(ky, 6.0));
+    pz = __dadd_rn(az[i], __ddiv_rn(kz, 6.0));
+    if (renorm) project_to(a, px, py, pz);
+    x[i] = px;
+    y[i] = py;
+    z[i] = pz;
+    q[i] = __dadd_rn(aq[i], __ddiv_rn(kq, 6.0));
+    return;
+  }
+  if (renorm) project_to(a, px, py, pz);
+  xin[i] = px;
+  yin[i] = py;
+  zin[i] = pz;
+}
+
+}  // namespace
+}  // namespace lpm
+
+using namespace lpm;
+
+struct lpm_ensemble {
+  Context* ctx = nullptr;
+  cudaStream_t stream = nullptr;
+  DeviceArena arena;
+  int K = 0;
+  int64_t n = 0;
+  int mode = LPM_MODE_FP32C;
+  std::vector<int64_t> off;  // host copy
+  std::vector<int64_t> ns_k;
+  double *x, *y, *z, *q, *u, *v, *w, *area;
+  double *ax, *ay, *az, *aq, *xin, *yin, *zin, *qin, *us, *vs, *ws;
+  int32_t* pinst = nullptr;
+  int64_t* d_off = nullptr;
+  double *radius = nullptr, *omega = nullptr, *inv_a = nullptr;
+  // FP32C work queue
+  int64_t nrec = 0;
+  int32_t* src_gidx = nullptr;
+  BveX2::Rec* rec = nullptr;
+  Item* items = nullptr;
+  int* queue = nullptr;
+  int n_items = 0;
+  int* head = nullptr;
+  int32_t *blk_off = nullptr, *blk_first = nullptr, *blk_cnt = nullptr;
+  double* partial = nullptr;
+  int grid = 0;
+  // FP64 per-instance scratch
+  std::vector<SumScratch> scratch64;
+  std::vector<int32_t*> idx64;
+  int* status = nullptr;
+  int* h_status = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  double graph_dt = 0.0;
+  int graph_renorm = -1;
+  cudaEvent_t ev[8] = {};
+  double kernel_ms = 0.0;
+  int64_t launches = 0;
+
+  int velocity(const double* px, const double* py, const double* pz, const double* pq, double* o0, double* o1,
+               double* o2, int kind = kSumBve) {
+    if (mode == LPM_MODE_FP64) {
+      for (int k = 0; k < K; ++k) {
+        const int64_t nk = off[k + 1] - off[k];
+        if (ns_k[k] == 0) {
+          LPM_CUDA_TRY(cudaMemsetAsync(o0 + off[k], 0, nk * sizeof(double), stream));
+          LPM_CUDA_TRY(cudaMemsetAsync(o1 + off[k], 0, nk * sizeof(double), stream));
+          LPM_CUDA_TRY(cudaMemsetAsync(o2 + off[k], 0, nk * sizeof(double), stream));
+          continue;
+        }
+        SumJob j;
+        j.kind = kind;
+        j.mode = LPM_MODE_FP64;
+        j.n = nk;
+        j.x = px + off[k];
+        j.y = py + off[k];
+        j.z = pz + off[k];
+        j.s1 = pq + off[k];
+        j.area = area + off[k];
+        j.src_idx = idx64[k];
+        j.ns = ns_k[k];
+        j.radius = h_radius[k];
+        j.ib = 0;
+        j.nt = nk;
+        j.out0 = o0 + off[k];
+        j.out1 = o1 + off[k];
+        j.out2 = o2 + off[k];
+        j.src_buf = scratch64[k].src_buf;
+        j.status = status;
+        j.stream = stream;
+        LPM_TRY(launch_sum(j, scratch64[k].plan));
+      }
+      return LPM_OK;
+    }
+    const unsigned pg = static_cast<unsigned>(ceil_div(nrec > 0 ? nrec : 1, 256));
+    ensemble_prep_kernel<<<pg, 256, 0, stream>>>(nrec, src_gidx, pinst, px, py, pz, pq, area, radius, rec);
+    LPM_CUDA_TRY(cudaMemsetAsync(head, 0, sizeof(int), stream));
+    EnsArgs a{items, queue, n_items, head, rec, px, py, pz, inv_a, partial, status};
+    ensemble_sweep_kernel<<<grid, kThreads, 0, stream>>>(a);
+    ensemble_finish_kernel<<<static_cast<unsigned>(ceil_div(n, 256)), 256, 0, stream>>>(
+        n, pinst, d_off, blk_off, blk_first, blk_cnt, partial, px, py, pz, inv_a, o0, o1, o2);
+    LPM_CUDA_TRY(cudaGetLastError());
+    return LPM_OK;
+  }
+
+  std::vector<double> h_radius, h_omega;
+
+  int enqueue_step(double dt, int renorm) {
+    const unsigned g = static_cast<unsigned>(ceil_div(n, kStage));
+    ensemble_stage_kernel<<<g, kStage, 0, stream>>>(n, 0, renorm, dt, pinst, radius, omega, x, y, z, q, u, v, w, ax,
+                                                    ay, az, aq, xin, yin, zin, qin);
+    LPM_CUDA_TRY(cudaGetLastError());
+    for (int s = 0; s < 3; ++s) {
+      LPM_CUDA_TRY(cudaEventRecordWithFlags(ev[2 * s], stream, cudaEventRecordExternal));
+      LPM_TRY(velocity(xin, yin, zin, qin, us, vs, ws));
+      LPM_CUDA_TRY(cudaEventRecordWithFlags(ev[2 * s + 1], stream, cudaEventRecordExternal));
+      ensemble_stage_kernel<<<g, kStage, 0, stream>>>(n, s + 1, renorm, dt, pinst, radius, omega, x, y, z, q, us, vs,
+                                                      ws, ax, ay, az, aq, xin, yin, zin, qin);
+      LPM_CUDA_TRY(cudaGetLastError());
+    }
+    LPM_CUDA_TRY(cudaEventRecordWithFlags(ev[6], stream, cudaEventRecordExternal));
+    LPM_TRY(velocity(x, y, z, q, u, v, w));
+    LPM_CUDA_TRY(cudaEventRecordWithFlags(ev[7], stream, cudaEventRecordExternal));
+    return LPM_OK;
+  }
+
+  int capture(double dt, int renorm) {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    exec = nullptr;
+    graph = nullptr;
+    LPM_CUDA_TRY(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    const int rc = enqueue_step(dt, renorm);
+    cudaGraph_t gr = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(stream, &gr);
+    if (rc != LPM_OK) {
+      if (gr) cudaGraphDestroy(gr);
+      return rc;
+    }
+    if (e != cudaSuccess) return set_error(LPM_ERR_CUDA, "stream capture failed: %s", cudaGetErrorString(e));
+    graph = gr;
+    LPM_CUDA_TRY(cudaGraphInstantiate(&exec, graph, 0));
+    graph_dt = dt;
+    graph_renorm = renorm;
+    return LPM_OK;
+  }
+
+  int check_status(const char* what) {
+    LPM_CUDA_TRY(cudaMemcpyAsync(h_status, status, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    const cudaError_t e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) return set_error(LPM_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+    if (*h_status != kDevOk) {
+      const int st = *h_status;
+      LPM_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int), stream));
+      LPM_CUDA_TRY(cudaStreamSynchronize(stream));
+      return set_error(st == kDevTimeout ? LPM_ERR_TIMEOUT : LPM_ERR_CUDA, "%s: device status %d", what, st);
+    }
+    return LPM_OK;
+  }
+
+  void destroy() {
+    if (stream) cudaStreamSynchronize(stream);
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    for (auto& e : ev)
+      if (e) cudaEventDestroy(e);
+    if (h_status) cudaFreeHost(h_status);
+    arena.release();
+    if (stream) cudaStreamDestroy(stream);
+  }
+
+  template <class T>
+  int dev_array(T** p, size_t count) {
+    void* q = nullptr;
+    LPM_TRY(arena.alloc(count * sizeof(T), &q));
+    *p = static_cast<T*>(q);
+    return LPM_OK;
+  }
+
+  template <class T>
+  int upload_vec(T** p, const std::vector<T>& h) {
+    LPM_TRY(dev_array(p, h.size()));
+    if (!h.empty()) LPM_CUDA_TRY(cudaMemcpyAsync(*p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, stream));
+    return LPM_OK;
+  }
+
+  // Builds the flattened work queue of the FP32C sweep.
+  int build_queue(const int32_t* active) {
+    std::vector<int32_t> gidx;
+    std::vector<int64_t> tile_off(K + 1, 0);
+    for (int k = 0; k < K; ++k) {
+      const int64_t start = static_cast<int64_t>(gidx.size());
+      for (int64_t j = off[k]; j < off[k + 1]; ++j)
+        if (active[j]) gidx.push_back(static_cast<int32_t>(j));
+      const int64_t cnt = static_cast<int64_t>(gidx.size()) - start;
+      const int64_t tiles = ceil_div(cnt, kTile);
+      gidx.resize(start + tiles * kTile, -1);
+      tile_off[k + 1] = tile_off[k] + tiles;
+    }
+    nrec = static_cast<int64_t>(gidx.size());
+    // item size: aim at ~8 items per resident CTA slot
+    double units = 0.0;
+    for (int k = 0; k < K; ++k)
+      units += static_cast<double>(ceil_div(off[k + 1] - off[k], kTB)) * static_cast<double>(tile_off[k + 1] - tile_off[k]);
+    const int slots = ctx->sm_count * kMinB;
+    const int64_t chunk_tiles = std::max<int64_t>(1, static_cast<int64_t>(std::ceil(units / (8.0 * slots))));
+    std::vector<Item> it;
+    std::vector<int32_t> boff(K + 1, 0), bfirst, bcnt;
+    for (int k = 0; k < K; ++k) {
+      const int64_t nk = off[k + 1] - off[k];
+      const int64_t tiles = tile_off[k + 1] - tile_off[k];
+      const int64_t nblk = ceil_div(nk, kTB);
+      boff[k + 1] = boff[k] + static_cast<int32_t>(nblk);
+      const int64_t nch = tiles > 0 ? ceil_div(tiles, chunk_tiles) : 0;
+      const int64_t per = nch > 0 ? ceil_div(tiles, nch) : 0;
+      for (int64_t b = 0; b < nblk; ++b) {
+        bfirst.push_back(static_cast<int32_t>(it.size()));
+        int cnt = 0;
+        for (int64_t t = 0; t < tiles; t += per) {
+          Item m;
+          m.inst = k;
+          m.t0 = off[k] + b * kTB;
+          m.nt = static_cast<int>(std::min<int64_t>(kTB, nk - b * kTB));
+          m.tile0 = tile_off[k] + t;
+          m.ntiles = static_cast<int>(std::min<int64_t>(per, tiles - t));
+          m.pad = 0;
+          m.slot = static_cast<long long>(it.size());
+          it.push_back(m);
+          ++cnt;
+        }
+        bcnt.push_back(cnt);
+      }
+    }
+    n_items = static_cast<int>(it.size());
+    std::vector<int> order(it.size());
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int p, int q) {
+      return static_cast<int64_t>(it[p].nt) * it[p].ntiles > static_cast<int64_t>(it[q].nt) * it[q].ntiles;
+    });
+    LPM_TRY(upload_vec(&src_gidx, gidx));
+    LPM_TRY(dev_array(&rec, std::max<int64_t>(nrec, 1)));
+    LPM_TRY(upload_vec(&items, it));
+    LPM_TRY(upload_vec(&queue, order));
+    LPM_TRY(upload_vec(&blk_off, boff));
+    LPM_TRY(upload_vec(&blk_first, bfirst));
+    LPM_TRY(upload_vec(&blk_cnt, bcnt));
+    LPM_TRY(dev_array(&head, 1));
+    LPM_TRY(dev_array(&partial, std::max<size_t>(1, static_cast<size_t>(n_items) * 3 * kTB)));
+    grid = std::max(1, std::min(n_items, slots));
+    return LPM_OK;
+  }
+};
+
+namespace {
+
+int ens_create(lpm_ensemble* E, int K, const int64_t* offsets, const double* x, const double* y, const double* z,
+               const double* q, const double* area, const int32_t* active, const double* radius,
+               const double* omega, int mode) {
+  LPM_TRY(get_context(&E->ctx));
+  E->K = K;
+  E->mode = mode;
+  E->off.assign(offsets, offsets + K + 1);
+  E->n = E->off[K];
+  E->h_radius.assign(radius, radius + K);
+  E->h_omega.assign(omega, omega + K);
+  LPM_CUDA_TRY(cudaStreamCreateWithFlags(&E->stream, cudaStreamNonBlocking));
+  const int64_t n = E->n;
+  double** arrs[] = {&E->x, &E->y, &E->z, &E->q, &E->u, &E->v, &E->w, &E->area, &E->ax, &E->ay, &E->az,
+                     &E->aq, &E->xin, &E->yin, &E->zin, &E->qin, &E->us, &E->vs, &E->ws};
+  for (double** a : arrs) LPM_TRY(E->dev_array(a, n));
+  std::vector<int32_t> pinst(n);
+  E->ns_k.assign(K, 0);
+  for (int k = 0; k < K; ++k) {
+    for (int64_t j = E->off[k]; j < E->off[k + 1]; ++j) {
+      pinst[j] = k;
+      E->ns_k[k] += active[j] ? 1 : 0;
+    }
+  }
+  std::vector<double> inv(K);
+  for (int k = 0; k < K; ++k) inv[k] = 1.0 / radius[k];
+  LPM_TRY(E->upload_vec(&E->pinst, pinst));
+  LPM_TRY(E->upload_vec(&E->d_off, E->off));
+  LPM_TRY(E->upload_vec(&E->radius, E->h_radius));
+  LPM_TRY(E->upload_vec(&E->omega, E->h_omega));
+  LPM_TRY(E->upload_vec(&E->inv_a, inv));
+  LPM_TRY(E->dev_array(&E->status, 1));
+  LPM_CUDA_TRY(cudaMemsetAsync(E->status, 0, sizeof(int), E->stream));
+  LPM_CUDA_TRY(cudaMallocHost(&E->h_status, sizeof(int)));
+  const size_t nb = n * sizeof(double);
+  LPM_CUDA_TRY(cudaMemcpyAsync(E->x, x, nb, cudaMemcpyHostToDevice, E->stream));
+  LPM_CUDA_TRY(cudaMemcpyAsync(E->y, y, nb, cudaMemcpyHostToDevice, E->stream));
+  LPM_CUDA_TRY(cudaMemcpyAsync(E->z, z, nb, cudaMemcpyHostToDevice, E->stream));
+  LPM_CUDA_TRY(cudaMemcpyAsync(E->q, q, nb, cudaMemcpyHostToDevice, E->stream));
+  LPM_CUDA_TRY(cudaMemcpyAsync(E->area, area, nb, cudaMemcpyHostToDevice, E->stream));
+  for (auto& e : E->ev) LPM_CUDA_TRY(cudaEventCreate(&e));
+  if (mode == LPM_MODE_FP64) {
+    E->scratch64.resize(K);
+    E->idx64.assign(K, nullptr);
+    for (int k = 0; k < K; ++k) {
+      const int64_t nk = E->off[k + 1] - E->off[k];
+      const std::vector<int32_t> idx = active_list(nk, active + E->off[k]);
+      LPM_TRY(E->upload_vec(&E->idx64[k], idx));
+      LPM_TRY(E->scratch64[k].init(E->arena, kSumBve, LPM_MODE_FP64, E->ns_k[k], nk, E->ctx->sm_count));
+    }
+  } else {
+    LPM_TRY(E->build_queue(active));
+  }
+  // initial velocity: setVelocityFromVorticity (SphereBVE.f90:489-531)
+  LPM_TRY(E->velocity(E->x, E->y, E->z, E->q, E->u, E->v, E->w, kSumBveMesh));
+  return E->check_status("lpm_ensemble_create");
+}
+
+}  // namespace
+
+extern "C" int lpm_ensemble_create(lpm_ensemble** out, int n_instances, const int64_t* offsets, const double* x,
+                                   const double* y, const double* z, const double* relvort, const double* area,
+                                   const int32_t* active, const double* radius, const double* rotation_rate,
+                                   int mode) {
+  if (!out) return set_error(LPM_ERR_ARG, "null ensemble handle pointer");
+  *out = nullptr;
+  if (n_instances <= 0 || !offsets) return set_error(LPM_ERR_ARG, "need at least one instance and offsets");
+  if (!x || !y || !z || !relvort || !area || !active || !radius || !rotation_rate)
+    return set_error(LPM_ERR_ARG, "null input array");
+  if (mode != LPM_MODE_FP64 && mode != LPM_MODE_FP32C) return set_error(LPM_ERR_ARG, "unknown mode %d", mode);
+  if (offsets[0] != 0) return set_error(LPM_ERR_ARG, "offsets[0] must be 0");
+  for (int k = 0; k < n_instances; ++k) {
+    if (offsets[k + 1] <= offsets[k]) return set_error(LPM_ERR_ARG, "instance %d is empty", k);
+    if (!(radius[k] > 0.0)) return set_error(LPM_ERR_ARG, "instance %d radius must be positive", k);
+  }
+  if (offsets[n_instances] > INT32_MAX) return set_error(LPM_ERR_ARG, "too many particles");
+  lpm_ensemble* E = new lpm_ensemble();
+  const int rc = ens_create(E, n_instances, offsets, x, y, z, relvort, area, active, radius, rotation_rate, mode);
+  if (rc != LPM_OK) {
+    E->destroy();
+    delete E;
+    return rc;
+  }
+  *out = E;
+  return LPM_OK;
+}
+
+extern "C" int lpm_ensemble_timestep(lpm_ensemble* E, double dt, int n_steps, int renormalize) {
+  if (!E) return set_error(LPM_ERR_ARG, "null ensemble");
+  if (n_steps < 0 || !std::isfinite(dt)) return set_error(LPM_ERR_ARG, "bad dt or n_steps");
+  const int renorm = renormalize ? 1 : 0;
+  if (!E->exec || E->graph_dt != dt || E->graph_renorm != renorm) LPM_TRY(E->capture(dt, renorm));
+  for (int s = 0; s < n_steps; ++s) {
+    LPM_CUDA_TRY(cudaGraphLaunch(E->exec, E->stream));
+    LPM_TRY(E->check_status("lpm_ensemble_timestep"));
+    for (int k = 0; k < 4; ++k) {
+      float ms = 0.f;
+      LPM_CUDA_TRY(cudaEventElapsedTime(&ms, E->ev[2 * k], E->ev[2 * k + 1]));
+      E->kernel_ms += ms;
+    }
+    E->launches += (E->mode == LPM_MODE_FP64) ? 4 * 2 * E->K : 4 * 3;
+  }
+  return LPM_OK;
+}
+
+extern "C" int lpm_ensemble_velocity(lpm_ensemble* E) {
+  if (!E) return set_error(LPM_ERR_ARG, "null ensemble");
+  LPM_TRY(E->velocity(E->x, E->y, E->z, E->q, E->u, E->v, E->w));
+  return E->check_status("lpm_ensemble_velocity");
+}
+
+extern "C" int lpm_ensemble_get_state(lpm_ensemble* E, double* x, double* y, double* z, double* relvort, double* u,
+                                      double* v, double* w) {
+  if (!E) return set_error(LPM_ERR_ARG, "null ensemble");
+  const size_t nb = E->n * sizeof(double);
+  double* hs[] = {x, y, z, relvort, u, v, w};
+  const double* ds[] = {E->x, E->y, E->z, E->q, E->u, E->v, E->w};
+  for (int c = 0; c < 7; ++c)
+    if (hs[c]) LPM_CUDA_TRY(cudaMemcpyAsync(hs[c], ds[c], nb, cudaMemcpyDeviceToHost, E->stream));
+  return E->check_status("lpm_ensemble_get_state");
+}
+
+extern "C" int lpm_ensemble_kernel_timing(lpm_ensemble* E, double* total_ms, int64_t* launches) {
+  if (!E) return set_error(LPM_ERR_ARG, "null ensemble");
+  if (total_ms) *total_ms = E->kernel_ms;
+  if (launches) *launches = E->launches;
+  return LPM_OK;
+}
+
+extern "C" int lpm_ensemble_destroy(lpm_ensemble* E) {
+  if (!E) return LPM_OK;
+  E->destroy();
+  delete E;
+  return LPM_OK;
+}

@@ -1,0 +1,30 @@
+// solver.cuh -- ownership helpers shared by the device-resident solvers and the ensemble.
+#pragma once
+
+#include <vector>
+
+#include "lpm_common.cuh"
+#include "sums.cuh"
+
+namespace lpm {
+
+// Device allocations owned by one handle, freed together.
+struct DeviceArena {
+  std::vector<void*> ptrs;
+  int alloc(size_t bytes, void** p);
+  void release();
+};
+
+// The scratch of one direct sum (source records + split-K partials), sized once so that
+// the launches can be captured into a CUDA graph.
+struct SumScratch {
+  SumPlan plan;
+  void* src_buf = nullptr;
+  double* partial = nullptr;
+  int init(DeviceArena& arena, int kind, int mode, int64_t ns, int64_t nt, int sm_count);
+};
+
+// Indices of the active particles, ascending.
+std::vector<int32_t> active_list(int64_t n, const int32_t* active);
+
+}  // namespace lpm

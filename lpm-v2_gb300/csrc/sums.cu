@@ -4,6 +4,7 @@
 #include <cmath>
 #include <vector>
 
+#include "bve_x2.cuh"
 #include "engine.cuh"
 #include "ops.cuh"
 #include "sums.cuh"
@@ -37,7 +38,9 @@ __global__ void __launch_bounds__(k64Threads) seq_fp64_kernel(P p, const Rec* __
   typename Op::Acc acc{};
   const int64_t n_tiles = ceil_div(ns, k64Tile);
   int64_t tile = 0;
-  staged_sweep<Rec, k64Tile>(src, 0, n_tiles, stage[0], stage[1], bars, status,
+  pipe_init(bars);
+  uint32_t g = 0;
+  staged_sweep<Rec, k64Tile>(src, 0, n_tiles, stage[0], stage[1], bars, g, status,
                              [&](const Rec* tl) {
                                const int64_t j0 = tile * k64Tile;
                                const int cnt = static_cast<int>(ns - j0 < k64Tile ? ns - j0 : k64Tile);
@@ -104,37 +107,6 @@ __global__ void prep_stream64_kernel(const double* x, const double* y, const dou
   r.area = area[j];
   r.idx = j;
   r.pad = 0;
-  out[k] = r;
-}
-
-// S_j = -zeta_j A_j / (2 pi a); position scaled by 1/a and split hi/lo; -c_j = 1 - |p_j|^2
-__global__ void prep_bve32_kernel(const double* x, const double* y, const double* z,
-                                  const double* zeta, const double* area, const int32_t* idx,
-                                  int64_t ns, int64_t npad, double inv_a, double s_scale,
-                                  BveF32::Rec* out) {
-  const int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (k >= npad) return;
-  BveF32::Rec r;
-  if (k < ns) {
-    const int64_t j = idx[k];
-    const double px = x[j] * inv_a, py = y[j] * inv_a, pz = z[j] * inv_a;
-    float h, l;
-    split2(px, h, l);
-    r.a.x = h;
-    r.b.y = l;
-    split2(py, h, l);
-    r.a.y = h;
-    r.b.z = l;
-    split2(pz, h, l);
-    r.a.z = h;
-    r.b.w = l;
-    r.a.w = __double2float_rn(-fma(px, px, fma(py, py, fma(pz, pz, -1.0))));
-    r.b.x = __double2float_rn(zeta[j] * area[j] * s_scale);
-  } else {
-    // inert: at the origin with zero strength (q = |p_i|^2 - c_i = 1 > 0, weight 0)
-    r.a = make_float4(0.f, 0.f, 0.f, 0.f);
-    r.b = make_float4(0.f, 0.f, 0.f, 0.f);
-  }
   out[k] = r;
 }
 
@@ -275,7 +247,7 @@ size_t rec_bytes(int kind, int mode) {
   switch (kind) {
     case kSumBve:
     case kSumBveMesh:
-      return sizeof(BveF32::Rec);
+      return sizeof(BveX2::Rec);
     case kSumPlane:
       return sizeof(PlaneF32::Rec);
     default:
@@ -419,11 +391,21 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
     case kSumBve:
     case kSumBveMesh: {
       const double inv_a = 1.0 / job.radius;
-      prep_bve32_kernel<<<prep_grid_pad, pb, 0, job.stream>>>(
+      prep_bve_x2_kernel<<<prep_grid_pad, pb, 0, job.stream>>>(
           job.x, job.y, job.z, job.s1, job.area, job.src_idx, job.ns, npad, inv_a,
-          -1.0 / (2.0 * kPi * job.radius), static_cast<BveF32::Rec*>(job.src_buf));
-      BveF32::Params p{job.x, job.y, job.z, inv_a};
-      launch_sweep<BveF32, kBveThreads, kBveTpt, kBveTile, kBveMinB>(job, plan, p);
+          -1.0 / (2.0 * kPi * job.radius), static_cast<BveX2::Rec*>(job.src_buf));
+      SweepArgs<BveF32> a;
+      a.p = BveF32::Params{job.x, job.y, job.z, inv_a};
+      a.src = reinterpret_cast<const BveF32::Rec*>(job.src_buf);
+      a.n_tiles = plan.n_tiles;
+      a.tiles_per_chunk = plan.tiles_per_chunk;
+      a.ib = job.ib;
+      a.nt = job.nt;
+      a.partial = job.partial;
+      a.status = job.status;
+      const dim3 grid(static_cast<unsigned>(ceil_div(job.nt, kBveThreads * kBveTpt)),
+                      static_cast<unsigned>(plan.nsplit));
+      bve_sweep_x2_kernel<kBveThreads, kBveTpt, kBveTile, kBveMinB><<<grid, kBveThreads, 0, job.stream>>>(a);
       finish_bve_kernel<<<fin_grid, pb, 0, job.stream>>>(job.partial, plan.nsplit, job.nt, job.ib, job.x,
                                                          job.y, job.z, inv_a, job.out0, job.out1, job.out2);
       break;

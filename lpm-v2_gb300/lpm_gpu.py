@@ -73,14 +73,17 @@ _SIGNATURES = {
     "lpm_bve_set_state": [_vp, _D, _D, _D, _D, _D, _D, _D],
     "lpm_bve_diagnostics": [_vp, _D, _D, _D],
     "lpm_bve_kernel_timing": [_vp, _D, _L],
+    "lpm_bve_solver_set_stream": [_vp, _vp],
+    "lpm_bve_solver_set_timing": [_vp, _int],
     "lpm_bve_solver_destroy": [_vp],
+    "lpm_measure_fp32_peak": [_dbl, _D],
     "lpm_plane_solver_create": [_pvp, _i64, _D, _D, _D, _D, _I, _D, _D, _dbl, _int],
     "lpm_plane_timestep": [_vp, _dbl, _int],
     "lpm_plane_get_state": [_vp, _D, _D, _D, _D],
     "lpm_plane_diagnostics": [_vp, _D, _D, _D],
     "lpm_plane_solver_destroy": [_vp],
     "lpm_ensemble_create": [_pvp, _int, _L, _D, _D, _D, _D, _D, _I, _D, _D, _int],
-    "lpm_ensemble_timestep": [_vp, _dbl, _int],
+    "lpm_ensemble_timestep": [_vp, _dbl, _int, _int],
     "lpm_ensemble_velocity": [_vp],
     "lpm_ensemble_get_state": [_vp, _D, _D, _D, _D, _D, _D, _D],
     "lpm_ensemble_kernel_timing": [_vp, _D, _L],
@@ -301,6 +304,14 @@ class BVESolver:
         _check(lib().lpm_bve_kernel_timing(self._h, ctypes.byref(ms), ctypes.byref(n)))
         return ms.value, n.value
 
+    def set_timing(self, enable: bool):
+        """True (default): synchronise after each step to accumulate kernel timing."""
+        _check(lib().lpm_bve_solver_set_timing(self._h, 1 if enable else 0))
+
+    def set_stream(self, stream_handle: int | None):
+        """Enqueue the solver's work on a caller's cudaStream_t (an integer handle)."""
+        _check(lib().lpm_bve_solver_set_stream(self._h, ctypes.c_void_p(stream_handle or None)))
+
     def close(self):
         if getattr(self, "_h", None):
             lib().lpm_bve_solver_destroy(self._h)
@@ -374,8 +385,8 @@ class Ensemble:
         self._h = h
         self.n = int(offs[-1])
 
-    def timestep(self, dt, n_steps=1):
-        _check(lib().lpm_ensemble_timestep(self._h, float(dt), int(n_steps)))
+    def timestep(self, dt, n_steps=1, renormalize=False):
+        _check(lib().lpm_ensemble_timestep(self._h, float(dt), int(n_steps), 1 if renormalize else 0))
 
     def velocity(self):
         _check(lib().lpm_ensemble_velocity(self._h))
@@ -400,6 +411,13 @@ class Ensemble:
             self.close()
         except Exception:
             pass
+
+
+def measure_fp32_peak(ms_target: float = 200.0) -> float:
+    """Measured FP32 FMA throughput of the current GPU in TFLOP/s."""
+    t = _dbl()
+    _check(lib().lpm_measure_fp32_peak(float(ms_target), ctypes.byref(t)))
+    return t.value
 
 
 # ------------------------------------------------------------------ meshes
