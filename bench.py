@@ -330,10 +330,10 @@ def run_ours(args):
                        "dt": args.dt, "l2": "flushed between steps (256 MB write, outside the timed events)",
                        "parallelism": f"replicas x{world}"},
             "clocks": clocks,
-            "gpu_launches": (k_n1 - k_n0) + 4 * args.steps,
+            "gpu_launches": k_n1 - k_n0,
             "roofline": {"bound": "fp32", "achieved": achieved_tflops, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved_tflops / peak, "traffic": None,
-                         "kernel": "sweep_fp32c_kernel<BveF32> (+prep, finish) per velocity sum",
+                         "kernel": "bve_rel_sweep_kernel (+ its prep and finish kernels) per velocity sum",
                          "ms_per_launch": sum_ms, "flops_per_interaction": FLOPS_PER_INTERACTION,
                          "peak_source": "measured in-process FFMA loop (lpm_measure_fp32_peak)"},
             "accuracy": {"velocity_rel_linf_vs_fp64": rel_linf, "velocity_rel_l2_vs_fp64": rel_l2,

@@ -145,8 +145,9 @@ int lpm_bve_set_state(lpm_bve_solver* solver, const double* x, const double* y,
  * active particles (src/SphereBVE.f90:410-441). */
 int lpm_bve_diagnostics(lpm_bve_solver* solver, double* kinetic_energy, double* enstrophy,
                         double* circulation);
-/* Accumulated device time of the velocity-sum kernels launched by lpm_bve_timestep,
- * measured with CUDA events on the solver's stream, and the number of such launches. */
+/* Accumulated device time of the velocity sums launched by lpm_bve_timestep, measured
+ * with CUDA events on the solver's stream, and the number of kernels lpm_bve_timestep has
+ * launched (stage kernels, direct sums and the per-step source sort). */
 int lpm_bve_kernel_timing(lpm_bve_solver* solver, double* total_ms, int64_t* launches);
 /* Makes the solver enqueue its work on `stream` (a cudaStream_t of the caller's context;
  * NULL restores the solver's own stream), so the caller can time it with events. */

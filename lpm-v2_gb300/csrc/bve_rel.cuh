@@ -1,0 +1,289 @@
+// bve_rel.cuh -- the sphere-BVE FP32C sweep on spatially sorted sources in tile-relative
+// coordinates (11 packed FP32x2 operations per target pair and source).
+//
+// Sources are Morton-ordered, so a tile of TILE sources covers a small patch of the sphere.
+// Each source is stored relative to an origin o of its tile as a two-float offset
+// (s_hi, s_lo) = rel2(p, o); once per tile every target forms its own offset (t_hi, t_lo)
+// with exactly the same operations, so a self pair cancels bit for bit.  The prep kernel
+// picks o and a precision per tile:
+//  - compact tile (radius R about its centroid <= a/8 and <= 64 x the smallest spacing of
+//    consecutive sources in the tile): o = centroid and the pair difference is
+//    d = t_hi - s_hi, one subtraction per component.  Its rounding error is ~2^-23 R, so
+//    the velocity error is ~1e-7 R sum_j S_j/|d_j|^2 / |u|, about 1e-7 relative when R <= a/8
+//    on a quasi-uniform point set; the spacing guard sends clustered sets to the wide path;
+//  - wide tile (sparse or clustered points): o = 0, so (s_hi, s_lo) are the absolute hi/lo
+//    parts and d = (t_hi - s_hi) + (t_lo - s_lo) keeps ~48 bits for near pairs.
+// Then  q = |d|^2 - c_i - c_j,  w = S_j / q,  D += w d  with c = |p|^2 - 1 and
+// S_j = -zeta_j A_j / (2 pi a) as in BveF32; u = D x p_i in FP64.  A compact tile costs
+// 11 packed FP32x2 operations per target pair and source, a wide one 17.
+// Targets keep their original order (only sources are sorted), so no scatter is needed.
+#pragma once
+
+#include "bve_x2.cuh"
+#include "engine.cuh"
+#include "ops.cuh"
+
+namespace lpm {
+
+struct BveRel {
+  struct __align__(16) Rec {
+    float4 a;  // -sx_hi, -sx_hi, -sy_hi, -sy_hi
+    float4 b;  // -sz_hi, -sz_hi, -c_j, -c_j
+    float4 c;  // S_j, S_j, -sz_lo, -sz_lo
+    float4 d;  // -sx_lo, -sx_lo, -sy_lo, -sy_lo
+  };
+  struct __align__(16) Origin {
+    float4 hi;  // o_hi.x, o_hi.y, o_hi.z, 1 if the tile is wide
+    float4 lo;  // o_lo.x, o_lo.y, o_lo.z, 0
+  };
+  static constexpr float kCompactRadius = 0.125f;  // on the unit sphere
+  static constexpr float kCompactRatio = 64.0f;
+};
+
+// Two-float offset of a hi/lo value from a hi/lo origin: (r_hi, r_lo) with r_hi + r_lo ~ p - o.
+__device__ __forceinline__ void rel2(float ph, float pl, float oh, float ol, float& rh, float& rl) {
+  const float a = __fadd_rn(ph, -oh);
+  const float b = __fadd_rn(pl, -ol);
+  rh = __fadd_rn(a, b);
+  rl = __fadd_rn(__fadd_rn(a, -rh), b);
+}
+
+__device__ __forceinline__ void rel2x2(float2 ph, float2 pl, float oh, float ol, float2& rh, float2& rl) {
+  const float2 a = __fadd2_rn(ph, make_float2(-oh, -oh));
+  const float2 b = __fadd2_rn(pl, make_float2(-ol, -ol));
+  rh = __fadd2_rn(a, b);
+  rl = __fadd2_rn(__fadd2_rn(a, make_float2(-rh.x, -rh.y)), b);
+}
+
+template <int THREADS, int TPT, int TILE, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB) bve_rel_sweep_kernel(SweepArgs<BveF32> a,
+                                                                      const BveRel::Origin* __restrict__ org) {
+  static_assert(TPT % 2 == 0, "targets come in pairs");
+  constexpr int NP = TPT / 2;
+  using Rec = BveRel::Rec;
+  __shared__ __align__(128) Rec stage[2][TILE];
+  __shared__ __align__(8) uint64_t bars[2];
+
+  const int64_t chunk = blockIdx.y;
+  const int64_t tile0 = chunk * a.tiles_per_chunk;
+  int64_t ntl = a.n_tiles - tile0;
+  if (ntl > a.tiles_per_chunk) ntl = a.tiles_per_chunk;
+  if (ntl < 0) ntl = 0;
+
+  BveX2::Pair pr[NP];
+  float2 hx[NP], hy[NP], hz[NP], lx[NP], ly[NP], lz[NP];
+  const int64_t base = static_cast<int64_t>(blockIdx.x) * (THREADS * TPT) + threadIdx.x;
+#pragma unroll
+  for (int p = 0; p < NP; ++p) {
+    int64_t i0 = base + (2 * p) * THREADS, i1 = base + (2 * p + 1) * THREADS;
+    if (i0 >= a.nt) i0 = a.nt - 1;  // duplicates of a valid target; results not stored
+    if (i1 >= a.nt) i1 = a.nt - 1;
+    const BveF32::Tgt t0 = BveF32::load_target(a.p, a.ib + i0);
+    const BveF32::Tgt t1 = BveF32::load_target(a.p, a.ib + i1);
+    pr[p].xh = make_float2(t0.xh, t1.xh);
+    pr[p].yh = make_float2(t0.yh, t1.yh);
+    pr[p].zh = make_float2(t0.zh, t1.zh);
+    pr[p].xl = make_float2(t0.xl, t1.xl);
+    pr[p].yl = make_float2(t0.yl, t1.yl);
+    pr[p].zl = make_float2(t0.zl, t1.zl);
+    pr[p].nc = make_float2(t0.nc, t1.nc);
+    hx[p] = hy[p] = hz[p] = lx[p] = ly[p] = lz[p] = make_float2(0.f, 0.f);
+  }
+
+  pipe_init(bars);
+  uint32_t g = 0;
+  int64_t tile = tile0;
+  const Rec* src = reinterpret_cast<const Rec*>(a.src);
+  staged_sweep<Rec, TILE>(src, tile0, ntl, stage[0], stage[1], bars, g, a.status, [&](const Rec* tl) {
+    const BveRel::Origin o = org[tile];
+    ++tile;
+    float2 ax[NP], ay[NP], az[NP];
+#pragma unroll
+    for (int p = 0; p < NP; ++p) ax[p] = ay[p] = az[p] = make_float2(0.f, 0.f);
+    if (o.hi.w == 0.f) {
+      // compact tile: d = t_hi - s_hi
+      float2 tx[NP], ty[NP], tz[NP], unused;
+#pragma unroll
+      for (int p = 0; p < NP; ++p) {
+        rel2x2(pr[p].xh, pr[p].xl, o.hi.x, o.lo.x, tx[p], unused);
+        rel2x2(pr[p].yh, pr[p].yl, o.hi.y, o.lo.y, ty[p], unused);
+        rel2x2(pr[p].zh, pr[p].zl, o.hi.z, o.lo.z, tz[p], unused);
+      }
+#pragma unroll 2
+      for (int j = 0; j < TILE; ++j) {
+        const float4 ra = tl[j].a, rb = tl[j].b, rc = tl[j].c;
+        const float2 nsx = lo2(ra), nsy = hi2(ra), nsz = lo2(rb), ncj = hi2(rb), s2 = lo2(rc);
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+          const float2 dx = __fadd2_rn(tx[p], nsx);
+          const float2 dy = __fadd2_rn(ty[p], nsy);
+          const float2 dz = __fadd2_rn(tz[p], nsz);
+          float2 q = __fadd2_rn(pr[p].nc, ncj);
+          q = __ffma2_rn(dx, dx, q);
+          q = __ffma2_rn(dy, dy, q);
+          q = __ffma2_rn(dz, dz, q);
+          const float2 inv = make_float2(rcp_approx(q.x), rcp_approx(q.y));
+          const float2 wgt = __fmul2_rn(s2, inv);
+          ax[p] = __ffma2_rn(wgt, dx, ax[p]);
+          ay[p] = __ffma2_rn(wgt, dy, ay[p]);
+          az[p] = __ffma2_rn(wgt, dz, az[p]);
+        }
+      }
+    } else {
+      // wide tile (o = 0): d = (t_hi - s_hi) + (t_lo - s_lo)
+      float2 txh[NP], tyh[NP], tzh[NP], txl[NP], tyl[NP], tzl[NP];
+#pragma unroll
+      for (int p = 0; p < NP; ++p) {
+        rel2x2(pr[p].xh, pr[p].xl, o.hi.x, o.lo.x, txh[p], txl[p]);
+        rel2x2(pr[p].yh, pr[p].yl, o.hi.y, o.lo.y, tyh[p], tyl[p]);
+        rel2x2(pr[p].zh, pr[p].zl, o.hi.z, o.lo.z, tzh[p], tzl[p]);
+      }
+      for (int j = 0; j < TILE; ++j) {
+        const float4 ra = tl[j].a, rb = tl[j].b, rc = tl[j].c, rd = tl[j].d;
+        const float2 nsx = lo2(ra), nsy = hi2(ra), nsz = lo2(rb), ncj = hi2(rb), s2 = lo2(rc);
+        const float2 nlx = lo2(rd), nly = hi2(rd), nlz = hi2(rc);
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+          const float2 dx = __fadd2_rn(__fadd2_rn(txh[p], nsx), __fadd2_rn(txl[p], nlx));
+          const float2 dy = __fadd2_rn(__fadd2_rn(tyh[p], nsy), __fadd2_rn(tyl[p], nly));
+          const float2 dz = __fadd2_rn(__fadd2_rn(tzh[p], nsz), __fadd2_rn(tzl[p], nlz));
+          float2 q = __fadd2_rn(pr[p].nc, ncj);
+          q = __ffma2_rn(dx, dx, q);
+          q = __ffma2_rn(dy, dy, q);
+          q = __ffma2_rn(dz, dz, q);
+          const float2 inv = make_float2(rcp_approx(q.x), rcp_approx(q.y));
+          const float2 wgt = __fmul2_rn(s2, inv);
+          ax[p] = __ffma2_rn(wgt, dx, ax[p]);
+          ay[p] = __ffma2_rn(wgt, dy, ay[p]);
+          az[p] = __ffma2_rn(wgt, dz, az[p]);
+        }
+      }
+    }
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+      comp_add(hx[p].x, lx[p].x, ax[p].x);
+      comp_add(hx[p].y, lx[p].y, ax[p].y);
+      comp_add(hy[p].x, ly[p].x, ay[p].x);
+      comp_add(hy[p].y, ly[p].y, ay[p].y);
+      comp_add(hz[p].x, lz[p].x, az[p].x);
+      comp_add(hz[p].y, lz[p].y, az[p].y);
+    }
+  });
+
+#pragma unroll
+  for (int p = 0; p < NP; ++p) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int64_t il = base + (2 * p + h) * THREADS;
+      if (il < a.nt) {
+        const float vx = h ? hx[p].y : hx[p].x, ex = h ? lx[p].y : lx[p].x;
+        const float vy = h ? hy[p].y : hy[p].x, ey = h ? ly[p].y : ly[p].x;
+        const float vz = h ? hz[p].y : hz[p].x, ez = h ? lz[p].y : lz[p].x;
+        a.partial[(chunk * 3 + 0) * a.nt + il] = static_cast<double>(vx) + static_cast<double>(ex);
+        a.partial[(chunk * 3 + 1) * a.nt + il] = static_cast<double>(vy) + static_cast<double>(ey);
+        a.partial[(chunk * 3 + 2) * a.nt + il] = static_cast<double>(vz) + static_cast<double>(ez);
+      }
+    }
+  }
+}
+
+// Tile-relative source records from the Morton-sorted source list `sorted` (ns entries,
+// records ns..npad-1 inert) and the per-tile origins.  One CTA of TILE threads per tile:
+// the CTA reduces the tile's centroid, its radius about the centroid and the smallest
+// distance between consecutive sources, picks compact (o = centroid) or wide (o = 0), and
+// writes every record as rel2(p_j, o) -- the same operations the sweep uses for targets.
+template <int TILE>
+__global__ void __launch_bounds__(TILE) bve_rel_prep_kernel(const double* x, const double* y, const double* z,
+                                                            const double* zeta, const double* area,
+                                                            const int32_t* sorted, int64_t ns, double inv_a,
+                                                            double s_scale, BveRel::Rec* out, BveRel::Origin* org) {
+  __shared__ double sp[3][TILE];
+  __shared__ double red[3][TILE];
+  __shared__ float fmax_[TILE], fmin_[TILE];
+  const int tid = threadIdx.x;
+  const int64_t t = blockIdx.x;
+  const int64_t k = t * TILE + tid;
+  const bool valid = k < ns;
+  double px = 0.0, py = 0.0, pz = 0.0;
+  int32_t j = 0;
+  if (valid) {
+    j = sorted[k];
+    px = x[j] * inv_a;
+    py = y[j] * inv_a;
+    pz = z[j] * inv_a;
+  }
+  sp[0][tid] = px;
+  sp[1][tid] = py;
+  sp[2][tid] = pz;
+  red[0][tid] = px;
+  red[1][tid] = py;
+  red[2][tid] = pz;
+  __syncthreads();
+  for (int w = TILE / 2; w > 0; w >>= 1) {
+    if (tid < w) {
+      red[0][tid] += red[0][tid + w];
+      red[1][tid] += red[1][tid + w];
+      red[2][tid] += red[2][tid + w];
+    }
+    __syncthreads();
+  }
+  const int64_t cnt64 = ns - t * TILE;
+  const double cnt = static_cast<double>(cnt64 < TILE ? cnt64 : TILE);
+  const double cx = red[0][0] / cnt, cy = red[1][0] / cnt, cz = red[2][0] / cnt;
+  // radius about the centroid and the smallest spacing of consecutive sources
+  float rad = 0.f, spc = 3.4e38f;
+  if (valid) {
+    const double dx = px - cx, dy = py - cy, dz = pz - cz;
+    rad = static_cast<float>(sqrt(dx * dx + dy * dy + dz * dz));
+    if (tid > 0) {
+      const double ex = px - sp[0][tid - 1], ey = py - sp[1][tid - 1], ez = pz - sp[2][tid - 1];
+      spc = static_cast<float>(sqrt(ex * ex + ey * ey + ez * ez));
+    }
+  }
+  fmax_[tid] = rad;
+  fmin_[tid] = spc;
+  __syncthreads();
+  for (int w = TILE / 2; w > 0; w >>= 1) {
+    if (tid < w) {
+      fmax_[tid] = fmaxf(fmax_[tid], fmax_[tid + w]);
+      fmin_[tid] = fminf(fmin_[tid], fmin_[tid + w]);
+    }
+    __syncthreads();
+  }
+  const bool wide = !(fmax_[0] <= BveRel::kCompactRadius && fmax_[0] <= BveRel::kCompactRatio * fmin_[0]);
+  float oxh = 0.f, oxl = 0.f, oyh = 0.f, oyl = 0.f, ozh = 0.f, ozl = 0.f;
+  if (!wide) {
+    split2(cx, oxh, oxl);
+    split2(cy, oyh, oyl);
+    split2(cz, ozh, ozl);
+  }
+  BveRel::Rec r;
+  if (valid) {
+    float h, l, sxh, sxl, syh, syl, szh, szl;
+    split2(px, h, l);
+    rel2(h, l, oxh, oxl, sxh, sxl);
+    split2(py, h, l);
+    rel2(h, l, oyh, oyl, syh, syl);
+    split2(pz, h, l);
+    rel2(h, l, ozh, ozl, szh, szl);
+    const float nc = __double2float_rn(-fma(px, px, fma(py, py, fma(pz, pz, -1.0))));
+    const float s = __double2float_rn(zeta[j] * area[j] * s_scale);
+    r.a = make_float4(-sxh, -sxh, -syh, -syh);
+    r.b = make_float4(-szh, -szh, nc, nc);
+    r.c = make_float4(s, s, -szl, -szl);
+    r.d = make_float4(-sxl, -sxl, -syl, -syl);
+  } else {
+    // inert: at the origin with zero strength and zero -c (weight 0 times a finite
+    // difference; q > 0 through the target's 2^-100 offset when the target sits on o)
+    r.a = r.b = r.c = r.d = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  out[k] = r;
+  if (tid == 0) {
+    BveRel::Origin o;
+    o.hi = make_float4(oxh, oyh, ozh, wide ? 1.f : 0.f);
+    o.lo = make_float4(oxl, oyl, ozl, 0.f);
+    org[t] = o;
+  }
+}
+
+}  // namespace lpm

@@ -13,6 +13,7 @@
 
 #include "lpm_common.cuh"
 #include "solver.cuh"
+#include "sort.cuh"
 #include "sums.cuh"
 
 namespace lpm {
@@ -265,6 +266,14 @@ struct lpm_bve_solver {
   double kernel_ms = 0.0;
   int64_t kernel_launches = 0;
   bool timing = true;
+  // FP32C: Morton order of the sources, refreshed at the start of every step
+  void* sort_scratch = nullptr;
+  size_t sort_bytes = 0;
+  int32_t* sorted = nullptr;
+
+  int sort_sources() {
+    return morton_sort(stream, ns, idx, x, y, z, 1.0 / radius, sort_scratch, sort_bytes, sorted);
+  }
 
   SumJob job(const double* px, const double* py, const double* pz, const double* pq, int kind,
              double* o0, double* o1, double* o2) const {
@@ -277,7 +286,7 @@ struct lpm_bve_solver {
     j.z = pz;
     j.s1 = pq;
     j.area = area;
-    j.src_idx = idx;
+    j.src_idx = sorted ? sorted : idx;
     j.ns = ns;
     j.radius = radius;
     j.ib = 0;
@@ -305,6 +314,7 @@ struct lpm_bve_solver {
 
   int enqueue_step(double dt, int renorm, bool with_events) {
     const unsigned g = static_cast<unsigned>(ceil_div(n, kStageThreads));
+    if (sorted) LPM_TRY(sort_sources());
     const double two_dt_omega = (dt * 2.0) * omega;  // (dt*2)*Omega, as the Fortran associates it
     bve_stage1_kernel<<<g, kStageThreads, 0, stream>>>(n, renorm, dt, two_dt_omega, radius, x, y, z, q, u, v, w, ax,
                                                        ay, az, aq, xin, yin, zin, qin);
@@ -430,6 +440,16 @@ int bve_create(lpm_bve_solver* S, int64_t n, const double* x, const double* y, c
   LPM_TRY(upload(S->stream, S->z, z, n));
   LPM_TRY(upload(S->stream, S->q, q, n));
   LPM_TRY(upload(S->stream, S->area, area, n));
+  if (S->ns > 0 && sum_uses_sorted_sources(kSumBve, mode)) {
+    // FP32C: the sources are ordered spatially at the start of every step (inside the step's
+    // graph), so tiles stay compact as the particles move; the order only affects rounding
+    S->sort_bytes = morton_sort_bytes(S->ns);
+    void* sorted = nullptr;
+    LPM_TRY(S->arena.alloc(S->sort_bytes, &S->sort_scratch));
+    LPM_TRY(S->arena.alloc(S->ns * sizeof(int32_t), &sorted));
+    S->sorted = static_cast<int32_t*>(sorted);
+    LPM_TRY(S->sort_sources());
+  }
   for (auto& e : S->ev) LPM_CUDA_TRY(cudaEventCreate(&e));
   if (u && v && w) {
     LPM_TRY(upload(S->stream, S->u, u, n));
@@ -475,7 +495,9 @@ extern "C" int lpm_bve_timestep(lpm_bve_solver* S, double dt, int n_steps, int r
   if (!S->exec || S->graph_dt != dt || S->graph_renorm != renorm) LPM_TRY(S->capture(dt, renorm));
   for (int s = 0; s < n_steps; ++s) {
     LPM_CUDA_TRY(cudaGraphLaunch(S->exec, S->stream));
-    S->kernel_launches += 4 * (S->ns ? kernels_per_sum(S->mode) : 0);
+    // 4 stage kernels, 4 direct sums, and the Morton sort of the sources (FP32C: one key
+    // kernel and the six kernels of the CUB radix sort over 30-bit keys)
+    S->kernel_launches += 4 + 4 * (S->ns ? kernels_per_sum(S->mode) : 0) + (S->sorted ? 7 : 0);
     if (!S->timing) continue;
     LPM_TRY(S->check_status("lpm_bve_timestep"));
     for (int k = 0; k < 4; ++k) {

@@ -4,9 +4,11 @@
 #include <cmath>
 #include <vector>
 
+#include "bve_rel.cuh"
 #include "bve_x2.cuh"
 #include "engine.cuh"
 #include "ops.cuh"
+#include "sort.cuh"
 #include "sums.cuh"
 
 namespace lpm {
@@ -247,7 +249,7 @@ size_t rec_bytes(int kind, int mode) {
   switch (kind) {
     case kSumBve:
     case kSumBveMesh:
-      return sizeof(BveX2::Rec);
+      return sizeof(BveRel::Rec);
     case kSumPlane:
       return sizeof(PlaneF32::Rec);
     default:
@@ -283,11 +285,19 @@ int targets_per_cta(int kind) {
 
 int kernels_per_sum(int mode) { return mode == LPM_MODE_FP64 ? 2 : 3; }
 
+bool sum_uses_sorted_sources(int kind, int mode) {
+  return mode == LPM_MODE_FP32C && (kind == kSumBve || kind == kSumBveMesh);
+}
+
 SumPlan plan_sum(int kind, int mode, int64_t ns, int64_t nt, int sm_count) {
   SumPlan pl;
   const int tile = tile_of(kind, mode);
   pl.n_tiles = ceil_div(ns > 0 ? ns : 1, tile);
   pl.src_bytes = static_cast<size_t>(pl.n_tiles) * tile * rec_bytes(kind, mode);
+  if (sum_uses_sorted_sources(kind, mode)) {
+    // the per-tile origins follow the records
+    pl.src_bytes = align_up(pl.src_bytes, 256) + static_cast<size_t>(pl.n_tiles) * sizeof(BveRel::Origin);
+  }
   if (mode == LPM_MODE_FP64) {
     pl.nsplit = 1;
     pl.tiles_per_chunk = pl.n_tiles;
@@ -391,9 +401,18 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
     case kSumBve:
     case kSumBveMesh: {
       const double inv_a = 1.0 / job.radius;
-      prep_bve_x2_kernel<<<prep_grid_pad, pb, 0, job.stream>>>(
-          job.x, job.y, job.z, job.s1, job.area, job.src_idx, job.ns, npad, inv_a,
-          -1.0 / (2.0 * kPi * job.radius), static_cast<BveX2::Rec*>(job.src_buf));
+      const int32_t* src_list = job.src_idx;
+      if (job.sort_scratch) {
+        LPM_TRY(morton_sort(job.stream, job.ns, job.src_idx, job.x, job.y, job.z, inv_a, job.sort_scratch,
+                            job.sort_bytes, job.sorted));
+        src_list = job.sorted;
+      }
+      BveRel::Rec* recs = static_cast<BveRel::Rec*>(job.src_buf);
+      BveRel::Origin* org = reinterpret_cast<BveRel::Origin*>(
+          static_cast<char*>(job.src_buf) + align_up(static_cast<size_t>(npad) * sizeof(BveRel::Rec), 256));
+      bve_rel_prep_kernel<kBveTile><<<static_cast<unsigned>(plan.n_tiles), kBveTile, 0, job.stream>>>(
+          job.x, job.y, job.z, job.s1, job.area, src_list, job.ns, inv_a, -1.0 / (2.0 * kPi * job.radius), recs,
+          org);
       SweepArgs<BveF32> a;
       a.p = BveF32::Params{job.x, job.y, job.z, inv_a};
       a.src = reinterpret_cast<const BveF32::Rec*>(job.src_buf);
@@ -405,7 +424,7 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
       a.status = job.status;
       const dim3 grid(static_cast<unsigned>(ceil_div(job.nt, kBveThreads * kBveTpt)),
                       static_cast<unsigned>(plan.nsplit));
-      bve_sweep_x2_kernel<kBveThreads, kBveTpt, kBveTile, kBveMinB><<<grid, kBveThreads, 0, job.stream>>>(a);
+      bve_rel_sweep_kernel<kBveThreads, kBveTpt, kBveTile, kBveMinB><<<grid, kBveThreads, 0, job.stream>>>(a, org);
       finish_bve_kernel<<<fin_grid, pb, 0, job.stream>>>(job.partial, plan.nsplit, job.nt, job.ib, job.x,
                                                          job.y, job.z, inv_a, job.out0, job.out1, job.out2);
       break;
@@ -563,6 +582,15 @@ int run_host(const HostArgs& a, int nout) {
     job.out1 = nout > 1 ? dout + nt : nullptr;
     job.out2 = nout > 2 ? dout + 2 * nt : nullptr;
     LPM_TRY(workspace(ctx, kWsSources, plan.src_bytes, &job.src_buf));
+    if (sum_uses_sorted_sources(a.kind, prec)) {
+      void* ps = nullptr;
+      const size_t sb = morton_sort_bytes(ns);
+      const size_t sorted_off = align_up(sb, 256);
+      LPM_TRY(workspace(ctx, kWsScan, sorted_off + static_cast<size_t>(ns) * sizeof(int32_t), &ps));
+      job.sort_scratch = ps;
+      job.sort_bytes = sb;
+      job.sorted = reinterpret_cast<int32_t*>(static_cast<char*>(ps) + sorted_off);
+    }
     if (plan.partial_bytes) {
       void* pp = nullptr;
       LPM_TRY(workspace(ctx, kWsPartial, plan.partial_bytes, &pp));

