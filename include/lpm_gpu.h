@@ -191,6 +191,28 @@ int lpm_ensemble_get_state(lpm_ensemble* ens, double* x, double* y, double* z,
 int lpm_ensemble_kernel_timing(lpm_ensemble* ens, double* total_ms, int64_t* launches);
 int lpm_ensemble_destroy(lpm_ensemble* ens);
 
+/* ------------------------------------------------------------------ allocation-free call */
+
+/* lpm_bve_velocity_noalloc has no counterpart in the reference.  It is for callers that
+ * cannot allocate device memory while they run: a host code whose own pool allocator
+ * already holds the GPU's memory, or a time loop that cannot pay the device-wide
+ * synchronisation cudaMalloc/cudaFree may cause.  Every input and output is a DEVICE
+ * pointer owned by the caller (same meaning as lpm_bve_velocity, 1-based i_begin..i_end,
+ * outputs outside the block untouched); the call computes the LPM_MODE_FP32C sum and
+ * allocates nothing -- no cudaMalloc, cudaFree or allocating library routine.  Its scratch
+ * is one array the library reserves on every GPU that loads it (about 24 MiB, held until
+ * the process exits), which limits n to LPM_NOALLOC_MAX_PARTICLES; larger n fails with
+ * LPM_ERR_ARG.  The first call on a device looks up that array's device address, so make
+ * it before any stream capture.  All calls on a device share the array: calls that overlap
+ * on the GPU (several host threads or streams) race, so serialise them.  Work is enqueued
+ * on `stream` (a cudaStream_t, NULL for the default stream) and the call returns after the
+ * stream has finished it. */
+#define LPM_NOALLOC_MAX_PARTICLES 262144
+int lpm_bve_velocity_noalloc(int64_t n, const double* x, const double* y, const double* z,
+                             const double* zeta, const double* area, const int32_t* active,
+                             double radius, int64_t i_begin, int64_t i_end, double* u,
+                             double* v, double* w, void* stream);
+
 /* ------------------------------------------------------------------ calibration */
 
 /* Runs a fused multiply-add throughput loop on every SM for about `ms_target` ms and
