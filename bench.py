@@ -47,6 +47,9 @@ METRIC = "BVE direct-sum Ginteractions/s, FP32-comp vs FP64 on GB300 at <=1e-6 r
 UNIT = "Ginteractions/s"
 FLOPS_PER_INTERACTION = 24  # dot 5, a^2-dot 1, x4pi a 1, zeta A/den 2, cross 9, accumulate 6
 L2_FLUSH_BYTES = 256 << 20
+# DRAM bytes (read + write) of one full-size sweep launch, from the ncu capture recorded in
+# profiles/bve_rel_sweep_icos8_dram.md (ncu cannot run inside the timed benchmark)
+SWEEP_TRAFFIC_ICOS8 = 2_029_860_864 + 57_271_808
 
 
 def parse_args():
@@ -61,6 +64,9 @@ def parse_args():
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline sample budget")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--workload", choices=["rk4", "ensemble"], default="rk4",
+                   help="rk4: the headline single-instance step; ensemble: the 64-instance batch")
+    p.add_argument("--instances", type=int, default=64)
     return p.parse_args()
 
 
@@ -332,7 +338,9 @@ def run_ours(args):
             "clocks": clocks,
             "gpu_launches": k_n1 - k_n0,
             "roofline": {"bound": "fp32", "achieved": achieved_tflops, "peak": peak, "unit": "TFLOP/s",
-                         "frac": achieved_tflops / peak, "traffic": None,
+                         "frac": achieved_tflops / peak,
+                         "traffic": SWEEP_TRAFFIC_ICOS8 if args.nest == 8 else None,
+                         "traffic_unit": "bytes per launch (ncu, profiles/bve_rel_sweep_icos8_dram.md)",
                          "kernel": "bve_rel_sweep_kernel (+ its prep and finish kernels) per velocity sum",
                          "ms_per_launch": sum_ms, "flops_per_interaction": FLOPS_PER_INTERACTION,
                          "peak_source": "measured in-process FFMA loop (lpm_measure_fp32_peak)"},
@@ -351,10 +359,101 @@ def run_ours(args):
     return 0
 
 
+# ------------------------------------------------------------------ ensemble
+def run_ensemble(args):
+    """64 independent sphere-BVE instances at seeded random refinement levels 3-6 (Gaussian
+    vortices with random strength, width and centre, mean removed, Omega = 2 pi), FP32C,
+    advanced `steps` RK4 steps (dt = 0.01, projected stages) as one batch -- one persistent
+    launch per stage over a flattened work queue, one CUDA graph per step -- and, for
+    comparison, as the same instances on separate solvers, one after another."""
+    import torch
+    import lpm_gpu as lg
+    import workloads as wl
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    inst = wl.config_ensemble(n_instances=args.instances, seed=0)
+    steps = args.steps if args.steps != 5 else 50
+    inter_eval = sum(int(d["x"].size) * int(d["active"].sum()) - int(d["active"].sum()) for d in inst)
+    ens = lg.Ensemble(inst, mode="fp32c")
+    ens.timestep(args.dt, max(args.warmup, 3), renormalize=True)
+    sampler = ClockSampler(gpu_id_for(torch, local))
+    sampler.start()
+    torch.cuda.synchronize()
+    k0 = ens.kernel_timing()
+    t0 = time.perf_counter()
+    ens.timestep(args.dt, steps, renormalize=True)
+    torch.cuda.synchronize()
+    t_batch = time.perf_counter() - t0
+    k1 = ens.kernel_timing()
+    clocks = sampler.stop()
+    # per-instance velocity error of the batched FP32C sums against FP64 (8 instances,
+    # a block of up to 4096 targets each)
+    st = ens.get_state()
+    offs = ens.offsets
+    errs = []
+    for k in range(0, len(inst), max(1, len(inst) // 8)):
+        a, b = int(offs[k]), int(offs[k + 1])
+        d = inst[k]
+        m = min(4096, b - a)
+        sl = slice(a, b)
+        ref = lg.bve_sphere_velocity(st["x"][sl], st["y"][sl], st["z"][sl], st["rel_vort"][sl], d["area"], d["active"],
+                                     d["radius"], i_begin=1, i_end=m, mode="fp64")
+        got = np.stack([st[c][a:a + m] for c in ("u", "v", "w")])
+        r = np.stack([q[:m] for q in ref])
+        errs.append(float(np.abs(got - r).max() / np.abs(r).max()))
+    ens.close()
+    # the same instances, solver by solver (each replays its own graph back to back)
+    solvers = [lg.BVESolver(d["x"], d["y"], d["z"], d["rel_vort"], d["area"], d["active"], d["radius"],
+                            d["rotation_rate"], mode="fp32c") for d in inst]
+    for s_ in solvers:
+        s_.set_timing(False)
+        s_.timestep(args.dt, max(args.warmup, 3), renormalize=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for s_ in solvers:
+        s_.timestep(args.dt, steps, renormalize=True)
+    torch.cuda.synchronize()
+    t_seq = time.perf_counter() - t0
+    for s_ in solvers:
+        s_.close()
+    total = 4 * steps * inter_eval
+    value = total / t_batch / 1e9
+    nests = collections_counter([d["nest"] for d in inst])
+    line = {
+        "metric": "BVE ensemble Ginteractions/s (64 uneven instances, batched persistent launch)", "value": value,
+        "unit": UNIT, "n_gpus": 1, "steps": steps, "warmup": max(args.warmup, 3),
+        "ms_per_step": 1e3 * t_batch / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"{len(inst)} sphere-BVE instances, icosahedral nests {nests}, Gaussian vortices "
+                               "(shape U[2,8], strength U[2pi,6pi], random centre), dt 0.01, projected stages",
+                   "interactions_per_eval": inter_eval, "timing": "host wall clock around the step loop, "
+                   "device synchronised before and after (each step ends with a status check)"},
+        "clocks": clocks,
+        "sequential": {"value": total / t_seq / 1e9, "unit": UNIT, "ms_per_step": 1e3 * t_seq / steps,
+                       "how": "one BVESolver per instance, each replaying its step graph back to back"},
+        "speedup_vs_sequential": t_seq / t_batch,
+        "sum_kernel_ms_per_step": (k1[0] - k0[0]) / steps,
+        "gpu_launches": k1[1] - k0[1] + 4 * steps,
+        "accuracy": {"velocity_rel_linf_vs_fp64_max": max(errs), "instances_checked": len(errs)},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def collections_counter(values):
+    out = {}
+    for v in values:
+        out[str(v)] = out.get(str(v), 0) + 1
+    return out
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "ensemble":
+        return run_ensemble(args)
     return run_ours(args)
 
 

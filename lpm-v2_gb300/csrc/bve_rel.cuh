@@ -13,9 +13,12 @@
 //    on a quasi-uniform point set; the spacing guard sends clustered sets to the wide path;
 //  - wide tile (sparse or clustered points): o = 0, so (s_hi, s_lo) are the absolute hi/lo
 //    parts and d = (t_hi - s_hi) + (t_lo - s_lo) keeps ~48 bits for near pairs.
+// A compact tile whose sources all lie on the sphere to within |c_j| <= 2^-30 h^2 (h its
+// smallest spacing; always the case once positions are renormalised) drops c_j: q is then
+// fma(dz,dz, fma(dy,dy, fma(dx,dx, -c_i))), one operation less per pair.
 // Then  q = |d|^2 - c_i - c_j,  w = S_j / q,  D += w d  with c = |p|^2 - 1 and
 // S_j = -zeta_j A_j / (2 pi a) as in BveF32; u = D x p_i in FP64.  A compact tile costs
-// 11 packed FP32x2 operations per target pair and source, a wide one 17.
+// 11 packed FP32x2 operations per target pair and source (10 on the sphere), a wide one 17.
 // Targets keep their original order (only sources are sorted), so no scatter is needed.
 #pragma once
 
@@ -34,7 +37,7 @@ struct BveRel {
   };
   struct __align__(16) Origin {
     float4 hi;  // o_hi.x, o_hi.y, o_hi.z, 1 if the tile is wide
-    float4 lo;  // o_lo.x, o_lo.y, o_lo.z, 0
+    float4 lo;  // o_lo.x, o_lo.y, o_lo.z, 1 if every c_j of the tile is negligible
   };
   static constexpr float kCompactRadius = 0.125f;  // on the unit sphere
   static constexpr float kCompactRatio = 64.0f;
@@ -109,24 +112,47 @@ __global__ void __launch_bounds__(THREADS, MINB) bve_rel_sweep_kernel(SweepArgs<
         rel2x2(pr[p].yh, pr[p].yl, o.hi.y, o.lo.y, ty[p], unused);
         rel2x2(pr[p].zh, pr[p].zl, o.hi.z, o.lo.z, tz[p], unused);
       }
+      if (o.lo.w != 0.f) {
+        // every source of the tile on the sphere: c_j dropped
 #pragma unroll 2
-      for (int j = 0; j < TILE; ++j) {
-        const float4 ra = tl[j].a, rb = tl[j].b, rc = tl[j].c;
-        const float2 nsx = lo2(ra), nsy = hi2(ra), nsz = lo2(rb), ncj = hi2(rb), s2 = lo2(rc);
+        for (int j = 0; j < TILE; ++j) {
+          const float4 ra = tl[j].a, rb = tl[j].b, rc = tl[j].c;
+          const float2 nsx = lo2(ra), nsy = hi2(ra), nsz = lo2(rb), s2 = lo2(rc);
 #pragma unroll
-        for (int p = 0; p < NP; ++p) {
-          const float2 dx = __fadd2_rn(tx[p], nsx);
-          const float2 dy = __fadd2_rn(ty[p], nsy);
-          const float2 dz = __fadd2_rn(tz[p], nsz);
-          float2 q = __fadd2_rn(pr[p].nc, ncj);
-          q = __ffma2_rn(dx, dx, q);
-          q = __ffma2_rn(dy, dy, q);
-          q = __ffma2_rn(dz, dz, q);
-          const float2 inv = make_float2(rcp_approx(q.x), rcp_approx(q.y));
-          const float2 wgt = __fmul2_rn(s2, inv);
-          ax[p] = __ffma2_rn(wgt, dx, ax[p]);
-          ay[p] = __ffma2_rn(wgt, dy, ay[p]);
-          az[p] = __ffma2_rn(wgt, dz, az[p]);
+          for (int p = 0; p < NP; ++p) {
+            const float2 dx = __fadd2_rn(tx[p], nsx);
+            const float2 dy = __fadd2_rn(ty[p], nsy);
+            const float2 dz = __fadd2_rn(tz[p], nsz);
+            float2 q = __ffma2_rn(dx, dx, pr[p].nc);
+            q = __ffma2_rn(dy, dy, q);
+            q = __ffma2_rn(dz, dz, q);
+            const float2 inv = make_float2(rcp_approx(q.x), rcp_approx(q.y));
+            const float2 wgt = __fmul2_rn(s2, inv);
+            ax[p] = __ffma2_rn(wgt, dx, ax[p]);
+            ay[p] = __ffma2_rn(wgt, dy, ay[p]);
+            az[p] = __ffma2_rn(wgt, dz, az[p]);
+          }
+        }
+      } else {
+#pragma unroll 2
+        for (int j = 0; j < TILE; ++j) {
+          const float4 ra = tl[j].a, rb = tl[j].b, rc = tl[j].c;
+          const float2 nsx = lo2(ra), nsy = hi2(ra), nsz = lo2(rb), ncj = hi2(rb), s2 = lo2(rc);
+#pragma unroll
+          for (int p = 0; p < NP; ++p) {
+            const float2 dx = __fadd2_rn(tx[p], nsx);
+            const float2 dy = __fadd2_rn(ty[p], nsy);
+            const float2 dz = __fadd2_rn(tz[p], nsz);
+            float2 q = __fadd2_rn(pr[p].nc, ncj);
+            q = __ffma2_rn(dx, dx, q);
+            q = __ffma2_rn(dy, dy, q);
+            q = __ffma2_rn(dz, dz, q);
+            const float2 inv = make_float2(rcp_approx(q.x), rcp_approx(q.y));
+            const float2 wgt = __fmul2_rn(s2, inv);
+            ax[p] = __ffma2_rn(wgt, dx, ax[p]);
+            ay[p] = __ffma2_rn(wgt, dy, ay[p]);
+            az[p] = __ffma2_rn(wgt, dz, az[p]);
+          }
         }
       }
     } else {
@@ -199,7 +225,7 @@ __global__ void __launch_bounds__(TILE) bve_rel_prep_kernel(const double* x, con
                                                             double s_scale, BveRel::Rec* out, BveRel::Origin* org) {
   __shared__ double sp[3][TILE];
   __shared__ double red[3][TILE];
-  __shared__ float fmax_[TILE], fmin_[TILE];
+  __shared__ float fmax_[TILE], fmin_[TILE], cmax_[TILE];
   const int tid = threadIdx.x;
   const int64_t t = blockIdx.x;
   const int64_t k = t * TILE + tid;
@@ -240,16 +266,21 @@ __global__ void __launch_bounds__(TILE) bve_rel_prep_kernel(const double* x, con
       spc = static_cast<float>(sqrt(ex * ex + ey * ey + ez * ez));
     }
   }
+  const double cj = valid ? fma(px, px, fma(py, py, fma(pz, pz, -1.0))) : 0.0;
   fmax_[tid] = rad;
   fmin_[tid] = spc;
+  cmax_[tid] = static_cast<float>(fabs(cj));
   __syncthreads();
   for (int w = TILE / 2; w > 0; w >>= 1) {
     if (tid < w) {
       fmax_[tid] = fmaxf(fmax_[tid], fmax_[tid + w]);
       fmin_[tid] = fminf(fmin_[tid], fmin_[tid + w]);
+      cmax_[tid] = fmaxf(cmax_[tid], cmax_[tid + w]);
     }
     __syncthreads();
   }
+  // on the sphere: dropping every c_j moves q by <= 2^-30 h^2 relative to the smallest |d|^2
+  const bool on_sphere = cmax_[0] <= 9.313225746154785e-10f * fmin_[0] * fmin_[0];
   const bool wide = !(fmax_[0] <= BveRel::kCompactRadius && fmax_[0] <= BveRel::kCompactRatio * fmin_[0]);
   float oxh = 0.f, oxl = 0.f, oyh = 0.f, oyl = 0.f, ozh = 0.f, ozl = 0.f;
   if (!wide) {
@@ -266,7 +297,7 @@ __global__ void __launch_bounds__(TILE) bve_rel_prep_kernel(const double* x, con
     rel2(h, l, oyh, oyl, syh, syl);
     split2(pz, h, l);
     rel2(h, l, ozh, ozl, szh, szl);
-    const float nc = __double2float_rn(-fma(px, px, fma(py, py, fma(pz, pz, -1.0))));
+    const float nc = __double2float_rn(-cj);
     const float s = __double2float_rn(zeta[j] * area[j] * s_scale);
     r.a = make_float4(-sxh, -sxh, -syh, -syh);
     r.b = make_float4(-szh, -szh, nc, nc);
@@ -281,7 +312,7 @@ __global__ void __launch_bounds__(TILE) bve_rel_prep_kernel(const double* x, con
   if (tid == 0) {
     BveRel::Origin o;
     o.hi = make_float4(oxh, oyh, ozh, wide ? 1.f : 0.f);
-    o.lo = make_float4(oxl, oyl, ozl, 0.f);
+    o.lo = make_float4(oxl, oyl, ozl, (!wide && on_sphere) ? 1.f : 0.f);
     org[t] = o;
   }
 }

@@ -218,7 +218,8 @@ void DeviceArena::release() {
 }
 
 int SumScratch::init(DeviceArena& arena, int kind, int mode, int64_t ns, int64_t nt, int sm_count) {
-  plan = plan_sum(kind, mode, ns, nt, sm_count);
+  // sized for every sweep shape, so the autotuner can time them all in this scratch
+  plan = plan_sum_max(kind, mode, ns, nt, sm_count);
   LPM_TRY(arena.alloc(plan.src_bytes, &src_buf));
   if (plan.partial_bytes) {
     void* p = nullptr;
@@ -449,6 +450,11 @@ int bve_create(lpm_bve_solver* S, int64_t n, const double* x, const double* y, c
     LPM_TRY(S->arena.alloc(S->ns * sizeof(int32_t), &sorted));
     S->sorted = static_cast<int32_t*>(sorted);
     LPM_TRY(S->sort_sources());
+    // choose the sweep shape on this problem (the timing runs write into the stage buffers)
+    int shape = 0;
+    LPM_TRY(autotune_bve_shape(S->job(S->x, S->y, S->z, S->q, kSumBve, S->us, S->vs, S->ws), S->ctx->sm_count,
+                               &shape));
+    S->scratch.plan = plan_sum(kSumBve, mode, S->ns, n, S->ctx->sm_count, shape);
   }
   for (auto& e : S->ev) LPM_CUDA_TRY(cudaEventCreate(&e));
   if (u && v && w) {

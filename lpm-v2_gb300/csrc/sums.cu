@@ -2,6 +2,9 @@
 // C-ABI entry points lpm_bve_velocity, lpm_plane_velocity, lpm_pse_*_laplacian and the
 // stream functions.
 #include <cmath>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <vector>
 
 #include "bve_rel.cuh"
@@ -18,7 +21,14 @@ namespace {
 constexpr double kPi = 3.1415926535897932384626433832795027975;
 
 // FP32C sweep shapes (threads per CTA, targets per thread, tile, min CTAs per SM)
-constexpr int kBveThreads = 128, kBveTpt = 4, kBveTile = 256, kBveMinB = 4;
+constexpr int kBveTile = 256;
+// Shapes of the sphere-BVE FP32C sweep the autotuner chooses from: threads per CTA,
+// targets per thread (in pairs), CTAs per SM.  All fit without register spills.
+struct BveShape {
+  int threads, tpt, minb;
+};
+constexpr BveShape kBveShapes[] = {{128, 4, 4}, {256, 4, 2}, {128, 6, 2}, {128, 8, 2}};
+constexpr int kBveShapeCount = sizeof(kBveShapes) / sizeof(kBveShapes[0]);
 constexpr int kPlaneThreads = 128, kPlaneTpt = 4, kPlaneTile = 256, kPlaneMinB = 4;
 constexpr int kPseThreads = 128, kPseTpt = 2, kPseTile = 128, kPseMinB = 4;
 // FP64 sequential sweep shape
@@ -269,11 +279,11 @@ int comps_of(int kind) {
   }
 }
 
-int targets_per_cta(int kind) {
+int targets_per_cta(int kind, int shape) {
   switch (kind) {
     case kSumBve:
     case kSumBveMesh:
-      return kBveThreads * kBveTpt;
+      return kBveShapes[shape].threads * kBveShapes[shape].tpt;
     case kSumPlane:
       return kPlaneThreads * kPlaneTpt;
     default:
@@ -289,8 +299,12 @@ bool sum_uses_sorted_sources(int kind, int mode) {
   return mode == LPM_MODE_FP32C && (kind == kSumBve || kind == kSumBveMesh);
 }
 
-SumPlan plan_sum(int kind, int mode, int64_t ns, int64_t nt, int sm_count) {
+int bve_shape_count() { return kBveShapeCount; }
+
+SumPlan plan_sum(int kind, int mode, int64_t ns, int64_t nt, int sm_count, int shape) {
+  if (shape < 0 || shape >= kBveShapeCount) shape = 0;
   SumPlan pl;
+  pl.shape = shape;
   const int tile = tile_of(kind, mode);
   pl.n_tiles = ceil_div(ns > 0 ? ns : 1, tile);
   pl.src_bytes = static_cast<size_t>(pl.n_tiles) * tile * rec_bytes(kind, mode);
@@ -305,8 +319,9 @@ SumPlan plan_sum(int kind, int mode, int64_t ns, int64_t nt, int sm_count) {
     return pl;
   }
   // Split the source range until the grid covers about two waves of resident CTAs.
-  const int64_t tblocks = ceil_div(nt, targets_per_cta(kind));
-  const int64_t want = static_cast<int64_t>(sm_count > 0 ? sm_count : 152) * 4 * 2;
+  const int64_t tblocks = ceil_div(nt, targets_per_cta(kind, shape));
+  const int minb = (kind == kSumBve || kind == kSumBveMesh) ? kBveShapes[shape].minb : 4;
+  const int64_t want = static_cast<int64_t>(sm_count > 0 ? sm_count : 152) * minb * 2;
   int64_t nsplit = ceil_div(want, tblocks);
   if (nsplit < 1) nsplit = 1;
   if (nsplit > pl.n_tiles) nsplit = pl.n_tiles;
@@ -422,9 +437,22 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
       a.nt = job.nt;
       a.partial = job.partial;
       a.status = job.status;
-      const dim3 grid(static_cast<unsigned>(ceil_div(job.nt, kBveThreads * kBveTpt)),
-                      static_cast<unsigned>(plan.nsplit));
-      bve_rel_sweep_kernel<kBveThreads, kBveTpt, kBveTile, kBveMinB><<<grid, kBveThreads, 0, job.stream>>>(a, org);
+      const BveShape sh = kBveShapes[plan.shape];
+      const dim3 grid(static_cast<unsigned>(ceil_div(job.nt, sh.threads * sh.tpt)), static_cast<unsigned>(plan.nsplit));
+      switch (plan.shape) {
+        case 0:
+          bve_rel_sweep_kernel<128, 4, kBveTile, 4><<<grid, 128, 0, job.stream>>>(a, org);
+          break;
+        case 1:
+          bve_rel_sweep_kernel<256, 4, kBveTile, 2><<<grid, 256, 0, job.stream>>>(a, org);
+          break;
+        case 2:
+          bve_rel_sweep_kernel<128, 6, kBveTile, 2><<<grid, 128, 0, job.stream>>>(a, org);
+          break;
+        default:
+          bve_rel_sweep_kernel<128, 8, kBveTile, 2><<<grid, 128, 0, job.stream>>>(a, org);
+          break;
+      }
       finish_bve_kernel<<<fin_grid, pb, 0, job.stream>>>(job.partial, plan.nsplit, job.nt, job.ib, job.x,
                                                          job.y, job.z, inv_a, job.out0, job.out1, job.out2);
       break;
@@ -477,6 +505,80 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
       return set_error(LPM_ERR_ARG, "sum kind %d has no FP32C form", job.kind);
   }
   LPM_CUDA_TRY(cudaGetLastError());
+  return LPM_OK;
+}
+
+// ------------------------------------------------------------------ autotuner
+
+namespace {
+constexpr int64_t kTuneTargets = 64 * 1024;  // timing subset of the targets
+std::mutex g_tune_mu;
+std::map<std::tuple<int, int, int, int>, int> g_tune_cache;  // (kind, log2 ns, log2 nt, SMs) -> shape
+
+int log2_bucket(int64_t v) {
+  int b = 0;
+  while ((int64_t{1} << (b + 1)) <= v) ++b;
+  return b;
+}
+}  // namespace
+
+SumPlan plan_sum_max(int kind, int mode, int64_t ns, int64_t nt, int sm_count) {
+  SumPlan best = plan_sum(kind, mode, ns, nt, sm_count, 0);
+  if (!sum_uses_sorted_sources(kind, mode)) return best;
+  const int64_t sub = nt < kTuneTargets ? nt : kTuneTargets;
+  for (int sh = 0; sh < kBveShapeCount; ++sh) {
+    for (const int64_t t : {nt, sub}) {
+      const SumPlan p = plan_sum(kind, mode, ns, t, sm_count, sh);
+      if (p.partial_bytes > best.partial_bytes) best.partial_bytes = p.partial_bytes;
+      if (p.src_bytes > best.src_bytes) best.src_bytes = p.src_bytes;
+    }
+  }
+  return best;
+}
+
+int autotune_bve_shape(const SumJob& job, int sm_count, int* shape) {
+  *shape = 0;
+  if (!sum_uses_sorted_sources(job.kind, job.mode) || job.ns == 0) return LPM_OK;
+  const auto key = std::make_tuple(job.kind == kSumBveMesh ? static_cast<int>(kSumBve) : job.kind,
+                                   log2_bucket(job.ns), log2_bucket(job.nt), sm_count);
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  const auto it = g_tune_cache.find(key);
+  if (it != g_tune_cache.end()) {
+    *shape = it->second;
+    return LPM_OK;
+  }
+  SumJob j = job;
+  if (j.nt > kTuneTargets) j.nt = kTuneTargets;
+  cudaEvent_t e0, e1;
+  LPM_CUDA_TRY(cudaEventCreate(&e0));
+  LPM_CUDA_TRY(cudaEventCreate(&e1));
+  float best_ms = 3.4e38f;
+  int best = 0;
+  int rc = LPM_OK;
+  for (int sh = 0; sh < kBveShapeCount && rc == LPM_OK; ++sh) {
+    const SumPlan p = plan_sum(j.kind, j.mode, j.ns, j.nt, sm_count, sh);
+    rc = launch_sum(j, p);  // warm-up (and sort) run
+    if (rc != LPM_OK) break;
+    cudaEventRecord(e0, j.stream);
+    rc = launch_sum(j, p);
+    cudaEventRecord(e1, j.stream);
+    if (rc != LPM_OK) break;
+    if (cudaEventSynchronize(e1) != cudaSuccess) {
+      rc = set_error(LPM_ERR_CUDA, "autotune: %s", cudaGetErrorString(cudaGetLastError()));
+      break;
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = sh;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc != LPM_OK) return rc;
+  g_tune_cache[key] = best;
+  *shape = best;
   return LPM_OK;
 }
 
@@ -560,7 +662,7 @@ int run_host(const HostArgs& a, int nout) {
     LPM_TRY(workspace(ctx, kWsActive, static_cast<size_t>(ns) * sizeof(int32_t), &p_idx));
     LPM_CUDA_TRY(cudaMemcpyAsync(p_idx, idx.data(), static_cast<size_t>(ns) * sizeof(int32_t),
                                  cudaMemcpyHostToDevice, s));
-    const SumPlan plan = plan_sum(a.kind, prec, ns, nt, ctx->sm_count);
+    SumPlan plan = plan_sum_max(a.kind, prec, ns, nt, ctx->sm_count);
     SumJob job;
     job.kind = a.kind;
     job.mode = prec;
@@ -598,6 +700,9 @@ int run_host(const HostArgs& a, int nout) {
     }
     job.status = ctx->d_status;
     job.stream = s;
+    int shape = 0;
+    LPM_TRY(autotune_bve_shape(job, ctx->sm_count, &shape));
+    plan = plan_sum(a.kind, prec, ns, nt, ctx->sm_count, shape);
     LPM_TRY(launch_sum(job, plan));
   }
   double* outs[3] = {a.out0, a.out1, a.out2};

@@ -15,6 +15,7 @@ struct SumPlan {
   int64_t nsplit = 1;        // split-K chunks (gridDim.y)
   size_t src_bytes = 0;      // bytes of the padded source-record array
   size_t partial_bytes = 0;  // bytes of the FP64 partial sums
+  int shape = 0;             // sweep shape (sphere BVE FP32C; see bve_shape_count)
 };
 
 enum SumKind : int {
@@ -59,8 +60,20 @@ struct SumJob {
   cudaStream_t stream = nullptr;
 };
 
-// Decides tiles and split-K for a job on a device with sm_count SMs.
-SumPlan plan_sum(int kind, int mode, int64_t ns, int64_t nt, int sm_count);
+// Decides tiles, split-K and (for the sphere BVE FP32C sweep) the CTA shape of a job on a
+// device with sm_count SMs.
+SumPlan plan_sum(int kind, int mode, int64_t ns, int64_t nt, int sm_count, int shape = 0);
+
+// Number of sweep shapes of the sphere BVE FP32C sum.
+int bve_shape_count();
+
+// Autotuner: the shape of the sphere BVE FP32C sweep for a problem size, chosen once per
+// size class by timing every shape on the job (its targets limited to a bounded subset) and
+// cached for the process.  `job` must hold scratch sized for plan_sum_max(); results of the
+// timing runs land in job.out*.  Returns the shape in *shape.
+int autotune_bve_shape(const SumJob& job, int sm_count, int* shape);
+// Plan with the largest scratch over all shapes (for allocating before tuning).
+SumPlan plan_sum_max(int kind, int mode, int64_t ns, int64_t nt, int sm_count);
 // Enqueues prep + sweep (+ finish) on job.stream.
 int launch_sum(const SumJob& job, const SumPlan& plan);
 
