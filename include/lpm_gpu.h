@@ -106,7 +106,10 @@ int lpm_pse_plane_laplacian(int64_t n, const double* x, const double* y, const d
                             int mode);
 
 /* Replaces SetStreamFunctionsOnMesh (src/SphereBVE.f90:445-485): psi = sum G zeta A with
- * G = -log(a^2 - x_i.x_j)/(4 pi), for the relative and absolute vorticity. */
+ * G = -log(a^2 - x_i.x_j)/(4 pi), for the relative and absolute vorticity, j != i.
+ * LPM_MODE_FP64 follows the Fortran loop (its log is CUDA's, so agreement is to ~1e-15
+ * relative, not bitwise); LPM_MODE_FP32C forms a^2 - x_i.x_j without cancellation and
+ * takes the log on the MUFU unit (error ~1e-7 of max |psi|). */
 int lpm_bve_stream_functions(int64_t n, const double* x, const double* y, const double* z,
                              const double* relvort, const double* absvort,
                              const double* area, const int32_t* active, double radius,
@@ -114,7 +117,7 @@ int lpm_bve_stream_functions(int64_t n, const double* x, const double* y, const 
                              double* psi_abs, int mode);
 
 /* Replaces SetStreamFunctionOnMesh (src/PlanarIncompressible.f90:470-505):
- * psi = sum log(|x_i - x_j|)/(2 pi) omega_j A_j. */
+ * psi = sum log(|x_i - x_j|)/(2 pi) omega_j A_j, j != i; modes as for the sphere. */
 int lpm_plane_stream_function(int64_t n, const double* x, const double* y,
                               const double* omega, const double* area,
                               const int32_t* active, int64_t i_begin, int64_t i_end,

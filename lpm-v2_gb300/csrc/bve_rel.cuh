@@ -1,24 +1,25 @@
-// bve_rel.cuh -- the sphere-BVE FP32C sweep on spatially sorted sources in tile-relative
-// coordinates (11 packed FP32x2 operations per target pair and source).
+// bve_rel.cuh -- the sphere-BVE FP32C sweep on spatially sorted sources in group-relative
+// coordinates (10-11 packed FP32x2 operations per target pair and source).
 //
-// Sources are Morton-ordered, so a tile of TILE sources covers a small patch of the sphere.
-// Each source is stored relative to an origin o of its tile as a two-float offset
-// (s_hi, s_lo) = rel2(p, o); once per tile every target forms its own offset (t_hi, t_lo)
-// with exactly the same operations, so a self pair cancels bit for bit.  The prep kernel
-// picks o and a precision per tile:
-//  - compact tile (radius R about its centroid <= a/8 and <= 64 x the smallest spacing of
-//    consecutive sources in the tile): o = centroid and the pair difference is
+// Sources are Morton-ordered, so a group of kGroup consecutive sources covers a small patch
+// of the sphere.  Each source is stored relative to an origin o of its group as a two-float
+// offset (s_hi, s_lo) = rel2(p, o); once per group every target forms its own offset
+// (t_hi, t_lo) with exactly the same operations, so a self pair cancels bit for bit.  The
+// prep kernel picks o and a precision per group:
+//  - compact group (radius R about its centroid <= a/8 and <= 64 x the smallest spacing of
+//    consecutive sources in the group): o = centroid and the pair difference is
 //    d = t_hi - s_hi, one subtraction per component.  Its rounding error is ~2^-23 R, so
 //    the velocity error is ~1e-7 R sum_j S_j/|d_j|^2 / |u|, about 1e-7 relative when R <= a/8
 //    on a quasi-uniform point set; the spacing guard sends clustered sets to the wide path;
-//  - wide tile (sparse or clustered points): o = 0, so (s_hi, s_lo) are the absolute hi/lo
+//  - wide group (sparse or clustered points): o = 0, so (s_hi, s_lo) are the absolute hi/lo
 //    parts and d = (t_hi - s_hi) + (t_lo - s_lo) keeps ~48 bits for near pairs.
-// A compact tile whose sources all lie on the sphere to within |c_j| <= 2^-30 h^2 (h its
+// A compact group whose sources all lie on the sphere to within |c_j| <= 2^-30 h^2 (h its
 // smallest spacing; always the case once positions are renormalised) drops c_j: q is then
 // fma(dz,dz, fma(dy,dy, fma(dx,dx, -c_i))), one operation less per pair.
 // Then  q = |d|^2 - c_i - c_j,  w = S_j / q,  D += w d  with c = |p|^2 - 1 and
-// S_j = -zeta_j A_j / (2 pi a) as in BveF32; u = D x p_i in FP64.  A compact tile costs
-// 11 packed FP32x2 operations per target pair and source (10 on the sphere), a wide one 17.
+// S_j = -zeta_j A_j / (2 pi a) as in BveF32; u = D x p_i in FP64.  A compact group costs
+// 11 packed FP32x2 operations per target pair and source (10 on the sphere), a wide one 17;
+// forming the targets' offsets costs 12 per pair and group.
 // Targets keep their original order (only sources are sorted), so no scatter is needed.
 #pragma once
 
@@ -36,9 +37,10 @@ struct BveRel {
     float4 d;  // -sx_lo, -sx_lo, -sy_lo, -sy_lo
   };
   struct __align__(16) Origin {
-    float4 hi;  // o_hi.x, o_hi.y, o_hi.z, 1 if the tile is wide
-    float4 lo;  // o_lo.x, o_lo.y, o_lo.z, 1 if every c_j of the tile is negligible
+    float4 hi;  // o_hi.x, o_hi.y, o_hi.z, 1 if the group is wide
+    float4 lo;  // o_lo.x, o_lo.y, o_lo.z, 1 if every c_j of the group is negligible
   };
+  static constexpr int kGroup = 64;                 // sources per origin
   static constexpr float kCompactRadius = 0.125f;  // on the unit sphere
   static constexpr float kCompactRatio = 64.0f;
 };
@@ -58,31 +60,18 @@ __device__ __forceinline__ void rel2x2(float2 ph, float2 pl, float oh, float ol,
   rl = __fadd2_rn(__fadd2_rn(a, make_float2(-rh.x, -rh.y)), b);
 }
 
-template <int THREADS, int TPT, int TILE, int MINB>
-__global__ void __launch_bounds__(THREADS, MINB) bve_rel_sweep_kernel(SweepArgs<BveF32> a,
-                                                                      const BveRel::Origin* __restrict__ org) {
-  static_assert(TPT % 2 == 0, "targets come in pairs");
-  constexpr int NP = TPT / 2;
-  using Rec = BveRel::Rec;
-  __shared__ __align__(128) Rec stage[2][TILE];
-  __shared__ __align__(8) uint64_t bars[2];
-
-  const int64_t chunk = blockIdx.y;
-  const int64_t tile0 = chunk * a.tiles_per_chunk;
-  int64_t ntl = a.n_tiles - tile0;
-  if (ntl > a.tiles_per_chunk) ntl = a.tiles_per_chunk;
-  if (ntl < 0) ntl = 0;
-
-  BveX2::Pair pr[NP];
-  float2 hx[NP], hy[NP], hz[NP], lx[NP], ly[NP], lz[NP];
-  const int64_t base = static_cast<int64_t>(blockIdx.x) * (THREADS * TPT) + threadIdx.x;
+// Target pairs of a sweep: thread t holds targets first + t + (2p + h) * threads, clamped
+// to the `count` valid ones (duplicates are computed but not stored).
+template <int NP>
+__device__ __forceinline__ void bve_load_pairs(const BveF32::Params& prm, int64_t first, int64_t count,
+                                               int threads, BveX2::Pair (&pr)[NP]) {
 #pragma unroll
   for (int p = 0; p < NP; ++p) {
-    int64_t i0 = base + (2 * p) * THREADS, i1 = base + (2 * p + 1) * THREADS;
-    if (i0 >= a.nt) i0 = a.nt - 1;  // duplicates of a valid target; results not stored
-    if (i1 >= a.nt) i1 = a.nt - 1;
-    const BveF32::Tgt t0 = BveF32::load_target(a.p, a.ib + i0);
-    const BveF32::Tgt t1 = BveF32::load_target(a.p, a.ib + i1);
+    int64_t i0 = (2 * p) * threads + threadIdx.x, i1 = (2 * p + 1) * threads + threadIdx.x;
+    if (i0 >= count) i0 = count - 1;
+    if (i1 >= count) i1 = count - 1;
+    const BveF32::Tgt t0 = BveF32::load_target(prm, first + i0);
+    const BveF32::Tgt t1 = BveF32::load_target(prm, first + i1);
     pr[p].xh = make_float2(t0.xh, t1.xh);
     pr[p].yh = make_float2(t0.yh, t1.yh);
     pr[p].zh = make_float2(t0.zh, t1.zh);
@@ -90,21 +79,21 @@ __global__ void __launch_bounds__(THREADS, MINB) bve_rel_sweep_kernel(SweepArgs<
     pr[p].yl = make_float2(t0.yl, t1.yl);
     pr[p].zl = make_float2(t0.zl, t1.zl);
     pr[p].nc = make_float2(t0.nc, t1.nc);
-    hx[p] = hy[p] = hz[p] = lx[p] = ly[p] = lz[p] = make_float2(0.f, 0.f);
   }
+}
 
-  pipe_init(bars);
-  uint32_t g = 0;
-  int64_t tile = tile0;
-  const Rec* src = reinterpret_cast<const Rec*>(a.src);
-  staged_sweep<Rec, TILE>(src, tile0, ntl, stage[0], stage[1], bars, g, a.status, [&](const Rec* tl) {
-    const BveRel::Origin o = org[tile];
-    ++tile;
-    float2 ax[NP], ay[NP], az[NP];
-#pragma unroll
-    for (int p = 0; p < NP; ++p) ax[p] = ay[p] = az[p] = make_float2(0.f, 0.f);
+// One staged tile against NP target pairs: FP32 partials of D added into (ax, ay, az).
+template <int NP, int TILE>
+__device__ __forceinline__ void bve_rel_tile(const BveRel::Rec* __restrict__ tl, const BveRel::Origin* __restrict__ og,
+                                             const BveX2::Pair (&pr)[NP], float2 (&ax)[NP], float2 (&ay)[NP],
+                                             float2 (&az)[NP]) {
+  constexpr int G = BveRel::kGroup;
+#pragma unroll 1
+  for (int g0 = 0; g0 < TILE; g0 += G) {
+    const BveRel::Origin o = og[g0 / G];
+    const BveRel::Rec* gr = tl + g0;
     if (o.hi.w == 0.f) {
-      // compact tile: d = t_hi - s_hi
+      // compact group: d = t_hi - s_hi
       float2 tx[NP], ty[NP], tz[NP], unused;
 #pragma unroll
       for (int p = 0; p < NP; ++p) {
@@ -113,10 +102,10 @@ __global__ void __launch_bounds__(THREADS, MINB) bve_rel_sweep_kernel(SweepArgs<
         rel2x2(pr[p].zh, pr[p].zl, o.hi.z, o.lo.z, tz[p], unused);
       }
       if (o.lo.w != 0.f) {
-        // every source of the tile on the sphere: c_j dropped
+        // every source of the group on the sphere: c_j dropped
 #pragma unroll 2
-        for (int j = 0; j < TILE; ++j) {
-          const float4 ra = tl[j].a, rb = tl[j].b, rc = tl[j].c;
+        for (int j = 0; j < G; ++j) {
+          const float4 ra = gr[j].a, rb = gr[j].b, rc = gr[j].c;
           const float2 nsx = lo2(ra), nsy = hi2(ra), nsz = lo2(rb), s2 = lo2(rc);
 #pragma unroll
           for (int p = 0; p < NP; ++p) {
@@ -135,8 +124,8 @@ __global__ void __launch_bounds__(THREADS, MINB) bve_rel_sweep_kernel(SweepArgs<
         }
       } else {
 #pragma unroll 2
-        for (int j = 0; j < TILE; ++j) {
-          const float4 ra = tl[j].a, rb = tl[j].b, rc = tl[j].c;
+        for (int j = 0; j < G; ++j) {
+          const float4 ra = gr[j].a, rb = gr[j].b, rc = gr[j].c;
           const float2 nsx = lo2(ra), nsy = hi2(ra), nsz = lo2(rb), ncj = hi2(rb), s2 = lo2(rc);
 #pragma unroll
           for (int p = 0; p < NP; ++p) {
@@ -156,7 +145,7 @@ __global__ void __launch_bounds__(THREADS, MINB) bve_rel_sweep_kernel(SweepArgs<
         }
       }
     } else {
-      // wide tile (o = 0): d = (t_hi - s_hi) + (t_lo - s_lo)
+      // wide group (o = 0): d = (t_hi - s_hi) + (t_lo - s_lo)
       float2 txh[NP], tyh[NP], tzh[NP], txl[NP], tyl[NP], tzl[NP];
 #pragma unroll
       for (int p = 0; p < NP; ++p) {
@@ -164,8 +153,8 @@ __global__ void __launch_bounds__(THREADS, MINB) bve_rel_sweep_kernel(SweepArgs<
         rel2x2(pr[p].yh, pr[p].yl, o.hi.y, o.lo.y, tyh[p], tyl[p]);
         rel2x2(pr[p].zh, pr[p].zl, o.hi.z, o.lo.z, tzh[p], tzl[p]);
       }
-      for (int j = 0; j < TILE; ++j) {
-        const float4 ra = tl[j].a, rb = tl[j].b, rc = tl[j].c, rd = tl[j].d;
+      for (int j = 0; j < G; ++j) {
+        const float4 ra = gr[j].a, rb = gr[j].b, rc = gr[j].c, rd = gr[j].d;
         const float2 nsx = lo2(ra), nsy = hi2(ra), nsz = lo2(rb), ncj = hi2(rb), s2 = lo2(rc);
         const float2 nlx = lo2(rd), nly = hi2(rd), nlz = hi2(rc);
 #pragma unroll
@@ -185,22 +174,68 @@ __global__ void __launch_bounds__(THREADS, MINB) bve_rel_sweep_kernel(SweepArgs<
         }
       }
     }
+  }
+}
+
+// Adds the FP32 tile partials into the compensated (hi, lo) accumulators.
+template <int NP>
+__device__ __forceinline__ void bve_merge_pairs(const float2 (&ax)[NP], const float2 (&ay)[NP], const float2 (&az)[NP],
+                                                float2 (&hx)[NP], float2 (&hy)[NP], float2 (&hz)[NP],
+                                                float2 (&lx)[NP], float2 (&ly)[NP], float2 (&lz)[NP]) {
 #pragma unroll
-    for (int p = 0; p < NP; ++p) {
-      comp_add(hx[p].x, lx[p].x, ax[p].x);
-      comp_add(hx[p].y, lx[p].y, ax[p].y);
-      comp_add(hy[p].x, ly[p].x, ay[p].x);
-      comp_add(hy[p].y, ly[p].y, ay[p].y);
-      comp_add(hz[p].x, lz[p].x, az[p].x);
-      comp_add(hz[p].y, lz[p].y, az[p].y);
-    }
+  for (int p = 0; p < NP; ++p) {
+    comp_add(hx[p].x, lx[p].x, ax[p].x);
+    comp_add(hx[p].y, lx[p].y, ax[p].y);
+    comp_add(hy[p].x, ly[p].x, ay[p].x);
+    comp_add(hy[p].y, ly[p].y, ay[p].y);
+    comp_add(hz[p].x, lz[p].x, az[p].x);
+    comp_add(hz[p].y, lz[p].y, az[p].y);
+  }
+}
+
+template <int THREADS, int TPT, int TILE, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB) bve_rel_sweep_kernel(SweepArgs<BveF32> a,
+                                                                      const BveRel::Origin* __restrict__ org) {
+  static_assert(TPT % 2 == 0, "targets come in pairs");
+  static_assert(TILE % BveRel::kGroup == 0, "whole origin groups per tile");
+  constexpr int NP = TPT / 2;
+  constexpr int GPT = TILE / BveRel::kGroup;
+  using Rec = BveRel::Rec;
+  __shared__ __align__(128) Rec stage[2][TILE];
+  __shared__ __align__(8) uint64_t bars[2];
+
+  const int64_t chunk = blockIdx.y;
+  const int64_t tile0 = chunk * a.tiles_per_chunk;
+  int64_t ntl = a.n_tiles - tile0;
+  if (ntl > a.tiles_per_chunk) ntl = a.tiles_per_chunk;
+  if (ntl < 0) ntl = 0;
+
+  BveX2::Pair pr[NP];
+  float2 hx[NP], hy[NP], hz[NP], lx[NP], ly[NP], lz[NP];
+  const int64_t first = static_cast<int64_t>(blockIdx.x) * (THREADS * TPT);
+  const int64_t count = a.nt - first < THREADS * TPT ? a.nt - first : THREADS * TPT;
+  bve_load_pairs<NP>(a.p, a.ib + first, count, THREADS, pr);
+#pragma unroll
+  for (int p = 0; p < NP; ++p) hx[p] = hy[p] = hz[p] = lx[p] = ly[p] = lz[p] = make_float2(0.f, 0.f);
+
+  pipe_init(bars);
+  uint32_t g = 0;
+  int64_t tile = tile0;
+  const Rec* src = reinterpret_cast<const Rec*>(a.src);
+  staged_sweep<Rec, TILE>(src, tile0, ntl, stage[0], stage[1], bars, g, a.status, [&](const Rec* tl) {
+    float2 ax[NP], ay[NP], az[NP];
+#pragma unroll
+    for (int p = 0; p < NP; ++p) ax[p] = ay[p] = az[p] = make_float2(0.f, 0.f);
+    bve_rel_tile<NP, TILE>(tl, org + tile * GPT, pr, ax, ay, az);
+    ++tile;
+    bve_merge_pairs<NP>(ax, ay, az, hx, hy, hz, lx, ly, lz);
   });
 
 #pragma unroll
   for (int p = 0; p < NP; ++p) {
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
-      const int64_t il = base + (2 * p + h) * THREADS;
+      const int64_t il = first + (2 * p + h) * THREADS + threadIdx.x;
       if (il < a.nt) {
         const float vx = h ? hx[p].y : hx[p].x, ex = h ? lx[p].y : lx[p].x;
         const float vy = h ? hy[p].y : hy[p].x, ey = h ? ly[p].y : ly[p].x;
@@ -213,27 +248,25 @@ __global__ void __launch_bounds__(THREADS, MINB) bve_rel_sweep_kernel(SweepArgs<
   }
 }
 
-// Tile-relative source records from the Morton-sorted source list `sorted` (ns entries,
-// records ns..npad-1 inert) and the per-tile origins.  One CTA of TILE threads per tile:
-// the CTA reduces the tile's centroid, its radius about the centroid and the smallest
-// distance between consecutive sources, picks compact (o = centroid) or wide (o = 0), and
-// writes every record as rel2(p_j, o) -- the same operations the sweep uses for targets.
+// Records and origins of one tile of TILE sources (one CTA of TILE threads; every thread
+// one record).  `j` is the thread's particle (meaningful only if `valid`), `inv_a` and
+// `s_scale` the tile's sphere scale.  Each group of kGroup sources reduces its centroid,
+// its radius about the centroid, the smallest distance between consecutive sources and its
+// largest |c_j|, picks compact (o = centroid) or wide (o = 0), and every record is written
+// as rel2(p_j, o) -- the operations the sweep uses for targets.
 template <int TILE>
-__global__ void __launch_bounds__(TILE) bve_rel_prep_kernel(const double* x, const double* y, const double* z,
-                                                            const double* zeta, const double* area,
-                                                            const int32_t* sorted, int64_t ns, double inv_a,
-                                                            double s_scale, BveRel::Rec* out, BveRel::Origin* org) {
+__device__ __forceinline__ void bve_rel_prep_tile(const double* x, const double* y, const double* z,
+                                                  const double* zeta, const double* area, bool valid, int32_t j,
+                                                  double inv_a, double s_scale, BveRel::Rec* out,
+                                                  BveRel::Origin* og) {
+  constexpr int G = BveRel::kGroup;
   __shared__ double sp[3][TILE];
   __shared__ double red[3][TILE];
-  __shared__ float fmax_[TILE], fmin_[TILE], cmax_[TILE];
+  __shared__ float fmax_[TILE], fmin_[TILE], cmax_[TILE], cntf[TILE];
   const int tid = threadIdx.x;
-  const int64_t t = blockIdx.x;
-  const int64_t k = t * TILE + tid;
-  const bool valid = k < ns;
+  const int lane = tid % G;  // position in the group
   double px = 0.0, py = 0.0, pz = 0.0;
-  int32_t j = 0;
   if (valid) {
-    j = sorted[k];
     px = x[j] * inv_a;
     py = y[j] * inv_a;
     pz = z[j] * inv_a;
@@ -244,44 +277,48 @@ __global__ void __launch_bounds__(TILE) bve_rel_prep_kernel(const double* x, con
   red[0][tid] = px;
   red[1][tid] = py;
   red[2][tid] = pz;
+  cntf[tid] = valid ? 1.f : 0.f;
   __syncthreads();
-  for (int w = TILE / 2; w > 0; w >>= 1) {
-    if (tid < w) {
+  for (int w = G / 2; w > 0; w >>= 1) {
+    if (lane < w) {
       red[0][tid] += red[0][tid + w];
       red[1][tid] += red[1][tid + w];
       red[2][tid] += red[2][tid + w];
+      cntf[tid] += cntf[tid + w];
     }
     __syncthreads();
   }
-  const int64_t cnt64 = ns - t * TILE;
-  const double cnt = static_cast<double>(cnt64 < TILE ? cnt64 : TILE);
-  const double cx = red[0][0] / cnt, cy = red[1][0] / cnt, cz = red[2][0] / cnt;
-  // radius about the centroid and the smallest spacing of consecutive sources
+  const int g0 = tid - lane;  // first thread of the group
+  const double cnt = cntf[g0] > 0.f ? static_cast<double>(cntf[g0]) : 1.0;
+  const double cx = red[0][g0] / cnt, cy = red[1][g0] / cnt, cz = red[2][g0] / cnt;
   float rad = 0.f, spc = 3.4e38f;
+  double cj = 0.0;
   if (valid) {
     const double dx = px - cx, dy = py - cy, dz = pz - cz;
     rad = static_cast<float>(sqrt(dx * dx + dy * dy + dz * dz));
-    if (tid > 0) {
+    if (lane > 0) {
       const double ex = px - sp[0][tid - 1], ey = py - sp[1][tid - 1], ez = pz - sp[2][tid - 1];
       spc = static_cast<float>(sqrt(ex * ex + ey * ey + ez * ez));
     }
+    cj = fma(px, px, fma(py, py, fma(pz, pz, -1.0)));
   }
-  const double cj = valid ? fma(px, px, fma(py, py, fma(pz, pz, -1.0))) : 0.0;
+  // sp is read above by the neighbour; the reductions below reuse other arrays only
   fmax_[tid] = rad;
   fmin_[tid] = spc;
   cmax_[tid] = static_cast<float>(fabs(cj));
   __syncthreads();
-  for (int w = TILE / 2; w > 0; w >>= 1) {
-    if (tid < w) {
+  for (int w = G / 2; w > 0; w >>= 1) {
+    if (lane < w) {
       fmax_[tid] = fmaxf(fmax_[tid], fmax_[tid + w]);
       fmin_[tid] = fminf(fmin_[tid], fmin_[tid + w]);
       cmax_[tid] = fmaxf(cmax_[tid], cmax_[tid + w]);
     }
     __syncthreads();
   }
+  const float grad = fmax_[g0], gspc = fmin_[g0], gcmax = cmax_[g0];
+  const bool wide = !(grad <= BveRel::kCompactRadius && grad <= BveRel::kCompactRatio * gspc);
   // on the sphere: dropping every c_j moves q by <= 2^-30 h^2 relative to the smallest |d|^2
-  const bool on_sphere = cmax_[0] <= 9.313225746154785e-10f * fmin_[0] * fmin_[0];
-  const bool wide = !(fmax_[0] <= BveRel::kCompactRadius && fmax_[0] <= BveRel::kCompactRatio * fmin_[0]);
+  const bool on_sphere = gcmax <= 9.313225746154785e-10f * gspc * gspc;
   float oxh = 0.f, oxl = 0.f, oyh = 0.f, oyl = 0.f, ozh = 0.f, ozl = 0.f;
   if (!wide) {
     split2(cx, oxh, oxl);
@@ -308,13 +345,28 @@ __global__ void __launch_bounds__(TILE) bve_rel_prep_kernel(const double* x, con
     // difference; q > 0 through the target's 2^-100 offset when the target sits on o)
     r.a = r.b = r.c = r.d = make_float4(0.f, 0.f, 0.f, 0.f);
   }
-  out[k] = r;
-  if (tid == 0) {
+  *out = r;
+  if (lane == 0) {
     BveRel::Origin o;
     o.hi = make_float4(oxh, oyh, ozh, wide ? 1.f : 0.f);
     o.lo = make_float4(oxl, oyl, ozl, (!wide && on_sphere) ? 1.f : 0.f);
-    org[t] = o;
+    og[tid / G] = o;
   }
+}
+
+// Tile-relative records of the Morton-sorted source list `sorted` (ns entries, records
+// ns..npad-1 inert) and the group origins: one CTA of TILE threads per tile.
+template <int TILE>
+__global__ void __launch_bounds__(TILE) bve_rel_prep_kernel(const double* x, const double* y, const double* z,
+                                                            const double* zeta, const double* area,
+                                                            const int32_t* sorted, int64_t ns, double inv_a,
+                                                            double s_scale, BveRel::Rec* out, BveRel::Origin* org) {
+  const int64_t t = blockIdx.x;
+  const int64_t k = t * TILE + threadIdx.x;
+  const bool valid = k < ns;
+  const int32_t j = valid ? sorted[k] : 0;
+  bve_rel_prep_tile<TILE>(x, y, z, zeta, area, valid, j, inv_a, s_scale, out + k,
+                          org + t * (TILE / BveRel::kGroup));
 }
 
 }  // namespace lpm

@@ -9,9 +9,21 @@
 // vote makes all threads leave together if one gives up, so a lost copy cannot hang the GPU.
 #pragma once
 
+#include <type_traits>
+
 #include "lpm_common.cuh"
 
 namespace lpm {
+
+// Sources per FP32 partial of an operator: Op::kFlush if it defines one, else a whole tile.
+template <class Op, class = void>
+struct FlushOf {
+  static constexpr int value = 0;
+};
+template <class Op>
+struct FlushOf<Op, std::void_t<decltype(Op::kFlush)>> {
+  static constexpr int value = Op::kFlush;
+};
 
 // Initialises the two stage barriers of a TMA pipeline (once per CTA).
 __device__ __forceinline__ void pipe_init(uint64_t* bars) {
@@ -84,8 +96,8 @@ struct SweepArgs {
 };
 
 // Compensated FP32 sweep: each thread owns TPT targets; pair terms are summed in FP32 per
-// tile and each tile partial is added into a (hi, lo) pair with TwoSum; the per-chunk
-// result hi + lo is written in FP64 for the cross-chunk reduction.
+// tile (or per Op::kFlush sources) and each partial is added into a (hi, lo) pair with
+// TwoSum; the per-chunk result hi + lo is written in FP64 for the cross-chunk reduction.
 template <class Op, int THREADS, int TPT, int TILE, int MINB>
 __global__ void __launch_bounds__(THREADS, MINB) sweep_fp32c_kernel(SweepArgs<Op> a) {
   using Rec = typename Op::Rec;
@@ -116,23 +128,28 @@ __global__ void __launch_bounds__(THREADS, MINB) sweep_fp32c_kernel(SweepArgs<Op
 
   pipe_init(bars);
   uint32_t g = 0;
+  constexpr int FL = (FlushOf<Op>::value > 0 && FlushOf<Op>::value < TILE) ? FlushOf<Op>::value : TILE;
+  static_assert(TILE % FL == 0, "flush interval must divide the tile");
   staged_sweep<Rec, TILE>(a.src, tile0, ntl, stage[0], stage[1], bars, g, a.status,
                           [&](const Rec* tile) {
-                            float acc[TPT][NC];
+#pragma unroll 1
+                            for (int j0 = 0; j0 < TILE; j0 += FL) {
+                              float acc[TPT][NC];
 #pragma unroll
-                            for (int t = 0; t < TPT; ++t)
+                              for (int t = 0; t < TPT; ++t)
 #pragma unroll
-                              for (int c = 0; c < NC; ++c) acc[t][c] = 0.0f;
+                                for (int c = 0; c < NC; ++c) acc[t][c] = 0.0f;
 #pragma unroll 4
-                            for (int j = 0; j < TILE; ++j) {
-                              const Rec r = tile[j];
+                              for (int j = j0; j < j0 + FL; ++j) {
+                                const Rec r = tile[j];
 #pragma unroll
-                              for (int t = 0; t < TPT; ++t) Op::interact(tg[t], r, acc[t]);
+                                for (int t = 0; t < TPT; ++t) Op::interact(tg[t], r, acc[t]);
+                              }
+#pragma unroll
+                              for (int t = 0; t < TPT; ++t)
+#pragma unroll
+                                for (int c = 0; c < NC; ++c) comp_add(hi[t][c], lo[t][c], acc[t][c]);
                             }
-#pragma unroll
-                            for (int t = 0; t < TPT; ++t)
-#pragma unroll
-                              for (int c = 0; c < NC; ++c) comp_add(hi[t][c], lo[t][c], acc[t][c]);
                           });
 
 #pragma unroll

@@ -4,13 +4,18 @@
 // particles off[k] .. off[k+1]-1); each instance's active sources are compacted into its
 // own tile-padded range of one packed source-record array.
 //
+// Sources: at the start of every velocity evaluation the active sources of all instances are
+// put in Morton order within their instance (one device sort on (instance, Morton code)
+// keys), and each instance's sources fill its own tile-padded range of group-relative
+// records -- the layout and arithmetic of the single-instance sweep (bve_rel.cuh).
+//
 // Work decomposition: each velocity evaluation of all instances is a flattened list of
 // work items (instance, block of 512 targets, range of source tiles).  Source ranges are cut
 // so that items cost about the same, and the items are sorted by decreasing cost.  One
 // persistent launch (a few CTAs per SM) pulls items from an atomic queue; each item writes
 // its own FP64 partial slot, and a finish kernel reduces the slots of a target block in a
-// fixed order, so the result does not depend on which CTA ran which item.  With the four
-// RK4 stage kernels, one step of all instances is 9 launches, captured in one CUDA graph.
+// fixed order, so the result does not depend on which CTA ran which item.  One RK4 step of
+// all instances (4 stage kernels, 4 x (sort, prep, sweep, finish)) is one CUDA graph.
 //
 // FP64 mode (parity) runs the bit-exact sequential sweep per instance instead.
 #include <algorithm>
@@ -18,9 +23,10 @@
 #include <numeric>
 #include <vector>
 
-#include "bve_x2.cuh"
+#include "bve_rel.cuh"
 #include "lpm_common.cuh"
 #include "solver.cuh"
+#include "sort.cuh"
 #include "sums.cuh"
 
 namespace lpm {
@@ -46,7 +52,8 @@ struct EnsArgs {
   const int* queue;
   int n_items;
   int* head;
-  const BveX2::Rec* src;
+  const BveRel::Rec* src;
+  const BveRel::Origin* org;
   const double *x, *y, *z;
   const double* inv_a;  // per instance
   double* partial;      // [slot][3][kTB]
@@ -55,7 +62,8 @@ struct EnsArgs {
 
 __global__ void __launch_bounds__(kThreads, kMinB) ensemble_sweep_kernel(EnsArgs a) {
   constexpr int NP = kTpt / 2;
-  using Rec = BveX2::Rec;
+  constexpr int GPT = kTile / BveRel::kGroup;
+  using Rec = BveRel::Rec;
   __shared__ __align__(128) Rec stage[2][kTile];
   __shared__ __align__(8) uint64_t bars[2];
   __shared__ int s_item;
@@ -71,57 +79,18 @@ __global__ void __launch_bounds__(kThreads, kMinB) ensemble_sweep_kernel(EnsArgs
     const BveF32::Params prm{a.x, a.y, a.z, a.inv_a[it.inst]};
     BveX2::Pair pr[NP];
     float2 hx[NP], hy[NP], hz[NP], lx[NP], ly[NP], lz[NP];
+    bve_load_pairs<NP>(prm, it.t0, it.nt, kThreads, pr);
 #pragma unroll
-    for (int p = 0; p < NP; ++p) {
-      int l0 = (2 * p) * kThreads + threadIdx.x, l1 = (2 * p + 1) * kThreads + threadIdx.x;
-      if (l0 >= it.nt) l0 = it.nt - 1;
-      if (l1 >= it.nt) l1 = it.nt - 1;
-      const BveF32::Tgt t0 = BveF32::load_target(prm, it.t0 + l0);
-      const BveF32::Tgt t1 = BveF32::load_target(prm, it.t0 + l1);
-      pr[p].xh = make_float2(t0.xh, t1.xh);
-      pr[p].yh = make_float2(t0.yh, t1.yh);
-      pr[p].zh = make_float2(t0.zh, t1.zh);
-      pr[p].xl = make_float2(t0.xl, t1.xl);
-      pr[p].yl = make_float2(t0.yl, t1.yl);
-      pr[p].zl = make_float2(t0.zl, t1.zl);
-      pr[p].nc = make_float2(t0.nc, t1.nc);
-      hx[p] = hy[p] = hz[p] = lx[p] = ly[p] = lz[p] = make_float2(0.f, 0.f);
-    }
+    for (int p = 0; p < NP; ++p) hx[p] = hy[p] = hz[p] = lx[p] = ly[p] = lz[p] = make_float2(0.f, 0.f);
+    int64_t tile = it.tile0;
     const bool ok = staged_sweep<Rec, kTile>(a.src, it.tile0, it.ntiles, stage[0], stage[1], bars, g, a.status,
-                                             [&](const Rec* tile) {
+                                             [&](const Rec* tl) {
       float2 ax[NP], ay[NP], az[NP];
 #pragma unroll
       for (int p = 0; p < NP; ++p) ax[p] = ay[p] = az[p] = make_float2(0.f, 0.f);
-#pragma unroll 2
-      for (int j = 0; j < kTile; ++j) {
-        const float4 ra = tile[j].a, rb = tile[j].b, rc = tile[j].c, rd = tile[j].d;
-        const float2 nxh = lo2(ra), nyh = hi2(ra), nzh = lo2(rb), nxl = hi2(rb), nyl = lo2(rc), nzl = hi2(rc);
-        const float2 ncj = lo2(rd), s2 = hi2(rd);
-#pragma unroll
-        for (int p = 0; p < NP; ++p) {
-          const float2 dx = __fadd2_rn(__fadd2_rn(pr[p].xh, nxh), __fadd2_rn(pr[p].xl, nxl));
-          const float2 dy = __fadd2_rn(__fadd2_rn(pr[p].yh, nyh), __fadd2_rn(pr[p].yl, nyl));
-          const float2 dz = __fadd2_rn(__fadd2_rn(pr[p].zh, nzh), __fadd2_rn(pr[p].zl, nzl));
-          float2 qq = __fadd2_rn(pr[p].nc, ncj);
-          qq = __ffma2_rn(dx, dx, qq);
-          qq = __ffma2_rn(dy, dy, qq);
-          qq = __ffma2_rn(dz, dz, qq);
-          const float2 inv = make_float2(rcp_approx(qq.x), rcp_approx(qq.y));
-          const float2 wgt = __fmul2_rn(s2, inv);
-          ax[p] = __ffma2_rn(wgt, dx, ax[p]);
-          ay[p] = __ffma2_rn(wgt, dy, ay[p]);
-          az[p] = __ffma2_rn(wgt, dz, az[p]);
-        }
-      }
-#pragma unroll
-      for (int p = 0; p < NP; ++p) {
-        comp_add(hx[p].x, lx[p].x, ax[p].x);
-        comp_add(hx[p].y, lx[p].y, ax[p].y);
-        comp_add(hy[p].x, ly[p].x, ay[p].x);
-        comp_add(hy[p].y, ly[p].y, ay[p].y);
-        comp_add(hz[p].x, lz[p].x, az[p].x);
-        comp_add(hz[p].y, lz[p].y, az[p].y);
-      }
+      bve_rel_tile<NP, kTile>(tl, a.org + tile * GPT, pr, ax, ay, az);
+      ++tile;
+      bve_merge_pairs<NP>(ax, ay, az, hx, hy, hz, lx, ly, lz);
     });
     if (!ok) break;
     double* slot = a.partial + it.slot * 3 * kTB;
@@ -140,32 +109,23 @@ __global__ void __launch_bounds__(kThreads, kMinB) ensemble_sweep_kernel(EnsArgs
   }
 }
 
-// Packed source records of all instances: record r holds particle src_gidx[r] (inert if < 0).
-__global__ void ensemble_prep_kernel(int64_t nrec, const int32_t* src_gidx, const int32_t* pinst,
-                                     const double* x, const double* y, const double* z, const double* zeta,
-                                     const double* area, const double* radius, BveX2::Rec* out) {
-  const int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (r >= nrec) return;
-  const int32_t j = src_gidx[r];
-  BveX2::Rec rec;
-  if (j >= 0) {
-    const double a = radius[pinst[j]];
-    const double inv_a = 1.0 / a;
-    const double px = x[j] * inv_a, py = y[j] * inv_a, pz = z[j] * inv_a;
-    float xh, xl, yh, yl, zh, zl;
-    split2(px, xh, xl);
-    split2(py, yh, yl);
-    split2(pz, zh, zl);
-    const float nc = __double2float_rn(-fma(px, px, fma(py, py, fma(pz, pz, -1.0))));
-    const float s = __double2float_rn(zeta[j] * area[j] * (-1.0 / (2.0 * kPi * a)));
-    rec.a = make_float4(-xh, -xh, -yh, -yh);
-    rec.b = make_float4(-zh, -zh, -xl, -xl);
-    rec.c = make_float4(-yl, -yl, -zl, -zl);
-    rec.d = make_float4(nc, nc, s, s);
-  } else {
-    rec.a = rec.b = rec.c = rec.d = make_float4(0.f, 0.f, 0.f, 0.f);
-  }
-  out[r] = rec;
+// Group-relative records of all instances: one CTA per (global) tile.  Tile t belongs to
+// instance tile_inst[t]; its sources are that instance's Morton-sorted sources
+// sorted[src_start[k] + (t - tile_off[k]) * kTile + lane], valid below ns_k.
+__global__ void __launch_bounds__(kTile) ensemble_prep_kernel(const int32_t* tile_inst, const int64_t* tile_off,
+                                                              const int64_t* src_start, const int64_t* ns_k,
+                                                              const int32_t* sorted, const double* x, const double* y,
+                                                              const double* z, const double* zeta, const double* area,
+                                                              const double* radius, BveRel::Rec* out,
+                                                              BveRel::Origin* org) {
+  const int64_t t = blockIdx.x;
+  const int k = tile_inst[t];
+  const int64_t local = (t - tile_off[k]) * kTile + threadIdx.x;
+  const bool valid = local < ns_k[k];
+  const int32_t j = valid ? sorted[src_start[k] + local] : 0;
+  const double a = radius[k];
+  bve_rel_prep_tile<kTile>(x, y, z, zeta, area, valid, j, 1.0 / a, -1.0 / (2.0 * kPi * a), out + t * kTile + threadIdx.x,
+                           org + t * (kTile / BveRel::kGroup));
 }
 
 // Per target: fixed-order FP64 sum of its block's item slots, then u = D x p.
@@ -275,9 +235,17 @@ struct lpm_ensemble {
   int64_t* d_off = nullptr;
   double *radius = nullptr, *omega = nullptr, *inv_a = nullptr;
   // FP32C work queue
-  int64_t nrec = 0;
-  int32_t* src_gidx = nullptr;
-  BveX2::Rec* rec = nullptr;
+  int64_t n_tiles = 0;
+  int64_t ns_total = 0;
+  int32_t* act_idx = nullptr;   // active sources in instance order
+  int32_t* act_grp = nullptr;   // their instance
+  int32_t* sorted = nullptr;    // Morton order within each instance
+  void* sort_scratch = nullptr;
+  size_t sort_bytes = 0;
+  int32_t* tile_inst = nullptr;
+  int64_t *d_tile_off = nullptr, *d_src_start = nullptr, *d_ns_k = nullptr;
+  BveRel::Rec* rec = nullptr;
+  BveRel::Origin* org = nullptr;
   Item* items = nullptr;
   int* queue = nullptr;
   int n_items = 0;
@@ -297,6 +265,7 @@ struct lpm_ensemble {
   cudaEvent_t ev[8] = {};
   double kernel_ms = 0.0;
   int64_t launches = 0;
+  int64_t step_kernels = 0;  // kernel nodes of the captured step graph
 
   int velocity(const double* px, const double* py, const double* pz, const double* pq, double* o0, double* o1,
                double* o2, int kind = kSumBve) {
@@ -333,10 +302,14 @@ struct lpm_ensemble {
       }
       return LPM_OK;
     }
-    const unsigned pg = static_cast<unsigned>(ceil_div(nrec > 0 ? nrec : 1, 256));
-    ensemble_prep_kernel<<<pg, 256, 0, stream>>>(nrec, src_gidx, pinst, px, py, pz, pq, area, radius, rec);
+    if (n_tiles > 0) {
+      LPM_TRY(grouped_morton_sort(stream, ns_total, K, act_idx, act_grp, px, py, pz, inv_a, sort_scratch, sort_bytes,
+                                  sorted));
+      ensemble_prep_kernel<<<static_cast<unsigned>(n_tiles), kTile, 0, stream>>>(
+          tile_inst, d_tile_off, d_src_start, d_ns_k, sorted, px, py, pz, pq, area, radius, rec, org);
+    }
     LPM_CUDA_TRY(cudaMemsetAsync(head, 0, sizeof(int), stream));
-    EnsArgs a{items, queue, n_items, head, rec, px, py, pz, inv_a, partial, status};
+    EnsArgs a{items, queue, n_items, head, rec, org, px, py, pz, inv_a, partial, status};
     ensemble_sweep_kernel<<<grid, kThreads, 0, stream>>>(a);
     ensemble_finish_kernel<<<static_cast<unsigned>(ceil_div(n, 256)), 256, 0, stream>>>(
         n, pinst, d_off, blk_off, blk_first, blk_cnt, partial, px, py, pz, inv_a, o0, o1, o2);
@@ -381,6 +354,7 @@ struct lpm_ensemble {
     if (e != cudaSuccess) return set_error(LPM_ERR_CUDA, "stream capture failed: %s", cudaGetErrorString(e));
     graph = gr;
     LPM_CUDA_TRY(cudaGraphInstantiate(&exec, graph, 0));
+    step_kernels = graph_kernel_nodes(graph);
     graph_dt = dt;
     graph_renorm = renorm;
     return LPM_OK;
@@ -425,20 +399,24 @@ struct lpm_ensemble {
     return LPM_OK;
   }
 
-  // Builds the flattened work queue of the FP32C sweep.
+  // Builds the source layout and the flattened work queue of the FP32C sweep.
   int build_queue(const int32_t* active) {
-    std::vector<int32_t> gidx;
-    std::vector<int64_t> tile_off(K + 1, 0);
+    std::vector<int32_t> aidx, agrp, tinst;
+    std::vector<int64_t> tile_off(K + 1, 0), src_start(K + 1, 0);
     for (int k = 0; k < K; ++k) {
-      const int64_t start = static_cast<int64_t>(gidx.size());
-      for (int64_t j = off[k]; j < off[k + 1]; ++j)
-        if (active[j]) gidx.push_back(static_cast<int32_t>(j));
-      const int64_t cnt = static_cast<int64_t>(gidx.size()) - start;
-      const int64_t tiles = ceil_div(cnt, kTile);
-      gidx.resize(start + tiles * kTile, -1);
+      for (int64_t j = off[k]; j < off[k + 1]; ++j) {
+        if (active[j]) {
+          aidx.push_back(static_cast<int32_t>(j));
+          agrp.push_back(k);
+        }
+      }
+      src_start[k + 1] = static_cast<int64_t>(aidx.size());
+      const int64_t tiles = ceil_div(src_start[k + 1] - src_start[k], kTile);
       tile_off[k + 1] = tile_off[k] + tiles;
+      for (int64_t t = 0; t < tiles; ++t) tinst.push_back(k);
     }
-    nrec = static_cast<int64_t>(gidx.size());
+    ns_total = static_cast<int64_t>(aidx.size());
+    n_tiles = tile_off[K];
     // item size: aim at ~8 items per resident CTA slot
     double units = 0.0;
     for (int k = 0; k < K; ++k)
@@ -478,8 +456,17 @@ struct lpm_ensemble {
     std::stable_sort(order.begin(), order.end(), [&](int p, int q) {
       return static_cast<int64_t>(it[p].nt) * it[p].ntiles > static_cast<int64_t>(it[q].nt) * it[q].ntiles;
     });
-    LPM_TRY(upload_vec(&src_gidx, gidx));
-    LPM_TRY(dev_array(&rec, std::max<int64_t>(nrec, 1)));
+    LPM_TRY(upload_vec(&act_idx, aidx));
+    LPM_TRY(upload_vec(&act_grp, agrp));
+    LPM_TRY(upload_vec(&tile_inst, tinst));
+    LPM_TRY(upload_vec(&d_tile_off, tile_off));
+    LPM_TRY(upload_vec(&d_src_start, src_start));
+    LPM_TRY(upload_vec(&d_ns_k, ns_k));
+    LPM_TRY(dev_array(&sorted, std::max<int64_t>(ns_total, 1)));
+    sort_bytes = grouped_morton_sort_bytes(std::max<int64_t>(ns_total, 1), K);
+    LPM_TRY(arena.alloc(sort_bytes, &sort_scratch));
+    LPM_TRY(dev_array(&rec, std::max<int64_t>(n_tiles * kTile, 1)));
+    LPM_TRY(dev_array(&org, std::max<int64_t>(n_tiles * (kTile / BveRel::kGroup), 1)));
     LPM_TRY(upload_vec(&items, it));
     LPM_TRY(upload_vec(&queue, order));
     LPM_TRY(upload_vec(&blk_off, boff));
@@ -593,7 +580,7 @@ extern "C" int lpm_ensemble_timestep(lpm_ensemble* E, double dt, int n_steps, in
       LPM_CUDA_TRY(cudaEventElapsedTime(&ms, E->ev[2 * k], E->ev[2 * k + 1]));
       E->kernel_ms += ms;
     }
-    E->launches += (E->mode == LPM_MODE_FP64) ? 4 * 2 * E->K : 4 * 3;
+    E->launches += E->step_kernels;
   }
   return LPM_OK;
 }

@@ -33,6 +33,7 @@
 #include "engine.cuh"
 #include "lpm_common.cuh"
 #include "ops.cuh"
+#include "sums.cuh"
 
 namespace lpm {
 namespace {
@@ -141,13 +142,10 @@ extern "C" int lpm_bve_velocity_noalloc(int64_t n, const double* x, const double
   const int64_t nt = i_end - i_begin + 1;
   const int64_t n_tiles = ceil_div(n, kNaTile);
   const int64_t npad = n_tiles * kNaTile;
-  // split the sources so the grid covers about two waves, within the partial-sum region
+  // split the sources so that the last wave is nearly full, within the partial-sum region
   const int64_t tblocks = ceil_div(nt, kNaThreads * kNaTpt);
-  int64_t nsplit = ceil_div(static_cast<int64_t>(sms) * kNaMinB * 2, tblocks);
   const int64_t cap = static_cast<int64_t>(kNaPartialBytes / (3 * sizeof(double) * static_cast<size_t>(nt)));
-  if (nsplit > cap) nsplit = cap;
-  if (nsplit > n_tiles) nsplit = n_tiles;
-  if (nsplit < 1) nsplit = 1;
+  int64_t nsplit = choose_split(tblocks, n_tiles, static_cast<int64_t>(sms) * kNaMinB, cap < 1 ? 1 : cap);
   const int64_t tpc = ceil_div(n_tiles, nsplit);
   nsplit = ceil_div(n_tiles, tpc);
 

@@ -229,6 +229,19 @@ int SumScratch::init(DeviceArena& arena, int kind, int mode, int64_t ns, int64_t
   return LPM_OK;
 }
 
+int64_t graph_kernel_nodes(cudaGraph_t graph) {
+  size_t n = 0;
+  if (cudaGraphGetNodes(graph, nullptr, &n) != cudaSuccess || n == 0) return 0;
+  std::vector<cudaGraphNode_t> nodes(n);
+  if (cudaGraphGetNodes(graph, nodes.data(), &n) != cudaSuccess) return 0;
+  int64_t k = 0;
+  for (size_t i = 0; i < n; ++i) {
+    cudaGraphNodeType t;
+    if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++k;
+  }
+  return k;
+}
+
 std::vector<int32_t> active_list(int64_t n, const int32_t* active) {
   std::vector<int32_t> idx;
   for (int64_t j = 0; j < n; ++j)
@@ -266,6 +279,7 @@ struct lpm_bve_solver {
   cudaEvent_t ev[8] = {};
   double kernel_ms = 0.0;
   int64_t kernel_launches = 0;
+  int64_t step_kernels = 0;  // kernel nodes of the captured step graph
   bool timing = true;
   // FP32C: Morton order of the sources, refreshed at the start of every step
   void* sort_scratch = nullptr;
@@ -360,6 +374,7 @@ struct lpm_bve_solver {
     if (e != cudaSuccess) return set_error(LPM_ERR_CUDA, "stream capture failed: %s", cudaGetErrorString(e));
     graph = gr;
     LPM_CUDA_TRY(cudaGraphInstantiate(&exec, graph, 0));
+    step_kernels = graph_kernel_nodes(graph);
     graph_dt = dt;
     graph_renorm = renorm;
     return LPM_OK;
@@ -501,9 +516,8 @@ extern "C" int lpm_bve_timestep(lpm_bve_solver* S, double dt, int n_steps, int r
   if (!S->exec || S->graph_dt != dt || S->graph_renorm != renorm) LPM_TRY(S->capture(dt, renorm));
   for (int s = 0; s < n_steps; ++s) {
     LPM_CUDA_TRY(cudaGraphLaunch(S->exec, S->stream));
-    // 4 stage kernels, 4 direct sums, and the Morton sort of the sources (FP32C: one key
-    // kernel and the six kernels of the CUB radix sort over 30-bit keys)
-    S->kernel_launches += 4 + 4 * (S->ns ? kernels_per_sum(S->mode) : 0) + (S->sorted ? 7 : 0);
+    // 4 stage kernels, 4 direct sums and (FP32C) the Morton sort of the sources
+    S->kernel_launches += S->step_kernels;
     if (!S->timing) continue;
     LPM_TRY(S->check_status("lpm_bve_timestep"));
     for (int k = 0; k < 4; ++k) {

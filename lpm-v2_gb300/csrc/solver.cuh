@@ -24,6 +24,9 @@ struct SumScratch {
   int init(DeviceArena& arena, int kind, int mode, int64_t ns, int64_t nt, int sm_count);
 };
 
+// Number of kernel nodes in a captured graph: the kernels one replay launches.
+int64_t graph_kernel_nodes(cudaGraph_t graph);
+
 // Indices of the active particles, ascending.
 std::vector<int32_t> active_list(int64_t n, const int32_t* active);
 

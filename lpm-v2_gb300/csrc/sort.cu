@@ -38,7 +38,60 @@ __global__ void morton_keys_kernel(int64_t ns, const int32_t* idx, const double*
   vals[k] = j;
 }
 
+// 64-bit keys: the group in the high bits, the Morton code of the group-scaled position low.
+__global__ void grouped_morton_keys_kernel(int64_t ns, const int32_t* idx, const int32_t* grp, const double* x,
+                                           const double* y, const double* z, const double* inv_a, uint64_t* keys,
+                                           int32_t* vals) {
+  const int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= ns) return;
+  const int32_t j = idx[k];
+  const int32_t g = grp[k];
+  const double s = inv_a[g];
+  const double px = x[j] * s, py = y[j] * s, pz = z[j] * s;
+  const uint32_t m = spread10(quant10(px)) | (spread10(quant10(py)) << 1) | (spread10(quant10(pz)) << 2);
+  keys[k] = (static_cast<uint64_t>(g) << 30) | m;
+  vals[k] = j;
+}
+
+int end_bit_for(int n_groups) {
+  int b = 0;
+  while ((1 << b) < n_groups) ++b;
+  return 30 + b;
+}
+
 }  // namespace
+
+size_t grouped_morton_sort_bytes(int64_t ns, int n_groups) {
+  size_t temp = 0;
+  cub::DeviceRadixSort::SortPairs(nullptr, temp, static_cast<const uint64_t*>(nullptr), static_cast<uint64_t*>(nullptr),
+                                  static_cast<const int32_t*>(nullptr), static_cast<int32_t*>(nullptr),
+                                  static_cast<int>(ns), 0, end_bit_for(n_groups));
+  return align_up(temp, 256) + 2 * align_up(static_cast<size_t>(ns) * 8, 256) + align_up(static_cast<size_t>(ns) * 4, 256);
+}
+
+int grouped_morton_sort(cudaStream_t stream, int64_t ns, int n_groups, const int32_t* idx, const int32_t* grp,
+                        const double* x, const double* y, const double* z, const double* inv_a, void* scratch,
+                        size_t scratch_bytes, int32_t* sorted) {
+  if (ns <= 0) return LPM_OK;
+  const int end_bit = end_bit_for(n_groups);
+  size_t temp = 0;
+  cub::DeviceRadixSort::SortPairs(nullptr, temp, static_cast<const uint64_t*>(nullptr), static_cast<uint64_t*>(nullptr),
+                                  static_cast<const int32_t*>(nullptr), static_cast<int32_t*>(nullptr),
+                                  static_cast<int>(ns), 0, end_bit);
+  const size_t k8 = align_up(static_cast<size_t>(ns) * 8, 256);
+  const size_t k4 = align_up(static_cast<size_t>(ns) * 4, 256);
+  if (scratch_bytes < align_up(temp, 256) + 2 * k8 + k4) return set_error(LPM_ERR_STATE, "grouped sort scratch too small");
+  char* base = static_cast<char*>(scratch);
+  uint64_t* keys_in = reinterpret_cast<uint64_t*>(base + align_up(temp, 256));
+  uint64_t* keys_out = reinterpret_cast<uint64_t*>(base + align_up(temp, 256) + k8);
+  int32_t* vals_in = reinterpret_cast<int32_t*>(base + align_up(temp, 256) + 2 * k8);
+  grouped_morton_keys_kernel<<<static_cast<unsigned>(ceil_div(ns, 256)), 256, 0, stream>>>(ns, idx, grp, x, y, z,
+                                                                                           inv_a, keys_in, vals_in);
+  LPM_CUDA_TRY(cudaGetLastError());
+  LPM_CUDA_TRY(cub::DeviceRadixSort::SortPairs(base, temp, keys_in, keys_out, vals_in, sorted, static_cast<int>(ns), 0,
+                                               end_bit, stream));
+  return LPM_OK;
+}
 
 size_t morton_sort_bytes(int64_t ns) {
   size_t temp = 0;

@@ -13,4 +13,12 @@ size_t morton_sort_bytes(int64_t ns);
 int morton_sort(cudaStream_t stream, int64_t ns, const int32_t* idx, const double* x, const double* y,
                 const double* z, double inv_a, void* scratch, size_t scratch_bytes, int32_t* sorted);
 
+// Morton order within groups (ensemble instances): entries are ordered by group first, then
+// by the Morton code of (x, y, z) * inv_a[group]; idx/grp are the particle and group of each
+// entry.  n_groups < 2^33.
+size_t grouped_morton_sort_bytes(int64_t ns, int n_groups);
+int grouped_morton_sort(cudaStream_t stream, int64_t ns, int n_groups, const int32_t* idx, const int32_t* grp,
+                        const double* x, const double* y, const double* z, const double* inv_a, void* scratch,
+                        size_t scratch_bytes, int32_t* sorted);
+
 }  // namespace lpm

@@ -31,6 +31,7 @@ constexpr BveShape kBveShapes[] = {{128, 4, 4}, {256, 4, 2}, {128, 6, 2}, {128, 
 constexpr int kBveShapeCount = sizeof(kBveShapes) / sizeof(kBveShapes[0]);
 constexpr int kPlaneThreads = 128, kPlaneTpt = 4, kPlaneTile = 256, kPlaneMinB = 4;
 constexpr int kPseThreads = 128, kPseTpt = 2, kPseTile = 128, kPseMinB = 4;
+constexpr int kStreamThreads = 128, kStreamTpt = 4, kStreamTile = 256, kStreamMinB = 4;
 // FP64 sequential sweep shape
 constexpr int k64Threads = 128, k64Tile = 128;
 
@@ -145,6 +146,92 @@ __global__ void prep_plane32_kernel(const double* x, const double* y, const doub
   out[k] = r;
 }
 
+// Stream-function records (FP32C); records ns..npad-1 are inert (zero strength).  A source
+// that is also a target (ib <= j < ib + nt) leaves its zeta A in self_w[c * nt + j - ib]
+// (zeroed before), for the finish to take out of the total.
+__global__ void prep_sstream32_kernel(const double* x, const double* y, const double* z, const double* qr,
+                                      const double* qa, const double* area, const int32_t* idx, int64_t ns,
+                                      int64_t npad, double scale, int64_t ib, int64_t nt,
+                                      SphereStreamF32::Rec* out, double* self_w) {
+  const int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= npad) return;
+  SphereStreamF32::Rec r;
+  if (k < ns) {
+    const int64_t j = idx[k];
+    const double px = x[j] * scale, py = y[j] * scale, pz = z[j] * scale;
+    float h, l;
+    split2(px, h, l);
+    r.a.x = h;
+    r.b.x = l;
+    split2(py, h, l);
+    r.a.y = h;
+    r.b.y = l;
+    split2(pz, h, l);
+    r.a.z = h;
+    r.b.z = l;
+    r.a.w = SphereStreamF32::neg_c(px, py, pz);
+    r.b.w = 0.f;
+    const double wr = qr[j] * area[j], wa = qa[j] * area[j];
+    r.c = make_float4(__double2float_rn(wr * -kInv4Pi), __double2float_rn(wa * -kInv4Pi), 0.f, 0.f);
+    if (j >= ib && j < ib + nt) {
+      self_w[j - ib] = wr;
+      self_w[nt + j - ib] = wa;
+    }
+  } else {
+    // inert: zero strength at the centre (q = |p_i|^2 - c_i = 1/2)
+    r.a = r.b = r.c = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  out[k] = r;
+}
+
+// Totals sum_j zeta_j A_j over the active sources (relative and absolute), FP64 in a fixed
+// order: one block, strided per thread, then a tree.
+__global__ void __launch_bounds__(1024) stream_totals_kernel(const double* qr, const double* qa, const double* area,
+                                                             const int32_t* idx, int64_t ns, double* tot) {
+  __shared__ double sr[1024], sa[1024];
+  double a = 0.0, b = 0.0;
+  for (int64_t k = threadIdx.x; k < ns; k += 1024) {
+    const int64_t j = idx[k];
+    a += qr[j] * area[j];
+    b += qa[j] * area[j];
+  }
+  sr[threadIdx.x] = a;
+  sa[threadIdx.x] = b;
+  __syncthreads();
+  for (int w = 512; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      sr[threadIdx.x] += sr[threadIdx.x + w];
+      sa[threadIdx.x] += sa[threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    tot[0] = sr[0];
+    tot[1] = sa[0];
+  }
+}
+
+__global__ void prep_pstream32_kernel(const double* x, const double* y, const double* omega, const double* area,
+                                      const int32_t* idx, int64_t ns, int64_t npad, PlaneStreamF32::Rec* out) {
+  const int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= npad) return;
+  PlaneStreamF32::Rec r;
+  if (k < ns) {
+    const int64_t j = idx[k];
+    float h, l;
+    split2(x[j], h, l);
+    r.a.x = h;
+    r.a.z = l;
+    split2(y[j], h, l);
+    r.a.y = h;
+    r.a.w = l;
+    r.b = make_float4(__double2float_rn(omega[j] * area[j] * kInv4Pi), 0.f, 0.f, 0.f);
+  } else {
+    r.a = r.b = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  out[k] = r;
+}
+
 template <int KIND>
 __global__ void prep_pse32_kernel(const double* x, const double* y, const double* z,
                                   const double* f, const double* area, const int32_t* idx,
@@ -222,6 +309,20 @@ __global__ void finish_scalar_kernel(const double* partial, int64_t nsplit, int6
   out[il] = s * scale;
 }
 
+// Stream functions: fixed-order chunk sum per component, plus (sphere) the ln(a^2) term
+// k_const * (total - own term).
+__global__ void finish_stream_kernel(const double* partial, int64_t nsplit, int64_t nt, int nc, double k_const,
+                                     const double* tot, const double* self_w, double* out0, double* out1) {
+  const int64_t il = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (il >= nt) return;
+  for (int c = 0; c < nc; ++c) {
+    double s = 0.0;
+    for (int64_t k = 0; k < nsplit; ++k) s += partial[(k * nc + c) * nt + il];
+    if (tot) s += k_const * (tot[c] - self_w[c * nt + il]);
+    (c == 0 ? out0 : out1)[il] = s;
+  }
+}
+
 template <class Op, int THREADS, int TPT, int TILE, int MINB>
 void launch_sweep(const SumJob& job, const SumPlan& plan, const typename Op::Params& p) {
   SweepArgs<Op> a;
@@ -245,6 +346,9 @@ int tile_of(int kind, int mode) {
       return kBveTile;
     case kSumPlane:
       return kPlaneTile;
+    case kSumSphereStream:
+    case kSumPlaneStream:
+      return kStreamTile;
     default:
       return kPseTile;
   }
@@ -262,6 +366,10 @@ size_t rec_bytes(int kind, int mode) {
       return sizeof(BveRel::Rec);
     case kSumPlane:
       return sizeof(PlaneF32::Rec);
+    case kSumSphereStream:
+      return sizeof(SphereStreamF32::Rec);
+    case kSumPlaneStream:
+      return sizeof(PlaneStreamF32::Rec);
     default:
       return sizeof(PseF32<0>::Rec);
   }
@@ -273,6 +381,7 @@ int comps_of(int kind) {
     case kSumBveMesh:
       return 3;
     case kSumPlane:
+    case kSumSphereStream:
       return 2;
     default:
       return 1;
@@ -286,6 +395,9 @@ int targets_per_cta(int kind, int shape) {
       return kBveShapes[shape].threads * kBveShapes[shape].tpt;
     case kSumPlane:
       return kPlaneThreads * kPlaneTpt;
+    case kSumSphereStream:
+    case kSumPlaneStream:
+      return kStreamThreads * kStreamTpt;
     default:
       return kPseThreads * kPseTpt;
   }
@@ -293,7 +405,24 @@ int targets_per_cta(int kind, int shape) {
 
 }  // namespace
 
-int kernels_per_sum(int mode) { return mode == LPM_MODE_FP64 ? 2 : 3; }
+int64_t choose_split(int64_t blocks, int64_t tiles, int64_t slots, int64_t max_split) {
+  if (blocks < 1) blocks = 1;
+  if (slots < 1) slots = 1;
+  int64_t lim = tiles < max_split ? tiles : max_split;
+  if (lim > 4096) lim = 4096;
+  int64_t best = 1;
+  double best_cost = 1e300;
+  for (int64_t s = 1; s <= lim; ++s) {
+    const int64_t tpc = ceil_div(tiles, s);
+    if (s > 1 && ceil_div(tiles, tpc) < s) continue;  // same chunks as a smaller split
+    const double cost = static_cast<double>(ceil_div(blocks * s, slots)) * static_cast<double>(tpc + 1);
+    if (cost < best_cost) {
+      best_cost = cost;
+      best = s;
+    }
+  }
+  return best;
+}
 
 bool sum_uses_sorted_sources(int kind, int mode) {
   return mode == LPM_MODE_FP32C && (kind == kSumBve || kind == kSumBveMesh);
@@ -310,7 +439,13 @@ SumPlan plan_sum(int kind, int mode, int64_t ns, int64_t nt, int sm_count, int s
   pl.src_bytes = static_cast<size_t>(pl.n_tiles) * tile * rec_bytes(kind, mode);
   if (sum_uses_sorted_sources(kind, mode)) {
     // the per-tile origins follow the records
-    pl.src_bytes = align_up(pl.src_bytes, 256) + static_cast<size_t>(pl.n_tiles) * sizeof(BveRel::Origin);
+    pl.src_bytes = align_up(pl.src_bytes, 256) +
+                   static_cast<size_t>(pl.n_tiles) * (tile / BveRel::kGroup) * sizeof(BveRel::Origin);
+  }
+  if (mode == LPM_MODE_FP32C && kind == kSumSphereStream) {
+    // the sources' own zeta A (2 x nt) and the two totals follow the records
+    pl.src_bytes = align_up(pl.src_bytes, 256) + align_up(2 * static_cast<size_t>(nt) * sizeof(double), 256) +
+                   2 * sizeof(double);
   }
   if (mode == LPM_MODE_FP64) {
     pl.nsplit = 1;
@@ -318,14 +453,11 @@ SumPlan plan_sum(int kind, int mode, int64_t ns, int64_t nt, int sm_count, int s
     pl.partial_bytes = 0;
     return pl;
   }
-  // Split the source range until the grid covers about two waves of resident CTAs.
+  // Split the source range so that the last wave of CTAs is nearly full.
   const int64_t tblocks = ceil_div(nt, targets_per_cta(kind, shape));
   const int minb = (kind == kSumBve || kind == kSumBveMesh) ? kBveShapes[shape].minb : 4;
-  const int64_t want = static_cast<int64_t>(sm_count > 0 ? sm_count : 152) * minb * 2;
-  int64_t nsplit = ceil_div(want, tblocks);
-  if (nsplit < 1) nsplit = 1;
-  if (nsplit > pl.n_tiles) nsplit = pl.n_tiles;
-  if (nsplit > 65535) nsplit = 65535;
+  const int64_t slots = static_cast<int64_t>(sm_count > 0 ? sm_count : 152) * minb;
+  const int64_t nsplit = choose_split(tblocks, pl.n_tiles, slots, 65535);
   pl.tiles_per_chunk = ceil_div(pl.n_tiles, nsplit);
   pl.nsplit = ceil_div(pl.n_tiles, pl.tiles_per_chunk);
   pl.partial_bytes = static_cast<size_t>(pl.nsplit) * comps_of(kind) * nt * sizeof(double);
@@ -499,6 +631,35 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
                                                                    Op::Params{job.x, job.y, job.z, job.s1, inv_r, ks});
       }
       finish_scalar_kernel<<<fin_grid, pb, 0, job.stream>>>(job.partial, plan.nsplit, job.nt, cscale, job.out0);
+      break;
+    }
+    case kSumSphereStream: {
+      char* tail = static_cast<char*>(job.src_buf) +
+                   align_up(static_cast<size_t>(npad) * sizeof(SphereStreamF32::Rec), 256);
+      double* self_w = reinterpret_cast<double*>(tail);
+      double* tot = reinterpret_cast<double*>(tail + align_up(2 * static_cast<size_t>(job.nt) * sizeof(double), 256));
+      LPM_CUDA_TRY(cudaMemsetAsync(self_w, 0, 2 * static_cast<size_t>(job.nt) * sizeof(double), job.stream));
+      const double scale = 1.0 / (job.radius * 1.41421356237309504880);
+      prep_sstream32_kernel<<<prep_grid_pad, pb, 0, job.stream>>>(job.x, job.y, job.z, job.s1, job.s2, job.area,
+                                                                  job.src_idx, job.ns, npad, scale, job.ib, job.nt,
+                                                                  static_cast<SphereStreamF32::Rec*>(job.src_buf),
+                                                                  self_w);
+      stream_totals_kernel<<<1, 1024, 0, job.stream>>>(job.s1, job.s2, job.area, job.src_idx, job.ns, tot);
+      launch_sweep<SphereStreamF32, kStreamThreads, kStreamTpt, kStreamTile, kStreamMinB>(
+          job, plan, SphereStreamF32::Params{job.x, job.y, job.z, scale});
+      const double k_const = -std::log(job.radius * job.radius) * kInv4Pi;
+      finish_stream_kernel<<<fin_grid, pb, 0, job.stream>>>(job.partial, plan.nsplit, job.nt, 2, k_const, tot, self_w,
+                                                            job.out0, job.out1);
+      break;
+    }
+    case kSumPlaneStream: {
+      prep_pstream32_kernel<<<prep_grid_pad, pb, 0, job.stream>>>(job.x, job.y, job.s1, job.area, job.src_idx,
+                                                                  job.ns, npad,
+                                                                  static_cast<PlaneStreamF32::Rec*>(job.src_buf));
+      launch_sweep<PlaneStreamF32, kStreamThreads, kStreamTpt, kStreamTile, kStreamMinB>(
+          job, plan, PlaneStreamF32::Params{job.x, job.y});
+      finish_stream_kernel<<<fin_grid, pb, 0, job.stream>>>(job.partial, plan.nsplit, job.nt, 1, 0.0, nullptr, nullptr,
+                                                            job.out0, nullptr);
       break;
     }
     default:
@@ -796,8 +957,6 @@ extern "C" int lpm_bve_stream_functions(int64_t n, const double* x, const double
   LPM_TRY(lpm::check_common(a, 2));
   if (!z || !absvort) return lpm::set_error(LPM_ERR_ARG, "null z or absvort array");
   if (!(radius > 0.0)) return lpm::set_error(LPM_ERR_ARG, "radius must be positive");
-  if ((mode & LPM_MODE_MASK) != LPM_MODE_FP64)
-    return lpm::set_error(LPM_ERR_ARG, "the stream functions are computed in LPM_MODE_FP64 only");
   return lpm::run_host(a, 2);
 }
 
@@ -807,7 +966,5 @@ extern "C" int lpm_plane_stream_function(int64_t n, const double* x, const doubl
   HostArgs a{lpm::kSumPlaneStream, n, x, y, nullptr, omega, nullptr, area, active, 1.0, 0.0, 0.0,
              i_begin, i_end, psi, nullptr, nullptr, mode};
   LPM_TRY(lpm::check_common(a, 1));
-  if ((mode & LPM_MODE_MASK) != LPM_MODE_FP64)
-    return lpm::set_error(LPM_ERR_ARG, "the stream function is computed in LPM_MODE_FP64 only");
   return lpm::run_host(a, 1);
 }

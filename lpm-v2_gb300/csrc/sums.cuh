@@ -25,8 +25,8 @@ enum SumKind : int {
   kSumPseK8Geo,       // PSE Laplacian, K8 + great-circle distance
   kSumPseGaussChord,  // PSE Laplacian, Gaussian + chord distance
   kSumPseK8Chord,     // PSE Laplacian, K8 + chord distance (plane)
-  kSumSphereStream,   // sphere stream functions (FP64 only)
-  kSumPlaneStream     // planar stream function (FP64 only)
+  kSumSphereStream,   // sphere stream functions
+  kSumPlaneStream     // planar stream function
 };
 
 // Inputs of one direct sum over particles [0, n): sources are the ns particles listed (in
@@ -60,6 +60,13 @@ struct SumJob {
   cudaStream_t stream = nullptr;
 };
 
+// Split-K factor for a sweep of `blocks` target blocks over `tiles` source tiles on `slots`
+// resident CTA slots (SMs x CTAs per SM): the nsplit <= max_split that minimises
+// waves x (tiles per chunk + one tile of per-CTA cost), where waves = ceil(blocks x nsplit /
+// slots).  Equal-length CTAs run in lock-step waves, so a grid of 1.3 waves costs 2; this
+// picks a split whose last wave is nearly full.  Ties go to the smaller split.
+int64_t choose_split(int64_t blocks, int64_t tiles, int64_t slots, int64_t max_split);
+
 // Decides tiles, split-K and (for the sphere BVE FP32C sweep) the CTA shape of a job on a
 // device with sm_count SMs.
 SumPlan plan_sum(int kind, int mode, int64_t ns, int64_t nt, int sm_count, int shape = 0);
@@ -76,10 +83,6 @@ int autotune_bve_shape(const SumJob& job, int sm_count, int* shape);
 SumPlan plan_sum_max(int kind, int mode, int64_t ns, int64_t nt, int sm_count);
 // Enqueues prep + sweep (+ finish) on job.stream.
 int launch_sum(const SumJob& job, const SumPlan& plan);
-
-// Kernels launched by launch_sum for a job (for launch counting; the Morton sort of a
-// host-buffer call is not included).
-int kernels_per_sum(int mode);
 
 // Whether the FP32C form of `kind` runs on Morton-sorted, tile-relative sources.
 bool sum_uses_sorted_sources(int kind, int mode);

@@ -73,10 +73,11 @@ def test_pse_bad_kernel_rejected(built_lib):
         built_lib.pse_plane_laplacian_at_particles(x, y, f, a, act, 0.1, kernel=0)
 
 
-def test_stream_fp32c_rejected(built_lib):
+def test_stream_bad_radius_rejected(built_lib):
     x, y, z, f, a, act = _tiny()
-    with pytest.raises(built_lib.LpmError):
-        built_lib.set_stream_functions_on_mesh(x, y, z, f, f, a, act, mode="fp32c")
+    with pytest.raises(built_lib.LpmError) as e:
+        built_lib.set_stream_functions_on_mesh(x, y, z, f, f, a, act, sphere_radius=0.0, mode="fp32c")
+    assert e.value.code == -1
 
 
 def test_no_gpu_fails_loudly(built_lib):

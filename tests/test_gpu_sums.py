@@ -216,3 +216,68 @@ def test_check_finite_flag(lg):
     with pytest.raises(lg.LpmError) as e:
         lg.bve_sphere_velocity(x, y, z, np.ones(n), np.ones(n), act, 1.0, mode=lg.MODE_FP64 | lg.FLAG_CHECK_FINITE)
     assert e.value.code == -4
+
+
+# ------------------------------------------------------------------ stream functions, FP32C
+# a^2 - x_i.x_j is formed without cancellation and the log runs on the MUFU unit (absolute
+# error ~2^-22 per term), so the bound is relative to max|psi| over the targets.
+STREAM_TOL = 1e-6
+
+
+def test_golden_stream_fp32c(lg):
+    g = np.load(GOLDEN / "bve_icos2.npz")
+    pr, pa = lg.set_stream_functions_on_mesh(g["x"], g["y"], g["z"], g["zeta"], g["absvort"], g["area"],
+                                             g["active"], 1.0, mode="fp32c")
+    assert rel_linf(pr, g["psi_rel"]) <= STREAM_TOL and rel_linf(pa, g["psi_abs"]) <= STREAM_TOL
+    gp = np.load(GOLDEN / "plane_quad3.npz")
+    ps = lg.set_stream_function_on_mesh(gp["x"], gp["y"], gp["omega"], gp["area"], gp["active"], mode="fp32c")
+    assert rel_linf(ps, gp["psi"]) <= STREAM_TOL
+
+
+@pytest.mark.parametrize("radius", [1.0, 6.37122e6])
+def test_sphere_stream_fp32c_vs_oracle(lg, wl, oracle_mod, radius):
+    """RH54 wave on a nest-4 icosahedral mesh, unit and Earth radius (absolute vorticity with
+    the Earth's rotation rate scaled to the radius)."""
+    c = wl.config_rh54_icos(4, seed=5)
+    x, y, z = c["x"] * radius, c["y"] * radius, c["z"] * radius
+    area = c["area"] * radius ** 2
+    absv = c["zeta"] + 2.0 * (2.0 * np.pi) * c["z"]
+    ref = oracle_mod.bve_stream(x, y, z, c["zeta"], absv, area, c["active"], radius)
+    got = lg.set_stream_functions_on_mesh(x, y, z, c["zeta"], absv, area, c["active"], radius, mode="fp32c")
+    assert rel_linf(got[0], ref[0]) <= STREAM_TOL and rel_linf(got[1], ref[1]) <= STREAM_TOL
+
+
+@pytest.mark.parametrize("n", [1, 2, 33, 257, 1000])
+def test_stream_fp32c_ragged_inactive_block(lg, oracle_mod, n):
+    """Odd sizes, random activity (inactive targets have no self term to remove), a block range,
+    and points slightly off the sphere (both signs of |x|^2 - a^2)."""
+    rng = np.random.default_rng(100 + n)
+    p = rng.normal(size=(3, n))
+    p /= np.linalg.norm(p, axis=0)
+    p *= 1.0 + 1e-9 * rng.normal(size=n)
+    zeta = rng.normal(size=n)
+    absv = zeta + rng.normal(size=n)
+    area = rng.uniform(0.5, 1.5, size=n) * 4 * np.pi / n
+    act = (rng.random(n) < 0.7).astype(np.int32)
+    if not act.any():
+        act[0] = 1
+    ib, ie = (n // 3 + 1, n) if n > 3 else (1, n)
+    ref = oracle_mod.bve_stream(p[0], p[1], p[2], zeta, absv, area, act)
+    got = lg.set_stream_functions_on_mesh(p[0], p[1], p[2], zeta, absv, area, act, 1.0, i_begin=ib, i_end=ie,
+                                          mode="fp32c")
+    sl = slice(ib - 1, ie)
+    # scale: max|psi|, or the sum of |zeta A| when psi nearly cancels (one active source)
+    mass = np.sum(np.abs(zeta * area) * act)
+    for got_c, ref_c in zip(got, ref):
+        assert np.abs(got_c[sl] - ref_c[sl]).max() <= STREAM_TOL * max(np.abs(ref_c[sl]).max(), mass)
+    q = rng.normal(size=(2, n))
+    pref = oracle_mod.plane_stream(q[0], q[1], zeta, area, act)
+    pgot = lg.set_stream_function_on_mesh(q[0], q[1], zeta, area, act, i_begin=ib, i_end=ie, mode="fp32c")
+    assert np.abs(pgot[sl] - pref[sl]).max() <= STREAM_TOL * max(np.abs(pref[sl]).max(), mass)
+
+
+def test_plane_stream_fp32c_dipoles(lg, wl, oracle_mod):
+    c = wl.config_colliding_dipoles(5)
+    ref = oracle_mod.plane_stream(c["x"], c["y"], c["omega"], c["area"], c["active"])
+    got = lg.set_stream_function_on_mesh(c["x"], c["y"], c["omega"], c["area"], c["active"], mode="fp32c")
+    assert rel_linf(got, ref) <= STREAM_TOL
