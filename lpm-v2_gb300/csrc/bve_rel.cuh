@@ -1,16 +1,19 @@
 // bve_rel.cuh -- the sphere-BVE FP32C sweep on spatially sorted sources in group-relative
 // coordinates (10-11 packed FP32x2 operations per target pair and source).
 //
-// Sources are Morton-ordered, so a group of kGroup consecutive sources covers a small patch
-// of the sphere.  Each source is stored relative to an origin o of its group as a two-float
-// offset (s_hi, s_lo) = rel2(p, o); once per group every target forms its own offset
-// (t_hi, t_lo) with exactly the same operations, so a self pair cancels bit for bit.  The
-// prep kernel picks o and a precision per group:
-//  - compact group (radius R about its centroid <= a/8 and <= 64 x the smallest spacing of
+// Sources are in Hilbert-curve order (sort.cu), so a group of kGroup consecutive sources
+// covers one connected patch of the sphere.  Each source is stored relative to an origin o
+// of its group as a two-float offset (s_hi, s_lo) = rel2(p, o); once per group every target
+// forms its own offset (t_hi, t_lo) with exactly the same operations, so a self pair
+// cancels bit for bit.  The prep kernel picks o and a precision per group:
+//  - compact group (radius R about its centroid <= a/2 and <= 64 x the smallest spacing of
 //    consecutive sources in the group): o = centroid and the pair difference is
-//    d = t_hi - s_hi, one subtraction per component.  Its rounding error is ~2^-23 R, so
-//    the velocity error is ~1e-7 R sum_j S_j/|d_j|^2 / |u|, about 1e-7 relative when R <= a/8
-//    on a quasi-uniform point set; the spacing guard sends clustered sets to the wide path;
+//    d = t_hi - s_hi, one subtraction per component.  The roundings of t_hi and s_hi are
+//    <= 2^-24 |t - o| and 2^-24 R: relative 2^-24 for a target far from the group, and an
+//    absolute 2^-24 R for one near it, which enters the near-field sum sum_j S_j / |d_j|^2
+//    that grows only like ln(1/h); the velocity error therefore scales with R, not R/h
+//    (emulated at icosahedral nests 5-6 it is 2-4e-8 relative for R <= a/8 and R <= a/2
+//    alike).  The spacing guard sends clustered point sets to the wide path;
 //  - wide group (sparse or clustered points): o = 0, so (s_hi, s_lo) are the absolute hi/lo
 //    parts and d = (t_hi - s_hi) + (t_lo - s_lo) keeps ~48 bits for near pairs.
 // A compact group whose sources all lie on the sphere to within |c_j| <= 2^-30 h^2 (h its
@@ -41,7 +44,7 @@ struct BveRel {
     float4 lo;  // o_lo.x, o_lo.y, o_lo.z, 1 if every c_j of the group is negligible
   };
   static constexpr int kGroup = 64;                 // sources per origin
-  static constexpr float kCompactRadius = 0.125f;  // on the unit sphere
+  static constexpr float kCompactRadius = 0.5f;  // on the unit sphere
   static constexpr float kCompactRatio = 64.0f;
 };
 
@@ -354,7 +357,7 @@ __device__ __forceinline__ void bve_rel_prep_tile(const double* x, const double*
   }
 }
 
-// Tile-relative records of the Morton-sorted source list `sorted` (ns entries, records
+// Tile-relative records of the Hilbert-sorted source list `sorted` (ns entries, records
 // ns..npad-1 inert) and the group origins: one CTA of TILE threads per tile.
 template <int TILE>
 __global__ void __launch_bounds__(TILE) bve_rel_prep_kernel(const double* x, const double* y, const double* z,

@@ -5,7 +5,7 @@
 // own tile-padded range of one packed source-record array.
 //
 // Sources: at the start of every velocity evaluation the active sources of all instances are
-// put in Morton order within their instance (one device sort on (instance, Morton code)
+// put in Hilbert-curve order within their instance (one device sort on (instance, curve index)
 // keys), and each instance's sources fill its own tile-padded range of group-relative
 // records -- the layout and arithmetic of the single-instance sweep (bve_rel.cuh).
 //
@@ -110,7 +110,7 @@ __global__ void __launch_bounds__(kThreads, kMinB) ensemble_sweep_kernel(EnsArgs
 }
 
 // Group-relative records of all instances: one CTA per (global) tile.  Tile t belongs to
-// instance tile_inst[t]; its sources are that instance's Morton-sorted sources
+// instance tile_inst[t]; its sources are that instance's Hilbert-sorted sources
 // sorted[src_start[k] + (t - tile_off[k]) * kTile + lane], valid below ns_k.
 __global__ void __launch_bounds__(kTile) ensemble_prep_kernel(const int32_t* tile_inst, const int64_t* tile_off,
                                                               const int64_t* src_start, const int64_t* ns_k,
@@ -239,7 +239,7 @@ struct lpm_ensemble {
   int64_t ns_total = 0;
   int32_t* act_idx = nullptr;   // active sources in instance order
   int32_t* act_grp = nullptr;   // their instance
-  int32_t* sorted = nullptr;    // Morton order within each instance
+  int32_t* sorted = nullptr;    // Hilbert-curve order within each instance
   void* sort_scratch = nullptr;
   size_t sort_bytes = 0;
   int32_t* tile_inst = nullptr;
@@ -303,7 +303,7 @@ struct lpm_ensemble {
       return LPM_OK;
     }
     if (n_tiles > 0) {
-      LPM_TRY(grouped_morton_sort(stream, ns_total, K, act_idx, act_grp, px, py, pz, inv_a, sort_scratch, sort_bytes,
+      LPM_TRY(grouped_curve_sort(stream, ns_total, K, act_idx, act_grp, px, py, pz, inv_a, sort_scratch, sort_bytes,
                                   sorted));
       ensemble_prep_kernel<<<static_cast<unsigned>(n_tiles), kTile, 0, stream>>>(
           tile_inst, d_tile_off, d_src_start, d_ns_k, sorted, px, py, pz, pq, area, radius, rec, org);
@@ -463,7 +463,7 @@ struct lpm_ensemble {
     LPM_TRY(upload_vec(&d_src_start, src_start));
     LPM_TRY(upload_vec(&d_ns_k, ns_k));
     LPM_TRY(dev_array(&sorted, std::max<int64_t>(ns_total, 1)));
-    sort_bytes = grouped_morton_sort_bytes(std::max<int64_t>(ns_total, 1), K);
+    sort_bytes = grouped_curve_sort_bytes(std::max<int64_t>(ns_total, 1), K);
     LPM_TRY(arena.alloc(sort_bytes, &sort_scratch));
     LPM_TRY(dev_array(&rec, std::max<int64_t>(n_tiles * kTile, 1)));
     LPM_TRY(dev_array(&org, std::max<int64_t>(n_tiles * (kTile / BveRel::kGroup), 1)));

@@ -281,13 +281,13 @@ struct lpm_bve_solver {
   int64_t kernel_launches = 0;
   int64_t step_kernels = 0;  // kernel nodes of the captured step graph
   bool timing = true;
-  // FP32C: Morton order of the sources, refreshed at the start of every step
+  // FP32C: Hilbert-curve order of the sources, refreshed at the start of every step
   void* sort_scratch = nullptr;
   size_t sort_bytes = 0;
   int32_t* sorted = nullptr;
 
   int sort_sources() {
-    return morton_sort(stream, ns, idx, x, y, z, 1.0 / radius, sort_scratch, sort_bytes, sorted);
+    return curve_sort(stream, ns, idx, x, y, z, 1.0 / radius, sort_scratch, sort_bytes, sorted);
   }
 
   SumJob job(const double* px, const double* py, const double* pz, const double* pq, int kind,
@@ -459,7 +459,7 @@ int bve_create(lpm_bve_solver* S, int64_t n, const double* x, const double* y, c
   if (S->ns > 0 && sum_uses_sorted_sources(kSumBve, mode)) {
     // FP32C: the sources are ordered spatially at the start of every step (inside the step's
     // graph), so tiles stay compact as the particles move; the order only affects rounding
-    S->sort_bytes = morton_sort_bytes(S->ns);
+    S->sort_bytes = curve_sort_bytes(S->ns);
     void* sorted = nullptr;
     LPM_TRY(S->arena.alloc(S->sort_bytes, &S->sort_scratch));
     LPM_TRY(S->arena.alloc(S->ns * sizeof(int32_t), &sorted));
@@ -516,7 +516,7 @@ extern "C" int lpm_bve_timestep(lpm_bve_solver* S, double dt, int n_steps, int r
   if (!S->exec || S->graph_dt != dt || S->graph_renorm != renorm) LPM_TRY(S->capture(dt, renorm));
   for (int s = 0; s < n_steps; ++s) {
     LPM_CUDA_TRY(cudaGraphLaunch(S->exec, S->stream));
-    // 4 stage kernels, 4 direct sums and (FP32C) the Morton sort of the sources
+    // 4 stage kernels, 4 direct sums and (FP32C) the Hilbert-curve sort of the sources
     S->kernel_launches += S->step_kernels;
     if (!S->timing) continue;
     LPM_TRY(S->check_status("lpm_bve_timestep"));

@@ -1,26 +1,21 @@
-// sort.cu -- spatial (Morton) ordering of the source particles on the device.
+// sort.cu -- spatial (Hilbert-curve) ordering of the source particles on the device.
 //
-// The FP32C sphere sweep stores every source relative to the origin of its tile, so the
-// tiles must be spatially compact: sources are ordered by the 30-bit Morton code of their
-// unit-scaled position (10 bits per axis), with a device radix sort (CUB).  The order only
+// The FP32C sphere sweep stores every source relative to the origin of its group of 64, so
+// groups must be spatially compact: sources are ordered by the 30-bit index, along a 3-D
+// Hilbert curve over a 2^10 grid per axis, of the cell holding their unit-scaled position,
+// with a device radix sort (CUB).  Consecutive Hilbert cells are face neighbours, so 64
+// consecutive sources form one connected patch (a Hilbert-curve order jumps across the grid at
+// its octant boundaries, which leaves some groups in two distant pieces).  The order only
 // affects rounding (the FP32C sum is order-independent to its error bound); FP64 sums keep
 // the reference's ascending order.
 #include <cub/device/device_radix_sort.cuh>
 
 #include "lpm_common.cuh"
+#include "hilbert.cuh"
 #include "sort.cuh"
 
 namespace lpm {
 namespace {
-
-__device__ __forceinline__ uint32_t spread10(uint32_t v) {
-  v &= 0x3ffu;
-  v = (v | (v << 16)) & 0x030000ffu;
-  v = (v | (v << 8)) & 0x0300f00fu;
-  v = (v | (v << 4)) & 0x030c30c3u;
-  v = (v | (v << 2)) & 0x09249249u;
-  return v;
-}
 
 __device__ __forceinline__ uint32_t quant10(double p) {
   double t = (p + 1.0) * 512.0;
@@ -28,18 +23,21 @@ __device__ __forceinline__ uint32_t quant10(double p) {
   return static_cast<uint32_t>(t);
 }
 
-__global__ void morton_keys_kernel(int64_t ns, const int32_t* idx, const double* x, const double* y,
+__device__ __forceinline__ uint32_t cell_key(double px, double py, double pz) {
+  return hilbert_index30(quant10(px), quant10(py), quant10(pz));
+}
+
+__global__ void curve_keys_kernel(int64_t ns, const int32_t* idx, const double* x, const double* y,
                                    const double* z, double inv_a, uint32_t* keys, int32_t* vals) {
   const int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (k >= ns) return;
   const int32_t j = idx[k];
-  const double px = x[j] * inv_a, py = y[j] * inv_a, pz = z ? z[j] * inv_a : 0.0;
-  keys[k] = spread10(quant10(px)) | (spread10(quant10(py)) << 1) | (spread10(quant10(pz)) << 2);
+  keys[k] = cell_key(x[j] * inv_a, y[j] * inv_a, z ? z[j] * inv_a : 0.0);
   vals[k] = j;
 }
 
-// 64-bit keys: the group in the high bits, the Morton code of the group-scaled position low.
-__global__ void grouped_morton_keys_kernel(int64_t ns, const int32_t* idx, const int32_t* grp, const double* x,
+// 64-bit keys: the group in the high bits, the curve index of the group-scaled position low.
+__global__ void grouped_curve_keys_kernel(int64_t ns, const int32_t* idx, const int32_t* grp, const double* x,
                                            const double* y, const double* z, const double* inv_a, uint64_t* keys,
                                            int32_t* vals) {
   const int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -47,9 +45,7 @@ __global__ void grouped_morton_keys_kernel(int64_t ns, const int32_t* idx, const
   const int32_t j = idx[k];
   const int32_t g = grp[k];
   const double s = inv_a[g];
-  const double px = x[j] * s, py = y[j] * s, pz = z[j] * s;
-  const uint32_t m = spread10(quant10(px)) | (spread10(quant10(py)) << 1) | (spread10(quant10(pz)) << 2);
-  keys[k] = (static_cast<uint64_t>(g) << 30) | m;
+  keys[k] = (static_cast<uint64_t>(g) << 30) | cell_key(x[j] * s, y[j] * s, z[j] * s);
   vals[k] = j;
 }
 
@@ -61,7 +57,7 @@ int end_bit_for(int n_groups) {
 
 }  // namespace
 
-size_t grouped_morton_sort_bytes(int64_t ns, int n_groups) {
+size_t grouped_curve_sort_bytes(int64_t ns, int n_groups) {
   size_t temp = 0;
   cub::DeviceRadixSort::SortPairs(nullptr, temp, static_cast<const uint64_t*>(nullptr), static_cast<uint64_t*>(nullptr),
                                   static_cast<const int32_t*>(nullptr), static_cast<int32_t*>(nullptr),
@@ -69,7 +65,7 @@ size_t grouped_morton_sort_bytes(int64_t ns, int n_groups) {
   return align_up(temp, 256) + 2 * align_up(static_cast<size_t>(ns) * 8, 256) + align_up(static_cast<size_t>(ns) * 4, 256);
 }
 
-int grouped_morton_sort(cudaStream_t stream, int64_t ns, int n_groups, const int32_t* idx, const int32_t* grp,
+int grouped_curve_sort(cudaStream_t stream, int64_t ns, int n_groups, const int32_t* idx, const int32_t* grp,
                         const double* x, const double* y, const double* z, const double* inv_a, void* scratch,
                         size_t scratch_bytes, int32_t* sorted) {
   if (ns <= 0) return LPM_OK;
@@ -85,7 +81,7 @@ int grouped_morton_sort(cudaStream_t stream, int64_t ns, int n_groups, const int
   uint64_t* keys_in = reinterpret_cast<uint64_t*>(base + align_up(temp, 256));
   uint64_t* keys_out = reinterpret_cast<uint64_t*>(base + align_up(temp, 256) + k8);
   int32_t* vals_in = reinterpret_cast<int32_t*>(base + align_up(temp, 256) + 2 * k8);
-  grouped_morton_keys_kernel<<<static_cast<unsigned>(ceil_div(ns, 256)), 256, 0, stream>>>(ns, idx, grp, x, y, z,
+  grouped_curve_keys_kernel<<<static_cast<unsigned>(ceil_div(ns, 256)), 256, 0, stream>>>(ns, idx, grp, x, y, z,
                                                                                            inv_a, keys_in, vals_in);
   LPM_CUDA_TRY(cudaGetLastError());
   LPM_CUDA_TRY(cub::DeviceRadixSort::SortPairs(base, temp, keys_in, keys_out, vals_in, sorted, static_cast<int>(ns), 0,
@@ -93,7 +89,7 @@ int grouped_morton_sort(cudaStream_t stream, int64_t ns, int n_groups, const int
   return LPM_OK;
 }
 
-size_t morton_sort_bytes(int64_t ns) {
+size_t curve_sort_bytes(int64_t ns) {
   size_t temp = 0;
   cub::DeviceRadixSort::SortPairs(nullptr, temp, static_cast<const uint32_t*>(nullptr), static_cast<uint32_t*>(nullptr),
                                   static_cast<const int32_t*>(nullptr), static_cast<int32_t*>(nullptr),
@@ -102,7 +98,7 @@ size_t morton_sort_bytes(int64_t ns) {
   return align_up(temp, 256) + 3 * align_up(static_cast<size_t>(ns) * 4, 256);
 }
 
-int morton_sort(cudaStream_t stream, int64_t ns, const int32_t* idx, const double* x, const double* y,
+int curve_sort(cudaStream_t stream, int64_t ns, const int32_t* idx, const double* x, const double* y,
                 const double* z, double inv_a, void* scratch, size_t scratch_bytes, int32_t* sorted) {
   if (ns <= 0) return LPM_OK;
   size_t temp = 0;
@@ -111,13 +107,13 @@ int morton_sort(cudaStream_t stream, int64_t ns, const int32_t* idx, const doubl
                                   static_cast<int>(ns), 0, 30);
   const size_t arr = align_up(static_cast<size_t>(ns) * 4, 256);
   if (scratch_bytes < align_up(temp, 256) + 3 * arr)
-    return set_error(LPM_ERR_STATE, "morton sort scratch too small");
+    return set_error(LPM_ERR_STATE, "curve sort scratch too small");
   char* base = static_cast<char*>(scratch);
   void* d_temp = base;
   uint32_t* keys_in = reinterpret_cast<uint32_t*>(base + align_up(temp, 256));
   uint32_t* keys_out = reinterpret_cast<uint32_t*>(base + align_up(temp, 256) + arr);
   int32_t* vals_in = reinterpret_cast<int32_t*>(base + align_up(temp, 256) + 2 * arr);
-  morton_keys_kernel<<<static_cast<unsigned>(ceil_div(ns, 256)), 256, 0, stream>>>(ns, idx, x, y, z, inv_a, keys_in,
+  curve_keys_kernel<<<static_cast<unsigned>(ceil_div(ns, 256)), 256, 0, stream>>>(ns, idx, x, y, z, inv_a, keys_in,
                                                                                    vals_in);
   LPM_CUDA_TRY(cudaGetLastError());
   LPM_CUDA_TRY(cub::DeviceRadixSort::SortPairs(d_temp, temp, keys_in, keys_out, vals_in, sorted,

@@ -1,23 +1,23 @@
-// sort.cuh -- Morton ordering of source particles (device radix sort).
+// sort.cuh -- Hilbert-curve ordering of source particles (device radix sort).
 #pragma once
 
 #include "lpm_common.cuh"
 
 namespace lpm {
 
-// Scratch bytes morton_sort needs for ns sources.
-size_t morton_sort_bytes(int64_t ns);
+// Scratch bytes curve_sort needs for ns sources.
+size_t curve_sort_bytes(int64_t ns);
 
-// sorted[0..ns) = idx[0..ns) ordered by the Morton code of (x, y, z) * inv_a.  z may be NULL
+// sorted[0..ns) = idx[0..ns) ordered by the Hilbert-curve index of (x, y, z) * inv_a.  z may be NULL
 // (planar particles).  Enqueued on `stream`; no allocation.
-int morton_sort(cudaStream_t stream, int64_t ns, const int32_t* idx, const double* x, const double* y,
+int curve_sort(cudaStream_t stream, int64_t ns, const int32_t* idx, const double* x, const double* y,
                 const double* z, double inv_a, void* scratch, size_t scratch_bytes, int32_t* sorted);
 
-// Morton order within groups (ensemble instances): entries are ordered by group first, then
-// by the Morton code of (x, y, z) * inv_a[group]; idx/grp are the particle and group of each
+// Hilbert-curve order within groups (ensemble instances): entries are ordered by group first, then
+// by the Hilbert-curve index of (x, y, z) * inv_a[group]; idx/grp are the particle and group of each
 // entry.  n_groups < 2^33.
-size_t grouped_morton_sort_bytes(int64_t ns, int n_groups);
-int grouped_morton_sort(cudaStream_t stream, int64_t ns, int n_groups, const int32_t* idx, const int32_t* grp,
+size_t grouped_curve_sort_bytes(int64_t ns, int n_groups);
+int grouped_curve_sort(cudaStream_t stream, int64_t ns, int n_groups, const int32_t* idx, const int32_t* grp,
                         const double* x, const double* y, const double* z, const double* inv_a, void* scratch,
                         size_t scratch_bytes, int32_t* sorted);
 

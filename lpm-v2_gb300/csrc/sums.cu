@@ -550,7 +550,7 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
       const double inv_a = 1.0 / job.radius;
       const int32_t* src_list = job.src_idx;
       if (job.sort_scratch) {
-        LPM_TRY(morton_sort(job.stream, job.ns, job.src_idx, job.x, job.y, job.z, inv_a, job.sort_scratch,
+        LPM_TRY(curve_sort(job.stream, job.ns, job.src_idx, job.x, job.y, job.z, inv_a, job.sort_scratch,
                             job.sort_bytes, job.sorted));
         src_list = job.sorted;
       }
@@ -672,7 +672,7 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
 // ------------------------------------------------------------------ autotuner
 
 namespace {
-constexpr int64_t kTuneTargets = 64 * 1024;  // timing subset of the targets
+constexpr int64_t kTuneTargets = 256 * 1024;  // timing subset of the targets
 std::mutex g_tune_mu;
 std::map<std::tuple<int, int, int, int>, int> g_tune_cache;  // (kind, log2 ns, log2 nt, SMs) -> shape
 
@@ -847,7 +847,7 @@ int run_host(const HostArgs& a, int nout) {
     LPM_TRY(workspace(ctx, kWsSources, plan.src_bytes, &job.src_buf));
     if (sum_uses_sorted_sources(a.kind, prec)) {
       void* ps = nullptr;
-      const size_t sb = morton_sort_bytes(ns);
+      const size_t sb = curve_sort_bytes(ns);
       const size_t sorted_off = align_up(sb, 256);
       LPM_TRY(workspace(ctx, kWsScan, sorted_off + static_cast<size_t>(ns) * sizeof(int32_t), &ps));
       job.sort_scratch = ps;

@@ -48,7 +48,7 @@ struct SumJob {
   double* out0 = nullptr;  // u / lap / psi_rel   (length nt)
   double* out1 = nullptr;  // v / psi_abs
   double* out2 = nullptr;  // w
-  // FP32C sphere BVE: Morton-sort src_idx into `sorted` with this scratch before the sweep
+  // FP32C sphere BVE: Hilbert-sort src_idx into `sorted` with this scratch before the sweep
   // (sort_scratch == nullptr: src_idx is already spatially ordered and is used as is)
   void* sort_scratch = nullptr;
   size_t sort_bytes = 0;
@@ -84,7 +84,7 @@ SumPlan plan_sum_max(int kind, int mode, int64_t ns, int64_t nt, int sm_count);
 // Enqueues prep + sweep (+ finish) on job.stream.
 int launch_sum(const SumJob& job, const SumPlan& plan);
 
-// Whether the FP32C form of `kind` runs on Morton-sorted, tile-relative sources.
+// Whether the FP32C form of `kind` runs on Hilbert-sorted, tile-relative sources.
 bool sum_uses_sorted_sources(int kind, int mode);
 
 }  // namespace lpm

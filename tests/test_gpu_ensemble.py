@@ -63,7 +63,7 @@ def test_ensemble_fp32c_steps_track_fp64(lg, instances):
     vel = np.stack([a["u"] - b["u"], a["v"] - b["v"], a["w"] - b["w"]])
     assert np.abs(vel).max() / np.abs(np.stack([b["u"], b["v"], b["w"]])).max() < 2e-6
     ms, launches = e32.kernel_timing()
-    # per step: 4 stage kernels and 4 sums of (Morton keys, radix sort, prep, sweep, finish)
+    # per step: 4 stage kernels and 4 sums of (curve keys, radix sort, prep, sweep, finish)
     per_step, rem = divmod(launches, 5)
     assert ms > 0 and rem == 0 and per_step >= 4 + 4 * 5 and (per_step - 4) % 4 == 0
     e32.close()
