@@ -49,7 +49,7 @@ FLOPS_PER_INTERACTION = 24  # dot 5, a^2-dot 1, x4pi a 1, zeta A/den 2, cross 9,
 L2_FLUSH_BYTES = 256 << 20
 # DRAM bytes (read + write) of one full-size sweep launch, from the ncu capture recorded in
 # profiles/bve_rel_sweep_icos8_dram.md (ncu cannot run inside the timed benchmark)
-SWEEP_TRAFFIC_ICOS8 = 2_029_860_864 + 57_271_808
+SWEEP_TRAFFIC_ICOS8 = 240_612_864 + 119_981_568
 
 
 def parse_args():
@@ -64,7 +64,7 @@ def parse_args():
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline sample budget")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--workload", choices=["rk4", "ensemble"], default="rk4",
+    p.add_argument("--workload", choices=["rk4", "ensemble", "stream", "configs"], default="rk4",
                    help="rk4: the headline single-instance step; ensemble: the 64-instance batch")
     p.add_argument("--instances", type=int, default=64)
     return p.parse_args()
@@ -441,6 +441,156 @@ def run_ensemble(args):
     return 0
 
 
+def run_stream(args):
+    """The sphere stream functions (SetStreamFunctionsOnMesh, src/SphereBVE.f90:445-485: psi_rel
+    and psi_abs, a log-kernel sum called once per reference time step) in LPM_MODE_FP32C
+    through the host-buffer C ABI at icosahedral nest `--nest`, on the RK4 workload's
+    initial state (absolute vorticity zeta + 2 Omega z / a).  Each step is one call, host
+    copies included.  The FP64 mode of the same call is timed on a bounded block of targets,
+    and the FP32C result is checked against it on that block."""
+    import torch
+    import lpm_gpu as lg
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    c, n, ns, per_sum = workload(args.nest)
+    omega = 2.0 * np.pi
+    absv = c["zeta"] + 2.0 * omega * c["z"]
+    a = (c["x"], c["y"], c["z"], c["zeta"], absv, c["area"], c["active"], 1.0)
+    for _ in range(max(args.warmup, 3)):
+        lg.set_stream_functions_on_mesh(*a, mode="fp32c")
+    sampler = ClockSampler(gpu_id_for(torch, local))
+    sampler.start()
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        pr, pa = lg.set_stream_functions_on_mesh(*a, mode="fp32c")
+        times.append(time.perf_counter() - t0)
+    clocks = sampler.stop()
+    # FP64 on a block of 4096 targets in the middle of the particle range
+    ib = n // 3 + 1
+    m = 4096
+    lg.set_stream_functions_on_mesh(*a, i_begin=ib, i_end=ib + 255, mode="fp64")
+    t0 = time.perf_counter()
+    r64, a64 = lg.set_stream_functions_on_mesh(*a, i_begin=ib, i_end=ib + m - 1, mode="fp64")
+    t64 = time.perf_counter() - t0
+    sl = slice(ib - 1, ib - 1 + m)
+    err = max(float(np.abs(pr[sl] - r64[sl]).max() / np.abs(r64[sl]).max()),
+              float(np.abs(pa[sl] - a64[sl]).max() / np.abs(a64[sl]).max()))
+    t = sum(times) / len(times)
+    value = per_sum / t / 1e9
+    line = {
+        "metric": "sphere stream functions Ginteractions/s (psi_rel and psi_abs), FP32C, host-buffer C ABI",
+        "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3),
+        "ms_per_step": 1e3 * t, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": f"sphere stream functions, icosahedral nest {args.nest} ({n} targets, {ns} sources), "
+                               "RH4 + Gaussian vortex", "interactions_per_call": per_sum,
+                   "timing": "host wall clock around each lpm_bve_stream_functions call (H2D of the inputs, "
+                             "prep, sweep, finish, D2H of psi_rel and psi_abs)"},
+        "clocks": clocks,
+        "fp64_same_call": {"value": m * ns / t64 / 1e9, "unit": UNIT, "targets": f"{ib}..{ib + m - 1}"},
+        "accuracy": {"psi_rel_linf_vs_fp64": err, "targets": f"{ib}..{ib + m - 1}"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 6 * 8 * n + 4 * ns,
+                "d2h_bytes_per_step": 2 * 8 * n},
+        "gpu_launches": 4 * args.steps,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def _best_time(fn, reps=3):
+    fn()
+    best = 1e300
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        fn()
+        best = min(best, time.perf_counter() - t0)
+    return best
+
+
+def run_configs(args):
+    """The other configurations of the path, each timed on the GPU (FP64 parity mode and
+    FP32C, through the host-buffer C ABI or the solver handle) and on the host cores (the
+    oracle, a bounded block of targets where the full sum would take minutes):
+      C1 sphere BVE, icos nest 4, 100 RK4 steps of dt 0.01 (Gaussian vortex, Omega = 2 pi);
+      C2 planar velocity, quad nest 7 on [-4,4]^2, Lamb-dipole-like vortices, delta 0 and 0.02;
+      C3 PSE sphere Laplacian, cubed sphere nest 7, K8-geodesic and Gaussian-chord kernels.
+    Rates are Ginteractions/s; GPU times are host wall clock around the call (copies included)."""
+    import torch
+    import lpm_gpu as lg
+    import workloads as wl
+    from oracle import oracle as orc
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    out = {}
+    cores = os.cpu_count() or 1
+    # C1
+    c = wl.config_gauss_vortex_icos(4)
+    n, ns = c["x"].size, int(c["active"].sum())
+    steps = 100
+    per_step = 4 * (n * ns - ns)
+    row = {"size": f"icos nest 4: {n} targets, {ns} sources", "interactions_per_step": per_step}
+    u0 = lg.set_velocity_from_vorticity(c["x"], c["y"], c["z"], c["zeta"], c["area"], c["active"], 1.0)
+    for mode in ("fp64", "fp32c"):
+        s_ = lg.BVESolver(c["x"], c["y"], c["z"], c["zeta"], c["area"], c["active"], 1.0, c["omega"],
+                          u0[0], u0[1], u0[2], mode=mode)
+        s_.set_timing(False)
+        s_.timestep(0.01, 3)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s_.timestep(0.01, steps)
+        torch.cuda.synchronize()
+        row[f"gpu_{mode}"] = steps * per_step / (time.perf_counter() - t0) / 1e9
+        s_.close()
+    t0 = time.perf_counter()
+    orc.bve_timestep(c["x"], c["y"], c["z"], c["zeta"], c["area"], c["active"], u0[0], u0[1], u0[2], 1.0,
+                     c["omega"], 0.01, 10)
+    row["cpu_oracle"] = 10 * per_step / (time.perf_counter() - t0) / 1e9
+    row["cpu_sample"] = "10 RK4 steps, all targets"
+    out["C1_sphere_bve_rk4"] = row
+    # C2
+    c = wl.config_colliding_dipoles(7)
+    n, ns = c["x"].size, int(c["active"].sum())
+    per = n * ns - ns
+    row = {"size": f"quad nest 7 on [-4,4]^2: {n} targets, {ns} sources", "interactions_per_eval": per}
+    a = (c["x"], c["y"], c["omega"], c["area"], c["active"])
+    for delta in (0.0, 0.02):
+        for mode in ("fp64", "fp32c"):
+            t = _best_time(lambda: lg.planar_incompressible_velocity(*a, delta, mode=mode))
+            row[f"gpu_{mode}_delta{delta}"] = per / t / 1e9
+    m = 4096
+    t = _best_time(lambda: orc.plane_velocity(*a, 0.0, ib=n // 3, ie=n // 3 + m), reps=1)
+    row["cpu_oracle"] = m * ns / t / 1e9
+    row["cpu_sample"] = f"delta 0, {m} targets against all sources"
+    out["C2_planar_velocity"] = row
+    # C3
+    c = wl.config_pse_cubed(7)
+    n, ns = c["x"].size, int(c["active"].sum())
+    per = n * ns
+    row = {"size": f"cubed sphere nest 7: {n} targets, {ns} sources", "interactions_per_eval": per}
+    a = (c["x"], c["y"], c["z"], c["f"], c["area"], c["active"])
+    for name, kern, eps in (("k8_geodesic", lg.PSE_K8_GEODESIC, c["eps_k8"]),
+                            ("gauss_chord", lg.PSE_GAUSS_CHORD, c["eps_gauss"])):
+        t = _best_time(lambda: lg.pse_sphere_laplacian_at_particles(*a, eps, 1.0, kern, mode="fp32c"))
+        row[f"gpu_fp32c_{name}"] = per / t / 1e9
+        mb = 16384
+        t = _best_time(lambda: lg.pse_sphere_laplacian_at_particles(*a, eps, 1.0, kern, i_begin=1, i_end=mb,
+                                                                   mode="fp64"), reps=1)
+        row[f"gpu_fp64_{name}"] = mb * ns / t / 1e9
+        mc = 2048
+        t = _best_time(lambda: orc.pse_laplacian(*a, eps, 1.0, kern, ib=n // 3, ie=n // 3 + mc), reps=1)
+        row[f"cpu_oracle_{name}"] = mc * ns / t / 1e9
+    row["gpu_fp64_sample"] = "16384 targets against all sources"
+    row["cpu_sample"] = "2048 targets against all sources"
+    out["C3_pse_laplacian"] = row
+    line = {"metric": "direct-sum Ginteractions/s per configuration (GPU FP64 / FP32C, CPU oracle)",
+            "unit": UNIT, "cpu_cores": cores, "data": "synthetic", "configs": out}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def collections_counter(values):
     out = {}
     for v in values:
@@ -454,6 +604,10 @@ def main():
         return run_reference(args)
     if args.workload == "ensemble":
         return run_ensemble(args)
+    if args.workload == "stream":
+        return run_stream(args)
+    if args.workload == "configs":
+        return run_configs(args)
     return run_ours(args)
 
 
