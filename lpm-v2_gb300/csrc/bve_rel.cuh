@@ -2,27 +2,36 @@
 // coordinates (10-11 packed FP32x2 operations per target pair and source).
 //
 // Sources are in Hilbert-curve order (sort.cu), so a group of kGroup consecutive sources
-// covers one connected patch of the sphere.  Each source is stored relative to an origin o
-// of its group as a two-float offset (s_hi, s_lo) = rel2(p, o); once per group every target
-// forms its own offset (t_hi, t_lo) with exactly the same operations, so a self pair
-// cancels bit for bit.  The prep kernel picks o and a precision per group:
-//  - compact group (radius R about its centroid <= a/2 and <= 64 x the smallest spacing of
-//    consecutive sources in the group): o = centroid and the pair difference is
-//    d = t_hi - s_hi, one subtraction per component.  The roundings of t_hi and s_hi are
-//    <= 2^-24 |t - o| and 2^-24 R: relative 2^-24 for a target far from the group, and an
-//    absolute 2^-24 R for one near it, which enters the near-field sum sum_j S_j / |d_j|^2
-//    that grows only like ln(1/h); the velocity error therefore scales with R, not R/h
-//    (emulated at icosahedral nests 5-6 it is 2-4e-8 relative for R <= a/8 and R <= a/2
-//    alike).  The spacing guard sends clustered point sets to the wide path;
-//  - wide group (sparse or clustered points): o = 0, so (s_hi, s_lo) are the absolute hi/lo
-//    parts and d = (t_hi - s_hi) + (t_lo - s_lo) keeps ~48 bits for near pairs.
-// A compact group whose sources all lie on the sphere to within |c_j| <= 2^-30 h^2 (h its
-// smallest spacing; always the case once positions are renormalised) drops c_j: q is then
+// covers one connected patch of the sphere.  Each source is stored relative to the centroid
+// o of its group as a two-float offset (s_hi, s_lo) = rel2(p, o) (p - o to ~2^-48), and the
+// group record holds o and the group radius R (the largest |p_j - o|).  The precision is
+// chosen per warp and group:
+//  - far (every target of the warp at |t - o| >= 3R): d = t_hi - s_hi with t_hi = fl(t - o),
+//    one subtraction per component.  The roundings of t_hi and s_hi are <= 2^-24 |t - o|
+//    and 2^-24 R, and |d| >= |t - o| - R >= 2R, so the relative error of d is at most
+//    ~2^-23 whatever the point distribution;
+//  - near (some target of the warp inside 3R, which includes the group's own sources and any
+//    target at a source's position): the target forms (t_hi, t_lo) = rel2(t, o) with
+//    exactly the operations of the sources, and d = (t_hi - s_hi) + (t_lo - s_lo) keeps ~48
+//    bits; a self pair cancels bit for bit.
+// A compact group (R <= a/2 and R <= 64 x its smallest spacing h, i.e. a patch of a
+// quasi-uniform point set) takes the far form for every target: the group record carries
+// R = 0, and its records use rel2_fast, the target's far-form operations, so a self pair
+// still cancels bit for bit.  For a target near such a group the roundings are an absolute
+// 2^-24 R inside the near-field sum sum_j S_j / |d_j|^2, which grows only like ln(1/h) on a
+// quasi-uniform set, so the velocity error scales with R, not R/h (1.0e-7 relative at
+// icosahedral nest 8).  Groups that fail the test (clustered or sparse points) keep the
+// near/far choice, whose error bound holds for any point distribution.
+// Particle order along the mesh or the curve keeps a warp's targets close together, so a
+// warp meets few near groups (at icosahedral nest 8 about one group in a thousand).
+// A group whose sources all lie on the sphere to within |c_j| <= 2^-30 h^2 (h its smallest
+// spacing; always the case once positions are renormalised) drops c_j: q is then
 // fma(dz,dz, fma(dy,dy, fma(dx,dx, -c_i))), one operation less per pair.
 // Then  q = |d|^2 - c_i - c_j,  w = S_j / q,  D += w d  with c = |p|^2 - 1 and
-// S_j = -zeta_j A_j / (2 pi a) as in BveF32; u = D x p_i in FP64.  A compact group costs
-// 11 packed FP32x2 operations per target pair and source (10 on the sphere), a wide one 17;
-// forming the targets' offsets costs 12 per pair and group.
+// S_j = -zeta_j A_j / (2 pi a) as in BveF32; u = D x p_i in FP64.  Far: 10 packed FP32x2
+// operations per target pair and source on the sphere (11 off it); near: 17.  Forming the
+// targets' offsets and the near test cost about 15 per pair and group (33 more for a near
+// group).
 // Targets keep their original order (only sources are sorted), so no scatter is needed.
 #pragma once
 
@@ -40,27 +49,53 @@ struct BveRel {
     float4 d;  // -sx_lo, -sx_lo, -sy_lo, -sy_lo
   };
   struct __align__(16) Origin {
-    float4 hi;  // o_hi.x, o_hi.y, o_hi.z, 1 if the group is wide
+    float4 hi;  // o_hi.x, o_hi.y, o_hi.z, R (the group radius about o)
     float4 lo;  // o_lo.x, o_lo.y, o_lo.z, 1 if every c_j of the group is negligible
   };
-  static constexpr int kGroup = 64;                 // sources per origin
-  static constexpr float kCompactRadius = 0.5f;  // on the unit sphere
-  static constexpr float kCompactRatio = 64.0f;
+  static constexpr int kGroup = 64;           // sources per origin
+  static constexpr float kNearFactor = 3.0f;  // near: |t - o| < kNearFactor R
+  static constexpr float kCompactRadius = 0.5f;  // compact: R <= kCompactRadius (unit sphere)
+  static constexpr float kCompactRatio = 64.0f;  // and R <= kCompactRatio h
 };
 
-// Two-float offset of a hi/lo value from a hi/lo origin: (r_hi, r_lo) with r_hi + r_lo ~ p - o.
-__device__ __forceinline__ void rel2(float ph, float pl, float oh, float ol, float& rh, float& rl) {
+// Offset of a hi/lo value from a hi/lo origin, rounded once: fl(p - o) to ~2^-24 relative
+// (the far form needs no more).
+__device__ __forceinline__ float2 rel1x2(float2 ph, float2 pl, float oh, float ol) {
+  return __fadd2_rn(__fadd2_rn(ph, make_float2(-oh, -oh)), __fadd2_rn(pl, make_float2(-ol, -ol)));
+}
+
+// The same offset as two floats from single roundings: r_hi = rel1 (the far form's target
+// offset), r_lo the rounding of its last addition only.  Records of compact groups use it,
+// so that a target at a source's position reproduces that source's r_hi bit for bit.
+__device__ __forceinline__ void rel2_fast(float ph, float pl, float oh, float ol, float& rh, float& rl) {
   const float a = __fadd_rn(ph, -oh);
   const float b = __fadd_rn(pl, -ol);
   rh = __fadd_rn(a, b);
   rl = __fadd_rn(__fadd_rn(a, -rh), b);
 }
 
+// Two-float offset (r_hi, r_lo) of a hi/lo value from a hi/lo origin, r_hi + r_lo = p - o to
+// ~2^-48 relative: the TwoSum of (p_hi, -o_hi) keeps the rounding of the leading difference
+// (it is not exact when o is far from p), then the small terms are added and renormalised.
+__device__ __forceinline__ void rel2(float ph, float pl, float oh, float ol, float& rh, float& rl) {
+  const float s = __fadd_rn(ph, -oh);
+  const float v = __fadd_rn(s, -ph);
+  const float e = __fadd_rn(__fadd_rn(ph, -__fadd_rn(s, -v)), __fadd_rn(-oh, -v));
+  const float r = __fadd_rn(e, __fadd_rn(pl, -ol));
+  rh = __fadd_rn(s, r);
+  rl = __fadd_rn(r, -__fadd_rn(rh, -s));
+}
+
 __device__ __forceinline__ void rel2x2(float2 ph, float2 pl, float oh, float ol, float2& rh, float2& rl) {
-  const float2 a = __fadd2_rn(ph, make_float2(-oh, -oh));
-  const float2 b = __fadd2_rn(pl, make_float2(-ol, -ol));
-  rh = __fadd2_rn(a, b);
-  rl = __fadd2_rn(__fadd2_rn(a, make_float2(-rh.x, -rh.y)), b);
+  const float2 noh = make_float2(-oh, -oh);
+  const float2 s = __fadd2_rn(ph, noh);
+  const float2 v = __fadd2_rn(s, make_float2(-ph.x, -ph.y));
+  const float2 sv = __fadd2_rn(s, make_float2(-v.x, -v.y));
+  const float2 e = __fadd2_rn(__fadd2_rn(ph, make_float2(-sv.x, -sv.y)), __fadd2_rn(noh, make_float2(-v.x, -v.y)));
+  const float2 r = __fadd2_rn(e, __fadd2_rn(pl, make_float2(-ol, -ol)));
+  rh = __fadd2_rn(s, r);
+  const float2 d = __fadd2_rn(rh, make_float2(-s.x, -s.y));
+  rl = __fadd2_rn(r, make_float2(-d.x, -d.y));
 }
 
 // Target pairs of a sweep: thread t holds targets first + t + (2p + h) * threads, clamped
@@ -85,6 +120,21 @@ __device__ __forceinline__ void bve_load_pairs(const BveF32::Params& prm, int64_
   }
 }
 
+// Whether any target of the warp lies within kNearFactor R of a group origin (t = t_hi,
+// the offsets from it).  Every lane of the warp must call it.
+template <int NP>
+__device__ __forceinline__ bool warp_near(const float2 (&tx)[NP], const float2 (&ty)[NP], const float2 (&tz)[NP],
+                                          float r) {
+  const float lim = (BveRel::kNearFactor * r) * (BveRel::kNearFactor * r);
+  bool near = false;
+#pragma unroll
+  for (int p = 0; p < NP; ++p) {
+    const float2 n2 = __ffma2_rn(tz[p], tz[p], __ffma2_rn(ty[p], ty[p], __fmul2_rn(tx[p], tx[p])));
+    near |= (n2.x < lim) | (n2.y < lim);
+  }
+  return __any_sync(0xffffffffu, near);
+}
+
 // One staged tile against NP target pairs: FP32 partials of D added into (ax, ay, az).
 template <int NP, int TILE>
 __device__ __forceinline__ void bve_rel_tile(const BveRel::Rec* __restrict__ tl, const BveRel::Origin* __restrict__ og,
@@ -95,15 +145,15 @@ __device__ __forceinline__ void bve_rel_tile(const BveRel::Rec* __restrict__ tl,
   for (int g0 = 0; g0 < TILE; g0 += G) {
     const BveRel::Origin o = og[g0 / G];
     const BveRel::Rec* gr = tl + g0;
-    if (o.hi.w == 0.f) {
-      // compact group: d = t_hi - s_hi
-      float2 tx[NP], ty[NP], tz[NP], unused;
+    float2 tx[NP], ty[NP], tz[NP];
 #pragma unroll
-      for (int p = 0; p < NP; ++p) {
-        rel2x2(pr[p].xh, pr[p].xl, o.hi.x, o.lo.x, tx[p], unused);
-        rel2x2(pr[p].yh, pr[p].yl, o.hi.y, o.lo.y, ty[p], unused);
-        rel2x2(pr[p].zh, pr[p].zl, o.hi.z, o.lo.z, tz[p], unused);
-      }
+    for (int p = 0; p < NP; ++p) {
+      tx[p] = rel1x2(pr[p].xh, pr[p].xl, o.hi.x, o.lo.x);
+      ty[p] = rel1x2(pr[p].yh, pr[p].yl, o.hi.y, o.lo.y);
+      tz[p] = rel1x2(pr[p].zh, pr[p].zl, o.hi.z, o.lo.z);
+    }
+    if (!warp_near<NP>(tx, ty, tz, o.hi.w)) {
+      // far group: d = t_hi - s_hi
       if (o.lo.w != 0.f) {
         // every source of the group on the sphere: c_j dropped
 #pragma unroll 2
@@ -148,7 +198,7 @@ __device__ __forceinline__ void bve_rel_tile(const BveRel::Rec* __restrict__ tl,
         }
       }
     } else {
-      // wide group (o = 0): d = (t_hi - s_hi) + (t_lo - s_lo)
+      // near group: d = (t_hi - s_hi) + (t_lo - s_lo)
       float2 txh[NP], tyh[NP], tzh[NP], txl[NP], tyl[NP], tzl[NP];
 #pragma unroll
       for (int p = 0; p < NP; ++p) {
@@ -253,10 +303,10 @@ __global__ void __launch_bounds__(THREADS, MINB) bve_rel_sweep_kernel(SweepArgs<
 
 // Records and origins of one tile of TILE sources (one CTA of TILE threads; every thread
 // one record).  `j` is the thread's particle (meaningful only if `valid`), `inv_a` and
-// `s_scale` the tile's sphere scale.  Each group of kGroup sources reduces its centroid,
-// its radius about the centroid, the smallest distance between consecutive sources and its
-// largest |c_j|, picks compact (o = centroid) or wide (o = 0), and every record is written
-// as rel2(p_j, o) -- the operations the sweep uses for targets.
+// `s_scale` the tile's sphere scale.  Each group of kGroup sources reduces its centroid o,
+// its radius R about o, the smallest distance between consecutive sources and its largest
+// |c_j|, and every record is written as rel2(p_j, o) (rel2_fast for a compact group) -- the
+// operations the sweep uses for targets.
 template <int TILE>
 __device__ __forceinline__ void bve_rel_prep_tile(const double* x, const double* y, const double* z,
                                                   const double* zeta, const double* area, bool valid, int32_t j,
@@ -319,24 +369,23 @@ __device__ __forceinline__ void bve_rel_prep_tile(const double* x, const double*
     __syncthreads();
   }
   const float grad = fmax_[g0], gspc = fmin_[g0], gcmax = cmax_[g0];
-  const bool wide = !(grad <= BveRel::kCompactRadius && grad <= BveRel::kCompactRatio * gspc);
+  const bool compact = grad <= BveRel::kCompactRadius && grad <= BveRel::kCompactRatio * gspc;
   // on the sphere: dropping every c_j moves q by <= 2^-30 h^2 relative to the smallest |d|^2
   const bool on_sphere = gcmax <= 9.313225746154785e-10f * gspc * gspc;
-  float oxh = 0.f, oxl = 0.f, oyh = 0.f, oyl = 0.f, ozh = 0.f, ozl = 0.f;
-  if (!wide) {
-    split2(cx, oxh, oxl);
-    split2(cy, oyh, oyl);
-    split2(cz, ozh, ozl);
-  }
+  float oxh, oxl, oyh, oyl, ozh, ozl;
+  split2(cx, oxh, oxl);
+  split2(cy, oyh, oyl);
+  split2(cz, ozh, ozl);
   BveRel::Rec r;
   if (valid) {
     float h, l, sxh, sxl, syh, syl, szh, szl;
+    const auto rel = compact ? rel2_fast : rel2;
     split2(px, h, l);
-    rel2(h, l, oxh, oxl, sxh, sxl);
+    rel(h, l, oxh, oxl, sxh, sxl);
     split2(py, h, l);
-    rel2(h, l, oyh, oyl, syh, syl);
+    rel(h, l, oyh, oyl, syh, syl);
     split2(pz, h, l);
-    rel2(h, l, ozh, ozl, szh, szl);
+    rel(h, l, ozh, ozl, szh, szl);
     const float nc = __double2float_rn(-cj);
     const float s = __double2float_rn(zeta[j] * area[j] * s_scale);
     r.a = make_float4(-sxh, -sxh, -syh, -syh);
@@ -351,8 +400,8 @@ __device__ __forceinline__ void bve_rel_prep_tile(const double* x, const double*
   *out = r;
   if (lane == 0) {
     BveRel::Origin o;
-    o.hi = make_float4(oxh, oyh, ozh, wide ? 1.f : 0.f);
-    o.lo = make_float4(oxl, oyl, ozl, (!wide && on_sphere) ? 1.f : 0.f);
+    o.hi = make_float4(oxh, oyh, ozh, compact ? 0.f : grad);  // R = 0: never near
+    o.lo = make_float4(oxl, oyl, ozl, on_sphere ? 1.f : 0.f);
     og[tid / G] = o;
   }
 }

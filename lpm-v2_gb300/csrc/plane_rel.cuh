@@ -1,0 +1,247 @@
+// plane_rel.cuh -- the planar Biot-Savart FP32C sweep on spatially sorted sources in
+// group-relative coordinates (7 packed FP32x2 operations per target pair and source).
+//
+// Reference: planarIncompressibleVelocity, src/PlaneIncompressibleSolver.f90:291-308:
+//   u_i = -sum_j S_j (y_i - y_j) / (r^2 + delta^2),  v_i = sum_j S_j (x_i - x_j) / (r^2 + delta^2)
+// with S_j = omega_j A_j / (2 pi) (delta = 0 in the reference, delta > 0 the regularised
+// extension).  The structure is that of the sphere sweep (bve_rel.cuh): sources in 2-D
+// Hilbert-curve order (sort.cu), each group of kGroup sources stored relative to its
+// centroid o as rel2(p, o) with the group radius R, and per warp and group a far form
+// d = t_hi - s_hi (every target at |t - o| >= 3R: relative error <= ~2^-23) or a near form
+// in which each target forms (t_hi, t_lo) = rel2(t, o) with the sources' operations and
+// keeps the lo parts (a self pair cancels bit for bit; delta^2 carries a 2^-100 offset so
+// that the self weight is finite).  Per target pair and source, far:
+//   d (2 FADD2), q = d.d + delta^2 (2 FFMA2), w = S rcp(q) (FMUL2 + 2 MUFU),
+//   U += w dy, V += w dx (2 FFMA2);
+// near: 4 more FADD2.  Each tile's FP32 partial goes into compensated (hi, lo) pairs; the
+// FP64 finish reduces the split-K chunks and sets u = -U, v = V.
+#pragma once
+
+#include "bve_x2.cuh"
+#include "bve_rel.cuh"
+#include "engine.cuh"
+#include "ops.cuh"
+
+namespace lpm {
+
+struct PlaneRel {
+  struct __align__(16) Rec {
+    float4 a;  // -sx_hi, -sx_hi, -sy_hi, -sy_hi
+    float4 b;  // S_j, S_j, -sx_lo, -sx_lo
+    float4 c;  // -sy_lo, -sy_lo, 0, 0
+  };
+  struct __align__(16) Origin {
+    float4 o;  // o_hi.x, o_hi.y, o_lo.x, o_lo.y
+    float4 f;  // R (the group radius about o), 0, 0, 0
+  };
+  struct Pair {
+    float2 xh, yh, xl, yl;
+  };
+  static constexpr int kGroup = 64;
+  static constexpr float kNearFactor = 3.0f;  // near: |t - o| < kNearFactor R
+};
+
+struct PlaneRelArgs {
+  const double *x, *y;
+  float d2;  // delta^2 + 2^-100
+  const PlaneRel::Rec* src;
+  const PlaneRel::Origin* org;
+  int64_t n_tiles, tiles_per_chunk, ib, nt;
+  double* partial;  // [chunk][2][nt]
+  int* status;
+};
+
+template <int THREADS, int TPT, int TILE, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB) plane_rel_sweep_kernel(PlaneRelArgs a) {
+  static_assert(TPT % 2 == 0, "targets come in pairs");
+  static_assert(TILE % PlaneRel::kGroup == 0, "whole origin groups per tile");
+  constexpr int NP = TPT / 2;
+  constexpr int G = PlaneRel::kGroup;
+  constexpr int GPT = TILE / G;
+  using Rec = PlaneRel::Rec;
+  __shared__ __align__(128) Rec stage[2][TILE];
+  __shared__ __align__(8) uint64_t bars[2];
+
+  const int64_t chunk = blockIdx.y;
+  const int64_t tile0 = chunk * a.tiles_per_chunk;
+  int64_t ntl = a.n_tiles - tile0;
+  if (ntl > a.tiles_per_chunk) ntl = a.tiles_per_chunk;
+  if (ntl < 0) ntl = 0;
+
+  PlaneRel::Pair pr[NP];
+  float2 hu[NP], hv[NP], lu[NP], lv[NP];
+  const int64_t first = static_cast<int64_t>(blockIdx.x) * (THREADS * TPT);
+  const int64_t count = a.nt - first < THREADS * TPT ? a.nt - first : THREADS * TPT;
+#pragma unroll
+  for (int p = 0; p < NP; ++p) {
+    int64_t i0 = (2 * p) * THREADS + threadIdx.x, i1 = (2 * p + 1) * THREADS + threadIdx.x;
+    if (i0 >= count) i0 = count - 1;  // duplicates of a valid target; results not stored
+    if (i1 >= count) i1 = count - 1;
+    float h0, l0, h1, l1;
+    split2(a.x[a.ib + first + i0], h0, l0);
+    split2(a.x[a.ib + first + i1], h1, l1);
+    pr[p].xh = make_float2(h0, h1);
+    pr[p].xl = make_float2(l0, l1);
+    split2(a.y[a.ib + first + i0], h0, l0);
+    split2(a.y[a.ib + first + i1], h1, l1);
+    pr[p].yh = make_float2(h0, h1);
+    pr[p].yl = make_float2(l0, l1);
+    hu[p] = hv[p] = lu[p] = lv[p] = make_float2(0.f, 0.f);
+  }
+  const float2 d2 = make_float2(a.d2, a.d2);
+
+  pipe_init(bars);
+  uint32_t g = 0;
+  int64_t tile = tile0;
+  staged_sweep<Rec, TILE>(a.src, tile0, ntl, stage[0], stage[1], bars, g, a.status, [&](const Rec* tl) {
+    float2 au[NP], av[NP];
+#pragma unroll
+    for (int p = 0; p < NP; ++p) au[p] = av[p] = make_float2(0.f, 0.f);
+    const PlaneRel::Origin* og = a.org + tile * GPT;
+#pragma unroll 1
+    for (int g0 = 0; g0 < TILE; g0 += G) {
+      const PlaneRel::Origin o = og[g0 / G];
+      const Rec* gr = tl + g0;
+      float2 tx[NP], ty[NP];
+      bool near = false;
+      const float lim = (PlaneRel::kNearFactor * o.f.x) * (PlaneRel::kNearFactor * o.f.x);
+#pragma unroll
+      for (int p = 0; p < NP; ++p) {
+        tx[p] = rel1x2(pr[p].xh, pr[p].xl, o.o.x, o.o.z);
+        ty[p] = rel1x2(pr[p].yh, pr[p].yl, o.o.y, o.o.w);
+        const float2 n2 = __ffma2_rn(ty[p], ty[p], __fmul2_rn(tx[p], tx[p]));
+        near |= (n2.x < lim) | (n2.y < lim);
+      }
+      if (!__any_sync(0xffffffffu, near)) {
+        // far group: d = t_hi - s_hi
+#pragma unroll 4
+        for (int j = 0; j < G; ++j) {
+          const float4 ra = gr[j].a, rb = gr[j].b;
+          const float2 nsx = lo2(ra), nsy = hi2(ra), s2 = lo2(rb);
+#pragma unroll
+          for (int p = 0; p < NP; ++p) {
+            const float2 dx = __fadd2_rn(tx[p], nsx);
+            const float2 dy = __fadd2_rn(ty[p], nsy);
+            float2 q = __ffma2_rn(dx, dx, d2);
+            q = __ffma2_rn(dy, dy, q);
+            const float2 w = __fmul2_rn(s2, make_float2(rcp_approx(q.x), rcp_approx(q.y)));
+            au[p] = __ffma2_rn(w, dy, au[p]);
+            av[p] = __ffma2_rn(w, dx, av[p]);
+          }
+        }
+      } else {
+        // near group: d = (t_hi - s_hi) + (t_lo - s_lo)
+        float2 txh[NP], tyh[NP], txl[NP], tyl[NP];
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+          rel2x2(pr[p].xh, pr[p].xl, o.o.x, o.o.z, txh[p], txl[p]);
+          rel2x2(pr[p].yh, pr[p].yl, o.o.y, o.o.w, tyh[p], tyl[p]);
+        }
+        for (int j = 0; j < G; ++j) {
+          const float4 ra = gr[j].a, rb = gr[j].b, rc = gr[j].c;
+          const float2 nsx = lo2(ra), nsy = hi2(ra), s2 = lo2(rb), nlx = hi2(rb), nly = lo2(rc);
+#pragma unroll
+          for (int p = 0; p < NP; ++p) {
+            const float2 dx = __fadd2_rn(__fadd2_rn(txh[p], nsx), __fadd2_rn(txl[p], nlx));
+            const float2 dy = __fadd2_rn(__fadd2_rn(tyh[p], nsy), __fadd2_rn(tyl[p], nly));
+            float2 q = __ffma2_rn(dx, dx, d2);
+            q = __ffma2_rn(dy, dy, q);
+            const float2 w = __fmul2_rn(s2, make_float2(rcp_approx(q.x), rcp_approx(q.y)));
+            au[p] = __ffma2_rn(w, dy, au[p]);
+            av[p] = __ffma2_rn(w, dx, av[p]);
+          }
+        }
+      }
+    }
+    ++tile;
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+      comp_add(hu[p].x, lu[p].x, au[p].x);
+      comp_add(hu[p].y, lu[p].y, au[p].y);
+      comp_add(hv[p].x, lv[p].x, av[p].x);
+      comp_add(hv[p].y, lv[p].y, av[p].y);
+    }
+  });
+
+#pragma unroll
+  for (int p = 0; p < NP; ++p) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int64_t il = first + (2 * p + h) * THREADS + threadIdx.x;
+      if (il < a.nt) {
+        a.partial[(chunk * 2 + 0) * a.nt + il] =
+            static_cast<double>(h ? hu[p].y : hu[p].x) + static_cast<double>(h ? lu[p].y : lu[p].x);
+        a.partial[(chunk * 2 + 1) * a.nt + il] =
+            static_cast<double>(h ? hv[p].y : hv[p].x) + static_cast<double>(h ? lv[p].y : lv[p].x);
+      }
+    }
+  }
+}
+
+// Records and origins of one tile of TILE sources (one CTA of TILE threads): each group of
+// kGroup sources reduces its centroid o and its radius R about o, and every record is
+// written as rel2(p_j, o) -- the operations the sweep uses for targets.  s_scale = 1/(2 pi).
+template <int TILE>
+__global__ void __launch_bounds__(TILE) plane_rel_prep_kernel(const double* x, const double* y, const double* omega,
+                                                              const double* area, const int32_t* sorted, int64_t ns,
+                                                              double s_scale, PlaneRel::Rec* out,
+                                                              PlaneRel::Origin* org) {
+  constexpr int G = PlaneRel::kGroup;
+  __shared__ double red[2][TILE];
+  __shared__ float fmax_[TILE], cntf[TILE];
+  const int64_t t = blockIdx.x;
+  const int tid = threadIdx.x;
+  const int64_t k = t * TILE + tid;
+  const bool valid = k < ns;
+  const int32_t j = valid ? sorted[k] : 0;
+  const int lane = tid % G;
+  const double px = valid ? x[j] : 0.0, py = valid ? y[j] : 0.0;
+  red[0][tid] = px;
+  red[1][tid] = py;
+  cntf[tid] = valid ? 1.f : 0.f;
+  __syncthreads();
+  for (int w = G / 2; w > 0; w >>= 1) {
+    if (lane < w) {
+      red[0][tid] += red[0][tid + w];
+      red[1][tid] += red[1][tid + w];
+      cntf[tid] += cntf[tid + w];
+    }
+    __syncthreads();
+  }
+  const int g0 = tid - lane;
+  const double cnt = cntf[g0] > 0.f ? static_cast<double>(cntf[g0]) : 1.0;
+  const double cx = red[0][g0] / cnt, cy = red[1][g0] / cnt;
+  fmax_[tid] = valid ? static_cast<float>(sqrt((px - cx) * (px - cx) + (py - cy) * (py - cy))) : 0.f;
+  __syncthreads();
+  for (int w = G / 2; w > 0; w >>= 1) {
+    if (lane < w) fmax_[tid] = fmaxf(fmax_[tid], fmax_[tid + w]);
+    __syncthreads();
+  }
+  float oxh, oxl, oyh, oyl;
+  split2(cx, oxh, oxl);
+  split2(cy, oyh, oyl);
+  PlaneRel::Rec r;
+  if (valid) {
+    float h, l, sxh, sxl, syh, syl;
+    split2(px, h, l);
+    rel2(h, l, oxh, oxl, sxh, sxl);
+    split2(py, h, l);
+    rel2(h, l, oyh, oyl, syh, syl);
+    const float s = __double2float_rn(omega[j] * area[j] * s_scale);
+    r.a = make_float4(-sxh, -sxh, -syh, -syh);
+    r.b = make_float4(s, s, -sxl, -sxl);
+    r.c = make_float4(-syl, -syl, 0.f, 0.f);
+  } else {
+    // inert: at the origin with zero strength (q >= delta^2 + 2^-100 > 0)
+    r.a = r.b = r.c = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  out[k] = r;
+  if (lane == 0) {
+    PlaneRel::Origin o;
+    o.o = make_float4(oxh, oyh, oxl, oyl);
+    o.f = make_float4(fmax_[g0], 0.f, 0.f, 0.f);
+    org[t * (TILE / G) + tid / G] = o;
+  }
+}
+
+}  // namespace lpm

@@ -644,6 +644,12 @@ struct lpm_plane_solver {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   double graph_dt = 0.0;
+  // FP32C: 2-D Hilbert-curve order of the sources, refreshed at the start of every step
+  void* sort_scratch = nullptr;
+  size_t sort_bytes = 0;
+  int32_t* sorted = nullptr;
+
+  int sort_sources() { return curve_sort2d(stream, ns, idx, x, y, sort_scratch, sort_bytes, sorted); }
 
   int velocity(const double* px, const double* py, double* o0, double* o1) {
     if (ns == 0) {
@@ -659,7 +665,7 @@ struct lpm_plane_solver {
     j.y = py;
     j.s1 = om;
     j.area = area;
-    j.src_idx = idx;
+    j.src_idx = sorted ? sorted : idx;
     j.ns = ns;
     j.delta = delta;
     j.ib = 0;
@@ -675,6 +681,7 @@ struct lpm_plane_solver {
 
   int enqueue_step(double dt) {
     const unsigned g = static_cast<unsigned>(ceil_div(n, kStageThreads));
+    if (sorted) LPM_TRY(sort_sources());
     plane_stage1_kernel<<<g, kStageThreads, 0, stream>>>(n, dt, x, y, u, v, ax, ay, xin, yin);
     LPM_CUDA_TRY(cudaGetLastError());
     for (int s = 0; s < 3; ++s) {
@@ -760,10 +767,17 @@ int plane_create(lpm_plane_solver* S, int64_t n, const double* x, const double* 
     LPM_CUDA_TRY(cudaMemcpyAsync(S->idx, idx.data(), idx.size() * sizeof(int32_t), cudaMemcpyHostToDevice, S->stream));
   }
   LPM_TRY(S->scratch.init(S->arena, kSumPlane, mode, S->ns, n, S->ctx->sm_count));
+  if (S->ns > 0 && sum_uses_sorted_sources(kSumPlane, mode)) {
+    S->sort_bytes = curve_sort2d_bytes(S->ns);
+    LPM_TRY(S->arena.alloc(S->sort_bytes, &S->sort_scratch));
+    LPM_TRY(S->arena.alloc(S->ns * sizeof(int32_t), &p));
+    S->sorted = static_cast<int32_t*>(p);
+  }
   LPM_TRY(upload(S->stream, S->x, x, n));
   LPM_TRY(upload(S->stream, S->y, y, n));
   LPM_TRY(upload(S->stream, S->om, om, n));
   LPM_TRY(upload(S->stream, S->area, area, n));
+  if (S->sorted) LPM_TRY(S->sort_sources());
   if (u && v) {
     LPM_TRY(upload(S->stream, S->u, u, n));
     LPM_TRY(upload(S->stream, S->v, v, n));

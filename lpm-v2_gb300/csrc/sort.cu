@@ -49,6 +49,51 @@ __global__ void grouped_curve_keys_kernel(int64_t ns, const int32_t* idx, const 
   vals[k] = j;
 }
 
+// Bounding box {x_min, y_min, x_max, y_max} of the listed points: one block, a fixed order.
+__global__ void __launch_bounds__(1024) bbox2d_kernel(int64_t ns, const int32_t* idx, const double* x,
+                                                      const double* y, double* box) {
+  __shared__ double r[4][1024];
+  double a = 1e300, b = 1e300, c = -1e300, d = -1e300;
+  for (int64_t k = threadIdx.x; k < ns; k += 1024) {
+    const int32_t j = idx[k];
+    a = fmin(a, x[j]);
+    b = fmin(b, y[j]);
+    c = fmax(c, x[j]);
+    d = fmax(d, y[j]);
+  }
+  r[0][threadIdx.x] = a;
+  r[1][threadIdx.x] = b;
+  r[2][threadIdx.x] = c;
+  r[3][threadIdx.x] = d;
+  __syncthreads();
+  for (int w = 512; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      r[0][threadIdx.x] = fmin(r[0][threadIdx.x], r[0][threadIdx.x + w]);
+      r[1][threadIdx.x] = fmin(r[1][threadIdx.x], r[1][threadIdx.x + w]);
+      r[2][threadIdx.x] = fmax(r[2][threadIdx.x], r[2][threadIdx.x + w]);
+      r[3][threadIdx.x] = fmax(r[3][threadIdx.x], r[3][threadIdx.x + w]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x < 4) box[threadIdx.x] = r[threadIdx.x][0];
+}
+
+// 2-D keys: the Hilbert index of the cell of a 2^16 grid laid over the bounding box (one
+// scale for both axes, so cells are square).
+__global__ void curve2d_keys_kernel(int64_t ns, const int32_t* idx, const double* x, const double* y,
+                                    const double* box, uint32_t* keys, int32_t* vals) {
+  const int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= ns) return;
+  const int32_t j = idx[k];
+  const double ext = fmax(fmax(box[2] - box[0], box[3] - box[1]), 1e-300);
+  const double s = 65535.0 / ext;
+  double u = (x[j] - box[0]) * s, v = (y[j] - box[1]) * s;
+  u = u < 0.0 ? 0.0 : (u > 65535.0 ? 65535.0 : u);
+  v = v < 0.0 ? 0.0 : (v > 65535.0 ? 65535.0 : v);
+  keys[k] = hilbert_index2d(static_cast<uint32_t>(u), static_cast<uint32_t>(v));
+  vals[k] = j;
+}
+
 int end_bit_for(int n_groups) {
   int b = 0;
   while ((1 << b) < n_groups) ++b;
@@ -118,6 +163,40 @@ int curve_sort(cudaStream_t stream, int64_t ns, const int32_t* idx, const double
   LPM_CUDA_TRY(cudaGetLastError());
   LPM_CUDA_TRY(cub::DeviceRadixSort::SortPairs(d_temp, temp, keys_in, keys_out, vals_in, sorted,
                                                static_cast<int>(ns), 0, 30, stream));
+  return LPM_OK;
+}
+
+size_t curve_sort2d_bytes(int64_t ns) {
+  size_t temp = 0;
+  cub::DeviceRadixSort::SortPairs(nullptr, temp, static_cast<const uint32_t*>(nullptr), static_cast<uint32_t*>(nullptr),
+                                  static_cast<const int32_t*>(nullptr), static_cast<int32_t*>(nullptr),
+                                  static_cast<int>(ns), 0, 32);
+  // box, then the CUB temporary, keys in/out and values in
+  return 256 + align_up(temp, 256) + 3 * align_up(static_cast<size_t>(ns) * 4, 256);
+}
+
+int curve_sort2d(cudaStream_t stream, int64_t ns, const int32_t* idx, const double* x, const double* y,
+                 void* scratch, size_t scratch_bytes, int32_t* sorted) {
+  if (ns <= 0) return LPM_OK;
+  size_t temp = 0;
+  cub::DeviceRadixSort::SortPairs(nullptr, temp, static_cast<const uint32_t*>(nullptr), static_cast<uint32_t*>(nullptr),
+                                  static_cast<const int32_t*>(nullptr), static_cast<int32_t*>(nullptr),
+                                  static_cast<int>(ns), 0, 32);
+  const size_t arr = align_up(static_cast<size_t>(ns) * 4, 256);
+  if (scratch_bytes < 256 + align_up(temp, 256) + 3 * arr)
+    return set_error(LPM_ERR_STATE, "2-D curve sort scratch too small");
+  char* base = static_cast<char*>(scratch);
+  double* box = reinterpret_cast<double*>(base);
+  void* d_temp = base + 256;
+  uint32_t* keys_in = reinterpret_cast<uint32_t*>(base + 256 + align_up(temp, 256));
+  uint32_t* keys_out = reinterpret_cast<uint32_t*>(base + 256 + align_up(temp, 256) + arr);
+  int32_t* vals_in = reinterpret_cast<int32_t*>(base + 256 + align_up(temp, 256) + 2 * arr);
+  bbox2d_kernel<<<1, 1024, 0, stream>>>(ns, idx, x, y, box);
+  curve2d_keys_kernel<<<static_cast<unsigned>(ceil_div(ns, 256)), 256, 0, stream>>>(ns, idx, x, y, box, keys_in,
+                                                                                    vals_in);
+  LPM_CUDA_TRY(cudaGetLastError());
+  LPM_CUDA_TRY(cub::DeviceRadixSort::SortPairs(d_temp, temp, keys_in, keys_out, vals_in, sorted,
+                                               static_cast<int>(ns), 0, 32, stream));
   return LPM_OK;
 }
 

@@ -21,4 +21,10 @@ int grouped_curve_sort(cudaStream_t stream, int64_t ns, int n_groups, const int3
                         const double* x, const double* y, const double* z, const double* inv_a, void* scratch,
                         size_t scratch_bytes, int32_t* sorted);
 
+// Planar sources: sorted[0..ns) = idx[0..ns) ordered along a 2-D Hilbert curve over the
+// sources' bounding box.
+size_t curve_sort2d_bytes(int64_t ns);
+int curve_sort2d(cudaStream_t stream, int64_t ns, const int32_t* idx, const double* x, const double* y,
+                 void* scratch, size_t scratch_bytes, int32_t* sorted);
+
 }  // namespace lpm

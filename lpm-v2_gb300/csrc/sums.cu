@@ -11,6 +11,7 @@
 #include "bve_x2.cuh"
 #include "engine.cuh"
 #include "ops.cuh"
+#include "plane_rel.cuh"
 #include "sort.cuh"
 #include "sums.cuh"
 
@@ -120,29 +121,6 @@ __global__ void prep_stream64_kernel(const double* x, const double* y, const dou
   r.area = area[j];
   r.idx = j;
   r.pad = 0;
-  out[k] = r;
-}
-
-__global__ void prep_plane32_kernel(const double* x, const double* y, const double* omega,
-                                    const double* area, const int32_t* idx, int64_t ns,
-                                    int64_t npad, double s_scale, PlaneF32::Rec* out) {
-  const int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (k >= npad) return;
-  PlaneF32::Rec r;
-  if (k < ns) {
-    const int64_t j = idx[k];
-    float h, l;
-    split2(x[j], h, l);
-    r.a.x = h;
-    r.a.z = l;
-    split2(y[j], h, l);
-    r.a.y = h;
-    r.a.w = l;
-    r.b = make_float4(__double2float_rn(omega[j] * area[j] * s_scale), 0.f, 0.f, 0.f);
-  } else {
-    r.a = make_float4(0.f, 0.f, 0.f, 0.f);
-    r.b = make_float4(0.f, 0.f, 0.f, 0.f);
-  }
   out[k] = r;
 }
 
@@ -365,7 +343,7 @@ size_t rec_bytes(int kind, int mode) {
     case kSumBveMesh:
       return sizeof(BveRel::Rec);
     case kSumPlane:
-      return sizeof(PlaneF32::Rec);
+      return sizeof(PlaneRel::Rec);
     case kSumSphereStream:
       return sizeof(SphereStreamF32::Rec);
     case kSumPlaneStream:
@@ -425,7 +403,11 @@ int64_t choose_split(int64_t blocks, int64_t tiles, int64_t slots, int64_t max_s
 }
 
 bool sum_uses_sorted_sources(int kind, int mode) {
-  return mode == LPM_MODE_FP32C && (kind == kSumBve || kind == kSumBveMesh);
+  return mode == LPM_MODE_FP32C && (kind == kSumBve || kind == kSumBveMesh || kind == kSumPlane);
+}
+
+size_t sort_scratch_bytes(int kind, int64_t ns) {
+  return kind == kSumPlane ? curve_sort2d_bytes(ns) : curve_sort_bytes(ns);
 }
 
 int bve_shape_count() { return kBveShapeCount; }
@@ -438,7 +420,9 @@ SumPlan plan_sum(int kind, int mode, int64_t ns, int64_t nt, int sm_count, int s
   pl.n_tiles = ceil_div(ns > 0 ? ns : 1, tile);
   pl.src_bytes = static_cast<size_t>(pl.n_tiles) * tile * rec_bytes(kind, mode);
   if (sum_uses_sorted_sources(kind, mode)) {
-    // the per-tile origins follow the records
+    // the group origins follow the records
+    static_assert(sizeof(BveRel::Origin) == sizeof(PlaneRel::Origin) && BveRel::kGroup == PlaneRel::kGroup,
+                  "one origin layout size");
     pl.src_bytes = align_up(pl.src_bytes, 256) +
                    static_cast<size_t>(pl.n_tiles) * (tile / BveRel::kGroup) * sizeof(BveRel::Origin);
   }
@@ -590,11 +574,32 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
       break;
     }
     case kSumPlane: {
-      prep_plane32_kernel<<<prep_grid_pad, pb, 0, job.stream>>>(job.x, job.y, job.s1, job.area, job.src_idx,
-                                                                job.ns, npad, 1.0 / (2.0 * kPi),
-                                                                static_cast<PlaneF32::Rec*>(job.src_buf));
-      PlaneF32::Params p{job.x, job.y, static_cast<float>(job.delta * job.delta) + 7.888609052210118e-31f};
-      launch_sweep<PlaneF32, kPlaneThreads, kPlaneTpt, kPlaneTile, kPlaneMinB>(job, plan, p);
+      const int32_t* src_list = job.src_idx;
+      if (job.sort_scratch) {
+        LPM_TRY(curve_sort2d(job.stream, job.ns, job.src_idx, job.x, job.y, job.sort_scratch, job.sort_bytes,
+                             job.sorted));
+        src_list = job.sorted;
+      }
+      PlaneRel::Rec* recs = static_cast<PlaneRel::Rec*>(job.src_buf);
+      PlaneRel::Origin* org = reinterpret_cast<PlaneRel::Origin*>(
+          static_cast<char*>(job.src_buf) + align_up(static_cast<size_t>(npad) * sizeof(PlaneRel::Rec), 256));
+      plane_rel_prep_kernel<kPlaneTile><<<static_cast<unsigned>(plan.n_tiles), kPlaneTile, 0, job.stream>>>(
+          job.x, job.y, job.s1, job.area, src_list, job.ns, 1.0 / (2.0 * kPi), recs, org);
+      PlaneRelArgs a;
+      a.x = job.x;
+      a.y = job.y;
+      a.d2 = static_cast<float>(job.delta * job.delta) + 7.888609052210118e-31f;  // + 2^-100
+      a.src = recs;
+      a.org = org;
+      a.n_tiles = plan.n_tiles;
+      a.tiles_per_chunk = plan.tiles_per_chunk;
+      a.ib = job.ib;
+      a.nt = job.nt;
+      a.partial = job.partial;
+      a.status = job.status;
+      const dim3 grid(static_cast<unsigned>(ceil_div(job.nt, kPlaneThreads * kPlaneTpt)),
+                      static_cast<unsigned>(plan.nsplit));
+      plane_rel_sweep_kernel<kPlaneThreads, kPlaneTpt, kPlaneTile, kPlaneMinB><<<grid, kPlaneThreads, 0, job.stream>>>(a);
       finish_plane_kernel<<<fin_grid, pb, 0, job.stream>>>(job.partial, plan.nsplit, job.nt, job.out0,
                                                            job.out1);
       break;
@@ -685,7 +690,7 @@ int log2_bucket(int64_t v) {
 
 SumPlan plan_sum_max(int kind, int mode, int64_t ns, int64_t nt, int sm_count) {
   SumPlan best = plan_sum(kind, mode, ns, nt, sm_count, 0);
-  if (!sum_uses_sorted_sources(kind, mode)) return best;
+  if (!sum_uses_sorted_sources(kind, mode) || kind == kSumPlane) return best;
   const int64_t sub = nt < kTuneTargets ? nt : kTuneTargets;
   for (int sh = 0; sh < kBveShapeCount; ++sh) {
     for (const int64_t t : {nt, sub}) {
@@ -699,7 +704,7 @@ SumPlan plan_sum_max(int kind, int mode, int64_t ns, int64_t nt, int sm_count) {
 
 int autotune_bve_shape(const SumJob& job, int sm_count, int* shape) {
   *shape = 0;
-  if (!sum_uses_sorted_sources(job.kind, job.mode) || job.ns == 0) return LPM_OK;
+  if (!sum_uses_sorted_sources(job.kind, job.mode) || job.kind == kSumPlane || job.ns == 0) return LPM_OK;
   const auto key = std::make_tuple(job.kind == kSumBveMesh ? static_cast<int>(kSumBve) : job.kind,
                                    log2_bucket(job.ns), log2_bucket(job.nt), sm_count);
   std::lock_guard<std::mutex> lock(g_tune_mu);
@@ -847,7 +852,7 @@ int run_host(const HostArgs& a, int nout) {
     LPM_TRY(workspace(ctx, kWsSources, plan.src_bytes, &job.src_buf));
     if (sum_uses_sorted_sources(a.kind, prec)) {
       void* ps = nullptr;
-      const size_t sb = curve_sort_bytes(ns);
+      const size_t sb = sort_scratch_bytes(a.kind, ns);
       const size_t sorted_off = align_up(sb, 256);
       LPM_TRY(workspace(ctx, kWsScan, sorted_off + static_cast<size_t>(ns) * sizeof(int32_t), &ps));
       job.sort_scratch = ps;

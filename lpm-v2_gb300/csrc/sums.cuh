@@ -48,8 +48,9 @@ struct SumJob {
   double* out0 = nullptr;  // u / lap / psi_rel   (length nt)
   double* out1 = nullptr;  // v / psi_abs
   double* out2 = nullptr;  // w
-  // FP32C sphere BVE: Hilbert-sort src_idx into `sorted` with this scratch before the sweep
-  // (sort_scratch == nullptr: src_idx is already spatially ordered and is used as is)
+  // FP32C sphere BVE and planar sums: curve-sort src_idx into `sorted` with this scratch
+  // before the sweep (sort_scratch == nullptr: src_idx is already spatially ordered and is
+  // used as is)
   void* sort_scratch = nullptr;
   size_t sort_bytes = 0;
   int32_t* sorted = nullptr;
@@ -84,7 +85,9 @@ SumPlan plan_sum_max(int kind, int mode, int64_t ns, int64_t nt, int sm_count);
 // Enqueues prep + sweep (+ finish) on job.stream.
 int launch_sum(const SumJob& job, const SumPlan& plan);
 
-// Whether the FP32C form of `kind` runs on Hilbert-sorted, tile-relative sources.
+// Whether the FP32C form of `kind` runs on curve-sorted, group-relative sources, and the
+// scratch bytes of that sort for ns sources.
 bool sum_uses_sorted_sources(int kind, int mode);
+size_t sort_scratch_bytes(int kind, int64_t ns);
 
 }  // namespace lpm

@@ -177,6 +177,77 @@ def test_plane_vs_oracle(lg, wl, oracle_mod, delta):
     assert rel_linf(lg.planar_incompressible_velocity(*args, delta, mode="fp32c"), ref) <= FP32C_TOL
 
 
+@pytest.mark.parametrize("n", [1, 2, 33, 257, 1000, 5000])
+@pytest.mark.parametrize("delta", [0.0, 0.02])
+def test_plane_fp32c_ragged_clustered(lg, oracle_mod, n, delta):
+    """Planar FP32C on odd sizes: a uniform scatter plus a tight cluster (spacings down to
+    ~1e-7), a smooth vorticity field, random activity, a rank block."""
+    rng = np.random.default_rng(7 + n)
+    m = n // 2
+    x = np.concatenate([rng.uniform(-4, 4, n - m), 1.0 + 1e-4 * rng.normal(size=m)])
+    y = np.concatenate([rng.uniform(-4, 4, n - m), -0.5 + 1e-4 * rng.normal(size=m)])
+    om = np.exp(-((x - 0.5) ** 2 + y ** 2)) - 0.5 * np.exp(-((x + 1.0) ** 2 + (y - 1.0) ** 2) / 2.0)
+    area = rng.uniform(0.5, 1.5, n) * 64.0 / n
+    act = (rng.random(n) < 0.7).astype(np.int32)
+    ib, ie = (n // 4 + 1, n) if n > 4 else (1, n)
+    ref = oracle_mod.plane_velocity(x, y, om, area, act, delta)
+    got = lg.planar_incompressible_velocity(x, y, om, area, act, delta, i_begin=ib, i_end=ie, mode="fp32c")
+    sl = slice(ib - 1, ie)
+    scale = max(np.abs(np.stack(ref)[:, sl]).max(), 1e-300)
+    assert np.abs(np.stack(got)[:, sl] - np.stack(ref)[:, sl]).max() <= FP32C_TOL * scale
+
+
+def bve_chord_reference(p, zeta, area, act):
+    """FP64 sphere velocity through the exact chord identity a^2 - x_i.x_j = (|d|^2 - c_i - c_j)/2
+    with d = x_i - x_j (no cancellation for close pairs, unlike the reference's 1 - x_i.x_j,
+    which loses ~2^-53 / (1 - x_i.x_j) relative and is useless below spacings of ~1e-6)."""
+    n = p.shape[1]
+    c = (p ** 2).sum(0) - 1.0
+    src = np.nonzero(act)[0]
+    s = -zeta[src] * area[src] / (4.0 * np.pi)
+    u = np.zeros((3, n))
+    for i0 in range(0, n, 512):
+        i1 = min(n, i0 + 512)
+        d = p[:, i0:i1, None] - p[:, None, src]
+        den = 0.5 * ((d ** 2).sum(0) - c[i0:i1, None] - c[None, src])
+        w = np.where(np.arange(i0, i1)[:, None] == src[None, :], 0.0, s[None, :] / np.where(den == 0, 1.0, den))
+        cr = np.cross(p[:, i0:i1, None], p[:, None, src], axis=0)
+        u[:, i0:i1] = (cr * w[None]).sum(2)
+    return u
+
+
+@pytest.mark.parametrize("n", [300, 1000, 5000])
+def test_bve_fp32c_clustered(lg, n):
+    """Sphere FP32C with half the points in a tight cluster (spacings down to ~1e-4 of the
+    radius, against ~0.05 in the scatter) next to a uniform scatter, smooth vorticity: the
+    near groups of a warp take the full-precision path.  The reference is the FP64 chord
+    form; the reference loop's 1 - x_i.x_j loses ~2^-53 / (1 - x_i.x_j) relative.  (Closer
+    than ~1e-6 the sum is ill-conditioned in the FP64 positions themselves: a^2 - x_i.x_j
+    then depends on |x|^2 - a^2 at the 1e-16 level, which the inputs do not carry.)"""
+    rng = np.random.default_rng(11 + n)
+    m = n // 2
+    p = rng.normal(size=(3, n))
+    c0 = np.array([0.3, -0.5, 0.8])
+    p[:, n - m:] = c0[:, None] + 1e-2 * rng.normal(size=(3, m))
+    p /= np.linalg.norm(p, axis=0)
+    zeta = np.exp(-4.0 * ((p - c0[:, None] / np.linalg.norm(c0)) ** 2).sum(0)) - 0.3 * p[2]
+    area = rng.uniform(0.5, 1.5, size=n) * 4 * np.pi / n
+    act = (rng.random(n) < 0.8).astype(np.int32)
+    ref = bve_chord_reference(p, zeta, area, act)
+    got = lg.bve_sphere_velocity(p[0], p[1], p[2], zeta, area, act, 1.0, mode="fp32c")
+    assert rel_linf(got, ref) <= FP32C_TOL
+
+
+def test_plane_fp32c_translated(lg, wl, oracle_mod):
+    """The Lamb-dipole configuration moved to (1000, -2000): FP32C keeps its accuracy (hi/lo
+    positions, group origins at the centroids)."""
+    c = wl.config_colliding_dipoles(5)
+    x, y = c["x"] + 1000.0, c["y"] - 2000.0
+    args = (x, y, c["omega"], c["area"], c["active"])
+    ref = oracle_mod.plane_velocity(*args, 0.0)
+    assert rel_linf(lg.planar_incompressible_velocity(*args, 0.0, mode="fp32c"), ref) <= FP32C_TOL
+
+
 def test_pse_reference_thresholds_on_gpu(lg, wl):
     """The reference regression test's thresholds hold for the GPU Laplacian (both modes)."""
     m = lg.PolyMesh2d(205, 3, 1.0)
