@@ -88,6 +88,13 @@ __device__ __forceinline__ float rcp_approx(float x) {
   return r;
 }
 
+// 2^x on the MUFU unit (PTX ex2.approx, flush-to-zero): relative error ~2^-22.
+__device__ __forceinline__ float ex2_approx(float x) {
+  float r;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
 // log2 on the MUFU unit (PTX lg2.approx, flush-to-zero): absolute error ~2^-22.
 __device__ __forceinline__ float lg2_approx(float x) {
   float r;

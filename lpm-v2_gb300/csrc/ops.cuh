@@ -199,13 +199,22 @@ struct PlaneF64 {
 // KIND 0: K8 of the great-circle distance (SphereDistance, SphereGeometry.f90:107-125)
 // KIND 1: Gaussian 4 exp(-r^2)/pi of the chord distance
 // KIND 2: K8 of the chord distance (ChordDistance, SphereGeometry.f90:67-73)
-enum { kPseK8Geodesic = 0, kPseGaussChord = 1, kPseK8Chord = 2 };
+// KIND 3: KIND 0 with the angle from the chord series below (FP32C only)
+enum { kPseK8Geodesic = 0, kPseGaussChord = 1, kPseK8Chord = 2, kPseK8GeoSeries = 3 };
 
 // FP32C form: positions scaled by 1/R and split hi/lo, f split hi/lo; per pair
 //   acc += (f_j - f_i) A_j P(r^2) exp(-r^2)
-// with the constant factor (1/pi or 4/pi, times eps^-4) applied once in the FP64 finish.
-// The great-circle angle is atan2(|d x p_i|, p_i.p_j) with p_i.p_j = (|p_i|^2+|p_j|^2-|d|^2)/2,
-// both free of cancellation for near pairs.
+// with the constant factor (1/pi or 4/pi, times eps^-4) applied once in the FP64 finish, and
+// exp(-r^2) = 2^(-r^2 log2 e) on the MUFU unit (relative error ~2^-22).
+//  - KIND 0: the great-circle angle is atan2(|d x p_i|, p_i.p_j) with
+//    p_i.p_j = (|p_i|^2 + |p_j|^2 - |d|^2)/2, both free of cancellation for near pairs.
+//  - KIND 3: positions are unit directions p/|p| (the angle between them is what atan2
+//    measures), the chord v = |d|^2 gives theta^2 = 4 asin^2(sqrt(v)/2) by the series
+//      theta^2 = v (1 + v/12 + v^2/90 + v^3/560 + v^4/3150 + ...),
+//    the terms 2 v^n / (n^2 C(2n,n)) of asin^2, truncated after v^5 (relative error < 4e-7
+//    for v <= 0.36, i.e. theta <= 0.61).  The launcher takes KIND 3 only when eps/R <= 0.06:
+//    then every pair beyond v = 0.36 has r^2 >= 0.36 (R/eps)^2 >= 100 even with the
+//    truncated (smaller) theta^2, and its kernel value is below 1e-37.
 template <int KIND>
 struct PseF32 {
   static constexpr int NC = 1;
@@ -222,10 +231,23 @@ struct PseF32 {
     double inv_r;  // 1/R (1 for the plane)
     float ks;      // R/eps: r = theta R/eps (geodesic) or |d| R/eps (chord)
   };
+  // position of particle i as used by the sum: scaled by 1/R, or (KIND 3) the unit direction
+  __device__ static void position(const double* x, const double* y, const double* z, int64_t i, double inv_r,
+                                  double& px, double& py, double& pz) {
+    px = x[i] * inv_r;
+    py = y[i] * inv_r;
+    pz = z ? z[i] * inv_r : 0.0;
+    if (KIND == kPseK8GeoSeries) {
+      const double s = 1.0 / sqrt(fma(px, px, fma(py, py, pz * pz)));
+      px *= s;
+      py *= s;
+      pz *= s;
+    }
+  }
   __device__ static Tgt load_target(const Params& p, int64_t i) {
     Tgt t;
-    const double px = p.x[i] * p.inv_r, py = p.y[i] * p.inv_r;
-    const double pz = p.z ? p.z[i] * p.inv_r : 0.0;
+    double px, py, pz;
+    position(p.x, p.y, p.z, i, p.inv_r, px, py, pz);
     split2(px, t.xh, t.xl);
     split2(py, t.yh, t.yl);
     split2(pz, t.zh, t.zl);
@@ -249,10 +271,16 @@ struct PseF32 {
       const float dot = 0.5f * ((t.n2 + r.c.y) - d2);
       const float rr = atan2f(cn, dot) * t.ks;
       r2 = rr * rr;
+    } else if (KIND == kPseK8GeoSeries) {
+      float sr = __fmaf_rn(d2, 3.1746032e-4f, 1.7857143e-3f);  // 1/3150, 1/560
+      sr = __fmaf_rn(sr, d2, 1.1111111e-2f);                    // 1/90
+      sr = __fmaf_rn(sr, d2, 8.3333336e-2f);                    // 1/12
+      sr = __fmaf_rn(sr, d2, 1.0f);
+      r2 = __fmul_rn(__fmul_rn(d2, t.ks * t.ks), sr);
     } else {
       r2 = d2 * (t.ks * t.ks);
     }
-    float k = expf(-r2);
+    float k = ex2_approx(__fmul_rn(r2, -1.4426950f));  // exp(-r^2)
     if (KIND != kPseGaussChord) {
       const float poly =
           __fmaf_rn(__fmaf_rn(__fmaf_rn(-0.6666666666666666f, r2, 10.0f), r2, -40.0f), r2, 40.0f);

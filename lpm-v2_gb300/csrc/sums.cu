@@ -220,7 +220,8 @@ __global__ void prep_pse32_kernel(const double* x, const double* y, const double
   typename PseF32<KIND>::Rec r;
   if (k < ns) {
     const int64_t j = idx[k];
-    const double px = x[j] * inv_r, py = y[j] * inv_r, pz = z ? z[j] * inv_r : 0.0;
+    double px, py, pz;
+    PseF32<KIND>::position(x, y, z, j, inv_r, px, py, pz);
     float h, l;
     split2(px, h, l);
     r.a.x = h;
@@ -613,7 +614,15 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
       const float ks = static_cast<float>(rscale / job.eps);
       const double e4 = (job.eps * job.eps) * (job.eps * job.eps);
       const double cscale = (job.kind == kSumPseGaussChord ? 4.0 : 1.0) / kPi / e4;
-      if (job.kind == kSumPseK8Geo) {
+      if (job.kind == kSumPseK8Geo && job.eps <= 0.06 * job.radius) {
+        // eps/R <= 0.06: the angle from the chord series (see PseF32)
+        using Op = PseF32<kPseK8GeoSeries>;
+        prep_pse32_kernel<kPseK8GeoSeries><<<prep_grid_pad, pb, 0, job.stream>>>(
+            job.x, job.y, job.z, job.s1, job.area, job.src_idx, job.ns, npad, inv_r,
+            static_cast<Op::Rec*>(job.src_buf));
+        launch_sweep<Op, kPseThreads, kPseTpt, kPseTile, kPseMinB>(job, plan,
+                                                                   Op::Params{job.x, job.y, job.z, job.s1, inv_r, ks});
+      } else if (job.kind == kSumPseK8Geo) {
         using Op = PseF32<kPseK8Geodesic>;
         prep_pse32_kernel<kPseK8Geodesic><<<prep_grid_pad, pb, 0, job.stream>>>(
             job.x, job.y, job.z, job.s1, job.area, job.src_idx, job.ns, npad, inv_r,
