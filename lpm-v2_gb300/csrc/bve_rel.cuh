@@ -301,29 +301,26 @@ __global__ void __launch_bounds__(THREADS, MINB) bve_rel_sweep_kernel(SweepArgs<
   }
 }
 
-// Records and origins of one tile of TILE sources (one CTA of TILE threads; every thread
-// one record).  `j` is the thread's particle (meaningful only if `valid`), `inv_a` and
-// `s_scale` the tile's sphere scale.  Each group of kGroup sources reduces its centroid o,
-// its radius R about o, the smallest distance between consecutive sources and its largest
-// |c_j|, and every record is written as rel2(p_j, o) (rel2_fast for a compact group) -- the
-// operations the sweep uses for targets.
+// The frame of the thread's group of kGroup sources within a tile of TILE (one CTA of TILE
+// threads, every thread one source): the centroid o as hi/lo floats, the radius R about o,
+// whether the group is compact (R <= a/2 and R <= 64 x the smallest distance h between
+// consecutive sources) and whether every |c_j| <= 2^-30 h^2 (c_j negligible in q).  (px, py,
+// pz) is the unit-scaled position and cj = |p|^2 - 1 (both meaningful only if `valid`).
+struct GroupFrame {
+  float oxh, oxl, oyh, oyl, ozh, ozl;
+  float radius;
+  bool compact, on_sphere;
+};
+
 template <int TILE>
-__device__ __forceinline__ void bve_rel_prep_tile(const double* x, const double* y, const double* z,
-                                                  const double* zeta, const double* area, bool valid, int32_t j,
-                                                  double inv_a, double s_scale, BveRel::Rec* out,
-                                                  BveRel::Origin* og) {
+__device__ __forceinline__ GroupFrame sphere_group_frame(bool valid, double px, double py, double pz, double cj) {
   constexpr int G = BveRel::kGroup;
   __shared__ double sp[3][TILE];
   __shared__ double red[3][TILE];
   __shared__ float fmax_[TILE], fmin_[TILE], cmax_[TILE], cntf[TILE];
   const int tid = threadIdx.x;
   const int lane = tid % G;  // position in the group
-  double px = 0.0, py = 0.0, pz = 0.0;
-  if (valid) {
-    px = x[j] * inv_a;
-    py = y[j] * inv_a;
-    pz = z[j] * inv_a;
-  }
+  if (!valid) px = py = pz = cj = 0.0;
   sp[0][tid] = px;
   sp[1][tid] = py;
   sp[2][tid] = pz;
@@ -345,7 +342,6 @@ __device__ __forceinline__ void bve_rel_prep_tile(const double* x, const double*
   const double cnt = cntf[g0] > 0.f ? static_cast<double>(cntf[g0]) : 1.0;
   const double cx = red[0][g0] / cnt, cy = red[1][g0] / cnt, cz = red[2][g0] / cnt;
   float rad = 0.f, spc = 3.4e38f;
-  double cj = 0.0;
   if (valid) {
     const double dx = px - cx, dy = py - cy, dz = pz - cz;
     rad = static_cast<float>(sqrt(dx * dx + dy * dy + dz * dz));
@@ -353,9 +349,7 @@ __device__ __forceinline__ void bve_rel_prep_tile(const double* x, const double*
       const double ex = px - sp[0][tid - 1], ey = py - sp[1][tid - 1], ez = pz - sp[2][tid - 1];
       spc = static_cast<float>(sqrt(ex * ex + ey * ey + ez * ez));
     }
-    cj = fma(px, px, fma(py, py, fma(pz, pz, -1.0)));
   }
-  // sp is read above by the neighbour; the reductions below reuse other arrays only
   fmax_[tid] = rad;
   fmin_[tid] = spc;
   cmax_[tid] = static_cast<float>(fabs(cj));
@@ -368,42 +362,78 @@ __device__ __forceinline__ void bve_rel_prep_tile(const double* x, const double*
     }
     __syncthreads();
   }
-  const float grad = fmax_[g0], gspc = fmin_[g0], gcmax = cmax_[g0];
-  const bool compact = grad <= BveRel::kCompactRadius && grad <= BveRel::kCompactRatio * gspc;
+  GroupFrame f;
+  f.radius = fmax_[g0];
+  const float gspc = fmin_[g0], gcmax = cmax_[g0];
+  f.compact = f.radius <= BveRel::kCompactRadius && f.radius <= BveRel::kCompactRatio * gspc;
   // on the sphere: dropping every c_j moves q by <= 2^-30 h^2 relative to the smallest |d|^2
-  const bool on_sphere = gcmax <= 9.313225746154785e-10f * gspc * gspc;
-  float oxh, oxl, oyh, oyl, ozh, ozl;
-  split2(cx, oxh, oxl);
-  split2(cy, oyh, oyl);
-  split2(cz, ozh, ozl);
+  f.on_sphere = gcmax <= 9.313225746154785e-10f * gspc * gspc;
+  split2(cx, f.oxh, f.oxl);
+  split2(cy, f.oyh, f.oyl);
+  split2(cz, f.ozh, f.ozl);
+  return f;
+}
+
+// Offsets of a unit-scaled position from its group's centroid: rel2_fast for a compact
+// group (the target's far-form operations), rel2 otherwise.
+__device__ __forceinline__ void group_offsets(const GroupFrame& f, double px, double py, double pz, float (&hi)[3],
+                                              float (&lo)[3]) {
+  const double p[3] = {px, py, pz};
+  const float oh[3] = {f.oxh, f.oyh, f.ozh}, ol[3] = {f.oxl, f.oyl, f.ozl};
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    float h, l;
+    split2(p[c], h, l);
+    if (f.compact) {
+      rel2_fast(h, l, oh[c], ol[c], hi[c], lo[c]);
+    } else {
+      rel2(h, l, oh[c], ol[c], hi[c], lo[c]);
+    }
+  }
+}
+
+// The group record: centroid, radius (0 for a compact group: never near), on-sphere flag.
+__device__ __forceinline__ BveRel::Origin group_origin(const GroupFrame& f) {
+  BveRel::Origin o;
+  o.hi = make_float4(f.oxh, f.oyh, f.ozh, f.compact ? 0.f : f.radius);
+  o.lo = make_float4(f.oxl, f.oyl, f.ozl, f.on_sphere ? 1.f : 0.f);
+  return o;
+}
+
+// Records and origins of one tile of TILE sources (one CTA of TILE threads; every thread
+// one record).  `j` is the thread's particle (meaningful only if `valid`), `inv_a` and
+// `s_scale` the tile's sphere scale.  Every record is written as the offset of p_j from its
+// group's centroid -- the operations the sweep uses for targets.
+template <int TILE>
+__device__ __forceinline__ void bve_rel_prep_tile(const double* x, const double* y, const double* z,
+                                                  const double* zeta, const double* area, bool valid, int32_t j,
+                                                  double inv_a, double s_scale, BveRel::Rec* out,
+                                                  BveRel::Origin* og) {
+  double px = 0.0, py = 0.0, pz = 0.0, cj = 0.0;
+  if (valid) {
+    px = x[j] * inv_a;
+    py = y[j] * inv_a;
+    pz = z[j] * inv_a;
+    cj = fma(px, px, fma(py, py, fma(pz, pz, -1.0)));
+  }
+  const GroupFrame f = sphere_group_frame<TILE>(valid, px, py, pz, cj);
   BveRel::Rec r;
   if (valid) {
-    float h, l, sxh, sxl, syh, syl, szh, szl;
-    const auto rel = compact ? rel2_fast : rel2;
-    split2(px, h, l);
-    rel(h, l, oxh, oxl, sxh, sxl);
-    split2(py, h, l);
-    rel(h, l, oyh, oyl, syh, syl);
-    split2(pz, h, l);
-    rel(h, l, ozh, ozl, szh, szl);
+    float hi[3], lo[3];
+    group_offsets(f, px, py, pz, hi, lo);
     const float nc = __double2float_rn(-cj);
     const float s = __double2float_rn(zeta[j] * area[j] * s_scale);
-    r.a = make_float4(-sxh, -sxh, -syh, -syh);
-    r.b = make_float4(-szh, -szh, nc, nc);
-    r.c = make_float4(s, s, -szl, -szl);
-    r.d = make_float4(-sxl, -sxl, -syl, -syl);
+    r.a = make_float4(-hi[0], -hi[0], -hi[1], -hi[1]);
+    r.b = make_float4(-hi[2], -hi[2], nc, nc);
+    r.c = make_float4(s, s, -lo[2], -lo[2]);
+    r.d = make_float4(-lo[0], -lo[0], -lo[1], -lo[1]);
   } else {
     // inert: at the origin with zero strength and zero -c (weight 0 times a finite
     // difference; q > 0 through the target's 2^-100 offset when the target sits on o)
     r.a = r.b = r.c = r.d = make_float4(0.f, 0.f, 0.f, 0.f);
   }
   *out = r;
-  if (lane == 0) {
-    BveRel::Origin o;
-    o.hi = make_float4(oxh, oyh, ozh, compact ? 0.f : grad);  // R = 0: never near
-    o.lo = make_float4(oxl, oyl, ozl, on_sphere ? 1.f : 0.f);
-    og[tid / G] = o;
-  }
+  if (threadIdx.x % BveRel::kGroup == 0) og[threadIdx.x / BveRel::kGroup] = group_origin(f);
 }
 
 // Tile-relative records of the Hilbert-sorted source list `sorted` (ns entries, records

@@ -408,17 +408,15 @@ struct PlaneStreamF64 {
 };
 
 // ============================================================ stream functions (FP32C)
-// Both kernels are logarithms, so each pair term is S_j ln(q_ij) with q_ij formed without
-// cancellation:
-//  - sphere: with p = x / (a sqrt(2)) and c = |p|^2 - 1/2 the identity
-//      1 - x_i.x_j / a^2 = |p_i - p_j|^2 - c_i - c_j
-//    is exact, so with S_j = -zeta_j A_j / (4 pi)
-//      psi_i = sum_{j != i} S_j ln(q_ij) - ln(a^2) / (4 pi) sum_{j != i} zeta_j A_j;
-//    the second sum is the total minus the target's own term, added in FP64 by the finish.
-//    Keeping ln(a^2) out of the pair terms keeps them O(1) for any radius, so their FP32
-//    rounding stays small next to psi.  zeta_rel and zeta_abs share q: two accumulators;
-//  - plane: q_ij = |x_i - x_j|^2 and S_j = omega_j A_j / (4 pi), since
-//    log(sqrt(r^2)) / (2 pi) = ln(r^2) / (4 pi).
+// Planar stream function, FP32C: SetStreamFunctionOnMesh's kernel log(sqrt(r^2)) / (2 pi) is
+// ln(r^2) / (4 pi), so each pair term is S_j ln(q_ij) with q_ij = |x_i - x_j|^2 from hi/lo
+// differences and S_j = omega_j A_j / (4 pi).  (The sphere's stream functions run on the
+// group-relative layout, stream_rel.cuh.)  The log is ln_q below, accurate to ~1 ulp.  A
+// pair with d = 0 (the self pair: hi/lo differences of identical splits are exactly 0) is
+// skipped by giving it q = 1, as the reference's j /= i skips it; q is otherwise clamped to
+// >= 2^-126 so that a degenerate pair stays finite.  The sums are over many terms of both
+// signs that cancel to a much smaller psi, so the FP32 partials are flushed into the
+// compensated accumulators every kFlush sources.
 constexpr float kLogFloor = 1.1754943508222875e-38f;  // 2^-126
 constexpr double kInv4Pi = 0.079577471545947667884;   // 1 / (4 pi)
 
@@ -445,46 +443,6 @@ __device__ __forceinline__ float ln_q(float q) {
   const float lnm = __fmaf_rn(__fmul_rn(tt, s), p, tt);
   return __fmaf_rn(kf, 0.69314718f, lnm);
 }
-
-struct SphereStreamF32 {
-  static constexpr int NC = 2;
-  static constexpr int kFlush = 32;
-  struct __align__(16) Rec {
-    float4 a;  // p_hi.x, p_hi.y, p_hi.z, -c
-    float4 b;  // p_lo.x, p_lo.y, p_lo.z, 0
-    float4 c;  // S_rel, S_abs, 0, 0
-  };
-  struct Tgt {
-    float xh, yh, zh, xl, yl, zl, nc;
-  };
-  struct Params {
-    const double *x, *y, *z;
-    double scale;  // 1 / (a sqrt(2))
-  };
-  // -c of a particle at p, in FP32 (its record and its target state carry the same value)
-  __device__ static float neg_c(double px, double py, double pz) {
-    return __double2float_rn(-fma(px, px, fma(py, py, fma(pz, pz, -0.5))));
-  }
-  __device__ static Tgt load_target(const Params& p, int64_t i) {
-    Tgt t;
-    const double px = p.x[i] * p.scale, py = p.y[i] * p.scale, pz = p.z[i] * p.scale;
-    split2(px, t.xh, t.xl);
-    split2(py, t.yh, t.yl);
-    split2(pz, t.zh, t.zl);
-    t.nc = neg_c(px, py, pz);
-    return t;
-  }
-  __device__ static __forceinline__ void interact(const Tgt& t, const Rec& r, float (&acc)[2]) {
-    const float dx = diff2(t.xh, t.xl, r.a.x, r.b.x);
-    const float dy = diff2(t.yh, t.yl, r.a.y, r.b.y);
-    const float dz = diff2(t.zh, t.zl, r.a.z, r.b.z);
-    const float u = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
-    const float q = fmaxf(__fadd_rn(u, __fadd_rn(t.nc, r.a.w)), kLogFloor);
-    const float lg = ln_q(u != 0.0f ? q : 1.0f);
-    acc[0] = __fmaf_rn(r.c.x, lg, acc[0]);
-    acc[1] = __fmaf_rn(r.c.y, lg, acc[1]);
-  }
-};
 
 struct PlaneStreamF32 {
   static constexpr int NC = 1;

@@ -13,6 +13,7 @@
 #include "ops.cuh"
 #include "plane_rel.cuh"
 #include "sort.cuh"
+#include "stream_rel.cuh"
 #include "sums.cuh"
 
 namespace lpm {
@@ -121,44 +122,6 @@ __global__ void prep_stream64_kernel(const double* x, const double* y, const dou
   r.area = area[j];
   r.idx = j;
   r.pad = 0;
-  out[k] = r;
-}
-
-// Stream-function records (FP32C); records ns..npad-1 are inert (zero strength).  A source
-// that is also a target (ib <= j < ib + nt) leaves its zeta A in self_w[c * nt + j - ib]
-// (zeroed before), for the finish to take out of the total.
-__global__ void prep_sstream32_kernel(const double* x, const double* y, const double* z, const double* qr,
-                                      const double* qa, const double* area, const int32_t* idx, int64_t ns,
-                                      int64_t npad, double scale, int64_t ib, int64_t nt,
-                                      SphereStreamF32::Rec* out, double* self_w) {
-  const int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (k >= npad) return;
-  SphereStreamF32::Rec r;
-  if (k < ns) {
-    const int64_t j = idx[k];
-    const double px = x[j] * scale, py = y[j] * scale, pz = z[j] * scale;
-    float h, l;
-    split2(px, h, l);
-    r.a.x = h;
-    r.b.x = l;
-    split2(py, h, l);
-    r.a.y = h;
-    r.b.y = l;
-    split2(pz, h, l);
-    r.a.z = h;
-    r.b.z = l;
-    r.a.w = SphereStreamF32::neg_c(px, py, pz);
-    r.b.w = 0.f;
-    const double wr = qr[j] * area[j], wa = qa[j] * area[j];
-    r.c = make_float4(__double2float_rn(wr * -kInv4Pi), __double2float_rn(wa * -kInv4Pi), 0.f, 0.f);
-    if (j >= ib && j < ib + nt) {
-      self_w[j - ib] = wr;
-      self_w[nt + j - ib] = wa;
-    }
-  } else {
-    // inert: zero strength at the centre (q = |p_i|^2 - c_i = 1/2)
-    r.a = r.b = r.c = make_float4(0.f, 0.f, 0.f, 0.f);
-  }
   out[k] = r;
 }
 
@@ -346,7 +309,7 @@ size_t rec_bytes(int kind, int mode) {
     case kSumPlane:
       return sizeof(PlaneRel::Rec);
     case kSumSphereStream:
-      return sizeof(SphereStreamF32::Rec);
+      return sizeof(StreamRel::Rec);
     case kSumPlaneStream:
       return sizeof(PlaneStreamF32::Rec);
     default:
@@ -404,7 +367,8 @@ int64_t choose_split(int64_t blocks, int64_t tiles, int64_t slots, int64_t max_s
 }
 
 bool sum_uses_sorted_sources(int kind, int mode) {
-  return mode == LPM_MODE_FP32C && (kind == kSumBve || kind == kSumBveMesh || kind == kSumPlane);
+  return mode == LPM_MODE_FP32C &&
+         (kind == kSumBve || kind == kSumBveMesh || kind == kSumPlane || kind == kSumSphereStream);
 }
 
 size_t sort_scratch_bytes(int kind, int64_t ns) {
@@ -428,7 +392,7 @@ SumPlan plan_sum(int kind, int mode, int64_t ns, int64_t nt, int sm_count, int s
                    static_cast<size_t>(pl.n_tiles) * (tile / BveRel::kGroup) * sizeof(BveRel::Origin);
   }
   if (mode == LPM_MODE_FP32C && kind == kSumSphereStream) {
-    // the sources' own zeta A (2 x nt) and the two totals follow the records
+    // the sources' own zeta A (2 x nt) and the two totals follow the group origins
     pl.src_bytes = align_up(pl.src_bytes, 256) + align_up(2 * static_cast<size_t>(nt) * sizeof(double), 256) +
                    2 * sizeof(double);
   }
@@ -648,20 +612,42 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
       break;
     }
     case kSumSphereStream: {
-      char* tail = static_cast<char*>(job.src_buf) +
-                   align_up(static_cast<size_t>(npad) * sizeof(SphereStreamF32::Rec), 256);
-      double* self_w = reinterpret_cast<double*>(tail);
-      double* tot = reinterpret_cast<double*>(tail + align_up(2 * static_cast<size_t>(job.nt) * sizeof(double), 256));
+      const double inv_a = 1.0 / job.radius;
+      const int32_t* src_list = job.src_idx;
+      if (job.sort_scratch) {
+        LPM_TRY(curve_sort(job.stream, job.ns, job.src_idx, job.x, job.y, job.z, inv_a, job.sort_scratch,
+                           job.sort_bytes, job.sorted));
+        src_list = job.sorted;
+      }
+      // layout of src_buf: records, group origins, the sources' own zeta A (2 x nt), totals
+      char* base = static_cast<char*>(job.src_buf);
+      StreamRel::Rec* recs = reinterpret_cast<StreamRel::Rec*>(base);
+      const size_t org_off = align_up(static_cast<size_t>(npad) * sizeof(StreamRel::Rec), 256);
+      BveRel::Origin* org = reinterpret_cast<BveRel::Origin*>(base + org_off);
+      const size_t self_off = align_up(
+          org_off + static_cast<size_t>(plan.n_tiles) * (kStreamTile / BveRel::kGroup) * sizeof(BveRel::Origin), 256);
+      double* self_w = reinterpret_cast<double*>(base + self_off);
+      double* tot =
+          reinterpret_cast<double*>(base + self_off + align_up(2 * static_cast<size_t>(job.nt) * sizeof(double), 256));
       LPM_CUDA_TRY(cudaMemsetAsync(self_w, 0, 2 * static_cast<size_t>(job.nt) * sizeof(double), job.stream));
-      const double scale = 1.0 / (job.radius * 1.41421356237309504880);
-      prep_sstream32_kernel<<<prep_grid_pad, pb, 0, job.stream>>>(job.x, job.y, job.z, job.s1, job.s2, job.area,
-                                                                  job.src_idx, job.ns, npad, scale, job.ib, job.nt,
-                                                                  static_cast<SphereStreamF32::Rec*>(job.src_buf),
-                                                                  self_w);
+      stream_rel_prep_kernel<kStreamTile><<<static_cast<unsigned>(plan.n_tiles), kStreamTile, 0, job.stream>>>(
+          job.x, job.y, job.z, job.s1, job.s2, job.area, src_list, job.ns, inv_a, job.ib, job.nt, recs, org, self_w);
       stream_totals_kernel<<<1, 1024, 0, job.stream>>>(job.s1, job.s2, job.area, job.src_idx, job.ns, tot);
-      launch_sweep<SphereStreamF32, kStreamThreads, kStreamTpt, kStreamTile, kStreamMinB>(
-          job, plan, SphereStreamF32::Params{job.x, job.y, job.z, scale});
-      const double k_const = -std::log(job.radius * job.radius) * kInv4Pi;
+      SweepArgs<BveF32> a;
+      a.p = BveF32::Params{job.x, job.y, job.z, inv_a};
+      a.src = nullptr;
+      a.n_tiles = plan.n_tiles;
+      a.tiles_per_chunk = plan.tiles_per_chunk;
+      a.ib = job.ib;
+      a.nt = job.nt;
+      a.partial = job.partial;
+      a.status = job.status;
+      const dim3 grid(static_cast<unsigned>(ceil_div(job.nt, kStreamThreads * kStreamTpt)),
+                      static_cast<unsigned>(plan.nsplit));
+      stream_rel_sweep_kernel<kStreamThreads, kStreamTpt, kStreamTile, kStreamMinB>
+          <<<grid, kStreamThreads, 0, job.stream>>>(a, recs, org);
+      // a^2 - x_i.x_j = (a^2 / 2) q_ij: the constant term is -ln(a^2 / 2) / (4 pi) per zeta A
+      const double k_const = -std::log(0.5 * job.radius * job.radius) * kInv4Pi;
       finish_stream_kernel<<<fin_grid, pb, 0, job.stream>>>(job.partial, plan.nsplit, job.nt, 2, k_const, tot, self_w,
                                                             job.out0, job.out1);
       break;
@@ -699,7 +685,7 @@ int log2_bucket(int64_t v) {
 
 SumPlan plan_sum_max(int kind, int mode, int64_t ns, int64_t nt, int sm_count) {
   SumPlan best = plan_sum(kind, mode, ns, nt, sm_count, 0);
-  if (!sum_uses_sorted_sources(kind, mode) || kind == kSumPlane) return best;
+  if (mode != LPM_MODE_FP32C || (kind != kSumBve && kind != kSumBveMesh)) return best;
   const int64_t sub = nt < kTuneTargets ? nt : kTuneTargets;
   for (int sh = 0; sh < kBveShapeCount; ++sh) {
     for (const int64_t t : {nt, sub}) {
@@ -713,7 +699,7 @@ SumPlan plan_sum_max(int kind, int mode, int64_t ns, int64_t nt, int sm_count) {
 
 int autotune_bve_shape(const SumJob& job, int sm_count, int* shape) {
   *shape = 0;
-  if (!sum_uses_sorted_sources(job.kind, job.mode) || job.kind == kSumPlane || job.ns == 0) return LPM_OK;
+  if (job.mode != LPM_MODE_FP32C || (job.kind != kSumBve && job.kind != kSumBveMesh) || job.ns == 0) return LPM_OK;
   const auto key = std::make_tuple(job.kind == kSumBveMesh ? static_cast<int>(kSumBve) : job.kind,
                                    log2_bucket(job.ns), log2_bucket(job.nt), sm_count);
   std::lock_guard<std::mutex> lock(g_tune_mu);
