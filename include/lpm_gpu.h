@@ -152,6 +152,15 @@ int lpm_bve_diagnostics(lpm_bve_solver* solver, double* kinetic_energy, double* 
  * with CUDA events on the solver's stream, and the number of kernels lpm_bve_timestep has
  * launched (stage kernels, direct sums and the per-step source sort). */
 int lpm_bve_kernel_timing(lpm_bve_solver* solver, double* total_ms, int64_t* launches);
+/* SetStreamFunctionsOnMesh (src/SphereBVE.f90:445-485) at the solver's current state, as
+ * the reference's Timestep calls it after every step (src/SphereBVESolver.f90:352): psi_rel
+ * and psi_abs (length n, host arrays) from the device-resident positions and vorticity, in
+ * the solver's mode.  absvort (length n, host) is the caller's absolute vorticity field; NULL
+ * uses zeta + 2 Omega z / a of the current state, which equals the reference's materially
+ * conserved field up to rounding when positions are not renormalised. */
+int lpm_bve_solver_stream_functions(lpm_bve_solver* solver, const double* absvort, double* psi_rel,
+                                    double* psi_abs);
+
 /* Makes the solver enqueue its work on `stream` (a cudaStream_t of the caller's context;
  * NULL restores the solver's own stream), so the caller can time it with events. */
 int lpm_bve_solver_set_stream(lpm_bve_solver* solver, void* stream);

@@ -285,6 +285,10 @@ struct lpm_bve_solver {
   void* sort_scratch = nullptr;
   size_t sort_bytes = 0;
   int32_t* sorted = nullptr;
+  // stream functions of the current state (allocated at the first request)
+  SumScratch stream_scratch;
+  double* absv = nullptr;
+  double* psi = nullptr;  // psi_rel, psi_abs
 
   int sort_sources() {
     return curve_sort(stream, ns, idx, x, y, z, 1.0 / radius, sort_scratch, sort_bytes, sorted);
@@ -596,6 +600,50 @@ extern "C" int lpm_bve_diagnostics(lpm_bve_solver* S, double* ke, double* en, do
   LPM_TRY(mask_buffer(S->arena, S->stream, S->n, S->ns, S->idx, &S->mask));
   return diagnostics(S->stream, S->n, S->u, S->v, S->w, S->q, S->area, S->mask, S->diag_part, S->diag_out, ke, en,
                      ci);
+}
+
+namespace lpm {
+// absolute vorticity of the current state: zeta + 2 Omega z / a (SphereBVE.f90:347)
+__global__ void bve_absvort_kernel(int64_t n, const double* q, const double* z, double two_omega_over_a,
+                                   double* out) {
+  const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = q[i] + two_omega_over_a * z[i];
+}
+}  // namespace lpm
+
+extern "C" int lpm_bve_solver_stream_functions(lpm_bve_solver* S, const double* absvort, double* psi_rel,
+                                               double* psi_abs) {
+  if (!S) return set_error(LPM_ERR_ARG, "null solver");
+  if (!psi_rel || !psi_abs) return set_error(LPM_ERR_ARG, "null output array");
+  const size_t nb = static_cast<size_t>(S->n) * sizeof(double);
+  if (!S->psi) {
+    void* p = nullptr;
+    LPM_TRY(S->arena.alloc(nb, &p));
+    S->absv = static_cast<double*>(p);
+    LPM_TRY(S->arena.alloc(2 * nb, &p));
+    S->psi = static_cast<double*>(p);
+    if (S->ns > 0)
+      LPM_TRY(S->stream_scratch.init(S->arena, kSumSphereStream, S->mode, S->ns, S->n, S->ctx->sm_count));
+  }
+  if (absvort) {
+    LPM_CUDA_TRY(cudaMemcpyAsync(S->absv, absvort, nb, cudaMemcpyHostToDevice, S->stream));
+  } else {
+    bve_absvort_kernel<<<static_cast<unsigned>(ceil_div(S->n, 256)), 256, 0, S->stream>>>(
+        S->n, S->q, S->z, 2.0 * S->omega / S->radius, S->absv);
+    LPM_CUDA_TRY(cudaGetLastError());
+  }
+  if (S->ns == 0) {
+    LPM_CUDA_TRY(cudaMemsetAsync(S->psi, 0, 2 * nb, S->stream));
+  } else {
+    SumJob j = S->job(S->x, S->y, S->z, S->q, kSumSphereStream, S->psi, S->psi + S->n, nullptr);
+    j.s2 = S->absv;
+    j.src_buf = S->stream_scratch.src_buf;
+    j.partial = S->stream_scratch.partial;
+    LPM_TRY(launch_sum(j, S->stream_scratch.plan));
+  }
+  LPM_CUDA_TRY(cudaMemcpyAsync(psi_rel, S->psi, nb, cudaMemcpyDeviceToHost, S->stream));
+  LPM_CUDA_TRY(cudaMemcpyAsync(psi_abs, S->psi + S->n, nb, cudaMemcpyDeviceToHost, S->stream));
+  return S->check_status("lpm_bve_solver_stream_functions");
 }
 
 extern "C" int lpm_bve_kernel_timing(lpm_bve_solver* S, double* total_ms, int64_t* launches) {

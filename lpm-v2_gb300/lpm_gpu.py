@@ -74,6 +74,7 @@ _SIGNATURES = {
     "lpm_bve_diagnostics": [_vp, _D, _D, _D],
     "lpm_bve_kernel_timing": [_vp, _D, _L],
     "lpm_bve_solver_set_stream": [_vp, _vp],
+    "lpm_bve_solver_stream_functions": [_vp, _D, _D, _D],
     "lpm_bve_solver_set_timing": [_vp, _int],
     "lpm_bve_solver_destroy": [_vp],
     "lpm_measure_fp32_peak": [_dbl, _D],
@@ -298,6 +299,14 @@ class BVESolver:
         ke, en, ci = _dbl(), _dbl(), _dbl()
         _check(lib().lpm_bve_diagnostics(self._h, ctypes.byref(ke), ctypes.byref(en), ctypes.byref(ci)))
         return {"kinetic_energy": ke.value, "enstrophy": en.value, "circulation": ci.value}
+
+    def stream_functions(self, abs_vort=None):
+        """SetStreamFunctionsOnMesh (src/SphereBVE.f90:445) at the current state, as the
+        reference's Timestep calls it after each step.  Returns (psi_rel, psi_abs)."""
+        pr, pa = np.empty(self.n), np.empty(self.n)
+        av = None if abs_vort is None else _f64(abs_vort)
+        _check(lib().lpm_bve_solver_stream_functions(self._h, None if av is None else _dp(av), _dp(pr), _dp(pa)))
+        return pr, pa
 
     def kernel_timing(self):
         ms, n = _dbl(), _i64()

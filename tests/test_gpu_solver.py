@@ -141,3 +141,25 @@ def test_solver_bad_arguments(lg):
 def test_measure_fp32_peak(lg):
     t = lg.measure_fp32_peak(50.0)
     assert 30.0 < t < 100.0  # 152 SMs x 128 FP32 lanes x 2 flops x clock
+
+
+@pytest.mark.parametrize("mode", ["fp64", "fp32c"])
+def test_solver_stream_functions(lg, wl, mode):
+    """The solver's stream functions at its current state equal the host-buffer call on the
+    same state (bit for bit in FP64, which sweeps the sources in the same order)."""
+    c = wl.config_gauss_vortex_icos(3)
+    s = lg.BVESolver(c["x"], c["y"], c["z"], c["zeta"], c["area"], c["active"], 1.0, c["omega"], mode=mode)
+    s.timestep(0.01, 3)
+    st = s.get_state()
+    absv = st["rel_vort"] + 2.0 * c["omega"] * st["z"]
+    pr, pa = s.stream_functions(absv)
+    rr, ra = lg.set_stream_functions_on_mesh(st["x"], st["y"], st["z"], st["rel_vort"], absv, c["area"],
+                                             c["active"], 1.0, mode=mode)
+    if mode == "fp64":
+        assert np.array_equal(pr, rr) and np.array_equal(pa, ra)
+    else:
+        assert np.abs(pr - rr).max() <= 1e-6 * np.abs(rr).max()
+        assert np.abs(pa - ra).max() <= 1e-6 * np.abs(ra).max()
+    qr, qa = s.stream_functions()  # absolute vorticity from the state
+    assert np.abs(qa - pa).max() <= 1e-9 * np.abs(pa).max() and np.array_equal(qr, pr)
+    s.close()
