@@ -21,6 +21,10 @@ public :: GpuMask, GpuBVESphereVelocity, GpuPlanarVelocity, GpuPSESphereLaplacia
 public :: lpm_bve_velocity, lpm_bve_set_velocity_from_vorticity, lpm_plane_velocity
 public :: lpm_pse_sphere_laplacian, lpm_pse_plane_laplacian, lpm_bve_stream_functions
 public :: lpm_plane_stream_function, lpm_last_error_string
+public :: lpm_bve_solver_create, lpm_bve_timestep, lpm_bve_get_state, lpm_bve_set_state
+public :: lpm_bve_diagnostics, lpm_bve_solver_stream_functions, lpm_bve_solver_destroy
+public :: lpm_plane_solver_create, lpm_plane_timestep, lpm_plane_get_state, lpm_plane_diagnostics
+public :: lpm_plane_solver_destroy
 
 integer(c_int), parameter :: LPM_MODE_FP64 = 0
 integer(c_int), parameter :: LPM_MODE_FP32C = 1
@@ -116,6 +120,99 @@ interface
 
 	type(c_ptr) function lpm_last_error_string() bind(C, name="lpm_last_error_string")
 		import :: c_ptr
+	end function
+
+	! ---- device-resident BVESolver (timestepPrivate, src/SphereBVESolver.f90:219-353).
+	! u, v, w may be c_null_ptr (then the initial velocity is computed on the device);
+	! otherwise pass c_loc of the arrays.
+	integer(c_int) function lpm_bve_solver_create(solver, n, x, y, z, relvort, area, active, u, v, w, &
+			radius, rotation_rate, mode) bind(C, name="lpm_bve_solver_create")
+		import :: c_int, c_int32_t, c_int64_t, c_double, c_ptr
+		type(c_ptr), intent(out) :: solver
+		integer(c_int64_t), value :: n
+		real(c_double), intent(in) :: x(*), y(*), z(*), relvort(*), area(*)
+		integer(c_int32_t), intent(in) :: active(*)
+		type(c_ptr), value :: u, v, w
+		real(c_double), value :: radius, rotation_rate
+		integer(c_int), value :: mode
+	end function
+
+	integer(c_int) function lpm_bve_timestep(solver, dt, n_steps, renormalize) bind(C, name="lpm_bve_timestep")
+		import :: c_int, c_double, c_ptr
+		type(c_ptr), value :: solver
+		real(c_double), value :: dt
+		integer(c_int), value :: n_steps, renormalize
+	end function
+
+	integer(c_int) function lpm_bve_get_state(solver, x, y, z, relvort, u, v, w) bind(C, name="lpm_bve_get_state")
+		import :: c_int, c_double, c_ptr
+		type(c_ptr), value :: solver
+		real(c_double), intent(out) :: x(*), y(*), z(*), relvort(*), u(*), v(*), w(*)
+	end function
+
+	integer(c_int) function lpm_bve_set_state(solver, x, y, z, relvort, u, v, w) bind(C, name="lpm_bve_set_state")
+		import :: c_int, c_double, c_ptr
+		type(c_ptr), value :: solver
+		real(c_double), intent(in) :: x(*), y(*), z(*), relvort(*), u(*), v(*), w(*)
+	end function
+
+	integer(c_int) function lpm_bve_diagnostics(solver, kinetic_energy, enstrophy, circulation) &
+			bind(C, name="lpm_bve_diagnostics")
+		import :: c_int, c_double, c_ptr
+		type(c_ptr), value :: solver
+		real(c_double), intent(out) :: kinetic_energy, enstrophy, circulation
+	end function
+
+	! SetStreamFunctionsOnMesh at the solver's state (the call at src/SphereBVESolver.f90:352);
+	! absvort may be c_null_ptr (then zeta + 2 Omega z / a of the state is used).
+	integer(c_int) function lpm_bve_solver_stream_functions(solver, absvort, psi_rel, psi_abs) &
+			bind(C, name="lpm_bve_solver_stream_functions")
+		import :: c_int, c_double, c_ptr
+		type(c_ptr), value :: solver, absvort
+		real(c_double), intent(out) :: psi_rel(*), psi_abs(*)
+	end function
+
+	integer(c_int) function lpm_bve_solver_destroy(solver) bind(C, name="lpm_bve_solver_destroy")
+		import :: c_int, c_ptr
+		type(c_ptr), value :: solver
+	end function
+
+	! ---- device-resident PlaneSolver (timestepPrivate, src/PlaneIncompressibleSolver.f90:171-259)
+	integer(c_int) function lpm_plane_solver_create(solver, n, x, y, omega, area, active, u, v, delta, mode) &
+			bind(C, name="lpm_plane_solver_create")
+		import :: c_int, c_int32_t, c_int64_t, c_double, c_ptr
+		type(c_ptr), intent(out) :: solver
+		integer(c_int64_t), value :: n
+		real(c_double), intent(in) :: x(*), y(*), omega(*), area(*)
+		integer(c_int32_t), intent(in) :: active(*)
+		type(c_ptr), value :: u, v
+		real(c_double), value :: delta
+		integer(c_int), value :: mode
+	end function
+
+	integer(c_int) function lpm_plane_timestep(solver, dt, n_steps) bind(C, name="lpm_plane_timestep")
+		import :: c_int, c_double, c_ptr
+		type(c_ptr), value :: solver
+		real(c_double), value :: dt
+		integer(c_int), value :: n_steps
+	end function
+
+	integer(c_int) function lpm_plane_get_state(solver, x, y, u, v) bind(C, name="lpm_plane_get_state")
+		import :: c_int, c_double, c_ptr
+		type(c_ptr), value :: solver
+		real(c_double), intent(out) :: x(*), y(*), u(*), v(*)
+	end function
+
+	integer(c_int) function lpm_plane_diagnostics(solver, kinetic_energy, enstrophy, circulation) &
+			bind(C, name="lpm_plane_diagnostics")
+		import :: c_int, c_double, c_ptr
+		type(c_ptr), value :: solver
+		real(c_double), intent(out) :: kinetic_energy, enstrophy, circulation
+	end function
+
+	integer(c_int) function lpm_plane_solver_destroy(solver) bind(C, name="lpm_plane_solver_destroy")
+		import :: c_int, c_ptr
+		type(c_ptr), value :: solver
 	end function
 end interface
 
