@@ -64,9 +64,13 @@ def parse_args():
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline sample budget")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--workload", choices=["rk4", "ensemble", "stream", "configs"], default="rk4",
+    p.add_argument("--workload", choices=["rk4", "ensemble", "stream", "configs", "sum"], default="rk4",
                    help="rk4: the headline single-instance step; ensemble: the 64-instance batch")
     p.add_argument("--instances", type=int, default=64)
+    p.add_argument("--sum", choices=["bve", "plane", "pse_k8", "pse_gauss", "stream"], default="bve",
+                   help="--workload sum: which direct sum (one host C-ABI call per step)")
+    p.add_argument("--mode", choices=["fp32c", "fp64"], default="fp32c", help="--workload sum: precision mode")
+    p.add_argument("--targets", type=int, default=0, help="--workload sum: first N targets only (0: all)")
     return p.parse_args()
 
 
@@ -591,6 +595,60 @@ def run_configs(args):
     return 0
 
 
+def run_sum(args):
+    """One direct sum through its host-buffer C-ABI entry point, `steps` calls after `warmup`
+    (a small, few-launch workload for profiling and per-row rates).  --nest is the refinement
+    level of the sum's mesh: icosahedral for bve and stream, quad on [-4,4]^2 for plane (Lamb
+    dipoles), cubed sphere for pse_* (Y54 plus noise; eps = h^0.75 for K8, 2 x mean edge for
+    the Gaussian)."""
+    import torch
+    import lpm_gpu as lg
+    import workloads as wl
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if args.sum in ("bve", "stream"):
+        c = wl.config_rh54_icos(args.nest, seed=0)
+        n, ns = c["x"].size, int(c["active"].sum())
+        absv = c["zeta"] + 4.0 * np.pi * c["z"]
+        if args.sum == "bve":
+            call = lambda ie: lg.bve_sphere_velocity(c["x"], c["y"], c["z"], c["zeta"], c["area"], c["active"], 1.0,
+                                                     i_end=ie, mode=args.mode)
+        else:
+            call = lambda ie: lg.set_stream_functions_on_mesh(c["x"], c["y"], c["z"], c["zeta"], absv, c["area"],
+                                                              c["active"], 1.0, i_end=ie, mode=args.mode)
+        mesh = f"icosahedral nest {args.nest}"
+    elif args.sum == "plane":
+        c = wl.config_colliding_dipoles(args.nest)
+        n, ns = c["x"].size, int(c["active"].sum())
+        call = lambda ie: lg.planar_incompressible_velocity(c["x"], c["y"], c["omega"], c["area"], c["active"], 0.0,
+                                                            i_end=ie, mode=args.mode)
+        mesh = f"quad nest {args.nest} on [-4,4]^2"
+    else:
+        c = wl.config_pse_cubed(args.nest)
+        n, ns = c["x"].size, int(c["active"].sum())
+        kern = lg.PSE_K8_GEODESIC if args.sum == "pse_k8" else lg.PSE_GAUSS_CHORD
+        eps = c["eps_k8"] if args.sum == "pse_k8" else c["eps_gauss"]
+        call = lambda ie: lg.pse_sphere_laplacian_at_particles(c["x"], c["y"], c["z"], c["f"], c["area"],
+                                                               c["active"], eps, 1.0, kern, i_end=ie, mode=args.mode)
+        mesh = f"cubed sphere nest {args.nest}, eps {eps:.4g}"
+    nt = n if args.targets <= 0 else min(args.targets, n)
+    for _ in range(max(args.warmup, 3)):
+        call(nt)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        call(nt)
+        times.append(time.perf_counter() - t0)
+    t = min(times)
+    line = {"metric": f"{args.sum} direct sum Ginteractions/s ({args.mode}, host-buffer C ABI)",
+            "value": nt * ns / t / 1e9, "unit": UNIT, "steps": args.steps, "ms_per_step": 1e3 * t,
+            "config": {"workload": f"{args.sum} on {mesh}: {nt} of {n} targets, {ns} sources",
+                       "timing": "host wall clock around each call (copies included), best of the steps"}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def collections_counter(values):
     out = {}
     for v in values:
@@ -608,6 +666,8 @@ def main():
         return run_stream(args)
     if args.workload == "configs":
         return run_configs(args)
+    if args.workload == "sum":
+        return run_sum(args)
     return run_ours(args)
 
 
