@@ -221,6 +221,7 @@ def run_ours(args):
     import ctypes
     import torch
     import lpm_gpu as lg
+    from replicas import max_over_ranks, replica_rate
 
     world, rank, local = dist_env()
     torch.cuda.set_device(local)
@@ -265,13 +266,9 @@ def run_ours(args):
     clocks = sampler.stop()
     k_ms1, k_n1 = solver.kernel_timing()
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    total_ms = sum(step_ms)
-    if dist is not None:
-        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
     inter_step = 4 * per_sum
-    value = world * inter_step * args.steps / (total_ms * 1e-3) / 1e9
+    total_ms = 1e3 * max_over_ranks(sum(step_ms) * 1e-3, dist, "cuda")
+    value = replica_rate(inter_step * args.steps, total_ms * 1e-3, dist, "cuda") / 1e9
 
     # velocity-sum kernels: events around each sum inside the graph
     sums = 4 * args.steps
@@ -313,13 +310,9 @@ def run_ours(args):
                 ee[k].record(stream)
         torch.cuda.synchronize()
         barrier()
-        e_ms = sum(s.elapsed_time(e) for s, e in zip(es, ee))
-        if dist is not None:
-            t = torch.tensor([e_ms], device="cuda", dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e_ms = float(t.item())
+        e_s = sum(s.elapsed_time(e) for s, e in zip(es, ee)) * 1e-3
         nbytes = 7 * n * 8
-        e2e = {"value": world * inter_step * args.steps / (e_ms * 1e-3) / 1e9, "unit": UNIT,
+        e2e = {"value": replica_rate(inter_step * args.steps, e_s, dist, "cuda") / 1e9, "unit": UNIT,
                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                "path": "lpm_bve_set_state + lpm_bve_timestep + lpm_bve_get_state, pinned host buffers"}
 
