@@ -156,7 +156,7 @@ __device__ __forceinline__ void bve_rel_tile(const BveRel::Rec* __restrict__ tl,
       // far group: d = t_hi - s_hi
       if (o.lo.w != 0.f) {
         // every source of the group on the sphere: c_j dropped
-#pragma unroll 2
+#pragma unroll 4
         for (int j = 0; j < G; ++j) {
           const float4 ra = gr[j].a, rb = gr[j].b, rc = gr[j].c;
           const float2 nsx = lo2(ra), nsy = hi2(ra), nsz = lo2(rb), s2 = lo2(rc);
@@ -176,7 +176,7 @@ __device__ __forceinline__ void bve_rel_tile(const BveRel::Rec* __restrict__ tl,
           }
         }
       } else {
-#pragma unroll 2
+#pragma unroll 4
         for (int j = 0; j < G; ++j) {
           const float4 ra = gr[j].a, rb = gr[j].b, rc = gr[j].c;
           const float2 nsx = lo2(ra), nsy = hi2(ra), nsz = lo2(rb), ncj = hi2(rb), s2 = lo2(rc);
