@@ -152,7 +152,7 @@ __device__ __forceinline__ void bve_rel_tile(const BveRel::Rec* __restrict__ tl,
       ty[p] = rel1x2(pr[p].yh, pr[p].yl, o.hi.y, o.lo.y);
       tz[p] = rel1x2(pr[p].zh, pr[p].zl, o.hi.z, o.lo.z);
     }
-    if (!warp_near<NP>(tx, ty, tz, o.hi.w)) {
+    if (o.hi.w == 0.f || !warp_near<NP>(tx, ty, tz, o.hi.w)) {  // R = 0: compact, never near
       // far group: d = t_hi - s_hi
       if (o.lo.w != 0.f) {
         // every source of the group on the sphere: c_j dropped

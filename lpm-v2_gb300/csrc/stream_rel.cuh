@@ -116,7 +116,7 @@ __global__ void __launch_bounds__(THREADS, MINB) stream_rel_sweep_kernel(SweepAr
         ty[p] = rel1x2(pr[p].yh, pr[p].yl, o.hi.y, o.lo.y);
         tz[p] = rel1x2(pr[p].zh, pr[p].zl, o.hi.z, o.lo.z);
       }
-      if (!warp_near<NP>(tx, ty, tz, o.hi.w)) {
+      if (o.hi.w == 0.f || !warp_near<NP>(tx, ty, tz, o.hi.w)) {  // R = 0: compact, never near
         // compact or far group: d = t_hi - s_hi
 #pragma unroll 1
         for (int j0 = 0; j0 < G; j0 += FL) {
