@@ -12,6 +12,7 @@
 #include "engine.cuh"
 #include "ops.cuh"
 #include "plane_rel.cuh"
+#include "pse_rel.cuh"
 #include "sort.cuh"
 #include "stream_rel.cuh"
 #include "sums.cuh"
@@ -32,7 +33,7 @@ struct BveShape {
 constexpr BveShape kBveShapes[] = {{128, 4, 4}, {256, 4, 2}, {128, 6, 2}, {128, 8, 2}};
 constexpr int kBveShapeCount = sizeof(kBveShapes) / sizeof(kBveShapes[0]);
 constexpr int kPlaneThreads = 128, kPlaneTpt = 4, kPlaneTile = 256, kPlaneMinB = 4;
-constexpr int kPseThreads = 128, kPseTpt = 2, kPseTile = 128, kPseMinB = 4;
+constexpr int kPseThreads = 128, kPseTpt = 4, kPseTile = 128, kPseMinB = 4;
 constexpr int kStreamThreads = 128, kStreamTpt = 4, kStreamTile = 256, kStreamMinB = 4;
 // FP64 sequential sweep shape
 constexpr int k64Threads = 128, k64Tile = 128;
@@ -312,6 +313,9 @@ size_t rec_bytes(int kind, int mode) {
       return sizeof(StreamRel::Rec);
     case kSumPlaneStream:
       return sizeof(PlaneStreamF32::Rec);
+    case kSumPseK8Geo:
+    case kSumPseGaussChord:
+      return sizeof(PseRel::Rec);  // the larger of PseRel and PseF32 records
     default:
       return sizeof(PseF32<0>::Rec);
   }
@@ -367,8 +371,8 @@ int64_t choose_split(int64_t blocks, int64_t tiles, int64_t slots, int64_t max_s
 }
 
 bool sum_uses_sorted_sources(int kind, int mode) {
-  return mode == LPM_MODE_FP32C &&
-         (kind == kSumBve || kind == kSumBveMesh || kind == kSumPlane || kind == kSumSphereStream);
+  return mode == LPM_MODE_FP32C && (kind == kSumBve || kind == kSumBveMesh || kind == kSumPlane ||
+                                    kind == kSumSphereStream || kind == kSumPseK8Geo || kind == kSumPseGaussChord);
 }
 
 size_t sort_scratch_bytes(int kind, int64_t ns) {
@@ -578,14 +582,47 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
       const float ks = static_cast<float>(rscale / job.eps);
       const double e4 = (job.eps * job.eps) * (job.eps * job.eps);
       const double cscale = (job.kind == kSumPseGaussChord ? 4.0 : 1.0) / kPi / e4;
-      if (job.kind == kSumPseK8Geo && job.eps <= 0.06 * job.radius) {
-        // eps/R <= 0.06: the angle from the chord series (see PseF32)
-        using Op = PseF32<kPseK8GeoSeries>;
-        prep_pse32_kernel<kPseK8GeoSeries><<<prep_grid_pad, pb, 0, job.stream>>>(
-            job.x, job.y, job.z, job.s1, job.area, job.src_idx, job.ns, npad, inv_r,
-            static_cast<Op::Rec*>(job.src_buf));
-        launch_sweep<Op, kPseThreads, kPseTpt, kPseTile, kPseMinB>(job, plan,
-                                                                   Op::Params{job.x, job.y, job.z, job.s1, inv_r, ks});
+      if (job.z && ((job.kind == kSumPseK8Geo && job.eps <= 0.06 * job.radius) || job.kind == kSumPseGaussChord)) {
+        // sphere: group-relative sweep with the r^2 >= 100 group cutoff (pse_rel.cuh)
+        const int32_t* src_list = job.src_idx;
+        if (job.sort_scratch) {
+          LPM_TRY(curve_sort(job.stream, job.ns, job.src_idx, job.x, job.y, job.z, inv_r, job.sort_scratch,
+                             job.sort_bytes, job.sorted));
+          src_list = job.sorted;
+        }
+        PseRel::Rec* recs = static_cast<PseRel::Rec*>(job.src_buf);
+        BveRel::Origin* org = reinterpret_cast<BveRel::Origin*>(
+            static_cast<char*>(job.src_buf) + align_up(static_cast<size_t>(npad) * sizeof(PseRel::Rec), 256));
+        PseRelArgs a;
+        a.x = job.x;
+        a.y = job.y;
+        a.z = job.z;
+        a.f = job.s1;
+        a.inv_a = inv_r;
+        a.ks2 = ks * ks;
+        a.c_cut = static_cast<float>(std::sqrt(static_cast<double>(PseRel::kCutR2)) * job.eps / job.radius);
+        a.src = recs;
+        a.org = org;
+        a.n_tiles = plan.n_tiles;
+        a.tiles_per_chunk = plan.tiles_per_chunk;
+        a.ib = job.ib;
+        a.nt = job.nt;
+        a.partial = job.partial;
+        a.status = job.status;
+        const dim3 grid(static_cast<unsigned>(ceil_div(job.nt, kPseThreads * kPseTpt)),
+                        static_cast<unsigned>(plan.nsplit));
+        const unsigned ptiles = static_cast<unsigned>(plan.n_tiles);
+        if (job.kind == kSumPseK8Geo) {
+          pse_rel_prep_kernel<kPseK8GeoSeries, kPseTile><<<ptiles, kPseTile, 0, job.stream>>>(
+              job.x, job.y, job.z, job.s1, job.area, src_list, job.ns, inv_r, recs, org);
+          pse_rel_sweep_kernel<kPseK8GeoSeries, kPseThreads, kPseTpt, kPseTile, kPseMinB>
+              <<<grid, kPseThreads, 0, job.stream>>>(a);
+        } else {
+          pse_rel_prep_kernel<kPseGaussChord, kPseTile><<<ptiles, kPseTile, 0, job.stream>>>(
+              job.x, job.y, job.z, job.s1, job.area, src_list, job.ns, inv_r, recs, org);
+          pse_rel_sweep_kernel<kPseGaussChord, kPseThreads, kPseTpt, kPseTile, kPseMinB>
+              <<<grid, kPseThreads, 0, job.stream>>>(a);
+        }
       } else if (job.kind == kSumPseK8Geo) {
         using Op = PseF32<kPseK8Geodesic>;
         prep_pse32_kernel<kPseK8Geodesic><<<prep_grid_pad, pb, 0, job.stream>>>(
