@@ -78,6 +78,18 @@ def config_gauss_vortex_icos(nest: int = 4):
                 omega=2.0 * PI)
 
 
+def rh54_velocity(x, y, z, zonal_wind: float = PI / 7.0, amplitude: float = 1.0):
+    """Exact velocity of rh54_vorticity on the unit sphere (examples/RossbyHaurwitz54.f90:419-428:
+    zeta = 2 w z + 30 K cos(4 lon) z (z^2 - 1)^2).  Its stream function is psi = -w z - K Y with
+    Y = z Re((x + i y)^4), a harmonic polynomial of degree 5 (so the surface Laplacian of Y is
+    -30 Y), and u = r x grad psi = w (-y, x, 0) - K r x grad Y."""
+    gx = z * (4 * x ** 3 - 12 * x * y ** 2)
+    gy = z * (4 * y ** 3 - 12 * x ** 2 * y)
+    gz = x ** 4 - 6 * x ** 2 * y ** 2 + y ** 4
+    return (-zonal_wind * y - amplitude * (y * gz - z * gy), zonal_wind * x - amplitude * (z * gx - x * gz),
+            -amplitude * (x * gy - y * gx))
+
+
 def config_rh54_icos(nest: int = 8, seed: int = 0):
     """RH wave 4 plus a Gaussian vortex (shape 6) at a seeded random centre, mean removed."""
     m = sphere_mesh(lg.ICOS_TRI_SPHERE_SEED, nest)

@@ -107,6 +107,19 @@ def test_bve_fp32c_vs_oracle_rh54(lg, wl, oracle_mod):
     assert rel_linf(got, ref) <= FP32C_TOL
 
 
+def test_bve_rh54_known_answer_gpu(lg, wl):
+    """The RH wave-4 field at icosahedral nest 6 (122,882 particles): both modes reproduce the
+    exact velocity to the discretisation error of the sum (4.1e-3, first order in h), and FP32C
+    stays within 1e-6 of FP64."""
+    m = wl.sphere_mesh(lg.ICOS_TRI_SPHERE_SEED, 6)
+    zeta = wl.rh54_vorticity(m)
+    ue = np.stack(wl.rh54_velocity(m.x, m.y, m.z))
+    u64 = lg.bve_sphere_velocity(m.x, m.y, m.z, zeta, m.area, m.active, 1.0)
+    u32 = lg.bve_sphere_velocity(m.x, m.y, m.z, zeta, m.area, m.active, 1.0, mode="fp32c")
+    assert rel_linf(u64, ue) < 5e-3
+    assert rel_linf(u32, u64) <= FP32C_TOL
+
+
 def test_bve_rank_block_range(lg, wl, oracle_mod):
     """i_begin/i_end (1-based, inclusive) write only the rank's block, as MPISetup splits it."""
     c = wl.config_gauss_vortex_icos(3)

@@ -85,6 +85,20 @@ def test_bve_solid_body_known_answer(lg, oracle_mod):
     assert errs[0] / errs[1] > 1.8 and errs[1] / errs[2] > 1.8
 
 
+def test_bve_rh54_known_answer(lg, wl, oracle_mod):
+    """The RH wave-4 vorticity of the reference's example: the direct sum converges at first
+    order to the exact velocity of its stream function (errors 2.9e-2, 1.5e-2, 8.1e-3 of
+    max|u| at icosahedral nests 3-5)."""
+    errs = []
+    for nest in (3, 4, 5):
+        m = wl.sphere_mesh(lg.ICOS_TRI_SPHERE_SEED, nest)
+        u = np.stack(oracle_mod.bve_velocity(m.x, m.y, m.z, wl.rh54_vorticity(m), m.area, m.active))
+        ue = np.stack(wl.rh54_velocity(m.x, m.y, m.z))
+        errs.append(np.abs(u - ue).max() / np.abs(ue).max())
+    assert errs[-1] < 1e-2
+    assert errs[0] / errs[1] > 1.8 and errs[1] / errs[2] > 1.8
+
+
 def test_oracle_associations_agree(lg, wl, oracle_mod):
     """The two reference associations of the BVE denominator differ only by rounding."""
     c = wl.config_gauss_vortex_icos(3)
