@@ -99,6 +99,25 @@ def test_bve_rh54_known_answer(lg, wl, oracle_mod):
     assert errs[0] / errs[1] > 1.8 and errs[1] / errs[2] > 1.8
 
 
+def test_plane_gaussian_vortex_known_answer(lg, oracle_mod):
+    """Planar sum (delta = 0) of the Gaussian vortex omega = exp(-r^2/s^2), s = 0.5, on the quad
+    mesh of [-4,4]^2: the exact velocity is azimuthal, v_theta = s^2 (1 - exp(-r^2/s^2)) / (2 r);
+    the midpoint-rule sum converges at second order (5.0e-2, 1.3e-2, 3.3e-3 of max|u| at quad
+    nests 4-6)."""
+    s2 = 0.25
+    errs = []
+    for nest in (4, 5, 6):
+        m = lg.PolyMesh2d(lg.QUAD_RECT_SEED, nest, 4.0)
+        x, y = m.x, m.y
+        r2 = x * x + y * y
+        u, v = oracle_mod.plane_velocity(x, y, np.exp(-r2 / s2), m.area, m.active, 0.0)
+        vt = np.where(r2 > 0, s2 * (1.0 - np.exp(-r2 / s2)) / (2.0 * np.where(r2 > 0, r2, 1.0)), 0.0)
+        ue, ve = -vt * y, vt * x
+        errs.append(max(np.abs(u - ue).max(), np.abs(v - ve).max()) / np.abs(np.stack([ue, ve])).max())
+    assert errs[-1] < 5e-3
+    assert errs[0] / errs[1] > 3.5 and errs[1] / errs[2] > 3.5
+
+
 def test_oracle_associations_agree(lg, wl, oracle_mod):
     """The two reference associations of the BVE denominator differ only by rounding."""
     c = wl.config_gauss_vortex_icos(3)
