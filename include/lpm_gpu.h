@@ -105,6 +105,22 @@ int lpm_pse_plane_laplacian(int64_t n, const double* x, const double* y, const d
                             int kernel, int64_t i_begin, int64_t i_end, double* lap,
                             int mode);
 
+/* Replaces PSESphereGradientAtParticles (src/PSEDirectSum.f90:220-267): the surface gradient
+ * (gx, gy, gz) of f with the first-derivative kernel K1 of the great-circle distance,
+ * eps**-4 P_i sum_j (f_j + f_i)(x_i - x_j) K1(d/eps) A_j with P_i = SphereProjection(x_i). */
+int lpm_pse_sphere_gradient(int64_t n, const double* x, const double* y, const double* z,
+                            const double* f, const double* area, const int32_t* active,
+                            double eps, double radius, int64_t i_begin, int64_t i_end,
+                            double* gx, double* gy, double* gz, int mode);
+
+/* Replaces PSESphereDivergenceAtParticles (src/PSEDirectSum.f90:537-579): the divergence of
+ * the vector field (vx, vy, vz), eps**-4 sum_j (P_i (x_i - x_j) K1(d/eps)) . (V_j + V_i) A_j. */
+int lpm_pse_sphere_divergence(int64_t n, const double* x, const double* y, const double* z,
+                              const double* vx, const double* vy, const double* vz,
+                              const double* area, const int32_t* active, double eps,
+                              double radius, int64_t i_begin, int64_t i_end, double* div,
+                              int mode);
+
 /* Replaces SetStreamFunctionsOnMesh (src/SphereBVE.f90:445-485): psi = sum G zeta A with
  * G = -log(a^2 - x_i.x_j)/(4 pi), for the relative and absolute vorticity, j != i.
  * LPM_MODE_FP64 follows the Fortran loop (its log is CUDA's, so agreement is to ~1e-15

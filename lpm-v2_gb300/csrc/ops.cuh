@@ -199,50 +199,36 @@ struct PlaneF64 {
 // KIND 0: K8 of the great-circle distance (SphereDistance, SphereGeometry.f90:107-125)
 // KIND 1: Gaussian 4 exp(-r^2)/pi of the chord distance
 // KIND 2: K8 of the chord distance (ChordDistance, SphereGeometry.f90:67-73)
-// KIND 3: KIND 0 with the angle from the chord series below (FP32C only)
-enum { kPseK8Geodesic = 0, kPseGaussChord = 1, kPseK8Chord = 2, kPseK8GeoSeries = 3 };
+enum { kPseK8Geodesic = 0, kPseGaussChord = 1, kPseK8Chord = 2 };
 
-// FP32C form: positions scaled by 1/R and split hi/lo, f split hi/lo; per pair
+// FP32C form of the planar PSE Laplacian (KIND 1, 2; the sphere's PSE operators run on the
+// group-relative layout, pse_rel.cuh): positions and f split hi/lo; per pair
 //   acc += (f_j - f_i) A_j P(r^2) exp(-r^2)
 // with the constant factor (1/pi or 4/pi, times eps^-4) applied once in the FP64 finish, and
 // exp(-r^2) = 2^(-r^2 log2 e) on the MUFU unit (relative error ~2^-22).
-//  - KIND 0: the great-circle angle is atan2(|d x p_i|, p_i.p_j) with
-//    p_i.p_j = (|p_i|^2 + |p_j|^2 - |d|^2)/2, both free of cancellation for near pairs.
-//  - KIND 3: positions are unit directions p/|p| (the angle between them is what atan2
-//    measures), the chord v = |d|^2 gives theta^2 = 4 asin^2(sqrt(v)/2) by the series
-//      theta^2 = v (1 + v/12 + v^2/90 + v^3/560 + v^4/3150 + ...),
-//    the terms 2 v^n / (n^2 C(2n,n)) of asin^2, truncated after v^5 (relative error < 4e-7
-//    for v <= 0.36, i.e. theta <= 0.61).  The launcher takes KIND 3 only when eps/R <= 0.06:
-//    then every pair beyond v = 0.36 has r^2 >= 0.36 (R/eps)^2 >= 100 even with the
-//    truncated (smaller) theta^2, and its kernel value is below 1e-37.
 template <int KIND>
 struct PseF32 {
+  static_assert(KIND == kPseGaussChord || KIND == kPseK8Chord, "chord kernels only");
   static constexpr int NC = 1;
   struct __align__(16) Rec {
     float4 a;  // p_hi.x, p_hi.y, p_hi.z, f_hi
     float4 b;  // p_lo.x, p_lo.y, p_lo.z, f_lo
-    float4 c;  // A, |p|^2, 0, 0
+    float4 c;  // A, 0, 0, 0
   };
   struct Tgt {
-    float xh, yh, zh, xl, yl, zl, fh, fl, n2, ks;
+    float xh, yh, zh, xl, yl, zl, fh, fl, ks;
   };
   struct Params {
     const double *x, *y, *z, *f;
     double inv_r;  // 1/R (1 for the plane)
-    float ks;      // R/eps: r = theta R/eps (geodesic) or |d| R/eps (chord)
+    float ks;      // R/eps: r = |d| R/eps
   };
-  // position of particle i as used by the sum: scaled by 1/R, or (KIND 3) the unit direction
+  // position of particle i as used by the sum (scaled by 1/R; z may be null)
   __device__ static void position(const double* x, const double* y, const double* z, int64_t i, double inv_r,
                                   double& px, double& py, double& pz) {
     px = x[i] * inv_r;
     py = y[i] * inv_r;
     pz = z ? z[i] * inv_r : 0.0;
-    if (KIND == kPseK8GeoSeries) {
-      const double s = 1.0 / sqrt(fma(px, px, fma(py, py, pz * pz)));
-      px *= s;
-      py *= s;
-      pz *= s;
-    }
   }
   __device__ static Tgt load_target(const Params& p, int64_t i) {
     Tgt t;
@@ -252,7 +238,6 @@ struct PseF32 {
     split2(py, t.yh, t.yl);
     split2(pz, t.zh, t.zl);
     split2(p.f[i], t.fh, t.fl);
-    t.n2 = __double2float_rn(fma(px, px, fma(py, py, pz * pz)));
     t.ks = p.ks;
     return t;
   }
@@ -262,26 +247,9 @@ struct PseF32 {
     const float dz = diff2(t.zh, t.zl, r.a.z, r.b.z);
     const float df = diff2(r.a.w, r.b.w, t.fh, t.fl);  // f_j - f_i
     const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
-    float r2;
-    if (KIND == kPseK8Geodesic) {
-      const float cx = __fmaf_rn(dy, t.zh, -__fmul_rn(dz, t.yh));
-      const float cy = __fmaf_rn(dz, t.xh, -__fmul_rn(dx, t.zh));
-      const float cz = __fmaf_rn(dx, t.yh, -__fmul_rn(dy, t.xh));
-      const float cn = sqrtf(__fmaf_rn(cz, cz, __fmaf_rn(cy, cy, __fmul_rn(cx, cx))));
-      const float dot = 0.5f * ((t.n2 + r.c.y) - d2);
-      const float rr = atan2f(cn, dot) * t.ks;
-      r2 = rr * rr;
-    } else if (KIND == kPseK8GeoSeries) {
-      float sr = __fmaf_rn(d2, 3.1746032e-4f, 1.7857143e-3f);  // 1/3150, 1/560
-      sr = __fmaf_rn(sr, d2, 1.1111111e-2f);                    // 1/90
-      sr = __fmaf_rn(sr, d2, 8.3333336e-2f);                    // 1/12
-      sr = __fmaf_rn(sr, d2, 1.0f);
-      r2 = __fmul_rn(__fmul_rn(d2, t.ks * t.ks), sr);
-    } else {
-      r2 = d2 * (t.ks * t.ks);
-    }
+    const float r2 = d2 * (t.ks * t.ks);
     float k = ex2_approx(__fmul_rn(r2, -1.4426950f));  // exp(-r^2)
-    if (KIND != kPseGaussChord) {
+    if (KIND == kPseK8Chord) {
       const float poly =
           __fmaf_rn(__fmaf_rn(__fmaf_rn(-0.6666666666666666f, r2, 10.0f), r2, -40.0f), r2, 40.0f);
       k = poly * k;
@@ -344,6 +312,110 @@ struct PseF64 {
   }
   __device__ static void store(const PseF64Params& p, int64_t i, int64_t il, const Acc& a) {
     p.lap[il] = __dmul_rn(a.l, p.scale);
+  }
+  static constexpr bool kSkipSelf = false;
+};
+
+// ============================================================ PSE gradient / divergence (FP64)
+// PSESphereGradientAtParticles, src/PSEDirectSum.f90:220-267, and
+// PSESphereDivergenceAtParticles, :537-579, with bivariateFirstDerivativeKernel8 (:629-634) in
+// gfortran's power chain and MATMUL(SphereProjection(x_i), .) (SphereGeometry.f90:578-590)
+// summed row by row left to right.
+__device__ __forceinline__ double k1_f64(double r) {
+  const double r2 = __dmul_rn(r, r);
+  const double r3 = __dmul_rn(r, r2);
+  const double r4 = __dmul_rn(r2, r2);
+  const double r6 = __dmul_rn(r3, r3);
+  const double poly = __dadd_rn(__dsub_rn(__dadd_rn(-20.0, __dmul_rn(20.0, r2)), __dmul_rn(5.0, r4)),
+                                __ddiv_rn(r6, 3.0));
+  return __ddiv_rn(__dmul_rn(poly, exp(-__dmul_rn(r, r))), 3.1415926535897932384626433832795027975);
+}
+
+// atan2(|x_j x x_i|, x_j . x_i): SphereDistance(x_j, x_i) / SphereRadius
+__device__ __forceinline__ double sphere_angle_f64(double ax, double ay, double az, double bx, double by, double bz) {
+  const double c1 = __dsub_rn(__dmul_rn(ay, bz), __dmul_rn(by, az));
+  const double c2 = __dsub_rn(__dmul_rn(bx, az), __dmul_rn(ax, bz));
+  const double c3 = __dsub_rn(__dmul_rn(ax, by), __dmul_rn(bx, ay));
+  const double cn = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(c1, c1), __dmul_rn(c2, c2)), __dmul_rn(c3, c3)));
+  const double dp = __dadd_rn(__dadd_rn(__dmul_rn(ax, bx), __dmul_rn(ay, by)), __dmul_rn(az, bz));
+  return atan2(cn, dp);
+}
+
+// (I - x x^T) g, rows summed left to right
+__device__ __forceinline__ void sphere_project_f64(double x, double y, double z, double g0, double g1, double g2,
+                                                   double& o0, double& o1, double& o2) {
+  const double p11 = __dsub_rn(1.0, __dmul_rn(x, x)), p12 = -__dmul_rn(x, y), p13 = -__dmul_rn(x, z);
+  const double p21 = -__dmul_rn(y, x), p22 = __dsub_rn(1.0, __dmul_rn(y, y)), p23 = -__dmul_rn(y, z);
+  const double p31 = -__dmul_rn(z, x), p32 = -__dmul_rn(z, y), p33 = __dsub_rn(1.0, __dmul_rn(z, z));
+  o0 = __dadd_rn(__dadd_rn(__dmul_rn(p11, g0), __dmul_rn(p12, g1)), __dmul_rn(p13, g2));
+  o1 = __dadd_rn(__dadd_rn(__dmul_rn(p21, g0), __dmul_rn(p22, g1)), __dmul_rn(p23, g2));
+  o2 = __dadd_rn(__dadd_rn(__dmul_rn(p31, g0), __dmul_rn(p32, g1)), __dmul_rn(p33, g2));
+}
+
+struct __align__(16) RecVec64 {
+  double x, y, z, vx, vy, vz, area;
+  long long idx;
+};
+
+struct PseVecF64Params {
+  const double *x, *y, *z, *f, *vx, *vy, *vz;
+  double eps, eps2, denom, radius, scale;  // eps**2, eps**3, 1/eps**2 (gradient) or 1/eps
+  double *o0, *o1, *o2;
+};
+
+// grad_i += (f_j + f_i) (x_i - x_j) K1(d/eps) / eps**2 A_j; then projected and scaled
+struct PseGradF64 {
+  struct Tgt {
+    double x, y, z, f;
+  };
+  struct Acc {
+    double g0, g1, g2;
+  };
+  __device__ static Tgt load(const PseVecF64Params& p, int64_t i) { return Tgt{p.x[i], p.y[i], p.z[i], p.f[i]}; }
+  __device__ static __forceinline__ void interact(const PseVecF64Params& p, const Tgt& t, const Rec64& r, Acc& a) {
+    const double kin = __ddiv_rn(__dmul_rn(sphere_angle_f64(r.x, r.y, r.z, t.x, t.y, t.z), p.radius), p.eps);
+    const double kout = __ddiv_rn(k1_f64(kin), p.eps2);
+    const double fs = __dadd_rn(r.q, t.f);
+    a.g0 = __dadd_rn(a.g0, __dmul_rn(__dmul_rn(__dmul_rn(fs, __dsub_rn(t.x, r.x)), kout), r.r));
+    a.g1 = __dadd_rn(a.g1, __dmul_rn(__dmul_rn(__dmul_rn(fs, __dsub_rn(t.y, r.y)), kout), r.r));
+    a.g2 = __dadd_rn(a.g2, __dmul_rn(__dmul_rn(__dmul_rn(fs, __dsub_rn(t.z, r.z)), kout), r.r));
+  }
+  __device__ static void store(const PseVecF64Params& p, int64_t i, int64_t il, const Acc& a) {
+    double o0, o1, o2;
+    sphere_project_f64(p.x[i], p.y[i], p.z[i], a.g0, a.g1, a.g2, o0, o1, o2);
+    p.o0[il] = __dmul_rn(o0, p.scale);
+    p.o1[il] = __dmul_rn(o1, p.scale);
+    p.o2[il] = __dmul_rn(o2, p.scale);
+  }
+  static constexpr bool kSkipSelf = false;
+};
+
+// div_i += (P_i ((x_i - x_j) K1(d/eps) / eps**3)) . (V_j + V_i) A_j; then scaled by 1/eps
+struct PseDivF64 {
+  struct Tgt {
+    double x, y, z, vx, vy, vz;
+  };
+  struct Acc {
+    double d;
+  };
+  __device__ static Tgt load(const PseVecF64Params& p, int64_t i) {
+    return Tgt{p.x[i], p.y[i], p.z[i], p.vx[i], p.vy[i], p.vz[i]};
+  }
+  __device__ static __forceinline__ void interact(const PseVecF64Params& p, const Tgt& t, const RecVec64& r,
+                                                  Acc& a) {
+    const double kin = __ddiv_rn(__dmul_rn(sphere_angle_f64(r.x, r.y, r.z, t.x, t.y, t.z), p.radius), p.eps);
+    const double k1 = k1_f64(kin);
+    const double g0 = __ddiv_rn(__dmul_rn(__dsub_rn(t.x, r.x), k1), p.denom);
+    const double g1 = __ddiv_rn(__dmul_rn(__dsub_rn(t.y, r.y), k1), p.denom);
+    const double g2 = __ddiv_rn(__dmul_rn(__dsub_rn(t.z, r.z), k1), p.denom);
+    double h0, h1, h2;
+    sphere_project_f64(t.x, t.y, t.z, g0, g1, g2, h0, h1, h2);
+    const double dot = __dadd_rn(__dadd_rn(__dmul_rn(h0, __dadd_rn(r.vx, t.vx)), __dmul_rn(h1, __dadd_rn(r.vy, t.vy))),
+                                 __dmul_rn(h2, __dadd_rn(r.vz, t.vz)));
+    a.d = __dadd_rn(a.d, __dmul_rn(dot, r.area));
+  }
+  __device__ static void store(const PseVecF64Params& p, int64_t i, int64_t il, const Acc& a) {
+    p.o0[il] = __dmul_rn(a.d, p.scale);
   }
   static constexpr bool kSkipSelf = false;
 };

@@ -94,6 +94,15 @@ __global__ void prep_rec64_kernel(const double* x, const double* y, const double
   out[k] = r;
 }
 
+__global__ void prep_vec64_kernel(const double* x, const double* y, const double* z, const double* vx,
+                                  const double* vy, const double* vz, const double* area, const int32_t* idx,
+                                  int64_t ns, RecVec64* out) {
+  const int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= ns) return;
+  const int64_t j = idx[k];
+  out[k] = RecVec64{x[j], y[j], z[j], vx[j], vy[j], vz[j], area[j], static_cast<long long>(j)};
+}
+
 __global__ void prep_plane64_kernel(const double* x, const double* y, const double* omega,
                                     const double* area, const int32_t* idx, int64_t ns,
                                     RecPlane64* out) {
@@ -199,8 +208,7 @@ __global__ void prep_pse32_kernel(const double* x, const double* y, const double
     split2(f[j], h, l);
     r.a.w = h;
     r.b.w = l;
-    r.c = make_float4(__double2float_rn(area[j]), __double2float_rn(fma(px, px, fma(py, py, pz * pz))),
-                      0.f, 0.f);
+    r.c = make_float4(__double2float_rn(area[j]), 0.f, 0.f, 0.f);
   } else {
     r.a = make_float4(0.f, 0.f, 0.f, 0.f);
     r.b = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -289,6 +297,9 @@ int tile_of(int kind, int mode) {
       return kBveTile;
     case kSumPlane:
       return kPlaneTile;
+    case kSumPseGrad:
+    case kSumPseDiv:
+      return kPseTile;
     case kSumSphereStream:
     case kSumPlaneStream:
       return kStreamTile;
@@ -300,6 +311,7 @@ int tile_of(int kind, int mode) {
 size_t rec_bytes(int kind, int mode) {
   if (mode == LPM_MODE_FP64) {
     if (kind == kSumPlane) return sizeof(RecPlane64);
+    if (kind == kSumPseDiv) return sizeof(RecVec64);
     if (kind == kSumSphereStream || kind == kSumPlaneStream) return sizeof(RecStream64);
     return sizeof(Rec64);
   }
@@ -315,9 +327,11 @@ size_t rec_bytes(int kind, int mode) {
       return sizeof(PlaneStreamF32::Rec);
     case kSumPseK8Geo:
     case kSumPseGaussChord:
+    case kSumPseGrad:
+    case kSumPseDiv:
       return sizeof(PseRel::Rec);  // the larger of PseRel and PseF32 records
     default:
-      return sizeof(PseF32<0>::Rec);
+      return sizeof(PseF32<kPseK8Chord>::Rec);
   }
 }
 
@@ -329,6 +343,8 @@ int comps_of(int kind) {
     case kSumPlane:
     case kSumSphereStream:
       return 2;
+    case kSumPseGrad:
+      return 3;
     default:
       return 1;
   }
@@ -372,7 +388,8 @@ int64_t choose_split(int64_t blocks, int64_t tiles, int64_t slots, int64_t max_s
 
 bool sum_uses_sorted_sources(int kind, int mode) {
   return mode == LPM_MODE_FP32C && (kind == kSumBve || kind == kSumBveMesh || kind == kSumPlane ||
-                                    kind == kSumSphereStream || kind == kSumPseK8Geo || kind == kSumPseGaussChord);
+                                    kind == kSumSphereStream || kind == kSumPseK8Geo || kind == kSumPseGaussChord ||
+                                    kind == kSumPseGrad || kind == kSumPseDiv);
 }
 
 size_t sort_scratch_bytes(int kind, int64_t ns) {
@@ -416,6 +433,68 @@ SumPlan plan_sum(int kind, int mode, int64_t ns, int64_t nt, int sm_count, int s
   pl.partial_bytes = static_cast<size_t>(pl.nsplit) * comps_of(kind) * nt * sizeof(double);
   return pl;
 }
+
+namespace {
+// The sphere PSE sums on the group-relative layout (pse_rel.cuh): sort, prep and sweep.
+template <int OP, int ANG>
+void pse_rel_launch(const SumJob& job, const SumPlan& plan, const int32_t* src_list, const PseRelArgs& a) {
+  pse_rel_prep_kernel<OP, ANG, kPseTile><<<static_cast<unsigned>(plan.n_tiles), kPseTile, 0, job.stream>>>(
+      job.x, job.y, job.z, job.s1, job.s2, job.s3, job.area, src_list, job.ns, a.inv_a,
+      const_cast<PseRel::Rec*>(a.src), const_cast<BveRel::Origin*>(a.org));
+  const dim3 grid(static_cast<unsigned>(ceil_div(job.nt, kPseThreads * kPseTpt)), static_cast<unsigned>(plan.nsplit));
+  pse_rel_sweep_kernel<OP, ANG, kPseThreads, kPseTpt, kPseTile, kPseMinB><<<grid, kPseThreads, 0, job.stream>>>(a);
+}
+
+int launch_pse_rel(const SumJob& job, const SumPlan& plan, int64_t npad) {
+  const double inv_a = 1.0 / job.radius;
+  const int32_t* src_list = job.src_idx;
+  if (job.sort_scratch) {
+    LPM_TRY(curve_sort(job.stream, job.ns, job.src_idx, job.x, job.y, job.z, inv_a, job.sort_scratch,
+                       job.sort_bytes, job.sorted));
+    src_list = job.sorted;
+  }
+  PseRelArgs a;
+  a.x = job.x;
+  a.y = job.y;
+  a.z = job.z;
+  a.f = job.s1;
+  a.vy = job.s2;
+  a.vz = job.s3;
+  a.inv_a = inv_a;
+  const double ks = job.radius / job.eps;
+  a.ks2 = static_cast<float>(ks * ks);
+  a.c_cut = static_cast<float>(std::sqrt(static_cast<double>(PseRel::kCutR2)) * job.eps / job.radius);
+  a.half_a2 = static_cast<float>(0.5 * job.radius * job.radius);
+  a.src = static_cast<PseRel::Rec*>(job.src_buf);
+  a.org = reinterpret_cast<BveRel::Origin*>(static_cast<char*>(job.src_buf) +
+                                            align_up(static_cast<size_t>(npad) * sizeof(PseRel::Rec), 256));
+  a.n_tiles = plan.n_tiles;
+  a.tiles_per_chunk = plan.tiles_per_chunk;
+  a.ib = job.ib;
+  a.nt = job.nt;
+  a.partial = job.partial;
+  a.status = job.status;
+  const bool series = job.eps <= 0.06 * job.radius;  // the asin^2 series angle (PseF32)
+  switch (job.kind) {
+    case kSumPseK8Geo:
+      if (series) pse_rel_launch<kPseOpLapK8, kPseAngleSeries>(job, plan, src_list, a);
+      else pse_rel_launch<kPseOpLapK8, kPseAngleAsin>(job, plan, src_list, a);
+      break;
+    case kSumPseGaussChord:
+      pse_rel_launch<kPseOpLapGauss, kPseAngleChord>(job, plan, src_list, a);
+      break;
+    case kSumPseGrad:
+      if (series) pse_rel_launch<kPseOpGrad, kPseAngleSeries>(job, plan, src_list, a);
+      else pse_rel_launch<kPseOpGrad, kPseAngleAsin>(job, plan, src_list, a);
+      break;
+    default:
+      if (series) pse_rel_launch<kPseOpDiv, kPseAngleSeries>(job, plan, src_list, a);
+      else pse_rel_launch<kPseOpDiv, kPseAngleAsin>(job, plan, src_list, a);
+      break;
+  }
+  return LPM_OK;
+}
+}  // namespace
 
 int launch_sum(const SumJob& job, const SumPlan& plan) {
   const int pb = 256;
@@ -470,6 +549,28 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
         } else {
           seq_fp64_kernel<PseF64<kPseK8Chord>, Rec64><<<g, k64Threads, 0, job.stream>>>(
               p, src, job.ns, job.ib, job.nt, job.status);
+        }
+        break;
+      }
+      case kSumPseGrad:
+      case kSumPseDiv: {
+        const double eps2 = job.eps * job.eps;
+        PseVecF64Params p{job.x, job.y, job.z, job.s1, job.s1, job.s2, job.s3, job.eps, eps2,
+                          job.eps * eps2, job.radius, 0.0, job.out0, job.out1, job.out2};
+        if (job.kind == kSumPseGrad) {
+          p.scale = 1.0 / eps2;  // MultiplyFieldByScalar(scalarGrad, 1/eps**2)
+          prep_rec64_kernel<<<prep_grid_ns, pb, 0, job.stream>>>(job.x, job.y, job.z, job.s1, job.area,
+                                                                 job.src_idx, job.ns, 1,
+                                                                 static_cast<Rec64*>(job.src_buf));
+          seq_fp64_kernel<PseGradF64, Rec64><<<g, k64Threads, 0, job.stream>>>(
+              p, static_cast<const Rec64*>(job.src_buf), job.ns, job.ib, job.nt, job.status);
+        } else {
+          p.scale = 1.0 / job.eps;  // MultiplyFieldByScalar(divergence, 1/eps)
+          prep_vec64_kernel<<<prep_grid_ns, pb, 0, job.stream>>>(job.x, job.y, job.z, job.s1, job.s2, job.s3,
+                                                                 job.area, job.src_idx, job.ns,
+                                                                 static_cast<RecVec64*>(job.src_buf));
+          seq_fp64_kernel<PseDivF64, RecVec64><<<g, k64Threads, 0, job.stream>>>(
+              p, static_cast<const RecVec64*>(job.src_buf), job.ns, job.ib, job.nt, job.status);
         }
         break;
       }
@@ -582,54 +683,9 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
       const float ks = static_cast<float>(rscale / job.eps);
       const double e4 = (job.eps * job.eps) * (job.eps * job.eps);
       const double cscale = (job.kind == kSumPseGaussChord ? 4.0 : 1.0) / kPi / e4;
-      if (job.z && ((job.kind == kSumPseK8Geo && job.eps <= 0.06 * job.radius) || job.kind == kSumPseGaussChord)) {
+      if (job.z && (job.kind == kSumPseK8Geo || job.kind == kSumPseGaussChord)) {
         // sphere: group-relative sweep with the r^2 >= 100 group cutoff (pse_rel.cuh)
-        const int32_t* src_list = job.src_idx;
-        if (job.sort_scratch) {
-          LPM_TRY(curve_sort(job.stream, job.ns, job.src_idx, job.x, job.y, job.z, inv_r, job.sort_scratch,
-                             job.sort_bytes, job.sorted));
-          src_list = job.sorted;
-        }
-        PseRel::Rec* recs = static_cast<PseRel::Rec*>(job.src_buf);
-        BveRel::Origin* org = reinterpret_cast<BveRel::Origin*>(
-            static_cast<char*>(job.src_buf) + align_up(static_cast<size_t>(npad) * sizeof(PseRel::Rec), 256));
-        PseRelArgs a;
-        a.x = job.x;
-        a.y = job.y;
-        a.z = job.z;
-        a.f = job.s1;
-        a.inv_a = inv_r;
-        a.ks2 = ks * ks;
-        a.c_cut = static_cast<float>(std::sqrt(static_cast<double>(PseRel::kCutR2)) * job.eps / job.radius);
-        a.src = recs;
-        a.org = org;
-        a.n_tiles = plan.n_tiles;
-        a.tiles_per_chunk = plan.tiles_per_chunk;
-        a.ib = job.ib;
-        a.nt = job.nt;
-        a.partial = job.partial;
-        a.status = job.status;
-        const dim3 grid(static_cast<unsigned>(ceil_div(job.nt, kPseThreads * kPseTpt)),
-                        static_cast<unsigned>(plan.nsplit));
-        const unsigned ptiles = static_cast<unsigned>(plan.n_tiles);
-        if (job.kind == kSumPseK8Geo) {
-          pse_rel_prep_kernel<kPseK8GeoSeries, kPseTile><<<ptiles, kPseTile, 0, job.stream>>>(
-              job.x, job.y, job.z, job.s1, job.area, src_list, job.ns, inv_r, recs, org);
-          pse_rel_sweep_kernel<kPseK8GeoSeries, kPseThreads, kPseTpt, kPseTile, kPseMinB>
-              <<<grid, kPseThreads, 0, job.stream>>>(a);
-        } else {
-          pse_rel_prep_kernel<kPseGaussChord, kPseTile><<<ptiles, kPseTile, 0, job.stream>>>(
-              job.x, job.y, job.z, job.s1, job.area, src_list, job.ns, inv_r, recs, org);
-          pse_rel_sweep_kernel<kPseGaussChord, kPseThreads, kPseTpt, kPseTile, kPseMinB>
-              <<<grid, kPseThreads, 0, job.stream>>>(a);
-        }
-      } else if (job.kind == kSumPseK8Geo) {
-        using Op = PseF32<kPseK8Geodesic>;
-        prep_pse32_kernel<kPseK8Geodesic><<<prep_grid_pad, pb, 0, job.stream>>>(
-            job.x, job.y, job.z, job.s1, job.area, job.src_idx, job.ns, npad, inv_r,
-            static_cast<Op::Rec*>(job.src_buf));
-        launch_sweep<Op, kPseThreads, kPseTpt, kPseTile, kPseMinB>(job, plan,
-                                                                   Op::Params{job.x, job.y, job.z, job.s1, inv_r, ks});
+        LPM_TRY(launch_pse_rel(job, plan, npad));
       } else if (job.kind == kSumPseGaussChord) {
         using Op = PseF32<kPseGaussChord>;
         prep_pse32_kernel<kPseGaussChord><<<prep_grid_pad, pb, 0, job.stream>>>(
@@ -646,6 +702,18 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
                                                                    Op::Params{job.x, job.y, job.z, job.s1, inv_r, ks});
       }
       finish_scalar_kernel<<<fin_grid, pb, 0, job.stream>>>(job.partial, plan.nsplit, job.nt, cscale, job.out0);
+      break;
+    }
+    case kSumPseGrad:
+    case kSumPseDiv: {
+      LPM_TRY(launch_pse_rel(job, plan, npad));
+      const double scale = job.radius / (kPi * (job.eps * job.eps) * (job.eps * job.eps));
+      if (job.kind == kSumPseGrad) {
+        pse_grad_finish_kernel<<<fin_grid, pb, 0, job.stream>>>(job.partial, plan.nsplit, job.nt, job.ib, job.x, job.y,
+                                                                job.z, scale, job.out0, job.out1, job.out2);
+      } else {
+        finish_scalar_kernel<<<fin_grid, pb, 0, job.stream>>>(job.partial, plan.nsplit, job.nt, scale, job.out0);
+      }
       break;
     }
     case kSumSphereStream: {
@@ -793,6 +861,7 @@ struct HostArgs {
   int64_t i_begin, i_end;  // 1-based inclusive
   double *out0, *out1, *out2;
   int mode;
+  const double* s3 = nullptr;  // vz (PSE divergence)
 };
 
 int check_common(const HostArgs& a, int nout) {
@@ -830,7 +899,8 @@ int run_host(const HostArgs& a, int nout) {
 
   const bool has_z = a.z != nullptr;
   const bool has_s2 = a.s2 != nullptr;
-  const int narr = 4 + (has_z ? 1 : 0) + (has_s2 ? 1 : 0);  // x, y, s1, area (+z, +s2)
+  const bool has_s3 = a.s3 != nullptr;
+  const int narr = 4 + (has_z ? 1 : 0) + (has_s2 ? 1 : 0) + (has_s3 ? 1 : 0);  // x, y, s1, area (+z, s2, s3)
   void* p_in = nullptr;
   LPM_TRY(workspace(ctx, kWsTargets, static_cast<size_t>(narr) * n * sizeof(double), &p_in));
   double* d = static_cast<double*>(p_in);
@@ -840,6 +910,7 @@ int run_host(const HostArgs& a, int nout) {
   double* darea = d + 3 * n;
   double* dz = has_z ? d + 4 * n : nullptr;
   double* ds2 = has_s2 ? d + (4 + (has_z ? 1 : 0)) * n : nullptr;
+  double* ds3 = has_s3 ? d + (4 + (has_z ? 1 : 0) + (has_s2 ? 1 : 0)) * n : nullptr;
   const size_t nb = static_cast<size_t>(n) * sizeof(double);
   cudaStream_t s = ctx->stream;
   LPM_CUDA_TRY(cudaMemcpyAsync(dx, a.x, nb, cudaMemcpyHostToDevice, s));
@@ -848,6 +919,7 @@ int run_host(const HostArgs& a, int nout) {
   LPM_CUDA_TRY(cudaMemcpyAsync(darea, a.area, nb, cudaMemcpyHostToDevice, s));
   if (has_z) LPM_CUDA_TRY(cudaMemcpyAsync(dz, a.z, nb, cudaMemcpyHostToDevice, s));
   if (has_s2) LPM_CUDA_TRY(cudaMemcpyAsync(ds2, a.s2, nb, cudaMemcpyHostToDevice, s));
+  if (has_s3) LPM_CUDA_TRY(cudaMemcpyAsync(ds3, a.s3, nb, cudaMemcpyHostToDevice, s));
 
   void* p_out = nullptr;
   LPM_TRY(workspace(ctx, kWsOutput, static_cast<size_t>(nout) * nt * sizeof(double), &p_out));
@@ -870,6 +942,7 @@ int run_host(const HostArgs& a, int nout) {
     job.z = dz;
     job.s1 = ds1;
     job.s2 = ds2;
+    job.s3 = ds3;
     job.area = darea;
     job.src_idx = static_cast<const int32_t*>(p_idx);
     job.ns = ns;
@@ -1003,5 +1076,27 @@ extern "C" int lpm_plane_stream_function(int64_t n, const double* x, const doubl
   HostArgs a{lpm::kSumPlaneStream, n, x, y, nullptr, omega, nullptr, area, active, 1.0, 0.0, 0.0,
              i_begin, i_end, psi, nullptr, nullptr, mode};
   LPM_TRY(lpm::check_common(a, 1));
+  return lpm::run_host(a, 1);
+}
+
+extern "C" int lpm_pse_sphere_gradient(int64_t n, const double* x, const double* y, const double* z, const double* f,
+                                       const double* area, const int32_t* active, double eps, double radius,
+                                       int64_t i_begin, int64_t i_end, double* gx, double* gy, double* gz, int mode) {
+  HostArgs a{lpm::kSumPseGrad, n, x, y, z, f, nullptr, area, active, radius, 0.0, eps, i_begin, i_end, gx, gy, gz, mode};
+  LPM_TRY(lpm::check_common(a, 3));
+  if (!z) return lpm::set_error(LPM_ERR_ARG, "null z array");
+  if (!(eps > 0.0) || !(radius > 0.0)) return lpm::set_error(LPM_ERR_ARG, "eps and radius must be positive");
+  return lpm::run_host(a, 3);
+}
+
+extern "C" int lpm_pse_sphere_divergence(int64_t n, const double* x, const double* y, const double* z,
+                                         const double* vx, const double* vy, const double* vz, const double* area,
+                                         const int32_t* active, double eps, double radius, int64_t i_begin,
+                                         int64_t i_end, double* div, int mode) {
+  HostArgs a{lpm::kSumPseDiv, n, x, y, z, vx, vy, area, active, radius, 0.0, eps, i_begin, i_end, div, nullptr,
+             nullptr, mode, vz};
+  LPM_TRY(lpm::check_common(a, 1));
+  if (!z || !vy || !vz) return lpm::set_error(LPM_ERR_ARG, "null z or vector component array");
+  if (!(eps > 0.0) || !(radius > 0.0)) return lpm::set_error(LPM_ERR_ARG, "eps and radius must be positive");
   return lpm::run_host(a, 1);
 }

@@ -26,7 +26,9 @@ enum SumKind : int {
   kSumPseGaussChord,  // PSE Laplacian, Gaussian + chord distance
   kSumPseK8Chord,     // PSE Laplacian, K8 + chord distance (plane)
   kSumSphereStream,   // sphere stream functions
-  kSumPlaneStream     // planar stream function
+  kSumPlaneStream,    // planar stream function
+  kSumPseGrad,        // PSE gradient on the sphere (K1 of the great-circle distance)
+  kSumPseDiv          // PSE divergence on the sphere
 };
 
 // Inputs of one direct sum over particles [0, n): sources are the ns particles listed (in
@@ -37,7 +39,8 @@ struct SumJob {
   int64_t n = 0;
   const double *x = nullptr, *y = nullptr, *z = nullptr;
   const double* s1 = nullptr;  // zeta (BVE), omega (plane), f (PSE), relvort (stream)
-  const double* s2 = nullptr;  // absvort (sphere stream), unused otherwise
+  const double* s2 = nullptr;  // absvort (sphere stream), vy (PSE divergence), unused otherwise
+  const double* s3 = nullptr;  // vz (PSE divergence), unused otherwise
   const double* area = nullptr;
   const int32_t* src_idx = nullptr;
   int64_t ns = 0;

@@ -66,6 +66,8 @@ _SIGNATURES = {
     "lpm_pse_sphere_laplacian": [_i64, _D, _D, _D, _D, _D, _I, _dbl, _dbl, _int, _i64, _i64, _D, _int],
     "lpm_pse_plane_laplacian": [_i64, _D, _D, _D, _D, _I, _dbl, _int, _i64, _i64, _D, _int],
     "lpm_bve_stream_functions": [_i64, _D, _D, _D, _D, _D, _D, _I, _dbl, _i64, _i64, _D, _D, _int],
+    "lpm_pse_sphere_gradient": [_i64, _D, _D, _D, _D, _D, _I, _dbl, _dbl, _i64, _i64, _D, _D, _D, _int],
+    "lpm_pse_sphere_divergence": [_i64, _D, _D, _D, _D, _D, _D, _D, _I, _dbl, _dbl, _i64, _i64, _D, _int],
     "lpm_plane_stream_function": [_i64, _D, _D, _D, _D, _I, _i64, _i64, _D, _int],
     "lpm_bve_solver_create": [_pvp, _i64, _D, _D, _D, _D, _D, _I, _D, _D, _D, _dbl, _dbl, _int],
     "lpm_bve_timestep": [_vp, _dbl, _int, _int],
@@ -240,6 +242,32 @@ def pse_plane_laplacian_at_particles(x, y, f, area, active_mask, eps, kernel=PSE
     _check(lib().lpm_pse_plane_laplacian(n, _dp(x), _dp(y), _dp(f), _dp(area), _ip(act), float(eps), int(kernel),
                                          ib, ie, _dp(lap), _mode(mode)))
     return lap
+
+
+def pse_sphere_gradient_at_particles(x, y, z, f, area, active_mask, eps, sphere_radius=1.0, i_begin=None,
+                                     i_end=None, mode="fp64"):
+    """PSESphereGradientAtParticles (src/PSEDirectSum.f90:220).  Returns (gx, gy, gz)."""
+    x, y, z, f, area = (_f64(a) for a in (x, y, z, f, area))
+    act = _i32(active_mask)
+    n = x.size
+    ib, ie = _range(n, i_begin, i_end)
+    g = [np.zeros(n) for _ in range(3)]
+    _check(lib().lpm_pse_sphere_gradient(n, _dp(x), _dp(y), _dp(z), _dp(f), _dp(area), _ip(act), float(eps),
+                                         float(sphere_radius), ib, ie, *(_dp(a) for a in g), _mode(mode)))
+    return tuple(g)
+
+
+def pse_sphere_divergence_at_particles(x, y, z, vx, vy, vz, area, active_mask, eps, sphere_radius=1.0, i_begin=None,
+                                       i_end=None, mode="fp64"):
+    """PSESphereDivergenceAtParticles (src/PSEDirectSum.f90:537)."""
+    x, y, z, vx, vy, vz, area = (_f64(a) for a in (x, y, z, vx, vy, vz, area))
+    act = _i32(active_mask)
+    n = x.size
+    ib, ie = _range(n, i_begin, i_end)
+    d = np.zeros(n)
+    _check(lib().lpm_pse_sphere_divergence(n, _dp(x), _dp(y), _dp(z), _dp(vx), _dp(vy), _dp(vz), _dp(area),
+                                           _ip(act), float(eps), float(sphere_radius), ib, ie, _dp(d), _mode(mode)))
+    return d
 
 
 def set_stream_functions_on_mesh(x, y, z, rel_vort, abs_vort, area, active_mask, sphere_radius=1.0, i_begin=None,

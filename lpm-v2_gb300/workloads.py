@@ -53,6 +53,16 @@ def y54(x, y, z):
     return 3.0 * math.sqrt(35.0) * np.cos(4.0 * lon) * s * (-1.0 + s * s) ** 2
 
 
+def y54_surface_gradient(x, y, z):
+    """Surface gradient of y54 on the unit sphere: y54 = 3 sqrt(35) z Re((x + i y)^4) is a
+    harmonic polynomial of degree 5, so grad_s y54 = grad y54 - 5 y54 p."""
+    c = 3.0 * math.sqrt(35.0)
+    q = x ** 4 - 6 * x ** 2 * y ** 2 + y ** 4
+    y5 = z * q
+    gx, gy, gz = z * (4 * x ** 3 - 12 * x * y ** 2), z * (4 * y ** 3 - 12 * x ** 2 * y), q
+    return c * (gx - 5 * y5 * x), c * (gy - 5 * y5 * y), c * (gz - 5 * y5 * z)
+
+
 def colliding_dipoles(x, y, amp: float = 40.0, width_sq: float = 0.04):
     """Two Gaussian dipoles at (+-1, +-0.2) travelling head-on: the dipole at x = -1 has +amp
     above and -amp below (it moves in +x), its mirror image at x = +1 moves in -x."""

@@ -170,6 +170,94 @@ void lpmo_pse_laplacian(int64_t n, const double* x, const double* y, const doubl
   }
 }
 
+/* bivariateFirstDerivativeKernel8, src/PSEDirectSum.f90:629-634, with the power chain of
+ * lpmo_k8. */
+double lpmo_k1(double r)
+{
+  const double r2 = r * r;
+  const double r3 = r * r2;
+  const double r4 = r2 * r2;
+  const double r6 = r3 * r3;
+  return (((-20.0 + 20.0 * r2) - 5.0 * r4) + r6 / 3.0) * exp(-(r * r)) / PI;
+}
+
+/* MATMUL(SphereProjection(x), g) (SphereGeometry.f90:578-590): (I - x x^T) g, each row
+ * summed left to right. */
+static void sphere_project(double xi, double yi, double zi, const double g[3], double out[3])
+{
+  const double p11 = 1.0 - xi * xi, p21 = -(yi * xi), p31 = -(zi * xi);
+  const double p12 = -(xi * yi), p22 = 1.0 - yi * yi, p32 = -(zi * yi);
+  const double p13 = -(xi * zi), p23 = -(yi * zi), p33 = 1.0 - zi * zi;
+  out[0] = (p11 * g[0] + p12 * g[1]) + p13 * g[2];
+  out[1] = (p21 * g[0] + p22 * g[1]) + p23 * g[2];
+  out[2] = (p31 * g[0] + p32 * g[1]) + p33 * g[2];
+}
+
+/*
+ * PSESphereGradientAtParticles, src/PSEDirectSum.f90:220-267: for every active j
+ *   grad += (f_j + f_i) (x_i - x_j) K1(SphereDistance(x_j, x_i)/eps) / eps**2 A_j,
+ * then grad = MATMUL(SphereProjection(x_i), grad) and the field is multiplied by 1/eps**2.
+ */
+void lpmo_pse_sphere_gradient(int64_t n, const double* x, const double* y, const double* z,
+                              const double* f, const double* area, const int32_t* active,
+                              double eps, double radius, int64_t ib, int64_t ie, double* gx,
+                              double* gy, double* gz, int nthreads)
+{
+  const double eps2 = eps * eps;
+  const double scale = 1.0 / eps2;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(pick_threads(nthreads))
+  for (int64_t i = ib; i < ie; ++i) {
+    const double xi = x[i], yi = y[i], zi = z[i];
+    double g[3] = {0.0, 0.0, 0.0};
+    for (int64_t j = 0; j < n; ++j) {
+      if (!active[j]) continue;
+      const double kin = sphere_distance(x[j], y[j], z[j], xi, yi, zi, radius) / eps;
+      const double kout = lpmo_k1(kin) / eps2;
+      const double fs = f[j] + f[i];
+      g[0] = g[0] + ((fs * (xi - x[j])) * kout) * area[j];
+      g[1] = g[1] + ((fs * (yi - y[j])) * kout) * area[j];
+      g[2] = g[2] + ((fs * (zi - z[j])) * kout) * area[j];
+    }
+    double pg[3];
+    sphere_project(xi, yi, zi, g, pg);
+    gx[i] = pg[0] * scale;
+    gy[i] = pg[1] * scale;
+    gz[i] = pg[2] * scale;
+  }
+}
+
+/*
+ * PSESphereDivergenceAtParticles, src/PSEDirectSum.f90:537-579: for every active j
+ *   g = MATMUL(SphereProjection(x_i), (x_i - x_j) K1(SphereDistance(x_j, x_i)/eps) / eps**3),
+ *   div += (g . (V_j + V_i)) A_j,
+ * and the field is multiplied by 1/eps.
+ */
+void lpmo_pse_sphere_divergence(int64_t n, const double* x, const double* y, const double* z,
+                                const double* vx, const double* vy, const double* vz,
+                                const double* area, const int32_t* active, double eps,
+                                double radius, int64_t ib, int64_t ie, double* div, int nthreads)
+{
+  const double denom = eps * (eps * eps); /* eps**3 */
+  const double scale = 1.0 / eps;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(pick_threads(nthreads))
+  for (int64_t i = ib; i < ie; ++i) {
+    const double xi = x[i], yi = y[i], zi = z[i];
+    double d = 0.0;
+    for (int64_t j = 0; j < n; ++j) {
+      if (!active[j]) continue;
+      const double kin = sphere_distance(x[j], y[j], z[j], xi, yi, zi, radius) / eps;
+      const double k1 = lpmo_k1(kin);
+      const double g[3] = {((xi - x[j]) * k1) / denom, ((yi - y[j]) * k1) / denom,
+                           ((zi - z[j]) * k1) / denom};
+      double h[3];
+      sphere_project(xi, yi, zi, g, h);
+      d = d + (((h[0] * (vx[j] + vx[i]) + h[1] * (vy[j] + vy[i])) + h[2] * (vz[j] + vz[i])) *
+               area[j]);
+    }
+    div[i] = d * scale;
+  }
+}
+
 /*
  * SetStreamFunctionsOnMesh, src/SphereBVE.f90:445-485: G = -log(a^2 - sum(xi*xj))/(4 pi),
  * psi_rel += G zeta_rel_j A_j, psi_abs += G zeta_abs_j A_j, j != i, active j.

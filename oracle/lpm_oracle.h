@@ -76,8 +76,21 @@ void lpmo_bve_diagnostics(int64_t n, const double* u, const double* v, const dou
                           const double* zeta, const double* area, const int32_t* active,
                           double* ke, double* enstrophy, double* circulation);
 
-/* K8(r) of PSEDirectSum.f90:622-627 */
+/* PSESphereGradientAtParticles, PSEDirectSum.f90:220-267 (gradient of f, 3 components) */
+void lpmo_pse_sphere_gradient(int64_t n, const double* x, const double* y, const double* z,
+                              const double* f, const double* area, const int32_t* active,
+                              double eps, double radius, int64_t ib, int64_t ie, double* gx,
+                              double* gy, double* gz, int nthreads);
+
+/* PSESphereDivergenceAtParticles, PSEDirectSum.f90:537-579 (divergence of (vx, vy, vz)) */
+void lpmo_pse_sphere_divergence(int64_t n, const double* x, const double* y, const double* z,
+                                const double* vx, const double* vy, const double* vz,
+                                const double* area, const int32_t* active, double eps,
+                                double radius, int64_t ib, int64_t ie, double* div, int nthreads);
+
+/* K8(r) of PSEDirectSum.f90:622-627 and the first-derivative kernel K1 of :629-634 */
 double lpmo_k8(double r);
+double lpmo_k1(double r);
 
 #ifdef __cplusplus
 }

@@ -45,7 +45,13 @@ def lib():
         L.lpmo_plane_timestep.argtypes = [_i64, _D, _D, _D, _D, _I, _D, _D, ctypes.c_double, ctypes.c_double,
                                           ctypes.c_int, ctypes.c_int]
         L.lpmo_bve_diagnostics.argtypes = [_i64, _D, _D, _D, _D, _D, _I, _D, _D, _D]
+        L.lpmo_pse_sphere_gradient.argtypes = [_i64, _D, _D, _D, _D, _D, _I, ctypes.c_double, ctypes.c_double,
+                                               _i64, _i64, _D, _D, _D, ctypes.c_int]
+        L.lpmo_pse_sphere_divergence.argtypes = [_i64, _D, _D, _D, _D, _D, _D, _D, _I, ctypes.c_double,
+                                                 ctypes.c_double, _i64, _i64, _D, ctypes.c_int]
         L.lpmo_k8.argtypes = [ctypes.c_double]
+        L.lpmo_k1.argtypes = [ctypes.c_double]
+        L.lpmo_k1.restype = ctypes.c_double
         L.lpmo_k8.restype = ctypes.c_double
         _LIB = L
     return _LIB
@@ -106,6 +112,29 @@ def pse_laplacian(x, y, z, f, area, active, eps, radius=1.0, kernel=PSE_K8_GEODE
     lib().lpmo_pse_laplacian(n, _d(x), _d(y), _d(z), _d(f), _d(area), active.ctypes.data_as(_I), eps, radius,
                              kernel, ib, ie, _d(lap), threads)
     return lap[ib:ie]
+
+
+def pse_sphere_gradient(x, y, z, f, area, active, eps, radius=1.0, ib=None, ie=None, threads=0):
+    """PSESphereGradientAtParticles (src/PSEDirectSum.f90:220-267); returns (gx, gy, gz) of the block."""
+    x, y, z, f, area, active = _f64(x), _f64(y), _f64(z), _f64(f), _f64(area), _i32(active)
+    n = x.size
+    ib, ie = _range(n, ib, ie)
+    g = [np.zeros(n) for _ in range(3)]
+    lib().lpmo_pse_sphere_gradient(n, _d(x), _d(y), _d(z), _d(f), _d(area), active.ctypes.data_as(_I), eps, radius,
+                                   ib, ie, _d(g[0]), _d(g[1]), _d(g[2]), threads)
+    return tuple(a[ib:ie] for a in g)
+
+
+def pse_sphere_divergence(x, y, z, vx, vy, vz, area, active, eps, radius=1.0, ib=None, ie=None, threads=0):
+    """PSESphereDivergenceAtParticles (src/PSEDirectSum.f90:537-579); returns div of the block."""
+    x, y, z, vx, vy, vz, area, active = (_f64(x), _f64(y), _f64(z), _f64(vx), _f64(vy), _f64(vz), _f64(area),
+                                         _i32(active))
+    n = x.size
+    ib, ie = _range(n, ib, ie)
+    d = np.zeros(n)
+    lib().lpmo_pse_sphere_divergence(n, _d(x), _d(y), _d(z), _d(vx), _d(vy), _d(vz), _d(area),
+                                     active.ctypes.data_as(_I), eps, radius, ib, ie, _d(d), threads)
+    return d[ib:ie]
 
 
 def bve_stream(x, y, z, relvort, absvort, area, active, radius=1.0, ib=None, ie=None, threads=0):

@@ -118,6 +118,26 @@ def test_plane_gaussian_vortex_known_answer(lg, oracle_mod):
     assert errs[0] / errs[1] > 3.5 and errs[1] / errs[2] > 3.5
 
 
+def test_pse_gradient_divergence_known_answer(lg, wl, oracle_mod):
+    """PSE gradient of y54 (tests/SpherePSETest.f90 computes it against HarmGradient) and
+    divergence of that gradient (the surface Laplacian, -30 y54) on the cubed sphere with
+    eps = h^0.5; the (f_j + f_i) form of the gradient needs eps well above h."""
+    eg, ed = [], []
+    for nest in (4, 5, 6):
+        m = wl.sphere_mesh(lg.CUBED_SPHERE_SEED, nest)
+        eps = m.max_edge_length ** 0.5
+        f = wl.y54(m.x, m.y, m.z)
+        ge = np.stack(wl.y54_surface_gradient(m.x, m.y, m.z))
+        blk = slice(0, min(m.n, 4096))
+        g = np.stack(oracle_mod.pse_sphere_gradient(m.x, m.y, m.z, f, m.area, m.active, eps, ib=0, ie=blk.stop))
+        eg.append(np.sqrt(((g - ge[:, blk]) ** 2).sum(0)).max() / np.sqrt((ge ** 2).sum(0)).max())
+        d = oracle_mod.pse_sphere_divergence(m.x, m.y, m.z, ge[0], ge[1], ge[2], m.area, m.active, eps, ib=0,
+                                             ie=blk.stop)
+        ed.append(np.abs(d + 30.0 * f[blk]).max() / np.abs(30.0 * f).max())
+    assert eg[-1] < 1.5e-2 and eg[0] > eg[1] > eg[2]
+    assert ed[-1] < 5e-3 and ed[0] > ed[2]
+
+
 def test_oracle_associations_agree(lg, wl, oracle_mod):
     """The two reference associations of the BVE denominator differ only by rounding."""
     c = wl.config_gauss_vortex_icos(3)
