@@ -67,7 +67,8 @@ def parse_args():
     p.add_argument("--workload", choices=["rk4", "ensemble", "stream", "configs", "sum"], default="rk4",
                    help="rk4: the headline single-instance step; ensemble: the 64-instance batch")
     p.add_argument("--instances", type=int, default=64)
-    p.add_argument("--sum", choices=["bve", "plane", "pse_k8", "pse_gauss", "stream"], default="bve",
+    p.add_argument("--sum", choices=["bve", "plane", "pse_k8", "pse_gauss", "pse_grad", "pse_div", "stream"],
+                   default="bve",
                    help="--workload sum: which direct sum (one host C-ABI call per step)")
     p.add_argument("--mode", choices=["fp32c", "fp64"], default="fp32c", help="--workload sum: precision mode")
     p.add_argument("--targets", type=int, default=0, help="--workload sum: first N targets only (0: all)")
@@ -617,6 +618,19 @@ def run_sum(args):
         call = lambda ie: lg.planar_incompressible_velocity(c["x"], c["y"], c["omega"], c["area"], c["active"], 0.0,
                                                             i_end=ie, mode=args.mode)
         mesh = f"quad nest {args.nest} on [-4,4]^2"
+    elif args.sum in ("pse_grad", "pse_div"):
+        c = wl.config_pse_cubed(args.nest)
+        n, ns = c["x"].size, int(c["active"].sum())
+        eps = c["eps_k8"]
+        f = wl.y54(c["x"], c["y"], c["z"])
+        v = wl.y54_surface_gradient(c["x"], c["y"], c["z"])
+        if args.sum == "pse_grad":
+            call = lambda ie: lg.pse_sphere_gradient_at_particles(c["x"], c["y"], c["z"], f, c["area"], c["active"],
+                                                                  eps, 1.0, i_end=ie, mode=args.mode)
+        else:
+            call = lambda ie: lg.pse_sphere_divergence_at_particles(c["x"], c["y"], c["z"], *v, c["area"],
+                                                                    c["active"], eps, 1.0, i_end=ie, mode=args.mode)
+        mesh = f"cubed sphere nest {args.nest}, eps {eps:.4g} (y54 and its gradient)"
     else:
         c = wl.config_pse_cubed(args.nest)
         n, ns = c["x"].size, int(c["active"].sum())

@@ -21,6 +21,7 @@ public :: GpuMask, GpuBVESphereVelocity, GpuPlanarVelocity, GpuPSESphereLaplacia
 public :: lpm_bve_velocity, lpm_bve_set_velocity_from_vorticity, lpm_plane_velocity
 public :: lpm_pse_sphere_laplacian, lpm_pse_plane_laplacian, lpm_bve_stream_functions
 public :: lpm_plane_stream_function, lpm_last_error_string
+public :: lpm_pse_sphere_gradient, lpm_pse_sphere_divergence
 public :: lpm_bve_solver_create, lpm_bve_timestep, lpm_bve_get_state, lpm_bve_set_state
 public :: lpm_bve_diagnostics, lpm_bve_solver_stream_functions, lpm_bve_solver_destroy
 public :: lpm_plane_solver_create, lpm_plane_timestep, lpm_plane_get_state, lpm_plane_diagnostics
@@ -115,6 +116,30 @@ interface
 		integer(c_int32_t), intent(in) :: active(*)
 		integer(c_int64_t), value :: i_begin, i_end
 		real(c_double), intent(inout) :: psi(*)
+		integer(c_int), value :: mode
+	end function
+
+	integer(c_int) function lpm_pse_sphere_gradient(n, x, y, z, f, area, active, eps, radius, &
+			i_begin, i_end, gx, gy, gz, mode) bind(C, name="lpm_pse_sphere_gradient")
+		import :: c_int, c_int32_t, c_int64_t, c_double
+		integer(c_int64_t), value :: n
+		real(c_double), intent(in) :: x(*), y(*), z(*), f(*), area(*)
+		integer(c_int32_t), intent(in) :: active(*)
+		real(c_double), value :: eps, radius
+		integer(c_int64_t), value :: i_begin, i_end
+		real(c_double), intent(inout) :: gx(*), gy(*), gz(*)
+		integer(c_int), value :: mode
+	end function
+
+	integer(c_int) function lpm_pse_sphere_divergence(n, x, y, z, vx, vy, vz, area, active, eps, radius, &
+			i_begin, i_end, div, mode) bind(C, name="lpm_pse_sphere_divergence")
+		import :: c_int, c_int32_t, c_int64_t, c_double
+		integer(c_int64_t), value :: n
+		real(c_double), intent(in) :: x(*), y(*), z(*), vx(*), vy(*), vz(*), area(*)
+		integer(c_int32_t), intent(in) :: active(*)
+		real(c_double), value :: eps, radius
+		integer(c_int64_t), value :: i_begin, i_end
+		real(c_double), intent(inout) :: div(*)
 		integer(c_int), value :: mode
 	end function
 
