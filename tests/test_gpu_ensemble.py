@@ -84,3 +84,39 @@ def test_ensemble_bad_arguments(lg, instances):
     bad[0]["radius"] = -1.0
     with pytest.raises(lg.LpmError):
         lg.Ensemble(bad)
+
+
+def test_ensemble_mixed_radii_and_rotation(lg, wl):
+    """Instances with different sphere radii (unit to Earth's) and rotation rates, and one with
+    few active sources: FP64 bit-identical to single solvers, FP32C within 1e-6 of FP64."""
+    base = wl.config_ensemble(n_instances=4, seed=9, nests=(2, 3))
+    radii = [1.0, 6.37122e6, 0.25, 1.0e3]
+    insts = []
+    for d, a in zip(base, radii):
+        e = dict(d)
+        e["x"], e["y"], e["z"] = d["x"] * a, d["y"] * a, d["z"] * a
+        e["area"] = d["area"] * a * a
+        e["radius"] = a
+        e["rotation_rate"] = 2.0 * np.pi / (a if a > 10 else 1.0)
+        insts.append(e)
+    act = insts[2]["active"].copy()
+    act[np.nonzero(act)[0][3:]] = 0  # 3 active sources only
+    insts[2]["active"] = act
+    e64 = lg.Ensemble(insts, mode="fp64")
+    e32 = lg.Ensemble(insts, mode="fp32c")
+    e64.timestep(0.01, 3)
+    e32.timestep(0.01, 3)
+    p64, p32 = _split(e64.get_state(), e64.sizes), _split(e32.get_state(), e32.sizes)
+    for d, g64, g32 in zip(insts, p64, p32):
+        s = lg.BVESolver(d["x"], d["y"], d["z"], d["rel_vort"], d["area"], d["active"], d["radius"],
+                         d["rotation_rate"], mode="fp64")
+        s.timestep(0.01, 3)
+        ref = s.get_state()
+        for k in ("x", "y", "z", "rel_vort", "u", "v", "w"):
+            assert np.array_equal(g64[k], ref[k]), k
+        s.close()
+        u64 = np.stack([g64["u"], g64["v"], g64["w"]])
+        u32 = np.stack([g32["u"], g32["v"], g32["w"]])
+        assert np.abs(u32 - u64).max() <= 1e-6 * np.abs(u64).max()
+    e64.close()
+    e32.close()
