@@ -67,7 +67,8 @@ def parse_args():
     p.add_argument("--workload", choices=["rk4", "ensemble", "stream", "configs", "sum"], default="rk4",
                    help="rk4: the headline single-instance step; ensemble: the 64-instance batch")
     p.add_argument("--instances", type=int, default=64)
-    p.add_argument("--sum", choices=["bve", "plane", "pse_k8", "pse_gauss", "pse_grad", "pse_div", "stream"],
+    p.add_argument("--sum", choices=["bve", "plane", "pse_k8", "pse_gauss", "pse_grad", "pse_div", "pse_plane",
+                                     "stream"],
                    default="bve",
                    help="--workload sum: which direct sum (one host C-ABI call per step)")
     p.add_argument("--mode", choices=["fp32c", "fp64"], default="fp32c", help="--workload sum: precision mode")
@@ -618,6 +619,14 @@ def run_sum(args):
         call = lambda ie: lg.planar_incompressible_velocity(c["x"], c["y"], c["omega"], c["area"], c["active"], 0.0,
                                                             i_end=ie, mode=args.mode)
         mesh = f"quad nest {args.nest} on [-4,4]^2"
+    elif args.sum == "pse_plane":
+        m = lg.PolyMesh2d(lg.QUAD_RECT_SEED, args.nest, 4.0)
+        n, ns = m.n, int(m.active.sum())
+        eps = m.max_edge_length ** 0.75
+        f = np.exp(-(m.x * m.x + m.y * m.y)) * np.cos(2.0 * m.x)
+        call = lambda ie: lg.pse_plane_laplacian_at_particles(m.x, m.y, f, m.area, m.active, eps, kernel=lg.PSE_K8_CHORD,
+                                                              i_end=ie, mode=args.mode)
+        mesh = f"quad nest {args.nest} on [-4,4]^2, K8 of the chord, eps {eps:.4g}"
     elif args.sum in ("pse_grad", "pse_div"):
         c = wl.config_pse_cubed(args.nest)
         n, ns = c["x"].size, int(c["active"].sum())

@@ -199,64 +199,9 @@ struct PlaneF64 {
 // KIND 0: K8 of the great-circle distance (SphereDistance, SphereGeometry.f90:107-125)
 // KIND 1: Gaussian 4 exp(-r^2)/pi of the chord distance
 // KIND 2: K8 of the chord distance (ChordDistance, SphereGeometry.f90:67-73)
+// (FP64 forms below; the FP32C forms are pse_rel.cuh on the sphere and plane_rel.cuh in
+// the plane.)
 enum { kPseK8Geodesic = 0, kPseGaussChord = 1, kPseK8Chord = 2 };
-
-// FP32C form of the planar PSE Laplacian (KIND 1, 2; the sphere's PSE operators run on the
-// group-relative layout, pse_rel.cuh): positions and f split hi/lo; per pair
-//   acc += (f_j - f_i) A_j P(r^2) exp(-r^2)
-// with the constant factor (1/pi or 4/pi, times eps^-4) applied once in the FP64 finish, and
-// exp(-r^2) = 2^(-r^2 log2 e) on the MUFU unit (relative error ~2^-22).
-template <int KIND>
-struct PseF32 {
-  static_assert(KIND == kPseGaussChord || KIND == kPseK8Chord, "chord kernels only");
-  static constexpr int NC = 1;
-  struct __align__(16) Rec {
-    float4 a;  // p_hi.x, p_hi.y, p_hi.z, f_hi
-    float4 b;  // p_lo.x, p_lo.y, p_lo.z, f_lo
-    float4 c;  // A, 0, 0, 0
-  };
-  struct Tgt {
-    float xh, yh, zh, xl, yl, zl, fh, fl, ks;
-  };
-  struct Params {
-    const double *x, *y, *z, *f;
-    double inv_r;  // 1/R (1 for the plane)
-    float ks;      // R/eps: r = |d| R/eps
-  };
-  // position of particle i as used by the sum (scaled by 1/R; z may be null)
-  __device__ static void position(const double* x, const double* y, const double* z, int64_t i, double inv_r,
-                                  double& px, double& py, double& pz) {
-    px = x[i] * inv_r;
-    py = y[i] * inv_r;
-    pz = z ? z[i] * inv_r : 0.0;
-  }
-  __device__ static Tgt load_target(const Params& p, int64_t i) {
-    Tgt t;
-    double px, py, pz;
-    position(p.x, p.y, p.z, i, p.inv_r, px, py, pz);
-    split2(px, t.xh, t.xl);
-    split2(py, t.yh, t.yl);
-    split2(pz, t.zh, t.zl);
-    split2(p.f[i], t.fh, t.fl);
-    t.ks = p.ks;
-    return t;
-  }
-  __device__ static __forceinline__ void interact(const Tgt& t, const Rec& r, float (&acc)[1]) {
-    const float dx = diff2(t.xh, t.xl, r.a.x, r.b.x);
-    const float dy = diff2(t.yh, t.yl, r.a.y, r.b.y);
-    const float dz = diff2(t.zh, t.zl, r.a.z, r.b.z);
-    const float df = diff2(r.a.w, r.b.w, t.fh, t.fl);  // f_j - f_i
-    const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
-    const float r2 = d2 * (t.ks * t.ks);
-    float k = ex2_approx(__fmul_rn(r2, -1.4426950f));  // exp(-r^2)
-    if (KIND == kPseK8Chord) {
-      const float poly =
-          __fmaf_rn(__fmaf_rn(__fmaf_rn(-0.6666666666666666f, r2, 10.0f), r2, -40.0f), r2, 40.0f);
-      k = poly * k;
-    }
-    acc[0] = __fmaf_rn(df, r.c.x * k, acc[0]);
-  }
-};
 
 // FP64 K8, bivariateLaplacianKernel8 with gfortran's integer-power chain
 // (r^2 = r r, r^4 = r^2 r^2, r^6 = r^3 r^3 with r^3 = r r^2).

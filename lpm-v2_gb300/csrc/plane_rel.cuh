@@ -245,3 +245,230 @@ __global__ void __launch_bounds__(TILE) plane_rel_prep_kernel(const double* x, c
 }
 
 }  // namespace lpm
+
+namespace lpm {
+
+// ====================================================================== planar PSE Laplacian
+// PSEPlaneLaplacianAtParticles (src/PSEDirectSum.f90:467-500, K8 of the chord distance) and
+// the Gaussian 4 exp(-r^2)/pi of the chord, on the planar group-relative layout with the
+// group cutoff of the sphere's PSE sweep (pse_rel.cuh): a warp skips a group when every one
+// of its targets is farther than R + 10 eps from its centroid, where r^2 >= 100 and a term
+// is below FP32 resolution of the sum.  Per target pair and evaluated source (far form):
+// d (2 FADD2), r^2 (2), exp(-r^2) (1 FMUL2 + 2 MUFU ex2), the K8 polynomial and product
+// (3 + 1), f_j - f_i from hi/lo parts (3), the accumulation (2).
+struct PlanePseRel {
+  struct __align__(16) Rec {
+    float4 a;  // -sx_hi, -sx_hi, -sy_hi, -sy_hi
+    float4 b;  // A_j, A_j, f_hi, f_hi
+    float4 c;  // -sx_lo, -sx_lo, -sy_lo, -sy_lo
+    float4 d;  // f_lo, f_lo, 0, 0
+  };
+};
+
+struct PlanePseRelArgs {
+  const double *x, *y, *f;
+  float ks2;    // eps^-2
+  float c_cut;  // 10 eps
+  const PlanePseRel::Rec* src;
+  const PlaneRel::Origin* org;
+  int64_t n_tiles, tiles_per_chunk, ib, nt;
+  double* partial;  // [chunk][nt]
+  int* status;
+};
+
+template <bool K8>
+__device__ __forceinline__ void plane_pse_pair(float2 dx, float2 dy, float2 ks2, float4 rb, float4 rd, float2 fh,
+                                               float2 fl, float2& acc) {
+  const float2 r2 = __fmul2_rn(__ffma2_rn(dy, dy, __fmul2_rn(dx, dx)), ks2);
+  const float2 ea = __fmul2_rn(r2, make_float2(-1.4426950f, -1.4426950f));
+  float2 k = make_float2(ex2_approx(ea.x), ex2_approx(ea.y));  // exp(-r^2)
+  if (K8) {
+    float2 poly = __ffma2_rn(make_float2(-0.6666666666666666f, -0.6666666666666666f), r2, make_float2(10.0f, 10.0f));
+    poly = __ffma2_rn(poly, r2, make_float2(-40.0f, -40.0f));
+    poly = __ffma2_rn(poly, r2, make_float2(40.0f, 40.0f));
+    k = __fmul2_rn(poly, k);
+  }
+  const float2 df = __fadd2_rn(__fadd2_rn(hi2(rb), make_float2(-fh.x, -fh.y)), __fadd2_rn(lo2(rd), make_float2(-fl.x, -fl.y)));
+  acc = __ffma2_rn(df, __fmul2_rn(lo2(rb), k), acc);
+}
+
+template <bool K8, int THREADS, int TPT, int TILE, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB) plane_pse_rel_sweep_kernel(PlanePseRelArgs a) {
+  static_assert(TPT % 2 == 0, "targets come in pairs");
+  constexpr int NP = TPT / 2;
+  constexpr int G = PlaneRel::kGroup;
+  constexpr int GPT = TILE / G;
+  using Rec = PlanePseRel::Rec;
+  __shared__ __align__(128) Rec stage[2][TILE];
+  __shared__ __align__(8) uint64_t bars[2];
+
+  const int64_t chunk = blockIdx.y;
+  const int64_t tile0 = chunk * a.tiles_per_chunk;
+  int64_t ntl = a.n_tiles - tile0;
+  if (ntl > a.tiles_per_chunk) ntl = a.tiles_per_chunk;
+  if (ntl < 0) ntl = 0;
+
+  PlaneRel::Pair pr[NP];
+  float2 fh[NP], fl[NP], hs[NP], ls[NP];
+  const int64_t first = static_cast<int64_t>(blockIdx.x) * (THREADS * TPT);
+  const int64_t count = a.nt - first < THREADS * TPT ? a.nt - first : THREADS * TPT;
+#pragma unroll
+  for (int p = 0; p < NP; ++p) {
+    float vh[2][3], vl[2][3];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      int64_t il = (2 * p + h) * THREADS + threadIdx.x;
+      if (il >= count) il = count - 1;  // duplicates of a valid target; results not stored
+      const int64_t i = a.ib + first + il;
+      split2(a.x[i], vh[h][0], vl[h][0]);
+      split2(a.y[i], vh[h][1], vl[h][1]);
+      split2(a.f[i], vh[h][2], vl[h][2]);
+    }
+    pr[p].xh = make_float2(vh[0][0], vh[1][0]);
+    pr[p].yh = make_float2(vh[0][1], vh[1][1]);
+    pr[p].xl = make_float2(vl[0][0], vl[1][0]);
+    pr[p].yl = make_float2(vl[0][1], vl[1][1]);
+    fh[p] = make_float2(vh[0][2], vh[1][2]);
+    fl[p] = make_float2(vl[0][2], vl[1][2]);
+    hs[p] = ls[p] = make_float2(0.f, 0.f);
+  }
+  const float2 ks2 = make_float2(a.ks2, a.ks2);
+
+  pipe_init(bars);
+  uint32_t g = 0;
+  int64_t tile = tile0;
+  staged_sweep<Rec, TILE>(a.src, tile0, ntl, stage[0], stage[1], bars, g, a.status, [&](const Rec* tl) {
+    float2 acc[NP];
+#pragma unroll
+    for (int p = 0; p < NP; ++p) acc[p] = make_float2(0.f, 0.f);
+    const PlaneRel::Origin* og = a.org + tile * GPT;
+#pragma unroll 1
+    for (int g0 = 0; g0 < TILE; g0 += G) {
+      const PlaneRel::Origin o = og[g0 / G];
+      const Rec* gr = tl + g0;
+      float2 tx[NP], ty[NP];
+      const float reach = o.f.x + a.c_cut;
+      const float lim = (PlaneRel::kNearFactor * o.f.x) * (PlaneRel::kNearFactor * o.f.x);
+      bool in_reach = false, near = false;
+#pragma unroll
+      for (int p = 0; p < NP; ++p) {
+        tx[p] = rel1x2(pr[p].xh, pr[p].xl, o.o.x, o.o.z);
+        ty[p] = rel1x2(pr[p].yh, pr[p].yl, o.o.y, o.o.w);
+        const float2 n2 = __ffma2_rn(ty[p], ty[p], __fmul2_rn(tx[p], tx[p]));
+        in_reach |= (n2.x < reach * reach) | (n2.y < reach * reach);
+        near |= (n2.x < lim) | (n2.y < lim);
+      }
+      if (!__any_sync(0xffffffffu, in_reach)) continue;  // every pair has r^2 > 100
+      if (!__any_sync(0xffffffffu, near)) {
+#pragma unroll 4
+        for (int j = 0; j < G; ++j) {
+          const float4 ra = gr[j].a, rb = gr[j].b, rd = gr[j].d;
+#pragma unroll
+          for (int p = 0; p < NP; ++p)
+            plane_pse_pair<K8>(__fadd2_rn(tx[p], lo2(ra)), __fadd2_rn(ty[p], hi2(ra)), ks2, rb, rd, fh[p], fl[p],
+                               acc[p]);
+        }
+      } else {
+        float2 txh[NP], tyh[NP], txl[NP], tyl[NP];
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+          rel2x2(pr[p].xh, pr[p].xl, o.o.x, o.o.z, txh[p], txl[p]);
+          rel2x2(pr[p].yh, pr[p].yl, o.o.y, o.o.w, tyh[p], tyl[p]);
+        }
+        for (int j = 0; j < G; ++j) {
+          const float4 ra = gr[j].a, rb = gr[j].b, rc = gr[j].c, rd = gr[j].d;
+#pragma unroll
+          for (int p = 0; p < NP; ++p) {
+            const float2 dx = __fadd2_rn(__fadd2_rn(txh[p], lo2(ra)), __fadd2_rn(txl[p], lo2(rc)));
+            const float2 dy = __fadd2_rn(__fadd2_rn(tyh[p], hi2(ra)), __fadd2_rn(tyl[p], hi2(rc)));
+            plane_pse_pair<K8>(dx, dy, ks2, rb, rd, fh[p], fl[p], acc[p]);
+          }
+        }
+      }
+    }
+    ++tile;
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+      comp_add(hs[p].x, ls[p].x, acc[p].x);
+      comp_add(hs[p].y, ls[p].y, acc[p].y);
+    }
+  });
+
+#pragma unroll
+  for (int p = 0; p < NP; ++p) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int64_t il = first + (2 * p + h) * THREADS + threadIdx.x;
+      if (il < a.nt)
+        a.partial[chunk * a.nt + il] = static_cast<double>(h ? hs[p].y : hs[p].x) + static_cast<double>(h ? ls[p].y : ls[p].x);
+    }
+  }
+}
+
+// Records and origins for the planar PSE sweep: one CTA of TILE threads per tile; the group
+// frame is that of plane_rel_prep_kernel.
+template <int TILE>
+__global__ void __launch_bounds__(TILE) plane_pse_rel_prep_kernel(const double* x, const double* y, const double* f,
+                                                                  const double* area, const int32_t* sorted,
+                                                                  int64_t ns, PlanePseRel::Rec* out,
+                                                                  PlaneRel::Origin* org) {
+  constexpr int G = PlaneRel::kGroup;
+  __shared__ double red[2][TILE];
+  __shared__ float fmax_[TILE], cntf[TILE];
+  const int64_t t = blockIdx.x;
+  const int tid = threadIdx.x;
+  const int64_t k = t * TILE + tid;
+  const bool valid = k < ns;
+  const int32_t j = valid ? sorted[k] : 0;
+  const int lane = tid % G;
+  const double px = valid ? x[j] : 0.0, py = valid ? y[j] : 0.0;
+  red[0][tid] = px;
+  red[1][tid] = py;
+  cntf[tid] = valid ? 1.f : 0.f;
+  __syncthreads();
+  for (int w = G / 2; w > 0; w >>= 1) {
+    if (lane < w) {
+      red[0][tid] += red[0][tid + w];
+      red[1][tid] += red[1][tid + w];
+      cntf[tid] += cntf[tid + w];
+    }
+    __syncthreads();
+  }
+  const int g0 = tid - lane;
+  const double cnt = cntf[g0] > 0.f ? static_cast<double>(cntf[g0]) : 1.0;
+  const double cx = red[0][g0] / cnt, cy = red[1][g0] / cnt;
+  fmax_[tid] = valid ? static_cast<float>(sqrt((px - cx) * (px - cx) + (py - cy) * (py - cy))) : 0.f;
+  __syncthreads();
+  for (int w = G / 2; w > 0; w >>= 1) {
+    if (lane < w) fmax_[tid] = fmaxf(fmax_[tid], fmax_[tid + w]);
+    __syncthreads();
+  }
+  float oxh, oxl, oyh, oyl;
+  split2(cx, oxh, oxl);
+  split2(cy, oyh, oyl);
+  PlanePseRel::Rec r;
+  if (valid) {
+    float h, l, sxh, sxl, syh, syl, fh, fl;
+    split2(px, h, l);
+    rel2(h, l, oxh, oxl, sxh, sxl);
+    split2(py, h, l);
+    rel2(h, l, oyh, oyl, syh, syl);
+    split2(f[j], fh, fl);
+    const float ar = __double2float_rn(area[j]);
+    r.a = make_float4(-sxh, -sxh, -syh, -syh);
+    r.b = make_float4(ar, ar, fh, fh);
+    r.c = make_float4(-sxl, -sxl, -syl, -syl);
+    r.d = make_float4(fl, fl, 0.f, 0.f);
+  } else {
+    r.a = r.b = r.c = r.d = make_float4(0.f, 0.f, 0.f, 0.f);  // zero area: no contribution
+  }
+  out[k] = r;
+  if (lane == 0) {
+    PlaneRel::Origin o;
+    o.o = make_float4(oxh, oyh, oxl, oyl);
+    o.f = make_float4(fmax_[g0], 0.f, 0.f, 0.f);
+    org[t * (TILE / G) + tid / G] = o;
+  }
+}
+
+}  // namespace lpm

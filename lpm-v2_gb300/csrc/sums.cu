@@ -183,40 +183,6 @@ __global__ void prep_pstream32_kernel(const double* x, const double* y, const do
   out[k] = r;
 }
 
-template <int KIND>
-__global__ void prep_pse32_kernel(const double* x, const double* y, const double* z,
-                                  const double* f, const double* area, const int32_t* idx,
-                                  int64_t ns, int64_t npad, double inv_r,
-                                  typename PseF32<KIND>::Rec* out) {
-  const int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (k >= npad) return;
-  typename PseF32<KIND>::Rec r;
-  if (k < ns) {
-    const int64_t j = idx[k];
-    double px, py, pz;
-    PseF32<KIND>::position(x, y, z, j, inv_r, px, py, pz);
-    float h, l;
-    split2(px, h, l);
-    r.a.x = h;
-    r.b.x = l;
-    split2(py, h, l);
-    r.a.y = h;
-    r.b.y = l;
-    split2(pz, h, l);
-    r.a.z = h;
-    r.b.z = l;
-    split2(f[j], h, l);
-    r.a.w = h;
-    r.b.w = l;
-    r.c = make_float4(__double2float_rn(area[j]), 0.f, 0.f, 0.f);
-  } else {
-    r.a = make_float4(0.f, 0.f, 0.f, 0.f);
-    r.b = make_float4(0.f, 0.f, 0.f, 0.f);
-    r.c = make_float4(0.f, 0.f, 0.f, 0.f);  // zero area: contributes nothing
-  }
-  out[k] = r;
-}
-
 // ------------------------------------------------------------------ finish kernels
 // Fixed-order FP64 reduction over the split-K chunks, then the per-target epilogue.
 
@@ -329,9 +295,9 @@ size_t rec_bytes(int kind, int mode) {
     case kSumPseGaussChord:
     case kSumPseGrad:
     case kSumPseDiv:
-      return sizeof(PseRel::Rec);  // the larger of PseRel and PseF32 records
+      return sizeof(PseRel::Rec);  // also covers the planar record of the Gaussian-chord kind
     default:
-      return sizeof(PseF32<kPseK8Chord>::Rec);
+      return sizeof(PlanePseRel::Rec);
   }
 }
 
@@ -389,11 +355,14 @@ int64_t choose_split(int64_t blocks, int64_t tiles, int64_t slots, int64_t max_s
 bool sum_uses_sorted_sources(int kind, int mode) {
   return mode == LPM_MODE_FP32C && (kind == kSumBve || kind == kSumBveMesh || kind == kSumPlane ||
                                     kind == kSumSphereStream || kind == kSumPseK8Geo || kind == kSumPseGaussChord ||
-                                    kind == kSumPseGrad || kind == kSumPseDiv);
+                                    kind == kSumPseK8Chord || kind == kSumPseGrad || kind == kSumPseDiv);
 }
 
 size_t sort_scratch_bytes(int kind, int64_t ns) {
-  return kind == kSumPlane ? curve_sort2d_bytes(ns) : curve_sort_bytes(ns);
+  // planar kinds sort in 2-D; the Gaussian-chord Laplacian serves the plane and the sphere
+  if (kind == kSumPlane || kind == kSumPseK8Chord) return curve_sort2d_bytes(ns);
+  if (kind == kSumPseGaussChord) return std::max(curve_sort_bytes(ns), curve_sort2d_bytes(ns));
+  return curve_sort_bytes(ns);
 }
 
 int bve_shape_count() { return kBveShapeCount; }
@@ -474,7 +443,7 @@ int launch_pse_rel(const SumJob& job, const SumPlan& plan, int64_t npad) {
   a.nt = job.nt;
   a.partial = job.partial;
   a.status = job.status;
-  const bool series = job.eps <= 0.06 * job.radius;  // the asin^2 series angle (PseF32)
+  const bool series = job.eps <= 0.06 * job.radius;  // the asin^2 series angle (pse_rel.cuh)
   switch (job.kind) {
     case kSumPseK8Geo:
       if (series) pse_rel_launch<kPseOpLapK8, kPseAngleSeries>(job, plan, src_list, a);
@@ -491,6 +460,42 @@ int launch_pse_rel(const SumJob& job, const SumPlan& plan, int64_t npad) {
       if (series) pse_rel_launch<kPseOpDiv, kPseAngleSeries>(job, plan, src_list, a);
       else pse_rel_launch<kPseOpDiv, kPseAngleAsin>(job, plan, src_list, a);
       break;
+  }
+  return LPM_OK;
+}
+}  // namespace
+
+namespace {
+int launch_plane_pse_rel(const SumJob& job, const SumPlan& plan, int64_t npad) {
+  const int32_t* src_list = job.src_idx;
+  if (job.sort_scratch) {
+    LPM_TRY(curve_sort2d(job.stream, job.ns, job.src_idx, job.x, job.y, job.sort_scratch, job.sort_bytes,
+                         job.sorted));
+    src_list = job.sorted;
+  }
+  PlanePseRelArgs a;
+  a.x = job.x;
+  a.y = job.y;
+  a.f = job.s1;
+  a.ks2 = static_cast<float>(1.0 / (job.eps * job.eps));
+  a.c_cut = static_cast<float>(std::sqrt(static_cast<double>(PseRel::kCutR2)) * job.eps);
+  a.src = static_cast<PlanePseRel::Rec*>(job.src_buf);
+  a.org = reinterpret_cast<PlaneRel::Origin*>(static_cast<char*>(job.src_buf) +
+                                              align_up(static_cast<size_t>(npad) * sizeof(PlanePseRel::Rec), 256));
+  a.n_tiles = plan.n_tiles;
+  a.tiles_per_chunk = plan.tiles_per_chunk;
+  a.ib = job.ib;
+  a.nt = job.nt;
+  a.partial = job.partial;
+  a.status = job.status;
+  plane_pse_rel_prep_kernel<kPseTile><<<static_cast<unsigned>(plan.n_tiles), kPseTile, 0, job.stream>>>(
+      job.x, job.y, job.s1, job.area, src_list, job.ns, const_cast<PlanePseRel::Rec*>(a.src),
+      const_cast<PlaneRel::Origin*>(a.org));
+  const dim3 grid(static_cast<unsigned>(ceil_div(job.nt, kPseThreads * kPseTpt)), static_cast<unsigned>(plan.nsplit));
+  if (job.kind == kSumPseK8Chord) {
+    plane_pse_rel_sweep_kernel<true, kPseThreads, kPseTpt, kPseTile, kPseMinB><<<grid, kPseThreads, 0, job.stream>>>(a);
+  } else {
+    plane_pse_rel_sweep_kernel<false, kPseThreads, kPseTpt, kPseTile, kPseMinB><<<grid, kPseThreads, 0, job.stream>>>(a);
   }
   return LPM_OK;
 }
@@ -677,29 +682,14 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
     case kSumPseK8Geo:
     case kSumPseGaussChord:
     case kSumPseK8Chord: {
-      const bool sphere = job.kind != kSumPseK8Chord;
-      const double inv_r = sphere ? 1.0 / job.radius : 1.0;
-      const double rscale = sphere ? job.radius : 1.0;
-      const float ks = static_cast<float>(rscale / job.eps);
       const double e4 = (job.eps * job.eps) * (job.eps * job.eps);
       const double cscale = (job.kind == kSumPseGaussChord ? 4.0 : 1.0) / kPi / e4;
       if (job.z && (job.kind == kSumPseK8Geo || job.kind == kSumPseGaussChord)) {
         // sphere: group-relative sweep with the r^2 >= 100 group cutoff (pse_rel.cuh)
         LPM_TRY(launch_pse_rel(job, plan, npad));
-      } else if (job.kind == kSumPseGaussChord) {
-        using Op = PseF32<kPseGaussChord>;
-        prep_pse32_kernel<kPseGaussChord><<<prep_grid_pad, pb, 0, job.stream>>>(
-            job.x, job.y, job.z, job.s1, job.area, job.src_idx, job.ns, npad, inv_r,
-            static_cast<Op::Rec*>(job.src_buf));
-        launch_sweep<Op, kPseThreads, kPseTpt, kPseTile, kPseMinB>(job, plan,
-                                                                   Op::Params{job.x, job.y, job.z, job.s1, inv_r, ks});
       } else {
-        using Op = PseF32<kPseK8Chord>;
-        prep_pse32_kernel<kPseK8Chord><<<prep_grid_pad, pb, 0, job.stream>>>(
-            job.x, job.y, job.z, job.s1, job.area, job.src_idx, job.ns, npad, inv_r,
-            static_cast<Op::Rec*>(job.src_buf));
-        launch_sweep<Op, kPseThreads, kPseTpt, kPseTile, kPseMinB>(job, plan,
-                                                                   Op::Params{job.x, job.y, job.z, job.s1, inv_r, ks});
+        // plane: the 2-D group-relative sweep with the same cutoff (plane_rel.cuh)
+        LPM_TRY(launch_plane_pse_rel(job, plan, npad));
       }
       finish_scalar_kernel<<<fin_grid, pb, 0, job.stream>>>(job.partial, plan.nsplit, job.nt, cscale, job.out0);
       break;

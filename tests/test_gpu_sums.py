@@ -332,6 +332,26 @@ def test_pse_gradient_divergence_vs_oracle(lg, wl, oracle_mod, nest, power, ib, 
         assert np.abs(d - ref_d).max() <= tol * np.abs(ref_d).max()
 
 
+@pytest.mark.parametrize("nest,power,m", [(5, 0.75, None), (5, 0.4, None), (7, 0.75, 2048)])
+@pytest.mark.parametrize("kernel", [2, 1])
+def test_pse_plane_fp32c_vs_oracle(lg, oracle_mod, nest, power, m, kernel):
+    """Planar PSE Laplacian (K8 and Gaussian of the chord) on the quad mesh of [-4,4]^2, FP32C
+    within 1e-4 of the oracle; eps = h^0.75 (the group cutoff skips most of the plane) and
+    h^0.4 (it skips little); a block of targets at nest 7."""
+    mesh = lg.PolyMesh2d(lg.QUAD_RECT_SEED, nest, 4.0)
+    x, y = mesh.x, mesh.y
+    rng = np.random.default_rng(nest)
+    f = np.exp(-(x * x + y * y)) * np.cos(2.0 * x) + 1e-3 * rng.random(mesh.n)
+    eps = mesh.max_edge_length ** power
+    n = mesh.n
+    ib = n // 3 if m else 0
+    ie = ib + m if m else n
+    ref = oracle_mod.pse_laplacian(x, y, None, f, mesh.area, mesh.active, eps, 1.0, kernel, ib=ib, ie=ie)
+    got = lg.pse_plane_laplacian_at_particles(x, y, f, mesh.area, mesh.active, eps, kernel=kernel,
+                                              i_begin=ib + 1, i_end=ie, mode="fp32c")[ib:ie]
+    assert np.abs(got - ref).max() <= 1e-4 * np.abs(ref).max()
+
+
 def test_check_finite_flag(lg):
     n = 4
     x = np.array([1.0, 0.0, 0.0, np.nan])
