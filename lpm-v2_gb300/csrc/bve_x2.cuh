@@ -124,32 +124,4 @@ __global__ void __launch_bounds__(THREADS, MINB) bve_sweep_x2_kernel(SweepArgs<B
   }
 }
 
-// Source records for the packed sweep: the BveF32 record values, negated (positions and -c
-// are subtracted from the target's) and replicated into both halves.
-static __global__ void prep_bve_x2_kernel(const double* x, const double* y, const double* z, const double* zeta,
-                                   const double* area, const int32_t* idx, int64_t ns, int64_t npad, double inv_a,
-                                   double s_scale, BveX2::Rec* out) {
-  const int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (k >= npad) return;
-  BveX2::Rec r;
-  if (k < ns) {
-    const int64_t j = idx[k];
-    const double px = x[j] * inv_a, py = y[j] * inv_a, pz = z[j] * inv_a;
-    float xh, xl, yh, yl, zh, zl;
-    split2(px, xh, xl);
-    split2(py, yh, yl);
-    split2(pz, zh, zl);
-    const float nc = __double2float_rn(-fma(px, px, fma(py, py, fma(pz, pz, -1.0))));
-    const float s = __double2float_rn(zeta[j] * area[j] * s_scale);
-    r.a = make_float4(-xh, -xh, -yh, -yh);
-    r.b = make_float4(-zh, -zh, -xl, -xl);
-    r.c = make_float4(-yl, -yl, -zl, -zl);
-    r.d = make_float4(nc, nc, s, s);
-  } else {
-    // inert: at the origin with zero strength (q = |p_i|^2 - c_i = 1 > 0, weight 0)
-    r.a = r.b = r.c = r.d = make_float4(0.f, 0.f, 0.f, 0.f);
-  }
-  out[k] = r;
-}
-
 }  // namespace lpm

@@ -34,7 +34,8 @@ __device__ __forceinline__ float diff2(float ah, float al, float bh, float bl) {
 //   a^2 - x_i.x_j = a^2 (|d|^2 - c_i - c_j) / 2      (exact identity, no cancellation)
 //   x_i x x_j     = a^2 (d x p_i)
 // so u_i = [ sum_j S_j d / (|d|^2 - c_i - c_j) ] x p_i with S_j = -zeta_j A_j / (2 pi a).
-// The cross product leaves the sum: per pair 17 FP32 operations + 1 MUFU.RCP.
+// The cross product leaves the sum.  BveF32 holds the target side of the FP32C sweeps
+// (bve_rel.cuh, and bve_x2.cuh for the allocation-free entry point).
 struct BveF32 {
   static constexpr int NC = 3;
   struct __align__(16) Rec {
@@ -60,19 +61,6 @@ struct BveF32 {
     const double c = fma(px, px, fma(py, py, fma(pz, pz, -1.0)));
     t.nc = __double2float_rn(-c) + 7.888609052210118e-31f;  // + 2^-100
     return t;
-  }
-  __device__ static __forceinline__ void interact(const Tgt& t, const Rec& r, float (&acc)[3]) {
-    const float dx = diff2(t.xh, t.xl, r.a.x, r.b.y);
-    const float dy = diff2(t.yh, t.yl, r.a.y, r.b.z);
-    const float dz = diff2(t.zh, t.zl, r.a.z, r.b.w);
-    float q = __fadd_rn(t.nc, r.a.w);
-    q = __fmaf_rn(dx, dx, q);
-    q = __fmaf_rn(dy, dy, q);
-    q = __fmaf_rn(dz, dz, q);
-    const float wgt = __fmul_rn(r.b.x, rcp_approx(q));
-    acc[0] = __fmaf_rn(wgt, dx, acc[0]);
-    acc[1] = __fmaf_rn(wgt, dy, acc[1]);
-    acc[2] = __fmaf_rn(wgt, dz, acc[2]);
   }
 };
 
@@ -125,39 +113,7 @@ struct BveF64 {
 
 // ============================================================ planar velocity
 // Reference: planarIncompressibleVelocity, src/PlaneIncompressibleSolver.f90:291-308.
-// FP32C: U = sum S d_y / (r^2 + delta^2), V = sum S d_x / (r^2 + delta^2), S = omega A/(2 pi);
-// u = -U, v = V.  delta^2 carries a 2^-100 offset so a self pair gives 0 * finite.
-struct PlaneF32 {
-  static constexpr int NC = 2;
-  struct __align__(16) Rec {
-    float4 a;  // x_hi, y_hi, x_lo, y_lo
-    float4 b;  // S, 0, 0, 0
-  };
-  struct Tgt {
-    float xh, yh, xl, yl, d2;
-  };
-  struct Params {
-    const double *x, *y;
-    float d2;  // delta^2 + 2^-100
-  };
-  __device__ static Tgt load_target(const Params& p, int64_t i) {
-    Tgt t;
-    split2(p.x[i], t.xh, t.xl);
-    split2(p.y[i], t.yh, t.yl);
-    t.d2 = p.d2;
-    return t;
-  }
-  __device__ static __forceinline__ void interact(const Tgt& t, const Rec& r, float (&acc)[2]) {
-    const float dx = diff2(t.xh, t.xl, r.a.x, r.a.z);
-    const float dy = diff2(t.yh, t.yl, r.a.y, r.a.w);
-    float q = __fmaf_rn(dx, dx, t.d2);
-    q = __fmaf_rn(dy, dy, q);
-    const float wgt = __fmul_rn(r.b.x, rcp_approx(q));
-    acc[0] = __fmaf_rn(wgt, dy, acc[0]);
-    acc[1] = __fmaf_rn(wgt, dx, acc[1]);
-  }
-};
-
+// (The FP32C form is plane_rel.cuh.)
 struct __align__(16) RecPlane64 {
   double x, y, q;
   long long idx;
