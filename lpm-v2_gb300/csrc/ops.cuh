@@ -381,67 +381,12 @@ struct PlaneStreamF64 {
 };
 
 // ============================================================ stream functions (FP32C)
-// Planar stream function, FP32C: SetStreamFunctionOnMesh's kernel log(sqrt(r^2)) / (2 pi) is
-// ln(r^2) / (4 pi), so each pair term is S_j ln(q_ij) with q_ij = |x_i - x_j|^2 from hi/lo
-// differences and S_j = omega_j A_j / (4 pi).  (The sphere's stream functions run on the
-// group-relative layout, stream_rel.cuh.)  The log is ln_q below, accurate to ~1 ulp.  A
-// pair with d = 0 (the self pair: hi/lo differences of identical splits are exactly 0) is
-// skipped by giving it q = 1, as the reference's j /= i skips it; q is otherwise clamped to
-// >= 2^-126 so that a degenerate pair stays finite.  The sums are over many terms of both
-// signs that cancel to a much smaller psi, so the FP32 partials are flushed into the
-// compensated accumulators every kFlush sources.
+// Both stream functions (stream_rel.cuh) sum S_j ln(q_ij) with ln from ln_q2, accurate to
+// about 1 ulp.  A pair with d = 0 (the self pair) is skipped by giving it q = 1, as the
+// reference's j /= i skips it; q is otherwise clamped to >= 2^-126 so that a degenerate pair
+// stays finite.  The sums are over many terms of both signs that cancel to a much smaller
+// psi, so the FP32 partials are flushed into the compensated accumulators every 32 sources.
 constexpr float kLogFloor = 1.1754943508222875e-38f;  // 2^-126
 constexpr double kInv4Pi = 0.079577471545947667884;   // 1 / (4 pi)
-
-// Natural log of a positive normal float, from q = 2^k m with m in [sqrt(1/2), sqrt(2))
-// and ln m = 2 atanh(t), t = (m - 1) / (m + 1), |t| <= 0.1716 (the series
-// 2 (t + t^3/3 + t^5/5 + t^7/7 + t^9/9) truncates at 2 t^11 / 11 < 7e-10).  t is one
-// reciprocal (MUFU) refined by one residual step against the exact denominator 2 + f, so
-// ln m is good to about 1 ulp; k ln 2 is added last.
-__device__ __forceinline__ float ln_q(float q) {
-  const int bits = __float_as_int(q);
-  const int k = (bits - 0x3f3504f3) >> 23;  // 0x3f3504f3 = fl(sqrt(1/2))
-  const float m = __int_as_float(bits - (k << 23));
-  const float kf = __fadd_rn(__int_as_float(k + 0x4b400000), -12582912.0f);  // exact float(k)
-  const float f = __fadd_rn(m, -1.0f);  // exact (Sterbenz)
-  const float r = rcp_approx(__fadd_rn(f, 2.0f));
-  const float t0 = __fmul_rn(f, r);
-  const float res = __fmaf_rn(-t0, f, __fmaf_rn(-2.0f, t0, f));  // f - t0 (2 + f)
-  const float t = __fmaf_rn(r, res, t0);
-  const float tt = __fadd_rn(t, t);
-  const float s = __fmul_rn(t, t);
-  float p = __fmaf_rn(0.11111111f, s, 0.14285715f);
-  p = __fmaf_rn(p, s, 0.2f);
-  p = __fmaf_rn(p, s, 0.33333334f);
-  const float lnm = __fmaf_rn(__fmul_rn(tt, s), p, tt);
-  return __fmaf_rn(kf, 0.69314718f, lnm);
-}
-
-struct PlaneStreamF32 {
-  static constexpr int NC = 1;
-  static constexpr int kFlush = 32;
-  struct __align__(16) Rec {
-    float4 a;  // x_hi, y_hi, x_lo, y_lo
-    float4 b;  // S, 0, 0, 0
-  };
-  struct Tgt {
-    float xh, yh, xl, yl;
-  };
-  struct Params {
-    const double *x, *y;
-  };
-  __device__ static Tgt load_target(const Params& p, int64_t i) {
-    Tgt t;
-    split2(p.x[i], t.xh, t.xl);
-    split2(p.y[i], t.yh, t.yl);
-    return t;
-  }
-  __device__ static __forceinline__ void interact(const Tgt& t, const Rec& r, float (&acc)[1]) {
-    const float dx = diff2(t.xh, t.xl, r.a.x, r.a.z);
-    const float dy = diff2(t.yh, t.yl, r.a.y, r.a.w);
-    const float u = __fmaf_rn(dx, dx, __fmul_rn(dy, dy));
-    acc[0] = __fmaf_rn(r.b.x, ln_q(u != 0.0f ? fmaxf(u, kLogFloor) : 1.0f), acc[0]);
-  }
-};
 
 }  // namespace lpm

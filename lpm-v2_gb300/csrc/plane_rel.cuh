@@ -32,7 +32,7 @@ struct PlaneRel {
   };
   struct __align__(16) Origin {
     float4 o;  // o_hi.x, o_hi.y, o_lo.x, o_lo.y
-    float4 f;  // R (the group radius about o), 0, 0, 0
+    float4 f;  // R (the group radius about o), S_g hi, S_g lo (S_g = sum of the group's S_j), 0
   };
   struct Pair {
     float2 xh, yh, xl, yl;
@@ -179,15 +179,16 @@ __global__ void __launch_bounds__(THREADS, MINB) plane_rel_sweep_kernel(PlaneRel
 }
 
 // Records and origins of one tile of TILE sources (one CTA of TILE threads): each group of
-// kGroup sources reduces its centroid o and its radius R about o, and every record is
-// written as rel2(p_j, o) -- the operations the sweep uses for targets.  s_scale = 1/(2 pi).
+// kGroup sources reduces its centroid o, its radius R about o and its total S_g (of the FP32
+// strengths), and every record is written as rel2(p_j, o) -- the operations the sweep uses
+// for targets.  s_scale = 1/(2 pi) for the velocity, 1/(4 pi) for the stream function.
 template <int TILE>
 __global__ void __launch_bounds__(TILE) plane_rel_prep_kernel(const double* x, const double* y, const double* omega,
                                                               const double* area, const int32_t* sorted, int64_t ns,
                                                               double s_scale, PlaneRel::Rec* out,
                                                               PlaneRel::Origin* org) {
   constexpr int G = PlaneRel::kGroup;
-  __shared__ double red[2][TILE];
+  __shared__ double red[3][TILE];
   __shared__ float fmax_[TILE], cntf[TILE];
   const int64_t t = blockIdx.x;
   const int tid = threadIdx.x;
@@ -196,14 +197,17 @@ __global__ void __launch_bounds__(TILE) plane_rel_prep_kernel(const double* x, c
   const int32_t j = valid ? sorted[k] : 0;
   const int lane = tid % G;
   const double px = valid ? x[j] : 0.0, py = valid ? y[j] : 0.0;
+  const float s = valid ? __double2float_rn(omega[j] * area[j] * s_scale) : 0.f;
   red[0][tid] = px;
   red[1][tid] = py;
+  red[2][tid] = s;
   cntf[tid] = valid ? 1.f : 0.f;
   __syncthreads();
   for (int w = G / 2; w > 0; w >>= 1) {
     if (lane < w) {
       red[0][tid] += red[0][tid + w];
       red[1][tid] += red[1][tid + w];
+      red[2][tid] += red[2][tid + w];
       cntf[tid] += cntf[tid + w];
     }
     __syncthreads();
@@ -227,7 +231,6 @@ __global__ void __launch_bounds__(TILE) plane_rel_prep_kernel(const double* x, c
     rel2(h, l, oxh, oxl, sxh, sxl);
     split2(py, h, l);
     rel2(h, l, oyh, oyl, syh, syl);
-    const float s = __double2float_rn(omega[j] * area[j] * s_scale);
     r.a = make_float4(-sxh, -sxh, -syh, -syh);
     r.b = make_float4(s, s, -sxl, -sxl);
     r.c = make_float4(-syl, -syl, 0.f, 0.f);
@@ -239,7 +242,9 @@ __global__ void __launch_bounds__(TILE) plane_rel_prep_kernel(const double* x, c
   if (lane == 0) {
     PlaneRel::Origin o;
     o.o = make_float4(oxh, oyh, oxl, oyl);
-    o.f = make_float4(fmax_[g0], 0.f, 0.f, 0.f);
+    float sgh, sgl;
+    split2(red[2][g0], sgh, sgl);
+    o.f = make_float4(fmax_[g0], sgh, sgl, 0.f);
     org[t * (TILE / G) + tid / G] = o;
   }
 }

@@ -17,6 +17,7 @@
 
 #include "bve_rel.cuh"
 #include "ops.cuh"
+#include "plane_rel.cuh"
 
 namespace lpm {
 
@@ -31,14 +32,38 @@ struct StreamRel {
   static constexpr int kFlush = 32;
 };
 
-// ln_q of two lanes at once: the integer exponent split per lane, the rest packed.  The
-// argument is a positive normal float (the sweep clamps it).
-__device__ __forceinline__ float2 ln_q2(float2 q) {
-  const int b0 = __float_as_int(q.x), b1 = __float_as_int(q.y);
-  const int k0 = (b0 - 0x3f3504f3) >> 23, k1 = (b1 - 0x3f3504f3) >> 23;
-  const float2 m = make_float2(__int_as_float(b0 - (k0 << 23)), __int_as_float(b1 - (k1 << 23)));
-  const float2 kf = __fadd2_rn(make_float2(__int_as_float(k0 + 0x4b400000), __int_as_float(k1 + 0x4b400000)),
-                               make_float2(-12582912.0f, -12582912.0f));
+// Natural log of two positive normal floats (the sweeps clamp them): per lane q = 2^k m with
+// m in [sqrt(1/2), sqrt(2)) (an integer split; 0x3f3504f3 = fl(sqrt(1/2))), then, packed,
+// ln m = 2 atanh(t), t = (m - 1) / (m + 1), |t| <= 0.1716, by the series
+// 2 (t + t^3/3 + t^5/5 + t^7/7 + t^9/9) (truncated at 2 t^11 / 11 < 7e-10).  t is one
+// reciprocal (MUFU) refined by one residual step against the exact denominator 2 + f, so
+// ln m is good to about 1 ulp; k ln 2 is added last (k is exact in float).
+// The exponent split of a positive normal float with bits b: q = 2^k m, m in [sqrt(1/2),
+// sqrt(2)) (0x3f3504f3 = fl(sqrt(1/2))); returns k and writes the bits of m.  Inline PTX
+// keeps the integer sequence as written: the same four operations in C++, fed straight
+// from a packed FFMA2 result in the planar stream sweep's far loop, gave (nvcc 13.0,
+// sm_103a) logs as if k were b - 0x3f3504f3, unshifted.
+__device__ __forceinline__ int exp_split(int b, int& mb) {
+  int k;
+  asm("{\n\t.reg .s32 t;\n\tsub.s32 t, %2, 0x3f3504f3;\n\tshr.s32 %0, t, 23;\n\tshl.b32 t, %0, 23;\n\t"
+      "sub.s32 %1, %2, t;\n\t}"
+      : "=r"(k), "=r"(mb)
+      : "r"(b));
+  return k;
+}
+
+// ln_q2_shift(q, shift_bias(s0, s1)) is (ln q.x - s0 ln 2, ln q.y - s1 ln 2) for small
+// integers s: the shift only moves the exponent k (the float k - s is exact), so it costs
+// nothing -- it replaces the constant of the magic-number conversion of k.
+__device__ __forceinline__ float2 shift_bias(int s0, int s1) {
+  return make_float2(-12582912.0f - static_cast<float>(s0), -12582912.0f - static_cast<float>(s1));
+}
+
+__device__ __forceinline__ float2 ln_q2_shift(float2 q, float2 bias) {
+  int m0, m1;
+  const int k0 = exp_split(__float_as_int(q.x), m0), k1 = exp_split(__float_as_int(q.y), m1);
+  const float2 m = make_float2(__int_as_float(m0), __int_as_float(m1));
+  const float2 kf = __fadd2_rn(make_float2(__int_as_float(k0 + 0x4b400000), __int_as_float(k1 + 0x4b400000)), bias);
   const float2 f = __fadd2_rn(m, make_float2(-1.0f, -1.0f));
   const float2 den = __fadd2_rn(f, make_float2(2.0f, 2.0f));
   const float2 r = make_float2(rcp_approx(den.x), rcp_approx(den.y));
@@ -53,6 +78,8 @@ __device__ __forceinline__ float2 ln_q2(float2 q) {
   const float2 lnm = __ffma2_rn(__fmul2_rn(tt, s), p, tt);
   return __ffma2_rn(kf, make_float2(0.69314718f, 0.69314718f), lnm);
 }
+
+__device__ __forceinline__ float2 ln_q2(float2 q) { return ln_q2_shift(q, shift_bias(0, 0)); }
 
 // The log argument of a pair: q clamped to >= 2^-126, or 1 (a zero term) when d = 0.
 __device__ __forceinline__ float2 stream_arg(float2 u, float2 q) {
@@ -231,6 +258,169 @@ __global__ void __launch_bounds__(TILE) stream_rel_prep_kernel(const double* x, 
   }
   out[k] = r;
   if (threadIdx.x % BveRel::kGroup == 0) org[t * (TILE / BveRel::kGroup) + threadIdx.x / BveRel::kGroup] = group_origin(f);
+}
+
+// ====================================================================== planar stream function
+// SetStreamFunctionOnMesh, src/PlanarIncompressible.f90:470-505: psi_i = sum_{j != i}
+// ln(|x_i - x_j|^2) omega_j A_j / (4 pi), on the planar group-relative layout (plane_rel.cuh;
+// plane_rel_prep_kernel writes S_j = omega_j A_j / (4 pi) and each group's total S_g).
+//
+// The terms are centred per target and group: with a power of two 2^k near
+// max(|t - o|^2, R^2) (k from the exponent split of ln_q2),
+//   sum_j S_j ln u_j = sum_j S_j (ln u_j - k ln 2) + k ln 2 S_g,
+// so the FP32 partials hold terms of size |S_j| (|ln(u_j 2^-k)| <= ~1.2 for a far group)
+// instead of |S_j ln u_j|, and the second part is carried exactly: S_g k as a product of
+// a (hi, lo) float pair and a small integer into its own compensated pair, times ln 2 in
+// FP64 at the end.  ln_q2_shift applies the shift for free.  A far group (every target of the
+// warp at |t - o| > 3R, so u_j > 0) needs no select; in a near group the self pair (u = 0,
+// the lo parts cancel bit for bit) takes q = 1, whose centred term -k ln 2 cancels the
+// target's own share of k ln 2 S_g.  Per target pair and source (far form): d (2 FADD2),
+// |d|^2 (2), ln (ln_q2_shift: 4 integer operations per lane, 15 packed, 2 MUFU) and the
+// accumulation (1 FFMA2).  Near partials are flushed every 16 sources, far ones per group.
+template <int THREADS, int TPT, int TILE, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB) plane_stream_rel_sweep_kernel(PlaneRelArgs a) {
+  static_assert(TPT % 2 == 0, "targets come in pairs");
+  constexpr int NP = TPT / 2;
+  constexpr int G = PlaneRel::kGroup;
+  constexpr int GPT = TILE / G;
+  constexpr int FLN = 16;
+  static_assert(G % FLN == 0, "flush interval must divide the group");
+  using Rec = PlaneRel::Rec;
+  __shared__ __align__(128) Rec stage[2][TILE];
+  __shared__ __align__(8) uint64_t bars[2];
+
+  const int64_t chunk = blockIdx.y;
+  const int64_t tile0 = chunk * a.tiles_per_chunk;
+  int64_t ntl = a.n_tiles - tile0;
+  if (ntl > a.tiles_per_chunk) ntl = a.tiles_per_chunk;
+  if (ntl < 0) ntl = 0;
+
+  PlaneRel::Pair pr[NP];
+  float2 hs[NP], ls[NP], hk[NP], lk[NP];
+  const int64_t first = static_cast<int64_t>(blockIdx.x) * (THREADS * TPT);
+  const int64_t count = a.nt - first < THREADS * TPT ? a.nt - first : THREADS * TPT;
+#pragma unroll
+  for (int p = 0; p < NP; ++p) {
+    int64_t i0 = (2 * p) * THREADS + threadIdx.x, i1 = (2 * p + 1) * THREADS + threadIdx.x;
+    if (i0 >= count) i0 = count - 1;  // duplicates of a valid target; results not stored
+    if (i1 >= count) i1 = count - 1;
+    float h0, l0, h1, l1;
+    split2(a.x[a.ib + first + i0], h0, l0);
+    split2(a.x[a.ib + first + i1], h1, l1);
+    pr[p].xh = make_float2(h0, h1);
+    pr[p].xl = make_float2(l0, l1);
+    split2(a.y[a.ib + first + i0], h0, l0);
+    split2(a.y[a.ib + first + i1], h1, l1);
+    pr[p].yh = make_float2(h0, h1);
+    pr[p].yl = make_float2(l0, l1);
+    hs[p] = ls[p] = hk[p] = lk[p] = make_float2(0.f, 0.f);
+  }
+  constexpr float kTiny = 7.888609052210118e-31f;  // 2^-100: centring and near floor
+  constexpr float kHuge = 1.2676506002282294e30f;  // 2^100
+
+  pipe_init(bars);
+  uint32_t g = 0;
+  int64_t tile = tile0;
+  staged_sweep<Rec, TILE>(a.src, tile0, ntl, stage[0], stage[1], bars, g, a.status, [&](const Rec* tl) {
+    const PlaneRel::Origin* og = a.org + tile * GPT;
+#pragma unroll 1
+    for (int g0 = 0; g0 < TILE; g0 += G) {
+      const PlaneRel::Origin o = og[g0 / G];
+      const Rec* gr = tl + g0;
+      float2 tx[NP], ty[NP];
+      float2 bias[NP];
+      bool near = false;
+      const float r2 = o.f.x * o.f.x;
+      const float lim = fmaxf(PlaneRel::kNearFactor * PlaneRel::kNearFactor * r2, kTiny);
+#pragma unroll
+      for (int p = 0; p < NP; ++p) {
+        tx[p] = rel1x2(pr[p].xh, pr[p].xl, o.o.x, o.o.z);
+        ty[p] = rel1x2(pr[p].yh, pr[p].yl, o.o.y, o.o.w);
+        const float2 n2 = __ffma2_rn(ty[p], ty[p], __fmul2_rn(tx[p], tx[p]));
+        near |= !(n2.x > lim) | !(n2.y > lim);
+        // the centring shift k: the exponent of max(|t - o|^2, R^2) clamped to [2^-100, 2^100]
+        const float c0 = fminf(fmaxf(fmaxf(n2.x, r2), kTiny), kHuge);
+        const float c1 = fminf(fmaxf(fmaxf(n2.y, r2), kTiny), kHuge);
+        int mb;
+        const int sh0 = exp_split(__float_as_int(c0), mb);
+        const int sh1 = exp_split(__float_as_int(c1), mb);
+        bias[p] = shift_bias(sh0, sh1);
+        // k S_g into (hk, lk): S_hi k is exact as a product and its error term
+        const float2 kf = make_float2(static_cast<float>(sh0), static_cast<float>(sh1));
+        const float2 ph = __fmul2_rn(make_float2(o.f.y, o.f.y), kf);
+        const float2 pe = __ffma2_rn(make_float2(o.f.y, o.f.y), kf, make_float2(-ph.x, -ph.y));
+        comp_add(hk[p].x, lk[p].x, ph.x);
+        comp_add(hk[p].y, lk[p].y, ph.y);
+        lk[p] = __ffma2_rn(make_float2(o.f.z, o.f.z), kf, __fadd2_rn(lk[p], pe));
+      }
+      if (!__any_sync(0xffffffffu, near)) {
+        // far group: d = t_hi - s_hi, u > 0
+        float2 acc[NP];
+#pragma unroll
+        for (int p = 0; p < NP; ++p) acc[p] = make_float2(0.f, 0.f);
+#pragma unroll 4
+        for (int j = 0; j < G; ++j) {
+          const float4 ra = gr[j].a, rb = gr[j].b;
+#pragma unroll
+          for (int p = 0; p < NP; ++p) {
+            const float2 dx = __fadd2_rn(tx[p], lo2(ra));
+            const float2 dy = __fadd2_rn(ty[p], hi2(ra));
+            const float2 u = __ffma2_rn(dy, dy, __fmul2_rn(dx, dx));
+            acc[p] = __ffma2_rn(lo2(rb), ln_q2_shift(u, bias[p]), acc[p]);
+          }
+        }
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+          comp_add(hs[p].x, ls[p].x, acc[p].x);
+          comp_add(hs[p].y, ls[p].y, acc[p].y);
+        }
+      } else {
+        // near group: d = (t_hi - s_hi) + (t_lo - s_lo)
+        float2 txh[NP], tyh[NP], txl[NP], tyl[NP];
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+          rel2x2(pr[p].xh, pr[p].xl, o.o.x, o.o.z, txh[p], txl[p]);
+          rel2x2(pr[p].yh, pr[p].yl, o.o.y, o.o.w, tyh[p], tyl[p]);
+        }
+#pragma unroll 1
+        for (int j0 = 0; j0 < G; j0 += FLN) {
+          float2 acc[NP];
+#pragma unroll
+          for (int p = 0; p < NP; ++p) acc[p] = make_float2(0.f, 0.f);
+          for (int j = j0; j < j0 + FLN; ++j) {
+            const float4 ra = gr[j].a, rb = gr[j].b, rc = gr[j].c;
+#pragma unroll
+            for (int p = 0; p < NP; ++p) {
+              const float2 dx = __fadd2_rn(__fadd2_rn(txh[p], lo2(ra)), __fadd2_rn(txl[p], hi2(rb)));
+              const float2 dy = __fadd2_rn(__fadd2_rn(tyh[p], hi2(ra)), __fadd2_rn(tyl[p], lo2(rc)));
+              const float2 u = __ffma2_rn(dy, dy, __fmul2_rn(dx, dx));
+              acc[p] = __ffma2_rn(lo2(rb), ln_q2_shift(stream_arg(u, u), bias[p]), acc[p]);
+            }
+          }
+#pragma unroll
+          for (int p = 0; p < NP; ++p) {
+            comp_add(hs[p].x, ls[p].x, acc[p].x);
+            comp_add(hs[p].y, ls[p].y, acc[p].y);
+          }
+        }
+      }
+    }
+    ++tile;
+  });
+
+  constexpr double kLn2 = 0.69314718055994530942;
+#pragma unroll
+  for (int p = 0; p < NP; ++p) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int64_t il = first + (2 * p + h) * THREADS + threadIdx.x;
+      if (il < a.nt) {
+        const double c = static_cast<double>(h ? hk[p].y : hk[p].x) + static_cast<double>(h ? lk[p].y : lk[p].x);
+        a.partial[chunk * a.nt + il] =
+            (static_cast<double>(h ? hs[p].y : hs[p].x) + static_cast<double>(h ? ls[p].y : ls[p].x)) + kLn2 * c;
+      }
+    }
+  }
 }
 
 }  // namespace lpm

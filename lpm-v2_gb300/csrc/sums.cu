@@ -162,27 +162,6 @@ __global__ void __launch_bounds__(1024) stream_totals_kernel(const double* qr, c
   }
 }
 
-__global__ void prep_pstream32_kernel(const double* x, const double* y, const double* omega, const double* area,
-                                      const int32_t* idx, int64_t ns, int64_t npad, PlaneStreamF32::Rec* out) {
-  const int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (k >= npad) return;
-  PlaneStreamF32::Rec r;
-  if (k < ns) {
-    const int64_t j = idx[k];
-    float h, l;
-    split2(x[j], h, l);
-    r.a.x = h;
-    r.a.z = l;
-    split2(y[j], h, l);
-    r.a.y = h;
-    r.a.w = l;
-    r.b = make_float4(__double2float_rn(omega[j] * area[j] * kInv4Pi), 0.f, 0.f, 0.f);
-  } else {
-    r.a = r.b = make_float4(0.f, 0.f, 0.f, 0.f);
-  }
-  out[k] = r;
-}
-
 // ------------------------------------------------------------------ finish kernels
 // Fixed-order FP64 reduction over the split-K chunks, then the per-target epilogue.
 
@@ -290,7 +269,7 @@ size_t rec_bytes(int kind, int mode) {
     case kSumSphereStream:
       return sizeof(StreamRel::Rec);
     case kSumPlaneStream:
-      return sizeof(PlaneStreamF32::Rec);
+      return sizeof(PlaneRel::Rec);
     case kSumPseK8Geo:
     case kSumPseGaussChord:
     case kSumPseGrad:
@@ -355,12 +334,13 @@ int64_t choose_split(int64_t blocks, int64_t tiles, int64_t slots, int64_t max_s
 bool sum_uses_sorted_sources(int kind, int mode) {
   return mode == LPM_MODE_FP32C && (kind == kSumBve || kind == kSumBveMesh || kind == kSumPlane ||
                                     kind == kSumSphereStream || kind == kSumPseK8Geo || kind == kSumPseGaussChord ||
-                                    kind == kSumPseK8Chord || kind == kSumPseGrad || kind == kSumPseDiv);
+                                    kind == kSumPseK8Chord || kind == kSumPseGrad || kind == kSumPseDiv ||
+                                    kind == kSumPlaneStream);
 }
 
 size_t sort_scratch_bytes(int kind, int64_t ns) {
   // planar kinds sort in 2-D; the Gaussian-chord Laplacian serves the plane and the sphere
-  if (kind == kSumPlane || kind == kSumPseK8Chord) return curve_sort2d_bytes(ns);
+  if (kind == kSumPlane || kind == kSumPseK8Chord || kind == kSumPlaneStream) return curve_sort2d_bytes(ns);
   if (kind == kSumPseGaussChord) return std::max(curve_sort_bytes(ns), curve_sort2d_bytes(ns));
   return curve_sort_bytes(ns);
 }
@@ -748,11 +728,33 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
       break;
     }
     case kSumPlaneStream: {
-      prep_pstream32_kernel<<<prep_grid_pad, pb, 0, job.stream>>>(job.x, job.y, job.s1, job.area, job.src_idx,
-                                                                  job.ns, npad,
-                                                                  static_cast<PlaneStreamF32::Rec*>(job.src_buf));
-      launch_sweep<PlaneStreamF32, kStreamThreads, kStreamTpt, kStreamTile, kStreamMinB>(
-          job, plan, PlaneStreamF32::Params{job.x, job.y});
+      const int32_t* src_list = job.src_idx;
+      if (job.sort_scratch) {
+        LPM_TRY(curve_sort2d(job.stream, job.ns, job.src_idx, job.x, job.y, job.sort_scratch, job.sort_bytes,
+                             job.sorted));
+        src_list = job.sorted;
+      }
+      PlaneRel::Rec* recs = static_cast<PlaneRel::Rec*>(job.src_buf);
+      PlaneRel::Origin* org = reinterpret_cast<PlaneRel::Origin*>(
+          static_cast<char*>(job.src_buf) + align_up(static_cast<size_t>(npad) * sizeof(PlaneRel::Rec), 256));
+      plane_rel_prep_kernel<kStreamTile><<<static_cast<unsigned>(plan.n_tiles), kStreamTile, 0, job.stream>>>(
+          job.x, job.y, job.s1, job.area, src_list, job.ns, kInv4Pi, recs, org);
+      PlaneRelArgs a;
+      a.x = job.x;
+      a.y = job.y;
+      a.d2 = 0.f;
+      a.src = recs;
+      a.org = org;
+      a.n_tiles = plan.n_tiles;
+      a.tiles_per_chunk = plan.tiles_per_chunk;
+      a.ib = job.ib;
+      a.nt = job.nt;
+      a.partial = job.partial;
+      a.status = job.status;
+      const dim3 grid(static_cast<unsigned>(ceil_div(job.nt, kStreamThreads * kStreamTpt)),
+                      static_cast<unsigned>(plan.nsplit));
+      plane_stream_rel_sweep_kernel<kStreamThreads, kStreamTpt, kStreamTile, kStreamMinB>
+          <<<grid, kStreamThreads, 0, job.stream>>>(a);
       finish_stream_kernel<<<fin_grid, pb, 0, job.stream>>>(job.partial, plan.nsplit, job.nt, 1, 0.0, nullptr, nullptr,
                                                             job.out0, nullptr);
       break;
