@@ -121,6 +121,68 @@ int lpm_pse_sphere_divergence(int64_t n, const double* x, const double* y, const
                               double radius, int64_t i_begin, int64_t i_end, double* div,
                               int mode);
 
+/* The remaining PSE operators and the shallow-water integrals have only LPM_MODE_FP64 (the
+ * reference's association, like the other FP64 sums); LPM_MODE_FP32C returns LPM_ERR_ARG. */
+
+/* Replaces PSEPlaneGradientAtParticles (src/PSEDirectSum.f90:180-217): (gx, gy) =
+ * eps**-4 sum_j (f_j + f_i)(x_i - x_j) K1(|x_i - x_j|/eps) A_j. */
+int lpm_pse_plane_gradient(int64_t n, const double* x, const double* y, const double* f,
+                           const double* area, const int32_t* active, double eps, int64_t i_begin,
+                           int64_t i_end, double* gx, double* gy, int mode);
+
+/* Replaces PSEPlaneSecondPartialsAtParticles (src/PSEDirectSum.f90:269-320): from the gradient
+ * field (gx, gy), the second partials (dxx, dxy, dyy); dxy is 0.5 (d_y gx + d_x gy). */
+int lpm_pse_plane_second_partials(int64_t n, const double* x, const double* y, const double* gx,
+                                  const double* gy, const double* area, const int32_t* active,
+                                  double eps, int64_t i_begin, int64_t i_end, double* dxx,
+                                  double* dxy, double* dyy, int mode);
+
+/* Replaces PSEPlaneDoubleDotProductAtParticles (src/PSEDirectSum.f90:322-365): the double dot
+ * product ux ux + 2 uy vx + vy vy of the velocity (u, v). */
+int lpm_pse_plane_double_dot(int64_t n, const double* x, const double* y, const double* u,
+                             const double* v, const double* area, const int32_t* active, double eps,
+                             int64_t i_begin, int64_t i_end, double* ddot, int mode);
+
+/* Replaces PSESphereDoubleDotProductAtParticles (src/PSEDirectSum.f90:367-418), including its
+ * pairing of w_j with v_i in the third row (:399-404).  radius is SphereDistance's radius. */
+int lpm_pse_sphere_double_dot(int64_t n, const double* x, const double* y, const double* z,
+                              const double* u, const double* v, const double* w, const double* area,
+                              const int32_t* active, double eps, double radius, int64_t i_begin,
+                              int64_t i_end, double* ddot, int mode);
+
+enum { LPM_GEOMETRY_PLANE = 0, LPM_GEOMETRY_SPHERE = 1 };
+
+/* Replaces PSEPlaneInterpolateScalar (geometry LPM_GEOMETRY_PLANE, chord distance) and
+ * PSESphereInterpolateScalar (LPM_GEOMETRY_SPHERE, great-circle distance times radius),
+ * src/PSEDirectSum.f90:128-168, evaluated at m query points (qx, qy, qz) at once:
+ * out_k = sum_j f_j A_j Kdelta8(dist(q_k, x_j)/eps) / eps**2.  z and qz may be NULL in the
+ * plane (zeros). */
+int lpm_pse_interpolate_scalar(int64_t n, const double* x, const double* y, const double* z,
+                               const double* f, const double* area, const int32_t* active, double eps,
+                               double radius, int geometry, int64_t m, const double* qx,
+                               const double* qy, const double* qz, double* out, int mode);
+
+/* Replaces SWEPlaneRHSIntegrals (src/SWEPlaneSolver.f90:457-534): velocity (u, v) from
+ * vorticity and divergence, the double dot product of the velocity gradient and the PSE
+ * Laplacian of the surface height.  surf_height = h + topoFn(x, y), evaluated by the caller
+ * (the Fortran shim) once per particle. */
+int lpm_swe_plane_rhs_integrals(int64_t n, const double* x, const double* y, const double* vort,
+                                const double* div, const double* surf_height, const double* area,
+                                const int32_t* active, double eps, int64_t i_begin, int64_t i_end,
+                                double* u, double* v, double* double_dot, double* lap_surf, int mode);
+
+/* Replaces SWESphereRHSIntegrals (src/SphereSWESolver.f90:299-372) as the reference computes
+ * it: (u, v, w) from relative vorticity and divergence on the sphere of radius `radius`, the
+ * surface-height Laplacian with K8(SphereDistance/eps)/eps**2 (SphereDistance scaled by the
+ * SphereGeometry module's SphereRadius, `sphere_radius`; no further 1/eps**2), and
+ * double_dot = 0 (the reference never sets it).  surf_height = h + topoFn(x, y, z). */
+int lpm_swe_sphere_rhs_integrals(int64_t n, const double* x, const double* y, const double* z,
+                                 const double* relvort, const double* div, const double* surf_height,
+                                 const double* area, const int32_t* active, double radius,
+                                 double sphere_radius, double eps, int64_t i_begin, int64_t i_end,
+                                 double* u, double* v, double* w, double* double_dot,
+                                 double* lap_surf, int mode);
+
 /* Replaces SetStreamFunctionsOnMesh (src/SphereBVE.f90:445-485): psi = sum G zeta A with
  * G = -log(a^2 - x_i.x_j)/(4 pi), for the relative and absolute vorticity, j != i.
  * LPM_MODE_FP64 follows the Fortran loop (its log is CUDA's, so agreement is to ~1e-15

@@ -380,6 +380,242 @@ struct PlaneStreamF64 {
   static constexpr bool kSkipSelf = true;
 };
 
+// ============================================================ more PSE operators, SWE integrals (FP64)
+// Each restates its Fortran loop body with explicit roundings, like the operators above.
+
+// bivariateDeltaKernel8, src/PSEDirectSum.f90:611-616, with the power chain of k8_f64
+__device__ __forceinline__ double kdelta8_f64(double r) {
+  const double r2 = __dmul_rn(r, r);
+  const double r3 = __dmul_rn(r, r2);
+  const double r4 = __dmul_rn(r2, r2);
+  const double r6 = __dmul_rn(r3, r3);
+  const double poly = __dsub_rn(__dadd_rn(__dsub_rn(4.0, __dmul_rn(6.0, r2)), __dmul_rn(2.0, r4)), __ddiv_rn(r6, 6.0));
+  return __ddiv_rn(__dmul_rn(poly, exp(-__dmul_rn(r, r))), 3.1415926535897932384626433832795027975);
+}
+
+// ChordDistance of two planar particles (z = 0 on both): sqrt((dx^2 + dy^2) + 0)
+__device__ __forceinline__ double plane_chord_f64(double ax, double ay, double bx, double by) {
+  const double d1 = __dsub_rn(bx, ax), d2 = __dsub_rn(by, ay);
+  return __dsqrt_rn(__dadd_rn(__dmul_rn(d1, d1), __dmul_rn(d2, d2)));
+}
+
+struct PseExtF64Params {
+  const double *x, *y, *z, *s1, *s2, *s3;  // positions and the target-side fields
+  double eps, eps2, eps3, radius, radius2, k0, scale;
+  double *o0, *o1, *o2, *o3;
+};
+
+// PSEPlaneGradientAtParticles, src/PSEDirectSum.f90:180-217 (Rec64: q = f_j, r = A_j):
+// g += (((f_j + f_i) (x_i - x_j)) K1) / eps**3 * A_j, then multiplied by 1/eps
+struct PsePlaneGradF64 {
+  struct Tgt {
+    double x, y, f;
+  };
+  struct Acc {
+    double gx, gy;
+  };
+  __device__ static Tgt load(const PseExtF64Params& p, int64_t i) { return Tgt{p.x[i], p.y[i], p.s1[i]}; }
+  __device__ static __forceinline__ void interact(const PseExtF64Params& p, const Tgt& t, const Rec64& r, Acc& a) {
+    const double k1 = k1_f64(__ddiv_rn(plane_chord_f64(t.x, t.y, r.x, r.y), p.eps));
+    const double fs = __dadd_rn(r.q, t.f);
+    a.gx = __dadd_rn(a.gx, __dmul_rn(__ddiv_rn(__dmul_rn(__dmul_rn(fs, __dsub_rn(t.x, r.x)), k1), p.eps3), r.r));
+    a.gy = __dadd_rn(a.gy, __dmul_rn(__ddiv_rn(__dmul_rn(__dmul_rn(fs, __dsub_rn(t.y, r.y)), k1), p.eps3), r.r));
+  }
+  __device__ static void store(const PseExtF64Params& p, int64_t i, int64_t il, const Acc& a) {
+    p.o0[il] = __dmul_rn(p.scale, a.gx);
+    p.o1[il] = __dmul_rn(p.scale, a.gy);
+  }
+  static constexpr bool kSkipSelf = false;
+};
+
+// The four planar sums of PSEPlaneSecondPartialsAtParticles (:286-301) and
+// PSEPlaneDoubleDotProductAtParticles (:339-354) (RecVec64: vx = a_j, vy = b_j):
+// s_ab += (((a_j + a_i) (x_b,i - x_b,j)) / eps) K1 / eps**2 * A_j
+struct PlaneD4F64 {
+  struct Tgt {
+    double x, y, a, b;
+  };
+  struct Acc {
+    double ax, ay, bx, by;
+  };
+  __device__ static Tgt load(const PseExtF64Params& p, int64_t i) { return Tgt{p.x[i], p.y[i], p.s1[i], p.s2[i]}; }
+  __device__ static __forceinline__ void interact(const PseExtF64Params& p, const Tgt& t, const RecVec64& r,
+                                                  Acc& a) {
+    const double kout = __ddiv_rn(k1_f64(__ddiv_rn(plane_chord_f64(t.x, t.y, r.x, r.y), p.eps)), p.eps2);
+    const double dx = __dsub_rn(t.x, r.x), dy = __dsub_rn(t.y, r.y);
+    const double sa = __dadd_rn(r.vx, t.a), sb = __dadd_rn(r.vy, t.b);
+    a.ax = __dadd_rn(a.ax, __dmul_rn(__dmul_rn(__ddiv_rn(__dmul_rn(sa, dx), p.eps), kout), r.area));
+    a.ay = __dadd_rn(a.ay, __dmul_rn(__dmul_rn(__ddiv_rn(__dmul_rn(sa, dy), p.eps), kout), r.area));
+    a.bx = __dadd_rn(a.bx, __dmul_rn(__dmul_rn(__ddiv_rn(__dmul_rn(sb, dx), p.eps), kout), r.area));
+    a.by = __dadd_rn(a.by, __dmul_rn(__dmul_rn(__ddiv_rn(__dmul_rn(sb, dy), p.eps), kout), r.area));
+  }
+  static constexpr bool kSkipSelf = false;
+};
+
+// PSEPlaneSecondPartialsAtParticles: xx = dxx, xy = 0.5 (dxy + dyx), yy = dyy, times 1/eps
+struct PsePlaneSecondF64 : PlaneD4F64 {
+  __device__ static void store(const PseExtF64Params& p, int64_t i, int64_t il, const Acc& a) {
+    p.o0[il] = __dmul_rn(p.scale, a.ax);
+    p.o1[il] = __dmul_rn(p.scale, __dmul_rn(0.5, __dadd_rn(a.ay, a.bx)));
+    p.o2[il] = __dmul_rn(p.scale, a.by);
+  }
+};
+
+// PSEPlaneDoubleDotProductAtParticles: (ux ux + 2 uy vx + vy vy) / eps**2
+struct PsePlaneDdotF64 : PlaneD4F64 {
+  __device__ static void store(const PseExtF64Params& p, int64_t i, int64_t il, const Acc& a) {
+    const double s = __dadd_rn(__dadd_rn(__dmul_rn(a.ax, a.ax), __dmul_rn(__dmul_rn(2.0, a.ay), a.bx)),
+                               __dmul_rn(a.by, a.by));
+    p.o0[il] = __ddiv_rn(s, p.eps2);
+  }
+};
+
+// PSESphereDoubleDotProductAtParticles, src/PSEDirectSum.f90:367-418 (RecVec64: u, v, w of
+// j).  The third row pairs w_j with v_i, as the reference does (:399-404).
+struct PseSphereDdotF64 {
+  struct Tgt {
+    double x, y, z, u, v;
+  };
+  struct Acc {
+    double ux, uy, uz, vx, vy, vz, wx, wy, wz;
+  };
+  __device__ static Tgt load(const PseExtF64Params& p, int64_t i) {
+    return Tgt{p.x[i], p.y[i], p.z[i], p.s1[i], p.s2[i]};
+  }
+  __device__ static __forceinline__ void interact(const PseExtF64Params& p, const Tgt& t, const RecVec64& r,
+                                                  Acc& a) {
+    const double kin = __ddiv_rn(__dmul_rn(sphere_angle_f64(t.x, t.y, t.z, r.x, r.y, r.z), p.radius), p.eps);
+    const double kout = __ddiv_rn(k1_f64(kin), p.eps2);
+    const double dx = __dsub_rn(t.x, r.x), dy = __dsub_rn(t.y, r.y), dz = __dsub_rn(t.z, r.z);
+    const double su = __dadd_rn(r.vx, t.u), sv = __dadd_rn(r.vy, t.v), sw = __dadd_rn(r.vz, t.v);
+#define LPM_DD(acc, s, d) acc = __dadd_rn(acc, __dmul_rn(__dmul_rn(__ddiv_rn(__dmul_rn(s, d), p.eps), kout), r.area))
+    LPM_DD(a.ux, su, dx);
+    LPM_DD(a.uy, su, dy);
+    LPM_DD(a.uz, su, dz);
+    LPM_DD(a.vx, sv, dx);
+    LPM_DD(a.vy, sv, dy);
+    LPM_DD(a.vz, sv, dz);
+    LPM_DD(a.wx, sw, dx);
+    LPM_DD(a.wy, sw, dy);
+    LPM_DD(a.wz, sw, dz);
+#undef LPM_DD
+  }
+  __device__ static void store(const PseExtF64Params& p, int64_t i, int64_t il, const Acc& a) {
+    const double d = __dadd_rn(__dadd_rn(__dmul_rn(a.ux, a.ux), __dmul_rn(a.vy, a.vy)), __dmul_rn(a.wz, a.wz));
+    const double c = __dadd_rn(__dadd_rn(__dmul_rn(a.uy, a.vx), __dmul_rn(a.uz, a.wx)), __dmul_rn(a.vz, a.wy));
+    p.o0[il] = __ddiv_rn(__dadd_rn(d, __dmul_rn(2.0, c)), p.eps2);
+  }
+  static constexpr bool kSkipSelf = false;
+};
+
+// PSEPlaneInterpolateScalar / PSESphereInterpolateScalar, src/PSEDirectSum.f90:128-168, at
+// query points (the targets; Rec64: q = f_j, r = A_j): s += ((f_j A_j) Kdelta8) / eps**2
+template <bool SPHERE>
+struct PseInterpF64 {
+  struct Tgt {
+    double x, y, z;
+  };
+  struct Acc {
+    double s;
+  };
+  __device__ static Tgt load(const PseExtF64Params& p, int64_t i) {
+    return Tgt{p.x[i], p.y[i], p.z ? p.z[i] : 0.0};
+  }
+  __device__ static __forceinline__ void interact(const PseExtF64Params& p, const Tgt& t, const Rec64& r, Acc& a) {
+    double d;
+    if (SPHERE) {
+      d = __dmul_rn(sphere_angle_f64(r.x, r.y, r.z, t.x, t.y, t.z), p.radius);
+    } else {
+      const double d1 = __dsub_rn(r.x, t.x), d2 = __dsub_rn(r.y, t.y), d3 = __dsub_rn(r.z, t.z);
+      d = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(d1, d1), __dmul_rn(d2, d2)), __dmul_rn(d3, d3)));
+    }
+    a.s = __dadd_rn(a.s, __ddiv_rn(__dmul_rn(__dmul_rn(r.q, r.r), kdelta8_f64(__ddiv_rn(d, p.eps))), p.eps2));
+  }
+  __device__ static void store(const PseExtF64Params& p, int64_t i, int64_t il, const Acc& a) { p.o0[il] = a.s; }
+  static constexpr bool kSkipSelf = false;
+};
+
+// SWEPlaneRHSIntegrals, src/SWEPlaneSolver.f90:457-534 (RecVec64: vx = vort_j, vy = div_j,
+// vz = sh_j, the surface height h + topoFn).  The Laplacian term includes j = i (a zero
+// term); the rest skips it, as the reference's `cycle` does.
+struct SwePlaneF64 {
+  struct Tgt {
+    double x, y, sh;
+    int64_t i;
+  };
+  struct Acc {
+    double u, v, l, ux, uy, vx, vy;
+  };
+  __device__ static Tgt load(const PseExtF64Params& p, int64_t i) { return Tgt{p.x[i], p.y[i], p.s3[i], i}; }
+  __device__ static __forceinline__ void interact(const PseExtF64Params& p, const Tgt& t, const RecVec64& r,
+                                                  Acc& a) {
+    const double dx = __dsub_rn(t.x, r.x), dy = __dsub_rn(t.y, r.y);
+    const double sq = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+    const double lk = __ddiv_rn(k8_f64(__ddiv_rn(__dsqrt_rn(sq), p.eps)), p.eps2);
+    a.l = __dadd_rn(a.l, __dmul_rn(__dmul_rn(lk, __dsub_rn(r.vz, t.sh)), r.area));
+    if (r.idx == t.i) return;
+    const double denom = __dmul_rn(p.k0, sq);  // (2 pi) r^2
+    const double denom2 = __dmul_rn(__dmul_rn(3.1415926535897932384626433832795027975, sq), sq);
+    const double rot = __ddiv_rn(__dmul_rn(r.vx, r.area), denom);
+    const double pot = __ddiv_rn(__dmul_rn(r.vy, r.area), denom);
+    a.u = __dadd_rn(__dsub_rn(a.u, __dmul_rn(dy, rot)), __dmul_rn(dx, pot));
+    a.v = __dadd_rn(__dadd_rn(a.v, __dmul_rn(dx, rot)), __dmul_rn(dy, pot));
+    const double cu = __dsub_rn(__dmul_rn(dx, r.vy), __dmul_rn(dy, r.vx));
+    const double cv = __dadd_rn(__dmul_rn(dy, r.vy), __dmul_rn(dx, r.vx));
+    a.ux = __dsub_rn(__dadd_rn(a.ux, pot), __ddiv_rn(__dmul_rn(__dmul_rn(dx, cu), r.area), denom2));
+    a.uy = __dsub_rn(__dsub_rn(a.uy, rot), __ddiv_rn(__dmul_rn(__dmul_rn(dy, cu), r.area), denom2));
+    a.vx = __dsub_rn(__dadd_rn(a.vx, rot), __ddiv_rn(__dmul_rn(__dmul_rn(dx, cv), r.area), denom2));
+    a.vy = __dsub_rn(__dadd_rn(a.vy, pot), __ddiv_rn(__dmul_rn(__dmul_rn(dy, cv), r.area), denom2));
+  }
+  __device__ static void store(const PseExtF64Params& p, int64_t i, int64_t il, const Acc& a) {
+    p.o0[il] = a.u;
+    p.o1[il] = a.v;
+    p.o2[il] = __dadd_rn(__dadd_rn(__dmul_rn(a.ux, a.ux), __dmul_rn(__dmul_rn(2.0, a.uy), a.vx)), __dmul_rn(a.vy, a.vy));
+    p.o3[il] = __ddiv_rn(a.l, p.eps2);
+  }
+  static constexpr bool kSkipSelf = false;
+};
+
+// SWESphereRHSIntegrals, src/SphereSWESolver.f90:299-372 (RecVec64: vx = zeta_j, vy = div_j,
+// vz = sh_j).  k0 = 4 pi a^2, radius = a, radius2 = the SphereRadius of SphereDistance.  As in
+// the reference, lapSurf keeps the 1/eps**2 inside the kernel only and doubleDot is 0.
+struct SweSphereF64 {
+  struct Tgt {
+    double x, y, z, sh;
+    int64_t i;
+  };
+  struct Acc {
+    double u, v, w, l;
+  };
+  __device__ static Tgt load(const PseExtF64Params& p, int64_t i) {
+    return Tgt{p.x[i], p.y[i], p.z[i], p.s3[i], i};
+  }
+  __device__ static __forceinline__ void interact(const PseExtF64Params& p, const Tgt& t, const RecVec64& r,
+                                                  Acc& a) {
+    const double kin = __ddiv_rn(__dmul_rn(sphere_angle_f64(t.x, t.y, t.z, r.x, r.y, r.z), p.radius2), p.eps);
+    const double lk = __ddiv_rn(k8_f64(kin), p.eps2);
+    a.l = __dadd_rn(a.l, __dmul_rn(__dmul_rn(lk, __dsub_rn(r.vz, t.sh)), r.area));
+    if (r.idx == t.i) return;
+    const double dp = __dadd_rn(__dadd_rn(__dmul_rn(t.x, r.x), __dmul_rn(t.y, r.y)), __dmul_rn(t.z, r.z));
+    const double denom = __dmul_rn(p.k0, __dsub_rn(__dmul_rn(p.radius, p.radius), dp));
+    const double rot = __ddiv_rn(__dmul_rn(r.vx, r.area), denom);
+    const double pot = __ddiv_rn(__dmul_rn(__dmul_rn(p.radius, r.vy), r.area), denom);
+    a.u = __dsub_rn(__dsub_rn(a.u, __dmul_rn(__dsub_rn(__dmul_rn(t.y, r.z), __dmul_rn(t.z, r.y)), rot)),
+                    __dmul_rn(r.x, pot));
+    a.v = __dsub_rn(__dsub_rn(a.v, __dmul_rn(__dsub_rn(__dmul_rn(t.z, r.x), __dmul_rn(t.x, r.z)), rot)),
+                    __dmul_rn(r.y, pot));
+    a.w = __dsub_rn(__dsub_rn(a.w, __dmul_rn(__dsub_rn(__dmul_rn(t.x, r.y), __dmul_rn(t.y, r.x)), rot)),
+                    __dmul_rn(r.z, pot));
+  }
+  __device__ static void store(const PseExtF64Params& p, int64_t i, int64_t il, const Acc& a) {
+    p.o0[il] = a.u;
+    p.o1[il] = a.v;
+    p.o2[il] = a.w;
+    p.o3[il] = a.l;
+  }
+  static constexpr bool kSkipSelf = false;
+};
+
 // ============================================================ stream functions (FP32C)
 // Both stream functions (stream_rel.cuh) sum S_j ln(q_ij) with ln from ln_q2, accurate to
 // about 1 ulp.  A pair with d = 0 (the self pair) is skipped by giving it q = 1, as the

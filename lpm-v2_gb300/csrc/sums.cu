@@ -100,7 +100,7 @@ __global__ void prep_vec64_kernel(const double* x, const double* y, const double
   const int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (k >= ns) return;
   const int64_t j = idx[k];
-  out[k] = RecVec64{x[j], y[j], z[j], vx[j], vy[j], vz[j], area[j], static_cast<long long>(j)};
+  out[k] = RecVec64{x[j], y[j], z ? z[j] : 0.0, vx[j], vy[j], vz ? vz[j] : 0.0, area[j], static_cast<long long>(j)};
 }
 
 __global__ void prep_plane64_kernel(const double* x, const double* y, const double* omega,
@@ -256,7 +256,9 @@ int tile_of(int kind, int mode) {
 size_t rec_bytes(int kind, int mode) {
   if (mode == LPM_MODE_FP64) {
     if (kind == kSumPlane) return sizeof(RecPlane64);
-    if (kind == kSumPseDiv) return sizeof(RecVec64);
+    if (kind == kSumPseDiv || kind == kSumPsePlaneSecond || kind == kSumPsePlaneDdot || kind == kSumPseSphereDdot ||
+        kind == kSumSwePlane || kind == kSumSweSphere)
+      return sizeof(RecVec64);
     if (kind == kSumSphereStream || kind == kSumPlaneStream) return sizeof(RecStream64);
     return sizeof(Rec64);
   }
@@ -575,12 +577,73 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
         }
         break;
       }
+      case kSumPsePlaneGrad:
+      case kSumPseInterpPlane:
+      case kSumPseInterpSphere: {
+        prep_rec64_kernel<<<prep_grid_ns, pb, 0, job.stream>>>(job.x, job.y, job.z, job.s1, job.area,
+                                                               job.src_idx, job.ns, 1,
+                                                               static_cast<Rec64*>(job.src_buf));
+        const double eps2 = job.eps * job.eps;
+        PseExtF64Params p{job.x, job.y, job.z, job.s1, job.s2, job.s3, job.eps, eps2, job.eps * eps2,
+                          job.radius, job.radius2, 0.0, 1.0 / job.eps, job.out0, job.out1, job.out2, job.out3};
+        const Rec64* src = static_cast<const Rec64*>(job.src_buf);
+        if (job.kind == kSumPsePlaneGrad) {
+          seq_fp64_kernel<PsePlaneGradF64, Rec64><<<g, k64Threads, 0, job.stream>>>(p, src, job.ns, job.ib, job.nt,
+                                                                                    job.status);
+        } else if (job.kind == kSumPseInterpPlane) {
+          seq_fp64_kernel<PseInterpF64<false>, Rec64><<<g, k64Threads, 0, job.stream>>>(p, src, job.ns, job.ib,
+                                                                                        job.nt, job.status);
+        } else {
+          seq_fp64_kernel<PseInterpF64<true>, Rec64><<<g, k64Threads, 0, job.stream>>>(p, src, job.ns, job.ib,
+                                                                                       job.nt, job.status);
+        }
+        break;
+      }
+      case kSumPsePlaneSecond:
+      case kSumPsePlaneDdot:
+      case kSumPseSphereDdot:
+      case kSumSwePlane:
+      case kSumSweSphere: {
+        prep_vec64_kernel<<<prep_grid_ns, pb, 0, job.stream>>>(job.x, job.y, job.z, job.s1, job.s2, job.s3,
+                                                               job.area, job.src_idx, job.ns,
+                                                               static_cast<RecVec64*>(job.src_buf));
+        const double eps2 = job.eps * job.eps;
+        PseExtF64Params p{job.x, job.y, job.z, job.s1, job.s2, job.s3, job.eps, eps2, job.eps * eps2,
+                          job.radius, job.radius2, 0.0, 1.0 / job.eps, job.out0, job.out1, job.out2, job.out3};
+        const RecVec64* src = static_cast<const RecVec64*>(job.src_buf);
+        switch (job.kind) {
+          case kSumPsePlaneSecond:
+            seq_fp64_kernel<PsePlaneSecondF64, RecVec64><<<g, k64Threads, 0, job.stream>>>(p, src, job.ns, job.ib,
+                                                                                          job.nt, job.status);
+            break;
+          case kSumPsePlaneDdot:
+            seq_fp64_kernel<PsePlaneDdotF64, RecVec64><<<g, k64Threads, 0, job.stream>>>(p, src, job.ns, job.ib,
+                                                                                        job.nt, job.status);
+            break;
+          case kSumPseSphereDdot:
+            seq_fp64_kernel<PseSphereDdotF64, RecVec64><<<g, k64Threads, 0, job.stream>>>(p, src, job.ns, job.ib,
+                                                                                         job.nt, job.status);
+            break;
+          case kSumSwePlane:
+            p.k0 = 2.0 * kPi;  // 2.0_kreal * PI
+            seq_fp64_kernel<SwePlaneF64, RecVec64><<<g, k64Threads, 0, job.stream>>>(p, src, job.ns, job.ib,
+                                                                                    job.nt, job.status);
+            break;
+          default:
+            p.k0 = ((4.0 * kPi) * job.radius) * job.radius;  // 4.0_kreal * PI * radius * radius
+            seq_fp64_kernel<SweSphereF64, RecVec64><<<g, k64Threads, 0, job.stream>>>(p, src, job.ns, job.ib,
+                                                                                     job.nt, job.status);
+            break;
+        }
+        break;
+      }
       default:
         return set_error(LPM_ERR_ARG, "unknown sum kind %d", job.kind);
     }
     LPM_CUDA_TRY(cudaGetLastError());
     return LPM_OK;
   }
+  if (sum_is_fp64_only(job.kind)) return set_error(LPM_ERR_ARG, "this operator has only the FP64 mode");
 
   // ---------------- FP32C
   switch (job.kind) {
@@ -853,14 +916,16 @@ struct HostArgs {
   int64_t i_begin, i_end;  // 1-based inclusive
   double *out0, *out1, *out2;
   int mode;
-  const double* s3 = nullptr;  // vz (PSE divergence)
+  const double* s3 = nullptr;  // vz (PSE divergence), w (sphere double dot), surface height (SWE)
+  double* out3 = nullptr;      // lapSurf (SWE)
+  double radius2 = 1.0;        // SphereRadius of SphereDistance (sphere SWE)
 };
 
 int check_common(const HostArgs& a, int nout) {
   if (a.n <= 0) return set_error(LPM_ERR_ARG, "n must be positive (got %lld)", (long long)a.n);
   if (!a.x || !a.y || !a.s1 || !a.area || !a.active)
     return set_error(LPM_ERR_ARG, "null input array");
-  if (!a.out0 || (nout > 1 && !a.out1) || (nout > 2 && !a.out2))
+  if (!a.out0 || (nout > 1 && !a.out1) || (nout > 2 && !a.out2) || (nout > 3 && !a.out3))
     return set_error(LPM_ERR_ARG, "null output array");
   if (a.i_begin < 1 || a.i_end > a.n || a.i_begin > a.i_end)
     return set_error(LPM_ERR_ARG, "target range [%lld, %lld] is not inside [1, %lld]", (long long)a.i_begin,
@@ -870,6 +935,8 @@ int check_common(const HostArgs& a, int nout) {
     return set_error(LPM_ERR_ARG, "unknown precision mode %d", prec);
   if ((a.mode & ~(LPM_MODE_MASK | LPM_FLAG_CHECK_FINITE)) != 0)
     return set_error(LPM_ERR_ARG, "unknown mode flags 0x%x", a.mode);
+  if (prec == LPM_MODE_FP32C && sum_is_fp64_only(a.kind))
+    return set_error(LPM_ERR_ARG, "this operator has only the FP64 mode (LPM_MODE_FP64)");
   return LPM_OK;
 }
 
@@ -941,11 +1008,13 @@ int run_host(const HostArgs& a, int nout) {
     job.radius = a.radius;
     job.delta = a.delta;
     job.eps = a.eps;
+    job.radius2 = a.radius2;
     job.ib = ib;
     job.nt = nt;
     job.out0 = dout;
     job.out1 = nout > 1 ? dout + nt : nullptr;
     job.out2 = nout > 2 ? dout + 2 * nt : nullptr;
+    job.out3 = nout > 3 ? dout + 3 * nt : nullptr;
     LPM_TRY(workspace(ctx, kWsSources, plan.src_bytes, &job.src_buf));
     if (sum_uses_sorted_sources(a.kind, prec)) {
       void* ps = nullptr;
@@ -968,7 +1037,7 @@ int run_host(const HostArgs& a, int nout) {
     plan = plan_sum(a.kind, prec, ns, nt, ctx->sm_count, shape);
     LPM_TRY(launch_sum(job, plan));
   }
-  double* outs[3] = {a.out0, a.out1, a.out2};
+  double* outs[4] = {a.out0, a.out1, a.out2, a.out3};
   for (int c = 0; c < nout; ++c) {
     LPM_CUDA_TRY(cudaMemcpyAsync(outs[c] + ib, dout + c * nt, static_cast<size_t>(nt) * sizeof(double),
                                  cudaMemcpyDeviceToHost, s));
@@ -1091,4 +1160,116 @@ extern "C" int lpm_pse_sphere_divergence(int64_t n, const double* x, const doubl
   if (!z || !vy || !vz) return lpm::set_error(LPM_ERR_ARG, "null z or vector component array");
   if (!(eps > 0.0) || !(radius > 0.0)) return lpm::set_error(LPM_ERR_ARG, "eps and radius must be positive");
   return lpm::run_host(a, 1);
+}
+
+extern "C" int lpm_pse_plane_gradient(int64_t n, const double* x, const double* y, const double* f, const double* area,
+                                      const int32_t* active, double eps, int64_t i_begin, int64_t i_end, double* gx,
+                                      double* gy, int mode) {
+  HostArgs a{lpm::kSumPsePlaneGrad, n, x, y, nullptr, f, nullptr, area, active, 1.0, 0.0, eps, i_begin, i_end, gx, gy,
+             nullptr, mode};
+  LPM_TRY(lpm::check_common(a, 2));
+  if (!(eps > 0.0)) return lpm::set_error(LPM_ERR_ARG, "eps must be positive");
+  return lpm::run_host(a, 2);
+}
+
+extern "C" int lpm_pse_plane_second_partials(int64_t n, const double* x, const double* y, const double* gx,
+                                             const double* gy, const double* area, const int32_t* active, double eps,
+                                             int64_t i_begin, int64_t i_end, double* dxx, double* dxy, double* dyy,
+                                             int mode) {
+  HostArgs a{lpm::kSumPsePlaneSecond, n, x, y, nullptr, gx, gy, area, active, 1.0, 0.0, eps, i_begin, i_end, dxx,
+             dxy, dyy, mode};
+  LPM_TRY(lpm::check_common(a, 3));
+  if (!gy) return lpm::set_error(LPM_ERR_ARG, "null gradient component array");
+  if (!(eps > 0.0)) return lpm::set_error(LPM_ERR_ARG, "eps must be positive");
+  return lpm::run_host(a, 3);
+}
+
+extern "C" int lpm_pse_plane_double_dot(int64_t n, const double* x, const double* y, const double* u, const double* v,
+                                        const double* area, const int32_t* active, double eps, int64_t i_begin,
+                                        int64_t i_end, double* ddot, int mode) {
+  HostArgs a{lpm::kSumPsePlaneDdot, n, x, y, nullptr, u, v, area, active, 1.0, 0.0, eps, i_begin, i_end, ddot, nullptr,
+             nullptr, mode};
+  LPM_TRY(lpm::check_common(a, 1));
+  if (!v) return lpm::set_error(LPM_ERR_ARG, "null velocity component array");
+  if (!(eps > 0.0)) return lpm::set_error(LPM_ERR_ARG, "eps must be positive");
+  return lpm::run_host(a, 1);
+}
+
+extern "C" int lpm_pse_sphere_double_dot(int64_t n, const double* x, const double* y, const double* z, const double* u,
+                                         const double* v, const double* w, const double* area, const int32_t* active,
+                                         double eps, double radius, int64_t i_begin, int64_t i_end, double* ddot,
+                                         int mode) {
+  HostArgs a{lpm::kSumPseSphereDdot, n, x, y, z, u, v, area, active, radius, 0.0, eps, i_begin, i_end, ddot, nullptr,
+             nullptr, mode, w};
+  LPM_TRY(lpm::check_common(a, 1));
+  if (!z || !v || !w) return lpm::set_error(LPM_ERR_ARG, "null z or velocity component array");
+  if (!(eps > 0.0) || !(radius > 0.0)) return lpm::set_error(LPM_ERR_ARG, "eps and radius must be positive");
+  return lpm::run_host(a, 1);
+}
+
+extern "C" int lpm_pse_interpolate_scalar(int64_t n, const double* x, const double* y, const double* z, const double* f,
+                                          const double* area, const int32_t* active, double eps, double radius,
+                                          int geometry, int64_t m, const double* qx, const double* qy,
+                                          const double* qz, double* out, int mode) {
+  if (m <= 0 || !qx || !qy || !out) return lpm::set_error(LPM_ERR_ARG, "need m > 0 query points and an output array");
+  if (geometry != LPM_GEOMETRY_PLANE && geometry != LPM_GEOMETRY_SPHERE)
+    return lpm::set_error(LPM_ERR_ARG, "unknown geometry %d", geometry);
+  if (geometry == LPM_GEOMETRY_SPHERE && (!z || !qz))
+    return lpm::set_error(LPM_ERR_ARG, "the sphere needs z and qz");
+  if (!(eps > 0.0) || !(radius > 0.0)) return lpm::set_error(LPM_ERR_ARG, "eps and radius must be positive");
+  if (n <= 0 || !x || !y || !f || !area || !active) return lpm::set_error(LPM_ERR_ARG, "null input array");
+  // The query points become passive particles n .. n+m-1 (area 0, inactive), the targets.
+  const int64_t nn = n + m;
+  std::vector<double> cx(nn), cy(nn), cz(nn), cf(nn, 0.0), ca(nn, 0.0), co(nn, 0.0);
+  std::vector<int32_t> act(nn, 0);
+  for (int64_t i = 0; i < n; ++i) {
+    cx[i] = x[i];
+    cy[i] = y[i];
+    cz[i] = z ? z[i] : 0.0;
+    cf[i] = f[i];
+    ca[i] = area[i];
+    act[i] = active[i] ? 1 : 0;
+  }
+  for (int64_t k = 0; k < m; ++k) {
+    cx[n + k] = qx[k];
+    cy[n + k] = qy[k];
+    cz[n + k] = qz ? qz[k] : 0.0;
+  }
+  const int kind = geometry == LPM_GEOMETRY_SPHERE ? lpm::kSumPseInterpSphere : lpm::kSumPseInterpPlane;
+  HostArgs a{kind, nn, cx.data(), cy.data(), cz.data(), cf.data(), nullptr, ca.data(), act.data(), radius, 0.0, eps,
+             n + 1, nn, co.data(), nullptr, nullptr, mode};
+  LPM_TRY(lpm::check_common(a, 1));
+  LPM_TRY(lpm::run_host(a, 1));
+  for (int64_t k = 0; k < m; ++k) out[k] = co[n + k];
+  return LPM_OK;
+}
+
+extern "C" int lpm_swe_plane_rhs_integrals(int64_t n, const double* x, const double* y, const double* vort,
+                                           const double* div, const double* surf_height, const double* area,
+                                           const int32_t* active, double eps, int64_t i_begin, int64_t i_end,
+                                           double* u, double* v, double* double_dot, double* lap_surf, int mode) {
+  HostArgs a{lpm::kSumSwePlane, n, x, y, nullptr, vort, div, area, active, 1.0, 0.0, eps, i_begin, i_end, u, v,
+             double_dot, mode, surf_height, lap_surf};
+  LPM_TRY(lpm::check_common(a, 4));
+  if (!div || !surf_height) return lpm::set_error(LPM_ERR_ARG, "null divergence or surface height array");
+  if (!(eps > 0.0)) return lpm::set_error(LPM_ERR_ARG, "eps must be positive");
+  return lpm::run_host(a, 4);
+}
+
+extern "C" int lpm_swe_sphere_rhs_integrals(int64_t n, const double* x, const double* y, const double* z,
+                                            const double* relvort, const double* div, const double* surf_height,
+                                            const double* area, const int32_t* active, double radius,
+                                            double sphere_radius, double eps, int64_t i_begin, int64_t i_end,
+                                            double* u, double* v, double* w, double* double_dot, double* lap_surf,
+                                            int mode) {
+  HostArgs a{lpm::kSumSweSphere, n, x, y, z, relvort, div, area, active, radius, 0.0, eps, i_begin, i_end, u, v, w,
+             mode, surf_height, lap_surf, sphere_radius};
+  LPM_TRY(lpm::check_common(a, 4));
+  if (!z || !div || !surf_height || !double_dot)
+    return lpm::set_error(LPM_ERR_ARG, "null z, divergence, surface height or doubleDot array");
+  if (!(eps > 0.0) || !(radius > 0.0) || !(sphere_radius > 0.0))
+    return lpm::set_error(LPM_ERR_ARG, "eps and the radii must be positive");
+  LPM_TRY(lpm::run_host(a, 4));
+  for (int64_t i = i_begin - 1; i < i_end; ++i) double_dot[i] = 0.0;  // never set by the reference
+  return LPM_OK;
 }

@@ -28,8 +28,19 @@ enum SumKind : int {
   kSumSphereStream,   // sphere stream functions
   kSumPlaneStream,    // planar stream function
   kSumPseGrad,        // PSE gradient on the sphere (K1 of the great-circle distance)
-  kSumPseDiv          // PSE divergence on the sphere
+  kSumPseDiv,         // PSE divergence on the sphere
+  kSumPsePlaneGrad,     // PSE gradient in the plane (FP64)
+  kSumPsePlaneSecond,   // PSE second partials in the plane, from a gradient field (FP64)
+  kSumPsePlaneDdot,     // PSE double dot product in the plane (FP64)
+  kSumPseSphereDdot,    // PSE double dot product on the sphere (FP64)
+  kSumPseInterpPlane,   // PSE interpolation at query points, chord distance (FP64)
+  kSumPseInterpSphere,  // PSE interpolation at query points, great-circle distance (FP64)
+  kSumSwePlane,         // planar SWE right-hand-side integrals (FP64)
+  kSumSweSphere         // sphere SWE right-hand-side integrals (FP64)
 };
+
+// Kinds that have only the FP64 form.
+inline bool sum_is_fp64_only(int kind) { return kind >= kSumPsePlaneGrad && kind <= kSumSweSphere; }
 
 // Inputs of one direct sum over particles [0, n): sources are the ns particles listed (in
 // ascending order) by src_idx; targets are particles ib .. ib+nt-1.
@@ -40,17 +51,19 @@ struct SumJob {
   const double *x = nullptr, *y = nullptr, *z = nullptr;
   const double* s1 = nullptr;  // zeta (BVE), omega (plane), f (PSE), relvort (stream)
   const double* s2 = nullptr;  // absvort (sphere stream), vy (PSE divergence), unused otherwise
-  const double* s3 = nullptr;  // vz (PSE divergence), unused otherwise
+  const double* s3 = nullptr;  // vz (PSE divergence), w (sphere double dot), surface height (SWE)
   const double* area = nullptr;
   const int32_t* src_idx = nullptr;
   int64_t ns = 0;
   double radius = 1.0;  // sphere radius (BVE, PSE, stream)
   double delta = 0.0;   // planar regularisation
   double eps = 1.0;     // PSE radius
+  double radius2 = 1.0;  // SphereRadius of SphereDistance in the sphere SWE integrals
   int64_t ib = 0, nt = 0;
   double* out0 = nullptr;  // u / lap / psi_rel   (length nt)
   double* out1 = nullptr;  // v / psi_abs
   double* out2 = nullptr;  // w
+  double* out3 = nullptr;  // lapSurf (SWE)
   // FP32C sphere BVE and planar sums: curve-sort src_idx into `sorted` with this scratch
   // before the sweep (sort_scratch == nullptr: src_idx is already spatially ordered and is
   // used as is)

@@ -22,6 +22,9 @@ public :: lpm_bve_velocity, lpm_bve_set_velocity_from_vorticity, lpm_plane_veloc
 public :: lpm_pse_sphere_laplacian, lpm_pse_plane_laplacian, lpm_bve_stream_functions
 public :: lpm_plane_stream_function, lpm_last_error_string
 public :: lpm_pse_sphere_gradient, lpm_pse_sphere_divergence
+public :: lpm_pse_plane_gradient, lpm_pse_plane_second_partials, lpm_pse_plane_double_dot
+public :: lpm_pse_sphere_double_dot, lpm_pse_interpolate_scalar
+public :: lpm_swe_plane_rhs_integrals, lpm_swe_sphere_rhs_integrals
 public :: lpm_bve_solver_create, lpm_bve_timestep, lpm_bve_get_state, lpm_bve_set_state
 public :: lpm_bve_diagnostics, lpm_bve_solver_stream_functions, lpm_bve_solver_destroy
 public :: lpm_plane_solver_create, lpm_plane_timestep, lpm_plane_get_state, lpm_plane_diagnostics
@@ -32,6 +35,8 @@ integer(c_int), parameter :: LPM_MODE_FP32C = 1
 integer(c_int), parameter :: LPM_PSE_K8_GEODESIC = 0
 integer(c_int), parameter :: LPM_PSE_GAUSS_CHORD = 1
 integer(c_int), parameter :: LPM_PSE_K8_CHORD = 2
+integer(c_int), parameter :: LPM_GEOMETRY_PLANE = 0
+integer(c_int), parameter :: LPM_GEOMETRY_SPHERE = 1
 
 interface
 	integer(c_int) function lpm_bve_velocity(n, x, y, z, zeta, area, active, radius, i_begin, i_end, &
@@ -140,6 +145,93 @@ interface
 		real(c_double), value :: eps, radius
 		integer(c_int64_t), value :: i_begin, i_end
 		real(c_double), intent(inout) :: div(*)
+		integer(c_int), value :: mode
+	end function
+
+	integer(c_int) function lpm_pse_plane_gradient(n, x, y, f, area, active, eps, i_begin, i_end, gx, gy, &
+			mode) bind(C, name="lpm_pse_plane_gradient")
+		import :: c_int, c_int32_t, c_int64_t, c_double
+		integer(c_int64_t), value :: n
+		real(c_double), intent(in) :: x(*), y(*), f(*), area(*)
+		integer(c_int32_t), intent(in) :: active(*)
+		real(c_double), value :: eps
+		integer(c_int64_t), value :: i_begin, i_end
+		real(c_double), intent(inout) :: gx(*), gy(*)
+		integer(c_int), value :: mode
+	end function
+
+	integer(c_int) function lpm_pse_plane_second_partials(n, x, y, gx, gy, area, active, eps, i_begin, i_end, &
+			dxx, dxy, dyy, mode) bind(C, name="lpm_pse_plane_second_partials")
+		import :: c_int, c_int32_t, c_int64_t, c_double
+		integer(c_int64_t), value :: n
+		real(c_double), intent(in) :: x(*), y(*), gx(*), gy(*), area(*)
+		integer(c_int32_t), intent(in) :: active(*)
+		real(c_double), value :: eps
+		integer(c_int64_t), value :: i_begin, i_end
+		real(c_double), intent(inout) :: dxx(*), dxy(*), dyy(*)
+		integer(c_int), value :: mode
+	end function
+
+	integer(c_int) function lpm_pse_plane_double_dot(n, x, y, u, v, area, active, eps, i_begin, i_end, ddot, &
+			mode) bind(C, name="lpm_pse_plane_double_dot")
+		import :: c_int, c_int32_t, c_int64_t, c_double
+		integer(c_int64_t), value :: n
+		real(c_double), intent(in) :: x(*), y(*), u(*), v(*), area(*)
+		integer(c_int32_t), intent(in) :: active(*)
+		real(c_double), value :: eps
+		integer(c_int64_t), value :: i_begin, i_end
+		real(c_double), intent(inout) :: ddot(*)
+		integer(c_int), value :: mode
+	end function
+
+	integer(c_int) function lpm_pse_sphere_double_dot(n, x, y, z, u, v, w, area, active, eps, radius, &
+			i_begin, i_end, ddot, mode) bind(C, name="lpm_pse_sphere_double_dot")
+		import :: c_int, c_int32_t, c_int64_t, c_double
+		integer(c_int64_t), value :: n
+		real(c_double), intent(in) :: x(*), y(*), z(*), u(*), v(*), w(*), area(*)
+		integer(c_int32_t), intent(in) :: active(*)
+		real(c_double), value :: eps, radius
+		integer(c_int64_t), value :: i_begin, i_end
+		real(c_double), intent(inout) :: ddot(*)
+		integer(c_int), value :: mode
+	end function
+
+	integer(c_int) function lpm_pse_interpolate_scalar(n, x, y, z, f, area, active, eps, radius, geometry, &
+			m, qx, qy, qz, out, mode) bind(C, name="lpm_pse_interpolate_scalar")
+		import :: c_int, c_int32_t, c_int64_t, c_double
+		integer(c_int64_t), value :: n
+		real(c_double), intent(in) :: x(*), y(*), z(*), f(*), area(*)
+		integer(c_int32_t), intent(in) :: active(*)
+		real(c_double), value :: eps, radius
+		integer(c_int), value :: geometry
+		integer(c_int64_t), value :: m
+		real(c_double), intent(in) :: qx(*), qy(*), qz(*)
+		real(c_double), intent(inout) :: out(*)
+		integer(c_int), value :: mode
+	end function
+
+	integer(c_int) function lpm_swe_plane_rhs_integrals(n, x, y, vort, div, surf_height, area, active, eps, &
+			i_begin, i_end, u, v, double_dot, lap_surf, mode) bind(C, name="lpm_swe_plane_rhs_integrals")
+		import :: c_int, c_int32_t, c_int64_t, c_double
+		integer(c_int64_t), value :: n
+		real(c_double), intent(in) :: x(*), y(*), vort(*), div(*), surf_height(*), area(*)
+		integer(c_int32_t), intent(in) :: active(*)
+		real(c_double), value :: eps
+		integer(c_int64_t), value :: i_begin, i_end
+		real(c_double), intent(inout) :: u(*), v(*), double_dot(*), lap_surf(*)
+		integer(c_int), value :: mode
+	end function
+
+	integer(c_int) function lpm_swe_sphere_rhs_integrals(n, x, y, z, relvort, div, surf_height, area, active, &
+			radius, sphere_radius, eps, i_begin, i_end, u, v, w, double_dot, lap_surf, mode) &
+			bind(C, name="lpm_swe_sphere_rhs_integrals")
+		import :: c_int, c_int32_t, c_int64_t, c_double
+		integer(c_int64_t), value :: n
+		real(c_double), intent(in) :: x(*), y(*), z(*), relvort(*), div(*), surf_height(*), area(*)
+		integer(c_int32_t), intent(in) :: active(*)
+		real(c_double), value :: radius, sphere_radius, eps
+		integer(c_int64_t), value :: i_begin, i_end
+		real(c_double), intent(inout) :: u(*), v(*), w(*), double_dot(*), lap_surf(*)
 		integer(c_int), value :: mode
 	end function
 

@@ -69,6 +69,14 @@ _SIGNATURES = {
     "lpm_pse_sphere_gradient": [_i64, _D, _D, _D, _D, _D, _I, _dbl, _dbl, _i64, _i64, _D, _D, _D, _int],
     "lpm_pse_sphere_divergence": [_i64, _D, _D, _D, _D, _D, _D, _D, _I, _dbl, _dbl, _i64, _i64, _D, _int],
     "lpm_plane_stream_function": [_i64, _D, _D, _D, _D, _I, _i64, _i64, _D, _int],
+    "lpm_pse_plane_gradient": [_i64, _D, _D, _D, _D, _I, _dbl, _i64, _i64, _D, _D, _int],
+    "lpm_pse_plane_second_partials": [_i64, _D, _D, _D, _D, _D, _I, _dbl, _i64, _i64, _D, _D, _D, _int],
+    "lpm_pse_plane_double_dot": [_i64, _D, _D, _D, _D, _D, _I, _dbl, _i64, _i64, _D, _int],
+    "lpm_pse_sphere_double_dot": [_i64, _D, _D, _D, _D, _D, _D, _D, _I, _dbl, _dbl, _i64, _i64, _D, _int],
+    "lpm_pse_interpolate_scalar": [_i64, _D, _D, _D, _D, _D, _I, _dbl, _dbl, _int, _i64, _D, _D, _D, _D, _int],
+    "lpm_swe_plane_rhs_integrals": [_i64, _D, _D, _D, _D, _D, _D, _I, _dbl, _i64, _i64, _D, _D, _D, _D, _int],
+    "lpm_swe_sphere_rhs_integrals": [_i64, _D, _D, _D, _D, _D, _D, _D, _I, _dbl, _dbl, _dbl, _i64, _i64, _D, _D, _D,
+                                     _D, _D, _int],
     "lpm_bve_solver_create": [_pvp, _i64, _D, _D, _D, _D, _D, _I, _D, _D, _D, _dbl, _dbl, _int],
     "lpm_bve_timestep": [_vp, _dbl, _int, _int],
     "lpm_bve_get_state": [_vp, _D, _D, _D, _D, _D, _D, _D],
@@ -268,6 +276,108 @@ def pse_sphere_divergence_at_particles(x, y, z, vx, vy, vz, area, active_mask, e
     _check(lib().lpm_pse_sphere_divergence(n, _dp(x), _dp(y), _dp(z), _dp(vx), _dp(vy), _dp(vz), _dp(area),
                                            _ip(act), float(eps), float(sphere_radius), ib, ie, _dp(d), _mode(mode)))
     return d
+
+
+def pse_plane_gradient_at_particles(x, y, f, area, active_mask, eps, i_begin=None, i_end=None, mode="fp64"):
+    """PSEPlaneGradientAtParticles (src/PSEDirectSum.f90:180).  Returns (gx, gy)."""
+    x, y, f, area = (_f64(a) for a in (x, y, f, area))
+    act = _i32(active_mask)
+    n = x.size
+    ib, ie = _range(n, i_begin, i_end)
+    gx, gy = np.zeros(n), np.zeros(n)
+    _check(lib().lpm_pse_plane_gradient(n, _dp(x), _dp(y), _dp(f), _dp(area), _ip(act), float(eps), ib, ie, _dp(gx),
+                                        _dp(gy), _mode(mode)))
+    return gx, gy
+
+
+def pse_plane_second_partials_at_particles(x, y, gx, gy, area, active_mask, eps, i_begin=None, i_end=None,
+                                           mode="fp64"):
+    """PSEPlaneSecondPartialsAtParticles (src/PSEDirectSum.f90:269).  Returns (dxx, dxy, dyy)."""
+    x, y, gx, gy, area = (_f64(a) for a in (x, y, gx, gy, area))
+    act = _i32(active_mask)
+    n = x.size
+    ib, ie = _range(n, i_begin, i_end)
+    o = [np.zeros(n) for _ in range(3)]
+    _check(lib().lpm_pse_plane_second_partials(n, _dp(x), _dp(y), _dp(gx), _dp(gy), _dp(area), _ip(act), float(eps),
+                                               ib, ie, _dp(o[0]), _dp(o[1]), _dp(o[2]), _mode(mode)))
+    return tuple(o)
+
+
+def pse_plane_double_dot_product_at_particles(x, y, u, v, area, active_mask, eps, i_begin=None, i_end=None,
+                                              mode="fp64"):
+    """PSEPlaneDoubleDotProductAtParticles (src/PSEDirectSum.f90:322)."""
+    x, y, u, v, area = (_f64(a) for a in (x, y, u, v, area))
+    act = _i32(active_mask)
+    n = x.size
+    ib, ie = _range(n, i_begin, i_end)
+    d = np.zeros(n)
+    _check(lib().lpm_pse_plane_double_dot(n, _dp(x), _dp(y), _dp(u), _dp(v), _dp(area), _ip(act), float(eps), ib, ie,
+                                          _dp(d), _mode(mode)))
+    return d
+
+
+def pse_sphere_double_dot_product_at_particles(x, y, z, u, v, w, area, active_mask, eps, sphere_radius=1.0,
+                                               i_begin=None, i_end=None, mode="fp64"):
+    """PSESphereDoubleDotProductAtParticles (src/PSEDirectSum.f90:367)."""
+    x, y, z, u, v, w, area = (_f64(a) for a in (x, y, z, u, v, w, area))
+    act = _i32(active_mask)
+    n = x.size
+    ib, ie = _range(n, i_begin, i_end)
+    d = np.zeros(n)
+    _check(lib().lpm_pse_sphere_double_dot(n, _dp(x), _dp(y), _dp(z), _dp(u), _dp(v), _dp(w), _dp(area), _ip(act),
+                                           float(eps), float(sphere_radius), ib, ie, _dp(d), _mode(mode)))
+    return d
+
+
+GEOMETRY_PLANE = 0
+GEOMETRY_SPHERE = 1
+
+
+def pse_interpolate_scalar(x, y, z, f, area, active_mask, eps, qx, qy, qz=None, geometry=GEOMETRY_PLANE,
+                           sphere_radius=1.0, mode="fp64"):
+    """PSEPlaneInterpolateScalar / PSESphereInterpolateScalar (src/PSEDirectSum.f90:128-168) at
+    every query point (qx, qy, qz) at once."""
+    x, y, f, area = (_f64(a) for a in (x, y, f, area))
+    act = _i32(active_mask)
+    qx, qy = _f64(qx), _f64(qy)
+    zp = None if z is None else _f64(z)
+    qzp = None if qz is None else _f64(qz)
+    out = np.zeros(qx.size)
+    _check(lib().lpm_pse_interpolate_scalar(x.size, _dp(x), _dp(y), None if zp is None else _dp(zp), _dp(f),
+                                            _dp(area), _ip(act), float(eps), float(sphere_radius), int(geometry),
+                                            qx.size, _dp(qx), _dp(qy), None if qzp is None else _dp(qzp), _dp(out),
+                                            _mode(mode)))
+    return out
+
+
+def swe_plane_rhs_integrals(x, y, vort, div, surf_height, area, active_mask, eps, i_begin=None, i_end=None,
+                            mode="fp64"):
+    """SWEPlaneRHSIntegrals (src/SWEPlaneSolver.f90:457), with surf_height = h + topoFn(x, y).
+    Returns (u, v, doubleDot, lapSurf)."""
+    x, y, vort, div, sh, area = (_f64(a) for a in (x, y, vort, div, surf_height, area))
+    act = _i32(active_mask)
+    n = x.size
+    ib, ie = _range(n, i_begin, i_end)
+    o = [np.zeros(n) for _ in range(4)]
+    _check(lib().lpm_swe_plane_rhs_integrals(n, _dp(x), _dp(y), _dp(vort), _dp(div), _dp(sh), _dp(area), _ip(act),
+                                             float(eps), ib, ie, _dp(o[0]), _dp(o[1]), _dp(o[2]), _dp(o[3]),
+                                             _mode(mode)))
+    return tuple(o)
+
+
+def swe_sphere_rhs_integrals(x, y, z, rel_vort, div, surf_height, area, active_mask, radius, pse_eps,
+                             sphere_radius=1.0, i_begin=None, i_end=None, mode="fp64"):
+    """SWESphereRHSIntegrals (src/SphereSWESolver.f90:299), with surf_height = h + topoFn(x, y, z)
+    and sphere_radius the SphereRadius of SphereDistance.  Returns (u, v, w, doubleDot, lapSurf)."""
+    x, y, z, rel_vort, div, sh, area = (_f64(a) for a in (x, y, z, rel_vort, div, surf_height, area))
+    act = _i32(active_mask)
+    n = x.size
+    ib, ie = _range(n, i_begin, i_end)
+    o = [np.zeros(n) for _ in range(5)]
+    _check(lib().lpm_swe_sphere_rhs_integrals(n, _dp(x), _dp(y), _dp(z), _dp(rel_vort), _dp(div), _dp(sh), _dp(area),
+                                              _ip(act), float(radius), float(sphere_radius), float(pse_eps), ib, ie,
+                                              _dp(o[0]), _dp(o[1]), _dp(o[2]), _dp(o[3]), _dp(o[4]), _mode(mode)))
+    return tuple(o)
 
 
 def set_stream_functions_on_mesh(x, y, z, rel_vort, abs_vort, area, active_mask, sphere_radius=1.0, i_begin=None,

@@ -432,3 +432,252 @@ void lpmo_bve_diagnostics(int64_t n, const double* u, const double* v, const dou
   *enstrophy = 0.5 * e;
   *circulation = c;
 }
+
+/* bivariateDeltaKernel8, src/PSEDirectSum.f90:611-616, with the power chain of lpmo_k8. */
+double lpmo_kdelta8(double r)
+{
+  const double r2 = r * r;
+  const double r3 = r * r2;
+  const double r4 = r2 * r2;
+  const double r6 = r3 * r3;
+  return (((4.0 - 6.0 * r2) + 2.0 * r4) - r6 / 6.0) * exp(-(r * r)) / PI;
+}
+
+/*
+ * PSEPlaneGradientAtParticles, src/PSEDirectSum.f90:180-217 (planar particles, z = 0): for
+ * every active j
+ *   grad += (f_j + f_i) (x_i - x_j) K1(ChordDistance(x_i, x_j)/eps) / eps**3 * A_j
+ * and the field is multiplied by 1/eps.
+ */
+void lpmo_pse_plane_gradient(int64_t n, const double* x, const double* y, const double* f,
+                             const double* area, const int32_t* active, double eps, int64_t ib,
+                             int64_t ie, double* gx, double* gy, int nthreads)
+{
+  const double eps3 = eps * (eps * eps);
+  const double scale = 1.0 / eps;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(pick_threads(nthreads))
+  for (int64_t i = ib; i < ie; ++i) {
+    double ax = 0.0, ay = 0.0;
+    for (int64_t j = 0; j < n; ++j) {
+      if (!active[j]) continue;
+      const double kin = chord_distance(x[i], y[i], 0.0, x[j], y[j], 0.0) / eps;
+      const double k1 = lpmo_k1(kin);
+      const double fs = f[j] + f[i];
+      ax = ax + (((fs * (x[i] - x[j])) * k1) / eps3) * area[j];
+      ay = ay + (((fs * (y[i] - y[j])) * k1) / eps3) * area[j];
+    }
+    gx[i] = scale * ax;
+    gy[i] = scale * ay;
+  }
+}
+
+/* The four planar first-derivative sums shared by the second partials and the double dot
+ * product, src/PSEDirectSum.f90:286-301 and :339-354:
+ *   s_ab += (a_j + a_i) (x_b,i - x_b,j) / eps * K1(chord/eps) / eps**2 * A_j. */
+static void plane_d4(int64_t n, const double* x, const double* y, const double* a, const double* b,
+                     const double* area, const int32_t* active, double eps, int64_t i, double s[4])
+{
+  const double eps2 = eps * eps;
+  double ax = 0.0, ay = 0.0, bx = 0.0, by = 0.0;
+  for (int64_t j = 0; j < n; ++j) {
+    if (!active[j]) continue;
+    const double kin = chord_distance(x[i], y[i], 0.0, x[j], y[j], 0.0) / eps;
+    const double kout = lpmo_k1(kin) / eps2;
+    const double dx = x[i] - x[j], dy = y[i] - y[j];
+    ax = ax + ((((a[j] + a[i]) * dx) / eps) * kout) * area[j];
+    ay = ay + ((((a[j] + a[i]) * dy) / eps) * kout) * area[j];
+    bx = bx + ((((b[j] + b[i]) * dx) / eps) * kout) * area[j];
+    by = by + ((((b[j] + b[i]) * dy) / eps) * kout) * area[j];
+  }
+  s[0] = ax;
+  s[1] = ay;
+  s[2] = bx;
+  s[3] = by;
+}
+
+/*
+ * PSEPlaneSecondPartialsAtParticles, src/PSEDirectSum.f90:269-320, from the gradient field
+ * (gx, gy): xx = dxx, xy = 0.5 (dxy + dyx), yy = dyy, each multiplied by 1/eps.
+ */
+void lpmo_pse_plane_second_partials(int64_t n, const double* x, const double* y, const double* gx,
+                                    const double* gy, const double* area, const int32_t* active,
+                                    double eps, int64_t ib, int64_t ie, double* dxx, double* dxy,
+                                    double* dyy, int nthreads)
+{
+  const double scale = 1.0 / eps;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(pick_threads(nthreads))
+  for (int64_t i = ib; i < ie; ++i) {
+    double s[4];
+    plane_d4(n, x, y, gx, gy, area, active, eps, i, s);
+    dxx[i] = scale * s[0];
+    dxy[i] = scale * (0.5 * (s[1] + s[2]));
+    dyy[i] = scale * s[3];
+  }
+}
+
+/* PSEPlaneDoubleDotProductAtParticles, src/PSEDirectSum.f90:322-365:
+ * (ux ux + 2 uy vx + vy vy) / eps**2 of the velocity (u, v). */
+void lpmo_pse_plane_double_dot(int64_t n, const double* x, const double* y, const double* u,
+                               const double* v, const double* area, const int32_t* active, double eps,
+                               int64_t ib, int64_t ie, double* ddot, int nthreads)
+{
+  const double eps2 = eps * eps;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(pick_threads(nthreads))
+  for (int64_t i = ib; i < ie; ++i) {
+    double s[4];
+    plane_d4(n, x, y, u, v, area, active, eps, i, s);
+    ddot[i] = ((s[0] * s[0] + (2.0 * s[1]) * s[2]) + s[3] * s[3]) / eps2;
+  }
+}
+
+/*
+ * PSESphereDoubleDotProductAtParticles, src/PSEDirectSum.f90:367-418: nine first-derivative
+ * sums with K1(SphereDistance(x_i, x_j)/eps) / eps**2.  As in the reference, the third row
+ * pairs w_j with v_i: (w_j + v_i) (:399-404).  Result (ux ux + vy vy + wz wz + 2 (uy vx +
+ * uz wx + vz wy)) / eps**2.
+ */
+void lpmo_pse_sphere_double_dot(int64_t n, const double* x, const double* y, const double* z,
+                                const double* u, const double* v, const double* w, const double* area,
+                                const int32_t* active, double eps, double radius, int64_t ib, int64_t ie,
+                                double* ddot, int nthreads)
+{
+  const double eps2 = eps * eps;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(pick_threads(nthreads))
+  for (int64_t i = ib; i < ie; ++i) {
+    double ux = 0.0, uy = 0.0, uz = 0.0, vx = 0.0, vy = 0.0, vz = 0.0, wx = 0.0, wy = 0.0, wz = 0.0;
+    for (int64_t j = 0; j < n; ++j) {
+      if (!active[j]) continue;
+      const double kin = sphere_distance(x[i], y[i], z[i], x[j], y[j], z[j], radius) / eps;
+      const double kout = lpmo_k1(kin) / eps2;
+      const double dx = x[i] - x[j], dy = y[i] - y[j], dz = z[i] - z[j];
+      const double su = u[j] + u[i], sv = v[j] + v[i], sw = w[j] + v[i];
+      ux = ux + (((su * dx) / eps) * kout) * area[j];
+      uy = uy + (((su * dy) / eps) * kout) * area[j];
+      uz = uz + (((su * dz) / eps) * kout) * area[j];
+      vx = vx + (((sv * dx) / eps) * kout) * area[j];
+      vy = vy + (((sv * dy) / eps) * kout) * area[j];
+      vz = vz + (((sv * dz) / eps) * kout) * area[j];
+      wx = wx + (((sw * dx) / eps) * kout) * area[j];
+      wy = wy + (((sw * dy) / eps) * kout) * area[j];
+      wz = wz + (((sw * dz) / eps) * kout) * area[j];
+    }
+    ddot[i] = (((ux * ux + vy * vy) + wz * wz) + 2.0 * ((uy * vx + uz * wx) + vz * wy)) / eps2;
+  }
+}
+
+/*
+ * PSEPlaneInterpolateScalar / PSESphereInterpolateScalar, src/PSEDirectSum.f90:128-168, at m
+ * query points q: sum over active j of f_j A_j Kdelta8(dist(q, x_j)/eps) / eps**2, with the
+ * chord distance (geometry 0) or the great-circle distance times radius (geometry 1).
+ */
+void lpmo_pse_interpolate(int64_t n, const double* x, const double* y, const double* z, const double* f,
+                          const double* area, const int32_t* active, double eps, double radius, int geometry,
+                          int64_t m, const double* qx, const double* qy, const double* qz, double* out,
+                          int nthreads)
+{
+  const double eps2 = eps * eps;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(pick_threads(nthreads))
+  for (int64_t k = 0; k < m; ++k) {
+    const double q0 = qx[k], q1 = qy[k], q2 = qz ? qz[k] : 0.0;
+    double s = 0.0;
+    for (int64_t j = 0; j < n; ++j) {
+      if (!active[j]) continue;
+      const double zj = z ? z[j] : 0.0;
+      const double d = geometry == 1 ? sphere_distance(x[j], y[j], zj, q0, q1, q2, radius)
+                                     : chord_distance(q0, q1, q2, x[j], y[j], zj);
+      s = s + ((f[j] * area[j]) * lpmo_kdelta8(d / eps)) / eps2;
+    }
+    out[k] = s;
+  }
+}
+
+/*
+ * SWEPlaneRHSIntegrals, src/SWEPlaneSolver.f90:457-534, with the surface height
+ * sh = h + topoFn(x, y) evaluated by the caller.  Per active j:
+ *   lapSurf += K8(r/eps)/eps**2 (sh_j - sh_i) A_j      (j = i included: a zero term)
+ * and for j != i, with r^2 = dx^2 + dy^2, denom = 2 pi r^2, denom2 = pi r^4,
+ *   rot = vort_j A_j / denom, pot = div_j A_j / denom,
+ *   u += -dy rot + dx pot,  v += dx rot + dy pot,
+ *   ux += pot - dx (dx div_j - dy vort_j) A_j / denom2,  uy += -rot - dy (dx div_j - dy vort_j) A_j / denom2,
+ *   vx += rot - dx (dy div_j + dx vort_j) A_j / denom2,  vy += pot - dy (dy div_j + dx vort_j) A_j / denom2;
+ * then lapSurf /= eps**2 and doubleDot = ux ux + 2 uy vx + vy vy.
+ */
+void lpmo_swe_plane_rhs(int64_t n, const double* x, const double* y, const double* vort, const double* div,
+                        const double* sh, const double* area, const int32_t* active, double eps, int64_t ib,
+                        int64_t ie, double* u, double* v, double* ddot, double* lap, int nthreads)
+{
+  const double eps2 = eps * eps;
+  const double two_pi = 2.0 * PI;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(pick_threads(nthreads))
+  for (int64_t i = ib; i < ie; ++i) {
+    double ui = 0.0, vi = 0.0, li = 0.0, ux = 0.0, uy = 0.0, vx = 0.0, vy = 0.0;
+    for (int64_t j = 0; j < n; ++j) {
+      if (!active[j]) continue;
+      const double dx = x[i] - x[j], dy = y[i] - y[j];
+      const double sq = dx * dx + dy * dy;
+      const double denom = two_pi * sq;
+      const double denom2 = (PI * sq) * sq;
+      const double rot = (vort[j] * area[j]) / denom;
+      const double pot = (div[j] * area[j]) / denom;
+      const double lk = lpmo_k8(sqrt(sq) / eps) / eps2;
+      li = li + (lk * (sh[j] - sh[i])) * area[j];
+      if (j == i) continue;
+      ui = (ui - dy * rot) + dx * pot;
+      vi = (vi + dx * rot) + dy * pot;
+      const double cu = dx * div[j] - dy * vort[j];
+      const double cv = dy * div[j] + dx * vort[j];
+      ux = (ux + pot) - ((dx * cu) * area[j]) / denom2;
+      uy = (uy - rot) - ((dy * cu) * area[j]) / denom2;
+      vx = (vx + rot) - ((dx * cv) * area[j]) / denom2;
+      vy = (vy + pot) - ((dy * cv) * area[j]) / denom2;
+    }
+    u[i] = ui;
+    v[i] = vi;
+    lap[i] = li / eps2;
+    ddot[i] = (ux * ux + (2.0 * uy) * vx) + vy * vy;
+  }
+}
+
+/*
+ * SWESphereRHSIntegrals, src/SphereSWESolver.f90:299-372, with sh = h + topoFn(x, y, z) from
+ * the caller.  Per active j:
+ *   lapSurf += K8(SphereDistance(x_i, x_j)/eps)/eps**2 (sh_j - sh_i) A_j   (j = i included)
+ * (SphereDistance scales by the module's SphereRadius, `sphere_radius` here), and for j != i,
+ * with denom = 4 pi a^2 (a^2 - x_i.x_j):
+ *   rot = zeta_j A_j / denom, pot = a div_j A_j / denom,
+ *   u -= (y_i z_j - z_i y_j) rot + x_j pot (and cyclically for v, w).
+ * As in the reference, doubleDot stays 0 and lapSurf is not divided again by eps**2.
+ */
+void lpmo_swe_sphere_rhs(int64_t n, const double* x, const double* y, const double* z, const double* relvort,
+                         const double* div, const double* sh, const double* area, const int32_t* active,
+                         double radius, double sphere_radius, double eps, int64_t ib, int64_t ie, double* u,
+                         double* v, double* w, double* ddot, double* lap, int nthreads)
+{
+  const double eps2 = eps * eps;
+  const double four_pi_r2 = ((4.0 * PI) * radius) * radius;
+  const double a2 = radius * radius;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(pick_threads(nthreads))
+  for (int64_t i = ib; i < ie; ++i) {
+    const double xi = x[i], yi = y[i], zi = z[i];
+    double ui = 0.0, vi = 0.0, wi = 0.0, li = 0.0;
+    for (int64_t j = 0; j < n; ++j) {
+      if (!active[j]) continue;
+      const double kin = sphere_distance(xi, yi, zi, x[j], y[j], z[j], sphere_radius) / eps;
+      const double lk = lpmo_k8(kin) / eps2;
+      li = li + (lk * (sh[j] - sh[i])) * area[j];
+      if (j == i) continue;
+      const double dp = (xi * x[j] + yi * y[j]) + zi * z[j];
+      const double denom = four_pi_r2 * (a2 - dp);
+      const double rot = (relvort[j] * area[j]) / denom;
+      const double pot = ((radius * div[j]) * area[j]) / denom;
+      ui = (ui - (yi * z[j] - zi * y[j]) * rot) - x[j] * pot;
+      vi = (vi - (zi * x[j] - xi * z[j]) * rot) - y[j] * pot;
+      wi = (wi - (xi * y[j] - yi * x[j]) * rot) - z[j] * pot;
+    }
+    u[i] = ui;
+    v[i] = vi;
+    w[i] = wi;
+    lap[i] = li;
+    ddot[i] = 0.0;
+  }
+}

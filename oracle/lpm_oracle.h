@@ -88,9 +88,51 @@ void lpmo_pse_sphere_divergence(int64_t n, const double* x, const double* y, con
                                 const double* area, const int32_t* active, double eps,
                                 double radius, int64_t ib, int64_t ie, double* div, int nthreads);
 
-/* K8(r) of PSEDirectSum.f90:622-627 and the first-derivative kernel K1 of :629-634 */
+/* K8(r) of PSEDirectSum.f90:622-627, the first-derivative kernel K1 of :629-634 and the
+ * delta kernel of :611-616 */
 double lpmo_k8(double r);
 double lpmo_k1(double r);
+double lpmo_kdelta8(double r);
+
+/* PSEPlaneGradientAtParticles, PSEDirectSum.f90:180-217 */
+void lpmo_pse_plane_gradient(int64_t n, const double* x, const double* y, const double* f,
+                             const double* area, const int32_t* active, double eps, int64_t ib,
+                             int64_t ie, double* gx, double* gy, int nthreads);
+
+/* PSEPlaneSecondPartialsAtParticles, PSEDirectSum.f90:269-320 (from the gradient field) */
+void lpmo_pse_plane_second_partials(int64_t n, const double* x, const double* y, const double* gx,
+                                    const double* gy, const double* area, const int32_t* active,
+                                    double eps, int64_t ib, int64_t ie, double* dxx, double* dxy,
+                                    double* dyy, int nthreads);
+
+/* PSEPlaneDoubleDotProductAtParticles, PSEDirectSum.f90:322-365 */
+void lpmo_pse_plane_double_dot(int64_t n, const double* x, const double* y, const double* u,
+                               const double* v, const double* area, const int32_t* active, double eps,
+                               int64_t ib, int64_t ie, double* ddot, int nthreads);
+
+/* PSESphereDoubleDotProductAtParticles, PSEDirectSum.f90:367-418 */
+void lpmo_pse_sphere_double_dot(int64_t n, const double* x, const double* y, const double* z,
+                                const double* u, const double* v, const double* w, const double* area,
+                                const int32_t* active, double eps, double radius, int64_t ib, int64_t ie,
+                                double* ddot, int nthreads);
+
+/* PSEPlaneInterpolateScalar (geometry 0) / PSESphereInterpolateScalar (geometry 1),
+ * PSEDirectSum.f90:128-168, at m query points */
+void lpmo_pse_interpolate(int64_t n, const double* x, const double* y, const double* z, const double* f,
+                          const double* area, const int32_t* active, double eps, double radius, int geometry,
+                          int64_t m, const double* qx, const double* qy, const double* qz, double* out,
+                          int nthreads);
+
+/* SWEPlaneRHSIntegrals, SWEPlaneSolver.f90:457-534 (sh = h + topoFn(x, y)) */
+void lpmo_swe_plane_rhs(int64_t n, const double* x, const double* y, const double* vort, const double* div,
+                        const double* sh, const double* area, const int32_t* active, double eps, int64_t ib,
+                        int64_t ie, double* u, double* v, double* ddot, double* lap, int nthreads);
+
+/* SWESphereRHSIntegrals, SphereSWESolver.f90:299-372 (sh = h + topoFn(x, y, z)) */
+void lpmo_swe_sphere_rhs(int64_t n, const double* x, const double* y, const double* z, const double* relvort,
+                         const double* div, const double* sh, const double* area, const int32_t* active,
+                         double radius, double sphere_radius, double eps, int64_t ib, int64_t ie, double* u,
+                         double* v, double* w, double* ddot, double* lap, int nthreads);
 
 #ifdef __cplusplus
 }

@@ -49,6 +49,19 @@ def lib():
                                                _i64, _i64, _D, _D, _D, ctypes.c_int]
         L.lpmo_pse_sphere_divergence.argtypes = [_i64, _D, _D, _D, _D, _D, _D, _D, _I, ctypes.c_double,
                                                  ctypes.c_double, _i64, _i64, _D, ctypes.c_int]
+        c_d, c_i = ctypes.c_double, ctypes.c_int
+        L.lpmo_pse_plane_gradient.argtypes = [_i64, _D, _D, _D, _D, _I, c_d, _i64, _i64, _D, _D, c_i]
+        L.lpmo_pse_plane_second_partials.argtypes = [_i64, _D, _D, _D, _D, _D, _I, c_d, _i64, _i64, _D, _D, _D,
+                                                     c_i]
+        L.lpmo_pse_plane_double_dot.argtypes = [_i64, _D, _D, _D, _D, _D, _I, c_d, _i64, _i64, _D, c_i]
+        L.lpmo_pse_sphere_double_dot.argtypes = [_i64, _D, _D, _D, _D, _D, _D, _D, _I, c_d, c_d, _i64, _i64, _D,
+                                                 c_i]
+        L.lpmo_pse_interpolate.argtypes = [_i64, _D, _D, _D, _D, _D, _I, c_d, c_d, c_i, _i64, _D, _D, _D, _D, c_i]
+        L.lpmo_swe_plane_rhs.argtypes = [_i64, _D, _D, _D, _D, _D, _D, _I, c_d, _i64, _i64, _D, _D, _D, _D, c_i]
+        L.lpmo_swe_sphere_rhs.argtypes = [_i64, _D, _D, _D, _D, _D, _D, _D, _I, c_d, c_d, c_d, _i64, _i64, _D, _D,
+                                          _D, _D, _D, c_i]
+        L.lpmo_kdelta8.argtypes = [ctypes.c_double]
+        L.lpmo_kdelta8.restype = ctypes.c_double
         L.lpmo_k8.argtypes = [ctypes.c_double]
         L.lpmo_k1.argtypes = [ctypes.c_double]
         L.lpmo_k1.restype = ctypes.c_double
@@ -135,6 +148,94 @@ def pse_sphere_divergence(x, y, z, vx, vy, vz, area, active, eps, radius=1.0, ib
     lib().lpmo_pse_sphere_divergence(n, _d(x), _d(y), _d(z), _d(vx), _d(vy), _d(vz), _d(area),
                                      active.ctypes.data_as(_I), eps, radius, ib, ie, _d(d), threads)
     return d[ib:ie]
+
+
+def pse_plane_gradient(x, y, f, area, active, eps, ib=None, ie=None, threads=0):
+    """PSEPlaneGradientAtParticles (src/PSEDirectSum.f90:180-217); returns (gx, gy) of the block."""
+    x, y, f, area, active = _f64(x), _f64(y), _f64(f), _f64(area), _i32(active)
+    n = x.size
+    ib, ie = _range(n, ib, ie)
+    g = [np.zeros(n) for _ in range(2)]
+    lib().lpmo_pse_plane_gradient(n, _d(x), _d(y), _d(f), _d(area), active.ctypes.data_as(_I), eps, ib, ie,
+                                  _d(g[0]), _d(g[1]), threads)
+    return tuple(a[ib:ie] for a in g)
+
+
+def pse_plane_second_partials(x, y, gx, gy, area, active, eps, ib=None, ie=None, threads=0):
+    """PSEPlaneSecondPartialsAtParticles (src/PSEDirectSum.f90:269-320); returns (xx, xy, yy)."""
+    x, y, gx, gy, area, active = _f64(x), _f64(y), _f64(gx), _f64(gy), _f64(area), _i32(active)
+    n = x.size
+    ib, ie = _range(n, ib, ie)
+    o = [np.zeros(n) for _ in range(3)]
+    lib().lpmo_pse_plane_second_partials(n, _d(x), _d(y), _d(gx), _d(gy), _d(area), active.ctypes.data_as(_I),
+                                         eps, ib, ie, _d(o[0]), _d(o[1]), _d(o[2]), threads)
+    return tuple(a[ib:ie] for a in o)
+
+
+def pse_plane_double_dot(x, y, u, v, area, active, eps, ib=None, ie=None, threads=0):
+    """PSEPlaneDoubleDotProductAtParticles (src/PSEDirectSum.f90:322-365)."""
+    x, y, u, v, area, active = _f64(x), _f64(y), _f64(u), _f64(v), _f64(area), _i32(active)
+    n = x.size
+    ib, ie = _range(n, ib, ie)
+    o = np.zeros(n)
+    lib().lpmo_pse_plane_double_dot(n, _d(x), _d(y), _d(u), _d(v), _d(area), active.ctypes.data_as(_I), eps,
+                                    ib, ie, _d(o), threads)
+    return o[ib:ie]
+
+
+def pse_sphere_double_dot(x, y, z, u, v, w, area, active, eps, radius=1.0, ib=None, ie=None, threads=0):
+    """PSESphereDoubleDotProductAtParticles (src/PSEDirectSum.f90:367-418)."""
+    x, y, z, u, v, w, area, active = (_f64(x), _f64(y), _f64(z), _f64(u), _f64(v), _f64(w), _f64(area),
+                                      _i32(active))
+    n = x.size
+    ib, ie = _range(n, ib, ie)
+    o = np.zeros(n)
+    lib().lpmo_pse_sphere_double_dot(n, _d(x), _d(y), _d(z), _d(u), _d(v), _d(w), _d(area),
+                                     active.ctypes.data_as(_I), eps, radius, ib, ie, _d(o), threads)
+    return o[ib:ie]
+
+
+def pse_interpolate(x, y, z, f, area, active, eps, qx, qy, qz, geometry, radius=1.0, threads=0):
+    """PSEPlaneInterpolateScalar (geometry 0) / PSESphereInterpolateScalar (geometry 1),
+    src/PSEDirectSum.f90:128-168, at the query points (qx, qy, qz)."""
+    x, y, f, area, active = _f64(x), _f64(y), _f64(f), _f64(area), _i32(active)
+    z = np.zeros_like(x) if z is None else _f64(z)
+    qx, qy = _f64(qx), _f64(qy)
+    qz = np.zeros_like(qx) if qz is None else _f64(qz)
+    o = np.zeros(qx.size)
+    lib().lpmo_pse_interpolate(x.size, _d(x), _d(y), _d(z), _d(f), _d(area), active.ctypes.data_as(_I), eps,
+                               radius, geometry, qx.size, _d(qx), _d(qy), _d(qz), _d(o), threads)
+    return o
+
+
+def swe_plane_rhs(x, y, vort, div, sh, area, active, eps, ib=None, ie=None, threads=0):
+    """SWEPlaneRHSIntegrals (src/SWEPlaneSolver.f90:457-534); returns (u, v, doubleDot, lapSurf)."""
+    x, y, vort, div, sh, area, active = (_f64(x), _f64(y), _f64(vort), _f64(div), _f64(sh), _f64(area),
+                                         _i32(active))
+    n = x.size
+    ib, ie = _range(n, ib, ie)
+    o = [np.zeros(n) for _ in range(4)]
+    lib().lpmo_swe_plane_rhs(n, _d(x), _d(y), _d(vort), _d(div), _d(sh), _d(area), active.ctypes.data_as(_I), eps,
+                             ib, ie, _d(o[0]), _d(o[1]), _d(o[2]), _d(o[3]), threads)
+    return tuple(a[ib:ie] for a in o)
+
+
+def swe_sphere_rhs(x, y, z, relvort, div, sh, area, active, radius, sphere_radius, eps, ib=None, ie=None,
+                   threads=0):
+    """SWESphereRHSIntegrals (src/SphereSWESolver.f90:299-372); returns (u, v, w, doubleDot, lapSurf)."""
+    x, y, z, relvort, div, sh, area, active = (_f64(x), _f64(y), _f64(z), _f64(relvort), _f64(div), _f64(sh),
+                                               _f64(area), _i32(active))
+    n = x.size
+    ib, ie = _range(n, ib, ie)
+    o = [np.zeros(n) for _ in range(5)]
+    lib().lpmo_swe_sphere_rhs(n, _d(x), _d(y), _d(z), _d(relvort), _d(div), _d(sh), _d(area),
+                              active.ctypes.data_as(_I), radius, sphere_radius, eps, ib, ie, _d(o[0]), _d(o[1]),
+                              _d(o[2]), _d(o[3]), _d(o[4]), threads)
+    return tuple(a[ib:ie] for a in o)
+
+
+def kdelta8(r):
+    return lib().lpmo_kdelta8(float(r))
 
 
 def bve_stream(x, y, z, relvort, absvort, area, active, radius=1.0, ib=None, ie=None, threads=0):

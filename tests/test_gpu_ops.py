@@ -1,0 +1,114 @@
+"""GPU parity of the remaining PSE operators and the shallow-water integrals (LPM_MODE_FP64)
+through the C ABI, against the oracle: bit-identical where the loop has no transcendental
+function (the SWE velocities and double dot products), within 1e-12 of max|result| where
+exp/atan2 enter (CUDA's and the C library's may differ by an ulp).  Block ranges
+(i_begin/i_end) and random activity masks are covered."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12
+
+
+@pytest.fixture(scope="module")
+def lg(built_lib):
+    return built_lib
+
+
+def rel(got, ref):
+    return np.abs(got - ref).max() / max(np.abs(ref).max(), 1e-300)
+
+
+def _plane(lg, nest, seed, frac_active=1.0):
+    m = lg.PolyMesh2d(202, nest, 4.0)
+    act = m.active.copy()
+    if frac_active < 1.0:
+        rng = np.random.default_rng(seed)
+        act = act * (rng.random(m.n) < frac_active).astype(np.int32)
+    eps = 2.0 * np.sqrt(m.area[m.active == 1].max())
+    return m, act, eps
+
+
+@pytest.mark.parametrize("nest,frac,block", [(3, 1.0, None), (4, 0.7, (17, 1500))])
+def test_pse_plane_gradient_second_ddot(lg, oracle_mod, nest, frac, block):
+    m, act, eps = _plane(lg, nest, 11, frac)
+    rng = np.random.default_rng(2)
+    f = np.sin(m.x) * np.cos(0.5 * m.y) + 0.01 * rng.random(m.n)
+    ib, ie = (1, m.n) if block is None else block
+    gx, gy = lg.pse_plane_gradient_at_particles(m.x, m.y, f, m.area, act, eps, ib, ie)
+    rx, ry = oracle_mod.pse_plane_gradient(m.x, m.y, f, m.area, act, eps, ib - 1, ie)
+    assert rel(gx[ib - 1:ie], rx) <= TOL and rel(gy[ib - 1:ie], ry) <= TOL
+    assert np.all(gx[:ib - 1] == 0) and np.all(gx[ie:] == 0)
+    xx, xy, yy = lg.pse_plane_second_partials_at_particles(m.x, m.y, f, 0.5 * f, m.area, act, eps, ib, ie)
+    r = oracle_mod.pse_plane_second_partials(m.x, m.y, f, 0.5 * f, m.area, act, eps, ib - 1, ie)
+    for g, rr in zip((xx, xy, yy), r):
+        assert rel(g[ib - 1:ie], rr) <= TOL
+    u, v = np.cos(m.y), 0.3 * np.sin(m.x)
+    dd = lg.pse_plane_double_dot_product_at_particles(m.x, m.y, u, v, m.area, act, eps, ib, ie)
+    rd = oracle_mod.pse_plane_double_dot(m.x, m.y, u, v, m.area, act, eps, ib - 1, ie)
+    assert rel(dd[ib - 1:ie], rd) <= TOL
+
+
+@pytest.mark.parametrize("radius", [1.0, 6.37122e6])
+def test_pse_sphere_double_dot(lg, oracle_mod, radius):
+    m = lg.PolyMesh2d(205, 3, 1.0)
+    x, y, z = m.x * radius, m.y * radius, m.z * radius
+    area = m.area * radius ** 2
+    u, v, w = -m.y, m.x, 0.2 * m.z
+    eps = 0.2 * radius
+    got = lg.pse_sphere_double_dot_product_at_particles(x, y, z, u, v, w, area, m.active, eps, radius)
+    ref = oracle_mod.pse_sphere_double_dot(x, y, z, u, v, w, area, m.active, eps, radius)
+    assert rel(got, ref) <= TOL
+
+
+def test_pse_interpolation_plane_and_sphere(lg, oracle_mod):
+    m, act, eps = _plane(lg, 4, 0)
+    f = np.cos(m.x) * np.sin(m.y)
+    rng = np.random.default_rng(9)
+    qx, qy = rng.uniform(-3, 3, 257), rng.uniform(-3, 3, 257)
+    got = lg.pse_interpolate_scalar(m.x, m.y, None, f, m.area, act, eps, qx, qy)
+    ref = oracle_mod.pse_interpolate(m.x, m.y, None, f, m.area, act, eps, qx, qy, None, 0)
+    assert rel(got, ref) <= TOL
+    s = lg.PolyMesh2d(206, 4, 1.0)
+    q = rng.standard_normal((3, 100))
+    q /= np.linalg.norm(q, axis=0)
+    fs = 1.0 + s.z + s.x * s.y
+    eps_s = 2.0 * np.sqrt(s.area[s.active == 1].max())
+    got = lg.pse_interpolate_scalar(s.x, s.y, s.z, fs, s.area, s.active, eps_s, q[0], q[1], q[2],
+                                    geometry=lg.GEOMETRY_SPHERE)
+    ref = oracle_mod.pse_interpolate(s.x, s.y, s.z, fs, s.area, s.active, eps_s, q[0], q[1], q[2], 1)
+    assert rel(got, ref) <= TOL
+
+
+@pytest.mark.parametrize("nest,block", [(3, None), (4, (100, 2000))])
+def test_swe_plane_rhs(lg, oracle_mod, nest, block):
+    m, act, eps = _plane(lg, nest, 4, 0.9)
+    vort = np.exp(-(m.x ** 2 + m.y ** 2))
+    div = 0.3 * np.exp(-((m.x - 1) ** 2 + m.y ** 2))
+    sh = 1.0 + 0.1 * np.cos(m.x)
+    ib, ie = (1, m.n) if block is None else block
+    got = lg.swe_plane_rhs_integrals(m.x, m.y, vort, div, sh, m.area, act, eps, ib, ie)
+    ref = oracle_mod.swe_plane_rhs(m.x, m.y, vort, div, sh, m.area, act, eps, ib - 1, ie)
+    s = slice(ib - 1, ie)
+    # velocity and double dot: no transcendental function in the loop -> bit-identical
+    assert np.array_equal(got[0][s], ref[0]) and np.array_equal(got[1][s], ref[1])
+    assert np.array_equal(got[2][s], ref[2])
+    assert rel(got[3][s], ref[3]) <= TOL
+
+
+@pytest.mark.parametrize("radius,sphere_radius", [(1.0, 1.0), (6.37122e6, 1.0)])
+def test_swe_sphere_rhs(lg, oracle_mod, radius, sphere_radius):
+    m = lg.PolyMesh2d(205, 3, 1.0)
+    x, y, z = m.x * radius, m.y * radius, m.z * radius
+    area = m.area * radius ** 2
+    zeta = np.exp(-4 * ((m.x - 0.5) ** 2 + m.y ** 2 + (m.z - 0.7) ** 2))
+    div = 0.1 * np.cos(3 * m.z)
+    sh = 1.0 + 0.2 * m.z
+    eps = 0.25
+    got = lg.swe_sphere_rhs_integrals(x, y, z, zeta, div, sh, area, m.active, radius, eps, sphere_radius, 5, 1800)
+    ref = oracle_mod.swe_sphere_rhs(x, y, z, zeta, div, sh, area, m.active, radius, sphere_radius, eps, 4, 1800)
+    s = slice(4, 1800)
+    for c in range(3):
+        assert np.array_equal(got[c][s], ref[c])
+    assert np.all(got[3][s] == 0.0)
+    assert rel(got[4][s], ref[4]) <= TOL
