@@ -183,6 +183,25 @@ int lpm_swe_sphere_rhs_integrals(int64_t n, const double* x, const double* y, co
                                  double* u, double* v, double* w, double* double_dot,
                                  double* lap_surf, int mode);
 
+/* Replaces BetaPlaneVelocity (src/BetaPlaneSolver.f90:227-268) and the beta plane's
+ * setVelocityFromVorticity (src/BetaPlane.f90:359-397), the x-periodic (period 1) sum
+ *   u_i = -sum_j sinh(2 pi dy) s_j,  v_i = sum_j sin(2 pi dx) s_j,
+ *   s_j = 0.5 zeta_j A_j / (cosh(2 pi dy) - cos(2 pi dx)),  dx = x_i - x_j, dy = y_i - y_j,
+ * over active j != i.  LPM_MODE_FP32C evaluates the kernel in FP32 in a form without
+ * cancellation (sinh/sin of half angles) with periodic neighbours kept to full precision,
+ * velocity error <= 1e-6 of max|u|. */
+int lpm_beta_plane_velocity(int64_t n, const double* x, const double* y, const double* zeta,
+                            const double* area, const int32_t* active, int64_t i_begin, int64_t i_end,
+                            double* u, double* v, int mode);
+
+/* Replaces the beta plane's SetStreamFunctionsOnMesh (src/BetaPlane.f90:399-442):
+ * psi = sum_{j != i} log(cosh(2 pi dy) - cos(2 pi dx)) / (4 pi) zeta_j A_j for the relative
+ * and the absolute vorticity.  LPM_MODE_FP64 only. */
+int lpm_beta_plane_stream_functions(int64_t n, const double* x, const double* y, const double* relvort,
+                                    const double* absvort, const double* area, const int32_t* active,
+                                    int64_t i_begin, int64_t i_end, double* psi_rel, double* psi_abs,
+                                    int mode);
+
 /* Replaces SetStreamFunctionsOnMesh (src/SphereBVE.f90:445-485): psi = sum G zeta A with
  * G = -log(a^2 - x_i.x_j)/(4 pi), for the relative and absolute vorticity, j != i.
  * LPM_MODE_FP64 follows the Fortran loop (its log is CUDA's, so agreement is to ~1e-15

@@ -616,6 +616,143 @@ struct SweSphereF64 {
   static constexpr bool kSkipSelf = false;
 };
 
+// BetaPlaneVelocity, src/BetaPlaneSolver.f90:227-268 (RecStream64: qr = zeta_j, area): the
+// x-periodic kernel, strength = ((0.5 zeta_j) A_j) / (cosh(2 pi dy) - cos(2 pi dx)),
+// u -= sinh(2 pi dy) strength, v += sin(2 pi dx) strength; j = i skipped.
+struct BetaF64Params {
+  const double *x, *y;
+  double two_pi, four_pi;
+  double *o0, *o1;
+};
+
+struct BetaVelF64 {
+  struct Tgt {
+    double x, y;
+  };
+  struct Acc {
+    double u, v;
+  };
+  __device__ static Tgt load(const BetaF64Params& p, int64_t i) { return Tgt{p.x[i], p.y[i]}; }
+  __device__ static __forceinline__ void interact(const BetaF64Params& p, const Tgt& t, const RecStream64& r,
+                                                  Acc& a) {
+    const double ay = __dmul_rn(p.two_pi, __dsub_rn(t.y, r.y)), ax = __dmul_rn(p.two_pi, __dsub_rn(t.x, r.x));
+    const double s = __ddiv_rn(__dmul_rn(__dmul_rn(0.5, r.qr), r.area), __dsub_rn(cosh(ay), cos(ax)));
+    a.u = __dsub_rn(a.u, __dmul_rn(sinh(ay), s));
+    a.v = __dadd_rn(a.v, __dmul_rn(sin(ax), s));
+  }
+  __device__ static void store(const BetaF64Params& p, int64_t i, int64_t il, const Acc& a) {
+    p.o0[il] = a.u;
+    p.o1[il] = a.v;
+  }
+  static constexpr bool kSkipSelf = true;
+};
+
+// SetStreamFunctionsOnMesh of the beta plane, src/BetaPlane.f90:399-442 (RecStream64: qr, qa
+// = relative and absolute vorticity): G = log(cosh(2 pi dy) - cos(2 pi dx)) / (4 pi),
+// psi += (G zeta_j) A_j; j = i skipped.
+struct BetaStreamF64 {
+  struct Tgt {
+    double x, y;
+  };
+  struct Acc {
+    double r, a;
+  };
+  __device__ static Tgt load(const BetaF64Params& p, int64_t i) { return Tgt{p.x[i], p.y[i]}; }
+  __device__ static __forceinline__ void interact(const BetaF64Params& p, const Tgt& t, const RecStream64& r,
+                                                  Acc& a) {
+    const double g = __ddiv_rn(log(__dsub_rn(cosh(__dmul_rn(p.two_pi, __dsub_rn(t.y, r.y))),
+                                             cos(__dmul_rn(p.two_pi, __dsub_rn(t.x, r.x))))),
+                               p.four_pi);
+    a.r = __dadd_rn(a.r, __dmul_rn(__dmul_rn(g, r.qr), r.area));
+    a.a = __dadd_rn(a.a, __dmul_rn(__dmul_rn(g, r.qa), r.area));
+  }
+  __device__ static void store(const BetaF64Params& p, int64_t i, int64_t il, const Acc& a) {
+    p.o0[il] = a.r;
+    p.o1[il] = a.a;
+  }
+  static constexpr bool kSkipSelf = true;
+};
+
+// ============================================================ beta-plane velocity (FP32C)
+// BetaPlaneVelocity, src/BetaPlaneSolver.f90:227-268, in FP32 with a form that does not
+// cancel: cosh(2a) - cos(2b) = 2 (sinh^2 a + sin^2 b), sinh 2a = 2 sinh a cosh a and
+// sin 2b = 2 sin b cos b with a = pi dy, b = pi dx, so per pair
+//   u -= S sh ch / (sh^2 + sn^2),  v += S sn cs / (sh^2 + sn^2),  S = zeta_j A_j / 2.
+// dx is reduced to t = dx - rint(dx) in [-1/2, 1/2] (the kernel has period 1 in x) with the
+// rounding of x_i - x_j kept (TwoSum), so that neighbours across the periodic boundary keep
+// full precision; sin(pi t), cos(pi t) are Taylor polynomials (|error| <= 6e-8 on the
+// interval).  sinh and cosh of a = pi |dy| use a = k ln 2 + r, |r| <= ln2/2, polynomials in
+// r, and sinh a = 2^(k-1) ((1 - 4^-k) cosh r + (1 + 4^-k) sinh r) (cosh alike); the common
+// factor 2^(k-1) is divided out of every term (sn, cs scaled by 2^(1-k)), so nothing
+// overflows for any dy.  The self pair (d = 0) has zero numerators and a denominator of
+// 2^-100, a zero term.
+struct BetaF32 {
+  static constexpr int NC = 2;
+  struct __align__(16) Rec {
+    float4 a;  // x_hi, y_hi, x_lo, y_lo
+    float4 b;  // S = zeta A / 2, 0, 0, 0
+  };
+  struct Tgt {
+    float xh, yh, xl, yl;
+  };
+  struct Params {
+    const double *x, *y;
+  };
+  __device__ static Tgt load_target(const Params& p, int64_t i) {
+    Tgt t;
+    split2(p.x[i], t.xh, t.xl);
+    split2(p.y[i], t.yh, t.yl);
+    return t;
+  }
+  __device__ static __forceinline__ void interact(const Tgt& t, const Rec& r, float (&acc)[2]) {
+    constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23: x + kMagic - kMagic = rint(x)
+    // t = (x_i - x_j) - rint(x_i - x_j), with the rounding error of the hi difference
+    const float dh = __fadd_rn(t.xh, -r.a.x);
+    const float bb = __fadd_rn(dh, -t.xh);
+    const float e = __fadd_rn(__fadd_rn(t.xh, -__fadd_rn(dh, -bb)), __fadd_rn(-r.a.x, -bb));
+    const float n = __fadd_rn(__fadd_rn(dh, kMagic), -kMagic);
+    const float tt = __fadd_rn(__fadd_rn(dh, -n), __fadd_rn(e, __fadd_rn(t.xl, -r.a.z)));
+    const float dy = diff2(t.yh, t.yl, r.a.y, r.a.w);
+    // sin(pi t), cos(pi t)
+    const float t2 = __fmul_rn(tt, tt);
+    float ps = __fmaf_rn(-0.00737043097615242f, t2, 0.08214588463306427f);
+    ps = __fmaf_rn(ps, t2, -0.5992645025253296f);
+    ps = __fmaf_rn(ps, t2, 2.550163984298706f);
+    ps = __fmaf_rn(ps, t2, -5.167712688446045f);
+    ps = __fmaf_rn(ps, t2, 3.1415927410125732f);
+    const float sn = __fmul_rn(ps, tt);
+    float pc = __fmaf_rn(0.001929574296809733f, t2, -0.025806890800595284f);
+    pc = __fmaf_rn(pc, t2, 0.23533062636852264f);
+    pc = __fmaf_rn(pc, t2, -1.3352627754211426f);
+    pc = __fmaf_rn(pc, t2, 4.058712005615234f);
+    pc = __fmaf_rn(pc, t2, -4.934802055358887f);
+    const float cs = __fmaf_rn(pc, t2, 1.0f);
+    // sinh, cosh of a = pi |dy| as 2^(k-1) (sh', ch')
+    const float a = __fmul_rn(3.1415927f, fabsf(dy));
+    const float kb = __fmaf_rn(a, 1.442695f, kMagic);  // kMagic + rint(a / ln 2)
+    const float kf = __fadd_rn(kb, -kMagic);
+    float rr = __fmaf_rn(-kf, 0.69314575f, a);
+    rr = __fmaf_rn(-kf, 1.4286068e-06f, rr);
+    const float r2 = __fmul_rn(rr, rr);
+    const float shr = __fmaf_rn(__fmul_rn(rr, r2),
+                                __fmaf_rn(__fmaf_rn(r2, 1.9841270e-4f, 8.3333333e-3f), r2, 0.16666667f), rr);
+    const float chr = __fmaf_rn(
+        __fmaf_rn(__fmaf_rn(__fmaf_rn(r2, 2.4801587e-5f, 1.3888889e-3f), r2, 4.1666667e-2f), r2, 0.5f), r2, 1.0f);
+    const int k = __float_as_int(kb) - 0x4b400000;
+    const int kq = k < 63 ? k : 63, ks = k < 126 ? k : 126;
+    const float q = __int_as_float((127 - 2 * kq) << 23);  // 4^-k
+    const float sc = __int_as_float((128 - ks) << 23);     // 2^(1-k)
+    const float om = __fadd_rn(1.0f, -q), op = __fadd_rn(1.0f, q);
+    const float shp = copysignf(__fmaf_rn(om, chr, __fmul_rn(op, shr)), dy);
+    const float chp = __fmaf_rn(op, chr, __fmul_rn(om, shr));
+    const float snp = __fmul_rn(sn, sc), csp = __fmul_rn(cs, sc);
+    const float den = __fmaf_rn(shp, shp, __fmaf_rn(snp, snp, 7.888609052210118e-31f));  // + 2^-100
+    const float w = __fmul_rn(r.b.x, rcp_approx(den));
+    acc[0] = __fmaf_rn(-__fmul_rn(w, shp), chp, acc[0]);
+    acc[1] = __fmaf_rn(__fmul_rn(w, snp), csp, acc[1]);
+  }
+};
+
 // ============================================================ stream functions (FP32C)
 // Both stream functions (stream_rel.cuh) sum S_j ln(q_ij) with ln from ln_q2, accurate to
 // about 1 ulp.  A pair with d = 0 (the self pair) is skipped by giving it q = 1, as the

@@ -162,6 +162,27 @@ __global__ void __launch_bounds__(1024) stream_totals_kernel(const double* qr, c
   }
 }
 
+__global__ void prep_beta32_kernel(const double* x, const double* y, const double* zeta, const double* area,
+                                   const int32_t* idx, int64_t ns, int64_t npad, BetaF32::Rec* out) {
+  const int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= npad) return;
+  BetaF32::Rec r;
+  if (k < ns) {
+    const int64_t j = idx[k];
+    float h, l;
+    split2(x[j], h, l);
+    r.a.x = h;
+    r.a.z = l;
+    split2(y[j], h, l);
+    r.a.y = h;
+    r.a.w = l;
+    r.b = make_float4(__double2float_rn(0.5 * zeta[j] * area[j]), 0.f, 0.f, 0.f);
+  } else {
+    r.a = r.b = make_float4(0.f, 0.f, 0.f, 0.f);  // zero strength
+  }
+  out[k] = r;
+}
+
 // ------------------------------------------------------------------ finish kernels
 // Fixed-order FP64 reduction over the split-K chunks, then the per-target epilogue.
 
@@ -259,7 +280,8 @@ size_t rec_bytes(int kind, int mode) {
     if (kind == kSumPseDiv || kind == kSumPsePlaneSecond || kind == kSumPsePlaneDdot || kind == kSumPseSphereDdot ||
         kind == kSumSwePlane || kind == kSumSweSphere)
       return sizeof(RecVec64);
-    if (kind == kSumSphereStream || kind == kSumPlaneStream) return sizeof(RecStream64);
+    if (kind == kSumSphereStream || kind == kSumPlaneStream || kind == kSumBetaPlane || kind == kSumBetaStream)
+      return sizeof(RecStream64);
     return sizeof(Rec64);
   }
   switch (kind) {
@@ -272,6 +294,8 @@ size_t rec_bytes(int kind, int mode) {
       return sizeof(StreamRel::Rec);
     case kSumPlaneStream:
       return sizeof(PlaneRel::Rec);
+    case kSumBetaPlane:
+      return sizeof(BetaF32::Rec);
     case kSumPseK8Geo:
     case kSumPseGaussChord:
     case kSumPseGrad:
@@ -289,6 +313,7 @@ int comps_of(int kind) {
       return 3;
     case kSumPlane:
     case kSumSphereStream:
+    case kSumBetaPlane:
       return 2;
     case kSumPseGrad:
       return 3;
@@ -637,6 +662,22 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
         }
         break;
       }
+      case kSumBetaPlane:
+      case kSumBetaStream: {
+        prep_stream64_kernel<<<prep_grid_ns, pb, 0, job.stream>>>(job.x, job.y, nullptr, job.s1, job.s2,
+                                                                  job.area, job.src_idx, job.ns,
+                                                                  static_cast<RecStream64*>(job.src_buf));
+        BetaF64Params p{job.x, job.y, 2.0 * kPi, 4.0 * kPi, job.out0, job.out1};
+        const RecStream64* src = static_cast<const RecStream64*>(job.src_buf);
+        if (job.kind == kSumBetaPlane) {
+          seq_fp64_kernel<BetaVelF64, RecStream64><<<g, k64Threads, 0, job.stream>>>(p, src, job.ns, job.ib, job.nt,
+                                                                                    job.status);
+        } else {
+          seq_fp64_kernel<BetaStreamF64, RecStream64><<<g, k64Threads, 0, job.stream>>>(p, src, job.ns, job.ib,
+                                                                                       job.nt, job.status);
+        }
+        break;
+      }
       default:
         return set_error(LPM_ERR_ARG, "unknown sum kind %d", job.kind);
     }
@@ -820,6 +861,14 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
           <<<grid, kStreamThreads, 0, job.stream>>>(a);
       finish_stream_kernel<<<fin_grid, pb, 0, job.stream>>>(job.partial, plan.nsplit, job.nt, 1, 0.0, nullptr, nullptr,
                                                             job.out0, nullptr);
+      break;
+    }
+    case kSumBetaPlane: {
+      prep_beta32_kernel<<<prep_grid_pad, pb, 0, job.stream>>>(job.x, job.y, job.s1, job.area, job.src_idx, job.ns,
+                                                               npad, static_cast<BetaF32::Rec*>(job.src_buf));
+      launch_sweep<BetaF32, kPseThreads, kPseTpt, kPseTile, kPseMinB>(job, plan, BetaF32::Params{job.x, job.y});
+      finish_stream_kernel<<<fin_grid, pb, 0, job.stream>>>(job.partial, plan.nsplit, job.nt, 2, 0.0, nullptr, nullptr,
+                                                            job.out0, job.out1);
       break;
     }
     default:
@@ -1272,4 +1321,24 @@ extern "C" int lpm_swe_sphere_rhs_integrals(int64_t n, const double* x, const do
   LPM_TRY(lpm::run_host(a, 4));
   for (int64_t i = i_begin - 1; i < i_end; ++i) double_dot[i] = 0.0;  // never set by the reference
   return LPM_OK;
+}
+
+extern "C" int lpm_beta_plane_velocity(int64_t n, const double* x, const double* y, const double* zeta,
+                                       const double* area, const int32_t* active, int64_t i_begin, int64_t i_end,
+                                       double* u, double* v, int mode) {
+  HostArgs a{lpm::kSumBetaPlane, n, x, y, nullptr, zeta, nullptr, area, active, 1.0, 0.0, 0.0, i_begin, i_end, u, v,
+             nullptr, mode};
+  LPM_TRY(lpm::check_common(a, 2));
+  return lpm::run_host(a, 2);
+}
+
+extern "C" int lpm_beta_plane_stream_functions(int64_t n, const double* x, const double* y, const double* relvort,
+                                               const double* absvort, const double* area, const int32_t* active,
+                                               int64_t i_begin, int64_t i_end, double* psi_rel, double* psi_abs,
+                                               int mode) {
+  HostArgs a{lpm::kSumBetaStream, n, x, y, nullptr, relvort, absvort, area, active, 1.0, 0.0, 0.0, i_begin, i_end,
+             psi_rel, psi_abs, nullptr, mode};
+  LPM_TRY(lpm::check_common(a, 2));
+  if (!absvort) return lpm::set_error(LPM_ERR_ARG, "null absolute vorticity array");
+  return lpm::run_host(a, 2);
 }

@@ -36,11 +36,15 @@ enum SumKind : int {
   kSumPseInterpPlane,   // PSE interpolation at query points, chord distance (FP64)
   kSumPseInterpSphere,  // PSE interpolation at query points, great-circle distance (FP64)
   kSumSwePlane,         // planar SWE right-hand-side integrals (FP64)
-  kSumSweSphere         // sphere SWE right-hand-side integrals (FP64)
+  kSumSweSphere,        // sphere SWE right-hand-side integrals (FP64)
+  kSumBetaPlane,        // beta-plane (x-periodic) velocity
+  kSumBetaStream        // beta-plane stream functions (FP64)
 };
 
 // Kinds that have only the FP64 form.
-inline bool sum_is_fp64_only(int kind) { return kind >= kSumPsePlaneGrad && kind <= kSumSweSphere; }
+inline bool sum_is_fp64_only(int kind) {
+  return (kind >= kSumPsePlaneGrad && kind <= kSumSweSphere) || kind == kSumBetaStream;
+}
 
 // Inputs of one direct sum over particles [0, n): sources are the ns particles listed (in
 // ascending order) by src_idx; targets are particles ib .. ib+nt-1.

@@ -25,6 +25,7 @@ public :: lpm_pse_sphere_gradient, lpm_pse_sphere_divergence
 public :: lpm_pse_plane_gradient, lpm_pse_plane_second_partials, lpm_pse_plane_double_dot
 public :: lpm_pse_sphere_double_dot, lpm_pse_interpolate_scalar
 public :: lpm_swe_plane_rhs_integrals, lpm_swe_sphere_rhs_integrals
+public :: lpm_beta_plane_velocity, lpm_beta_plane_stream_functions
 public :: lpm_bve_solver_create, lpm_bve_timestep, lpm_bve_get_state, lpm_bve_set_state
 public :: lpm_bve_diagnostics, lpm_bve_solver_stream_functions, lpm_bve_solver_destroy
 public :: lpm_plane_solver_create, lpm_plane_timestep, lpm_plane_get_state, lpm_plane_diagnostics
@@ -232,6 +233,28 @@ interface
 		real(c_double), value :: radius, sphere_radius, eps
 		integer(c_int64_t), value :: i_begin, i_end
 		real(c_double), intent(inout) :: u(*), v(*), w(*), double_dot(*), lap_surf(*)
+		integer(c_int), value :: mode
+	end function
+
+	integer(c_int) function lpm_beta_plane_velocity(n, x, y, zeta, area, active, i_begin, i_end, u, v, mode) &
+			bind(C, name="lpm_beta_plane_velocity")
+		import :: c_int, c_int32_t, c_int64_t, c_double
+		integer(c_int64_t), value :: n
+		real(c_double), intent(in) :: x(*), y(*), zeta(*), area(*)
+		integer(c_int32_t), intent(in) :: active(*)
+		integer(c_int64_t), value :: i_begin, i_end
+		real(c_double), intent(inout) :: u(*), v(*)
+		integer(c_int), value :: mode
+	end function
+
+	integer(c_int) function lpm_beta_plane_stream_functions(n, x, y, relvort, absvort, area, active, i_begin, &
+			i_end, psi_rel, psi_abs, mode) bind(C, name="lpm_beta_plane_stream_functions")
+		import :: c_int, c_int32_t, c_int64_t, c_double
+		integer(c_int64_t), value :: n
+		real(c_double), intent(in) :: x(*), y(*), relvort(*), absvort(*), area(*)
+		integer(c_int32_t), intent(in) :: active(*)
+		integer(c_int64_t), value :: i_begin, i_end
+		real(c_double), intent(inout) :: psi_rel(*), psi_abs(*)
 		integer(c_int), value :: mode
 	end function
 

@@ -69,6 +69,8 @@ _SIGNATURES = {
     "lpm_pse_sphere_gradient": [_i64, _D, _D, _D, _D, _D, _I, _dbl, _dbl, _i64, _i64, _D, _D, _D, _int],
     "lpm_pse_sphere_divergence": [_i64, _D, _D, _D, _D, _D, _D, _D, _I, _dbl, _dbl, _i64, _i64, _D, _int],
     "lpm_plane_stream_function": [_i64, _D, _D, _D, _D, _I, _i64, _i64, _D, _int],
+    "lpm_beta_plane_velocity": [_i64, _D, _D, _D, _D, _I, _i64, _i64, _D, _D, _int],
+    "lpm_beta_plane_stream_functions": [_i64, _D, _D, _D, _D, _D, _I, _i64, _i64, _D, _D, _int],
     "lpm_pse_plane_gradient": [_i64, _D, _D, _D, _D, _I, _dbl, _i64, _i64, _D, _D, _int],
     "lpm_pse_plane_second_partials": [_i64, _D, _D, _D, _D, _D, _I, _dbl, _i64, _i64, _D, _D, _D, _int],
     "lpm_pse_plane_double_dot": [_i64, _D, _D, _D, _D, _D, _I, _dbl, _i64, _i64, _D, _int],
@@ -276,6 +278,30 @@ def pse_sphere_divergence_at_particles(x, y, z, vx, vy, vz, area, active_mask, e
     _check(lib().lpm_pse_sphere_divergence(n, _dp(x), _dp(y), _dp(z), _dp(vx), _dp(vy), _dp(vz), _dp(area),
                                            _ip(act), float(eps), float(sphere_radius), ib, ie, _dp(d), _mode(mode)))
     return d
+
+
+def beta_plane_velocity(x, y, rel_vort, area, active_mask, i_begin=None, i_end=None, mode="fp64"):
+    """BetaPlaneVelocity (src/BetaPlaneSolver.f90:227), the x-periodic sum.  Returns (u, v)."""
+    x, y, rel_vort, area = (_f64(a) for a in (x, y, rel_vort, area))
+    act = _i32(active_mask)
+    n = x.size
+    ib, ie = _range(n, i_begin, i_end)
+    u, v = np.zeros(n), np.zeros(n)
+    _check(lib().lpm_beta_plane_velocity(n, _dp(x), _dp(y), _dp(rel_vort), _dp(area), _ip(act), ib, ie, _dp(u),
+                                         _dp(v), _mode(mode)))
+    return u, v
+
+
+def beta_plane_stream_functions(x, y, rel_vort, abs_vort, area, active_mask, i_begin=None, i_end=None, mode="fp64"):
+    """The beta plane's SetStreamFunctionsOnMesh (src/BetaPlane.f90:399).  Returns (psi_rel, psi_abs)."""
+    x, y, rel_vort, abs_vort, area = (_f64(a) for a in (x, y, rel_vort, abs_vort, area))
+    act = _i32(active_mask)
+    n = x.size
+    ib, ie = _range(n, i_begin, i_end)
+    pr, pa = np.zeros(n), np.zeros(n)
+    _check(lib().lpm_beta_plane_stream_functions(n, _dp(x), _dp(y), _dp(rel_vort), _dp(abs_vort), _dp(area),
+                                                 _ip(act), ib, ie, _dp(pr), _dp(pa), _mode(mode)))
+    return pr, pa
 
 
 def pse_plane_gradient_at_particles(x, y, f, area, active_mask, eps, i_begin=None, i_end=None, mode="fp64"):

@@ -116,6 +116,17 @@ def config_colliding_dipoles(nest: int = 7, mesh_radius: float = 4.0):
     return dict(mesh=m, x=m.x, y=m.y, omega=w, area=m.area, active=m.active)
 
 
+def config_beta_plane(nest: int = 7):
+    """The beta plane's particle set: the quad refinement on the box [0, 1] x [-1/2, 1/2]
+    (src/PolyMesh2d.f90:880-884 maps the seed x -> x/2 + 1/2, y -> y/2), with a Rossby-wave
+    vorticity sin(2 pi x) exp(-8 y^2) plus a zonal jet 0.5 tanh(10 y)."""
+    m = lg.PolyMesh2d(lg.QUAD_RECT_SEED, nest, 1.0)
+    x = 0.5 * m.x + 0.5
+    y = 0.5 * m.y
+    zeta = np.sin(2.0 * PI * x) * np.exp(-8.0 * y * y) + 0.5 * np.tanh(10.0 * y)
+    return dict(x=x, y=y, zeta=zeta, area=0.25 * m.area, active=m.active)
+
+
 def config_pse_cubed(nest: int = 7, seed: int = 0):
     m = sphere_mesh(lg.CUBED_SPHERE_SEED, nest)
     rng = np.random.default_rng(seed)

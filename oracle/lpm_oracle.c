@@ -681,3 +681,54 @@ void lpmo_swe_sphere_rhs(int64_t n, const double* x, const double* y, const doub
     ddot[i] = 0.0;
   }
 }
+
+/*
+ * BetaPlaneVelocity, src/BetaPlaneSolver.f90:227-268 (and the same sum in
+ * setVelocityFromVorticity, src/BetaPlane.f90:359-397): the x-periodic (period 1) point-vortex
+ * kernel.  Per active j != i, in ascending j:
+ *   strength = 0.5 zeta_j A_j / (cosh(2 pi dy) - cos(2 pi dx)),
+ *   u -= sinh(2 pi dy) strength,  v += sin(2 pi dx) strength,   dx = x_i - x_j, dy = y_i - y_j.
+ */
+void lpmo_beta_plane_velocity(int64_t n, const double* x, const double* y, const double* zeta,
+                              const double* area, const int32_t* active, int64_t ib, int64_t ie, double* u,
+                              double* v, int nthreads)
+{
+  const double two_pi = 2.0 * PI;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(pick_threads(nthreads))
+  for (int64_t i = ib; i < ie; ++i) {
+    double ui = 0.0, vi = 0.0;
+    for (int64_t j = 0; j < n; ++j) {
+      if (j == i || !active[j]) continue;
+      const double ay = two_pi * (y[i] - y[j]), ax = two_pi * (x[i] - x[j]);
+      const double s = ((0.5 * zeta[j]) * area[j]) / (cosh(ay) - cos(ax));
+      ui = ui - sinh(ay) * s;
+      vi = vi + sin(ax) * s;
+    }
+    u[i] = ui;
+    v[i] = vi;
+  }
+}
+
+/*
+ * SetStreamFunctionsOnMesh of the beta plane, src/BetaPlane.f90:399-442:
+ *   G = log(cosh(2 pi dy) - cos(2 pi dx)) / (4 pi),  psi_rel += G zeta_rel_j A_j,
+ *   psi_abs += G zeta_abs_j A_j,  j != i, active.
+ */
+void lpmo_beta_plane_stream(int64_t n, const double* x, const double* y, const double* relvort,
+                            const double* absvort, const double* area, const int32_t* active, int64_t ib,
+                            int64_t ie, double* psi_rel, double* psi_abs, int nthreads)
+{
+  const double two_pi = 2.0 * PI, four_pi = 4.0 * PI;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(pick_threads(nthreads))
+  for (int64_t i = ib; i < ie; ++i) {
+    double pr = 0.0, pa = 0.0;
+    for (int64_t j = 0; j < n; ++j) {
+      if (j == i || !active[j]) continue;
+      const double g = log(cosh(two_pi * (y[i] - y[j])) - cos(two_pi * (x[i] - x[j]))) / four_pi;
+      pr = pr + (g * relvort[j]) * area[j];
+      pa = pa + (g * absvort[j]) * area[j];
+    }
+    psi_rel[i] = pr;
+    psi_abs[i] = pa;
+  }
+}

@@ -134,6 +134,16 @@ void lpmo_swe_sphere_rhs(int64_t n, const double* x, const double* y, const doub
                          double radius, double sphere_radius, double eps, int64_t ib, int64_t ie, double* u,
                          double* v, double* w, double* ddot, double* lap, int nthreads);
 
+/* BetaPlaneVelocity, BetaPlaneSolver.f90:227-268 (x-periodic kernel, period 1) */
+void lpmo_beta_plane_velocity(int64_t n, const double* x, const double* y, const double* zeta,
+                              const double* area, const int32_t* active, int64_t ib, int64_t ie, double* u,
+                              double* v, int nthreads);
+
+/* SetStreamFunctionsOnMesh of the beta plane, BetaPlane.f90:399-442 */
+void lpmo_beta_plane_stream(int64_t n, const double* x, const double* y, const double* relvort,
+                            const double* absvort, const double* area, const int32_t* active, int64_t ib,
+                            int64_t ie, double* psi_rel, double* psi_abs, int nthreads);
+
 #ifdef __cplusplus
 }
 #endif

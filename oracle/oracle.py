@@ -60,6 +60,8 @@ def lib():
         L.lpmo_swe_plane_rhs.argtypes = [_i64, _D, _D, _D, _D, _D, _D, _I, c_d, _i64, _i64, _D, _D, _D, _D, c_i]
         L.lpmo_swe_sphere_rhs.argtypes = [_i64, _D, _D, _D, _D, _D, _D, _D, _I, c_d, c_d, c_d, _i64, _i64, _D, _D,
                                           _D, _D, _D, c_i]
+        L.lpmo_beta_plane_velocity.argtypes = [_i64, _D, _D, _D, _D, _I, _i64, _i64, _D, _D, c_i]
+        L.lpmo_beta_plane_stream.argtypes = [_i64, _D, _D, _D, _D, _D, _I, _i64, _i64, _D, _D, c_i]
         L.lpmo_kdelta8.argtypes = [ctypes.c_double]
         L.lpmo_kdelta8.restype = ctypes.c_double
         L.lpmo_k8.argtypes = [ctypes.c_double]
@@ -232,6 +234,29 @@ def swe_sphere_rhs(x, y, z, relvort, div, sh, area, active, radius, sphere_radiu
                               active.ctypes.data_as(_I), radius, sphere_radius, eps, ib, ie, _d(o[0]), _d(o[1]),
                               _d(o[2]), _d(o[3]), _d(o[4]), threads)
     return tuple(a[ib:ie] for a in o)
+
+
+def beta_plane_velocity(x, y, zeta, area, active, ib=None, ie=None, threads=0):
+    """BetaPlaneVelocity (src/BetaPlaneSolver.f90:227-268); returns (u, v) of the block."""
+    x, y, zeta, area, active = _f64(x), _f64(y), _f64(zeta), _f64(area), _i32(active)
+    n = x.size
+    ib, ie = _range(n, ib, ie)
+    u, v = np.zeros(n), np.zeros(n)
+    lib().lpmo_beta_plane_velocity(n, _d(x), _d(y), _d(zeta), _d(area), active.ctypes.data_as(_I), ib, ie, _d(u),
+                                   _d(v), threads)
+    return u[ib:ie], v[ib:ie]
+
+
+def beta_plane_stream(x, y, relvort, absvort, area, active, ib=None, ie=None, threads=0):
+    """SetStreamFunctionsOnMesh of the beta plane (src/BetaPlane.f90:399-442); returns (psi_rel, psi_abs)."""
+    x, y, relvort, absvort, area, active = (_f64(x), _f64(y), _f64(relvort), _f64(absvort), _f64(area),
+                                            _i32(active))
+    n = x.size
+    ib, ie = _range(n, ib, ie)
+    pr, pa = np.zeros(n), np.zeros(n)
+    lib().lpmo_beta_plane_stream(n, _d(x), _d(y), _d(relvort), _d(absvort), _d(area), active.ctypes.data_as(_I), ib,
+                                 ie, _d(pr), _d(pa), threads)
+    return pr[ib:ie], pa[ib:ie]
 
 
 def kdelta8(r):

@@ -112,3 +112,72 @@ def test_swe_sphere_rhs(lg, oracle_mod, radius, sphere_radius):
         assert np.array_equal(got[c][s], ref[c])
     assert np.all(got[3][s] == 0.0)
     assert rel(got[4][s], ref[4]) <= TOL
+
+
+@pytest.mark.parametrize("n,frac,block", [(1000, 0.8, None), (4099, 1.0, (33, 4000))])
+def test_beta_plane_velocity_and_stream(lg, oracle_mod, n, frac, block):
+    rng = np.random.default_rng(n)
+    x, y = rng.random(n), rng.uniform(-0.5, 0.5, n)
+    area = rng.uniform(0.5, 1.5, n) / n
+    zeta = np.sin(2 * np.pi * x) * np.exp(-8 * y * y)
+    absv = zeta + 3.0 * y
+    act = (rng.random(n) < frac).astype(np.int32)
+    ib, ie = (1, n) if block is None else block
+    # The reference's denominator cosh(2 pi dy) - cos(2 pi dx) cancels for close pairs: an ulp
+    # of difference between CUDA's and the C library's cosh/cos (about 1e-16 of 1) becomes
+    # 1e-16 / (2 pi^2 r^2) of that pair's term, ~1e-11 for the closest random pairs here.
+    tol = 1e-9
+    u, v = lg.beta_plane_velocity(x, y, zeta, area, act, ib, ie)
+    ru, rv = oracle_mod.beta_plane_velocity(x, y, zeta, area, act, ib - 1, ie)
+    s = slice(ib - 1, ie)
+    assert rel(u[s], ru) <= tol and rel(v[s], rv) <= tol
+    pr, pa = lg.beta_plane_stream_functions(x, y, zeta, absv, area, act, ib, ie)
+    rr, ra = oracle_mod.beta_plane_stream(x, y, zeta, absv, area, act, ib - 1, ie)
+    assert rel(pr[s], rr) <= tol and rel(pa[s], ra) <= tol
+
+
+def test_beta_plane_band_known_answer_gpu(lg):
+    nx = ny = 64
+    xs = (np.arange(nx) + 0.5) / nx
+    ys = -0.5 + (np.arange(ny) + 0.5) / ny
+    X, Y = (a.ravel() for a in np.meshgrid(xs, ys))
+    A = np.full(X.size, 1.0 / (nx * ny))
+    Z = np.where(np.abs(Y) < 0.25, 1.0, 0.0)
+    u, v = lg.beta_plane_velocity(X, Y, Z, A, np.ones(X.size, dtype=np.int32))
+    assert np.abs(u + Y)[np.abs(Y) < 0.2].max() < 1e-11 and np.abs(v).max() < 1e-12
+
+
+FP32C_TOL = 1e-6
+
+
+@pytest.mark.parametrize("n,frac,block,spread", [(1000, 0.8, None, 0.5), (5003, 1.0, (7, 4900), 0.5),
+                                                 (3000, 0.9, None, 3.0)])
+def test_beta_plane_velocity_fp32c(lg, oracle_mod, n, frac, block, spread):
+    """FP32C against the oracle: random particles on the strip (y up to +-spread, so sinh/cosh
+    reach e^(2 pi spread)), a cluster straddling the periodic boundary x = 0 ~ 1, positions
+    shifted by whole periods (x outside [0, 1])."""
+    rng = np.random.default_rng(n + 1)
+    x, y = rng.random(n), rng.uniform(-spread, spread, n)
+    x[:50] = np.mod(rng.normal(0.0, 1e-3, 50), 1.0)  # neighbours across x = 0 / 1
+    y[:50] = rng.normal(0.0, 1e-3, 50)
+    x[50:80] += rng.integers(-3, 4, 30)  # whole periods
+    area = rng.uniform(0.5, 1.5, n) / n
+    zeta = np.sin(2 * np.pi * x) * np.exp(-4 * y * y) + 0.3
+    act = (rng.random(n) < frac).astype(np.int32)
+    ib, ie = (1, n) if block is None else block
+    s = slice(ib - 1, ie)
+    u, v = lg.beta_plane_velocity(x, y, zeta, area, act, ib, ie, mode="fp32c")
+    ru, rv = oracle_mod.beta_plane_velocity(x, y, zeta, area, act, ib - 1, ie)
+    scale = max(np.abs(ru).max(), np.abs(rv).max())
+    assert max(np.abs(u[s] - ru).max(), np.abs(v[s] - rv).max()) <= FP32C_TOL * scale
+
+
+def test_beta_plane_band_fp32c(lg):
+    nx = ny = 128
+    xs = (np.arange(nx) + 0.5) / nx
+    ys = -0.5 + (np.arange(ny) + 0.5) / ny
+    X, Y = (a.ravel() for a in np.meshgrid(xs, ys))
+    A = np.full(X.size, 1.0 / (nx * ny))
+    Z = np.where(np.abs(Y) < 0.25, 1.0, 0.0)
+    u, v = lg.beta_plane_velocity(X, Y, Z, A, np.ones(X.size, dtype=np.int32), mode="fp32c")
+    assert np.abs(u + Y)[np.abs(Y) < 0.2].max() < FP32C_TOL * 0.25 and np.abs(v).max() < FP32C_TOL * 0.25

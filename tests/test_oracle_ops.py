@@ -203,3 +203,39 @@ def test_fp32c_rejected_for_fp64_only_operators(lg, call):
     with pytest.raises(lg.LpmError) as e:
         fn()
     assert "FP64" in str(e.value)
+
+
+def _band(nx=64, ny=64, b=0.25):
+    xs = (np.arange(nx) + 0.5) / nx
+    ys = -0.5 + (np.arange(ny) + 0.5) / ny
+    X, Y = np.meshgrid(xs, ys)
+    X, Y = X.ravel(), Y.ravel()
+    return X, Y, np.full(X.size, 1.0 / (nx * ny)), np.where(np.abs(Y) < b, 1.0, 0.0)
+
+
+def test_beta_plane_band_known_answer(oracle_mod):
+    """A band of uniform vorticity |y| < b on the periodic strip is a pair of vortex sheets:
+    u = -zeta y inside, -+zeta b outside, v = 0 (the x-integral of the periodic kernel is
+    1/sinh|2 pi dy|, and a midpoint grid sums it exactly)."""
+    X, Y, A, Z = _band()
+    u, v = oracle_mod.beta_plane_velocity(X, Y, Z, A, np.ones(X.size, dtype=np.int32))
+    inside, outside = np.abs(Y) < 0.2, np.abs(Y) > 0.3
+    assert np.abs(u + Y)[inside].max() < 1e-11
+    assert np.abs(np.abs(u) - 0.25)[outside].max() < 1e-11
+    assert np.abs(v).max() < 1e-12
+
+
+def test_beta_plane_stream_vs_numpy(oracle_mod):
+    rng = np.random.default_rng(8)
+    n = 300
+    x, y = rng.random(n), rng.uniform(-0.5, 0.5, n)
+    a = rng.uniform(0.5, 1.5, n) / n
+    zr, za = rng.standard_normal(n), rng.standard_normal(n)
+    act = (rng.random(n) < 0.8).astype(np.int32)
+    pr, pa = oracle_mod.beta_plane_stream(x, y, zr, za, a, act)
+    j = act == 1
+    for i in (0, 17, 299):
+        m = j & (np.arange(n) != i)
+        g = np.log(np.cosh(2 * np.pi * (y[i] - y[m])) - np.cos(2 * np.pi * (x[i] - x[m]))) / (4 * np.pi)
+        assert abs(pr[i] - (g * zr[m] * a[m]).sum()) <= 1e-12 * np.abs(g * zr[m] * a[m]).sum()
+        assert abs(pa[i] - (g * za[m] * a[m]).sum()) <= 1e-12 * np.abs(g * za[m] * a[m]).sum()
