@@ -241,6 +241,18 @@ int lpm_bve_get_state(lpm_bve_solver* solver, double* x, double* y, double* z,
 int lpm_bve_set_state(lpm_bve_solver* solver, const double* x, const double* y,
                       const double* z, const double* relvort, const double* u,
                       const double* v, const double* w);
+/* Replaces the Delete(solver) + New(solver, sphere) pair that follows a remesh
+ * (examples/BVESingleGaussianVortex.f90:241-245, src/SphereBVESolver.f90:112-168): loads a
+ * new particle set (n may change, and the active mask with it) into the existing solver.
+ * The device buffers are reused when the new set fits them and grown with 1/8 headroom
+ * when it does not, so a run that remeshes every few steps does not reallocate; the step
+ * graph is re-captured at the next lpm_bve_timestep.  u, v, w as for lpm_bve_solver_create
+ * (NULL: the velocity is computed from the vorticity).  The state is then identical to a
+ * newly created solver's. */
+int lpm_bve_solver_remesh(lpm_bve_solver* solver, int64_t n, const double* x, const double* y,
+                          const double* z, const double* relvort, const double* area,
+                          const int32_t* active, const double* u, const double* v,
+                          const double* w);
 /* KE = 1/2 sum |u|^2 A, enstrophy = 1/2 sum zeta^2 A, circulation = sum zeta A over
  * active particles (src/SphereBVE.f90:410-441). */
 int lpm_bve_diagnostics(lpm_bve_solver* solver, double* kinetic_energy, double* enstrophy,

@@ -212,6 +212,17 @@ int DeviceArena::alloc(size_t bytes, void** p) {
   return LPM_OK;
 }
 
+void DeviceArena::free(void* p) {
+  if (!p) return;
+  for (size_t i = 0; i < ptrs.size(); ++i) {
+    if (ptrs[i] == p) {
+      cudaFree(p);
+      ptrs.erase(ptrs.begin() + static_cast<std::ptrdiff_t>(i));
+      return;
+    }
+  }
+}
+
 void DeviceArena::release() {
   for (void* p : ptrs) cudaFree(p);
   ptrs.clear();
@@ -221,10 +232,33 @@ int SumScratch::init(DeviceArena& arena, int kind, int mode, int64_t ns, int64_t
   // sized for every sweep shape, so the autotuner can time them all in this scratch
   plan = plan_sum_max(kind, mode, ns, nt, sm_count);
   LPM_TRY(arena.alloc(plan.src_bytes, &src_buf));
+  src_cap = plan.src_bytes;
   if (plan.partial_bytes) {
     void* p = nullptr;
     LPM_TRY(arena.alloc(plan.partial_bytes, &p));
     partial = static_cast<double*>(p);
+  }
+  partial_cap = plan.partial_bytes;
+  return LPM_OK;
+}
+
+int SumScratch::fit(DeviceArena& arena, int kind, int mode, int64_t ns, int64_t nt, int sm_count) {
+  plan = plan_sum_max(kind, mode, ns, nt, sm_count);
+  if (plan.src_bytes > src_cap) {
+    arena.free(src_buf);
+    src_buf = nullptr;
+    src_cap = 0;
+    LPM_TRY(arena.alloc(plan.src_bytes, &src_buf));
+    src_cap = plan.src_bytes;
+  }
+  if (plan.partial_bytes > partial_cap) {
+    arena.free(partial);
+    partial = nullptr;
+    partial_cap = 0;
+    void* p = nullptr;
+    LPM_TRY(arena.alloc(plan.partial_bytes, &p));
+    partial = static_cast<double*>(p);
+    partial_cap = plan.partial_bytes;
   }
   return LPM_OK;
 }
@@ -260,6 +294,7 @@ struct lpm_bve_solver {
   cudaStream_t own = nullptr;     // the solver's own stream (graphs are captured on it)
   DeviceArena arena;
   int64_t n = 0, ns = 0;
+  int64_t cap_n = 0, cap_ns = 0;  // particles and sources the buffers hold
   int mode = LPM_MODE_FP64;
   double radius = 1.0, omega = 0.0;
   double *x, *y, *z, *q, *u, *v, *w, *area;
@@ -421,27 +456,18 @@ int download(cudaStream_t s, double* h, const double* d, int64_t n) {
   return LPM_OK;
 }
 
-int bve_create(lpm_bve_solver* S, int64_t n, const double* x, const double* y, const double* z, const double* q,
-               const double* area, const int32_t* active, const double* u, const double* v, const double* w,
-               double radius, double omega, int mode) {
-  LPM_TRY(get_context(&S->ctx));
-  S->n = n;
-  S->mode = mode;
-  S->radius = radius;
-  S->omega = omega;
-  LPM_CUDA_TRY(cudaStreamCreateWithFlags(&S->own, cudaStreamNonBlocking));
-  S->stream = S->own;
+// Device buffers for up to ncap particles and nscap sources (everything but the pinned
+// status word, the events and the stream).
+int bve_alloc(lpm_bve_solver* S, int64_t ncap, int64_t nscap) {
   double** arrs[] = {&S->x, &S->y, &S->z, &S->q, &S->u, &S->v, &S->w, &S->area, &S->ax, &S->ay, &S->az,
                      &S->aq, &S->xin, &S->yin, &S->zin, &S->qin, &S->us, &S->vs, &S->ws};
   for (double** a : arrs) {
     void* p = nullptr;
-    LPM_TRY(S->arena.alloc(n * sizeof(double), &p));
+    LPM_TRY(S->arena.alloc(ncap * sizeof(double), &p));
     *a = static_cast<double*>(p);
   }
-  const std::vector<int32_t> idx = active_list(n, active);
-  S->ns = static_cast<int64_t>(idx.size());
   void* p = nullptr;
-  LPM_TRY(S->arena.alloc(idx.size() * sizeof(int32_t), &p));
+  LPM_TRY(S->arena.alloc((nscap > 0 ? nscap : 1) * sizeof(int32_t), &p));
   S->idx = static_cast<int32_t*>(p);
   LPM_TRY(S->arena.alloc(sizeof(int), &p));
   S->status = static_cast<int*>(p);
@@ -449,33 +475,49 @@ int bve_create(lpm_bve_solver* S, int64_t n, const double* x, const double* y, c
   S->diag_part = static_cast<double*>(p);
   LPM_TRY(S->arena.alloc(4 * sizeof(double), &p));
   S->diag_out = static_cast<double*>(p);
-  LPM_CUDA_TRY(cudaMallocHost(&S->h_status, sizeof(int)));
+  LPM_TRY(S->scratch.init(S->arena, kSumBve, S->mode, nscap, ncap, S->ctx->sm_count));
+  S->sort_scratch = nullptr;
+  S->sorted = nullptr;
+  S->sort_bytes = 0;
+  if (nscap > 0 && sum_uses_sorted_sources(kSumBve, S->mode)) {
+    S->sort_bytes = curve_sort_bytes(nscap);
+    void* sorted = nullptr;
+    LPM_TRY(S->arena.alloc(S->sort_bytes, &S->sort_scratch));
+    LPM_TRY(S->arena.alloc(nscap * sizeof(int32_t), &sorted));
+    S->sorted = static_cast<int32_t*>(sorted);
+  }
+  S->cap_n = ncap;
+  S->cap_ns = nscap;
+  return LPM_OK;
+}
+
+// Loads a particle set into buffers that hold it: uploads, source list, sweep plan (and the
+// FP32C source order and sweep shape), and the initial velocity when u, v, w are NULL.
+int bve_load(lpm_bve_solver* S, int64_t n, const std::vector<int32_t>& idx, const double* x, const double* y,
+             const double* z, const double* q, const double* area, const double* u, const double* v,
+             const double* w) {
+  S->n = n;
+  S->ns = static_cast<int64_t>(idx.size());
   LPM_CUDA_TRY(cudaMemsetAsync(S->status, 0, sizeof(int), S->stream));
   if (!idx.empty()) {
     LPM_CUDA_TRY(cudaMemcpyAsync(S->idx, idx.data(), idx.size() * sizeof(int32_t), cudaMemcpyHostToDevice, S->stream));
   }
-  LPM_TRY(S->scratch.init(S->arena, kSumBve, mode, S->ns, n, S->ctx->sm_count));
+  LPM_TRY(S->scratch.fit(S->arena, kSumBve, S->mode, S->ns, n, S->ctx->sm_count));
   LPM_TRY(upload(S->stream, S->x, x, n));
   LPM_TRY(upload(S->stream, S->y, y, n));
   LPM_TRY(upload(S->stream, S->z, z, n));
   LPM_TRY(upload(S->stream, S->q, q, n));
   LPM_TRY(upload(S->stream, S->area, area, n));
-  if (S->ns > 0 && sum_uses_sorted_sources(kSumBve, mode)) {
+  if (S->ns > 0 && S->sorted) {
     // FP32C: the sources are ordered spatially at the start of every step (inside the step's
     // graph), so tiles stay compact as the particles move; the order only affects rounding
-    S->sort_bytes = curve_sort_bytes(S->ns);
-    void* sorted = nullptr;
-    LPM_TRY(S->arena.alloc(S->sort_bytes, &S->sort_scratch));
-    LPM_TRY(S->arena.alloc(S->ns * sizeof(int32_t), &sorted));
-    S->sorted = static_cast<int32_t*>(sorted);
     LPM_TRY(S->sort_sources());
     // choose the sweep shape on this problem (the timing runs write into the stage buffers)
     int shape = 0;
     LPM_TRY(autotune_bve_shape(S->job(S->x, S->y, S->z, S->q, kSumBve, S->us, S->vs, S->ws), S->ctx->sm_count,
                                &shape));
-    S->scratch.plan = plan_sum(kSumBve, mode, S->ns, n, S->ctx->sm_count, shape);
+    S->scratch.plan = plan_sum(kSumBve, S->mode, S->ns, n, S->ctx->sm_count, shape);
   }
-  for (auto& e : S->ev) LPM_CUDA_TRY(cudaEventCreate(&e));
   if (u && v && w) {
     LPM_TRY(upload(S->stream, S->u, u, n));
     LPM_TRY(upload(S->stream, S->v, v, n));
@@ -484,6 +526,23 @@ int bve_create(lpm_bve_solver* S, int64_t n, const double* x, const double* y, c
     // SetVelocityOnMesh -> setVelocityFromVorticity (SphereBVE.f90:489-531)
     LPM_TRY(S->velocity(S->x, S->y, S->z, S->q, S->u, S->v, S->w, kSumBveMesh));
   }
+  return LPM_OK;
+}
+
+int bve_create(lpm_bve_solver* S, int64_t n, const double* x, const double* y, const double* z, const double* q,
+               const double* area, const int32_t* active, const double* u, const double* v, const double* w,
+               double radius, double omega, int mode) {
+  LPM_TRY(get_context(&S->ctx));
+  S->mode = mode;
+  S->radius = radius;
+  S->omega = omega;
+  LPM_CUDA_TRY(cudaStreamCreateWithFlags(&S->own, cudaStreamNonBlocking));
+  S->stream = S->own;
+  LPM_CUDA_TRY(cudaMallocHost(&S->h_status, sizeof(int)));
+  for (auto& e : S->ev) LPM_CUDA_TRY(cudaEventCreate(&e));
+  const std::vector<int32_t> idx = active_list(n, active);
+  LPM_TRY(bve_alloc(S, n, static_cast<int64_t>(idx.size())));
+  LPM_TRY(bve_load(S, n, idx, x, y, z, q, area, u, v, w));
   return S->check_status("lpm_bve_solver_create");
 }
 
@@ -558,6 +617,46 @@ extern "C" int lpm_bve_set_state(lpm_bve_solver* S, const double* x, const doubl
   LPM_TRY(upload(S->stream, S->v, v, S->n));
   LPM_TRY(upload(S->stream, S->w, w, S->n));
   return S->check_status("lpm_bve_set_state");
+}
+
+extern "C" int lpm_bve_solver_remesh(lpm_bve_solver* S, int64_t n, const double* x, const double* y, const double* z,
+                                     const double* relvort, const double* area, const int32_t* active, const double* u,
+                                     const double* v, const double* w) {
+  if (!S) return set_error(LPM_ERR_ARG, "null solver");
+  if (n <= 0) return set_error(LPM_ERR_ARG, "n must be positive");
+  if (!x || !y || !z || !relvort || !area || !active) return set_error(LPM_ERR_ARG, "null input array");
+  if ((u == nullptr) != (v == nullptr) || (u == nullptr) != (w == nullptr))
+    return set_error(LPM_ERR_ARG, "u, v, w must be all given or all NULL");
+  LPM_CUDA_TRY(cudaStreamSynchronize(S->stream));
+  // the step graph and the stream-function buffers are sized for the old particle set
+  if (S->exec) cudaGraphExecDestroy(S->exec);
+  if (S->graph) cudaGraphDestroy(S->graph);
+  S->exec = nullptr;
+  S->graph = nullptr;
+  const std::vector<int32_t> idx = active_list(n, active);
+  const int64_t ns = static_cast<int64_t>(idx.size());
+  if (n > S->cap_n || ns > S->cap_ns) {
+    // grow with 1/8 headroom, so that the next remeshes of a similar size reuse the buffers
+    S->arena.release();
+    S->mask = nullptr;
+    S->absv = S->psi = nullptr;
+    S->stream_scratch = SumScratch();
+    S->scratch = SumScratch();
+    LPM_TRY(bve_alloc(S, n + n / 8, ns + ns / 8));
+  } else {
+    S->arena.free(S->mask);  // the diagnostics' mask of the old set
+    S->mask = nullptr;
+  }
+  if (S->psi) {
+    S->arena.free(S->absv);
+    S->arena.free(S->psi);
+    S->arena.free(S->stream_scratch.src_buf);
+    S->arena.free(S->stream_scratch.partial);
+    S->absv = S->psi = nullptr;
+    S->stream_scratch = SumScratch();
+  }
+  LPM_TRY(bve_load(S, n, idx, x, y, z, relvort, area, u, v, w));
+  return S->check_status("lpm_bve_solver_remesh");
 }
 
 namespace {

@@ -12,6 +12,7 @@ namespace lpm {
 struct DeviceArena {
   std::vector<void*> ptrs;
   int alloc(size_t bytes, void** p);
+  void free(void* p);  // one allocation (no-op for nullptr)
   void release();
 };
 
@@ -21,7 +22,11 @@ struct SumScratch {
   SumPlan plan;
   void* src_buf = nullptr;
   double* partial = nullptr;
+  size_t src_cap = 0, partial_cap = 0;  // allocated bytes
   int init(DeviceArena& arena, int kind, int mode, int64_t ns, int64_t nt, int sm_count);
+  // Makes the buffers hold plan_sum_max(kind, mode, ns, nt) (growing them if needed) and
+  // sets plan to it.
+  int fit(DeviceArena& arena, int kind, int mode, int64_t ns, int64_t nt, int sm_count);
 };
 
 // Number of kernel nodes in a captured graph: the kernels one replay launches.

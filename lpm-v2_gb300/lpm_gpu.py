@@ -83,6 +83,7 @@ _SIGNATURES = {
     "lpm_bve_timestep": [_vp, _dbl, _int, _int],
     "lpm_bve_get_state": [_vp, _D, _D, _D, _D, _D, _D, _D],
     "lpm_bve_set_state": [_vp, _D, _D, _D, _D, _D, _D, _D],
+    "lpm_bve_solver_remesh": [_vp, _i64, _D, _D, _D, _D, _D, _I, _D, _D, _D],
     "lpm_bve_diagnostics": [_vp, _D, _D, _D],
     "lpm_bve_kernel_timing": [_vp, _D, _L],
     "lpm_bve_solver_set_stream": [_vp, _vp],
@@ -458,6 +459,16 @@ class BVESolver:
     def set_state(self, x, y, z, rel_vort, u, v, w):
         arrs = [_f64(a) for a in (x, y, z, rel_vort, u, v, w)]
         _check(lib().lpm_bve_set_state(self._h, *(_dp(a) for a in arrs)))
+
+    def remesh(self, x, y, z, rel_vort, area, active_mask, u=None, v=None, w=None):
+        """Loads a remeshed particle set in place of Delete(solver) + New(solver, sphere)."""
+        arrs = [_f64(a) for a in (x, y, z, rel_vort, area)]
+        act = _i32(active_mask)
+        uvw = [None if a is None else _f64(a) for a in (u, v, w)]
+        _check(lib().lpm_bve_solver_remesh(self._h, arrs[0].size, *(_dp(a) for a in arrs), _ip(act),
+                                           *(_dp(a) for a in uvw)))
+        self.n = arrs[0].size
+        self._keep = arrs
 
     def diagnostics(self):
         ke, en, ci = _dbl(), _dbl(), _dbl()

@@ -163,3 +163,30 @@ def test_solver_stream_functions(lg, wl, mode):
     qr, qa = s.stream_functions()  # absolute vorticity from the state
     assert np.abs(qa - pa).max() <= 1e-9 * np.abs(pa).max() and np.array_equal(qr, pr)
     s.close()
+
+
+@pytest.mark.parametrize("mode", ["fp64", "fp32c"])
+def test_bve_remesh_in_place_matches_new_solver(lg, wl, mode):
+    """lpm_bve_solver_remesh in place of Delete(solver) + New(solver, sphere): after a remesh to
+    a larger set (the buffers grow), to a smaller one (they are reused), and with a velocity
+    given, the states, diagnostics and stream functions are those of a newly created solver."""
+    a, b, c = (wl.config_gauss_vortex_icos(k) for k in (3, 4, 2))
+    s = lg.BVESolver(a["x"], a["y"], a["z"], a["zeta"], a["area"], a["active"], 1.0, a["omega"], mode=mode)
+    s.timestep(0.01, 2)
+    for cfg, uvw in ((b, None), (c, None), (b, "given")):
+        kw = {}
+        if uvw:
+            kw = dict(zip("uvw", (-0.1 * cfg["y"], 0.1 * cfg["x"], 0.0 * cfg["z"])))  # tangent: solid body
+        s.remesh(cfg["x"], cfg["y"], cfg["z"], cfg["zeta"], cfg["area"], cfg["active"], **kw)
+        fresh = lg.BVESolver(cfg["x"], cfg["y"], cfg["z"], cfg["zeta"], cfg["area"], cfg["active"], 1.0,
+                             a["omega"], mode=mode, **kw)
+        s.timestep(0.01, 3)
+        fresh.timestep(0.01, 3)
+        st, sf = s.get_state(), fresh.get_state()
+        for k in st:
+            assert np.array_equal(st[k], sf[k]), k
+        assert s.diagnostics() == fresh.diagnostics()
+        p1, p2 = s.stream_functions(), fresh.stream_functions()
+        assert np.array_equal(p1[0], p2[0]) and np.array_equal(p1[1], p2[1])
+        fresh.close()
+    s.close()
