@@ -68,7 +68,7 @@ def parse_args():
                    help="rk4: the headline single-instance step; ensemble: the 64-instance batch")
     p.add_argument("--instances", type=int, default=64)
     p.add_argument("--sum", choices=["bve", "plane", "pse_k8", "pse_gauss", "pse_grad", "pse_div", "pse_plane",
-                                     "stream", "plane_stream", "beta"],
+                                     "stream", "plane_stream", "beta", "swe_plane"],
                    default="bve",
                    help="--workload sum: which direct sum (one host C-ABI call per step)")
     p.add_argument("--mode", choices=["fp32c", "fp64"], default="fp32c", help="--workload sum: precision mode")
@@ -619,6 +619,15 @@ def run_sum(args):
         call = lambda ie: lg.set_stream_function_on_mesh(c["x"], c["y"], c["omega"], c["area"], c["active"],
                                                          i_end=ie, mode=args.mode)
         mesh = f"quad nest {args.nest} on [-4,4]^2"
+    elif args.sum == "swe_plane":
+        c = wl.config_colliding_dipoles(args.nest)
+        n, ns = c["x"].size, int(c["active"].sum())
+        div = 0.2 * c["omega"] * np.exp(-(c["x"] ** 2))
+        sh = 1.0 + 0.1 * np.cos(c["x"]) * np.sin(c["y"])
+        eps = 2.0 * float(np.sqrt(c["area"][c["active"] == 1].max()))
+        call = lambda ie: lg.swe_plane_rhs_integrals(c["x"], c["y"], c["omega"], div, sh, c["area"], c["active"],
+                                                     eps, i_end=ie, mode=args.mode)
+        mesh = f"quad nest {args.nest} on [-4,4]^2 (SWE velocity, double dot and surface Laplacian, eps = 2h)"
     elif args.sum == "beta":
         c = wl.config_beta_plane(args.nest)
         n, ns = c["x"].size, int(c["active"].sum())

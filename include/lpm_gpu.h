@@ -121,8 +121,9 @@ int lpm_pse_sphere_divergence(int64_t n, const double* x, const double* y, const
                               double radius, int64_t i_begin, int64_t i_end, double* div,
                               int mode);
 
-/* The remaining PSE operators and the shallow-water integrals have only LPM_MODE_FP64 (the
- * reference's association, like the other FP64 sums); LPM_MODE_FP32C returns LPM_ERR_ARG. */
+/* The remaining PSE operators and the sphere shallow-water integrals have only LPM_MODE_FP64
+ * (the reference's association, like the other FP64 sums); LPM_MODE_FP32C returns
+ * LPM_ERR_ARG.  The planar shallow-water integrals have both modes. */
 
 /* Replaces PSEPlaneGradientAtParticles (src/PSEDirectSum.f90:180-217): (gx, gy) =
  * eps**-4 sum_j (f_j + f_i)(x_i - x_j) K1(|x_i - x_j|/eps) A_j. */
@@ -165,7 +166,8 @@ int lpm_pse_interpolate_scalar(int64_t n, const double* x, const double* y, cons
 /* Replaces SWEPlaneRHSIntegrals (src/SWEPlaneSolver.f90:457-534): velocity (u, v) from
  * vorticity and divergence, the double dot product of the velocity gradient and the PSE
  * Laplacian of the surface height.  surf_height = h + topoFn(x, y), evaluated by the caller
- * (the Fortran shim) once per particle. */
+ * (the Fortran shim) once per particle.  LPM_MODE_FP32C: velocity <= 1e-6 of max|u|, double
+ * dot product <= 2e-6 of its max, Laplacian as the planar PSE FP32C sweep. */
 int lpm_swe_plane_rhs_integrals(int64_t n, const double* x, const double* y, const double* vort,
                                 const double* div, const double* surf_height, const double* area,
                                 const int32_t* active, double eps, int64_t i_begin, int64_t i_end,

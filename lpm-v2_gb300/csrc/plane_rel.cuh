@@ -182,11 +182,12 @@ __global__ void __launch_bounds__(THREADS, MINB) plane_rel_sweep_kernel(PlaneRel
 // kGroup sources reduces its centroid o, its radius R about o and its total S_g (of the FP32
 // strengths), and every record is written as rel2(p_j, o) -- the operations the sweep uses
 // for targets.  s_scale = 1/(2 pi) for the velocity, 1/(4 pi) for the stream function.
+// `second` (optional): a second strength second_j A_j s_scale into c.zw (the SWE divergence).
 template <int TILE>
 __global__ void __launch_bounds__(TILE) plane_rel_prep_kernel(const double* x, const double* y, const double* omega,
                                                               const double* area, const int32_t* sorted, int64_t ns,
                                                               double s_scale, PlaneRel::Rec* out,
-                                                              PlaneRel::Origin* org) {
+                                                              PlaneRel::Origin* org, const double* second = nullptr) {
   constexpr int G = PlaneRel::kGroup;
   __shared__ double red[3][TILE];
   __shared__ float fmax_[TILE], cntf[TILE];
@@ -233,7 +234,8 @@ __global__ void __launch_bounds__(TILE) plane_rel_prep_kernel(const double* x, c
     rel2(h, l, oyh, oyl, syh, syl);
     r.a = make_float4(-sxh, -sxh, -syh, -syh);
     r.b = make_float4(s, s, -sxl, -sxl);
-    r.c = make_float4(-syl, -syl, 0.f, 0.f);
+    const float s2 = second ? __double2float_rn(second[j] * area[j] * s_scale) : 0.f;
+    r.c = make_float4(-syl, -syl, s2, s2);
   } else {
     // inert: at the origin with zero strength (q >= delta^2 + 2^-100 > 0)
     r.a = r.b = r.c = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -473,6 +475,157 @@ __global__ void __launch_bounds__(TILE) plane_pse_rel_prep_kernel(const double* 
     o.o = make_float4(oxh, oyh, oxl, oyl);
     o.f = make_float4(fmax_[g0], 0.f, 0.f, 0.f);
     org[t * (TILE / G) + tid / G] = o;
+  }
+}
+
+// ====================================================================== planar SWE integrals
+// SWEPlaneRHSIntegrals, src/SWEPlaneSolver.f90:457-534, velocity and velocity-gradient part
+// (the surface-height Laplacian is the planar PSE sweep above).  With W = vort_j A_j / (2 pi),
+// D = div_j A_j / (2 pi) (records: b.xy = W, c.zw = D) and s = 1/r^2, the reference's terms are
+//   u += s P, v += s Q,  P = D dx - W dy, Q = W dx + D dy,
+//   ux += D s - 2 s dx (s P),  uy += -W s - 2 s dy (s P),
+//   vx +=  W s - 2 s dx (s Q), vy += D s - 2 s dy (s Q)
+// (1/(pi r^4) = 2 s^2 / (2 pi)).  Each gradient term is formed per pair before it is summed, so
+// the cancellation between the D s and the s^2 terms happens per pair, as in the reference.
+// Far groups: 23 packed operations and 2 MUFU per target pair and source; near groups add the
+// lo parts and give the self pair s = 0.  Partials: [chunk][6][nt] (u, v, ux, uy, vx, vy).
+template <int THREADS, int TPT, int TILE, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB) plane_swe_rel_sweep_kernel(PlaneRelArgs a) {
+  static_assert(TPT % 2 == 0, "targets come in pairs");
+  static_assert(TILE % PlaneRel::kGroup == 0, "whole origin groups per tile");
+  constexpr int NP = TPT / 2;
+  constexpr int G = PlaneRel::kGroup;
+  constexpr int GPT = TILE / G;
+  constexpr int NC = 6;
+  using Rec = PlaneRel::Rec;
+  __shared__ __align__(128) Rec stage[2][TILE];
+  __shared__ __align__(8) uint64_t bars[2];
+
+  const int64_t chunk = blockIdx.y;
+  const int64_t tile0 = chunk * a.tiles_per_chunk;
+  int64_t ntl = a.n_tiles - tile0;
+  if (ntl > a.tiles_per_chunk) ntl = a.tiles_per_chunk;
+  if (ntl < 0) ntl = 0;
+
+  PlaneRel::Pair pr[NP];
+  float2 hs[NP][NC], ls[NP][NC];
+  const int64_t first = static_cast<int64_t>(blockIdx.x) * (THREADS * TPT);
+  const int64_t count = a.nt - first < THREADS * TPT ? a.nt - first : THREADS * TPT;
+#pragma unroll
+  for (int p = 0; p < NP; ++p) {
+    int64_t i0 = (2 * p) * THREADS + threadIdx.x, i1 = (2 * p + 1) * THREADS + threadIdx.x;
+    if (i0 >= count) i0 = count - 1;  // duplicates of a valid target; results not stored
+    if (i1 >= count) i1 = count - 1;
+    float h0, l0, h1, l1;
+    split2(a.x[a.ib + first + i0], h0, l0);
+    split2(a.x[a.ib + first + i1], h1, l1);
+    pr[p].xh = make_float2(h0, h1);
+    pr[p].xl = make_float2(l0, l1);
+    split2(a.y[a.ib + first + i0], h0, l0);
+    split2(a.y[a.ib + first + i1], h1, l1);
+    pr[p].yh = make_float2(h0, h1);
+    pr[p].yl = make_float2(l0, l1);
+#pragma unroll
+    for (int c = 0; c < NC; ++c) hs[p][c] = ls[p][c] = make_float2(0.f, 0.f);
+  }
+  const float2 m2 = make_float2(-2.0f, -2.0f);
+
+  pipe_init(bars);
+  uint32_t g = 0;
+  int64_t tile = tile0;
+  staged_sweep<Rec, TILE>(a.src, tile0, ntl, stage[0], stage[1], bars, g, a.status, [&](const Rec* tl) {
+    float2 acc[NP][NC];
+#pragma unroll
+    for (int p = 0; p < NP; ++p)
+#pragma unroll
+      for (int c = 0; c < NC; ++c) acc[p][c] = make_float2(0.f, 0.f);
+    // one pair's terms from d = (dx, dy) and s = 1/r^2 (0 for the self pair)
+    auto terms = [&](float2 (&ac)[NC], float2 dx, float2 dy, float2 sv, float2 w, float2 dd) {
+      const float2 pp = __ffma2_rn(dd, dx, __fmul2_rn(make_float2(-w.x, -w.y), dy));
+      const float2 qq = __ffma2_rn(w, dx, __fmul2_rn(dd, dy));
+      const float2 sp = __fmul2_rn(sv, pp), sq = __fmul2_rn(sv, qq);
+      const float2 ds = __fmul2_rn(dd, sv), ws = __fmul2_rn(w, sv);
+      const float2 s2 = __fmul2_rn(sv, m2);
+      const float2 t1 = __fmul2_rn(s2, dx), t2 = __fmul2_rn(s2, dy);
+      ac[0] = __fadd2_rn(ac[0], sp);
+      ac[1] = __fadd2_rn(ac[1], sq);
+      ac[2] = __fadd2_rn(ac[2], __ffma2_rn(t1, sp, ds));
+      ac[3] = __fadd2_rn(ac[3], __ffma2_rn(t2, sp, make_float2(-ws.x, -ws.y)));
+      ac[4] = __fadd2_rn(ac[4], __ffma2_rn(t1, sq, ws));
+      ac[5] = __fadd2_rn(ac[5], __ffma2_rn(t2, sq, ds));
+    };
+    const PlaneRel::Origin* og = a.org + tile * GPT;
+#pragma unroll 1
+    for (int g0 = 0; g0 < TILE; g0 += G) {
+      const PlaneRel::Origin o = og[g0 / G];
+      const Rec* gr = tl + g0;
+      float2 tx[NP], ty[NP];
+      bool near = false;
+      const float lim = fmaxf((PlaneRel::kNearFactor * o.f.x) * (PlaneRel::kNearFactor * o.f.x),
+                              7.888609052210118e-31f);
+#pragma unroll
+      for (int p = 0; p < NP; ++p) {
+        tx[p] = rel1x2(pr[p].xh, pr[p].xl, o.o.x, o.o.z);
+        ty[p] = rel1x2(pr[p].yh, pr[p].yl, o.o.y, o.o.w);
+        const float2 n2 = __ffma2_rn(ty[p], ty[p], __fmul2_rn(tx[p], tx[p]));
+        near |= !(n2.x > lim) | !(n2.y > lim);
+      }
+      if (!__any_sync(0xffffffffu, near)) {
+        // far group: d = t_hi - s_hi, r^2 > 0
+#pragma unroll 2
+        for (int j = 0; j < G; ++j) {
+          const float4 ra = gr[j].a, rb = gr[j].b, rc = gr[j].c;
+#pragma unroll
+          for (int p = 0; p < NP; ++p) {
+            const float2 dx = __fadd2_rn(tx[p], lo2(ra));
+            const float2 dy = __fadd2_rn(ty[p], hi2(ra));
+            const float2 r2 = __ffma2_rn(dy, dy, __fmul2_rn(dx, dx));
+            terms(acc[p], dx, dy, make_float2(rcp_approx(r2.x), rcp_approx(r2.y)), lo2(rb), hi2(rc));
+          }
+        }
+      } else {
+        // near group: d = (t_hi - s_hi) + (t_lo - s_lo); the self pair has d = 0 exactly
+        float2 txh[NP], tyh[NP], txl[NP], tyl[NP];
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+          rel2x2(pr[p].xh, pr[p].xl, o.o.x, o.o.z, txh[p], txl[p]);
+          rel2x2(pr[p].yh, pr[p].yl, o.o.y, o.o.w, tyh[p], tyl[p]);
+        }
+        for (int j = 0; j < G; ++j) {
+          const float4 ra = gr[j].a, rb = gr[j].b, rc = gr[j].c;
+#pragma unroll
+          for (int p = 0; p < NP; ++p) {
+            const float2 dx = __fadd2_rn(__fadd2_rn(txh[p], lo2(ra)), __fadd2_rn(txl[p], hi2(rb)));
+            const float2 dy = __fadd2_rn(__fadd2_rn(tyh[p], hi2(ra)), __fadd2_rn(tyl[p], lo2(rc)));
+            const float2 r2 = __ffma2_rn(dy, dy, __fmul2_rn(dx, dx));
+            const float2 sv = make_float2(r2.x > 0.f ? rcp_approx(r2.x) : 0.f, r2.y > 0.f ? rcp_approx(r2.y) : 0.f);
+            terms(acc[p], dx, dy, sv, lo2(rb), hi2(rc));
+          }
+        }
+      }
+    }
+    ++tile;
+#pragma unroll
+    for (int p = 0; p < NP; ++p)
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        comp_add(hs[p][c].x, ls[p][c].x, acc[p][c].x);
+        comp_add(hs[p][c].y, ls[p][c].y, acc[p][c].y);
+      }
+  });
+
+#pragma unroll
+  for (int p = 0; p < NP; ++p) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int64_t il = first + (2 * p + h) * THREADS + threadIdx.x;
+      if (il < a.nt) {
+#pragma unroll
+        for (int c = 0; c < NC; ++c)
+          a.partial[(chunk * NC + c) * a.nt + il] = static_cast<double>(h ? hs[p][c].y : hs[p][c].x) +
+                                                    static_cast<double>(h ? ls[p][c].y : ls[p][c].x);
+      }
+    }
   }
 }
 

@@ -35,6 +35,7 @@ constexpr int kBveShapeCount = sizeof(kBveShapes) / sizeof(kBveShapes[0]);
 constexpr int kPlaneThreads = 128, kPlaneTpt = 4, kPlaneTile = 256, kPlaneMinB = 4;
 constexpr int kPseThreads = 128, kPseTpt = 4, kPseTile = 128, kPseMinB = 4;
 constexpr int kStreamThreads = 128, kStreamTpt = 4, kStreamTile = 256, kStreamMinB = 4;
+constexpr int kSweMinB = 3;  // planar SWE velocity sweep: 128 x 4 targets, 3 CTAs per SM
 // FP64 sequential sweep shape
 constexpr int k64Threads = 128, k64Tile = 128;
 
@@ -217,6 +218,20 @@ __global__ void finish_plane_kernel(const double* partial, int64_t nsplit, int64
   v[il] = sv;
 }
 
+// u, v and the double dot product ux ux + 2 uy vx + vy vy of the SWE velocity sweep's six
+// partials [chunk][6][nt] (SWEPlaneSolver.f90:530)
+__global__ void swe_finish_kernel(const double* partial, int64_t nsplit, int64_t nt, double* u, double* v,
+                                  double* ddot) {
+  const int64_t il = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (il >= nt) return;
+  double s[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  for (int64_t k = 0; k < nsplit; ++k)
+    for (int c = 0; c < 6; ++c) s[c] += partial[(k * 6 + c) * nt + il];
+  u[il] = s[0];
+  v[il] = s[1];
+  ddot[il] = (s[2] * s[2] + (2.0 * s[3]) * s[4]) + s[5] * s[5];
+}
+
 __global__ void finish_scalar_kernel(const double* partial, int64_t nsplit, int64_t nt,
                                      double scale, double* out) {
   const int64_t il = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -262,6 +277,7 @@ int tile_of(int kind, int mode) {
     case kSumBveMesh:
       return kBveTile;
     case kSumPlane:
+    case kSumSwePlane:
       return kPlaneTile;
     case kSumPseGrad:
     case kSumPseDiv:
@@ -296,6 +312,8 @@ size_t rec_bytes(int kind, int mode) {
       return sizeof(PlaneRel::Rec);
     case kSumBetaPlane:
       return sizeof(BetaF32::Rec);
+    case kSumSwePlane:
+      return sizeof(PlaneRel::Rec);
     case kSumPseK8Geo:
     case kSumPseGaussChord:
     case kSumPseGrad:
@@ -317,6 +335,8 @@ int comps_of(int kind) {
       return 2;
     case kSumPseGrad:
       return 3;
+    case kSumSwePlane:
+      return 6;
     default:
       return 1;
   }
@@ -362,12 +382,13 @@ bool sum_uses_sorted_sources(int kind, int mode) {
   return mode == LPM_MODE_FP32C && (kind == kSumBve || kind == kSumBveMesh || kind == kSumPlane ||
                                     kind == kSumSphereStream || kind == kSumPseK8Geo || kind == kSumPseGaussChord ||
                                     kind == kSumPseK8Chord || kind == kSumPseGrad || kind == kSumPseDiv ||
-                                    kind == kSumPlaneStream);
+                                    kind == kSumPlaneStream || kind == kSumSwePlane);
 }
 
 size_t sort_scratch_bytes(int kind, int64_t ns) {
   // planar kinds sort in 2-D; the Gaussian-chord Laplacian serves the plane and the sphere
-  if (kind == kSumPlane || kind == kSumPseK8Chord || kind == kSumPlaneStream) return curve_sort2d_bytes(ns);
+  if (kind == kSumPlane || kind == kSumPseK8Chord || kind == kSumPlaneStream || kind == kSumSwePlane)
+    return curve_sort2d_bytes(ns);
   if (kind == kSumPseGaussChord) return std::max(curve_sort_bytes(ns), curve_sort2d_bytes(ns));
   return curve_sort_bytes(ns);
 }
@@ -401,12 +422,22 @@ SumPlan plan_sum(int kind, int mode, int64_t ns, int64_t nt, int sm_count, int s
   }
   // Split the source range so that the last wave of CTAs is nearly full.
   const int64_t tblocks = ceil_div(nt, targets_per_cta(kind, shape));
-  const int minb = (kind == kSumBve || kind == kSumBveMesh) ? kBveShapes[shape].minb : 4;
+  const int minb = (kind == kSumBve || kind == kSumBveMesh) ? kBveShapes[shape].minb : kind == kSumSwePlane ? kSweMinB : 4;
   const int64_t slots = static_cast<int64_t>(sm_count > 0 ? sm_count : 152) * minb;
   const int64_t nsplit = choose_split(tblocks, pl.n_tiles, slots, 65535);
   pl.tiles_per_chunk = ceil_div(pl.n_tiles, nsplit);
   pl.nsplit = ceil_div(pl.n_tiles, pl.tiles_per_chunk);
   pl.partial_bytes = static_cast<size_t>(pl.nsplit) * comps_of(kind) * nt * sizeof(double);
+  if (kind == kSumSwePlane) {
+    // the surface-height Laplacian: the planar K8 PSE sweep, after the velocity sweep
+    const SumPlan pp = plan_sum(kSumPseK8Chord, mode, ns, nt, sm_count, 0);
+    pl.aux_n_tiles = pp.n_tiles;
+    pl.aux_tiles_per_chunk = pp.tiles_per_chunk;
+    pl.aux_nsplit = pp.nsplit;
+    pl.aux_src_offset = align_up(pl.src_bytes, 256);
+    pl.src_bytes = pl.aux_src_offset + pp.src_bytes;
+    pl.partial_bytes = std::max(pl.partial_bytes, pp.partial_bytes);
+  }
   return pl;
 }
 
@@ -869,6 +900,53 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
       launch_sweep<BetaF32, kPseThreads, kPseTpt, kPseTile, kPseMinB>(job, plan, BetaF32::Params{job.x, job.y});
       finish_stream_kernel<<<fin_grid, pb, 0, job.stream>>>(job.partial, plan.nsplit, job.nt, 2, 0.0, nullptr, nullptr,
                                                             job.out0, job.out1);
+      break;
+    }
+    case kSumSwePlane: {
+      const int32_t* src_list = job.src_idx;
+      if (job.sort_scratch) {
+        LPM_TRY(curve_sort2d(job.stream, job.ns, job.src_idx, job.x, job.y, job.sort_scratch, job.sort_bytes,
+                             job.sorted));
+        src_list = job.sorted;
+      }
+      // velocity and velocity gradient (W = vort A / (2 pi), D = div A / (2 pi))
+      PlaneRel::Rec* recs = static_cast<PlaneRel::Rec*>(job.src_buf);
+      PlaneRel::Origin* org = reinterpret_cast<PlaneRel::Origin*>(
+          static_cast<char*>(job.src_buf) + align_up(static_cast<size_t>(npad) * sizeof(PlaneRel::Rec), 256));
+      plane_rel_prep_kernel<kPlaneTile><<<static_cast<unsigned>(plan.n_tiles), kPlaneTile, 0, job.stream>>>(
+          job.x, job.y, job.s1, job.area, src_list, job.ns, 1.0 / (2.0 * kPi), recs, org, job.s2);
+      PlaneRelArgs a;
+      a.x = job.x;
+      a.y = job.y;
+      a.d2 = 0.f;
+      a.src = recs;
+      a.org = org;
+      a.n_tiles = plan.n_tiles;
+      a.tiles_per_chunk = plan.tiles_per_chunk;
+      a.ib = job.ib;
+      a.nt = job.nt;
+      a.partial = job.partial;
+      a.status = job.status;
+      const dim3 grid(static_cast<unsigned>(ceil_div(job.nt, kPseThreads * kPseTpt)),
+                      static_cast<unsigned>(plan.nsplit));
+      plane_swe_rel_sweep_kernel<kPseThreads, kPseTpt, kPlaneTile, kSweMinB><<<grid, kPseThreads, 0, job.stream>>>(a);
+      swe_finish_kernel<<<fin_grid, pb, 0, job.stream>>>(job.partial, plan.nsplit, job.nt, job.out0, job.out1,
+                                                         job.out2);
+      // surface-height Laplacian: the planar K8 PSE sweep on sh = s3, same source order
+      SumJob jp = job;
+      jp.kind = kSumPseK8Chord;
+      jp.s1 = job.s3;
+      jp.src_idx = src_list;
+      jp.sort_scratch = nullptr;
+      jp.src_buf = static_cast<char*>(job.src_buf) + plan.aux_src_offset;
+      SumPlan pp;
+      pp.n_tiles = plan.aux_n_tiles;
+      pp.tiles_per_chunk = plan.aux_tiles_per_chunk;
+      pp.nsplit = plan.aux_nsplit;
+      LPM_TRY(launch_plane_pse_rel(jp, pp, plan.aux_n_tiles * kPseTile));
+      const double e4 = (job.eps * job.eps) * (job.eps * job.eps);
+      finish_scalar_kernel<<<fin_grid, pb, 0, job.stream>>>(job.partial, pp.nsplit, job.nt, 1.0 / kPi / e4,
+                                                            job.out3);
       break;
     }
     default:

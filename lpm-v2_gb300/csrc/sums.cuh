@@ -16,6 +16,10 @@ struct SumPlan {
   size_t src_bytes = 0;      // bytes of the padded source-record array
   size_t partial_bytes = 0;  // bytes of the FP64 partial sums
   int shape = 0;             // sweep shape (sphere BVE FP32C; see bve_shape_count)
+  // a second sweep of the same job (the planar SWE surface-height Laplacian): its tiles and
+  // split, its source records at src_buf + aux_src_offset; it reuses the partials
+  int64_t aux_n_tiles = 0, aux_tiles_per_chunk = 0, aux_nsplit = 0;
+  size_t aux_src_offset = 0;
 };
 
 enum SumKind : int {
@@ -43,7 +47,7 @@ enum SumKind : int {
 
 // Kinds that have only the FP64 form.
 inline bool sum_is_fp64_only(int kind) {
-  return (kind >= kSumPsePlaneGrad && kind <= kSumSweSphere) || kind == kSumBetaStream;
+  return (kind >= kSumPsePlaneGrad && kind <= kSumSweSphere && kind != kSumSwePlane) || kind == kSumBetaStream;
 }
 
 // Inputs of one direct sum over particles [0, n): sources are the ns particles listed (in

@@ -181,3 +181,25 @@ def test_beta_plane_band_fp32c(lg):
     Z = np.where(np.abs(Y) < 0.25, 1.0, 0.0)
     u, v = lg.beta_plane_velocity(X, Y, Z, A, np.ones(X.size, dtype=np.int32), mode="fp32c")
     assert np.abs(u + Y)[np.abs(Y) < 0.2].max() < FP32C_TOL * 0.25 and np.abs(v).max() < FP32C_TOL * 0.25
+
+
+@pytest.mark.parametrize("nest,frac,block", [(4, 1.0, None), (5, 0.9, (100, 7000))])
+def test_swe_plane_rhs_fp32c(lg, oracle_mod, nest, frac, block):
+    """FP32C planar SWE integrals against the FP64 oracle: velocity to 1e-6 of max|(u, v)|, the
+    double dot product to 2e-6 of its max (a quadratic form of 1/r^2 sums; 6.9e-7 measured),
+    the surface-height Laplacian to the planar PSE FP32C bound 1e-4."""
+    m, act, eps = _plane(lg, nest, 7, frac)
+    vort = 4.0 * np.exp(-((m.x - 0.5) ** 2 + m.y ** 2) / 0.3) - 4.0 * np.exp(-((m.x + 0.5) ** 2 + m.y ** 2) / 0.3)
+    div = 0.5 * np.exp(-(m.x ** 2 + (m.y - 0.5) ** 2) / 0.5)
+    sh = 1.0 + 0.1 * np.cos(m.x) * np.sin(0.5 * m.y)
+    ib, ie = (1, m.n) if block is None else block
+    s = slice(ib - 1, ie)
+    got = lg.swe_plane_rhs_integrals(m.x, m.y, vort, div, sh, m.area, act, eps, ib, ie, mode="fp32c")
+    ref = oracle_mod.swe_plane_rhs(m.x, m.y, vort, div, sh, m.area, act, eps, ib - 1, ie)
+    vel = max(np.abs(ref[0]).max(), np.abs(ref[1]).max())
+    err = [np.abs(got[0][s] - ref[0]).max() / vel, np.abs(got[1][s] - ref[1]).max() / vel,
+           rel(got[2][s], ref[2]), rel(got[3][s], ref[3])]
+    print("swe fp32c errors", err)
+    assert err[0] <= FP32C_TOL and err[1] <= FP32C_TOL
+    assert err[2] <= 2e-6
+    assert err[3] <= 1e-4
