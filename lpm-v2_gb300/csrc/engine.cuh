@@ -25,6 +25,16 @@ struct FlushOf<Op, std::void_t<decltype(Op::kFlush)>> {
   static constexpr int value = Op::kFlush;
 };
 
+// Whether an operator evaluates two targets at once (Op::interact2, packed FP32x2 math).
+template <class Op, class = void>
+struct PairsOf {
+  static constexpr bool value = false;
+};
+template <class Op>
+struct PairsOf<Op, std::void_t<decltype(Op::kPairs)>> {
+  static constexpr bool value = Op::kPairs;
+};
+
 // Initialises the two stage barriers of a TMA pipeline (once per CTA).
 __device__ __forceinline__ void pipe_init(uint64_t* bars) {
   if (threadIdx.x == 0) {
@@ -142,8 +152,14 @@ __global__ void __launch_bounds__(THREADS, MINB) sweep_fp32c_kernel(SweepArgs<Op
 #pragma unroll 4
                               for (int j = j0; j < j0 + FL; ++j) {
                                 const Rec r = tile[j];
+                                if constexpr (PairsOf<Op>::value) {
+                                  static_assert(TPT % 2 == 0, "targets come in pairs");
 #pragma unroll
-                                for (int t = 0; t < TPT; ++t) Op::interact(tg[t], r, acc[t]);
+                                  for (int t = 0; t < TPT; t += 2) Op::interact2(tg[t], tg[t + 1], r, acc[t], acc[t + 1]);
+                                } else {
+#pragma unroll
+                                  for (int t = 0; t < TPT; ++t) Op::interact(tg[t], r, acc[t]);
+                                }
                               }
 #pragma unroll
                               for (int t = 0; t < TPT; ++t)

@@ -704,52 +704,85 @@ struct BetaF32 {
     split2(p.y[i], t.yh, t.yl);
     return t;
   }
-  __device__ static __forceinline__ void interact(const Tgt& t, const Rec& r, float (&acc)[2]) {
-    constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23: x + kMagic - kMagic = rint(x)
-    // t = (x_i - x_j) - rint(x_i - x_j), with the rounding error of the hi difference
-    const float dh = __fadd_rn(t.xh, -r.a.x);
-    const float bb = __fadd_rn(dh, -t.xh);
-    const float e = __fadd_rn(__fadd_rn(t.xh, -__fadd_rn(dh, -bb)), __fadd_rn(-r.a.x, -bb));
-    const float n = __fadd_rn(__fadd_rn(dh, kMagic), -kMagic);
-    const float tt = __fadd_rn(__fadd_rn(dh, -n), __fadd_rn(e, __fadd_rn(t.xl, -r.a.z)));
-    const float dy = diff2(t.yh, t.yl, r.a.y, r.a.w);
+  // Two targets at once in packed FP32x2 arithmetic (the engine calls interact2 for target
+  // pairs).  2^-k comes from the bits of the magic-number sum that rounds a / ln 2 (a clamped
+  // to 87 < 126 ln 2: beyond it the terms have reached their limits, u -> S sign(dy), v -> 0);
+  // 2^(1-k) = 2^-k + 2^-k and 4^-k = (2^-k)^2, which underflows to 0 for k > 63 as it should.
+  static constexpr bool kPairs = true;
+  __device__ static __forceinline__ float2 bits_abs(float2 v) {
+    return make_float2(__int_as_float(__float_as_int(v.x) & 0x7fffffff),
+                       __int_as_float(__float_as_int(v.y) & 0x7fffffff));
+  }
+  __device__ static __forceinline__ void interact2(const Tgt& t0, const Tgt& t1, const Rec& r, float (&a0)[2],
+                                                   float (&a1)[2]) {
+    const float2 kM = make_float2(12582912.0f, 12582912.0f), kNM = make_float2(-12582912.0f, -12582912.0f);
+    const float2 nxh = make_float2(-r.a.x, -r.a.x);
+    const float2 txh = make_float2(t0.xh, t1.xh);
+    // t = (x_i - x_j) - rint(x_i - x_j), keeping the rounding of the hi difference (TwoSum)
+    const float2 dh = __fadd2_rn(txh, nxh);
+    const float2 bb = __fadd2_rn(dh, make_float2(-txh.x, -txh.y));
+    const float2 dv = __fadd2_rn(dh, make_float2(-bb.x, -bb.y));
+    const float2 e = __fadd2_rn(__fadd2_rn(txh, make_float2(-dv.x, -dv.y)), __fadd2_rn(nxh, make_float2(-bb.x, -bb.y)));
+    const float2 nn = __fadd2_rn(__fadd2_rn(dh, kM), kNM);
+    const float2 lo = __fadd2_rn(e, __fadd2_rn(make_float2(t0.xl, t1.xl), make_float2(-r.a.z, -r.a.z)));
+    const float2 tt = __fadd2_rn(__fadd2_rn(dh, make_float2(-nn.x, -nn.y)), lo);
+    const float2 dy = __fadd2_rn(__fadd2_rn(make_float2(t0.yh, t1.yh), make_float2(-r.a.y, -r.a.y)),
+                                 __fadd2_rn(make_float2(t0.yl, t1.yl), make_float2(-r.a.w, -r.a.w)));
     // sin(pi t), cos(pi t)
-    const float t2 = __fmul_rn(tt, tt);
-    float ps = __fmaf_rn(-0.00737043097615242f, t2, 0.08214588463306427f);
-    ps = __fmaf_rn(ps, t2, -0.5992645025253296f);
-    ps = __fmaf_rn(ps, t2, 2.550163984298706f);
-    ps = __fmaf_rn(ps, t2, -5.167712688446045f);
-    ps = __fmaf_rn(ps, t2, 3.1415927410125732f);
-    const float sn = __fmul_rn(ps, tt);
-    float pc = __fmaf_rn(0.001929574296809733f, t2, -0.025806890800595284f);
-    pc = __fmaf_rn(pc, t2, 0.23533062636852264f);
-    pc = __fmaf_rn(pc, t2, -1.3352627754211426f);
-    pc = __fmaf_rn(pc, t2, 4.058712005615234f);
-    pc = __fmaf_rn(pc, t2, -4.934802055358887f);
-    const float cs = __fmaf_rn(pc, t2, 1.0f);
+    const float2 t2 = __fmul2_rn(tt, tt);
+    float2 ps = __ffma2_rn(make_float2(-0.00737043097615242f, -0.00737043097615242f), t2,
+                           make_float2(0.08214588463306427f, 0.08214588463306427f));
+    ps = __ffma2_rn(ps, t2, make_float2(-0.5992645025253296f, -0.5992645025253296f));
+    ps = __ffma2_rn(ps, t2, make_float2(2.550163984298706f, 2.550163984298706f));
+    ps = __ffma2_rn(ps, t2, make_float2(-5.167712688446045f, -5.167712688446045f));
+    ps = __ffma2_rn(ps, t2, make_float2(3.1415927410125732f, 3.1415927410125732f));
+    const float2 sn = __fmul2_rn(ps, tt);
+    float2 pc = __ffma2_rn(make_float2(0.001929574296809733f, 0.001929574296809733f), t2,
+                           make_float2(-0.025806890800595284f, -0.025806890800595284f));
+    pc = __ffma2_rn(pc, t2, make_float2(0.23533062636852264f, 0.23533062636852264f));
+    pc = __ffma2_rn(pc, t2, make_float2(-1.3352627754211426f, -1.3352627754211426f));
+    pc = __ffma2_rn(pc, t2, make_float2(4.058712005615234f, 4.058712005615234f));
+    pc = __ffma2_rn(pc, t2, make_float2(-4.934802055358887f, -4.934802055358887f));
+    const float2 cs = __ffma2_rn(pc, t2, make_float2(1.0f, 1.0f));
     // sinh, cosh of a = pi |dy| as 2^(k-1) (sh', ch')
-    const float a = __fmul_rn(3.1415927f, fabsf(dy));
-    const float kb = __fmaf_rn(a, 1.442695f, kMagic);  // kMagic + rint(a / ln 2)
-    const float kf = __fadd_rn(kb, -kMagic);
-    float rr = __fmaf_rn(-kf, 0.69314575f, a);
-    rr = __fmaf_rn(-kf, 1.4286068e-06f, rr);
-    const float r2 = __fmul_rn(rr, rr);
-    const float shr = __fmaf_rn(__fmul_rn(rr, r2),
-                                __fmaf_rn(__fmaf_rn(r2, 1.9841270e-4f, 8.3333333e-3f), r2, 0.16666667f), rr);
-    const float chr = __fmaf_rn(
-        __fmaf_rn(__fmaf_rn(__fmaf_rn(r2, 2.4801587e-5f, 1.3888889e-3f), r2, 4.1666667e-2f), r2, 0.5f), r2, 1.0f);
-    const int k = __float_as_int(kb) - 0x4b400000;
-    const int kq = k < 63 ? k : 63, ks = k < 126 ? k : 126;
-    const float q = __int_as_float((127 - 2 * kq) << 23);  // 4^-k
-    const float sc = __int_as_float((128 - ks) << 23);     // 2^(1-k)
-    const float om = __fadd_rn(1.0f, -q), op = __fadd_rn(1.0f, q);
-    const float shp = copysignf(__fmaf_rn(om, chr, __fmul_rn(op, shr)), dy);
-    const float chp = __fmaf_rn(op, chr, __fmul_rn(om, shr));
-    const float snp = __fmul_rn(sn, sc), csp = __fmul_rn(cs, sc);
-    const float den = __fmaf_rn(shp, shp, __fmaf_rn(snp, snp, 7.888609052210118e-31f));  // + 2^-100
-    const float w = __fmul_rn(r.b.x, rcp_approx(den));
-    acc[0] = __fmaf_rn(-__fmul_rn(w, shp), chp, acc[0]);
-    acc[1] = __fmaf_rn(__fmul_rn(w, snp), csp, acc[1]);
+    float2 a = __fmul2_rn(make_float2(3.1415927f, 3.1415927f), bits_abs(dy));
+    a = make_float2(fminf(a.x, 87.0f), fminf(a.y, 87.0f));
+    const float2 kb = __ffma2_rn(a, make_float2(1.442695f, 1.442695f), kM);
+    const float2 kf = __fadd2_rn(kb, kNM);
+    float2 rr = __ffma2_rn(make_float2(-kf.x, -kf.y), make_float2(0.69314575f, 0.69314575f), a);
+    rr = __ffma2_rn(make_float2(-kf.x, -kf.y), make_float2(1.4286068e-06f, 1.4286068e-06f), rr);
+    const float2 r2 = __fmul2_rn(rr, rr);
+    const float2 shr = __ffma2_rn(
+        __fmul2_rn(rr, r2),
+        __ffma2_rn(__ffma2_rn(r2, make_float2(1.9841270e-4f, 1.9841270e-4f), make_float2(8.3333333e-3f, 8.3333333e-3f)),
+                   r2, make_float2(0.16666667f, 0.16666667f)),
+        rr);
+    const float2 chr = __ffma2_rn(
+        __ffma2_rn(__ffma2_rn(__ffma2_rn(r2, make_float2(2.4801587e-5f, 2.4801587e-5f),
+                                         make_float2(1.3888889e-3f, 1.3888889e-3f)),
+                              r2, make_float2(4.1666667e-2f, 4.1666667e-2f)),
+                   r2, make_float2(0.5f, 0.5f)),
+        r2, make_float2(1.0f, 1.0f));
+    // 2^-k: 0x3f800000 - (k << 23) with k = bits(kb) - bits(kM) (bits(kM) << 23 vanishes mod 2^32)
+    const float2 pk = make_float2(__uint_as_float(0x3f800000u - (__float_as_uint(kb.x) << 23)),
+                                  __uint_as_float(0x3f800000u - (__float_as_uint(kb.y) << 23)));
+    const float2 sc = __fadd2_rn(pk, pk);
+    const float2 q = __fmul2_rn(pk, pk);
+    const float2 om = __fadd2_rn(make_float2(1.0f, 1.0f), make_float2(-q.x, -q.y));
+    const float2 op = __fadd2_rn(make_float2(1.0f, 1.0f), q);
+    float2 shp = __ffma2_rn(om, chr, __fmul2_rn(op, shr));
+    shp = make_float2(copysignf(shp.x, dy.x), copysignf(shp.y, dy.y));
+    const float2 chp = __ffma2_rn(op, chr, __fmul2_rn(om, shr));
+    const float2 snp = __fmul2_rn(sn, sc), csp = __fmul2_rn(cs, sc);
+    const float2 den = __ffma2_rn(shp, shp, __ffma2_rn(snp, snp, make_float2(7.888609052210118e-31f, 7.888609052210118e-31f)));
+    const float2 w = __fmul2_rn(make_float2(r.b.x, r.b.x), make_float2(rcp_approx(den.x), rcp_approx(den.y)));
+    const float2 wsh = __fmul2_rn(w, shp), wsn = __fmul2_rn(w, snp);
+    const float2 au = __ffma2_rn(make_float2(-wsh.x, -wsh.y), chp, make_float2(a0[0], a1[0]));
+    const float2 av = __ffma2_rn(wsn, csp, make_float2(a0[1], a1[1]));
+    a0[0] = au.x;
+    a1[0] = au.y;
+    a0[1] = av.x;
+    a1[1] = av.y;
   }
 };
 
