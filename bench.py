@@ -68,7 +68,7 @@ def parse_args():
                    help="rk4: the headline single-instance step; ensemble: the 64-instance batch")
     p.add_argument("--instances", type=int, default=64)
     p.add_argument("--sum", choices=["bve", "plane", "pse_k8", "pse_gauss", "pse_grad", "pse_div", "pse_plane",
-                                     "stream", "plane_stream", "beta", "swe_plane"],
+                                     "stream", "plane_stream", "beta", "swe_plane", "swe_sphere"],
                    default="bve",
                    help="--workload sum: which direct sum (one host C-ABI call per step)")
     p.add_argument("--mode", choices=["fp32c", "fp64"], default="fp32c", help="--workload sum: precision mode")
@@ -628,6 +628,15 @@ def run_sum(args):
         call = lambda ie: lg.swe_plane_rhs_integrals(c["x"], c["y"], c["omega"], div, sh, c["area"], c["active"],
                                                      eps, i_end=ie, mode=args.mode)
         mesh = f"quad nest {args.nest} on [-4,4]^2 (SWE velocity, double dot and surface Laplacian, eps = 2h)"
+    elif args.sum == "swe_sphere":
+        c = wl.config_rh54_icos(args.nest, seed=0)
+        n, ns = c["x"].size, int(c["active"].sum())
+        div = 0.1 * np.cos(3.0 * c["z"]) * np.sin(2.0 * c["x"])
+        sh = 1.0 + 0.2 * c["z"]
+        eps = 2.0 * float(np.sqrt(c["area"][c["active"] == 1].max()))
+        call = lambda ie: lg.swe_sphere_rhs_integrals(c["x"], c["y"], c["z"], c["zeta"], div, sh, c["area"],
+                                                      c["active"], 1.0, eps, 1.0, i_end=ie, mode=args.mode)
+        mesh = f"icosahedral nest {args.nest} (RH54 vorticity, divergence, surface Laplacian, eps = 2h)"
     elif args.sum == "beta":
         c = wl.config_beta_plane(args.nest)
         n, ns = c["x"].size, int(c["active"].sum())

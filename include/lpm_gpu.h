@@ -121,9 +121,9 @@ int lpm_pse_sphere_divergence(int64_t n, const double* x, const double* y, const
                               double radius, int64_t i_begin, int64_t i_end, double* div,
                               int mode);
 
-/* The remaining PSE operators and the sphere shallow-water integrals have only LPM_MODE_FP64
- * (the reference's association, like the other FP64 sums); LPM_MODE_FP32C returns
- * LPM_ERR_ARG.  The planar shallow-water integrals have both modes. */
+/* The remaining PSE operators have only LPM_MODE_FP64 (the reference's association, like the
+ * other FP64 sums); LPM_MODE_FP32C returns LPM_ERR_ARG.  The shallow-water integrals have
+ * both modes. */
 
 /* Replaces PSEPlaneGradientAtParticles (src/PSEDirectSum.f90:180-217): (gx, gy) =
  * eps**-4 sum_j (f_j + f_i)(x_i - x_j) K1(|x_i - x_j|/eps) A_j. */
@@ -177,7 +177,9 @@ int lpm_swe_plane_rhs_integrals(int64_t n, const double* x, const double* y, con
  * it: (u, v, w) from relative vorticity and divergence on the sphere of radius `radius`, the
  * surface-height Laplacian with K8(SphereDistance/eps)/eps**2 (SphereDistance scaled by the
  * SphereGeometry module's SphereRadius, `sphere_radius`; no further 1/eps**2), and
- * double_dot = 0 (the reference never sets it).  surf_height = h + topoFn(x, y, z). */
+ * double_dot = 0 (the reference never sets it).  surf_height = h + topoFn(x, y, z).
+ * LPM_MODE_FP32C: velocity <= 1e-6 of max|u| (one sweep for the rotational and potential
+ * parts), Laplacian as the geodesic PSE FP32C sweep. */
 int lpm_swe_sphere_rhs_integrals(int64_t n, const double* x, const double* y, const double* z,
                                  const double* relvort, const double* div, const double* surf_height,
                                  const double* area, const int32_t* active, double radius,

@@ -222,7 +222,8 @@ __global__ void __launch_bounds__(TILE) stream_rel_prep_kernel(const double* x, 
                                                                const double* qr, const double* qa, const double* area,
                                                                const int32_t* sorted, int64_t ns, double inv_a,
                                                                int64_t ib, int64_t nt, StreamRel::Rec* out,
-                                                               BveRel::Origin* org, double* self_w) {
+                                                               BveRel::Origin* org, double* self_w,
+                                                               double scale_r = -kInv4Pi, double scale_a = -kInv4Pi) {
   const int64_t t = blockIdx.x;
   const int64_t k = t * TILE + threadIdx.x;
   const bool valid = k < ns;
@@ -241,13 +242,13 @@ __global__ void __launch_bounds__(TILE) stream_rel_prep_kernel(const double* x, 
     group_offsets(f, px, py, pz, hi, lo);
     const float nc = __double2float_rn(-cj);
     const double wr = qr[j] * area[j], wa = qa[j] * area[j];
-    const float sr = __double2float_rn(wr * -kInv4Pi), sa = __double2float_rn(wa * -kInv4Pi);
+    const float sr = __double2float_rn(wr * scale_r), sa = __double2float_rn(wa * scale_a);
     r.a = make_float4(-hi[0], -hi[0], -hi[1], -hi[1]);
     r.b = make_float4(-hi[2], -hi[2], nc, nc);
     r.c = make_float4(sr, sr, sa, sa);
     r.d = make_float4(-lo[0], -lo[0], -lo[1], -lo[1]);
     r.e = make_float4(-lo[2], -lo[2], 0.f, 0.f);
-    if (j >= ib && j < ib + nt) {
+    if (self_w && j >= ib && j < ib + nt) {
       self_w[j - ib] = wr;
       self_w[nt + j - ib] = wa;
     }
@@ -418,6 +419,142 @@ __global__ void __launch_bounds__(THREADS, MINB) plane_stream_rel_sweep_kernel(P
         const double c = static_cast<double>(h ? hk[p].y : hk[p].x) + static_cast<double>(h ? lk[p].y : lk[p].x);
         a.partial[chunk * a.nt + il] =
             (static_cast<double>(h ? hs[p].y : hs[p].x) + static_cast<double>(h ? ls[p].y : ls[p].x)) + kLn2 * c;
+      }
+    }
+  }
+}
+
+// ====================================================================== sphere SWE velocity
+// SWESphereRHSIntegrals, src/SphereSWESolver.f90:299-372, velocity part, on the stream
+// functions' layout (two strengths per record: S_r = -zeta_j A_j / (2 pi a^2) and
+// S_p = div_j A_j / (2 pi a^2), written by stream_rel_prep_kernel).  With p = x/a, d = p_i - p_j
+// and a^2 - x_i.x_j = (a^2/2) q, q = |d|^2 - c_i - c_j, the reference's
+//   u -= (x_i x x_j) zeta_j A_j / (4 pi a^2 (a^2 - x_i.x_j)) + x_j a div_j A_j / (4 pi a^2 (a^2 - x_i.x_j))
+// is u = Dr x p_i + Dp - p_i W with Dr = sum (S_r/q) d, Dp = sum (S_p/q) d, W = sum S_p/q
+// (x_i x x_j = a^2 d x p_i and p_j = p_i - d).  The self pair (d = 0 exactly, in a near or a
+// compact group) gets 1/q = 0.  Per target pair and source (far form): d (3 FADD2), |d|^2
+// (3), q (1), the select and 2 MUFU, two weights (2), 7 accumulations.  Partials:
+// [chunk][7][nt] (Dr, Dp, W).
+template <int THREADS, int TPT, int TILE, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB) sphere_swe_rel_sweep_kernel(SweepArgs<BveF32> a,
+                                                                             const StreamRel::Rec* __restrict__ src,
+                                                                             const BveRel::Origin* __restrict__ org) {
+  static_assert(TPT % 2 == 0, "targets come in pairs");
+  constexpr int NP = TPT / 2;
+  constexpr int G = BveRel::kGroup;
+  constexpr int GPT = TILE / G;
+  constexpr int NC = 7;
+  using Rec = StreamRel::Rec;
+  __shared__ __align__(128) Rec stage[2][TILE];
+  __shared__ __align__(8) uint64_t bars[2];
+
+  const int64_t chunk = blockIdx.y;
+  const int64_t tile0 = chunk * a.tiles_per_chunk;
+  int64_t ntl = a.n_tiles - tile0;
+  if (ntl > a.tiles_per_chunk) ntl = a.tiles_per_chunk;
+  if (ntl < 0) ntl = 0;
+
+  BveX2::Pair pr[NP];
+  float2 hs[NP][NC], ls[NP][NC];
+  const int64_t first = static_cast<int64_t>(blockIdx.x) * (THREADS * TPT);
+  const int64_t count = a.nt - first < THREADS * TPT ? a.nt - first : THREADS * TPT;
+  bve_load_pairs<NP>(a.p, a.ib + first, count, THREADS, pr);
+#pragma unroll
+  for (int p = 0; p < NP; ++p)
+#pragma unroll
+    for (int c = 0; c < NC; ++c) hs[p][c] = ls[p][c] = make_float2(0.f, 0.f);
+
+  pipe_init(bars);
+  uint32_t g = 0;
+  int64_t tile = tile0;
+  staged_sweep<Rec, TILE>(src, tile0, ntl, stage[0], stage[1], bars, g, a.status, [&](const Rec* tl) {
+    float2 ac[NP][NC];
+#pragma unroll
+    for (int p = 0; p < NP; ++p)
+#pragma unroll
+      for (int c = 0; c < NC; ++c) ac[p][c] = make_float2(0.f, 0.f);
+    auto terms = [&](float2 (&acc)[NC], float2 dx, float2 dy, float2 dz, float2 q, float2 u, float2 sr, float2 sp) {
+      const float2 inv = make_float2(u.x != 0.f ? rcp_approx(q.x) : 0.f, u.y != 0.f ? rcp_approx(q.y) : 0.f);
+      const float2 wr = __fmul2_rn(sr, inv), wp = __fmul2_rn(sp, inv);
+      acc[0] = __ffma2_rn(wr, dx, acc[0]);
+      acc[1] = __ffma2_rn(wr, dy, acc[1]);
+      acc[2] = __ffma2_rn(wr, dz, acc[2]);
+      acc[3] = __ffma2_rn(wp, dx, acc[3]);
+      acc[4] = __ffma2_rn(wp, dy, acc[4]);
+      acc[5] = __ffma2_rn(wp, dz, acc[5]);
+      acc[6] = __fadd2_rn(wp, acc[6]);
+    };
+    const BveRel::Origin* og = org + tile * GPT;
+#pragma unroll 1
+    for (int g0 = 0; g0 < TILE; g0 += G) {
+      const BveRel::Origin o = og[g0 / G];
+      const Rec* gr = tl + g0;
+      float2 tx[NP], ty[NP], tz[NP];
+#pragma unroll
+      for (int p = 0; p < NP; ++p) {
+        tx[p] = rel1x2(pr[p].xh, pr[p].xl, o.hi.x, o.lo.x);
+        ty[p] = rel1x2(pr[p].yh, pr[p].yl, o.hi.y, o.lo.y);
+        tz[p] = rel1x2(pr[p].zh, pr[p].zl, o.hi.z, o.lo.z);
+      }
+      if (o.hi.w == 0.f || !warp_near<NP>(tx, ty, tz, o.hi.w)) {  // R = 0: compact, never near
+        // compact or far group: d = t_hi - s_hi
+#pragma unroll 2
+        for (int j = 0; j < G; ++j) {
+          const float4 ra = gr[j].a, rb = gr[j].b, rc = gr[j].c;
+          const float2 nsx = lo2(ra), nsy = hi2(ra), nsz = lo2(rb), ncj = hi2(rb), sr = lo2(rc), sp = hi2(rc);
+#pragma unroll
+          for (int p = 0; p < NP; ++p) {
+            const float2 dx = __fadd2_rn(tx[p], nsx);
+            const float2 dy = __fadd2_rn(ty[p], nsy);
+            const float2 dz = __fadd2_rn(tz[p], nsz);
+            const float2 u = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+            terms(ac[p], dx, dy, dz, __fadd2_rn(u, __fadd2_rn(pr[p].nc, ncj)), u, sr, sp);
+          }
+        }
+      } else {
+        // near group: d = (t_hi - s_hi) + (t_lo - s_lo)
+        float2 txh[NP], tyh[NP], tzh[NP], txl[NP], tyl[NP], tzl[NP];
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+          rel2x2(pr[p].xh, pr[p].xl, o.hi.x, o.lo.x, txh[p], txl[p]);
+          rel2x2(pr[p].yh, pr[p].yl, o.hi.y, o.lo.y, tyh[p], tyl[p]);
+          rel2x2(pr[p].zh, pr[p].zl, o.hi.z, o.lo.z, tzh[p], tzl[p]);
+        }
+        for (int j = 0; j < G; ++j) {
+          const float4 ra = gr[j].a, rb = gr[j].b, rc = gr[j].c, rd = gr[j].d, re = gr[j].e;
+          const float2 nsx = lo2(ra), nsy = hi2(ra), nsz = lo2(rb), ncj = hi2(rb), sr = lo2(rc), sp = hi2(rc);
+          const float2 nlx = lo2(rd), nly = hi2(rd), nlz = lo2(re);
+#pragma unroll
+          for (int p = 0; p < NP; ++p) {
+            const float2 dx = __fadd2_rn(__fadd2_rn(txh[p], nsx), __fadd2_rn(txl[p], nlx));
+            const float2 dy = __fadd2_rn(__fadd2_rn(tyh[p], nsy), __fadd2_rn(tyl[p], nly));
+            const float2 dz = __fadd2_rn(__fadd2_rn(tzh[p], nsz), __fadd2_rn(tzl[p], nlz));
+            const float2 u = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+            terms(ac[p], dx, dy, dz, __fadd2_rn(u, __fadd2_rn(pr[p].nc, ncj)), u, sr, sp);
+          }
+        }
+      }
+    }
+    ++tile;
+#pragma unroll
+    for (int p = 0; p < NP; ++p)
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        comp_add(hs[p][c].x, ls[p][c].x, ac[p][c].x);
+        comp_add(hs[p][c].y, ls[p][c].y, ac[p][c].y);
+      }
+  });
+
+#pragma unroll
+  for (int p = 0; p < NP; ++p) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int64_t il = first + (2 * p + h) * THREADS + threadIdx.x;
+      if (il < a.nt) {
+#pragma unroll
+        for (int c = 0; c < NC; ++c)
+          a.partial[(chunk * NC + c) * a.nt + il] = static_cast<double>(h ? hs[p][c].y : hs[p][c].x) +
+                                                    static_cast<double>(h ? ls[p][c].y : ls[p][c].x);
       }
     }
   }

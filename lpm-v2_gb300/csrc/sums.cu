@@ -35,7 +35,8 @@ constexpr int kBveShapeCount = sizeof(kBveShapes) / sizeof(kBveShapes[0]);
 constexpr int kPlaneThreads = 128, kPlaneTpt = 4, kPlaneTile = 256, kPlaneMinB = 4;
 constexpr int kPseThreads = 128, kPseTpt = 4, kPseTile = 128, kPseMinB = 4;
 constexpr int kStreamThreads = 128, kStreamTpt = 4, kStreamTile = 256, kStreamMinB = 4;
-constexpr int kSweMinB = 3;  // planar SWE velocity sweep: 128 x 4 targets, 3 CTAs per SM
+constexpr int kSweMinB = 3;        // planar SWE velocity sweep: 128 x 4 targets, 3 CTAs per SM
+constexpr int kSweSphereMinB = 2;  // sphere SWE velocity sweep: 2 CTAs per SM (no spills; 10 % over 3)
 // FP64 sequential sweep shape
 constexpr int k64Threads = 128, k64Tile = 128;
 
@@ -232,6 +233,23 @@ __global__ void swe_finish_kernel(const double* partial, int64_t nsplit, int64_t
   ddot[il] = (s[2] * s[2] + (2.0 * s[3]) * s[4]) + s[5] * s[5];
 }
 
+// The sphere SWE velocity from the seven partials [chunk][7][nt] (Dr, Dp, W):
+// u = Dr x p_i + Dp - p_i W with p_i = x_i / a, in FP64.
+__global__ void swe_sphere_finish_kernel(const double* partial, int64_t nsplit, int64_t nt, int64_t ib,
+                                         const double* x, const double* y, const double* z, double inv_a, double* u,
+                                         double* v, double* w) {
+  const int64_t il = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (il >= nt) return;
+  double s[7] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  for (int64_t k = 0; k < nsplit; ++k)
+    for (int c = 0; c < 7; ++c) s[c] += partial[(k * 7 + c) * nt + il];
+  const int64_t i = ib + il;
+  const double px = x[i] * inv_a, py = y[i] * inv_a, pz = z[i] * inv_a;
+  u[il] = (s[1] * pz - s[2] * py) + (s[3] - px * s[6]);
+  v[il] = (s[2] * px - s[0] * pz) + (s[4] - py * s[6]);
+  w[il] = (s[0] * py - s[1] * px) + (s[5] - pz * s[6]);
+}
+
 __global__ void finish_scalar_kernel(const double* partial, int64_t nsplit, int64_t nt,
                                      double scale, double* out) {
   const int64_t il = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -284,6 +302,7 @@ int tile_of(int kind, int mode) {
       return kPseTile;
     case kSumSphereStream:
     case kSumPlaneStream:
+    case kSumSweSphere:
       return kStreamTile;
     default:
       return kPseTile;
@@ -307,6 +326,7 @@ size_t rec_bytes(int kind, int mode) {
     case kSumPlane:
       return sizeof(PlaneRel::Rec);
     case kSumSphereStream:
+    case kSumSweSphere:
       return sizeof(StreamRel::Rec);
     case kSumPlaneStream:
       return sizeof(PlaneRel::Rec);
@@ -337,6 +357,8 @@ int comps_of(int kind) {
       return 3;
     case kSumSwePlane:
       return 6;
+    case kSumSweSphere:
+      return 7;
     default:
       return 1;
   }
@@ -351,6 +373,7 @@ int targets_per_cta(int kind, int shape) {
       return kPlaneThreads * kPlaneTpt;
     case kSumSphereStream:
     case kSumPlaneStream:
+    case kSumSweSphere:
       return kStreamThreads * kStreamTpt;
     default:
       return kPseThreads * kPseTpt;
@@ -382,7 +405,7 @@ bool sum_uses_sorted_sources(int kind, int mode) {
   return mode == LPM_MODE_FP32C && (kind == kSumBve || kind == kSumBveMesh || kind == kSumPlane ||
                                     kind == kSumSphereStream || kind == kSumPseK8Geo || kind == kSumPseGaussChord ||
                                     kind == kSumPseK8Chord || kind == kSumPseGrad || kind == kSumPseDiv ||
-                                    kind == kSumPlaneStream || kind == kSumSwePlane);
+                                    kind == kSumPlaneStream || kind == kSumSwePlane || kind == kSumSweSphere);
 }
 
 size_t sort_scratch_bytes(int kind, int64_t ns) {
@@ -422,15 +445,18 @@ SumPlan plan_sum(int kind, int mode, int64_t ns, int64_t nt, int sm_count, int s
   }
   // Split the source range so that the last wave of CTAs is nearly full.
   const int64_t tblocks = ceil_div(nt, targets_per_cta(kind, shape));
-  const int minb = (kind == kSumBve || kind == kSumBveMesh) ? kBveShapes[shape].minb : kind == kSumSwePlane ? kSweMinB : 4;
+  const int minb = (kind == kSumBve || kind == kSumBveMesh)          ? kBveShapes[shape].minb
+                   : kind == kSumSwePlane                            ? kSweMinB
+                   : kind == kSumSweSphere                           ? kSweSphereMinB
+                                                                     : 4;
   const int64_t slots = static_cast<int64_t>(sm_count > 0 ? sm_count : 152) * minb;
   const int64_t nsplit = choose_split(tblocks, pl.n_tiles, slots, 65535);
   pl.tiles_per_chunk = ceil_div(pl.n_tiles, nsplit);
   pl.nsplit = ceil_div(pl.n_tiles, pl.tiles_per_chunk);
   pl.partial_bytes = static_cast<size_t>(pl.nsplit) * comps_of(kind) * nt * sizeof(double);
-  if (kind == kSumSwePlane) {
-    // the surface-height Laplacian: the planar K8 PSE sweep, after the velocity sweep
-    const SumPlan pp = plan_sum(kSumPseK8Chord, mode, ns, nt, sm_count, 0);
+  if (kind == kSumSwePlane || kind == kSumSweSphere) {
+    // the surface-height Laplacian: the K8 PSE sweep (planar or geodesic), after the velocity sweep
+    const SumPlan pp = plan_sum(kind == kSumSwePlane ? kSumPseK8Chord : kSumPseK8Geo, mode, ns, nt, sm_count, 0);
     pl.aux_n_tiles = pp.n_tiles;
     pl.aux_tiles_per_chunk = pp.tiles_per_chunk;
     pl.aux_nsplit = pp.nsplit;
@@ -900,6 +926,54 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
       launch_sweep<BetaF32, kPseThreads, kPseTpt, kPseTile, kPseMinB>(job, plan, BetaF32::Params{job.x, job.y});
       finish_stream_kernel<<<fin_grid, pb, 0, job.stream>>>(job.partial, plan.nsplit, job.nt, 2, 0.0, nullptr, nullptr,
                                                             job.out0, job.out1);
+      break;
+    }
+    case kSumSweSphere: {
+      const double inv_a = 1.0 / job.radius;
+      const int32_t* src_list = job.src_idx;
+      if (job.sort_scratch) {
+        LPM_TRY(curve_sort(job.stream, job.ns, job.src_idx, job.x, job.y, job.z, inv_a, job.sort_scratch,
+                            job.sort_bytes, job.sorted));
+        src_list = job.sorted;
+      }
+      // velocity: S_r = -zeta A / (2 pi a^2), S_p = div A / (2 pi a^2) on the two-strength layout
+      StreamRel::Rec* recs = static_cast<StreamRel::Rec*>(job.src_buf);
+      BveRel::Origin* org = reinterpret_cast<BveRel::Origin*>(
+          static_cast<char*>(job.src_buf) + align_up(static_cast<size_t>(npad) * sizeof(StreamRel::Rec), 256));
+      const double k2 = 1.0 / (2.0 * kPi * job.radius * job.radius);
+      stream_rel_prep_kernel<kStreamTile><<<static_cast<unsigned>(plan.n_tiles), kStreamTile, 0, job.stream>>>(
+          job.x, job.y, job.z, job.s1, job.s2, job.area, src_list, job.ns, inv_a, job.ib, job.nt, recs, org, nullptr,
+          -k2, k2);
+      SweepArgs<BveF32> a;
+      a.p = BveF32::Params{job.x, job.y, job.z, inv_a};
+      a.n_tiles = plan.n_tiles;
+      a.tiles_per_chunk = plan.tiles_per_chunk;
+      a.ib = job.ib;
+      a.nt = job.nt;
+      a.partial = job.partial;
+      a.status = job.status;
+      const dim3 grid(static_cast<unsigned>(ceil_div(job.nt, kStreamThreads * kStreamTpt)),
+                      static_cast<unsigned>(plan.nsplit));
+      sphere_swe_rel_sweep_kernel<kStreamThreads, kStreamTpt, kStreamTile, kSweSphereMinB>
+          <<<grid, kStreamThreads, 0, job.stream>>>(a, recs, org);
+      swe_sphere_finish_kernel<<<fin_grid, pb, 0, job.stream>>>(job.partial, plan.nsplit, job.nt, job.ib, job.x, job.y,
+                                                                job.z, inv_a, job.out0, job.out1, job.out2);
+      // surface-height Laplacian: K8(SphereDistance / eps) / eps**2 with SphereDistance scaled by
+      // radius2, i.e. the geodesic PSE sweep at eps' = eps a / radius2 on the sphere of radius a
+      SumJob jp = job;
+      jp.kind = kSumPseK8Geo;
+      jp.s1 = job.s3;
+      jp.src_idx = src_list;
+      jp.sort_scratch = nullptr;
+      jp.eps = job.eps * job.radius / job.radius2;
+      jp.src_buf = static_cast<char*>(job.src_buf) + plan.aux_src_offset;
+      SumPlan pp;
+      pp.n_tiles = plan.aux_n_tiles;
+      pp.tiles_per_chunk = plan.aux_tiles_per_chunk;
+      pp.nsplit = plan.aux_nsplit;
+      LPM_TRY(launch_pse_rel(jp, pp, plan.aux_n_tiles * kPseTile));
+      finish_scalar_kernel<<<fin_grid, pb, 0, job.stream>>>(job.partial, pp.nsplit, job.nt,
+                                                            1.0 / (kPi * job.eps * job.eps), job.out3);
       break;
     }
     case kSumSwePlane: {

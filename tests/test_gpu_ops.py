@@ -203,3 +203,29 @@ def test_swe_plane_rhs_fp32c(lg, oracle_mod, nest, frac, block):
     assert err[0] <= FP32C_TOL and err[1] <= FP32C_TOL
     assert err[2] <= 2e-6
     assert err[3] <= 1e-4
+
+
+@pytest.mark.parametrize("nest,radius,sphere_radius,block", [(4, 1.0, 1.0, None), (5, 6.37122e6, 1.0, (50, 20000)),
+                                                             (4, 2.0, 2.0, None)])
+def test_swe_sphere_rhs_fp32c(lg, oracle_mod, nest, radius, sphere_radius, block):
+    """FP32C sphere SWE integrals against the FP64 oracle: velocity (rotational and potential
+    parts in one sweep) to 1e-6 of max|(u, v, w)|, the surface-height Laplacian (the geodesic
+    PSE sweep at eps a / SphereRadius) to the PSE FP32C bound 1e-4, doubleDot 0."""
+    m = lg.PolyMesh2d(205, nest, 1.0)
+    x, y, z = m.x * radius, m.y * radius, m.z * radius
+    area = m.area * radius ** 2
+    zeta = np.exp(-4 * ((m.x - 0.5) ** 2 + m.y ** 2 + (m.z - 0.7) ** 2)) + 0.3 * m.z
+    div = 0.2 * np.cos(3 * m.z) * np.sin(2 * m.x)
+    sh = 1.0 + 0.2 * m.z + 0.05 * m.x * m.y
+    eps = 0.15 * sphere_radius
+    ib, ie = (1, m.n) if block is None else block
+    s = slice(ib - 1, ie)
+    got = lg.swe_sphere_rhs_integrals(x, y, z, zeta, div, sh, area, m.active, radius, eps, sphere_radius, ib, ie,
+                                      mode="fp32c")
+    ref = oracle_mod.swe_sphere_rhs(x, y, z, zeta, div, sh, area, m.active, radius, sphere_radius, eps, ib - 1, ie)
+    vel = max(np.abs(ref[c]).max() for c in range(3))
+    err = [np.abs(got[c][s] - ref[c]).max() / vel for c in range(3)] + [rel(got[4][s], ref[4])]
+    print("swe sphere fp32c errors", err)
+    assert max(err[:3]) <= FP32C_TOL
+    assert np.all(got[3][s] == 0.0)
+    assert err[3] <= 1e-4

@@ -183,8 +183,7 @@ def test_swe_sphere_vs_parts(sphere, oracle_mod):
     assert abs(u2[i] + (m.x * pot)[sel].sum()) <= 1e-12 * np.abs(m.x * pot)[sel].sum()
 
 
-@pytest.mark.parametrize("call", ["plane_grad", "plane_second", "plane_ddot", "sphere_ddot", "swe_sphere",
-                                  "interp"])
+@pytest.mark.parametrize("call", ["plane_grad", "plane_second", "plane_ddot", "sphere_ddot", "interp"])
 def test_fp32c_rejected_for_fp64_only_operators(lg, call):
     n = 4
     x = np.linspace(0.0, 1.0, n)
@@ -196,7 +195,6 @@ def test_fp32c_rejected_for_fp64_only_operators(lg, call):
         "plane_ddot": lambda: lg.pse_plane_double_dot_product_at_particles(x, x, a, a, a, act, 0.1, mode="fp32c"),
         "sphere_ddot": lambda: lg.pse_sphere_double_dot_product_at_particles(x, x, x, a, a, a, a, act, 0.1,
                                                                              mode="fp32c"),
-        "swe_sphere": lambda: lg.swe_sphere_rhs_integrals(x, x, x, a, a, a, a, act, 1.0, 0.1, mode="fp32c"),
         "interp": lambda: lg.pse_interpolate_scalar(x, x, None, a, a, act, 0.1, x[:2], x[:2], mode="fp32c"),
     }[call]
     with pytest.raises(lg.LpmError) as e:
