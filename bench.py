@@ -68,7 +68,7 @@ def parse_args():
                    help="rk4: the headline single-instance step; ensemble: the 64-instance batch")
     p.add_argument("--instances", type=int, default=64)
     p.add_argument("--sum", choices=["bve", "plane", "pse_k8", "pse_gauss", "pse_grad", "pse_div", "pse_plane",
-                                     "stream", "plane_stream", "beta", "swe_plane", "swe_sphere"],
+                                     "stream", "plane_stream", "beta", "beta_stream", "swe_plane", "swe_sphere"],
                    default="bve",
                    help="--workload sum: which direct sum (one host C-ABI call per step)")
     p.add_argument("--mode", choices=["fp32c", "fp64"], default="fp32c", help="--workload sum: precision mode")
@@ -637,6 +637,13 @@ def run_sum(args):
         call = lambda ie: lg.swe_sphere_rhs_integrals(c["x"], c["y"], c["z"], c["zeta"], div, sh, c["area"],
                                                       c["active"], 1.0, eps, 1.0, i_end=ie, mode=args.mode)
         mesh = f"icosahedral nest {args.nest} (RH54 vorticity, divergence, surface Laplacian, eps = 2h)"
+    elif args.sum == "beta_stream":
+        c = wl.config_beta_plane(args.nest)
+        n, ns = c["x"].size, int(c["active"].sum())
+        absv = c["zeta"] + 10.0 * c["y"]
+        call = lambda ie: lg.beta_plane_stream_functions(c["x"], c["y"], c["zeta"], absv, c["area"], c["active"],
+                                                         i_end=ie, mode=args.mode)
+        mesh = f"beta-plane quad nest {args.nest} on [0,1]x[-1/2,1/2]"
     elif args.sum == "beta":
         c = wl.config_beta_plane(args.nest)
         n, ns = c["x"].size, int(c["active"].sum())

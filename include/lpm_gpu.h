@@ -200,7 +200,8 @@ int lpm_beta_plane_velocity(int64_t n, const double* x, const double* y, const d
 
 /* Replaces the beta plane's SetStreamFunctionsOnMesh (src/BetaPlane.f90:399-442):
  * psi = sum_{j != i} log(cosh(2 pi dy) - cos(2 pi dx)) / (4 pi) zeta_j A_j for the relative
- * and the absolute vorticity.  LPM_MODE_FP64 only. */
+ * and the absolute vorticity.  LPM_MODE_FP32C uses the cancellation-free form
+ * log(2 (sinh^2 + sin^2)) of the half angles, <= 1e-6 of max|psi|. */
 int lpm_beta_plane_stream_functions(int64_t n, const double* x, const double* y, const double* relvort,
                                     const double* absvort, const double* area, const int32_t* active,
                                     int64_t i_begin, int64_t i_end, double* psi_rel, double* psi_abs,

@@ -686,15 +686,82 @@ struct BetaStreamF64 {
 // factor 2^(k-1) is divided out of every term (sn, cs scaled by 2^(1-k)), so nothing
 // overflows for any dy.  The self pair (d = 0) has zero numerators and a denominator of
 // 2^-100, a zero term.
+// Shared pieces of the x-periodic kernels, two targets at a time.  A record holds
+// (x_hi, y_hi, x_lo, y_lo) of the source in its first float4.
+struct BetaTgt {
+  float xh, yh, xl, yl;
+};
+
+__device__ __forceinline__ float2 bits_abs(float2 v) {
+  return make_float2(__uint_as_float(__float_as_uint(v.x) & 0x7fffffffu),
+                     __uint_as_float(__float_as_uint(v.y) & 0x7fffffffu));
+}
+
+// t = (x_i - x_j) - rint(x_i - x_j) in [-1/2, 1/2] keeping the rounding of the hi difference
+// (TwoSum), and dy = (y_i - y_j) from the hi/lo parts.
+__device__ __forceinline__ void beta_deltas2(const BetaTgt& t0, const BetaTgt& t1, float4 ra, float2& tt, float2& dy) {
+  const float2 kM = make_float2(12582912.0f, 12582912.0f), kNM = make_float2(-12582912.0f, -12582912.0f);
+  const float2 nxh = make_float2(-ra.x, -ra.x);
+  const float2 txh = make_float2(t0.xh, t1.xh);
+  const float2 dh = __fadd2_rn(txh, nxh);
+  const float2 bb = __fadd2_rn(dh, make_float2(-txh.x, -txh.y));
+  const float2 dv = __fadd2_rn(dh, make_float2(-bb.x, -bb.y));
+  const float2 e = __fadd2_rn(__fadd2_rn(txh, make_float2(-dv.x, -dv.y)), __fadd2_rn(nxh, make_float2(-bb.x, -bb.y)));
+  const float2 nn = __fadd2_rn(__fadd2_rn(dh, kM), kNM);
+  const float2 lo = __fadd2_rn(e, __fadd2_rn(make_float2(t0.xl, t1.xl), make_float2(-ra.z, -ra.z)));
+  tt = __fadd2_rn(__fadd2_rn(dh, make_float2(-nn.x, -nn.y)), lo);
+  dy = __fadd2_rn(__fadd2_rn(make_float2(t0.yh, t1.yh), make_float2(-ra.y, -ra.y)),
+                  __fadd2_rn(make_float2(t0.yl, t1.yl), make_float2(-ra.w, -ra.w)));
+}
+
+// sin(pi t) and cos(pi t), |t| <= 1/2, Taylor polynomials in t^2 (|error| <= 6e-8)
+__device__ __forceinline__ float2 sinpi2(float2 tt, float2 t2) {
+  float2 ps = __ffma2_rn(make_float2(-0.00737043097615242f, -0.00737043097615242f), t2,
+                         make_float2(0.08214588463306427f, 0.08214588463306427f));
+  ps = __ffma2_rn(ps, t2, make_float2(-0.5992645025253296f, -0.5992645025253296f));
+  ps = __ffma2_rn(ps, t2, make_float2(2.550163984298706f, 2.550163984298706f));
+  ps = __ffma2_rn(ps, t2, make_float2(-5.167712688446045f, -5.167712688446045f));
+  ps = __ffma2_rn(ps, t2, make_float2(3.1415927410125732f, 3.1415927410125732f));
+  return __fmul2_rn(ps, tt);
+}
+__device__ __forceinline__ float2 cospi2(float2 t2) {
+  float2 pc = __ffma2_rn(make_float2(0.001929574296809733f, 0.001929574296809733f), t2,
+                         make_float2(-0.025806890800595284f, -0.025806890800595284f));
+  pc = __ffma2_rn(pc, t2, make_float2(0.23533062636852264f, 0.23533062636852264f));
+  pc = __ffma2_rn(pc, t2, make_float2(-1.3352627754211426f, -1.3352627754211426f));
+  pc = __ffma2_rn(pc, t2, make_float2(4.058712005615234f, 4.058712005615234f));
+  pc = __ffma2_rn(pc, t2, make_float2(-4.934802055358887f, -4.934802055358887f));
+  return __ffma2_rn(pc, t2, make_float2(1.0f, 1.0f));
+}
+
+// a = k ln 2 + r, |r| <= ln 2 / 2: sinh r, cosh r (Taylor), and kb = 1.5 2^23 + k (its bits
+// minus those of 1.5 2^23 are k), for a >= 0 below 2^22 ln 2.
+__device__ __forceinline__ void sinh_cosh_reduced2(float2 a, float2& shr, float2& chr, float2& kb) {
+  kb = __ffma2_rn(a, make_float2(1.442695f, 1.442695f), make_float2(12582912.0f, 12582912.0f));
+  const float2 kf = __fadd2_rn(kb, make_float2(-12582912.0f, -12582912.0f));
+  float2 rr = __ffma2_rn(make_float2(-kf.x, -kf.y), make_float2(0.69314575f, 0.69314575f), a);
+  rr = __ffma2_rn(make_float2(-kf.x, -kf.y), make_float2(1.4286068e-06f, 1.4286068e-06f), rr);
+  const float2 r2 = __fmul2_rn(rr, rr);
+  shr = __ffma2_rn(
+      __fmul2_rn(rr, r2),
+      __ffma2_rn(__ffma2_rn(r2, make_float2(1.9841270e-4f, 1.9841270e-4f), make_float2(8.3333333e-3f, 8.3333333e-3f)),
+                 r2, make_float2(0.16666667f, 0.16666667f)),
+      rr);
+  chr = __ffma2_rn(
+      __ffma2_rn(__ffma2_rn(__ffma2_rn(r2, make_float2(2.4801587e-5f, 2.4801587e-5f),
+                                       make_float2(1.3888889e-3f, 1.3888889e-3f)),
+                            r2, make_float2(4.1666667e-2f, 4.1666667e-2f)),
+                 r2, make_float2(0.5f, 0.5f)),
+      r2, make_float2(1.0f, 1.0f));
+}
+
 struct BetaF32 {
   static constexpr int NC = 2;
   struct __align__(16) Rec {
     float4 a;  // x_hi, y_hi, x_lo, y_lo
     float4 b;  // S = zeta A / 2, 0, 0, 0
   };
-  struct Tgt {
-    float xh, yh, xl, yl;
-  };
+  using Tgt = BetaTgt;
   struct Params {
     const double *x, *y;
   };
@@ -709,60 +776,16 @@ struct BetaF32 {
   // to 87 < 126 ln 2: beyond it the terms have reached their limits, u -> S sign(dy), v -> 0);
   // 2^(1-k) = 2^-k + 2^-k and 4^-k = (2^-k)^2, which underflows to 0 for k > 63 as it should.
   static constexpr bool kPairs = true;
-  __device__ static __forceinline__ float2 bits_abs(float2 v) {
-    return make_float2(__int_as_float(__float_as_int(v.x) & 0x7fffffff),
-                       __int_as_float(__float_as_int(v.y) & 0x7fffffff));
-  }
   __device__ static __forceinline__ void interact2(const Tgt& t0, const Tgt& t1, const Rec& r, float (&a0)[2],
                                                    float (&a1)[2]) {
-    const float2 kM = make_float2(12582912.0f, 12582912.0f), kNM = make_float2(-12582912.0f, -12582912.0f);
-    const float2 nxh = make_float2(-r.a.x, -r.a.x);
-    const float2 txh = make_float2(t0.xh, t1.xh);
-    // t = (x_i - x_j) - rint(x_i - x_j), keeping the rounding of the hi difference (TwoSum)
-    const float2 dh = __fadd2_rn(txh, nxh);
-    const float2 bb = __fadd2_rn(dh, make_float2(-txh.x, -txh.y));
-    const float2 dv = __fadd2_rn(dh, make_float2(-bb.x, -bb.y));
-    const float2 e = __fadd2_rn(__fadd2_rn(txh, make_float2(-dv.x, -dv.y)), __fadd2_rn(nxh, make_float2(-bb.x, -bb.y)));
-    const float2 nn = __fadd2_rn(__fadd2_rn(dh, kM), kNM);
-    const float2 lo = __fadd2_rn(e, __fadd2_rn(make_float2(t0.xl, t1.xl), make_float2(-r.a.z, -r.a.z)));
-    const float2 tt = __fadd2_rn(__fadd2_rn(dh, make_float2(-nn.x, -nn.y)), lo);
-    const float2 dy = __fadd2_rn(__fadd2_rn(make_float2(t0.yh, t1.yh), make_float2(-r.a.y, -r.a.y)),
-                                 __fadd2_rn(make_float2(t0.yl, t1.yl), make_float2(-r.a.w, -r.a.w)));
-    // sin(pi t), cos(pi t)
+    float2 tt, dy;
+    beta_deltas2(t0, t1, r.a, tt, dy);
     const float2 t2 = __fmul2_rn(tt, tt);
-    float2 ps = __ffma2_rn(make_float2(-0.00737043097615242f, -0.00737043097615242f), t2,
-                           make_float2(0.08214588463306427f, 0.08214588463306427f));
-    ps = __ffma2_rn(ps, t2, make_float2(-0.5992645025253296f, -0.5992645025253296f));
-    ps = __ffma2_rn(ps, t2, make_float2(2.550163984298706f, 2.550163984298706f));
-    ps = __ffma2_rn(ps, t2, make_float2(-5.167712688446045f, -5.167712688446045f));
-    ps = __ffma2_rn(ps, t2, make_float2(3.1415927410125732f, 3.1415927410125732f));
-    const float2 sn = __fmul2_rn(ps, tt);
-    float2 pc = __ffma2_rn(make_float2(0.001929574296809733f, 0.001929574296809733f), t2,
-                           make_float2(-0.025806890800595284f, -0.025806890800595284f));
-    pc = __ffma2_rn(pc, t2, make_float2(0.23533062636852264f, 0.23533062636852264f));
-    pc = __ffma2_rn(pc, t2, make_float2(-1.3352627754211426f, -1.3352627754211426f));
-    pc = __ffma2_rn(pc, t2, make_float2(4.058712005615234f, 4.058712005615234f));
-    pc = __ffma2_rn(pc, t2, make_float2(-4.934802055358887f, -4.934802055358887f));
-    const float2 cs = __ffma2_rn(pc, t2, make_float2(1.0f, 1.0f));
-    // sinh, cosh of a = pi |dy| as 2^(k-1) (sh', ch')
+    const float2 sn = sinpi2(tt, t2), cs = cospi2(t2);
     float2 a = __fmul2_rn(make_float2(3.1415927f, 3.1415927f), bits_abs(dy));
     a = make_float2(fminf(a.x, 87.0f), fminf(a.y, 87.0f));
-    const float2 kb = __ffma2_rn(a, make_float2(1.442695f, 1.442695f), kM);
-    const float2 kf = __fadd2_rn(kb, kNM);
-    float2 rr = __ffma2_rn(make_float2(-kf.x, -kf.y), make_float2(0.69314575f, 0.69314575f), a);
-    rr = __ffma2_rn(make_float2(-kf.x, -kf.y), make_float2(1.4286068e-06f, 1.4286068e-06f), rr);
-    const float2 r2 = __fmul2_rn(rr, rr);
-    const float2 shr = __ffma2_rn(
-        __fmul2_rn(rr, r2),
-        __ffma2_rn(__ffma2_rn(r2, make_float2(1.9841270e-4f, 1.9841270e-4f), make_float2(8.3333333e-3f, 8.3333333e-3f)),
-                   r2, make_float2(0.16666667f, 0.16666667f)),
-        rr);
-    const float2 chr = __ffma2_rn(
-        __ffma2_rn(__ffma2_rn(__ffma2_rn(r2, make_float2(2.4801587e-5f, 2.4801587e-5f),
-                                         make_float2(1.3888889e-3f, 1.3888889e-3f)),
-                              r2, make_float2(4.1666667e-2f, 4.1666667e-2f)),
-                   r2, make_float2(0.5f, 0.5f)),
-        r2, make_float2(1.0f, 1.0f));
+    float2 shr, chr, kb;
+    sinh_cosh_reduced2(a, shr, chr, kb);
     // 2^-k: 0x3f800000 - (k << 23) with k = bits(kb) - bits(kM) (bits(kM) << 23 vanishes mod 2^32)
     const float2 pk = make_float2(__uint_as_float(0x3f800000u - (__float_as_uint(kb.x) << 23)),
                                   __uint_as_float(0x3f800000u - (__float_as_uint(kb.y) << 23)));

@@ -560,4 +560,55 @@ __global__ void __launch_bounds__(THREADS, MINB) sphere_swe_rel_sweep_kernel(Swe
   }
 }
 
+// ====================================================================== beta-plane stream functions
+// The beta plane's SetStreamFunctionsOnMesh, src/BetaPlane.f90:399-442, in FP32 for two
+// targets at a time on the generic hi/lo engine:
+//   G = log(cosh(2 pi dy) - cos(2 pi dx)) / (4 pi),  psi += G zeta_j A_j  (j != i).
+// cosh 2a - cos 2b = 2 (sinh^2 a + sin^2 b) = 2 4^(k-1) (sh'^2 + sn'^2) with a = pi |dy| =
+// k ln 2 + r, b = pi dx and the 2^(k-1)-scaled sh', sn' of BetaF32, so
+//   4 pi G = (2k - 1) ln 2 + ln(sh'^2 + sn'^2),
+// no cancellation for close pairs and no overflow for far ones; the (2k - 1) ln 2 rides on the
+// exponent of ln_q2_shift.  S = zeta A / (4 pi); the self pair (sh' = sn' = 0) is a zero term.
+// Terms of both signs cancel to psi, so the FP32 partials are flushed every 32 sources.
+struct BetaStreamF32 {
+  static constexpr int NC = 2;
+  static constexpr int kFlush = 32;
+  static constexpr bool kPairs = true;
+  struct __align__(16) Rec {
+    float4 a;  // x_hi, y_hi, x_lo, y_lo
+    float4 b;  // S_rel, S_abs, 0, 0
+  };
+  using Tgt = BetaTgt;
+  using Params = BetaF32::Params;
+  __device__ static Tgt load_target(const Params& p, int64_t i) { return BetaF32::load_target(p, i); }
+  __device__ static __forceinline__ void interact2(const Tgt& t0, const Tgt& t1, const Rec& r, float (&a0)[2],
+                                                   float (&a1)[2]) {
+    float2 tt, dy;
+    beta_deltas2(t0, t1, r.a, tt, dy);
+    const float2 sn = sinpi2(tt, __fmul2_rn(tt, tt));
+    const float2 a = __fmul2_rn(make_float2(3.1415927f, 3.1415927f), bits_abs(dy));
+    float2 shr, chr, kb;
+    sinh_cosh_reduced2(a, shr, chr, kb);
+    const int k0 = static_cast<int>(__float_as_uint(kb.x) - 0x4b400000u);
+    const int k1 = static_cast<int>(__float_as_uint(kb.y) - 0x4b400000u);
+    const unsigned c0 = static_cast<unsigned>(k0 < 126 ? k0 : 126), c1 = static_cast<unsigned>(k1 < 126 ? k1 : 126);
+    const float2 pk = make_float2(__uint_as_float(0x3f800000u - (c0 << 23)), __uint_as_float(0x3f800000u - (c1 << 23)));
+    const float2 sc = __fadd2_rn(pk, pk);
+    const float2 q = __fmul2_rn(pk, pk);
+    const float2 shp = __ffma2_rn(__fadd2_rn(make_float2(1.0f, 1.0f), make_float2(-q.x, -q.y)), chr,
+                                  __fmul2_rn(__fadd2_rn(make_float2(1.0f, 1.0f), q), shr));
+    const float2 snp = __fmul2_rn(sn, sc);
+    const float2 x = __ffma2_rn(shp, shp, __fmul2_rn(snp, snp));
+    const float2 lg = ln_q2_shift(make_float2(x.x > 0.f ? x.x : 1.0f, x.y > 0.f ? x.y : 1.0f),
+                                  shift_bias(1 - 2 * k0, 1 - 2 * k1));
+    const float2 g = make_float2(x.x > 0.f ? lg.x : 0.f, x.y > 0.f ? lg.y : 0.f);
+    const float2 pr = __ffma2_rn(make_float2(r.b.x, r.b.x), g, make_float2(a0[0], a1[0]));
+    const float2 pa = __ffma2_rn(make_float2(r.b.y, r.b.y), g, make_float2(a0[1], a1[1]));
+    a0[0] = pr.x;
+    a1[0] = pr.y;
+    a0[1] = pa.x;
+    a1[1] = pa.y;
+  }
+};
+
 }  // namespace lpm

@@ -185,6 +185,29 @@ __global__ void prep_beta32_kernel(const double* x, const double* y, const doubl
   out[k] = r;
 }
 
+__global__ void prep_beta_stream32_kernel(const double* x, const double* y, const double* qr, const double* qa,
+                                          const double* area, const int32_t* idx, int64_t ns, int64_t npad,
+                                          BetaStreamF32::Rec* out) {
+  const int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= npad) return;
+  BetaStreamF32::Rec r;
+  if (k < ns) {
+    const int64_t j = idx[k];
+    float h, l;
+    split2(x[j], h, l);
+    r.a.x = h;
+    r.a.z = l;
+    split2(y[j], h, l);
+    r.a.y = h;
+    r.a.w = l;
+    r.b = make_float4(__double2float_rn(qr[j] * area[j] * kInv4Pi), __double2float_rn(qa[j] * area[j] * kInv4Pi),
+                      0.f, 0.f);
+  } else {
+    r.a = r.b = make_float4(0.f, 0.f, 0.f, 0.f);  // zero strength
+  }
+  out[k] = r;
+}
+
 // ------------------------------------------------------------------ finish kernels
 // Fixed-order FP64 reduction over the split-K chunks, then the per-target epilogue.
 
@@ -332,6 +355,8 @@ size_t rec_bytes(int kind, int mode) {
       return sizeof(PlaneRel::Rec);
     case kSumBetaPlane:
       return sizeof(BetaF32::Rec);
+    case kSumBetaStream:
+      return sizeof(BetaStreamF32::Rec);
     case kSumSwePlane:
       return sizeof(PlaneRel::Rec);
     case kSumPseK8Geo:
@@ -352,6 +377,7 @@ int comps_of(int kind) {
     case kSumPlane:
     case kSumSphereStream:
     case kSumBetaPlane:
+    case kSumBetaStream:
       return 2;
     case kSumPseGrad:
       return 3;
@@ -974,6 +1000,16 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
       LPM_TRY(launch_pse_rel(jp, pp, plan.aux_n_tiles * kPseTile));
       finish_scalar_kernel<<<fin_grid, pb, 0, job.stream>>>(job.partial, pp.nsplit, job.nt,
                                                             1.0 / (kPi * job.eps * job.eps), job.out3);
+      break;
+    }
+    case kSumBetaStream: {
+      prep_beta_stream32_kernel<<<prep_grid_pad, pb, 0, job.stream>>>(job.x, job.y, job.s1, job.s2, job.area,
+                                                                      job.src_idx, job.ns, npad,
+                                                                      static_cast<BetaStreamF32::Rec*>(job.src_buf));
+      launch_sweep<BetaStreamF32, kPseThreads, kPseTpt, kPseTile, kPseMinB>(job, plan,
+                                                                              BetaF32::Params{job.x, job.y});
+      finish_stream_kernel<<<fin_grid, pb, 0, job.stream>>>(job.partial, plan.nsplit, job.nt, 2, 0.0, nullptr, nullptr,
+                                                            job.out0, job.out1);
       break;
     }
     case kSumSwePlane: {

@@ -47,7 +47,7 @@ enum SumKind : int {
 
 // Kinds that have only the FP64 form.
 inline bool sum_is_fp64_only(int kind) {
-  return (kind >= kSumPsePlaneGrad && kind <= kSumPseInterpSphere) || kind == kSumBetaStream;
+  return kind >= kSumPsePlaneGrad && kind <= kSumPseInterpSphere;
 }
 
 // Inputs of one direct sum over particles [0, n): sources are the ns particles listed (in

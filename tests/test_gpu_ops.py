@@ -229,3 +229,23 @@ def test_swe_sphere_rhs_fp32c(lg, oracle_mod, nest, radius, sphere_radius, block
     assert max(err[:3]) <= FP32C_TOL
     assert np.all(got[3][s] == 0.0)
     assert err[3] <= 1e-4
+
+
+@pytest.mark.parametrize("n,frac,spread", [(1000, 0.8, 0.5), (4099, 1.0, 0.5), (3000, 0.9, 3.0)])
+def test_beta_plane_stream_fp32c(lg, oracle_mod, n, frac, spread):
+    """FP32C beta-plane stream functions against the oracle, to 1e-6 of max|psi|, with
+    neighbours across the periodic boundary and positions shifted by whole periods."""
+    rng = np.random.default_rng(n + 7)
+    x, y = rng.random(n), rng.uniform(-spread, spread, n)
+    x[:50] = np.mod(rng.normal(0.0, 1e-3, 50), 1.0)
+    y[:50] = rng.normal(0.0, 1e-3, 50)
+    x[50:80] += rng.integers(-3, 4, 30)
+    area = rng.uniform(0.5, 1.5, n) / n
+    zeta = np.sin(2 * np.pi * x) * np.exp(-4 * y * y)
+    absv = zeta + 5.0 * y
+    act = (rng.random(n) < frac).astype(np.int32)
+    pr, pa = lg.beta_plane_stream_functions(x, y, zeta, absv, area, act, mode="fp32c")
+    rr, ra = oracle_mod.beta_plane_stream(x, y, zeta, absv, area, act)
+    err = (rel(pr, rr), rel(pa, ra))
+    print("beta stream fp32c", err)
+    assert max(err) <= FP32C_TOL
