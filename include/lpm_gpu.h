@@ -292,6 +292,12 @@ int lpm_plane_solver_create(lpm_plane_solver** solver, int64_t n, const double* 
 int lpm_plane_timestep(lpm_plane_solver* solver, double dt, int n_steps);
 int lpm_plane_get_state(lpm_plane_solver* solver, double* x, double* y, double* u,
                         double* v);
+/* The planar counterpart of lpm_bve_solver_remesh (the Delete + New of the solver after a
+ * remesh in examples/CollidingDipoles.f90): loads a new particle set into the solver,
+ * reusing its device buffers when the set fits them. */
+int lpm_plane_solver_remesh(lpm_plane_solver* solver, int64_t n, const double* x, const double* y,
+                            const double* omega, const double* area, const int32_t* active,
+                            const double* u, const double* v);
 int lpm_plane_diagnostics(lpm_plane_solver* solver, double* kinetic_energy,
                           double* enstrophy, double* circulation);
 int lpm_plane_solver_destroy(lpm_plane_solver* solver);

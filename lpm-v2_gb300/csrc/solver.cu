@@ -778,6 +778,7 @@ struct lpm_plane_solver {
   cudaStream_t stream = nullptr;
   DeviceArena arena;
   int64_t n = 0, ns = 0;
+  int64_t cap_n = 0, cap_ns = 0;  // particles and sources the buffers hold
   int mode = LPM_MODE_FP64;
   double delta = 0.0;
   double *x, *y, *om, *u, *v, *area, *ax, *ay, *xin, *yin, *us, *vs;
@@ -883,24 +884,16 @@ struct lpm_plane_solver {
 };
 
 namespace {
-int plane_create(lpm_plane_solver* S, int64_t n, const double* x, const double* y, const double* om,
-                 const double* area, const int32_t* active, const double* u, const double* v, double delta,
-                 int mode) {
-  LPM_TRY(get_context(&S->ctx));
-  S->n = n;
-  S->mode = mode;
-  S->delta = delta;
-  LPM_CUDA_TRY(cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking));
+// Device buffers for up to ncap particles and nscap sources.
+int plane_alloc(lpm_plane_solver* S, int64_t ncap, int64_t nscap) {
   double** arrs[] = {&S->x, &S->y, &S->om, &S->u, &S->v, &S->area, &S->ax, &S->ay, &S->xin, &S->yin, &S->us, &S->vs};
   for (double** a : arrs) {
     void* p = nullptr;
-    LPM_TRY(S->arena.alloc(n * sizeof(double), &p));
+    LPM_TRY(S->arena.alloc(ncap * sizeof(double), &p));
     *a = static_cast<double*>(p);
   }
-  const std::vector<int32_t> idx = active_list(n, active);
-  S->ns = static_cast<int64_t>(idx.size());
   void* p = nullptr;
-  LPM_TRY(S->arena.alloc(idx.size() * sizeof(int32_t), &p));
+  LPM_TRY(S->arena.alloc((nscap > 0 ? nscap : 1) * sizeof(int32_t), &p));
   S->idx = static_cast<int32_t*>(p);
   LPM_TRY(S->arena.alloc(sizeof(int), &p));
   S->status = static_cast<int*>(p);
@@ -908,29 +901,57 @@ int plane_create(lpm_plane_solver* S, int64_t n, const double* x, const double* 
   S->diag_part = static_cast<double*>(p);
   LPM_TRY(S->arena.alloc(4 * sizeof(double), &p));
   S->diag_out = static_cast<double*>(p);
-  LPM_CUDA_TRY(cudaMallocHost(&S->h_status, sizeof(int)));
+  LPM_TRY(S->scratch.init(S->arena, kSumPlane, S->mode, nscap, ncap, S->ctx->sm_count));
+  S->sort_scratch = nullptr;
+  S->sorted = nullptr;
+  S->sort_bytes = 0;
+  if (nscap > 0 && sum_uses_sorted_sources(kSumPlane, S->mode)) {
+    S->sort_bytes = curve_sort2d_bytes(nscap);
+    LPM_TRY(S->arena.alloc(S->sort_bytes, &S->sort_scratch));
+    LPM_TRY(S->arena.alloc(nscap * sizeof(int32_t), &p));
+    S->sorted = static_cast<int32_t*>(p);
+  }
+  S->cap_n = ncap;
+  S->cap_ns = nscap;
+  return LPM_OK;
+}
+
+// Loads a particle set into buffers that hold it (uploads, source list and order, plan, and
+// the initial velocity when u, v are NULL).
+int plane_load(lpm_plane_solver* S, int64_t n, const std::vector<int32_t>& idx, const double* x, const double* y,
+               const double* om, const double* area, const double* u, const double* v) {
+  S->n = n;
+  S->ns = static_cast<int64_t>(idx.size());
   LPM_CUDA_TRY(cudaMemsetAsync(S->status, 0, sizeof(int), S->stream));
   if (!idx.empty()) {
     LPM_CUDA_TRY(cudaMemcpyAsync(S->idx, idx.data(), idx.size() * sizeof(int32_t), cudaMemcpyHostToDevice, S->stream));
   }
-  LPM_TRY(S->scratch.init(S->arena, kSumPlane, mode, S->ns, n, S->ctx->sm_count));
-  if (S->ns > 0 && sum_uses_sorted_sources(kSumPlane, mode)) {
-    S->sort_bytes = curve_sort2d_bytes(S->ns);
-    LPM_TRY(S->arena.alloc(S->sort_bytes, &S->sort_scratch));
-    LPM_TRY(S->arena.alloc(S->ns * sizeof(int32_t), &p));
-    S->sorted = static_cast<int32_t*>(p);
-  }
+  LPM_TRY(S->scratch.fit(S->arena, kSumPlane, S->mode, S->ns, n, S->ctx->sm_count));
   LPM_TRY(upload(S->stream, S->x, x, n));
   LPM_TRY(upload(S->stream, S->y, y, n));
   LPM_TRY(upload(S->stream, S->om, om, n));
   LPM_TRY(upload(S->stream, S->area, area, n));
-  if (S->sorted) LPM_TRY(S->sort_sources());
+  if (S->sorted && S->ns > 0) LPM_TRY(S->sort_sources());
   if (u && v) {
     LPM_TRY(upload(S->stream, S->u, u, n));
     LPM_TRY(upload(S->stream, S->v, v, n));
   } else {
     LPM_TRY(S->velocity(S->x, S->y, S->u, S->v));
   }
+  return LPM_OK;
+}
+
+int plane_create(lpm_plane_solver* S, int64_t n, const double* x, const double* y, const double* om,
+                 const double* area, const int32_t* active, const double* u, const double* v, double delta,
+                 int mode) {
+  LPM_TRY(get_context(&S->ctx));
+  S->mode = mode;
+  S->delta = delta;
+  LPM_CUDA_TRY(cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking));
+  LPM_CUDA_TRY(cudaMallocHost(&S->h_status, sizeof(int)));
+  const std::vector<int32_t> idx = active_list(n, active);
+  LPM_TRY(plane_alloc(S, n, static_cast<int64_t>(idx.size())));
+  LPM_TRY(plane_load(S, n, idx, x, y, om, area, u, v));
   return S->check_status("lpm_plane_solver_create");
 }
 }  // namespace
@@ -973,6 +994,33 @@ extern "C" int lpm_plane_get_state(lpm_plane_solver* S, double* x, double* y, do
   LPM_TRY(download(S->stream, u, S->u, S->n));
   LPM_TRY(download(S->stream, v, S->v, S->n));
   return S->check_status("lpm_plane_get_state");
+}
+
+extern "C" int lpm_plane_solver_remesh(lpm_plane_solver* S, int64_t n, const double* x, const double* y,
+                                       const double* omega, const double* area, const int32_t* active,
+                                       const double* u, const double* v) {
+  if (!S) return set_error(LPM_ERR_ARG, "null solver");
+  if (n <= 0) return set_error(LPM_ERR_ARG, "n must be positive");
+  if (!x || !y || !omega || !area || !active) return set_error(LPM_ERR_ARG, "null input array");
+  if ((u == nullptr) != (v == nullptr)) return set_error(LPM_ERR_ARG, "u and v must be both given or both NULL");
+  LPM_CUDA_TRY(cudaStreamSynchronize(S->stream));
+  if (S->exec) cudaGraphExecDestroy(S->exec);
+  if (S->graph) cudaGraphDestroy(S->graph);
+  S->exec = nullptr;
+  S->graph = nullptr;
+  const std::vector<int32_t> idx = active_list(n, active);
+  const int64_t ns = static_cast<int64_t>(idx.size());
+  if (n > S->cap_n || ns > S->cap_ns) {
+    S->arena.release();  // grow with 1/8 headroom
+    S->mask = nullptr;
+    S->scratch = SumScratch();
+    LPM_TRY(plane_alloc(S, n + n / 8, ns + ns / 8));
+  } else {
+    S->arena.free(S->mask);
+    S->mask = nullptr;
+  }
+  LPM_TRY(plane_load(S, n, idx, x, y, omega, area, u, v));
+  return S->check_status("lpm_plane_solver_remesh");
 }
 
 extern "C" int lpm_plane_diagnostics(lpm_plane_solver* S, double* ke, double* en, double* ci) {

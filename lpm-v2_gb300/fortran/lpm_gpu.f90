@@ -26,6 +26,7 @@ public :: lpm_pse_plane_gradient, lpm_pse_plane_second_partials, lpm_pse_plane_d
 public :: lpm_pse_sphere_double_dot, lpm_pse_interpolate_scalar
 public :: lpm_swe_plane_rhs_integrals, lpm_swe_sphere_rhs_integrals
 public :: lpm_beta_plane_velocity, lpm_beta_plane_stream_functions, lpm_bve_solver_remesh
+public :: lpm_plane_solver_remesh
 public :: lpm_bve_solver_create, lpm_bve_timestep, lpm_bve_get_state, lpm_bve_set_state
 public :: lpm_bve_diagnostics, lpm_bve_solver_stream_functions, lpm_bve_solver_destroy
 public :: lpm_plane_solver_create, lpm_plane_timestep, lpm_plane_get_state, lpm_plane_diagnostics
@@ -234,6 +235,16 @@ interface
 		integer(c_int64_t), value :: i_begin, i_end
 		real(c_double), intent(inout) :: u(*), v(*), w(*), double_dot(*), lap_surf(*)
 		integer(c_int), value :: mode
+	end function
+
+	integer(c_int) function lpm_plane_solver_remesh(solver, n, x, y, omega, area, active, u, v) &
+			bind(C, name="lpm_plane_solver_remesh")
+		import :: c_int, c_int32_t, c_int64_t, c_double, c_ptr
+		type(c_ptr), value :: solver
+		integer(c_int64_t), value :: n
+		real(c_double), intent(in) :: x(*), y(*), omega(*), area(*)
+		integer(c_int32_t), intent(in) :: active(*)
+		type(c_ptr), value :: u, v
 	end function
 
 	integer(c_int) function lpm_bve_solver_remesh(solver, n, x, y, z, relvort, area, active, u, v, w) &

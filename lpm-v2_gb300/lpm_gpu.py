@@ -92,6 +92,7 @@ _SIGNATURES = {
     "lpm_bve_solver_destroy": [_vp],
     "lpm_measure_fp32_peak": [_dbl, _D],
     "lpm_plane_solver_create": [_pvp, _i64, _D, _D, _D, _D, _I, _D, _D, _dbl, _int],
+    "lpm_plane_solver_remesh": [_vp, _i64, _D, _D, _D, _D, _I, _D, _D],
     "lpm_plane_timestep": [_vp, _dbl, _int],
     "lpm_plane_get_state": [_vp, _D, _D, _D, _D],
     "lpm_plane_diagnostics": [_vp, _D, _D, _D],
@@ -529,6 +530,16 @@ class PlaneSolver:
         out = [np.empty(self.n) for _ in range(4)]
         _check(lib().lpm_plane_get_state(self._h, *(_dp(a) for a in out)))
         return dict(zip(("x", "y", "u", "v"), out))
+
+    def remesh(self, x, y, vort, area, active_mask, u=None, v=None):
+        """Loads a remeshed particle set in place of Delete(solver) + New(solver, plane)."""
+        arrs = [_f64(a) for a in (x, y, vort, area)]
+        act = _i32(active_mask)
+        uv = [None if a is None else _f64(a) for a in (u, v)]
+        _check(lib().lpm_plane_solver_remesh(self._h, arrs[0].size, *(_dp(a) for a in arrs), _ip(act),
+                                             *(_dp(a) for a in uv)))
+        self.n = arrs[0].size
+        self._keep = arrs
 
     def diagnostics(self):
         ke, en, ci = _dbl(), _dbl(), _dbl()

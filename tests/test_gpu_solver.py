@@ -190,3 +190,23 @@ def test_bve_remesh_in_place_matches_new_solver(lg, wl, mode):
         assert np.array_equal(p1[0], p2[0]) and np.array_equal(p1[1], p2[1])
         fresh.close()
     s.close()
+
+
+@pytest.mark.parametrize("mode", ["fp64", "fp32c"])
+def test_plane_remesh_in_place_matches_new_solver(lg, wl, mode):
+    """lpm_plane_solver_remesh through growth and reuse: the state after a remesh and a few
+    steps is that of a newly created solver on the same particle set."""
+    a, b, c = (wl.config_colliding_dipoles(k) for k in (4, 5, 3))
+    s = lg.PlaneSolver(a["x"], a["y"], a["omega"], a["area"], a["active"], mode=mode)
+    s.timestep(0.005, 2)
+    for cfg in (b, c, b):
+        s.remesh(cfg["x"], cfg["y"], cfg["omega"], cfg["area"], cfg["active"])
+        fresh = lg.PlaneSolver(cfg["x"], cfg["y"], cfg["omega"], cfg["area"], cfg["active"], mode=mode)
+        s.timestep(0.005, 3)
+        fresh.timestep(0.005, 3)
+        st, sf = s.get_state(), fresh.get_state()
+        for k in st:
+            assert np.array_equal(st[k], sf[k]), k
+        assert s.diagnostics() == fresh.diagnostics()
+        fresh.close()
+    s.close()
