@@ -163,7 +163,7 @@ int lpm_pse_interpolate_scalar(int64_t n, const double* x, const double* y, cons
                                double radius, int geometry, int64_t m, const double* qx,
                                const double* qy, const double* qz, double* out, int mode);
 
-/* Replaces SWEPlaneRHSIntegrals (src/SWEPlaneSolver.f90:457-534): velocity (u, v) from
+/* Replaces SWEPlaneRHSIntegrals (src/SWEPlaneSolver.f90:457-571): velocity (u, v) from
  * vorticity and divergence, the double dot product of the velocity gradient and the PSE
  * Laplacian of the surface height.  surf_height = h + topoFn(x, y), evaluated by the caller
  * (the Fortran shim) once per particle.  LPM_MODE_FP32C: velocity <= 1e-6 of max|u|, double

@@ -535,7 +535,7 @@ struct PseInterpF64 {
   static constexpr bool kSkipSelf = false;
 };
 
-// SWEPlaneRHSIntegrals, src/SWEPlaneSolver.f90:457-534 (RecVec64: vx = vort_j, vy = div_j,
+// SWEPlaneRHSIntegrals, src/SWEPlaneSolver.f90:457-571 (RecVec64: vx = vort_j, vy = div_j,
 // vz = sh_j, the surface height h + topoFn).  The Laplacian term includes j = i (a zero
 // term); the rest skips it, as the reference's `cycle` does.
 struct SwePlaneF64 {

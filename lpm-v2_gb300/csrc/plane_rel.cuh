@@ -479,7 +479,7 @@ __global__ void __launch_bounds__(TILE) plane_pse_rel_prep_kernel(const double* 
 }
 
 // ====================================================================== planar SWE integrals
-// SWEPlaneRHSIntegrals, src/SWEPlaneSolver.f90:457-534, velocity and velocity-gradient part
+// SWEPlaneRHSIntegrals, src/SWEPlaneSolver.f90:457-571, velocity and velocity-gradient part
 // (the surface-height Laplacian is the planar PSE sweep above).  With W = vort_j A_j / (2 pi),
 // D = div_j A_j / (2 pi) (records: b.xy = W, c.zw = D) and s = 1/r^2, the reference's terms are
 //   u += s P, v += s Q,  P = D dx - W dy, Q = W dx + D dy,

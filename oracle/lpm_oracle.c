@@ -592,7 +592,7 @@ void lpmo_pse_interpolate(int64_t n, const double* x, const double* y, const dou
 }
 
 /*
- * SWEPlaneRHSIntegrals, src/SWEPlaneSolver.f90:457-534, with the surface height
+ * SWEPlaneRHSIntegrals, src/SWEPlaneSolver.f90:457-571, with the surface height
  * sh = h + topoFn(x, y) evaluated by the caller.  Per active j:
  *   lapSurf += K8(r/eps)/eps**2 (sh_j - sh_i) A_j      (j = i included: a zero term)
  * and for j != i, with r^2 = dx^2 + dy^2, denom = 2 pi r^2, denom2 = pi r^4,

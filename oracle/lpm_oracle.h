@@ -123,7 +123,7 @@ void lpmo_pse_interpolate(int64_t n, const double* x, const double* y, const dou
                           int64_t m, const double* qx, const double* qy, const double* qz, double* out,
                           int nthreads);
 
-/* SWEPlaneRHSIntegrals, SWEPlaneSolver.f90:457-534 (sh = h + topoFn(x, y)) */
+/* SWEPlaneRHSIntegrals, SWEPlaneSolver.f90:457-571 (sh = h + topoFn(x, y)) */
 void lpmo_swe_plane_rhs(int64_t n, const double* x, const double* y, const double* vort, const double* div,
                         const double* sh, const double* area, const int32_t* active, double eps, int64_t ib,
                         int64_t ie, double* u, double* v, double* ddot, double* lap, int nthreads);

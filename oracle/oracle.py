@@ -211,7 +211,7 @@ def pse_interpolate(x, y, z, f, area, active, eps, qx, qy, qz, geometry, radius=
 
 
 def swe_plane_rhs(x, y, vort, div, sh, area, active, eps, ib=None, ie=None, threads=0):
-    """SWEPlaneRHSIntegrals (src/SWEPlaneSolver.f90:457-534); returns (u, v, doubleDot, lapSurf)."""
+    """SWEPlaneRHSIntegrals (src/SWEPlaneSolver.f90:457-571); returns (u, v, doubleDot, lapSurf)."""
     x, y, vort, div, sh, area, active = (_f64(x), _f64(y), _f64(vort), _f64(div), _f64(sh), _f64(area),
                                          _i32(active))
     n = x.size

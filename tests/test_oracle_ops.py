@@ -1,5 +1,5 @@
 """CPU tests of the oracle's remaining PSE operators and shallow-water integrals
-(src/PSEDirectSum.f90:128-456, src/SWEPlaneSolver.f90:457-534, src/SphereSWESolver.f90:299-372):
+(src/PSEDirectSum.f90:128-456, src/SWEPlaneSolver.f90:457-571, src/SphereSWESolver.f90:299-372):
 known answers for the planar PSE operators, cross-checks of the sphere double dot product and
 the SWE integrals against independent numpy restatements and against the velocity and
 Laplacian sums they contain, and the C ABI's refusal of LPM_MODE_FP32C for them."""
