@@ -28,10 +28,17 @@
 // spacing; always the case once positions are renormalised) drops c_j: q is then
 // fma(dz,dz, fma(dy,dy, fma(dx,dx, -c_i))), one operation less per pair.
 // Then  q = |d|^2 - c_i - c_j,  w = S_j / q,  D += w d  with c = |p|^2 - 1 and
-// S_j = -zeta_j A_j / (2 pi a) as in BveF32; u = D x p_i in FP64.  Far: 10 packed FP32x2
-// operations per target pair and source on the sphere (11 off it); near: 17.  Forming the
-// targets' offsets and the near test cost about 15 per pair and group (33 more for a near
-// group).
+// S_j = -zeta_j A_j / (2 pi a) as in BveF32; u = D x p_i in FP64.
+// A group whose warp is far (every target at |t - o| >= 3R, compact or not) takes the
+// expanded form: with B_j = |s_j|^2 - c_j and S_j s_j stored per source,
+//   q/2 = (|t|^2 - c_i)/2 + B_j/2 - t.s_j,  W = sum_j S_j / (q/2),  V = sum_j S_j s_j / (q/2),
+//   D += (t W - V) / 2  (once per group),
+// 8 packed FP32x2 operations and 2 MUFU per target pair and source: the FMA and MUFU pipes
+// are then about equally loaded.  |t|^2 + |s|^2 - 2 t.s cancels by at most
+// ((|t| + R) / (|t| - R))^2 <= 4 at the 3R boundary, so q stays within a few ulps.  A compact
+// group with a target of the warp near it keeps d = t_hi - s_hi (10-11 operations; it
+// contains the self pairs), any other near group the two-float form (17).  Forming the
+// targets' offsets and the near test cost about 15 per pair and group.
 // Targets keep their original order (only sources are sorted), so no scatter is needed.
 #pragma once
 
@@ -44,12 +51,13 @@ namespace lpm {
 struct BveRel {
   struct __align__(16) Rec {
     float4 a;  // -sx_hi, -sx_hi, -sy_hi, -sy_hi
-    float4 b;  // -sz_hi, -sz_hi, -c_j, -c_j
-    float4 c;  // S_j, S_j, -sz_lo, -sz_lo
-    float4 d;  // -sx_lo, -sx_lo, -sy_lo, -sy_lo
+    float4 b;  // -sz_hi, -sz_hi, S_j, S_j
+    float4 c;  // B_j / 2, B_j / 2, -S_j sx_hi, -S_j sx_hi   (B_j = |s_hi|^2 - c_j)
+    float4 d;  // -S_j sy_hi, -S_j sy_hi, -S_j sz_hi, -S_j sz_hi
+    float4 e;  // -sx_lo, -sy_lo, -sz_lo, -c_j             (near and compact-near forms)
   };
   struct __align__(16) Origin {
-    float4 hi;  // o_hi.x, o_hi.y, o_hi.z, R (the group radius about o)
+    float4 hi;  // o_hi.x, o_hi.y, o_hi.z, R (the group radius about o; -R for a compact group)
     float4 lo;  // o_lo.x, o_lo.y, o_lo.z, 1 if every c_j of the group is negligible
   };
   static constexpr int kGroup = 64;           // sources per origin
@@ -152,14 +160,47 @@ __device__ __forceinline__ void bve_rel_tile(const BveRel::Rec* __restrict__ tl,
       ty[p] = rel1x2(pr[p].yh, pr[p].yl, o.hi.y, o.lo.y);
       tz[p] = rel1x2(pr[p].zh, pr[p].zl, o.hi.z, o.lo.z);
     }
-    if (o.hi.w == 0.f || !warp_near<NP>(tx, ty, tz, o.hi.w)) {  // R = 0: compact, never near
-      // far group: d = t_hi - s_hi
+    if (!warp_near<NP>(tx, ty, tz, fabsf(o.hi.w))) {
+      // far group, expanded form: h = q/2 = (|t|^2 - c_i)/2 + B_j/2 - t.s_j, D += (t W - V)/2
+      float2 ct[NP], ww[NP], vx[NP], vy[NP], vz[NP];
+#pragma unroll
+      for (int p = 0; p < NP; ++p) {
+        ct[p] = __fmul2_rn(__ffma2_rn(tz[p], tz[p], __ffma2_rn(ty[p], ty[p], __ffma2_rn(tx[p], tx[p], pr[p].nc))),
+                           make_float2(0.5f, 0.5f));
+        ww[p] = vx[p] = vy[p] = vz[p] = make_float2(0.f, 0.f);
+      }
+#pragma unroll 2
+      for (int j = 0; j < G; ++j) {
+        const float4 ra = gr[j].a, rb = gr[j].b, rc = gr[j].c, rd = gr[j].d;
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+          // records hold -s, so t.(-s) = -t.s
+          float2 h = __fadd2_rn(ct[p], lo2(rc));
+          h = __ffma2_rn(tx[p], lo2(ra), h);
+          h = __ffma2_rn(ty[p], hi2(ra), h);
+          h = __ffma2_rn(tz[p], lo2(rb), h);
+          const float2 inv = make_float2(rcp_approx(h.x), rcp_approx(h.y));
+          ww[p] = __ffma2_rn(hi2(rb), inv, ww[p]);
+          vx[p] = __ffma2_rn(hi2(rc), inv, vx[p]);
+          vy[p] = __ffma2_rn(lo2(rd), inv, vy[p]);
+          vz[p] = __ffma2_rn(hi2(rd), inv, vz[p]);
+        }
+      }
+#pragma unroll
+      for (int p = 0; p < NP; ++p) {  // V holds -sum S s / h: D += (t W + V) / 2
+        const float2 half = make_float2(0.5f, 0.5f);
+        ax[p] = __ffma2_rn(__ffma2_rn(tx[p], ww[p], vx[p]), half, ax[p]);
+        ay[p] = __ffma2_rn(__ffma2_rn(ty[p], ww[p], vy[p]), half, ay[p]);
+        az[p] = __ffma2_rn(__ffma2_rn(tz[p], ww[p], vz[p]), half, az[p]);
+      }
+    } else if (o.hi.w < 0.f) {
+      // compact group near the warp (it may hold the targets themselves): d = t_hi - s_hi with
+      // the records' rel2_fast offsets, so a self pair cancels bit for bit
       if (o.lo.w != 0.f) {
         // every source of the group on the sphere: c_j dropped
-#pragma unroll 4
         for (int j = 0; j < G; ++j) {
-          const float4 ra = gr[j].a, rb = gr[j].b, rc = gr[j].c;
-          const float2 nsx = lo2(ra), nsy = hi2(ra), nsz = lo2(rb), s2 = lo2(rc);
+          const float4 ra = gr[j].a, rb = gr[j].b;
+          const float2 nsx = lo2(ra), nsy = hi2(ra), nsz = lo2(rb), s2 = hi2(rb);
 #pragma unroll
           for (int p = 0; p < NP; ++p) {
             const float2 dx = __fadd2_rn(tx[p], nsx);
@@ -176,10 +217,10 @@ __device__ __forceinline__ void bve_rel_tile(const BveRel::Rec* __restrict__ tl,
           }
         }
       } else {
-#pragma unroll 4
         for (int j = 0; j < G; ++j) {
-          const float4 ra = gr[j].a, rb = gr[j].b, rc = gr[j].c;
-          const float2 nsx = lo2(ra), nsy = hi2(ra), nsz = lo2(rb), ncj = hi2(rb), s2 = lo2(rc);
+          const float4 ra = gr[j].a, rb = gr[j].b;
+          const float ncj1 = gr[j].e.w;
+          const float2 nsx = lo2(ra), nsy = hi2(ra), nsz = lo2(rb), ncj = make_float2(ncj1, ncj1), s2 = hi2(rb);
 #pragma unroll
           for (int p = 0; p < NP; ++p) {
             const float2 dx = __fadd2_rn(tx[p], nsx);
@@ -207,9 +248,10 @@ __device__ __forceinline__ void bve_rel_tile(const BveRel::Rec* __restrict__ tl,
         rel2x2(pr[p].zh, pr[p].zl, o.hi.z, o.lo.z, tzh[p], tzl[p]);
       }
       for (int j = 0; j < G; ++j) {
-        const float4 ra = gr[j].a, rb = gr[j].b, rc = gr[j].c, rd = gr[j].d;
-        const float2 nsx = lo2(ra), nsy = hi2(ra), nsz = lo2(rb), ncj = hi2(rb), s2 = lo2(rc);
-        const float2 nlx = lo2(rd), nly = hi2(rd), nlz = hi2(rc);
+        const float4 ra = gr[j].a, rb = gr[j].b, re = gr[j].e;
+        const float2 nsx = lo2(ra), nsy = hi2(ra), nsz = lo2(rb), s2 = hi2(rb);
+        const float2 nlx = make_float2(re.x, re.x), nly = make_float2(re.y, re.y), nlz = make_float2(re.z, re.z);
+        const float2 ncj = make_float2(re.w, re.w);
 #pragma unroll
         for (int p = 0; p < NP; ++p) {
           const float2 dx = __fadd2_rn(__fadd2_rn(txh[p], nsx), __fadd2_rn(txl[p], nlx));
@@ -422,18 +464,27 @@ __device__ __forceinline__ void bve_rel_prep_tile(const double* x, const double*
     float hi[3], lo[3];
     group_offsets(f, px, py, pz, hi, lo);
     const float nc = __double2float_rn(-cj);
-    const float s = __double2float_rn(zeta[j] * area[j] * s_scale);
+    const double sd = zeta[j] * area[j] * s_scale;
+    const float s = __double2float_rn(sd);
+    const double h0 = hi[0], h1 = hi[1], h2 = hi[2];
+    const float b = __double2float_rn(0.5 * fma(h0, h0, fma(h1, h1, fma(h2, h2, -cj))));  // (|s_hi|^2 - c_j) / 2
     r.a = make_float4(-hi[0], -hi[0], -hi[1], -hi[1]);
-    r.b = make_float4(-hi[2], -hi[2], nc, nc);
-    r.c = make_float4(s, s, -lo[2], -lo[2]);
-    r.d = make_float4(-lo[0], -lo[0], -lo[1], -lo[1]);
+    r.b = make_float4(-hi[2], -hi[2], s, s);
+    const float sx = __double2float_rn(-sd * h0), sy = __double2float_rn(-sd * h1), sz = __double2float_rn(-sd * h2);
+    r.c = make_float4(b, b, sx, sx);
+    r.d = make_float4(sy, sy, sz, sz);
+    r.e = make_float4(-lo[0], -lo[1], -lo[2], nc);
   } else {
-    // inert: at the origin with zero strength and zero -c (weight 0 times a finite
-    // difference; q > 0 through the target's 2^-100 offset when the target sits on o)
-    r.a = r.b = r.c = r.d = make_float4(0.f, 0.f, 0.f, 0.f);
+    // inert: at the origin with zero strength and zero -c (weight 0 times a finite value;
+    // q > 0 through the target's 2^-100 offset when the target sits on o)
+    r.a = r.b = r.c = r.d = r.e = make_float4(0.f, 0.f, 0.f, 0.f);
   }
   *out = r;
-  if (threadIdx.x % BveRel::kGroup == 0) og[threadIdx.x / BveRel::kGroup] = group_origin(f);
+  if (threadIdx.x % BveRel::kGroup == 0) {
+    BveRel::Origin o = group_origin(f);
+    o.hi.w = f.compact ? -f.radius : f.radius;  // the sign marks a compact group
+    og[threadIdx.x / BveRel::kGroup] = o;
+  }
 }
 
 // Tile-relative records of the Hilbert-sorted source list `sorted` (ns entries, records
