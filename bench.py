@@ -49,7 +49,7 @@ FLOPS_PER_INTERACTION = 24  # dot 5, a^2-dot 1, x4pi a 1, zeta A/den 2, cross 9,
 L2_FLUSH_BYTES = 256 << 20
 # DRAM bytes (read + write) of one full-size sweep launch, from the ncu capture recorded in
 # profiles/bve_rel_sweep_icos8_dram.md (ncu cannot run inside the timed benchmark)
-SWEEP_TRAFFIC_ICOS8 = 240_612_864 + 119_981_568
+SWEEP_TRAFFIC_ICOS8 = 270_783_744 + 127_093_760
 
 
 def parse_args():
