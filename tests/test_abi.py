@@ -92,3 +92,34 @@ def test_no_gpu_fails_loudly(built_lib):
     with pytest.raises(built_lib.LpmError) as e:
         built_lib.bve_sphere_velocity(x, y, z, zeta, area, act)
     assert e.value.code in (-6, -2)
+
+
+@pytest.mark.parametrize("call", ["pse_plane_grad", "pse_plane_second", "pse_plane_ddot", "pse_sphere_ddot",
+                                  "pse_sphere_grad", "pse_sphere_div", "swe_plane", "swe_sphere", "beta",
+                                  "beta_stream", "interp_geometry", "interp_sphere_no_z", "interp_no_points"])
+def test_operator_argument_checks(built_lib, call):
+    """Bad eps, radius, block or geometry arguments of the PSE, SWE and beta-plane entry points
+    fail with LPM_ERR_ARG before any device work (so they also fail this way without a GPU)."""
+    lg = built_lib
+    x, y, z, f, a, act = _tiny()
+    fn = {
+        "pse_plane_grad": lambda: lg.pse_plane_gradient_at_particles(x, y, f, a, act, 0.0),
+        "pse_plane_second": lambda: lg.pse_plane_second_partials_at_particles(x, y, f, f, a, act, -1.0),
+        "pse_plane_ddot": lambda: lg.pse_plane_double_dot_product_at_particles(x, y, f, f, a, act, 0.1, i_end=5),
+        "pse_sphere_ddot": lambda: lg.pse_sphere_double_dot_product_at_particles(x, y, z, f, f, f, a, act, 0.1,
+                                                                                  sphere_radius=0.0),
+        "pse_sphere_grad": lambda: lg.pse_sphere_gradient_at_particles(x, y, z, f, a, act, 0.0),
+        "pse_sphere_div": lambda: lg.pse_sphere_divergence_at_particles(x, y, z, f, f, f, a, act, 0.1, i_begin=0),
+        "swe_plane": lambda: lg.swe_plane_rhs_integrals(x, y, f, f, f, a, act, 0.0),
+        "swe_sphere": lambda: lg.swe_sphere_rhs_integrals(x, y, z, f, f, f, a, act, 1.0, 0.1, sphere_radius=-1.0),
+        "beta": lambda: lg.beta_plane_velocity(x, y, f, a, act, i_begin=2, i_end=1),
+        "beta_stream": lambda: lg.beta_plane_stream_functions(x, y, f, f, a, act, mode="fp16"),
+        "interp_geometry": lambda: lg.pse_interpolate_scalar(x, y, None, f, a, act, 0.1, x[:1], y[:1], geometry=3),
+        "interp_sphere_no_z": lambda: lg.pse_interpolate_scalar(x, y, None, f, a, act, 0.1, x[:1], y[:1],
+                                                                geometry=lg.GEOMETRY_SPHERE),
+        "interp_no_points": lambda: lg.pse_interpolate_scalar(x, y, None, f, a, act, 0.1, x[:0], y[:0]),
+    }[call]
+    with pytest.raises((lg.LpmError, ValueError, KeyError)) as e:
+        fn()
+    if isinstance(e.value, lg.LpmError):
+        assert e.value.code == -1
