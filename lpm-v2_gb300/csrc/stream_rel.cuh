@@ -8,11 +8,14 @@
 // (exact), so
 //   psi_i = sum_{j != i} S_j ln q_ij - ln(a^2 / 2) / (4 pi) sum_{j != i} zeta_j A_j,
 // S_j = -zeta_j A_j / (4 pi).  The sweep forms the first sum; the finish adds the second from
-// a fixed-order FP64 total minus the target's own term.  Per target pair and source (far
-// form): d (3 FADD2), |d|^2 (3), q (1-2), the self-pair select and the clamp to >= 2^-126
-// (scalar), ln q (ln_q2: 4 integer operations per lane, 15 packed, 2 MUFU), and the two
-// accumulations (2 FFMA2).  The FP32 partials are flushed into compensated (hi, lo) pairs
-// every 32 sources, because the terms cancel to a much smaller psi.
+// a fixed-order FP64 total minus the target's own term.  Per target pair and source, far
+// warp (every target beyond 3R of the group's centroid): the expanded form of the BVE sweep,
+// h = q/2 = (|t|^2 - c_i)/2 + B_j/2 - t.s_j (4 packed), ln q = ln h + ln 2 (ln_q2_shift:
+// 4 integer operations per lane, 15 packed, 2 MUFU) and the two accumulations (2 FFMA2); no
+// select, since q > 0.  A compact group near the warp takes d = t_hi - s_hi with the
+// self-pair select and the clamp to >= 2^-126, any other near group the two-float form.  The
+// FP32 partials are flushed into compensated (hi, lo) pairs every 32 sources, because the
+// terms cancel to a much smaller psi.
 #pragma once
 
 #include "bve_rel.cuh"
@@ -27,7 +30,7 @@ struct StreamRel {
     float4 b;  // -sz_hi, -sz_hi, -c_j, -c_j
     float4 c;  // S_rel, S_rel, S_abs, S_abs
     float4 d;  // -sx_lo, -sx_lo, -sy_lo, -sy_lo
-    float4 e;  // -sz_lo, -sz_lo, 0, 0
+    float4 e;  // -sz_lo, -sz_lo, B_j / 2, B_j / 2   (B_j = |s_hi|^2 - c_j)
   };
   static constexpr int kFlush = 32;
 };
@@ -143,11 +146,46 @@ __global__ void __launch_bounds__(THREADS, MINB) stream_rel_sweep_kernel(SweepAr
         ty[p] = rel1x2(pr[p].yh, pr[p].yl, o.hi.y, o.lo.y);
         tz[p] = rel1x2(pr[p].zh, pr[p].zl, o.hi.z, o.lo.z);
       }
-      if (o.hi.w == 0.f || !warp_near<NP>(tx, ty, tz, o.hi.w)) {  // R = 0: compact, never near
-        // compact or far group: d = t_hi - s_hi
+      // far: every target of the warp beyond 3R (and off the centroid of a zero-radius group)
+      const float rg = fabsf(o.hi.w);
+      const float lim = fmaxf((BveRel::kNearFactor * rg) * (BveRel::kNearFactor * rg), 7.888609052210118e-31f);
+      bool nearw = false;
+#pragma unroll
+      for (int p = 0; p < NP; ++p) {
+        const float2 n2 = __ffma2_rn(tz[p], tz[p], __ffma2_rn(ty[p], ty[p], __fmul2_rn(tx[p], tx[p])));
+        nearw |= !(n2.x > lim) | !(n2.y > lim);
+      }
+      if (!__any_sync(0xffffffffu, nearw)) {
+        // expanded form: h = q/2 = (|t|^2 - c_i)/2 + B_j/2 - t.s_j > 0, ln q = ln h + ln 2
+        float2 ct[NP];
+#pragma unroll
+        for (int p = 0; p < NP; ++p)
+          ct[p] = __fmul2_rn(__ffma2_rn(tz[p], tz[p], __ffma2_rn(ty[p], ty[p], __ffma2_rn(tx[p], tx[p], pr[p].nc))),
+                             make_float2(0.5f, 0.5f));
+        const float2 bias = shift_bias(-1, -1);
 #pragma unroll 1
         for (int j0 = 0; j0 < G; j0 += FL) {
 #pragma unroll 2
+          for (int j = j0; j < j0 + FL; ++j) {
+            const float4 ra = gr[j].a, rb = gr[j].b, rc = gr[j].c, re = gr[j].e;
+            const float2 sr = lo2(rc), sa = hi2(rc);
+#pragma unroll
+            for (int p = 0; p < NP; ++p) {
+              float2 h = __fadd2_rn(ct[p], hi2(re));
+              h = __ffma2_rn(tx[p], lo2(ra), h);
+              h = __ffma2_rn(ty[p], hi2(ra), h);
+              h = __ffma2_rn(tz[p], lo2(rb), h);
+              const float2 lg = ln_q2_shift(h, bias);
+              ar[p] = __ffma2_rn(sr, lg, ar[p]);
+              aa[p] = __ffma2_rn(sa, lg, aa[p]);
+            }
+          }
+          stream_flush<NP>(ar, aa, hr, lr, ha, la);
+        }
+      } else if (o.hi.w < 0.f) {
+        // compact group near the warp: d = t_hi - s_hi (rel2_fast records: a self pair gives d = 0)
+#pragma unroll 1
+        for (int j0 = 0; j0 < G; j0 += FL) {
           for (int j = j0; j < j0 + FL; ++j) {
             const float4 ra = gr[j].a, rb = gr[j].b, rc = gr[j].c;
             const float2 nsx = lo2(ra), nsy = hi2(ra), nsz = lo2(rb), ncj = hi2(rb), sr = lo2(rc), sa = hi2(rc);
@@ -247,7 +285,9 @@ __global__ void __launch_bounds__(TILE) stream_rel_prep_kernel(const double* x, 
     r.b = make_float4(-hi[2], -hi[2], nc, nc);
     r.c = make_float4(sr, sr, sa, sa);
     r.d = make_float4(-lo[0], -lo[0], -lo[1], -lo[1]);
-    r.e = make_float4(-lo[2], -lo[2], 0.f, 0.f);
+    const double h0 = hi[0], h1 = hi[1], h2 = hi[2];
+    const float b = __double2float_rn(0.5 * fma(h0, h0, fma(h1, h1, fma(h2, h2, -cj))));
+    r.e = make_float4(-lo[2], -lo[2], b, b);
     if (self_w && j >= ib && j < ib + nt) {
       self_w[j - ib] = wr;
       self_w[nt + j - ib] = wa;
@@ -258,7 +298,11 @@ __global__ void __launch_bounds__(TILE) stream_rel_prep_kernel(const double* x, 
     r.a = r.b = r.c = r.d = r.e = make_float4(0.f, 0.f, 0.f, 0.f);
   }
   out[k] = r;
-  if (threadIdx.x % BveRel::kGroup == 0) org[t * (TILE / BveRel::kGroup) + threadIdx.x / BveRel::kGroup] = group_origin(f);
+  if (threadIdx.x % BveRel::kGroup == 0) {
+    BveRel::Origin o = group_origin(f);
+    o.hi.w = f.compact ? -f.radius : f.radius;  // the sign marks a compact group
+    org[t * (TILE / BveRel::kGroup) + threadIdx.x / BveRel::kGroup] = o;
+  }
 }
 
 // ====================================================================== planar stream function
@@ -496,7 +540,7 @@ __global__ void __launch_bounds__(THREADS, MINB) sphere_swe_rel_sweep_kernel(Swe
         ty[p] = rel1x2(pr[p].yh, pr[p].yl, o.hi.y, o.lo.y);
         tz[p] = rel1x2(pr[p].zh, pr[p].zl, o.hi.z, o.lo.z);
       }
-      if (o.hi.w == 0.f || !warp_near<NP>(tx, ty, tz, o.hi.w)) {  // R = 0: compact, never near
+      if (o.hi.w <= 0.f || !warp_near<NP>(tx, ty, tz, o.hi.w)) {  // -R: compact, taken as far
         // compact or far group: d = t_hi - s_hi
 #pragma unroll 2
         for (int j = 0; j < G; ++j) {
