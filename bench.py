@@ -590,6 +590,67 @@ def run_configs(args):
     return 0
 
 
+def sum_oracle_call(kind, v):
+    """The oracle restatement of --sum `kind` as f(ib, ie) on 0-based target blocks, from the
+    arrays run_sum built (its locals `v`)."""
+    from oracle import oracle as orc
+    c = v.get("c")
+    if kind == "bve":
+        return lambda ib, ie: orc.bve_velocity(c["x"], c["y"], c["z"], c["zeta"], c["area"], c["active"], 1.0,
+                                               ib=ib, ie=ie)
+    if kind == "stream":
+        return lambda ib, ie: orc.bve_stream(c["x"], c["y"], c["z"], c["zeta"], v["absv"], c["area"], c["active"],
+                                             1.0, ib=ib, ie=ie)
+    if kind == "plane_stream":
+        return lambda ib, ie: orc.plane_stream(c["x"], c["y"], c["omega"], c["area"], c["active"], ib=ib, ie=ie)
+    if kind == "plane":
+        return lambda ib, ie: orc.plane_velocity(c["x"], c["y"], c["omega"], c["area"], c["active"], 0.0, ib=ib,
+                                                 ie=ie)
+    if kind == "swe_plane":
+        return lambda ib, ie: orc.swe_plane_rhs(c["x"], c["y"], c["omega"], v["div"], v["sh"], c["area"],
+                                                c["active"], v["eps"], ib=ib, ie=ie)
+    if kind == "swe_sphere":
+        return lambda ib, ie: orc.swe_sphere_rhs(c["x"], c["y"], c["z"], c["zeta"], v["div"], v["sh"], c["area"],
+                                                 c["active"], 1.0, 1.0, v["eps"], ib=ib, ie=ie)
+    if kind == "beta":
+        return lambda ib, ie: orc.beta_plane_velocity(c["x"], c["y"], c["zeta"], c["area"], c["active"], ib=ib,
+                                                      ie=ie)
+    if kind == "beta_stream":
+        return lambda ib, ie: orc.beta_plane_stream(c["x"], c["y"], c["zeta"], v["absv"], c["area"], c["active"],
+                                                    ib=ib, ie=ie)
+    if kind == "pse_plane":
+        m = v["m"]
+        return lambda ib, ie: orc.pse_laplacian(m.x, m.y, None, v["f"], m.area, m.active, v["eps"], 1.0,
+                                                orc.PSE_K8_CHORD, ib=ib, ie=ie)
+    if kind == "pse_grad":
+        return lambda ib, ie: orc.pse_sphere_gradient(c["x"], c["y"], c["z"], v["f"], c["area"], c["active"],
+                                                      v["eps"], 1.0, ib=ib, ie=ie)
+    if kind == "pse_div":
+        vv = v["v"]
+        return lambda ib, ie: orc.pse_sphere_divergence(c["x"], c["y"], c["z"], *vv, c["area"], c["active"],
+                                                        v["eps"], 1.0, ib=ib, ie=ie)
+    kern = orc.PSE_K8_GEODESIC if kind == "pse_k8" else orc.PSE_GAUSS_CHORD
+    return lambda ib, ie: orc.pse_laplacian(c["x"], c["y"], c["z"], c["f"], c["area"], c["active"], v["eps"], 1.0,
+                                            kern, ib=ib, ie=ie)
+
+
+def sum_cpu_sample(ocall, n, ns, budget_s: float):
+    """Times the oracle on a contiguous block of targets against all sources, sized to about
+    budget_s seconds; the cpu_baseline object of a --workload sum line."""
+    start, probe = n // 3, 32
+    t0 = time.perf_counter()
+    ocall(start, min(n, start + probe))
+    dt = max(time.perf_counter() - t0, 1e-6)
+    m = int(min(n - start, max(probe, probe * budget_s / dt)))
+    t0 = time.perf_counter()
+    ocall(start, start + m)
+    el = time.perf_counter() - t0
+    cores = os.cpu_count() or 1
+    return {"value": m * ns / el / 1e9, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"oracle (OpenMP, {cores} threads), targets {start + 1}..{start + m} of {n} against all "
+                      f"{ns} sources, {el:.1f} s"}
+
+
 def run_sum(args):
     """One direct sum through its host-buffer C-ABI entry point, `steps` calls after `warmup`
     (a small, few-launch workload for profiling and per-row rates).  --nest is the refinement
@@ -686,6 +747,7 @@ def run_sum(args):
                                                                c["active"], eps, 1.0, kern, i_end=ie, mode=args.mode)
         mesh = f"cubed sphere nest {args.nest}, eps {eps:.4g}"
     nt = n if args.targets <= 0 else min(args.targets, n)
+    ocall = None if args.no_cpu_baseline else sum_oracle_call(args.sum, locals())
     for _ in range(max(args.warmup, 3)):
         call(nt)
     times = []
@@ -698,6 +760,8 @@ def run_sum(args):
             "value": nt * ns / t / 1e9, "unit": UNIT, "steps": args.steps, "ms_per_step": 1e3 * t,
             "config": {"workload": f"{args.sum} on {mesh}: {nt} of {n} targets, {ns} sources",
                        "timing": "host wall clock around each call (copies included), best of the steps"}}
+    if ocall is not None:
+        line["cpu_baseline"] = sum_cpu_sample(ocall, n, ns, 3.0)
     print(json.dumps(line), flush=True)
     return 0
 
