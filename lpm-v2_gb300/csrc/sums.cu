@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "bve_rel.cuh"
+#include "beta_rel.cuh"
 #include "bve_x2.cuh"
 #include "engine.cuh"
 #include "ops.cuh"
@@ -35,6 +36,7 @@ constexpr int kBveShapeCount = sizeof(kBveShapes) / sizeof(kBveShapes[0]);
 constexpr int kPlaneThreads = 128, kPlaneTpt = 4, kPlaneTile = 256, kPlaneMinB = 4;
 constexpr int kPseThreads = 128, kPseTpt = 4, kPseTile = 128, kPseMinB = 4;
 constexpr int kStreamThreads = 128, kStreamTpt = 4, kStreamTile = 256, kStreamMinB = 4;
+constexpr int kBetaThreads = 128, kBetaTpt = 4, kBetaTile = 256, kBetaMinB = 4;
 constexpr int kSweMinB = 3;        // planar SWE velocity sweep: 128 x 4 targets, 3 CTAs per SM
 constexpr int kSweSphereMinB = 2;  // sphere SWE velocity sweep: 2 CTAs per SM (no spills; 10 % over 3)
 // FP64 sequential sweep shape
@@ -164,50 +166,6 @@ __global__ void __launch_bounds__(1024) stream_totals_kernel(const double* qr, c
   }
 }
 
-__global__ void prep_beta32_kernel(const double* x, const double* y, const double* zeta, const double* area,
-                                   const int32_t* idx, int64_t ns, int64_t npad, BetaF32::Rec* out) {
-  const int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (k >= npad) return;
-  BetaF32::Rec r;
-  if (k < ns) {
-    const int64_t j = idx[k];
-    float h, l;
-    split2(x[j], h, l);
-    r.a.x = h;
-    r.a.z = l;
-    split2(y[j], h, l);
-    r.a.y = h;
-    r.a.w = l;
-    r.b = make_float4(__double2float_rn(0.5 * zeta[j] * area[j]), 0.f, 0.f, 0.f);
-  } else {
-    r.a = r.b = make_float4(0.f, 0.f, 0.f, 0.f);  // zero strength
-  }
-  out[k] = r;
-}
-
-__global__ void prep_beta_stream32_kernel(const double* x, const double* y, const double* qr, const double* qa,
-                                          const double* area, const int32_t* idx, int64_t ns, int64_t npad,
-                                          BetaStreamF32::Rec* out) {
-  const int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (k >= npad) return;
-  BetaStreamF32::Rec r;
-  if (k < ns) {
-    const int64_t j = idx[k];
-    float h, l;
-    split2(x[j], h, l);
-    r.a.x = h;
-    r.a.z = l;
-    split2(y[j], h, l);
-    r.a.y = h;
-    r.a.w = l;
-    r.b = make_float4(__double2float_rn(qr[j] * area[j] * kInv4Pi), __double2float_rn(qa[j] * area[j] * kInv4Pi),
-                      0.f, 0.f);
-  } else {
-    r.a = r.b = make_float4(0.f, 0.f, 0.f, 0.f);  // zero strength
-  }
-  out[k] = r;
-}
-
 // ------------------------------------------------------------------ finish kernels
 // Fixed-order FP64 reduction over the split-K chunks, then the per-target epilogue.
 
@@ -327,6 +285,9 @@ int tile_of(int kind, int mode) {
     case kSumPlaneStream:
     case kSumSweSphere:
       return kStreamTile;
+    case kSumBetaPlane:
+    case kSumBetaStream:
+      return kBetaTile;
     default:
       return kPseTile;
   }
@@ -354,9 +315,9 @@ size_t rec_bytes(int kind, int mode) {
     case kSumPlaneStream:
       return sizeof(PlaneRel::Rec);
     case kSumBetaPlane:
-      return sizeof(BetaF32::Rec);
+      return sizeof(BetaRel::Rec);
     case kSumBetaStream:
-      return sizeof(BetaStreamF32::Rec);
+      return sizeof(BetaStreamRel::Rec);
     case kSumSwePlane:
       return sizeof(PlaneRel::Rec);
     case kSumPseK8Geo:
@@ -401,6 +362,9 @@ int targets_per_cta(int kind, int shape) {
     case kSumPlaneStream:
     case kSumSweSphere:
       return kStreamThreads * kStreamTpt;
+    case kSumBetaPlane:
+    case kSumBetaStream:
+      return kBetaThreads * kBetaTpt;
     default:
       return kPseThreads * kPseTpt;
   }
@@ -431,12 +395,14 @@ bool sum_uses_sorted_sources(int kind, int mode) {
   return mode == LPM_MODE_FP32C && (kind == kSumBve || kind == kSumBveMesh || kind == kSumPlane ||
                                     kind == kSumSphereStream || kind == kSumPseK8Geo || kind == kSumPseGaussChord ||
                                     kind == kSumPseK8Chord || kind == kSumPseGrad || kind == kSumPseDiv ||
-                                    kind == kSumPlaneStream || kind == kSumSwePlane || kind == kSumSweSphere);
+                                    kind == kSumPlaneStream || kind == kSumSwePlane || kind == kSumSweSphere ||
+                                    kind == kSumBetaPlane || kind == kSumBetaStream);
 }
 
 size_t sort_scratch_bytes(int kind, int64_t ns) {
   // planar kinds sort in 2-D; the Gaussian-chord Laplacian serves the plane and the sphere
-  if (kind == kSumPlane || kind == kSumPseK8Chord || kind == kSumPlaneStream || kind == kSumSwePlane)
+  if (kind == kSumPlane || kind == kSumPseK8Chord || kind == kSumPlaneStream || kind == kSumSwePlane ||
+      kind == kSumBetaPlane || kind == kSumBetaStream)
     return curve_sort2d_bytes(ns);
   if (kind == kSumPseGaussChord) return std::max(curve_sort_bytes(ns), curve_sort2d_bytes(ns));
   return curve_sort_bytes(ns);
@@ -453,7 +419,10 @@ SumPlan plan_sum(int kind, int mode, int64_t ns, int64_t nt, int sm_count, int s
   pl.src_bytes = static_cast<size_t>(pl.n_tiles) * tile * rec_bytes(kind, mode);
   if (sum_uses_sorted_sources(kind, mode)) {
     // the group origins follow the records
-    static_assert(sizeof(BveRel::Origin) == sizeof(PlaneRel::Origin) && BveRel::kGroup == PlaneRel::kGroup,
+    static_assert(sizeof(BveRel::Origin) == sizeof(PlaneRel::Origin) && BveRel::kGroup == PlaneRel::kGroup &&
+                      sizeof(BveRel::Origin) == sizeof(BetaRel::Origin) && BveRel::kGroup == BetaRel::kGroup &&
+                      sizeof(BveRel::Origin) == sizeof(BetaStreamRel::Origin) &&
+                      BveRel::kGroup == BetaStreamRel::kGroup,
                   "one origin layout size");
     pl.src_bytes = align_up(pl.src_bytes, 256) +
                    static_cast<size_t>(pl.n_tiles) * (tile / BveRel::kGroup) * sizeof(BveRel::Origin);
@@ -947,9 +916,31 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
       break;
     }
     case kSumBetaPlane: {
-      prep_beta32_kernel<<<prep_grid_pad, pb, 0, job.stream>>>(job.x, job.y, job.s1, job.area, job.src_idx, job.ns,
-                                                               npad, static_cast<BetaF32::Rec*>(job.src_buf));
-      launch_sweep<BetaF32, kPseThreads, kPseTpt, kPseTile, kPseMinB>(job, plan, BetaF32::Params{job.x, job.y});
+      const int32_t* src_list = job.src_idx;
+      if (job.sort_scratch) {
+        LPM_TRY(curve_sort2d(job.stream, job.ns, job.src_idx, job.x, job.y, job.sort_scratch, job.sort_bytes,
+                             job.sorted));
+        src_list = job.sorted;
+      }
+      BetaRel::Rec* recs = static_cast<BetaRel::Rec*>(job.src_buf);
+      BetaRel::Origin* org = reinterpret_cast<BetaRel::Origin*>(
+          static_cast<char*>(job.src_buf) + align_up(static_cast<size_t>(npad) * sizeof(BetaRel::Rec), 256));
+      beta_rel_prep_kernel<kBetaTile><<<static_cast<unsigned>(plan.n_tiles), kBetaTile, 0, job.stream>>>(
+          job.x, job.y, job.s1, job.area, src_list, job.ns, recs, org);
+      BetaRelArgs a;
+      a.x = job.x;
+      a.y = job.y;
+      a.src = recs;
+      a.org = org;
+      a.n_tiles = plan.n_tiles;
+      a.tiles_per_chunk = plan.tiles_per_chunk;
+      a.ib = job.ib;
+      a.nt = job.nt;
+      a.partial = job.partial;
+      a.status = job.status;
+      const dim3 grid(static_cast<unsigned>(ceil_div(job.nt, kBetaThreads * kBetaTpt)),
+                      static_cast<unsigned>(plan.nsplit));
+      beta_rel_sweep_kernel<kBetaThreads, kBetaTpt, kBetaTile, kBetaMinB><<<grid, kBetaThreads, 0, job.stream>>>(a);
       finish_stream_kernel<<<fin_grid, pb, 0, job.stream>>>(job.partial, plan.nsplit, job.nt, 2, 0.0, nullptr, nullptr,
                                                             job.out0, job.out1);
       break;
@@ -1003,11 +994,32 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
       break;
     }
     case kSumBetaStream: {
-      prep_beta_stream32_kernel<<<prep_grid_pad, pb, 0, job.stream>>>(job.x, job.y, job.s1, job.s2, job.area,
-                                                                      job.src_idx, job.ns, npad,
-                                                                      static_cast<BetaStreamF32::Rec*>(job.src_buf));
-      launch_sweep<BetaStreamF32, kPseThreads, kPseTpt, kPseTile, kPseMinB>(job, plan,
-                                                                              BetaF32::Params{job.x, job.y});
+      const int32_t* src_list = job.src_idx;
+      if (job.sort_scratch) {
+        LPM_TRY(curve_sort2d(job.stream, job.ns, job.src_idx, job.x, job.y, job.sort_scratch, job.sort_bytes,
+                             job.sorted));
+        src_list = job.sorted;
+      }
+      BetaStreamRel::Rec* recs = static_cast<BetaStreamRel::Rec*>(job.src_buf);
+      BetaStreamRel::Origin* org = reinterpret_cast<BetaStreamRel::Origin*>(
+          static_cast<char*>(job.src_buf) + align_up(static_cast<size_t>(npad) * sizeof(BetaStreamRel::Rec), 256));
+      beta_stream_rel_prep_kernel<kBetaTile><<<static_cast<unsigned>(plan.n_tiles), kBetaTile, 0, job.stream>>>(
+          job.x, job.y, job.s1, job.s2, job.area, src_list, job.ns, recs, org);
+      BetaStreamRelArgs a;
+      a.x = job.x;
+      a.y = job.y;
+      a.src = recs;
+      a.org = org;
+      a.n_tiles = plan.n_tiles;
+      a.tiles_per_chunk = plan.tiles_per_chunk;
+      a.ib = job.ib;
+      a.nt = job.nt;
+      a.partial = job.partial;
+      a.status = job.status;
+      const dim3 grid(static_cast<unsigned>(ceil_div(job.nt, kBetaThreads * kBetaTpt)),
+                      static_cast<unsigned>(plan.nsplit));
+      beta_stream_rel_sweep_kernel<kBetaThreads, kBetaTpt, kBetaTile, kBetaMinB>
+          <<<grid, kBetaThreads, 0, job.stream>>>(a);
       finish_stream_kernel<<<fin_grid, pb, 0, job.stream>>>(job.partial, plan.nsplit, job.nt, 2, 0.0, nullptr, nullptr,
                                                             job.out0, job.out1);
       break;
