@@ -249,3 +249,67 @@ def test_beta_plane_stream_fp32c(lg, oracle_mod, n, frac, spread):
     err = (rel(pr, rr), rel(pa, ra))
     print("beta stream fp32c", err)
     assert max(err) <= FP32C_TOL
+
+
+def test_beta_plane_fp32c_far_groups_quad7(lg, oracle_mod):
+    """The beta-plane particle set at quad nest 7 (R = 0.019 for 64-source groups, so most
+    target/group pairs take the complex far form), FP32C against the oracle on two target
+    blocks, velocity and stream functions to 1e-6 of their max."""
+    import workloads as wl
+
+    c = wl.config_beta_plane(7)
+    x, y, zeta, area, act = c["x"], c["y"], c["zeta"], c["area"], c["active"]
+    absv = zeta + 3.0 * y
+    u, v = lg.beta_plane_velocity(x, y, zeta, area, act, mode="fp32c")
+    pr, pa = lg.beta_plane_stream_functions(x, y, zeta, absv, area, act, mode="fp32c")
+    for ib, ie in ((0, 2048), (70001, 72048)):
+        ru, rv = oracle_mod.beta_plane_velocity(x, y, zeta, area, act, ib, ie)
+        rr, ra = oracle_mod.beta_plane_stream(x, y, zeta, absv, area, act, ib, ie)
+        s = slice(ib, ie)
+        assert max(rel(u[s], ru), rel(v[s], rv)) <= FP32C_TOL
+        assert max(rel(pr[s], rr), rel(pa[s], ra)) <= FP32C_TOL
+
+
+def test_beta_plane_fp32c_distant_clusters(lg, oracle_mod):
+    """Two compact clusters 14 apart in y (and a sparse band between them): the velocity's far
+    form clamps |y_i - y_o| to 6 (the terms have reached their limits there), and the stream's
+    far form hands |y_i - y_o| > 6 to the direct form."""
+    rng = np.random.default_rng(11)
+    n = 3000
+    x = rng.random(n)
+    y = np.concatenate([rng.normal(-7.0, 0.02, 1400), rng.normal(7.0, 0.02, 1400), rng.uniform(-8, 8, 200)])
+    area = rng.uniform(0.5, 1.5, n) / n
+    zeta = np.cos(2 * np.pi * x) + 0.2 * np.sign(y)
+    absv = zeta + 0.5 * y
+    act = np.ones(n, np.int32)
+    u, v = lg.beta_plane_velocity(x, y, zeta, area, act, mode="fp32c")
+    ru, rv = oracle_mod.beta_plane_velocity(x, y, zeta, area, act)
+    assert max(rel(u, ru), rel(v, rv)) <= FP32C_TOL
+    pr, pa = lg.beta_plane_stream_functions(x, y, zeta, absv, area, act, mode="fp32c")
+    rr, ra = oracle_mod.beta_plane_stream(x, y, zeta, absv, area, act)
+    assert max(rel(pr, rr), rel(pa, ra)) <= FP32C_TOL
+
+
+@pytest.mark.parametrize("n", [1, 2, 63, 65, 257, 1031])
+def test_beta_plane_fp32c_ragged_and_empty(lg, oracle_mod, n):
+    """Ragged sizes (partial groups and tiles, inert records) and a set with no active source
+    (every sum is exactly zero)."""
+    rng = np.random.default_rng(n)
+    x, y = rng.random(n), rng.uniform(-0.5, 0.5, n)
+    area = rng.uniform(0.5, 1.5, n) / n
+    zeta = np.sin(2 * np.pi * x) + y
+    absv = zeta + y
+    act = (rng.random(n) < 0.8).astype(np.int32)
+    act[0] = 1
+    u, v = lg.beta_plane_velocity(x, y, zeta, area, act, mode="fp32c")
+    ru, rv = oracle_mod.beta_plane_velocity(x, y, zeta, area, act)
+    scale = max(np.abs(ru).max(), np.abs(rv).max(), 1e-300)
+    assert max(np.abs(u - ru).max(), np.abs(v - rv).max()) <= FP32C_TOL * scale
+    pr, pa = lg.beta_plane_stream_functions(x, y, zeta, absv, area, act, mode="fp32c")
+    rr, ra = oracle_mod.beta_plane_stream(x, y, zeta, absv, area, act)
+    scale = max(np.abs(rr).max(), np.abs(ra).max(), 1e-300)
+    assert max(np.abs(pr - rr).max(), np.abs(pa - ra).max()) <= FP32C_TOL * scale
+    none = np.zeros(n, np.int32)
+    u, v = lg.beta_plane_velocity(x, y, zeta, area, none, mode="fp32c")
+    pr, pa = lg.beta_plane_stream_functions(x, y, zeta, absv, area, none, mode="fp32c")
+    assert not np.any(u) and not np.any(v) and not np.any(pr) and not np.any(pa)
