@@ -352,6 +352,7 @@ __global__ void __launch_bounds__(THREADS, MINB) beta_stream_rel_sweep_kernel(Be
   using Rec = BetaStreamRel::Rec;
   __shared__ __align__(128) Rec stage[2][TILE];
   __shared__ __align__(8) uint64_t bars[2];
+  __shared__ __align__(8) float2 ln_tab[32];
 
   const int64_t chunk = blockIdx.y;
   const int64_t tile0 = chunk * a.tiles_per_chunk;
@@ -372,6 +373,7 @@ __global__ void __launch_bounds__(THREADS, MINB) beta_stream_rel_sweep_kernel(Be
     hr[t] = lr[t] = ha[t] = la[t] = 0.f;
   }
 
+  ln_tab_load(ln_tab);
   pipe_init(bars);
   uint32_t g = 0;
   int64_t tile = tile0;
@@ -444,7 +446,7 @@ __global__ void __launch_bounds__(THREADS, MINB) beta_stream_rel_sweep_kernel(Be
             const float2 br = __fadd2_rn(er[p], make_float2(-rc.x, -rc.y));
             const float2 bi = __fadd2_rn(ei[p], make_float2(-rc.z, -rc.w));
             const float2 mm = __ffma2_rn(bi, bi, __fmul2_rn(br, br));
-            const float2 lg = ln_q2_shift(mm, bias[p]);
+            const float2 lg = ln_q2_shift(mm, bias[p], ln_tab);
             ar[p] = __ffma2_rn(make_float2(rb.x, rb.x), lg, ar[p]);
             aa[p] = __ffma2_rn(make_float2(rb.y, rb.y), lg, aa[p]);
           }
@@ -477,7 +479,7 @@ __global__ void __launch_bounds__(THREADS, MINB) beta_stream_rel_sweep_kernel(Be
 #pragma unroll
             for (int p = 0; p < NP; ++p) {
               float a0[2] = {ar[p].x, aa[p].x}, a1[2] = {ar[p].y, aa[p].y};
-              BetaStreamF32::interact2(tg[2 * p], tg[2 * p + 1], r, a0, a1);
+              BetaStreamF32::interact2(tg[2 * p], tg[2 * p + 1], r, a0, a1, ln_tab);
               ar[p] = make_float2(a0[0], a1[0]);
               aa[p] = make_float2(a0[1], a1[1]);
             }

@@ -19,6 +19,7 @@
 #pragma once
 
 #include "bve_rel.cuh"
+#include "ln_table.cuh"
 #include "ops.cuh"
 #include "plane_rel.cuh"
 
@@ -36,11 +37,13 @@ struct StreamRel {
 };
 
 // Natural log of two positive normal floats (the sweeps clamp them): per lane q = 2^k m with
-// m in [sqrt(1/2), sqrt(2)) (an integer split; 0x3f3504f3 = fl(sqrt(1/2))), then, packed,
-// ln m = 2 atanh(t), t = (m - 1) / (m + 1), |t| <= 0.1716, by the series
-// 2 (t + t^3/3 + t^5/5 + t^7/7 + t^9/9) (truncated at 2 t^11 / 11 < 7e-10).  t is one
-// reciprocal (MUFU) refined by one residual step against the exact denominator 2 + f, so
-// ln m is good to about 1 ulp; k ln 2 is added last (k is exact in float).
+// m in [sqrt(1/2), sqrt(2)) (an integer split; 0x3f3504f3 = fl(sqrt(1/2))).  Bits 19..23 of
+// m pick (inv, ln c) from a 32-entry table in shared memory (ln_table.cuh: 1/c for c the
+// midpoint of the key's interval, with ln c exact to ~2e-4 ulp in float -- Gal's accurate
+// tables).  Then, packed, r = m inv - 1 (one FMA, |r| <= 0.0305, exact to 2^-30),
+// ln(1 + r) = r + r^2 (-1/2 + r/3 - r^2/4 + r^3/5) (truncated at r^6/6 < 2e-10), and
+// ln q = (k ln 2 + ln c) + ln(1 + r): 9 packed operations and two 8-byte shared loads (keys
+// 6 and 22 alone share banks), no MUFU; good to about 1 ulp of the larger part.
 // The exponent split of a positive normal float with bits b: q = 2^k m, m in [sqrt(1/2),
 // sqrt(2)) (0x3f3504f3 = fl(sqrt(1/2))); returns k and writes the bits of m.  Inline PTX
 // keeps the integer sequence as written: the same four operations in C++, fed straight
@@ -62,27 +65,27 @@ __device__ __forceinline__ float2 shift_bias(int s0, int s1) {
   return make_float2(-12582912.0f - static_cast<float>(s0), -12582912.0f - static_cast<float>(s1));
 }
 
-__device__ __forceinline__ float2 ln_q2_shift(float2 q, float2 bias) {
-  int m0, m1;
-  const int k0 = exp_split(__float_as_int(q.x), m0), k1 = exp_split(__float_as_int(q.y), m1);
-  const float2 m = make_float2(__int_as_float(m0), __int_as_float(m1));
-  const float2 kf = __fadd2_rn(make_float2(__int_as_float(k0 + 0x4b400000), __int_as_float(k1 + 0x4b400000)), bias);
-  const float2 f = __fadd2_rn(m, make_float2(-1.0f, -1.0f));
-  const float2 den = __fadd2_rn(f, make_float2(2.0f, 2.0f));
-  const float2 r = make_float2(rcp_approx(den.x), rcp_approx(den.y));
-  const float2 t0 = __fmul2_rn(f, r);
-  const float2 res = __ffma2_rn(make_float2(-t0.x, -t0.y), f, __ffma2_rn(make_float2(-2.0f, -2.0f), t0, f));
-  const float2 t = __ffma2_rn(r, res, t0);
-  const float2 tt = __fadd2_rn(t, t);
-  const float2 s = __fmul2_rn(t, t);
-  float2 p = __ffma2_rn(make_float2(0.11111111f, 0.11111111f), s, make_float2(0.14285715f, 0.14285715f));
-  p = __ffma2_rn(p, s, make_float2(0.2f, 0.2f));
-  p = __ffma2_rn(p, s, make_float2(0.33333334f, 0.33333334f));
-  const float2 lnm = __ffma2_rn(__fmul2_rn(tt, s), p, tt);
-  return __ffma2_rn(kf, make_float2(0.69314718f, 0.69314718f), lnm);
+// The table into shared memory (threads 0..31; the caller's next __syncthreads publishes it).
+__device__ __forceinline__ void ln_tab_load(float2* tab) {
+  if (threadIdx.x < 32) tab[threadIdx.x] = make_float2(kLnTabInv[threadIdx.x], kLnTabLog[threadIdx.x]);
 }
 
-__device__ __forceinline__ float2 ln_q2(float2 q) { return ln_q2_shift(q, shift_bias(0, 0)); }
+__device__ __forceinline__ float2 ln_q2_shift(float2 q, float2 bias, const float2* tab) {
+  int m0, m1;
+  const int k0 = exp_split(__float_as_int(q.x), m0), k1 = exp_split(__float_as_int(q.y), m1);
+  const float2 e0 = tab[(m0 >> 19) & 31], e1 = tab[(m1 >> 19) & 31];
+  const float2 m = make_float2(__int_as_float(m0), __int_as_float(m1));
+  const float2 kf = __fadd2_rn(make_float2(__int_as_float(k0 + 0x4b400000), __int_as_float(k1 + 0x4b400000)), bias);
+  const float2 r = __ffma2_rn(m, make_float2(e0.x, e1.x), make_float2(-1.0f, -1.0f));
+  float2 p = __ffma2_rn(make_float2(0.2f, 0.2f), r, make_float2(-0.25f, -0.25f));
+  p = __ffma2_rn(p, r, make_float2(0.33333334f, 0.33333334f));
+  p = __ffma2_rn(p, r, make_float2(-0.5f, -0.5f));
+  const float2 b = __ffma2_rn(__fmul2_rn(r, r), p, r);
+  const float2 a = __ffma2_rn(kf, make_float2(0.69314718f, 0.69314718f), make_float2(e0.y, e1.y));
+  return __fadd2_rn(a, b);
+}
+
+__device__ __forceinline__ float2 ln_q2(float2 q, const float2* tab) { return ln_q2_shift(q, shift_bias(0, 0), tab); }
 
 // The log argument of a pair: q clamped to >= 2^-126, or 1 (a zero term) when d = 0.
 __device__ __forceinline__ float2 stream_arg(float2 u, float2 q) {
@@ -115,6 +118,7 @@ __global__ void __launch_bounds__(THREADS, MINB) stream_rel_sweep_kernel(SweepAr
   using Rec = StreamRel::Rec;
   __shared__ __align__(128) Rec stage[2][TILE];
   __shared__ __align__(8) uint64_t bars[2];
+  __shared__ __align__(8) float2 ln_tab[32];
 
   const int64_t chunk = blockIdx.y;
   const int64_t tile0 = chunk * a.tiles_per_chunk;
@@ -130,6 +134,7 @@ __global__ void __launch_bounds__(THREADS, MINB) stream_rel_sweep_kernel(SweepAr
 #pragma unroll
   for (int p = 0; p < NP; ++p) hr[p] = lr[p] = ha[p] = la[p] = ar[p] = aa[p] = make_float2(0.f, 0.f);
 
+  ln_tab_load(ln_tab);
   pipe_init(bars);
   uint32_t g = 0;
   int64_t tile = tile0;
@@ -175,7 +180,7 @@ __global__ void __launch_bounds__(THREADS, MINB) stream_rel_sweep_kernel(SweepAr
               h = __ffma2_rn(tx[p], lo2(ra), h);
               h = __ffma2_rn(ty[p], hi2(ra), h);
               h = __ffma2_rn(tz[p], lo2(rb), h);
-              const float2 lg = ln_q2_shift(h, bias);
+              const float2 lg = ln_q2_shift(h, bias, ln_tab);
               ar[p] = __ffma2_rn(sr, lg, ar[p]);
               aa[p] = __ffma2_rn(sa, lg, aa[p]);
             }
@@ -196,7 +201,7 @@ __global__ void __launch_bounds__(THREADS, MINB) stream_rel_sweep_kernel(SweepAr
               const float2 dz = __fadd2_rn(tz[p], nsz);
               const float2 u = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
               const float2 q = __fadd2_rn(u, __fadd2_rn(pr[p].nc, ncj));
-              const float2 lg = ln_q2(stream_arg(u, q));
+              const float2 lg = ln_q2(stream_arg(u, q), ln_tab);
               ar[p] = __ffma2_rn(sr, lg, ar[p]);
               aa[p] = __ffma2_rn(sa, lg, aa[p]);
             }
@@ -225,7 +230,7 @@ __global__ void __launch_bounds__(THREADS, MINB) stream_rel_sweep_kernel(SweepAr
               const float2 dz = __fadd2_rn(__fadd2_rn(tzh[p], nsz), __fadd2_rn(tzl[p], nlz));
               const float2 u = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
               const float2 q = __fadd2_rn(u, __fadd2_rn(pr[p].nc, ncj));
-              const float2 lg = ln_q2(stream_arg(u, q));
+              const float2 lg = ln_q2(stream_arg(u, q), ln_tab);
               ar[p] = __ffma2_rn(sr, lg, ar[p]);
               aa[p] = __ffma2_rn(sa, lg, aa[p]);
             }
@@ -333,6 +338,7 @@ __global__ void __launch_bounds__(THREADS, MINB) plane_stream_rel_sweep_kernel(P
   using Rec = PlaneRel::Rec;
   __shared__ __align__(128) Rec stage[2][TILE];
   __shared__ __align__(8) uint64_t bars[2];
+  __shared__ __align__(8) float2 ln_tab[32];
 
   const int64_t chunk = blockIdx.y;
   const int64_t tile0 = chunk * a.tiles_per_chunk;
@@ -363,6 +369,7 @@ __global__ void __launch_bounds__(THREADS, MINB) plane_stream_rel_sweep_kernel(P
   constexpr float kTiny = 7.888609052210118e-31f;  // 2^-100: centring and near floor
   constexpr float kHuge = 1.2676506002282294e30f;  // 2^100
 
+  ln_tab_load(ln_tab);
   pipe_init(bars);
   uint32_t g = 0;
   int64_t tile = tile0;
@@ -411,7 +418,7 @@ __global__ void __launch_bounds__(THREADS, MINB) plane_stream_rel_sweep_kernel(P
             const float2 dx = __fadd2_rn(tx[p], lo2(ra));
             const float2 dy = __fadd2_rn(ty[p], hi2(ra));
             const float2 u = __ffma2_rn(dy, dy, __fmul2_rn(dx, dx));
-            acc[p] = __ffma2_rn(lo2(rb), ln_q2_shift(u, bias[p]), acc[p]);
+            acc[p] = __ffma2_rn(lo2(rb), ln_q2_shift(u, bias[p], ln_tab), acc[p]);
           }
         }
 #pragma unroll
@@ -439,7 +446,7 @@ __global__ void __launch_bounds__(THREADS, MINB) plane_stream_rel_sweep_kernel(P
               const float2 dx = __fadd2_rn(__fadd2_rn(txh[p], lo2(ra)), __fadd2_rn(txl[p], hi2(rb)));
               const float2 dy = __fadd2_rn(__fadd2_rn(tyh[p], hi2(ra)), __fadd2_rn(tyl[p], lo2(rc)));
               const float2 u = __ffma2_rn(dy, dy, __fmul2_rn(dx, dx));
-              acc[p] = __ffma2_rn(lo2(rb), ln_q2_shift(stream_arg(u, u), bias[p]), acc[p]);
+              acc[p] = __ffma2_rn(lo2(rb), ln_q2_shift(stream_arg(u, u), bias[p], ln_tab), acc[p]);
             }
           }
 #pragma unroll
@@ -626,7 +633,7 @@ struct BetaStreamF32 {
   using Params = BetaF32::Params;
   __device__ static Tgt load_target(const Params& p, int64_t i) { return BetaF32::load_target(p, i); }
   __device__ static __forceinline__ void interact2(const Tgt& t0, const Tgt& t1, const Rec& r, float (&a0)[2],
-                                                   float (&a1)[2]) {
+                                                   float (&a1)[2], const float2* tab) {
     float2 tt, dy;
     beta_deltas2(t0, t1, r.a, tt, dy);
     const float2 sn = sinpi2(tt, __fmul2_rn(tt, tt));
@@ -644,7 +651,7 @@ struct BetaStreamF32 {
     const float2 snp = __fmul2_rn(sn, sc);
     const float2 x = __ffma2_rn(shp, shp, __fmul2_rn(snp, snp));
     const float2 lg = ln_q2_shift(make_float2(x.x > 0.f ? x.x : 1.0f, x.y > 0.f ? x.y : 1.0f),
-                                  shift_bias(1 - 2 * k0, 1 - 2 * k1));
+                                  shift_bias(1 - 2 * k0, 1 - 2 * k1), tab);
     const float2 g = make_float2(x.x > 0.f ? lg.x : 0.f, x.y > 0.f ? lg.y : 0.f);
     const float2 pr = __ffma2_rn(make_float2(r.b.x, r.b.x), g, make_float2(a0[0], a1[0]));
     const float2 pa = __ffma2_rn(make_float2(r.b.y, r.b.y), g, make_float2(a0[1], a1[1]));
