@@ -11,7 +11,7 @@
 // a fixed-order FP64 total minus the target's own term.  Per target pair and source, far
 // warp (every target beyond 3R of the group's centroid): the expanded form of the BVE sweep,
 // h = q/2 = (|t|^2 - c_i)/2 + B_j/2 - t.s_j (4 packed), ln q = ln h + ln 2 (ln_q2_shift:
-// 4 integer operations per lane, 15 packed, 2 MUFU) and the two accumulations (2 FFMA2); no
+// integer exponent split, a table load per lane, 9 packed) and the two accumulations; no
 // select, since q > 0.  A compact group near the warp takes d = t_hi - s_hi with the
 // self-pair select and the clamp to >= 2^-126, any other near group the two-float form.  The
 // FP32 partials are flushed into compensated (hi, lo) pairs every 32 sources, because the
@@ -325,7 +325,7 @@ __global__ void __launch_bounds__(TILE) stream_rel_prep_kernel(const double* x, 
 // warp at |t - o| > 3R, so u_j > 0) needs no select; in a near group the self pair (u = 0,
 // the lo parts cancel bit for bit) takes q = 1, whose centred term -k ln 2 cancels the
 // target's own share of k ln 2 S_g.  Per target pair and source (far form): d (2 FADD2),
-// |d|^2 (2), ln (ln_q2_shift: 4 integer operations per lane, 15 packed, 2 MUFU) and the
+// |d|^2 (2), ln (ln_q2_shift: integer split, a table load per lane, 9 packed) and the
 // accumulation (1 FFMA2).  Near partials are flushed every 16 sources, far ones per group.
 template <int THREADS, int TPT, int TILE, int MINB>
 __global__ void __launch_bounds__(THREADS, MINB) plane_stream_rel_sweep_kernel(PlaneRelArgs a) {
