@@ -1,12 +1,8 @@
 // ops.cuh -- pair operators of the direct sums, FP64 (reference association) and FP32C.
 //
-// Each FP32C operator defines
-//   Rec     : the source record staged through shared memory (16-byte multiple)
-//   Tgt     : the per-target register state
-//   NC      : number of accumulated components
-//   load_target(p, i) and interact(tgt, rec, acc[NC])
-// and a matching prep functor (in sums.cu) builds Rec from the particle arrays.  Each FP64
-// operator restates one Fortran loop body with explicit round-to-nearest intrinsics so
+// The FP32C pieces here (BveF32's target split, BetaF32's direct pair form) are called by
+// the group-relative sweeps (bve_rel.cuh, stream_rel.cuh, beta_rel.cuh), whose prep kernels
+// build the records from the particle arrays.  Each FP64 operator restates one Fortran loop body with explicit round-to-nearest intrinsics so
 // that nvcc cannot fuse a multiply into an add: every intermediate rounds exactly where
 // the Fortran rounds it.
 #pragma once
@@ -756,26 +752,15 @@ __device__ __forceinline__ void sinh_cosh_reduced2(float2 a, float2& shr, float2
 }
 
 struct BetaF32 {
-  static constexpr int NC = 2;
   struct __align__(16) Rec {
     float4 a;  // x_hi, y_hi, x_lo, y_lo
     float4 b;  // S = zeta A / 2, 0, 0, 0
   };
   using Tgt = BetaTgt;
-  struct Params {
-    const double *x, *y;
-  };
-  __device__ static Tgt load_target(const Params& p, int64_t i) {
-    Tgt t;
-    split2(p.x[i], t.xh, t.xl);
-    split2(p.y[i], t.yh, t.yl);
-    return t;
-  }
-  // Two targets at once in packed FP32x2 arithmetic (the engine calls interact2 for target
-  // pairs).  2^-k comes from the bits of the magic-number sum that rounds a / ln 2 (a clamped
-  // to 87 < 126 ln 2: beyond it the terms have reached their limits, u -> S sign(dy), v -> 0);
-  // 2^(1-k) = 2^-k + 2^-k and 4^-k = (2^-k)^2, which underflows to 0 for k > 63 as it should.
-  static constexpr bool kPairs = true;
+  // Two targets at once in packed FP32x2 arithmetic.  2^-k comes from the bits of the
+  // magic-number sum that rounds a / ln 2 (a clamped to 87 < 126 ln 2: beyond it the terms
+  // have reached their limits, u -> S sign(dy), v -> 0); 2^(1-k) = 2^-k + 2^-k and
+  // 4^-k = (2^-k)^2, which underflows to 0 for k > 63 as it should.
   __device__ static __forceinline__ void interact2(const Tgt& t0, const Tgt& t1, const Rec& r, float (&a0)[2],
                                                    float (&a1)[2]) {
     float2 tt, dy;

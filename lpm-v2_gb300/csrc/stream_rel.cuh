@@ -613,25 +613,20 @@ __global__ void __launch_bounds__(THREADS, MINB) sphere_swe_rel_sweep_kernel(Swe
 
 // ====================================================================== beta-plane stream functions
 // The beta plane's SetStreamFunctionsOnMesh, src/BetaPlane.f90:399-442, in FP32 for two
-// targets at a time on the generic hi/lo engine:
+// targets at a time (the direct form of beta_stream_rel_sweep_kernel, csrc/beta_rel.cuh):
 //   G = log(cosh(2 pi dy) - cos(2 pi dx)) / (4 pi),  psi += G zeta_j A_j  (j != i).
 // cosh 2a - cos 2b = 2 (sinh^2 a + sin^2 b) = 2 4^(k-1) (sh'^2 + sn'^2) with a = pi |dy| =
 // k ln 2 + r, b = pi dx and the 2^(k-1)-scaled sh', sn' of BetaF32, so
 //   4 pi G = (2k - 1) ln 2 + ln(sh'^2 + sn'^2),
 // no cancellation for close pairs and no overflow for far ones; the (2k - 1) ln 2 rides on the
 // exponent of ln_q2_shift.  S = zeta A / (4 pi); the self pair (sh' = sn' = 0) is a zero term.
-// Terms of both signs cancel to psi, so the FP32 partials are flushed every 32 sources.
+// Terms of both signs cancel to psi, so the caller flushes the FP32 partials often.
 struct BetaStreamF32 {
-  static constexpr int NC = 2;
-  static constexpr int kFlush = 32;
-  static constexpr bool kPairs = true;
   struct __align__(16) Rec {
     float4 a;  // x_hi, y_hi, x_lo, y_lo
     float4 b;  // S_rel, S_abs, 0, 0
   };
   using Tgt = BetaTgt;
-  using Params = BetaF32::Params;
-  __device__ static Tgt load_target(const Params& p, int64_t i) { return BetaF32::load_target(p, i); }
   __device__ static __forceinline__ void interact2(const Tgt& t0, const Tgt& t1, const Rec& r, float (&a0)[2],
                                                    float (&a1)[2], const float2* tab) {
     float2 tt, dy;

@@ -254,21 +254,6 @@ __global__ void finish_stream_kernel(const double* partial, int64_t nsplit, int6
   }
 }
 
-template <class Op, int THREADS, int TPT, int TILE, int MINB>
-void launch_sweep(const SumJob& job, const SumPlan& plan, const typename Op::Params& p) {
-  SweepArgs<Op> a;
-  a.p = p;
-  a.src = static_cast<const typename Op::Rec*>(job.src_buf);
-  a.n_tiles = plan.n_tiles;
-  a.tiles_per_chunk = plan.tiles_per_chunk;
-  a.ib = job.ib;
-  a.nt = job.nt;
-  a.partial = job.partial;
-  a.status = job.status;
-  const dim3 grid(static_cast<unsigned>(ceil_div(job.nt, THREADS * TPT)), static_cast<unsigned>(plan.nsplit));
-  sweep_fp32c_kernel<Op, THREADS, TPT, TILE, MINB><<<grid, THREADS, 0, job.stream>>>(a);
-}
-
 int tile_of(int kind, int mode) {
   if (mode == LPM_MODE_FP64) return k64Tile;
   switch (kind) {
