@@ -45,6 +45,9 @@ sys.path.insert(0, str(ROOT / "lpm-v2_gb300"))
 
 METRIC = "BVE direct-sum Ginteractions/s, FP32-comp vs FP64 on GB300 at <=1e-6 rel err"
 UNIT = "Ginteractions/s"
+# the PSE operators that have an FP64 form only (their FP32C form would be ill-conditioned):
+# --workload sum runs them in FP64 whatever --mode says
+FP64_ONLY_SUMS = ("pse_plane_grad", "pse_plane_second", "pse_plane_ddot", "pse_sphere_ddot", "pse_interp")
 FLOPS_PER_INTERACTION = 24  # dot 5, a^2-dot 1, x4pi a 1, zeta A/den 2, cross 9, accumulate 6
 L2_FLUSH_BYTES = 256 << 20
 # DRAM bytes (read + write) of one full-size sweep launch, from the ncu capture recorded in
@@ -68,7 +71,8 @@ def parse_args():
                    help="rk4: the headline single-instance step; ensemble: the 64-instance batch")
     p.add_argument("--instances", type=int, default=64)
     p.add_argument("--sum", choices=["bve", "plane", "pse_k8", "pse_gauss", "pse_grad", "pse_div", "pse_plane",
-                                     "stream", "plane_stream", "beta", "beta_stream", "swe_plane", "swe_sphere"],
+                                     "stream", "plane_stream", "beta", "beta_stream", "swe_plane", "swe_sphere"]
+                   + list(FP64_ONLY_SUMS),
                    default="bve",
                    help="--workload sum: which direct sum (one host C-ABI call per step)")
     p.add_argument("--mode", choices=["fp32c", "fp64"], default="fp32c", help="--workload sum: precision mode")
@@ -618,6 +622,23 @@ def sum_oracle_call(kind, v):
     if kind == "beta_stream":
         return lambda ib, ie: orc.beta_plane_stream(c["x"], c["y"], c["zeta"], v["absv"], c["area"], c["active"],
                                                     ib=ib, ie=ie)
+    if kind == "pse_plane_grad":
+        m = v["m"]
+        return lambda ib, ie: orc.pse_plane_gradient(m.x, m.y, v["f"], m.area, m.active, v["eps"], ib=ib, ie=ie)
+    if kind == "pse_plane_second":
+        m = v["m"]
+        return lambda ib, ie: orc.pse_plane_second_partials(m.x, m.y, *v["g"], m.area, m.active, v["eps"], ib=ib,
+                                                            ie=ie)
+    if kind == "pse_plane_ddot":
+        m = v["m"]
+        return lambda ib, ie: orc.pse_plane_double_dot(m.x, m.y, *v["g"], m.area, m.active, v["eps"], ib=ib, ie=ie)
+    if kind == "pse_sphere_ddot":
+        return lambda ib, ie: orc.pse_sphere_double_dot(c["x"], c["y"], c["z"], *v["v"], c["area"], c["active"],
+                                                        v["eps"], 1.0, ib=ib, ie=ie)
+    if kind == "pse_interp":
+        m, q = v["m"], v["q"]
+        return lambda ib, ie: orc.pse_interpolate(m.x, m.y, None, v["f"], m.area, m.active, v["eps"], q[0][ib:ie],
+                                                  q[1][ib:ie], None, 0)
     if kind == "pse_plane":
         m = v["m"]
         return lambda ib, ie: orc.pse_laplacian(m.x, m.y, None, v["f"], m.area, m.active, v["eps"], 1.0,
@@ -663,6 +684,7 @@ def run_sum(args):
 
     world, rank, local = dist_env()
     torch.cuda.set_device(local)
+    mode = "fp64" if args.sum in FP64_ONLY_SUMS else args.mode
     if args.sum in ("bve", "stream"):
         c = wl.config_rh54_icos(args.nest, seed=0)
         n, ns = c["x"].size, int(c["active"].sum())
@@ -725,6 +747,39 @@ def run_sum(args):
         call = lambda ie: lg.pse_plane_laplacian_at_particles(m.x, m.y, f, m.area, m.active, eps, kernel=lg.PSE_K8_CHORD,
                                                               i_end=ie, mode=args.mode)
         mesh = f"quad nest {args.nest} on [-4,4]^2, K8 of the chord, eps {eps:.4g}"
+    elif args.sum in ("pse_plane_grad", "pse_plane_second", "pse_plane_ddot", "pse_interp"):
+        m = lg.PolyMesh2d(lg.QUAD_RECT_SEED, args.nest, 4.0)
+        n, ns = m.n, int(m.active.sum())
+        eps = m.max_edge_length ** 0.75
+        f = np.exp(-(m.x * m.x + m.y * m.y)) * np.cos(2.0 * m.x)
+        # a smooth velocity-like pair of fields (the gradient of f, in closed form)
+        g = (np.exp(-(m.x * m.x + m.y * m.y)) * (-2.0 * m.x * np.cos(2.0 * m.x) - 2.0 * np.sin(2.0 * m.x)),
+             np.exp(-(m.x * m.x + m.y * m.y)) * (-2.0 * m.y * np.cos(2.0 * m.x)))
+        if args.sum == "pse_plane_grad":
+            call = lambda ie: lg.pse_plane_gradient_at_particles(m.x, m.y, f, m.area, m.active, eps, i_end=ie,
+                                                                 mode=mode)
+        elif args.sum == "pse_plane_second":
+            call = lambda ie: lg.pse_plane_second_partials_at_particles(m.x, m.y, *g, m.area, m.active, eps,
+                                                                        i_end=ie, mode=mode)
+        elif args.sum == "pse_plane_ddot":
+            call = lambda ie: lg.pse_plane_double_dot_product_at_particles(m.x, m.y, *g, m.area, m.active, eps,
+                                                                           i_end=ie, mode=mode)
+        else:
+            # query points: the particles shifted by a third of an edge (seeded), one per particle
+            rng = np.random.default_rng(0)
+            h = float(np.sqrt(m.area[m.active == 1].max()))
+            q = (m.x + rng.uniform(-h / 3, h / 3, n), m.y + rng.uniform(-h / 3, h / 3, n))
+            call = lambda ie: lg.pse_interpolate_scalar(m.x, m.y, None, f, m.area, m.active, eps, q[0][:ie],
+                                                        q[1][:ie], geometry=lg.GEOMETRY_PLANE, mode=mode)
+        mesh = f"quad nest {args.nest} on [-4,4]^2, K8 of the chord, eps {eps:.4g}"
+    elif args.sum == "pse_sphere_ddot":
+        c = wl.config_pse_cubed(args.nest)
+        n, ns = c["x"].size, int(c["active"].sum())
+        eps = c["eps_k8"]
+        v = wl.y54_surface_gradient(c["x"], c["y"], c["z"])
+        call = lambda ie: lg.pse_sphere_double_dot_product_at_particles(c["x"], c["y"], c["z"], *v, c["area"],
+                                                                        c["active"], eps, 1.0, i_end=ie, mode=mode)
+        mesh = f"cubed sphere nest {args.nest}, eps {eps:.4g} (the surface gradient of y54)"
     elif args.sum in ("pse_grad", "pse_div"):
         c = wl.config_pse_cubed(args.nest)
         n, ns = c["x"].size, int(c["active"].sum())
@@ -756,7 +811,7 @@ def run_sum(args):
         call(nt)
         times.append(time.perf_counter() - t0)
     t = min(times)
-    line = {"metric": f"{args.sum} direct sum Ginteractions/s ({args.mode}, host-buffer C ABI)",
+    line = {"metric": f"{args.sum} direct sum Ginteractions/s ({mode}, host-buffer C ABI)",
             "value": nt * ns / t / 1e9, "unit": UNIT, "steps": args.steps, "ms_per_step": 1e3 * t,
             "config": {"workload": f"{args.sum} on {mesh}: {nt} of {n} targets, {ns} sources",
                        "timing": "host wall clock around each call (copies included), best of the steps"}}

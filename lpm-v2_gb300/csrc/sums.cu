@@ -45,10 +45,38 @@ constexpr int k64Threads = 128, k64Tile = 128;
 // ------------------------------------------------------------------ FP64 sequential sweep
 // One thread per target, sources in ascending particle order, one accumulator: the same
 // summation order as the Fortran j loop, hence bit-identical sums.
+//
+// The PSE kernels all carry exp(-r^2), r = distance / eps: a pair with r >= 10 adds less than
+// 1e-37 of a near pair's term, far below the FP64 sums' 1e-12 agreement with the reference
+// (whose exp is not CUDA's anyway).  For those a warp skips a whole source tile when every one
+// of its targets is farther than the tile's radius plus `reach` from the tile's centre, in the
+// space the distance is measured in:
+//   - unit directions for the great-circle kernels (reach 10 eps / radius; the angle is never
+//     shorter than the chord of the unit directions);
+//   - raw positions for the chord and planar ones (reach 10 eps).
+// The pairs it keeps are summed in the reference's order.
+struct Fp64Cut {
+  const double4* bounds = nullptr;  // per source tile: centre and radius in the test space
+  const double *x = nullptr, *y = nullptr, *z = nullptr;  // target positions (z may be null)
+  double reach = 0.0;
+  int unit = 0;  // 1: the test space is unit directions
+};
+
+__device__ __forceinline__ double3 cut_point(const double* x, const double* y, const double* z, int64_t i,
+                                             int unit) {
+  double3 q = make_double3(x[i], y[i], z ? z[i] : 0.0);
+  if (unit) {
+    const double nq = sqrt(q.x * q.x + q.y * q.y + q.z * q.z);
+    const double inv = nq > 0.0 ? 1.0 / nq : 0.0;
+    q = make_double3(q.x * inv, q.y * inv, q.z * inv);
+  }
+  return q;
+}
+
 template <class Op, class Rec, class P>
 __global__ void __launch_bounds__(k64Threads) seq_fp64_kernel(P p, const Rec* __restrict__ src,
                                                               int64_t ns, int64_t ib, int64_t nt,
-                                                              int* status) {
+                                                              int* status, Fp64Cut cut = Fp64Cut{}) {
   __shared__ __align__(128) Rec stage[2][k64Tile];
   __shared__ __align__(8) uint64_t bars[2];
   const int64_t il = static_cast<int64_t>(blockIdx.x) * k64Threads + threadIdx.x;
@@ -57,21 +85,69 @@ __global__ void __launch_bounds__(k64Threads) seq_fp64_kernel(P p, const Rec* __
   const typename Op::Tgt t = Op::load(p, i);
   typename Op::Acc acc{};
   const int64_t n_tiles = ceil_div(ns, k64Tile);
+  const double3 tp = cut.bounds ? cut_point(cut.x, cut.y, cut.z, i, cut.unit) : make_double3(0.0, 0.0, 0.0);
   int64_t tile = 0;
   pipe_init(bars);
   uint32_t g = 0;
   staged_sweep<Rec, k64Tile>(src, 0, n_tiles, stage[0], stage[1], bars, g, status,
                              [&](const Rec* tl) {
-                               const int64_t j0 = tile * k64Tile;
-                               const int cnt = static_cast<int>(ns - j0 < k64Tile ? ns - j0 : k64Tile);
-                               for (int j = 0; j < cnt; ++j) {
-                                 const Rec& r = tl[j];
-                                 if (Op::kSkipSelf && r.idx == i) continue;
-                                 Op::interact(p, t, r, acc);
+                               bool run = true;
+                               if (cut.bounds) {
+                                 const double4 b = cut.bounds[tile];
+                                 const double dx = tp.x - b.x, dy = tp.y - b.y, dz = tp.z - b.z;
+                                 const double lim = b.w + cut.reach;
+                                 run = __any_sync(0xffffffffu, dx * dx + dy * dy + dz * dz <= lim * lim);
+                               }
+                               if (run) {
+                                 const int64_t j0 = tile * k64Tile;
+                                 const int cnt = static_cast<int>(ns - j0 < k64Tile ? ns - j0 : k64Tile);
+                                 for (int j = 0; j < cnt; ++j) {
+                                   const Rec& r = tl[j];
+                                   if (Op::kSkipSelf && r.idx == i) continue;
+                                   Op::interact(p, t, r, acc);
+                                 }
                                }
                                ++tile;
                              });
   if (valid) Op::store(p, i, il, acc);
+}
+
+// The bounding ball (centre, radius) of each FP64 source tile (k64Tile consecutive active
+// sources) in the cutoff's test space; one CTA of k64Tile threads per tile.  The radius is
+// widened by 1e-9 of itself and of the centre's size, which covers the rounding of the test.
+__global__ void __launch_bounds__(k64Tile) tile_bounds64_kernel(const double* x, const double* y, const double* z,
+                                                                const int32_t* idx, int64_t ns, int unit,
+                                                                double4* bounds) {
+  __shared__ double red[4][k64Tile];
+  const int tid = threadIdx.x;
+  const int64_t k = static_cast<int64_t>(blockIdx.x) * k64Tile + tid;
+  const bool valid = k < ns;
+  const double3 q = valid ? cut_point(x, y, z, idx[k], unit) : make_double3(0.0, 0.0, 0.0);
+  red[0][tid] = q.x;
+  red[1][tid] = q.y;
+  red[2][tid] = q.z;
+  red[3][tid] = valid ? 1.0 : 0.0;
+  __syncthreads();
+  for (int w = k64Tile / 2; w > 0; w >>= 1) {
+    if (tid < w) {
+#pragma unroll
+      for (int c = 0; c < 4; ++c) red[c][tid] += red[c][tid + w];
+    }
+    __syncthreads();
+  }
+  const double cnt = red[3][0] > 0.0 ? red[3][0] : 1.0;
+  const double cx = red[0][0] / cnt, cy = red[1][0] / cnt, cz = red[2][0] / cnt;
+  __syncthreads();
+  red[0][tid] = valid ? sqrt((q.x - cx) * (q.x - cx) + (q.y - cy) * (q.y - cy) + (q.z - cz) * (q.z - cz)) : 0.0;
+  __syncthreads();
+  for (int w = k64Tile / 2; w > 0; w >>= 1) {
+    if (tid < w) red[0][tid] = fmax(red[0][tid], red[0][tid + w]);
+    __syncthreads();
+  }
+  if (tid == 0) {
+    const double sz = fabs(cx) + fabs(cy) + fabs(cz);
+    bounds[blockIdx.x] = make_double4(cx, cy, cz, red[0][0] * (1.0 + 1e-9) + 1e-9 * sz);
+  }
 }
 
 // ------------------------------------------------------------------ prep kernels
@@ -254,6 +330,30 @@ __global__ void finish_stream_kernel(const double* partial, int64_t nsplit, int6
   }
 }
 
+// The FP64 kinds whose kernel decays as exp(-r^2) (the PSE operators), whose sweep skips
+// source tiles beyond r = 10; *unit tells whether the distance is a great-circle one.
+bool fp64_cutoff(int kind, int* unit) {
+  switch (kind) {
+    case kSumPseK8Geo:
+    case kSumPseGrad:
+    case kSumPseDiv:
+    case kSumPseSphereDdot:
+    case kSumPseInterpSphere:
+      *unit = 1;
+      return true;
+    case kSumPseGaussChord:
+    case kSumPseK8Chord:
+    case kSumPsePlaneGrad:
+    case kSumPsePlaneSecond:
+    case kSumPsePlaneDdot:
+    case kSumPseInterpPlane:
+      *unit = 0;
+      return true;
+    default:
+      return false;
+  }
+}
+
 int tile_of(int kind, int mode) {
   if (mode == LPM_MODE_FP64) return k64Tile;
   switch (kind) {
@@ -418,6 +518,11 @@ SumPlan plan_sum(int kind, int mode, int64_t ns, int64_t nt, int sm_count, int s
                    2 * sizeof(double);
   }
   if (mode == LPM_MODE_FP64) {
+    int unit = 0;
+    if (fp64_cutoff(kind, &unit)) {
+      // the tiles' bounding balls follow the records
+      pl.src_bytes = align_up(pl.src_bytes, 256) + static_cast<size_t>(pl.n_tiles) * sizeof(double4);
+    }
     pl.nsplit = 1;
     pl.tiles_per_chunk = pl.n_tiles;
     pl.partial_bytes = 0;
@@ -555,6 +660,19 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
 
   if (job.mode == LPM_MODE_FP64) {
     const unsigned g = static_cast<unsigned>(ceil_div(job.nt, k64Threads));
+    Fp64Cut cut;
+    if (fp64_cutoff(job.kind, &cut.unit)) {
+      double4* bounds = reinterpret_cast<double4*>(
+          static_cast<char*>(job.src_buf) +
+          align_up(static_cast<size_t>(plan.n_tiles) * k64Tile * rec_bytes(job.kind, job.mode), 256));
+      tile_bounds64_kernel<<<static_cast<unsigned>(plan.n_tiles), k64Tile, 0, job.stream>>>(
+          job.x, job.y, job.z, job.src_idx, job.ns, cut.unit, bounds);
+      cut.bounds = bounds;
+      cut.x = job.x;
+      cut.y = job.y;
+      cut.z = job.z;
+      cut.reach = 10.0 * job.eps / (cut.unit ? job.radius : 1.0);
+    }
     switch (job.kind) {
       case kSumBve:
       case kSumBveMesh: {
@@ -591,13 +709,13 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
         const Rec64* src = static_cast<const Rec64*>(job.src_buf);
         if (job.kind == kSumPseK8Geo) {
           seq_fp64_kernel<PseF64<kPseK8Geodesic>, Rec64><<<g, k64Threads, 0, job.stream>>>(
-              p, src, job.ns, job.ib, job.nt, job.status);
+              p, src, job.ns, job.ib, job.nt, job.status, cut);
         } else if (job.kind == kSumPseGaussChord) {
           seq_fp64_kernel<PseF64<kPseGaussChord>, Rec64><<<g, k64Threads, 0, job.stream>>>(
-              p, src, job.ns, job.ib, job.nt, job.status);
+              p, src, job.ns, job.ib, job.nt, job.status, cut);
         } else {
           seq_fp64_kernel<PseF64<kPseK8Chord>, Rec64><<<g, k64Threads, 0, job.stream>>>(
-              p, src, job.ns, job.ib, job.nt, job.status);
+              p, src, job.ns, job.ib, job.nt, job.status, cut);
         }
         break;
       }
@@ -612,14 +730,14 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
                                                                  job.src_idx, job.ns, 1,
                                                                  static_cast<Rec64*>(job.src_buf));
           seq_fp64_kernel<PseGradF64, Rec64><<<g, k64Threads, 0, job.stream>>>(
-              p, static_cast<const Rec64*>(job.src_buf), job.ns, job.ib, job.nt, job.status);
+              p, static_cast<const Rec64*>(job.src_buf), job.ns, job.ib, job.nt, job.status, cut);
         } else {
           p.scale = 1.0 / job.eps;  // MultiplyFieldByScalar(divergence, 1/eps)
           prep_vec64_kernel<<<prep_grid_ns, pb, 0, job.stream>>>(job.x, job.y, job.z, job.s1, job.s2, job.s3,
                                                                  job.area, job.src_idx, job.ns,
                                                                  static_cast<RecVec64*>(job.src_buf));
           seq_fp64_kernel<PseDivF64, RecVec64><<<g, k64Threads, 0, job.stream>>>(
-              p, static_cast<const RecVec64*>(job.src_buf), job.ns, job.ib, job.nt, job.status);
+              p, static_cast<const RecVec64*>(job.src_buf), job.ns, job.ib, job.nt, job.status, cut);
         }
         break;
       }
@@ -651,13 +769,13 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
         const Rec64* src = static_cast<const Rec64*>(job.src_buf);
         if (job.kind == kSumPsePlaneGrad) {
           seq_fp64_kernel<PsePlaneGradF64, Rec64><<<g, k64Threads, 0, job.stream>>>(p, src, job.ns, job.ib, job.nt,
-                                                                                    job.status);
+                                                                                    job.status, cut);
         } else if (job.kind == kSumPseInterpPlane) {
           seq_fp64_kernel<PseInterpF64<false>, Rec64><<<g, k64Threads, 0, job.stream>>>(p, src, job.ns, job.ib,
-                                                                                        job.nt, job.status);
+                                                                                        job.nt, job.status, cut);
         } else {
           seq_fp64_kernel<PseInterpF64<true>, Rec64><<<g, k64Threads, 0, job.stream>>>(p, src, job.ns, job.ib,
-                                                                                       job.nt, job.status);
+                                                                                       job.nt, job.status, cut);
         }
         break;
       }
@@ -676,15 +794,15 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
         switch (job.kind) {
           case kSumPsePlaneSecond:
             seq_fp64_kernel<PsePlaneSecondF64, RecVec64><<<g, k64Threads, 0, job.stream>>>(p, src, job.ns, job.ib,
-                                                                                          job.nt, job.status);
+                                                                                          job.nt, job.status, cut);
             break;
           case kSumPsePlaneDdot:
             seq_fp64_kernel<PsePlaneDdotF64, RecVec64><<<g, k64Threads, 0, job.stream>>>(p, src, job.ns, job.ib,
-                                                                                        job.nt, job.status);
+                                                                                        job.nt, job.status, cut);
             break;
           case kSumPseSphereDdot:
             seq_fp64_kernel<PseSphereDdotF64, RecVec64><<<g, k64Threads, 0, job.stream>>>(p, src, job.ns, job.ib,
-                                                                                         job.nt, job.status);
+                                                                                         job.nt, job.status, cut);
             break;
           case kSumSwePlane:
             p.k0 = 2.0 * kPi;  // 2.0_kreal * PI
