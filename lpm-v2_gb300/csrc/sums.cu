@@ -41,6 +41,7 @@ constexpr int kSweMinB = 3;        // planar SWE velocity sweep: 128 x 4 targets
 constexpr int kSweSphereMinB = 2;  // sphere SWE velocity sweep: 2 CTAs per SM (no spills; 10 % over 3)
 // FP64 sequential sweep shape
 constexpr int k64Threads = 128, k64Tile = 128;
+constexpr int kSplit64 = 4;  // lanes per target of the split FP64 sweep (small target sets; 8 was slower)
 
 // ------------------------------------------------------------------ FP64 sequential sweep
 // One thread per target, sources in ascending particle order, one accumulator: the same
@@ -79,7 +80,7 @@ __global__ void __launch_bounds__(k64Threads) seq_fp64_kernel(P p, const Rec* __
                                                               int* status, Fp64Cut cut = Fp64Cut{}) {
   __shared__ __align__(128) Rec stage[2][k64Tile];
   __shared__ __align__(8) uint64_t bars[2];
-  const int64_t il = static_cast<int64_t>(blockIdx.x) * k64Threads + threadIdx.x;
+  const int64_t il = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   const bool valid = il < nt;
   const int64_t i = ib + (valid ? il : nt - 1);
   const typename Op::Tgt t = Op::load(p, i);
@@ -110,6 +111,59 @@ __global__ void __launch_bounds__(k64Threads) seq_fp64_kernel(P p, const Rec* __
                                ++tile;
                              });
   if (valid) Op::store(p, i, il, acc);
+}
+
+// The FP64 sweep for a small target set, S lanes per target.  Lane k of a target's group
+// evaluates sources j = j0 + k of each run of S, on an accumulator of zero, so it holds the
+// term itself (0 + X = X).  The group's first lane adds the S terms in ascending j, with the
+// same rounding as the sequential sweep.  This is for operators whose interact adds exactly
+// one term to each accumulator component (a = a + X, or a = a - X, which is a + (-X)), so the
+// sums stay bit-identical up to the sign of an exact zero.  S times as many warps share the
+// FP64 work.
+template <class Op, class Rec, class P, int S>
+__global__ void __launch_bounds__(k64Threads) seq_fp64_split_kernel(P p, const Rec* __restrict__ src,
+                                                                    int64_t ns, int64_t ib, int64_t nt,
+                                                                    int* status) {
+  static_assert(32 % S == 0, "a target's lanes stay in one warp");
+  using Acc = typename Op::Acc;
+  static_assert(sizeof(Acc) % sizeof(double) == 0, "accumulators are doubles");
+  constexpr int NA = static_cast<int>(sizeof(Acc) / sizeof(double));
+  __shared__ __align__(128) Rec stage[2][k64Tile];
+  __shared__ __align__(8) uint64_t bars[2];
+  const int k = static_cast<int>(threadIdx.x) % S;
+  const int lane0 = static_cast<int>(threadIdx.x & 31u) - k;  // the group's first lane in the warp
+  const int64_t il = static_cast<int64_t>(blockIdx.x) * (k64Threads / S) + threadIdx.x / S;
+  const bool valid = il < nt;
+  const int64_t i = ib + (valid ? il : nt - 1);
+  const typename Op::Tgt t = Op::load(p, i);
+  Acc acc{};
+  double* av = reinterpret_cast<double*>(&acc);
+  const int64_t n_tiles = ceil_div(ns, k64Tile);
+  int64_t tile = 0;
+  pipe_init(bars);
+  uint32_t g = 0;
+  staged_sweep<Rec, k64Tile>(src, 0, n_tiles, stage[0], stage[1], bars, g, status, [&](const Rec* tl) {
+    const int64_t j0 = tile * k64Tile;
+    const int cnt = static_cast<int>(ns - j0 < k64Tile ? ns - j0 : k64Tile);
+    for (int jb = 0; jb < cnt; jb += S) {
+      const int j = jb + k;
+      Acc d{};
+      const bool has = j < cnt && !(Op::kSkipSelf && tl[j < cnt ? j : 0].idx == i);
+      if (has) Op::interact(p, t, tl[j], d);
+      const double* dv = reinterpret_cast<const double*>(&d);
+#pragma unroll
+      for (int q = 0; q < S; ++q) {
+        const bool hq = __shfl_sync(0xffffffffu, has, lane0 + q);
+#pragma unroll
+        for (int c = 0; c < NA; ++c) {
+          const double x = __shfl_sync(0xffffffffu, dv[c], lane0 + q);
+          if (hq) av[c] = __dadd_rn(av[c], x);
+        }
+      }
+    }
+    ++tile;
+  });
+  if (valid && k == 0) Op::store(p, i, il, acc);
 }
 
 // The bounding ball (centre, radius) of each FP64 source tile (k64Tile consecutive active
@@ -523,6 +577,10 @@ SumPlan plan_sum(int kind, int mode, int64_t ns, int64_t nt, int sm_count, int s
       // the tiles' bounding balls follow the records
       pl.src_bytes = align_up(pl.src_bytes, 256) + static_cast<size_t>(pl.n_tiles) * sizeof(double4);
     }
+    // one target per thread and no split (the sum is sequential per target): a small target
+    // set takes CTAs of one warp so that more SMs share the FP64 work
+    const int64_t sms = sm_count > 0 ? sm_count : 152;
+    pl.fp64_threads = ceil_div(nt, k64Threads) < 2 * sms ? 32 : k64Threads;
     pl.nsplit = 1;
     pl.tiles_per_chunk = pl.n_tiles;
     pl.partial_bytes = 0;
@@ -659,7 +717,9 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
   const unsigned prep_grid_pad = static_cast<unsigned>(ceil_div(npad, pb));
 
   if (job.mode == LPM_MODE_FP64) {
-    const unsigned g = static_cast<unsigned>(ceil_div(job.nt, k64Threads));
+    const int t64 = plan.fp64_threads == 32 ? 32 : k64Threads;
+    const unsigned g = static_cast<unsigned>(ceil_div(job.nt, t64));
+    const unsigned gs = static_cast<unsigned>(ceil_div(job.nt, k64Threads / kSplit64));  // the split sweep's grid
     Fp64Cut cut;
     if (fp64_cutoff(job.kind, &cut.unit)) {
       double4* bounds = reinterpret_cast<double4*>(
@@ -681,12 +741,20 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
                                                                static_cast<Rec64*>(job.src_buf));
         BveF64Params p{job.x, job.y, job.z, job.radius * job.radius, (4.0 * kPi) * job.radius,
                        job.out0, job.out1, job.out2};
-        if (job.kind == kSumBve) {
-          seq_fp64_kernel<BveF64<0>, Rec64><<<g, k64Threads, 0, job.stream>>>(
-              p, static_cast<const Rec64*>(job.src_buf), job.ns, job.ib, job.nt, job.status);
+        const Rec64* src = static_cast<const Rec64*>(job.src_buf);
+        if (t64 == 32) {
+          // a small target set: kSplit64 lanes per target (the terms in parallel, the sum in order)
+          if (job.kind == kSumBve) {
+            seq_fp64_split_kernel<BveF64<0>, Rec64, BveF64Params, kSplit64><<<gs, k64Threads, 0, job.stream>>>(
+                p, src, job.ns, job.ib, job.nt, job.status);
+          } else {
+            seq_fp64_split_kernel<BveF64<1>, Rec64, BveF64Params, kSplit64><<<gs, k64Threads, 0, job.stream>>>(
+                p, src, job.ns, job.ib, job.nt, job.status);
+          }
+        } else if (job.kind == kSumBve) {
+          seq_fp64_kernel<BveF64<0>, Rec64><<<g, t64, 0, job.stream>>>(p, src, job.ns, job.ib, job.nt, job.status);
         } else {
-          seq_fp64_kernel<BveF64<1>, Rec64><<<g, k64Threads, 0, job.stream>>>(
-              p, static_cast<const Rec64*>(job.src_buf), job.ns, job.ib, job.nt, job.status);
+          seq_fp64_kernel<BveF64<1>, Rec64><<<g, t64, 0, job.stream>>>(p, src, job.ns, job.ib, job.nt, job.status);
         }
         break;
       }
@@ -694,8 +762,14 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
         prep_plane64_kernel<<<prep_grid_ns, pb, 0, job.stream>>>(job.x, job.y, job.s1, job.area, job.src_idx,
                                                                  job.ns, static_cast<RecPlane64*>(job.src_buf));
         PlaneF64Params p{job.x, job.y, 2.0 * kPi, job.delta * job.delta, job.out0, job.out1};
-        seq_fp64_kernel<PlaneF64, RecPlane64><<<g, k64Threads, 0, job.stream>>>(
-            p, static_cast<const RecPlane64*>(job.src_buf), job.ns, job.ib, job.nt, job.status);
+        const RecPlane64* src = static_cast<const RecPlane64*>(job.src_buf);
+        if (t64 == 32) {
+          seq_fp64_split_kernel<PlaneF64, RecPlane64, PlaneF64Params, kSplit64><<<gs, k64Threads, 0, job.stream>>>(
+              p, src, job.ns, job.ib, job.nt, job.status);
+        } else {
+          seq_fp64_kernel<PlaneF64, RecPlane64><<<g, t64, 0, job.stream>>>(p, src, job.ns, job.ib, job.nt,
+                                                                           job.status);
+        }
         break;
       }
       case kSumPseK8Geo:
@@ -708,13 +782,13 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
         PseF64Params p{job.x, job.y, job.z, job.s1, job.eps, eps2, 1.0 / eps2, job.radius, job.out0};
         const Rec64* src = static_cast<const Rec64*>(job.src_buf);
         if (job.kind == kSumPseK8Geo) {
-          seq_fp64_kernel<PseF64<kPseK8Geodesic>, Rec64><<<g, k64Threads, 0, job.stream>>>(
+          seq_fp64_kernel<PseF64<kPseK8Geodesic>, Rec64><<<g, t64, 0, job.stream>>>(
               p, src, job.ns, job.ib, job.nt, job.status, cut);
         } else if (job.kind == kSumPseGaussChord) {
-          seq_fp64_kernel<PseF64<kPseGaussChord>, Rec64><<<g, k64Threads, 0, job.stream>>>(
+          seq_fp64_kernel<PseF64<kPseGaussChord>, Rec64><<<g, t64, 0, job.stream>>>(
               p, src, job.ns, job.ib, job.nt, job.status, cut);
         } else {
-          seq_fp64_kernel<PseF64<kPseK8Chord>, Rec64><<<g, k64Threads, 0, job.stream>>>(
+          seq_fp64_kernel<PseF64<kPseK8Chord>, Rec64><<<g, t64, 0, job.stream>>>(
               p, src, job.ns, job.ib, job.nt, job.status, cut);
         }
         break;
@@ -729,14 +803,14 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
           prep_rec64_kernel<<<prep_grid_ns, pb, 0, job.stream>>>(job.x, job.y, job.z, job.s1, job.area,
                                                                  job.src_idx, job.ns, 1,
                                                                  static_cast<Rec64*>(job.src_buf));
-          seq_fp64_kernel<PseGradF64, Rec64><<<g, k64Threads, 0, job.stream>>>(
+          seq_fp64_kernel<PseGradF64, Rec64><<<g, t64, 0, job.stream>>>(
               p, static_cast<const Rec64*>(job.src_buf), job.ns, job.ib, job.nt, job.status, cut);
         } else {
           p.scale = 1.0 / job.eps;  // MultiplyFieldByScalar(divergence, 1/eps)
           prep_vec64_kernel<<<prep_grid_ns, pb, 0, job.stream>>>(job.x, job.y, job.z, job.s1, job.s2, job.s3,
                                                                  job.area, job.src_idx, job.ns,
                                                                  static_cast<RecVec64*>(job.src_buf));
-          seq_fp64_kernel<PseDivF64, RecVec64><<<g, k64Threads, 0, job.stream>>>(
+          seq_fp64_kernel<PseDivF64, RecVec64><<<g, t64, 0, job.stream>>>(
               p, static_cast<const RecVec64*>(job.src_buf), job.ns, job.ib, job.nt, job.status, cut);
         }
         break;
@@ -749,10 +823,10 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
         StreamF64Params p{job.x, job.y, job.z, job.radius * job.radius, 4.0 * kPi, 2.0 * kPi, job.out0, job.out1};
         const RecStream64* src = static_cast<const RecStream64*>(job.src_buf);
         if (job.kind == kSumSphereStream) {
-          seq_fp64_kernel<SphereStreamF64, RecStream64><<<g, k64Threads, 0, job.stream>>>(
+          seq_fp64_kernel<SphereStreamF64, RecStream64><<<g, t64, 0, job.stream>>>(
               p, src, job.ns, job.ib, job.nt, job.status);
         } else {
-          seq_fp64_kernel<PlaneStreamF64, RecStream64><<<g, k64Threads, 0, job.stream>>>(
+          seq_fp64_kernel<PlaneStreamF64, RecStream64><<<g, t64, 0, job.stream>>>(
               p, src, job.ns, job.ib, job.nt, job.status);
         }
         break;
@@ -768,13 +842,13 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
                           job.radius, job.radius2, 0.0, 1.0 / job.eps, job.out0, job.out1, job.out2, job.out3};
         const Rec64* src = static_cast<const Rec64*>(job.src_buf);
         if (job.kind == kSumPsePlaneGrad) {
-          seq_fp64_kernel<PsePlaneGradF64, Rec64><<<g, k64Threads, 0, job.stream>>>(p, src, job.ns, job.ib, job.nt,
+          seq_fp64_kernel<PsePlaneGradF64, Rec64><<<g, t64, 0, job.stream>>>(p, src, job.ns, job.ib, job.nt,
                                                                                     job.status, cut);
         } else if (job.kind == kSumPseInterpPlane) {
-          seq_fp64_kernel<PseInterpF64<false>, Rec64><<<g, k64Threads, 0, job.stream>>>(p, src, job.ns, job.ib,
+          seq_fp64_kernel<PseInterpF64<false>, Rec64><<<g, t64, 0, job.stream>>>(p, src, job.ns, job.ib,
                                                                                         job.nt, job.status, cut);
         } else {
-          seq_fp64_kernel<PseInterpF64<true>, Rec64><<<g, k64Threads, 0, job.stream>>>(p, src, job.ns, job.ib,
+          seq_fp64_kernel<PseInterpF64<true>, Rec64><<<g, t64, 0, job.stream>>>(p, src, job.ns, job.ib,
                                                                                        job.nt, job.status, cut);
         }
         break;
@@ -793,25 +867,25 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
         const RecVec64* src = static_cast<const RecVec64*>(job.src_buf);
         switch (job.kind) {
           case kSumPsePlaneSecond:
-            seq_fp64_kernel<PsePlaneSecondF64, RecVec64><<<g, k64Threads, 0, job.stream>>>(p, src, job.ns, job.ib,
+            seq_fp64_kernel<PsePlaneSecondF64, RecVec64><<<g, t64, 0, job.stream>>>(p, src, job.ns, job.ib,
                                                                                           job.nt, job.status, cut);
             break;
           case kSumPsePlaneDdot:
-            seq_fp64_kernel<PsePlaneDdotF64, RecVec64><<<g, k64Threads, 0, job.stream>>>(p, src, job.ns, job.ib,
+            seq_fp64_kernel<PsePlaneDdotF64, RecVec64><<<g, t64, 0, job.stream>>>(p, src, job.ns, job.ib,
                                                                                         job.nt, job.status, cut);
             break;
           case kSumPseSphereDdot:
-            seq_fp64_kernel<PseSphereDdotF64, RecVec64><<<g, k64Threads, 0, job.stream>>>(p, src, job.ns, job.ib,
+            seq_fp64_kernel<PseSphereDdotF64, RecVec64><<<g, t64, 0, job.stream>>>(p, src, job.ns, job.ib,
                                                                                          job.nt, job.status, cut);
             break;
           case kSumSwePlane:
             p.k0 = 2.0 * kPi;  // 2.0_kreal * PI
-            seq_fp64_kernel<SwePlaneF64, RecVec64><<<g, k64Threads, 0, job.stream>>>(p, src, job.ns, job.ib,
+            seq_fp64_kernel<SwePlaneF64, RecVec64><<<g, t64, 0, job.stream>>>(p, src, job.ns, job.ib,
                                                                                     job.nt, job.status);
             break;
           default:
             p.k0 = ((4.0 * kPi) * job.radius) * job.radius;  // 4.0_kreal * PI * radius * radius
-            seq_fp64_kernel<SweSphereF64, RecVec64><<<g, k64Threads, 0, job.stream>>>(p, src, job.ns, job.ib,
+            seq_fp64_kernel<SweSphereF64, RecVec64><<<g, t64, 0, job.stream>>>(p, src, job.ns, job.ib,
                                                                                      job.nt, job.status);
             break;
         }
@@ -825,10 +899,10 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
         BetaF64Params p{job.x, job.y, 2.0 * kPi, 4.0 * kPi, job.out0, job.out1};
         const RecStream64* src = static_cast<const RecStream64*>(job.src_buf);
         if (job.kind == kSumBetaPlane) {
-          seq_fp64_kernel<BetaVelF64, RecStream64><<<g, k64Threads, 0, job.stream>>>(p, src, job.ns, job.ib, job.nt,
+          seq_fp64_kernel<BetaVelF64, RecStream64><<<g, t64, 0, job.stream>>>(p, src, job.ns, job.ib, job.nt,
                                                                                     job.status);
         } else {
-          seq_fp64_kernel<BetaStreamF64, RecStream64><<<g, k64Threads, 0, job.stream>>>(p, src, job.ns, job.ib,
+          seq_fp64_kernel<BetaStreamF64, RecStream64><<<g, t64, 0, job.stream>>>(p, src, job.ns, job.ib,
                                                                                        job.nt, job.status);
         }
         break;
