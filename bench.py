@@ -67,7 +67,7 @@ def parse_args():
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline sample budget")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--workload", choices=["rk4", "ensemble", "stream", "configs", "sum"], default="rk4",
+    p.add_argument("--workload", choices=["rk4", "ensemble", "stream", "configs", "sum", "remesh"], default="rk4",
                    help="rk4: the headline single-instance step; ensemble: the 64-instance batch")
     p.add_argument("--instances", type=int, default=64)
     p.add_argument("--sum", choices=["bve", "plane", "pse_k8", "pse_gauss", "pse_grad", "pse_div", "pse_plane",
@@ -826,6 +826,58 @@ def collections_counter(values):
     return out
 
 
+def run_remesh(args):
+    """Remesh without rebuilding the solver (lpm_bve_solver_remesh) against the reference's
+    Delete + New of the solver per remesh (examples/BVESingleGaussianVortex.f90:218-246), in
+    FP32C at icosahedral nest `--nest`.  The new particle set is the mesh's own (positions,
+    vorticity, area, mask), loaded after the solver has advanced one step; both paths compute
+    the new set's velocity (setVelocityFromVorticity), as New does.  Each timed pass is
+    remesh (or create) followed by one RK4 step, synchronised."""
+    import torch
+    import lpm_gpu as lg
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    c, n, ns, per_sum = workload(args.nest)
+    omega = 2.0 * np.pi
+    new_set = (c["x"], c["y"], c["z"], c["zeta"], c["area"], c["active"])
+    s = lg.BVESolver(*new_set, 1.0, omega, mode="fp32c")
+    s.timestep(0.01)
+
+    def via_remesh():
+        s.remesh(*new_set)
+        s.timestep(0.01)
+        torch.cuda.synchronize()
+
+    def via_create():
+        t = lg.BVESolver(*new_set, 1.0, omega, mode="fp32c")
+        t.timestep(0.01)
+        torch.cuda.synchronize()
+        t.close()
+
+    for _ in range(max(args.warmup, 3)):
+        via_remesh()
+        via_create()
+    tr, tc = [], []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        via_remesh()
+        tr.append(time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        via_create()
+        tc.append(time.perf_counter() - t0)
+    r_ms, c_ms = 1e3 * min(tr), 1e3 * min(tc)
+    line = {"metric": "remesh + one RK4 step, ms (FP32C)", "value": r_ms, "unit": "ms", "higher_is_better": False,
+            "steps": args.steps, "rebuild_ms": c_ms, "rebuild_over_remesh": c_ms / r_ms,
+            "config": {"workload": f"icosahedral nest {args.nest} ({n} particles, {ns} sources): remesh with the "
+                                   f"mesh's own set, then one RK4 step (4 velocity sums), against destroy + "
+                                   f"create + one step",
+                       "timing": "host wall clock, synchronised, best of the steps"}}
+    s.close()
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
@@ -838,6 +890,8 @@ def main():
         return run_configs(args)
     if args.workload == "sum":
         return run_sum(args)
+    if args.workload == "remesh":
+        return run_remesh(args)
     return run_ours(args)
 
 
