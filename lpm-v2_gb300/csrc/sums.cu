@@ -34,7 +34,7 @@ struct BveShape {
 constexpr BveShape kBveShapes[] = {{128, 4, 4}, {256, 4, 2}, {128, 6, 2}, {128, 8, 2}};
 constexpr int kBveShapeCount = sizeof(kBveShapes) / sizeof(kBveShapes[0]);
 constexpr int kPlaneThreads = 128, kPlaneTpt = 4, kPlaneTile = 256, kPlaneMinB = 4;
-constexpr int kPseThreads = 128, kPseTpt = 4, kPseTile = 128, kPseMinB = 4;
+constexpr int kPseThreads = 128, kPseTpt = 4, kPseTile = 256, kPseMinB = 4;
 constexpr int kStreamThreads = 128, kStreamTpt = 4, kStreamTile = 256, kStreamMinB = 4;
 constexpr int kBetaThreads = 128, kBetaTpt = 4, kBetaTile = 256, kBetaMinB = 4;
 constexpr int kSweMinB = 3;        // planar SWE velocity sweep: 128 x 4 targets, 3 CTAs per SM
