@@ -313,3 +313,60 @@ def test_beta_plane_fp32c_ragged_and_empty(lg, oracle_mod, n):
     u, v = lg.beta_plane_velocity(x, y, zeta, area, none, mode="fp32c")
     pr, pa = lg.beta_plane_stream_functions(x, y, zeta, absv, area, none, mode="fp32c")
     assert not np.any(u) and not np.any(v) and not np.any(pr) and not np.any(pa)
+
+
+def test_pse_fp64_tile_cutoff_plane(lg, oracle_mod):
+    """The FP64 PSE sweeps skip source tiles beyond r = 10 (exp(-r^2) < 1e-43): at quad nest 6
+    on [-4,4]^2 with eps = 2h = 0.25 (reach 2.5) most tiles are out of a warp's reach, and every
+    planar operator stays within 1e-12 of the all-pairs oracle, on a block of targets too."""
+    m, act, eps = _plane(lg, 6, 21)
+    f = np.exp(-0.3 * (m.x ** 2 + m.y ** 2)) * np.cos(m.x) + 0.2
+    u, v = np.cos(0.5 * m.y), 0.3 * np.sin(m.x)
+    for ib, ie in ((1, m.n), (5001, 9000)):
+        s = slice(ib - 1, ie)
+        gx, gy = lg.pse_plane_gradient_at_particles(m.x, m.y, f, m.area, act, eps, ib, ie)
+        rx, ry = oracle_mod.pse_plane_gradient(m.x, m.y, f, m.area, act, eps, ib - 1, ie)
+        assert rel(gx[s], rx) <= TOL and rel(gy[s], ry) <= TOL
+        xx, xy, yy = lg.pse_plane_second_partials_at_particles(m.x, m.y, u, v, m.area, act, eps, ib, ie)
+        r = oracle_mod.pse_plane_second_partials(m.x, m.y, u, v, m.area, act, eps, ib - 1, ie)
+        for g, rr in zip((xx, xy, yy), r):
+            assert rel(g[s], rr) <= TOL
+        dd = lg.pse_plane_double_dot_product_at_particles(m.x, m.y, u, v, m.area, act, eps, ib, ie)
+        rd = oracle_mod.pse_plane_double_dot(m.x, m.y, u, v, m.area, act, eps, ib - 1, ie)
+        assert rel(dd[s], rd) <= TOL
+        lap = lg.pse_plane_laplacian_at_particles(m.x, m.y, f, m.area, act, eps, kernel=lg.PSE_K8_CHORD,
+                                                  i_begin=ib, i_end=ie, mode="fp64")
+        rl = oracle_mod.pse_laplacian(m.x, m.y, None, f, m.area, act, eps, 1.0, oracle_mod.PSE_K8_CHORD, ib - 1, ie)
+        assert rel(lap[s], rl) <= TOL
+    rng = np.random.default_rng(4)
+    qx, qy = rng.uniform(-3.5, 3.5, 2000), rng.uniform(-3.5, 3.5, 2000)
+    got = lg.pse_interpolate_scalar(m.x, m.y, None, f, m.area, act, eps, qx, qy)
+    ref = oracle_mod.pse_interpolate(m.x, m.y, None, f, m.area, act, eps, qx, qy, None, 0)
+    assert rel(got, ref) <= TOL
+
+
+@pytest.mark.parametrize("radius", [1.0, 6.37122e6])
+def test_pse_fp64_tile_cutoff_sphere(lg, oracle_mod, radius):
+    """The great-circle FP64 PSE sweeps with the tile cutoff (reach 10 eps / radius on unit
+    directions) at cubed nest 5 with eps = 0.06 radius: Laplacian (K8 geodesic and Gaussian
+    chord), gradient, divergence and double dot within 1e-12 of the all-pairs oracle."""
+    m = lg.PolyMesh2d(lg.CUBED_SPHERE_SEED, 5, 1.0)
+    x, y, z = m.x * radius, m.y * radius, m.z * radius
+    area = m.area * radius ** 2
+    f = np.cos(3.0 * m.x) * np.sin(2.0 * m.z) + 0.5
+    u, v, w = -m.y, m.x, 0.2 * m.z
+    eps = 0.06 * radius
+    for kern in (lg.PSE_K8_GEODESIC, lg.PSE_GAUSS_CHORD):
+        got = lg.pse_sphere_laplacian_at_particles(x, y, z, f, area, m.active, eps, radius, kern, mode="fp64")
+        ref = oracle_mod.pse_laplacian(x, y, z, f, area, m.active, eps, radius, kern)
+        assert rel(got, ref) <= TOL
+    g = lg.pse_sphere_gradient_at_particles(x, y, z, f, area, m.active, eps, radius, mode="fp64")
+    r = oracle_mod.pse_sphere_gradient(x, y, z, f, area, m.active, eps, radius)
+    for a, b in zip(g, r):
+        assert rel(a, b) <= TOL
+    d = lg.pse_sphere_divergence_at_particles(x, y, z, u, v, w, area, m.active, eps, radius, mode="fp64")
+    rd = oracle_mod.pse_sphere_divergence(x, y, z, u, v, w, area, m.active, eps, radius)
+    assert rel(d, rd) <= TOL
+    dd = lg.pse_sphere_double_dot_product_at_particles(x, y, z, u, v, w, area, m.active, eps, radius)
+    rdd = oracle_mod.pse_sphere_double_dot(x, y, z, u, v, w, area, m.active, eps, radius)
+    assert rel(dd, rdd) <= TOL
