@@ -577,10 +577,12 @@ SumPlan plan_sum(int kind, int mode, int64_t ns, int64_t nt, int sm_count, int s
       // the tiles' bounding balls follow the records
       pl.src_bytes = align_up(pl.src_bytes, 256) + static_cast<size_t>(pl.n_tiles) * sizeof(double4);
     }
-    // one target per thread and no split (the sum is sequential per target): a small target
-    // set takes CTAs of one warp so that more SMs share the FP64 work
+    // one target per thread and no split (the sum is sequential per target): a target set
+    // too small for one 128-thread CTA per SM takes CTAs of one warp (and, for the BVE and
+    // planar velocity, the split sweep) so that more SMs share the FP64 work.  At one CTA
+    // per SM and above the sequential sweep keeps the FP64 pipe busy (85 % at icos nest 5).
     const int64_t sms = sm_count > 0 ? sm_count : 152;
-    pl.fp64_threads = ceil_div(nt, k64Threads) < 2 * sms ? 32 : k64Threads;
+    pl.fp64_threads = ceil_div(nt, k64Threads) < sms ? 32 : k64Threads;
     pl.nsplit = 1;
     pl.tiles_per_chunk = pl.n_tiles;
     pl.partial_bytes = 0;
