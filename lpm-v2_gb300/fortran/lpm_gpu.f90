@@ -31,6 +31,8 @@ public :: lpm_bve_solver_create, lpm_bve_timestep, lpm_bve_get_state, lpm_bve_se
 public :: lpm_bve_diagnostics, lpm_bve_solver_stream_functions, lpm_bve_solver_destroy
 public :: lpm_plane_solver_create, lpm_plane_timestep, lpm_plane_get_state, lpm_plane_diagnostics
 public :: lpm_plane_solver_destroy
+public :: lpm_ensemble_create, lpm_ensemble_timestep, lpm_ensemble_velocity, lpm_ensemble_get_state
+public :: lpm_ensemble_destroy, lpm_bve_kernel_timing, lpm_bve_solver_set_timing, lpm_version
 
 integer(c_int), parameter :: LPM_MODE_FP64 = 0
 integer(c_int), parameter :: LPM_MODE_FP32C = 1
@@ -374,6 +376,61 @@ interface
 	integer(c_int) function lpm_plane_solver_destroy(solver) bind(C, name="lpm_plane_solver_destroy")
 		import :: c_int, c_ptr
 		type(c_ptr), value :: solver
+	end function
+
+	! ---- many BVE instances advanced together (instance k owns offsets(k+1) .. offsets(k+2)-1,
+	!      0-based, of the concatenated arrays; radius and rotation_rate per instance)
+	integer(c_int) function lpm_ensemble_create(ens, n_instances, offsets, x, y, z, relvort, area, active, &
+			radius, rotation_rate, mode) bind(C, name="lpm_ensemble_create")
+		import :: c_int, c_int32_t, c_int64_t, c_double, c_ptr
+		type(c_ptr), intent(out) :: ens
+		integer(c_int), value :: n_instances
+		integer(c_int64_t), intent(in) :: offsets(*)
+		real(c_double), intent(in) :: x(*), y(*), z(*), relvort(*), area(*), radius(*), rotation_rate(*)
+		integer(c_int32_t), intent(in) :: active(*)
+		integer(c_int), value :: mode
+	end function
+
+	integer(c_int) function lpm_ensemble_timestep(ens, dt, n_steps, renormalize) bind(C, name="lpm_ensemble_timestep")
+		import :: c_int, c_double, c_ptr
+		type(c_ptr), value :: ens
+		real(c_double), value :: dt
+		integer(c_int), value :: n_steps, renormalize
+	end function
+
+	integer(c_int) function lpm_ensemble_velocity(ens) bind(C, name="lpm_ensemble_velocity")
+		import :: c_int, c_ptr
+		type(c_ptr), value :: ens
+	end function
+
+	integer(c_int) function lpm_ensemble_get_state(ens, x, y, z, relvort, u, v, w) &
+			bind(C, name="lpm_ensemble_get_state")
+		import :: c_int, c_double, c_ptr
+		type(c_ptr), value :: ens
+		real(c_double), intent(out) :: x(*), y(*), z(*), relvort(*), u(*), v(*), w(*)
+	end function
+
+	integer(c_int) function lpm_ensemble_destroy(ens) bind(C, name="lpm_ensemble_destroy")
+		import :: c_int, c_ptr
+		type(c_ptr), value :: ens
+	end function
+
+	! ---- timing and version
+	integer(c_int) function lpm_bve_kernel_timing(solver, total_ms, launches) bind(C, name="lpm_bve_kernel_timing")
+		import :: c_int, c_int64_t, c_double, c_ptr
+		type(c_ptr), value :: solver
+		real(c_double), intent(out) :: total_ms
+		integer(c_int64_t), intent(out) :: launches
+	end function
+
+	integer(c_int) function lpm_bve_solver_set_timing(solver, enable) bind(C, name="lpm_bve_solver_set_timing")
+		import :: c_int, c_ptr
+		type(c_ptr), value :: solver
+		integer(c_int), value :: enable
+	end function
+
+	type(c_ptr) function lpm_version() bind(C, name="lpm_version")
+		import :: c_ptr
 	end function
 end interface
 
