@@ -1,5 +1,6 @@
-// beta_rel.cuh -- the beta-plane (x-periodic) velocity in FP32C on 2-D Hilbert-ordered sources
-// in groups of 64, with a complex far form.
+// beta_rel.cuh -- the beta-plane (x-periodic) velocity and stream functions in FP32C on 2-D
+// Hilbert-ordered sources in groups of 64, with complex far forms (the stream functions'
+// follow the velocity kernel below).
 //
 // Reference: BetaPlaneVelocity, src/BetaPlaneSolver.f90:227-268:
 //   s_j = 0.5 zeta_j A_j / (cosh(2 pi dy) - cos(2 pi dx)),  u -= sinh(2 pi dy) s_j,
@@ -10,8 +11,8 @@
 // (e_i - e_j) = i (1 + 2 e_j / (e_i - e_j)), so a group contributes
 //   v + i u = i (S_g + 2 G),  G = sum_j S_j e_j / (e_i - e_j),  S_g = sum_j S_j:
 // u += S_g + 2 Re G, v -= 2 Im G.  Per target pair and source: e_i - e_j (2 FADD2), |.|^2 (2),
-// 2 MUFU, S_j e_j conj(e_i - e_j) (4) and the accumulation (2) -- 12 packed operations against
-// about 28 for the direct form.  e_j is formed in FP64 by the prep kernel; e_i once per target
+// 2 MUFU, S_j e_j conj(e_i - e_j) (4) and the accumulation (2) -- 10 packed operations and 2
+// MUFU against about 28 packed operations for the direct form.  e_j is formed in FP64 by the prep kernel; e_i once per target
 // and group with expf and sincospif.  The periodicity in x is in e itself.
 // An error delta in e_i moves e_i - e_j by delta |e_i|, i.e. by delta / (2 pi |z_i - z_j|)
 // relative, so the complex form is kept for targets beyond max(5 R, 0.02) of the group
