@@ -56,19 +56,26 @@ constexpr int kSplit64 = 4;  // lanes per target of the split FP64 sweep (small 
 //     shorter than the chord of the unit directions);
 //   - raw positions for the chord and planar ones (reach 10 eps).
 // The pairs it keeps are summed in the reference's order.
+struct __align__(32) TileBall {
+  double x, y, z, r;  // centre and radius in the test space
+};
+
 struct Fp64Cut {
-  const double4* bounds = nullptr;  // per source tile: centre and radius in the test space
+  const TileBall* bounds = nullptr;  // per source tile
   const double *x = nullptr, *y = nullptr, *z = nullptr;  // target positions (z may be null)
   double reach = 0.0;
   int unit = 0;  // 1: the test space is unit directions
 };
 
+// The point of particle i in the test space.  A point at the origin has no direction (and
+// atan2(0, 0) puts it at distance 0 from everything): it becomes NaN, which the tests below
+// read as "in reach", so nothing is skipped for it.
 __device__ __forceinline__ double3 cut_point(const double* x, const double* y, const double* z, int64_t i,
                                              int unit) {
   double3 q = make_double3(x[i], y[i], z ? z[i] : 0.0);
   if (unit) {
     const double nq = sqrt(q.x * q.x + q.y * q.y + q.z * q.z);
-    const double inv = nq > 0.0 ? 1.0 / nq : 0.0;
+    const double inv = nq > 0.0 ? 1.0 / nq : __longlong_as_double(0x7ff8000000000000LL);
     q = make_double3(q.x * inv, q.y * inv, q.z * inv);
   }
   return q;
@@ -94,10 +101,10 @@ __global__ void __launch_bounds__(k64Threads) seq_fp64_kernel(P p, const Rec* __
                              [&](const Rec* tl) {
                                bool run = true;
                                if (cut.bounds) {
-                                 const double4 b = cut.bounds[tile];
+                                 const TileBall b = cut.bounds[tile];
                                  const double dx = tp.x - b.x, dy = tp.y - b.y, dz = tp.z - b.z;
-                                 const double lim = b.w + cut.reach;
-                                 run = __any_sync(0xffffffffu, dx * dx + dy * dy + dz * dz <= lim * lim);
+                                 const double lim = b.r + cut.reach;
+                                 run = __any_sync(0xffffffffu, !(dx * dx + dy * dy + dz * dz > lim * lim));
                                }
                                if (run) {
                                  const int64_t j0 = tile * k64Tile;
@@ -171,16 +178,19 @@ __global__ void __launch_bounds__(k64Threads) seq_fp64_split_kernel(P p, const R
 // widened by 1e-9 of itself and of the centre's size, which covers the rounding of the test.
 __global__ void __launch_bounds__(k64Tile) tile_bounds64_kernel(const double* x, const double* y, const double* z,
                                                                 const int32_t* idx, int64_t ns, int unit,
-                                                                double4* bounds) {
+                                                                TileBall* bounds) {
   __shared__ double red[4][k64Tile];
   const int tid = threadIdx.x;
   const int64_t k = static_cast<int64_t>(blockIdx.x) * k64Tile + tid;
   const bool valid = k < ns;
   const double3 q = valid ? cut_point(x, y, z, idx[k], unit) : make_double3(0.0, 0.0, 0.0);
-  red[0][tid] = q.x;
-  red[1][tid] = q.y;
-  red[2][tid] = q.z;
-  red[3][tid] = valid ? 1.0 : 0.0;
+  // a source without a direction (NaN point) leaves the centre alone and makes the radius
+  // infinite: the tile is in reach of every target
+  const bool dirless = valid && !(q.x == q.x && q.y == q.y && q.z == q.z);
+  red[0][tid] = dirless ? 0.0 : q.x;
+  red[1][tid] = dirless ? 0.0 : q.y;
+  red[2][tid] = dirless ? 0.0 : q.z;
+  red[3][tid] = valid && !dirless ? 1.0 : 0.0;
   __syncthreads();
   for (int w = k64Tile / 2; w > 0; w >>= 1) {
     if (tid < w) {
@@ -192,7 +202,9 @@ __global__ void __launch_bounds__(k64Tile) tile_bounds64_kernel(const double* x,
   const double cnt = red[3][0] > 0.0 ? red[3][0] : 1.0;
   const double cx = red[0][0] / cnt, cy = red[1][0] / cnt, cz = red[2][0] / cnt;
   __syncthreads();
-  red[0][tid] = valid ? sqrt((q.x - cx) * (q.x - cx) + (q.y - cy) * (q.y - cy) + (q.z - cz) * (q.z - cz)) : 0.0;
+  red[0][tid] = dirless ? __longlong_as_double(0x7ff0000000000000LL)
+                : valid ? sqrt((q.x - cx) * (q.x - cx) + (q.y - cy) * (q.y - cy) + (q.z - cz) * (q.z - cz))
+                        : 0.0;
   __syncthreads();
   for (int w = k64Tile / 2; w > 0; w >>= 1) {
     if (tid < w) red[0][tid] = fmax(red[0][tid], red[0][tid + w]);
@@ -200,7 +212,7 @@ __global__ void __launch_bounds__(k64Tile) tile_bounds64_kernel(const double* x,
   }
   if (tid == 0) {
     const double sz = fabs(cx) + fabs(cy) + fabs(cz);
-    bounds[blockIdx.x] = make_double4(cx, cy, cz, red[0][0] * (1.0 + 1e-9) + 1e-9 * sz);
+    bounds[blockIdx.x] = TileBall{cx, cy, cz, red[0][0] * (1.0 + 1e-9) + 1e-9 * sz};
   }
 }
 
@@ -575,7 +587,7 @@ SumPlan plan_sum(int kind, int mode, int64_t ns, int64_t nt, int sm_count, int s
     int unit = 0;
     if (fp64_cutoff(kind, &unit)) {
       // the tiles' bounding balls follow the records
-      pl.src_bytes = align_up(pl.src_bytes, 256) + static_cast<size_t>(pl.n_tiles) * sizeof(double4);
+      pl.src_bytes = align_up(pl.src_bytes, 256) + static_cast<size_t>(pl.n_tiles) * sizeof(TileBall);
     }
     // one target per thread and no split (the sum is sequential per target): a target set
     // too small for one 128-thread CTA per SM takes CTAs of one warp (and, for the BVE and
@@ -724,7 +736,7 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
     const unsigned gs = static_cast<unsigned>(ceil_div(job.nt, k64Threads / kSplit64));  // the split sweep's grid
     Fp64Cut cut;
     if (fp64_cutoff(job.kind, &cut.unit)) {
-      double4* bounds = reinterpret_cast<double4*>(
+      TileBall* bounds = reinterpret_cast<TileBall*>(
           static_cast<char*>(job.src_buf) +
           align_up(static_cast<size_t>(plan.n_tiles) * k64Tile * rec_bytes(job.kind, job.mode), 256));
       tile_bounds64_kernel<<<static_cast<unsigned>(plan.n_tiles), k64Tile, 0, job.stream>>>(

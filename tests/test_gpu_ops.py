@@ -353,20 +353,29 @@ def test_pse_fp64_tile_cutoff_sphere(lg, oracle_mod, radius):
     m = lg.PolyMesh2d(lg.CUBED_SPHERE_SEED, 5, 1.0)
     x, y, z = m.x * radius, m.y * radius, m.z * radius
     area = m.area * radius ** 2
+    act = m.active.copy()
     f = np.cos(3.0 * m.x) * np.sin(2.0 * m.z) + 0.5
     u, v, w = -m.y, m.x, 0.2 * m.z
     eps = 0.06 * radius
-    for kern in (lg.PSE_K8_GEODESIC, lg.PSE_GAUSS_CHORD):
-        got = lg.pse_sphere_laplacian_at_particles(x, y, z, f, area, m.active, eps, radius, kern, mode="fp64")
-        ref = oracle_mod.pse_laplacian(x, y, z, f, area, m.active, eps, radius, kern)
-        assert rel(got, ref) <= TOL
-    g = lg.pse_sphere_gradient_at_particles(x, y, z, f, area, m.active, eps, radius, mode="fp64")
-    r = oracle_mod.pse_sphere_gradient(x, y, z, f, area, m.active, eps, radius)
-    for a, b in zip(g, r):
-        assert rel(a, b) <= TOL
-    d = lg.pse_sphere_divergence_at_particles(x, y, z, u, v, w, area, m.active, eps, radius, mode="fp64")
-    rd = oracle_mod.pse_sphere_divergence(x, y, z, u, v, w, area, m.active, eps, radius)
-    assert rel(d, rd) <= TOL
-    dd = lg.pse_sphere_double_dot_product_at_particles(x, y, z, u, v, w, area, m.active, eps, radius)
-    rdd = oracle_mod.pse_sphere_double_dot(x, y, z, u, v, w, area, m.active, eps, radius)
-    assert rel(dd, rdd) <= TOL
+    for origin in (False, True):
+        if origin:
+            # a particle at the centre: no direction, and at great-circle distance 0 from every
+            # other (atan2(0, 0) = 0), so no tile may be skipped for it or for its tile
+            x, y, z, area, f, u, v, w = (np.append(a, val) for a, val in
+                                         ((x, 0.0), (y, 0.0), (z, 0.0), (area, 1e-4 * radius ** 2), (f, 0.7),
+                                          (u, 0.1), (v, 0.2), (w, 0.3)))
+            act = np.append(act, 1).astype(np.int32)
+        for kern in (lg.PSE_K8_GEODESIC, lg.PSE_GAUSS_CHORD):
+            got = lg.pse_sphere_laplacian_at_particles(x, y, z, f, area, act, eps, radius, kern, mode="fp64")
+            ref = oracle_mod.pse_laplacian(x, y, z, f, area, act, eps, radius, kern)
+            assert rel(got, ref) <= TOL
+        g = lg.pse_sphere_gradient_at_particles(x, y, z, f, area, act, eps, radius, mode="fp64")
+        r = oracle_mod.pse_sphere_gradient(x, y, z, f, area, act, eps, radius)
+        for a, b in zip(g, r):
+            assert rel(a, b) <= TOL
+        d = lg.pse_sphere_divergence_at_particles(x, y, z, u, v, w, area, act, eps, radius, mode="fp64")
+        rd = oracle_mod.pse_sphere_divergence(x, y, z, u, v, w, area, act, eps, radius)
+        assert rel(d, rd) <= TOL
+        dd = lg.pse_sphere_double_dot_product_at_particles(x, y, z, u, v, w, area, act, eps, radius)
+        rdd = oracle_mod.pse_sphere_double_dot(x, y, z, u, v, w, area, act, eps, radius)
+        assert rel(dd, rdd) <= TOL
