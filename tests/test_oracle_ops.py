@@ -236,3 +236,76 @@ def test_beta_plane_stream_vs_numpy(oracle_mod):
         g = np.log(np.cosh(2 * np.pi * (y[i] - y[m])) - np.cos(2 * np.pi * (x[i] - x[m]))) / (4 * np.pi)
         assert abs(pr[i] - (g * zr[m] * a[m]).sum()) <= 1e-12 * np.abs(g * zr[m] * a[m]).sum()
         assert abs(pa[i] - (g * za[m] * a[m]).sum()) <= 1e-12 * np.abs(g * za[m] * a[m]).sum()
+
+
+def _beta_groups(rng, n_groups=6, per=64):
+    """Compact groups of sources on the strip, each with its centroid z_o and radius R."""
+    groups = []
+    for _ in range(n_groups):
+        c = np.array([rng.random(), rng.uniform(-0.5, 0.5)])
+        pts = c + rng.normal(0.0, 0.01, (per, 2))
+        groups.append(pts)
+    return groups
+
+
+def test_beta_complex_far_form_identity(oracle_mod):
+    """The beta-plane FP32C far form, in FP64 numpy: with e = exp(2 pi i (z - z_o)) about a
+    group's centroid, the group's velocity at a far target is u = S_g + 2 Re G, v = -2 Im G,
+    G = sum_j S_j e_j / (e_i - e_j); it equals the reference sum (the oracle) to rounding,
+    for targets beyond 4R of the group in the periodic distance, across x = 0 / 1 too."""
+    rng = np.random.default_rng(31)
+    groups = _beta_groups(rng)
+    tx, ty = rng.random(300), rng.uniform(-1.5, 1.5, 300)
+    for pts in groups:
+        ns = len(pts)
+        zeta = rng.uniform(-1.0, 1.0, ns)
+        area = rng.uniform(0.5, 1.5, ns) * 1e-4
+        x = np.concatenate([pts[:, 0], tx])
+        y = np.concatenate([pts[:, 1], ty])
+        zz = np.concatenate([zeta, np.zeros(tx.size)])
+        aa = np.concatenate([area, np.zeros(tx.size)])
+        act = np.concatenate([np.ones(ns), np.zeros(tx.size)]).astype(np.int32)
+        ru, rv = oracle_mod.beta_plane_velocity(x, y, zz, aa, act, ns, ns + tx.size)
+        zo = pts.mean(0)
+        R = np.sqrt(((pts - zo) ** 2).sum(1)).max()
+        S = 0.5 * zeta * area
+        ej = np.exp(2j * np.pi * ((pts[:, 0] - zo[0]) + 1j * (pts[:, 1] - zo[1])))
+        dx = tx - zo[0]
+        dx -= np.rint(dx)
+        far = dx * dx + (ty - zo[1]) ** 2 > (5.0 * R) ** 2
+        ei = np.exp(2j * np.pi * (dx + 1j * (ty - zo[1])))
+        G = (S[None, :] * ej[None, :] / (ei[:, None] - ej[None, :])).sum(1)
+        u = S.sum() + 2.0 * G.real
+        v = -2.0 * G.imag
+        scale = max(np.abs(ru).max(), np.abs(rv).max())
+        assert far.sum() > 200
+        assert np.abs(u - ru)[far].max() <= 1e-12 * scale and np.abs(v - rv)[far].max() <= 1e-12 * scale
+
+
+def test_beta_stream_far_form_identity(oracle_mod):
+    """The beta-plane stream far form, in FP64 numpy: |e_i - e_j|^2 = 2 |e_i| |e_j| (cosh 2 pi dy -
+    cos 2 pi dx) with ln|e| = -2 pi (y - y_o), so a group adds sum_j w_j ln|e_i - e_j|^2 +
+    W 2 pi (y_i - y_o) + C, W = sum w_j, C = sum w_j (2 pi (y_j - y_o) - ln 2), w = q A / (4 pi);
+    it equals the oracle's log(cosh - cos) / (4 pi) sum to rounding."""
+    rng = np.random.default_rng(32)
+    groups = _beta_groups(rng)
+    tx, ty = rng.random(300), rng.uniform(-2.0, 2.0, 300)
+    for pts in groups:
+        ns = len(pts)
+        q = rng.uniform(-1.0, 1.0, ns)
+        area = rng.uniform(0.5, 1.5, ns) * 1e-4
+        x = np.concatenate([pts[:, 0], tx])
+        y = np.concatenate([pts[:, 1], ty])
+        qq = np.concatenate([q, np.zeros(tx.size)])
+        aa = np.concatenate([area, np.zeros(tx.size)])
+        act = np.concatenate([np.ones(ns), np.zeros(tx.size)]).astype(np.int32)
+        rr, _ = oracle_mod.beta_plane_stream(x, y, qq, qq, aa, act, ns, ns + tx.size)
+        zo = pts.mean(0)
+        w = q * area / (4.0 * np.pi)
+        W = w.sum()
+        C = (w * (2.0 * np.pi * (pts[:, 1] - zo[1]) - np.log(2.0))).sum()
+        ej = np.exp(2j * np.pi * ((pts[:, 0] - zo[0]) + 1j * (pts[:, 1] - zo[1])))
+        ei = np.exp(2j * np.pi * ((tx - zo[0]) + 1j * (ty - zo[1])))
+        lg = np.log(np.abs(ei[:, None] - ej[None, :]) ** 2)
+        psi = (w[None, :] * lg).sum(1) + W * 2.0 * np.pi * (ty - zo[1]) + C
+        assert np.abs(psi - rr).max() <= 1e-12 * np.abs(rr).max()
