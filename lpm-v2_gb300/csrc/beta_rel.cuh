@@ -15,8 +15,8 @@
 // MUFU against about 28 packed operations for the direct form.  e_j is formed in FP64 by the prep kernel; e_i once per target
 // and group with expf and sincospif.  The periodicity in x is in e itself.
 // An error delta in e_i moves e_i - e_j by delta |e_i|, i.e. by delta / (2 pi |z_i - z_j|)
-// relative, so the complex form is kept for targets beyond max(5 R, 0.02) of the group
-// (|z_i - z_j| >= 4 R): a warp with any target nearer (in the periodic distance) sums that
+// relative, so the complex form is kept for targets beyond max(4 R, 0.02) of the group
+// (|z_i - z_j| >= 3 R): a warp with any target nearer (in the periodic distance) sums that
 // group with the direct, cancellation-free form of BetaF32 (csrc/ops.cuh), which also drops
 // the self pair.
 // Each tile's FP32 partial goes into compensated (hi, lo) pairs; partials [chunk][2][nt].
@@ -41,7 +41,7 @@ struct BetaRel {
     float4 f;  // R (the group radius about z_o), S_g, 0, 0
   };
   static constexpr int kGroup = 64;
-  static constexpr float kNearFactor = 5.0f;    // direct form for targets within 5 R
+  static constexpr float kNearFactor = 4.0f;    // direct form for targets within 4 R
   static constexpr float kMaxFarRadius = 2.0f;  // wider groups: direct form for all targets
 };
 
@@ -266,7 +266,7 @@ __global__ void __launch_bounds__(TILE) beta_rel_prep_kernel(const double* x, co
     split2(cy, oyh, oyl);
     o.o = make_float4(oxh, oyh, oxl, oyl);
     // a group wider than 2 (|e_j| up to e^(2 pi R)) is summed with the direct form by every
-    // target: its R is replaced by a value whose near limit (5 R)^2 is infinite
+    // target: its R is replaced by a value whose near limit (4 R)^2 is infinite
     const float rg = fmax_[g0] <= BetaRel::kMaxFarRadius ? fmax_[g0] : 3e37f;
     o.f = make_float4(rg, __double2float_rn(red[2][g0]), 0.f, 0.f);
     org[t * (TILE / G) + tid / G] = o;
