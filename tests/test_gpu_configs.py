@@ -1,0 +1,205 @@
+"""GPU parity at the benchmark configurations themselves, against the oracle.
+
+The other GPU tests pin each sum on small and ragged inputs.  These run the configurations
+the benchmarks are quoted on, at their own sizes (or, where the FP64 oracle would take
+minutes, on bounded target blocks of the full-size problem):
+
+  config 1  sphere BVE single Gaussian vortex, icos nest 4 (7,682 targets, 5,120 sources),
+            100 RK4 steps of dt = 0.01 in FP64: bit-identical to the oracle's timestepPrivate
+            (src/SphereBVESolver.f90:219-353; examples/BVESingleGaussianVortex.f90:216-270 with
+            remesh off).
+  config 2  planar colliding dipoles, quad nest 7 on [-4,4]^2 (131,585 targets, 65,536
+            sources), delta = 0 and 0.02: FP64 bit-identical and FP32C within 1e-6 on target
+            blocks against planarIncompressibleVelocity (src/PlaneIncompressibleSolver.f90:
+            278-316); 200 RK4 steps of dt = 0.005 (at quad nest 5, where the FP64 oracle
+            finishes in seconds) FP64 bit-identical to the oracle, with the FP32C solver
+            tracking the FP64 one.
+  config 4  sphere BVE at icos nest 8 (1,966,082 targets, 1,310,720 sources), RH4 + Gaussian
+            vortex: the FP32C sum on target blocks against the oracle, before and after one
+            RK4 step of the renormalising solver the benchmark times.
+  config 5  the 64-instance ensemble at icos nests 3-6: every instance's FP32C velocity on a
+            target block against the oracle, before and after two RK4 steps; and one
+            instance per nest 3-6 advanced one FP64 step, bit-identical to the oracle.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+FP32C_TOL = 1e-6
+
+
+@pytest.fixture(scope="module")
+def lg(built_lib):
+    return built_lib
+
+
+@pytest.fixture(scope="module")
+def wl(built_lib):
+    import workloads
+    return workloads
+
+
+def _rel_linf(got, ref):
+    got, ref = np.stack(got), np.stack(ref)
+    return float(np.abs(got - ref).max() / np.abs(ref).max())
+
+
+# ------------------------------------------------------------------ config 1
+def test_config1_icos4_100_steps_fp64_bit_exact(lg, wl, oracle_mod):
+    c = wl.config_gauss_vortex_icos(4)
+    assert c["x"].size == 7682 and int(c["active"].sum()) == 5120
+    a = (c["x"], c["y"], c["z"], c["zeta"], c["area"], c["active"])
+    u, v, w = oracle_mod.bve_velocity(*a, 1.0, oracle_mod.ASSOC_MESH)
+    ref = oracle_mod.bve_timestep(*a, u, v, w, 1.0, c["omega"], 0.01, 100)
+    s = lg.BVESolver(*a, 1.0, c["omega"], mode="fp64")
+    s.timestep(0.01, 100)
+    st = s.get_state()
+    s.close()
+    for k, r in zip(("x", "y", "z", "rel_vort", "u", "v", "w"), ref):
+        assert np.array_equal(st[k], r), k
+
+
+# ------------------------------------------------------------------ config 2
+@pytest.fixture(scope="module")
+def dipoles7(wl):
+    c = wl.config_colliding_dipoles(7)
+    assert c["x"].size == 131585 and int(c["active"].sum()) == 65536
+    return c
+
+
+@pytest.mark.parametrize("delta", [0.0, 0.02])
+def test_config2_quad7_velocity_blocks(lg, oracle_mod, dipoles7, delta):
+    """FP64 bit-identical to the oracle on three target blocks; FP32C within 1e-6 of the
+    largest velocity of the whole set (the relative L-infinity error the benchmark spec bounds).
+    Normalised by each block's own largest velocity instead, the block in the slow corner of
+    the domain, where the two dipoles' fields cancel, would read 1.3e-6 at delta = 0."""
+    c = dipoles7
+    a = (c["x"], c["y"], c["omega"], c["area"], c["active"])
+    n = c["x"].size
+    full32 = np.stack(lg.planar_incompressible_velocity(*a, delta, mode="fp32c"))
+    full64 = np.stack(lg.planar_incompressible_velocity(*a, delta, mode="fp64"))
+    umax = np.abs(full64).max()
+    for ib in (1, n // 2 - 2047, n - 4095):
+        ie = ib + 4095
+        ref = np.stack(oracle_mod.plane_velocity(*a, delta, ib=ib - 1, ie=ie))
+        assert np.array_equal(full64[:, ib - 1:ie], ref)
+        got64 = lg.planar_incompressible_velocity(*a, delta, i_begin=ib, i_end=ie, mode="fp64")
+        assert np.array_equal(np.stack(got64)[:, ib - 1:ie], ref)
+        assert np.abs(full32[:, ib - 1:ie] - ref).max() / umax <= FP32C_TOL
+    # the whole set against the bit-exact FP64 GPU sum
+    assert np.abs(full32 - full64).max() / umax <= FP32C_TOL
+
+
+def test_config2_200_steps_fp64_bit_exact_and_fp32c_track(lg, wl, oracle_mod):
+    """200 RK4 steps of dt = 0.005 with delta = 0.02 (quad nest 5): the FP64 solver is
+    bit-identical to the oracle's timestepPrivate (src/PlaneIncompressibleSolver.f90:171-259),
+    and the FP32C solver tracks it.  Over the first 20 steps (t = 0.1) the positions agree
+    to the velocity tolerance's reach, ~t 1e-6 |u|.  By t = 1 the dipoles have collided and
+    the strain at the collision amplifies any difference (1.3e-4 on a domain of size 8 was
+    measured), so the later bound only asks that the two runs stay on the same flow."""
+    c = wl.config_colliding_dipoles(5)
+    a = (c["x"], c["y"], c["omega"], c["area"], c["active"])
+    u0, v0 = oracle_mod.plane_velocity(*a, 0.02)
+    ref = oracle_mod.plane_timestep(*a, u0, v0, 0.02, 0.005, 200)
+    s64 = lg.PlaneSolver(*a, delta=0.02, mode="fp64")
+    s32 = lg.PlaneSolver(*a, delta=0.02, mode="fp32c")
+    track = {}
+    done = 0
+    for upto in (20, 50, 100, 200):
+        s64.timestep(0.005, upto - done)
+        s32.timestep(0.005, upto - done)
+        done = upto
+        g64, g32 = s64.get_state(), s32.get_state()
+        track[upto] = float(np.abs(np.stack([g32["x"] - g64["x"], g32["y"] - g64["y"]])).max())
+    d64, d32 = s64.diagnostics(), s32.diagnostics()
+    s64.close()
+    s32.close()
+    print("FP32C - FP64 position difference by step:", track)
+    for k, r in zip(("x", "y", "u", "v"), ref):
+        assert np.array_equal(g64[k], r), k
+    umax = np.abs(np.stack([g64["u"], g64["v"]])).max()
+    assert track[20] <= 0.1 * 1e-5 * max(umax, 1.0), track
+    assert track[200] <= 1e-3, track
+    assert abs(d32["kinetic_energy"] - d64["kinetic_energy"]) <= 1e-4 * d64["kinetic_energy"]
+    assert d32["circulation"] == d64["circulation"]  # omega is carried unchanged
+
+
+# ------------------------------------------------------------------ config 4
+@pytest.fixture(scope="module")
+def rh54_icos8(wl):
+    c = wl.config_rh54_icos(8, seed=0)
+    assert c["x"].size == 1966082 and int(c["active"].sum()) == 1310720
+    return c
+
+
+def _blocks(n, m=4096):
+    return [(n // 4, n // 4 + m - 1), (3 * n // 4, 3 * n // 4 + m - 1)]
+
+
+def test_config4_icos8_fp32c_blocks_vs_oracle(lg, oracle_mod, rh54_icos8):
+    c = rh54_icos8
+    a = (c["x"], c["y"], c["z"], c["zeta"], c["area"], c["active"])
+    got = lg.bve_sphere_velocity(*a, 1.0, mode="fp32c")
+    for ib, ie in _blocks(c["x"].size):
+        ref = oracle_mod.bve_velocity(*a, 1.0, ib=ib - 1, ie=ie)
+        assert _rel_linf([q[ib - 1:ie] for q in got], ref) <= FP32C_TOL
+
+
+def test_config4_icos8_rk4_step_vs_oracle(lg, oracle_mod, rh54_icos8):
+    """One RK4 step of the renormalising FP32C solver (the benchmark's step): the velocity it
+    leaves at the new positions, on target blocks, against the oracle at that state."""
+    c = rh54_icos8
+    s = lg.BVESolver(c["x"], c["y"], c["z"], c["zeta"], c["area"], c["active"], 1.0, c["omega"], mode="fp32c")
+    s.timestep(0.01, 1, renormalize=True)
+    st = s.get_state()
+    s.close()
+    for ib, ie in _blocks(c["x"].size):
+        ref = oracle_mod.bve_velocity(st["x"], st["y"], st["z"], st["rel_vort"], c["area"], c["active"], 1.0,
+                                      ib=ib - 1, ie=ie)
+        assert _rel_linf([st[k][ib - 1:ie] for k in ("u", "v", "w")], ref) <= FP32C_TOL
+
+
+# ------------------------------------------------------------------ config 5
+def _check_instances_vs_oracle(oracle_mod, inst, st, offs, m=512):
+    worst = 0.0
+    for k, d in enumerate(inst):
+        a, b = int(offs[k]), int(offs[k + 1])
+        sl = slice(a, b)
+        rng = np.random.default_rng(k)
+        ib = int(rng.integers(0, max(1, b - a - m)))
+        ie = min(b - a, ib + m)
+        ref = oracle_mod.bve_velocity(st["x"][sl], st["y"][sl], st["z"][sl], st["rel_vort"][sl], d["area"],
+                                      d["active"], d["radius"], ib=ib, ie=ie)
+        err = _rel_linf([st[q][a + ib:a + ie] for q in ("u", "v", "w")], ref)
+        assert err <= FP32C_TOL, (k, d["nest"], err)
+        worst = max(worst, err)
+    return worst
+
+
+def test_config5_ensemble_64_fp32c_vs_oracle(lg, wl, oracle_mod):
+    inst = wl.config_ensemble(n_instances=64, seed=0)
+    assert sorted({d["nest"] for d in inst}) == [3, 4, 5, 6]
+    ens = lg.Ensemble(inst, mode="fp32c")
+    _check_instances_vs_oracle(oracle_mod, inst, ens.get_state(), ens.offsets)
+    ens.timestep(0.01, 2, renormalize=True)
+    _check_instances_vs_oracle(oracle_mod, inst, ens.get_state(), ens.offsets)
+    ens.close()
+
+
+def test_config5_ensemble_one_per_nest_fp64_step_bit_exact(lg, wl, oracle_mod):
+    inst = []
+    for nest in (3, 4, 5, 6):
+        inst += [d for d in wl.config_ensemble(n_instances=1, seed=nest, nests=(nest,))]
+    ens = lg.Ensemble(inst, mode="fp64")
+    ens.timestep(0.01, 1)
+    st = ens.get_state()
+    offs = ens.offsets
+    ens.close()
+    for k, d in enumerate(inst):
+        a = (d["x"], d["y"], d["z"], d["rel_vort"], d["area"], d["active"])
+        u, v, w = oracle_mod.bve_velocity(*a, d["radius"], oracle_mod.ASSOC_MESH)
+        ref = oracle_mod.bve_timestep(*a, u, v, w, d["radius"], d["rotation_rate"], 0.01, 1)
+        sl = slice(int(offs[k]), int(offs[k + 1]))
+        for q, r in zip(("x", "y", "z", "rel_vort", "u", "v", "w"), ref):
+            assert np.array_equal(st[q][sl], r), (d["nest"], q)
