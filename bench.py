@@ -16,7 +16,13 @@ Metric: Ginteractions/s (interactions = N_targets * N_sources - self pairs per s
   e2e   : the same steps through the C ABI with the state copied from pinned host memory
           before and back after every step (lpm_bve_set_state / lpm_bve_timestep /
           lpm_bve_get_state), timed with CUDA events on the same stream
-  roofline: the velocity-sum kernels against the measured FP32 FMA peak (24 flops/pair)
+  roofline: the velocity-sum kernels against the measured FP32 FMA peak (24 flops/pair),
+          with the sweep's recorded ncu pipe utilisation beside the contract fraction
+  accuracy: the FP32C velocity at the final state against the oracle (FP64) on a target block
+  fp64_gpu: the plain FP64 GPU kernel (parity mode) on the same state, on a block of targets
+          that fills every SM, and the FP32C/FP64 ratio
+  ensemble: config 5 (64 uneven instances at icos nests 3-6), batched persistent launch
+          against one solver per instance, a few RK4 steps each
   cpu_baseline: the CPU oracle (the reference loop restated in C, OpenMP over targets) on
           a bounded sample of targets against all sources
 
@@ -50,9 +56,21 @@ UNIT = "Ginteractions/s"
 FP64_ONLY_SUMS = ("pse_plane_grad", "pse_plane_second", "pse_plane_ddot", "pse_sphere_ddot", "pse_interp")
 FLOPS_PER_INTERACTION = 24  # dot 5, a^2-dot 1, x4pi a 1, zeta A/den 2, cross 9, accumulate 6
 L2_FLUSH_BYTES = 256 << 20
-# DRAM bytes (read + write) of one full-size sweep launch, from the ncu capture recorded in
-# profiles/bve_rel_sweep_icos8_dram.md (ncu cannot run inside the timed benchmark)
+# DRAM bytes (ncu dram__bytes_read.sum + dram__bytes_write.sum) of one full-size icos nest 8
+# sweep launch, from a single-pass ncu capture of this benchmark's own step (ncu cannot run
+# inside the timed region, so this is a recorded constant, not a figure of this run)
 SWEEP_TRAFFIC_ICOS8 = 270_783_744 + 127_093_760
+# Pipe utilisation of the same sweep kernel (ncu --set full of bve_rel_sweep_kernel<128,8,256,2>
+# on this workload at icos nest 7, one launch): the pipe-level counterpart of the flop-contract
+# fraction; recorded constants, not figures of this run
+SWEEP_PIPES_ICOS7 = {"fma_pipe_active": 0.6608, "xu_pipe_active": 0.6144, "issue_active": 0.4797}
+# FP32 CUDA-core nominal peak: 152 SMs x 128 lanes x 2 flops per FMA, per MHz of SM clock
+FP32_NOMINAL_TFLOPS_PER_MHZ = 152 * 128 * 2 / 1e6
+# FP64: 2 DFMA per clock per SM (4 flops), per MHz
+FP64_NOMINAL_TFLOPS_PER_MHZ = 152 * 4 / 1e6
+# FP64 parity-mode rate at the headline size: the FP64 sweep on a block of targets that gives
+# every SM two 128-thread CTAs (the per-target cost is the same for every target)
+FP64_BLOCK_TARGETS = 152 * 2 * 128
 
 
 def parse_args():
@@ -67,6 +85,9 @@ def parse_args():
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline sample budget")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-fp64", action="store_true", help="skip the FP64 parity-mode rate at the headline size")
+    p.add_argument("--no-ensemble", action="store_true", help="skip the 64-instance ensemble object")
+    p.add_argument("--ensemble-steps", type=int, default=10, help="RK4 steps of the ensemble object")
     p.add_argument("--workload", choices=["rk4", "ensemble", "stream", "configs", "sum", "remesh"], default="rk4",
                    help="rk4: the headline single-instance step; ensemble: the 64-instance batch")
     p.add_argument("--instances", type=int, default=64)
@@ -281,18 +302,41 @@ def run_ours(args):
     sum_ms = (k_ms1 - k_ms0) / sums
     achieved_tflops = FLOPS_PER_INTERACTION * per_sum / (sum_ms * 1e-3) / 1e12
 
-    # ---------------- accuracy of the FP32C velocity at the final state vs the FP64 sum
+    # ---------------- accuracy of the FP32C velocity at the final state against the oracle
+    # (the reference loop restated in C, FP64) on a seeded block of targets
+    from oracle import oracle as orc
     st = solver.get_state()
     rng = np.random.default_rng(1)
     m = min(args.accuracy_targets, n)
     ib = int(rng.integers(0, n - m + 1)) + 1
-    u64 = lg.bve_sphere_velocity(st["x"], st["y"], st["z"], st["rel_vort"], c["area"], c["active"], c["radius"],
-                                 i_begin=ib, i_end=ib + m - 1, mode="fp64")
-    ref = np.stack([a[ib - 1:ib - 1 + m] for a in u64])
+    ref = np.stack(orc.bve_velocity(st["x"], st["y"], st["z"], st["rel_vort"], c["area"], c["active"], c["radius"],
+                                    ib=ib - 1, ie=ib - 1 + m))
     got = np.stack([st[k][ib - 1:ib - 1 + m] for k in ("u", "v", "w")])
     rel_linf = float(np.abs(got - ref).max() / np.abs(ref).max())
     rel_l2 = float(np.sqrt(np.sum((got - ref) ** 2) / np.sum(ref ** 2)))
     diag1 = solver.diagnostics()
+
+    # ---------------- the plain FP64 GPU kernel (parity mode) at the same size and state
+    fp64 = None
+    if not args.no_fp64:
+        m64 = min(FP64_BLOCK_TARGETS, n)
+        b64 = n // 2 - m64 // 2 + 1
+        fa = (st["x"], st["y"], st["z"], st["rel_vort"], c["area"], c["active"], c["radius"])
+        lg.bve_sphere_velocity(*fa, i_begin=b64, i_end=b64 + 127, mode="fp64")  # warm-up
+        t0 = time.perf_counter()
+        lg.bve_sphere_velocity(*fa, i_begin=b64, i_end=b64 + m64 - 1, mode="fp64")
+        t64 = time.perf_counter() - t0
+        inter64 = m64 * ns - int(c["active"][b64 - 1:b64 - 1 + m64].sum())
+        r64 = inter64 / t64 / 1e9
+        mhz = clocks.get("sm_mhz") or 2070.0
+        fp64 = {"value": r64, "unit": UNIT, "fp32c_over_fp64": value / r64,
+                "contract_tflops": FLOPS_PER_INTERACTION * r64 / 1e3,
+                "frac_of_nominal_fp64_peak": FLOPS_PER_INTERACTION * r64 / 1e3 / (FP64_NOMINAL_TFLOPS_PER_MHZ * mhz),
+                "kernel": "seq_fp64_kernel<BveF64<0>> (one target per thread, sources in ascending order, "
+                          "bit-identical to the oracle)",
+                "sample": f"targets {b64}..{b64 + m64 - 1} against all {ns} sources ({inter64:.3e} interactions), "
+                          "one host C-ABI call, wall clock, copies included",
+                "seconds": t64}
 
     # ---------------- end to end through the C ABI with host buffers
     e2e = None
@@ -322,6 +366,12 @@ def run_ours(args):
                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                "path": "lpm_bve_set_state + lpm_bve_timestep + lpm_bve_get_state, pinned host buffers"}
 
+    ens = None
+    if not args.no_ensemble and world == 1:
+        import workloads as wl
+        ens = measure_ensemble(torch, lg, wl, args.instances, args.ensemble_steps, 3, args.dt)
+        ens.pop("errs", None)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline and world == 1:
         rate, cores, desc, _ = cpu_sample_rate(c, n, ns, args.cpu_seconds)
@@ -342,12 +392,23 @@ def run_ours(args):
             "gpu_launches": k_n1 - k_n0,
             "roofline": {"bound": "fp32", "achieved": achieved_tflops, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved_tflops / peak,
+                         "frac_of_nominal": achieved_tflops / (FP32_NOMINAL_TFLOPS_PER_MHZ * (clocks.get("sm_mhz")
+                                                                                            or 2070.0)),
                          "traffic": SWEEP_TRAFFIC_ICOS8 if args.nest == 8 else None,
-                         "traffic_unit": "bytes per launch (ncu, profiles/bve_rel_sweep_icos8_dram.md)",
+                         "traffic_unit": "bytes per sweep launch: ncu dram__bytes_read.sum + dram__bytes_write.sum "
+                                         "of one full-size launch (a recorded capture, not measured in this run)",
+                         "pipes": dict(SWEEP_PIPES_ICOS7, source="ncu --set full of the same sweep kernel on this "
+                                       "workload at icos nest 7 (sm__pipe_fma_cycles_active, "
+                                       "sm__pipe_xu_cycles_active, smsp__issue_active; recorded, not this run)"),
                          "kernel": "bve_rel_sweep_kernel (+ its prep and finish kernels) per velocity sum",
                          "ms_per_launch": sum_ms, "flops_per_interaction": FLOPS_PER_INTERACTION,
-                         "peak_source": "measured in-process FFMA loop (lpm_measure_fp32_peak)"},
-            "accuracy": {"velocity_rel_linf_vs_fp64": rel_linf, "velocity_rel_l2_vs_fp64": rel_l2,
+                         "peak_source": "measured in-process FFMA loop (lpm_measure_fp32_peak); "
+                                        "frac_of_nominal: 152 SMs x 128 lanes x 2 flops x the median SM clock"},
+            "fp64_gpu": fp64,
+            "ensemble": ens,
+            "accuracy": {"velocity_rel_linf_vs_fp64_oracle": rel_linf, "velocity_rel_l2_vs_fp64_oracle": rel_l2,
+                         "reference": "the oracle (the reference BVESphereVelocity loop restated in C, FP64) at "
+                                      "the final state",
                          "targets": f"{ib}..{ib + m - 1}",
                          "circulation_drift": diag1["circulation"] - diag0["circulation"],
                          "ke_rel_drift": (diag1["kinetic_energy"] - diag0["kinetic_energy"]) / diag0["kinetic_energy"],
@@ -363,39 +424,32 @@ def run_ours(args):
 
 
 # ------------------------------------------------------------------ ensemble
-def run_ensemble(args):
-    """64 independent sphere-BVE instances at seeded random refinement levels 3-6 (Gaussian
-    vortices with random strength, width and centre, mean removed, Omega = 2 pi), FP32C,
-    advanced `steps` RK4 steps (dt = 0.01, projected stages) as one batch -- one persistent
-    launch per stage over a flattened work queue, one CUDA graph per step -- and, for
-    comparison, as the same instances on separate solvers, one after another."""
-    import torch
-    import lpm_gpu as lg
-    import workloads as wl
-
-    world, rank, local = dist_env()
-    torch.cuda.set_device(local)
-    inst = wl.config_ensemble(n_instances=args.instances, seed=0)
-    steps = args.steps if args.steps != 5 else 50
+def measure_ensemble(torch, lg, wl, n_instances, steps, warmup, dt, inst=None, check=8):
+    """Config 5: `n_instances` independent sphere-BVE instances at seeded random icosahedral
+    nests 3-6 (Gaussian vortices with random strength, width and centre, mean removed,
+    Omega = 2 pi), FP32C, advanced `steps` RK4 steps (dt, projected stages) as one batch -- one
+    persistent launch per stage over a flattened work queue, one CUDA graph per step -- and the
+    same instances on separate solvers, one after another.  Both are timed by the host wall
+    clock around the step loop, the device synchronised before and after (each step ends with
+    a status check).  Returns a dict (Ginteractions/s, the ratio, accuracy against FP64)."""
+    if inst is None:
+        inst = wl.config_ensemble(n_instances=n_instances, seed=0)
     inter_eval = sum(int(d["x"].size) * int(d["active"].sum()) - int(d["active"].sum()) for d in inst)
     ens = lg.Ensemble(inst, mode="fp32c")
-    ens.timestep(args.dt, max(args.warmup, 3), renormalize=True)
-    sampler = ClockSampler(gpu_id_for(torch, local))
-    sampler.start()
+    ens.timestep(dt, max(warmup, 3), renormalize=True)
     torch.cuda.synchronize()
     k0 = ens.kernel_timing()
     t0 = time.perf_counter()
-    ens.timestep(args.dt, steps, renormalize=True)
+    ens.timestep(dt, steps, renormalize=True)
     torch.cuda.synchronize()
     t_batch = time.perf_counter() - t0
     k1 = ens.kernel_timing()
-    clocks = sampler.stop()
-    # per-instance velocity error of the batched FP32C sums against FP64 (8 instances,
-    # a block of up to 4096 targets each)
+    # per-instance velocity error of the batched FP32C sums against FP64 (up to `check`
+    # instances, a block of up to 4096 targets each)
     st = ens.get_state()
     offs = ens.offsets
     errs = []
-    for k in range(0, len(inst), max(1, len(inst) // 8)):
+    for k in range(0, len(inst), max(1, len(inst) // max(check, 1))):
         a, b = int(offs[k]), int(offs[k + 1])
         d = inst[k]
         m = min(4096, b - a)
@@ -406,39 +460,70 @@ def run_ensemble(args):
         r = np.stack([q[:m] for q in ref])
         errs.append(float(np.abs(got - r).max() / np.abs(r).max()))
     ens.close()
-    # the same instances, solver by solver (each replays its own graph back to back)
     solvers = [lg.BVESolver(d["x"], d["y"], d["z"], d["rel_vort"], d["area"], d["active"], d["radius"],
                             d["rotation_rate"], mode="fp32c") for d in inst]
     for s_ in solvers:
         s_.set_timing(False)
-        s_.timestep(args.dt, max(args.warmup, 3), renormalize=True)
+        s_.timestep(dt, max(warmup, 3), renormalize=True)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for s_ in solvers:
-        s_.timestep(args.dt, steps, renormalize=True)
+        s_.timestep(dt, steps, renormalize=True)
     torch.cuda.synchronize()
     t_seq = time.perf_counter() - t0
     for s_ in solvers:
         s_.close()
     total = 4 * steps * inter_eval
-    value = total / t_batch / 1e9
-    nests = collections_counter([d["nest"] for d in inst])
+    return {"value": total / t_batch / 1e9, "unit": UNIT, "steps": steps, "instances": len(inst),
+            "nests": collections_counter([d["nest"] for d in inst]), "interactions_per_eval": inter_eval,
+            "ms_per_step": 1e3 * t_batch / steps,
+            "sequential": {"value": total / t_seq / 1e9, "unit": UNIT, "ms_per_step": 1e3 * t_seq / steps,
+                           "how": "one BVESolver per instance, each replaying its step graph back to back"},
+            "speedup_vs_sequential": t_seq / t_batch,
+            "sum_kernel_ms_per_step": (k1[0] - k0[0]) / steps,
+            "gpu_launches": k1[1] - k0[1],
+            "velocity_rel_linf_vs_fp64_max": max(errs), "instances_checked": len(errs),
+            "timing": "host wall clock around the step loop, device synchronised before and after", "errs": errs}
+
+
+def run_ensemble(args):
+    """The 64-instance ensemble (config 5) as its own line, with the same measurement for each
+    refinement level of the mix on its own (the per-size-class rates)."""
+    import torch
+    import lpm_gpu as lg
+    import workloads as wl
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    steps = args.steps if args.steps != 5 else 50
+    inst = wl.config_ensemble(n_instances=args.instances, seed=0)
+    sampler = ClockSampler(gpu_id_for(torch, local))
+    sampler.start()
+    r = measure_ensemble(torch, lg, wl, args.instances, steps, args.warmup, args.dt, inst=inst)
+    clocks = sampler.stop()
+    classes = {}
+    for nest in sorted({d["nest"] for d in inst}):
+        sub = [d for d in inst if d["nest"] == nest]
+        q = measure_ensemble(torch, lg, wl, len(sub), max(2, steps // 5), args.warmup, args.dt, inst=sub, check=2)
+        classes[str(nest)] = {"instances": len(sub), "batched": q["value"], "sequential": q["sequential"]["value"],
+                              "speedup_vs_sequential": q["speedup_vs_sequential"],
+                              "interactions_per_eval": q["interactions_per_eval"], "steps": q["steps"]}
     line = {
-        "metric": "BVE ensemble Ginteractions/s (64 uneven instances, batched persistent launch)", "value": value,
+        "metric": "BVE ensemble Ginteractions/s (64 uneven instances, batched persistent launch)", "value": r["value"],
         "unit": UNIT, "n_gpus": 1, "steps": steps, "warmup": max(args.warmup, 3),
-        "ms_per_step": 1e3 * t_batch / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"{len(inst)} sphere-BVE instances, icosahedral nests {nests}, Gaussian vortices "
+        "config": {"workload": f"{len(inst)} sphere-BVE instances, icosahedral nests {r['nests']}, Gaussian vortices "
                                "(shape U[2,8], strength U[2pi,6pi], random centre), dt 0.01, projected stages",
-                   "interactions_per_eval": inter_eval, "timing": "host wall clock around the step loop, "
-                   "device synchronised before and after (each step ends with a status check)"},
+                   "interactions_per_eval": r["interactions_per_eval"], "timing": r["timing"]},
         "clocks": clocks,
-        "sequential": {"value": total / t_seq / 1e9, "unit": UNIT, "ms_per_step": 1e3 * t_seq / steps,
-                       "how": "one BVESolver per instance, each replaying its step graph back to back"},
-        "speedup_vs_sequential": t_seq / t_batch,
-        "sum_kernel_ms_per_step": (k1[0] - k0[0]) / steps,
-        "gpu_launches": k1[1] - k0[1],
-        "accuracy": {"velocity_rel_linf_vs_fp64_max": max(errs), "instances_checked": len(errs)},
+        "sequential": r["sequential"],
+        "speedup_vs_sequential": r["speedup_vs_sequential"],
+        "sum_kernel_ms_per_step": r["sum_kernel_ms_per_step"],
+        "gpu_launches": r["gpu_launches"],
+        "accuracy": {"velocity_rel_linf_vs_fp64_max": r["velocity_rel_linf_vs_fp64_max"],
+                     "instances_checked": r["instances_checked"]},
+        "size_classes": classes,
     }
     print(json.dumps(line), flush=True)
     return 0
