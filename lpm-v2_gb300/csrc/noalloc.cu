@@ -9,9 +9,13 @@
 //    synchronisation that cudaMalloc/cudaFree may perform.
 // Such a caller owns every input and output array (device pointers) and calls this entry
 // point, which keeps its own scratch -- the source records and the FP64 partial sums -- in
-// one file-scope __device__ array, g_noalloc_scratch, reserved when the library is loaded:
-// kNoAllocScratchBytes (about 24 MiB) on every GPU that loads the library, held until the
-// process exits.  That fixes the largest problem it accepts: n <= LPM_NOALLOC_MAX_PARTICLES.
+// one file-scope __device__ array, g_noalloc_scratch, of kNoAllocScratchBytes (about
+// 24 MiB).  That fixes the largest problem it accepts: n <= LPM_NOALLOC_MAX_PARTICLES.
+// With CUDA's lazy module loading (the default since CUDA 12.2) the array is reserved when
+// this file's module is first loaded on a device -- by the first call of this entry point
+// there -- not when the library is loaded; from then on it is held until the context is
+// destroyed (normally at process exit).  A caller whose pool takes most of HBM should make
+// one call before its pool reserves the memory, or the first call can fail for lack of it.
 //
 // The sum is the FP32C one of lpm_bve_velocity (hi/lo positions, chord-form denominator,
 // per-tile TwoSum accumulation, FP64 reduction), run over every particle as a source with
@@ -19,14 +23,19 @@
 //
 // Rules of use:
 //  - Host code must not pass g_noalloc_scratch itself to a kernel: in host code that name is
-//    a host-side stand-in, not a device address.  The device address is looked up once per
-//    device with cudaGetSymbolAddress, with that device current, by the first call made on
-//    it; make that first call before any stream capture.
+//    a host-side stand-in, not a device address.  The device address is looked up with
+//    cudaGetSymbolAddress, with the device current, by the first call made in a CUDA context
+//    (and again if that context is replaced, e.g. after cudaDeviceReset); make that first
+//    call before any stream capture.
 //  - Every call on a device shares the one array, which keeps the previous call's contents;
 //    the call clears the status word it reads and overwrites every record and partial sum
 //    before reading it.  Calls that overlap on the GPU (from several host threads or on
 //    several streams) race on the array: serialise them.
+//  - On an error return (a bounded device wait that gave up) u, v and w are left as they
+//    were: the finish kernel writes nothing once the status word is set.
 //  - The call is synchronous with respect to `stream` (it waits for the result status).
+#include <cuda.h>
+
 #include <mutex>
 
 #include "bve_x2.cuh"
@@ -50,7 +59,14 @@ __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
 constexpr int kNaMaxDevices = 64;
 std::mutex g_na_mu;
-void* g_na_addr[kNaMaxDevices] = {};
+// The scratch address per device, with the id of the CUDA context it was looked up in: a
+// __device__ array lives in a module of one context, so a new context (cudaDeviceReset, or a
+// context the caller made current) holds it at another address.
+struct NaAddr {
+  unsigned long long ctx_id = 0;
+  void* ptr = nullptr;
+};
+NaAddr g_na_addr[kNaMaxDevices];
 
 // Source records of every particle: passive particles get zero strength.
 __global__ void noalloc_prep_kernel(int64_t n, int64_t npad, const double* x, const double* y, const double* z,
@@ -78,10 +94,11 @@ __global__ void noalloc_prep_kernel(int64_t n, int64_t npad, const double* x, co
 }
 
 __global__ void noalloc_finish_kernel(const double* partial, int64_t nsplit, int64_t nt, int64_t ib, const double* x,
-                                      const double* y, const double* z, double inv_a, double* u, double* v,
-                                      double* w) {
+                                      const double* y, const double* z, double inv_a, const int* status, double* u,
+                                      double* v, double* w) {
   const int64_t il = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (il >= nt) return;
+  if (*status != kDevOk) return;  // the sweep gave up: its partial sums are incomplete
   double d0 = 0.0, d1 = 0.0, d2 = 0.0;
   for (int64_t c = 0; c < nsplit; ++c) {
     d0 += partial[(c * 3 + 0) * nt + il];
@@ -95,20 +112,58 @@ __global__ void noalloc_finish_kernel(const double* partial, int64_t nsplit, int
   w[i] = d0 * py - d1 * px;
 }
 
-// Device address of g_noalloc_scratch on the current device (looked up once per device).
+// Driver entry points for the identity of the current context, through the runtime (no
+// link-time dependency on libcuda).
+using PfnCtxGetCurrent = CUresult (*)(CUcontext*);
+using PfnCtxGetId = CUresult (*)(CUcontext, unsigned long long*);
+
+int current_context_id(int device, unsigned long long* id) {
+  static PfnCtxGetCurrent get_current = nullptr;
+  static PfnCtxGetId get_id = nullptr;
+  if (!get_current || !get_id) {
+    void* f0 = nullptr;
+    void* f1 = nullptr;
+    cudaDriverEntryPointQueryResult q0 = cudaDriverEntryPointSymbolNotFound, q1 = cudaDriverEntryPointSymbolNotFound;
+    const cudaError_t e0 = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f0, 12000, cudaEnableDefault, &q0);
+    const cudaError_t e1 = cudaGetDriverEntryPointByVersion("cuCtxGetId", &f1, 12000, cudaEnableDefault, &q1);
+    if (e0 != cudaSuccess || e1 != cudaSuccess || q0 != cudaDriverEntryPointSuccess ||
+        q1 != cudaDriverEntryPointSuccess || !f0 || !f1) {
+      return set_error(LPM_ERR_CUDA, "cuCtxGetCurrent/cuCtxGetId are not available from the driver");
+    }
+    get_current = reinterpret_cast<PfnCtxGetCurrent>(f0);
+    get_id = reinterpret_cast<PfnCtxGetId>(f1);
+  }
+  CUcontext ctx = nullptr;
+  if (get_current(&ctx) != CUDA_SUCCESS) return set_error(LPM_ERR_CUDA, "cuCtxGetCurrent failed");
+  if (!ctx) {
+    // no context bound to this thread yet: cudaSetDevice makes the device's primary one current
+    LPM_CUDA_TRY(cudaSetDevice(device));
+    if (get_current(&ctx) != CUDA_SUCCESS || !ctx) return set_error(LPM_ERR_CUDA, "no current CUDA context");
+  }
+  if (get_id(ctx, id) != CUDA_SUCCESS) return set_error(LPM_ERR_CUDA, "cuCtxGetId failed");
+  return LPM_OK;
+}
+
+// Device address of g_noalloc_scratch in the current context of `device` (looked up once
+// per context; context ids are never reused within a process).
 int scratch_address(int device, void** addr) {
   if (device < 0 || device >= kNaMaxDevices) return set_error(LPM_ERR_ARG, "device %d out of range", device);
   std::lock_guard<std::mutex> lock(g_na_mu);
-  if (!g_na_addr[device]) {
+  unsigned long long id = 0;
+  LPM_TRY(current_context_id(device, &id));
+  NaAddr& slot = g_na_addr[device];
+  if (!slot.ptr || slot.ctx_id != id) {
     void* p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || !p) {
+      slot.ptr = nullptr;
       return set_error(LPM_ERR_CUDA, "cudaGetSymbolAddress(g_noalloc_scratch) failed on device %d: %s", device,
                        cudaGetErrorString(e));
     }
-    g_na_addr[device] = p;
+    slot.ptr = p;
+    slot.ctx_id = id;
   }
-  *addr = g_na_addr[device];
+  *addr = slot.ptr;
   return LPM_OK;
 }
 
@@ -166,7 +221,7 @@ extern "C" int lpm_bve_velocity_noalloc(int64_t n, const double* x, const double
   bve_sweep_x2_kernel<kNaThreads, kNaTpt, kNaTile, kNaMinB>
       <<<dim3(static_cast<unsigned>(tblocks), static_cast<unsigned>(nsplit)), kNaThreads, 0, stream>>>(a);
   noalloc_finish_kernel<<<static_cast<unsigned>(ceil_div(nt, 256)), 256, 0, stream>>>(partial, nsplit, nt, ib, x, y,
-                                                                                        z, inv_a, u, v, w);
+                                                                                        z, inv_a, status, u, v, w);
   LPM_CUDA_TRY(cudaGetLastError());
   int h_status = 0;
   LPM_CUDA_TRY(cudaMemcpyAsync(&h_status, status, sizeof(int), cudaMemcpyDeviceToHost, stream));
