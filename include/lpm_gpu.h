@@ -332,18 +332,46 @@ int lpm_ensemble_destroy(lpm_ensemble* ens);
  * pointer owned by the caller (same meaning as lpm_bve_velocity, 1-based i_begin..i_end,
  * outputs outside the block untouched); the call computes the LPM_MODE_FP32C sum and
  * allocates nothing -- no cudaMalloc, cudaFree or allocating library routine.  Its scratch
- * is one array the library reserves on every GPU that loads it (about 24 MiB, held until
- * the process exits), which limits n to LPM_NOALLOC_MAX_PARTICLES; larger n fails with
- * LPM_ERR_ARG.  The first call on a device looks up that array's device address, so make
- * it before any stream capture.  All calls on a device share the array: calls that overlap
- * on the GPU (several host threads or streams) race, so serialise them.  Work is enqueued
- * on `stream` (a cudaStream_t, NULL for the default stream) and the call returns after the
- * stream has finished it. */
+ * is one file-scope device array of about 24 MiB, which limits n to
+ * LPM_NOALLOC_MAX_PARTICLES; larger n fails with LPM_ERR_ARG.  Under CUDA's lazy module
+ * loading (the default) the array is reserved on a device by the first call made there, and
+ * held until the context is destroyed: a caller whose pool takes most of HBM should make one
+ * call before the pool does.  The first call in a CUDA context also looks up the array's
+ * device address, so make it before any stream capture.  All calls on a device share the
+ * array: calls that overlap on the GPU (several host threads or streams) race, so serialise
+ * them.  Work is enqueued on `stream` (a cudaStream_t, NULL for the default stream) and the
+ * call returns after the stream has finished it; on an error return u, v and w are left as
+ * they were. */
 #define LPM_NOALLOC_MAX_PARTICLES 262144
 int lpm_bve_velocity_noalloc(int64_t n, const double* x, const double* y, const double* z,
                              const double* zeta, const double* area, const int32_t* active,
                              double radius, int64_t i_begin, int64_t i_end, double* u,
                              double* v, double* w, void* stream);
+
+/* ------------------------------------------------------------------ workspace and test hooks */
+
+/* Frees the device workspace the host-buffer calls keep between calls (it grows to the
+ * largest sum seen and is otherwise held until the process exits).  Synchronous; the next
+ * host-buffer call allocates again.  No counterpart in the reference, which has no device
+ * memory; the analogue of releasing a cached allocator's free blocks. */
+int lpm_release_workspace(void);
+
+/* Test hooks (no counterpart in the reference; they exercise the error paths that the
+ * Fortran shim maps to LogMessage(..., ERROR_LOGGING_LEVEL, ...), src/Logger.f90:159).
+ *
+ * lpm_debug_fail_device_alloc(k): the k-th device allocation the library makes from now on
+ * (k >= 1) fails as if cudaMalloc had run out of memory, and the call that made it returns
+ * LPM_ERR_ALLOC; k = 0 disarms.  Every handle or workspace allocated before the failure is
+ * released or kept consistent, so the next call succeeds.
+ *
+ * lpm_debug_inject_wait_timeout(skip_tile, budget_ns): the next host-buffer sphere-BVE
+ * LPM_MODE_FP32C sum (lpm_bve_velocity or lpm_bve_set_velocity_from_vorticity) does not issue
+ * the copy of source tile `skip_tile` and bounds its waits by budget_ns (0 < budget_ns <= 1e9)
+ * instead of 1 s.  The waits for that tile run out, the call returns LPM_ERR_TIMEOUT with the
+ * caller's outputs untouched, and the context stays usable.  Nothing faults: no copy is in
+ * flight for the skipped tile.  One-shot. */
+int lpm_debug_fail_device_alloc(int64_t k);
+int lpm_debug_inject_wait_timeout(int64_t skip_tile, int64_t budget_ns);
 
 /* ------------------------------------------------------------------ calibration */
 

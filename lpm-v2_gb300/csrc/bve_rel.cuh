@@ -317,7 +317,7 @@ __global__ void __launch_bounds__(THREADS, MINB) bve_rel_sweep_kernel(SweepArgs<
   uint32_t g = 0;
   int64_t tile = tile0;
   const Rec* src = reinterpret_cast<const Rec*>(a.src);
-  staged_sweep<Rec, TILE>(src, tile0, ntl, stage[0], stage[1], bars, g, a.status, [&](const Rec* tl) {
+  staged_sweep<Rec, TILE>(src, tile0, ntl, stage[0], stage[1], bars, g, a.status, a.wait, [&](const Rec* tl) {
     float2 ax[NP], ay[NP], az[NP];
 #pragma unroll
     for (int p = 0; p < NP; ++p) ax[p] = ay[p] = az[p] = make_float2(0.f, 0.f);

@@ -7,7 +7,37 @@ namespace {
 thread_local std::string g_last_error;
 Context* g_ctx = nullptr;
 std::mutex g_ctx_mu;
+// test hooks (lpm_debug_*): the countdown to an injected allocation failure, and wait limits
+// armed for the next host-buffer sphere-BVE FP32C sweep
+std::mutex g_hook_mu;
+int64_t g_fail_alloc_in = 0;
+bool g_wait_armed = false;
+WaitCfg g_wait = default_wait();
 }  // namespace
+
+int device_alloc(void** p, size_t bytes) {
+  *p = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_hook_mu);
+    if (g_fail_alloc_in > 0 && --g_fail_alloc_in == 0) {
+      return set_error(LPM_ERR_ALLOC, "device allocation of %zu bytes failed: injected failure "
+                       "(lpm_debug_fail_device_alloc)", bytes);
+    }
+  }
+  const cudaError_t e = cudaMalloc(p, bytes > 0 ? bytes : 16);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    return set_error(LPM_ERR_ALLOC, "device allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+  }
+  return LPM_OK;
+}
+
+WaitCfg take_injected_wait() {
+  std::lock_guard<std::mutex> lock(g_hook_mu);
+  if (!g_wait_armed) return default_wait();
+  g_wait_armed = false;
+  return g_wait;
+}
 
 int set_error(int code, const char* fmt, ...) {
   char buf[1024];
@@ -62,12 +92,7 @@ int workspace(Context* ctx, int slot, size_t bytes, void** p) {
     b.ptr = nullptr;
     b.bytes = 0;
     const size_t want = align_up(bytes + bytes / 4, 1 << 20);
-    cudaError_t e = cudaMalloc(&b.ptr, want);
-    if (e != cudaSuccess) {
-      b.ptr = nullptr;
-      return set_error(LPM_ERR_ALLOC, "device allocation of %zu bytes failed: %s", want,
-                       cudaGetErrorString(e));
-    }
+    LPM_TRY(device_alloc(&b.ptr, want));
     b.bytes = want;
   }
   *p = b.ptr;
@@ -96,5 +121,39 @@ int sync_and_check(Context* ctx, const char* what) {
 }  // namespace lpm
 
 extern "C" const char* lpm_last_error_string(void) { return lpm::g_last_error.c_str(); }
+
+extern "C" int lpm_release_workspace(void) {
+  using namespace lpm;
+  Context* ctx = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_ctx_mu);
+    ctx = g_ctx;
+  }
+  if (!ctx) return LPM_OK;  // nothing allocated yet
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  LPM_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  for (DevBuf& b : ctx->bufs) {
+    if (b.ptr) LPM_CUDA_TRY(cudaFree(b.ptr));
+    b.ptr = nullptr;
+    b.bytes = 0;
+  }
+  return LPM_OK;
+}
+
+extern "C" int lpm_debug_fail_device_alloc(int64_t k) {
+  if (k < 0) return lpm::set_error(LPM_ERR_ARG, "k must be >= 0 (got %lld)", static_cast<long long>(k));
+  std::lock_guard<std::mutex> lock(lpm::g_hook_mu);
+  lpm::g_fail_alloc_in = k;
+  return LPM_OK;
+}
+
+extern "C" int lpm_debug_inject_wait_timeout(int64_t skip_tile, int64_t budget_ns) {
+  if (skip_tile < 0 || budget_ns <= 0 || budget_ns > 1000000000ll)
+    return lpm::set_error(LPM_ERR_ARG, "need skip_tile >= 0 and 0 < budget_ns <= 1e9");
+  std::lock_guard<std::mutex> lock(lpm::g_hook_mu);
+  lpm::g_wait = lpm::WaitCfg{static_cast<uint64_t>(budget_ns), skip_tile};
+  lpm::g_wait_armed = true;
+  return LPM_OK;
+}
 
 extern "C" const char* lpm_version(void) { return "lpm_gpu 0.1 (sm_103a)"; }

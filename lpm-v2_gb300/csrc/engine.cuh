@@ -1,12 +1,20 @@
-// engine.cuh -- the tile pipeline shared by every FP32C sweep.
+// engine.cuh -- the tile pipelines shared by the direct sums.
 //
 // Layout: sources are compacted (active particles only) into an array of fixed-size
 // records, padded with inert records to a multiple of the tile size.  A CTA owns a block of
 // targets (held in registers) and a contiguous range of source tiles (one split-K chunk).
-// Tiles are staged into shared memory by 1-D TMA bulk copies (cp.async.bulk) on a two-stage
-// mbarrier pipeline (staged_sweep); every thread then sweeps the tile with broadcast
-// shared-memory reads.  Each wait on a tile is bounded (~1 s) and a block-wide
-// vote makes all threads leave together if one gives up, so a lost copy cannot hang the GPU.
+// Tiles are staged into shared memory by 1-D TMA bulk copies (cp.async.bulk), and every
+// thread then sweeps a tile with broadcast shared-memory reads.  Two pipelines:
+//  - staged_sweep: two stages, block-synchronous (every warp finishes a tile before its stage
+//    is refilled; two block barriers per tile);
+//  - warp_sweep: S stages, warp-decoupled.  Each stage has a "full" mbarrier (the copy's
+//    transaction count) and an "empty" one (one arrival per warp when it is done with the
+//    tile).  Thread 0 refills a stage as soon as every warp has released it, so warps that
+//    skip a tile's work run ahead by up to S - 1 tiles instead of waiting at a barrier.
+// Every wait is bounded (WaitCfg::ns, 1 s by default); a thread that gives up records
+// kDevTimeout in the device status word, its warp (or block) leaves the sweep, and copies
+// still in flight are waited for (bounded again) before the CTA moves on, so a lost copy
+// cannot hang the GPU.
 #pragma once
 
 #include "lpm_common.cuh"
@@ -31,12 +39,14 @@ __device__ __forceinline__ void pipe_init(uint64_t* bars) {
 template <class Rec, int TILE, class Body>
 __device__ __forceinline__ bool staged_sweep(const Rec* __restrict__ src, int64_t tile0,
                                              int64_t ntl, Rec* stage0, Rec* stage1,
-                                             uint64_t* bars, uint32_t& g, int* status, Body&& body) {
+                                             uint64_t* bars, uint32_t& g, int* status, const WaitCfg& w,
+                                             Body&& body) {
   constexpr uint32_t kBytes = TILE * sizeof(Rec);
   static_assert(kBytes % 16 == 0, "tile bytes must be a multiple of 16");
   if (threadIdx.x == 0) {
     for (int64_t k = 0; k < ntl && k < 2; ++k) {
       const uint32_t gk = g + static_cast<uint32_t>(k);
+      if (tile0 + k == w.skip_tile) continue;
       mbar_arrive_expect_tx(&bars[gk & 1u], kBytes);
       tma_load_1d((gk & 1u) ? stage1 : stage0, src + (tile0 + k) * TILE, kBytes, &bars[gk & 1u]);
     }
@@ -47,14 +57,14 @@ __device__ __forceinline__ bool staged_sweep(const Rec* __restrict__ src, int64_
     const uint32_t gk = g + static_cast<uint32_t>(k);
     const int s = static_cast<int>(gk & 1u);
     const uint32_t phase = (gk >> 1) & 1u;
-    const bool mine = mbar_wait_bounded(&bars[s], phase, status);
+    const bool mine = mbar_wait_bounded(&bars[s], phase, status, w.ns);
     if (!__syncthreads_and(mine)) {
       ok = false;
       break;
     }
     body(s ? stage1 : stage0);
     __syncthreads();  // every thread is done with stage s
-    if (threadIdx.x == 0 && k + 2 < ntl) {
+    if (threadIdx.x == 0 && k + 2 < ntl && tile0 + k + 2 != w.skip_tile) {
       mbar_arrive_expect_tx(&bars[s], kBytes);
       tma_load_1d(s ? stage1 : stage0, src + (tile0 + k + 2) * TILE, kBytes, &bars[s]);
     }
@@ -62,12 +72,110 @@ __device__ __forceinline__ bool staged_sweep(const Rec* __restrict__ src, int64_
   if (!ok && threadIdx.x == 0) {
     // let copies that are still in flight land before the CTA moves on (bounded again)
     for (int64_t kk = k; kk < ntl && kk < k + 2; ++kk) {
+      if (tile0 + kk == w.skip_tile) continue;  // never issued
       const uint32_t gk = g + static_cast<uint32_t>(kk);
-      mbar_wait_bounded(&bars[gk & 1u], (gk >> 1) & 1u, status);
+      mbar_wait_bounded(&bars[gk & 1u], (gk >> 1) & 1u, status, w.ns);
     }
   }
   g += static_cast<uint32_t>(ntl);
   return ok;
+}
+
+template <class Rec, int TILE, class Body>
+__device__ __forceinline__ bool staged_sweep(const Rec* __restrict__ src, int64_t tile0,
+                                             int64_t ntl, Rec* stage0, Rec* stage1,
+                                             uint64_t* bars, uint32_t& g, int* status, Body&& body) {
+  return staged_sweep<Rec, TILE>(src, tile0, ntl, stage0, stage1, bars, g, status, default_wait(),
+                                 static_cast<Body&&>(body));
+}
+
+// Shared memory of an S-stage warp-decoupled pipeline.
+template <class Rec, int TILE, int S>
+struct __align__(128) TilePipe {
+  Rec stage[S][TILE];
+  uint64_t full[S];   // completes when tile data has landed (1 arrival + the copy's bytes)
+  uint64_t empty[S];  // completes when every warp is done with the stage (one arrival per warp)
+};
+
+template <class Rec, int TILE, int S>
+__device__ __forceinline__ void tile_pipe_init(TilePipe<Rec, TILE, S>& pp) {
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < S; ++s) {
+      mbar_init(&pp.full[s], 1);
+      mbar_init(&pp.empty[s], blockDim.x / 32);
+    }
+    fence_mbar_init();
+  }
+  __syncthreads();
+}
+
+// S-stage warp-decoupled sweep over tiles [tile0, tile0 + ntl) of `src`: body(const Rec*)
+// runs once per tile in every warp, each warp at its own pace.  `g` counts the tiles this CTA
+// has pushed through the pipeline (identical in every thread): tile number q uses stage
+// q % S, whose full barrier completes phase (q / S) & 1 for it and whose empty barrier
+// completes phase (q / S) & 1 when every warp has released it.  Thread 0 (a consumer too)
+// issues the copies: before each of its tiles it refills every stage already released,
+// keeping up to S tiles in flight, and it blocks (bounded) on a release only when the tile
+// it needs next has not been issued.  Returns false in every thread when any wait gave up.
+template <class Rec, int TILE, int S, class Body>
+__device__ __forceinline__ bool warp_sweep(const Rec* __restrict__ src, int64_t tile0, int64_t ntl,
+                                           TilePipe<Rec, TILE, S>& pp, uint32_t& g, int* status,
+                                           const WaitCfg& w, Body&& body) {
+  constexpr uint32_t kBytes = TILE * sizeof(Rec);
+  static_assert(kBytes % 16 == 0, "tile bytes must be a multiple of 16");
+  static_assert(S >= 2, "at least two stages");
+  const bool producer = threadIdx.x == 0;
+  int64_t next = 0;  // next tile to issue (thread 0)
+  bool ok = true;    // thread 0: no wait for a release gave up
+  // Issues tile kk if its stage is free: waits (bounded) for the release when `block`,
+  // otherwise probes once.  Returns 1 when issued, 0 when not yet free, -1 on a timeout.
+  auto issue = [&](int64_t kk, bool block) -> int {
+    const uint32_t q = g + static_cast<uint32_t>(kk);
+    const uint32_t s = q % S;
+    if (q >= static_cast<uint32_t>(S)) {
+      const uint32_t ph = ((q - S) / S) & 1u;
+      if (block) {
+        if (!mbar_wait_bounded(&pp.empty[s], ph, status, w.ns)) return -1;
+      } else if (!mbar_try_wait(&pp.empty[s], ph)) {
+        return 0;
+      }
+    }
+    if (tile0 + kk != w.skip_tile) {
+      mbar_arrive_expect_tx(&pp.full[s], kBytes);
+      tma_load_1d(pp.stage[s], src + (tile0 + kk) * TILE, kBytes, &pp.full[s]);
+    }
+    return 1;
+  };
+  int64_t k = 0;
+  for (; k < ntl; ++k) {
+    if (producer && ok) {
+      while (next < ntl && next < k + S) {
+        const int r = issue(next, next <= k);
+        if (r < 0) ok = false;
+        if (r <= 0) break;
+        ++next;
+      }
+    }
+    const uint32_t q = g + static_cast<uint32_t>(k);
+    const uint32_t s = q % S;
+    const bool mine = ok && mbar_wait_bounded(&pp.full[s], (q / S) & 1u, status, w.ns);
+    if (!__all_sync(0xffffffffu, mine)) break;
+    body(pp.stage[s]);
+    __syncwarp();
+    if ((threadIdx.x & 31u) == 0u) mbar_arrive(&pp.empty[s]);
+  }
+  const bool all = __syncthreads_and(k == ntl);
+  if (!all && producer) {
+    // copies issued for tiles this warp did not wait for must land before the CTA moves on
+    // (bounded again); tiles below k completed, every stage before them too
+    for (int64_t kk = k; kk < next; ++kk) {
+      if (tile0 + kk == w.skip_tile) continue;  // never issued
+      const uint32_t q = g + static_cast<uint32_t>(kk);
+      mbar_wait_bounded(&pp.full[q % S], (q / S) & 1u, status, w.ns);
+    }
+  }
+  g += static_cast<uint32_t>(ntl);
+  return all;
 }
 
 // Arguments of a compensated FP32 sweep (targets, records, split-K partials).
@@ -81,6 +189,7 @@ struct SweepArgs {
   int64_t nt;         // number of targets
   double* partial;    // [gridDim.y][Op::NC][nt]
   int* status;
+  WaitCfg wait = default_wait();
 };
 
 }  // namespace lpm

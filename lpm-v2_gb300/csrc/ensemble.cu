@@ -10,12 +10,17 @@
 // records -- the layout and arithmetic of the single-instance sweep (bve_rel.cuh).
 //
 // Work decomposition: each velocity evaluation of all instances is a flattened list of
-// work items (instance, block of 512 targets, range of source tiles).  Source ranges are cut
+// work items (instance, block of targets, range of source tiles).  Source ranges are cut
 // so that items cost about the same, and the items are sorted by decreasing cost.  One
 // persistent launch (a few CTAs per SM) pulls items from an atomic queue; each item writes
 // its own FP64 partial slot, and a finish kernel reduces the slots of a target block in a
 // fixed order, so the result does not depend on which CTA ran which item.  One RK4 step of
 // all instances (4 stage kernels, 4 x (sort, prep, sweep, finish)) is one CUDA graph.
+//
+// Autotuner: the persistent kernel comes in the CTA shapes the single-instance tuner picks
+// from (128 threads x 4 targets at 4 CTAs per SM: 512 targets per item; 128 x 8 at 2 per SM:
+// 1024).  At creation each shape's work queue is built and one velocity evaluation of all
+// instances is timed; the faster shape is kept for the ensemble's life.
 //
 // FP64 mode (parity) runs the bit-exact sequential sweep per instance instead.
 #include <algorithm>
@@ -32,19 +37,32 @@
 namespace lpm {
 namespace {
 
-constexpr int kThreads = 128, kTpt = 4, kTile = 256, kMinB = 4;
-constexpr int kTB = kThreads * kTpt;  // targets per block (work item)
+constexpr int kTile = 256;
+// CTA shapes of the persistent sweep: threads, targets per thread, CTAs per SM
+struct EnsShape {
+  int threads, tpt, minb;
+};
+constexpr EnsShape kEnsShapes[] = {{128, 4, 4}, {128, 8, 2}};
+constexpr int kEnsShapeCount = sizeof(kEnsShapes) / sizeof(kEnsShapes[0]);
 constexpr double kPi = 3.1415926535897932384626433832795027975;
 constexpr int kStage = 256;
 
 struct Item {
   int inst;
-  int nt;         // targets in this item (<= kTB)
+  int nt;         // targets in this item (<= the shape's targets per item)
   long long t0;   // first target (global particle index)
   long long tile0;  // first source tile (global tile index)
   int ntiles;
   int pad;
   long long slot;  // partial slot (item id in block order)
+};
+
+// The flattened work queue of one sweep shape, on the host.
+struct Queue {
+  std::vector<Item> items;
+  std::vector<int> order;  // items by decreasing cost
+  std::vector<int32_t> boff, bfirst, bcnt;
+  int grid = 0;
 };
 
 struct EnsArgs {
@@ -56,12 +74,14 @@ struct EnsArgs {
   const BveRel::Origin* org;
   const double *x, *y, *z;
   const double* inv_a;  // per instance
-  double* partial;      // [slot][3][kTB]
+  double* partial;      // [slot][3][targets per item]
   int* status;
 };
 
-__global__ void __launch_bounds__(kThreads, kMinB) ensemble_sweep_kernel(EnsArgs a) {
-  constexpr int NP = kTpt / 2;
+template <int THREADS, int TPT, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB) ensemble_sweep_kernel(EnsArgs a) {
+  constexpr int NP = TPT / 2;
+  constexpr int TB = THREADS * TPT;  // targets per item
   constexpr int GPT = kTile / BveRel::kGroup;
   using Rec = BveRel::Rec;
   __shared__ __align__(128) Rec stage[2][kTile];
@@ -79,7 +99,7 @@ __global__ void __launch_bounds__(kThreads, kMinB) ensemble_sweep_kernel(EnsArgs
     const BveF32::Params prm{a.x, a.y, a.z, a.inv_a[it.inst]};
     BveX2::Pair pr[NP];
     float2 hx[NP], hy[NP], hz[NP], lx[NP], ly[NP], lz[NP];
-    bve_load_pairs<NP>(prm, it.t0, it.nt, kThreads, pr);
+    bve_load_pairs<NP>(prm, it.t0, it.nt, THREADS, pr);
 #pragma unroll
     for (int p = 0; p < NP; ++p) hx[p] = hy[p] = hz[p] = lx[p] = ly[p] = lz[p] = make_float2(0.f, 0.f);
     int64_t tile = it.tile0;
@@ -93,16 +113,16 @@ __global__ void __launch_bounds__(kThreads, kMinB) ensemble_sweep_kernel(EnsArgs
       bve_merge_pairs<NP>(ax, ay, az, hx, hy, hz, lx, ly, lz);
     });
     if (!ok) break;
-    double* slot = a.partial + it.slot * 3 * kTB;
+    double* slot = a.partial + it.slot * 3 * TB;
 #pragma unroll
     for (int p = 0; p < NP; ++p) {
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
-        const int l = (2 * p + h) * kThreads + threadIdx.x;
+        const int l = (2 * p + h) * THREADS + threadIdx.x;
         if (l < it.nt) {
-          slot[0 * kTB + l] = static_cast<double>(h ? hx[p].y : hx[p].x) + static_cast<double>(h ? lx[p].y : lx[p].x);
-          slot[1 * kTB + l] = static_cast<double>(h ? hy[p].y : hy[p].x) + static_cast<double>(h ? ly[p].y : ly[p].x);
-          slot[2 * kTB + l] = static_cast<double>(h ? hz[p].y : hz[p].x) + static_cast<double>(h ? lz[p].y : lz[p].x);
+          slot[0 * TB + l] = static_cast<double>(h ? hx[p].y : hx[p].x) + static_cast<double>(h ? lx[p].y : lx[p].x);
+          slot[1 * TB + l] = static_cast<double>(h ? hy[p].y : hy[p].x) + static_cast<double>(h ? ly[p].y : ly[p].x);
+          slot[2 * TB + l] = static_cast<double>(h ? hz[p].y : hz[p].x) + static_cast<double>(h ? lz[p].y : lz[p].x);
         }
       }
     }
@@ -128,8 +148,9 @@ __global__ void __launch_bounds__(kTile) ensemble_prep_kernel(const int32_t* til
                            org + t * (kTile / BveRel::kGroup));
 }
 
-// Per target: fixed-order FP64 sum of its block's item slots, then u = D x p.
-__global__ void ensemble_finish_kernel(int64_t n, const int32_t* pinst, const int64_t* off,
+// Per target: fixed-order FP64 sum of its block's item slots (tb targets per block), then
+// u = D x p.
+__global__ void ensemble_finish_kernel(int64_t n, int tb, const int32_t* pinst, const int64_t* off,
                                        const int32_t* blk_off, const int32_t* blk_first, const int32_t* blk_cnt,
                                        const double* partial, const double* x, const double* y, const double* z,
                                        const double* inv_a, double* u, double* v, double* w) {
@@ -137,14 +158,14 @@ __global__ void ensemble_finish_kernel(int64_t n, const int32_t* pinst, const in
   if (i >= n) return;
   const int k = pinst[i];
   const int64_t local = i - off[k];
-  const int b = blk_off[k] + static_cast<int>(local / kTB);
-  const int l = static_cast<int>(local % kTB);
+  const int b = blk_off[k] + static_cast<int>(local / tb);
+  const int l = static_cast<int>(local % tb);
   double d0 = 0.0, d1 = 0.0, d2 = 0.0;
   for (int c = 0; c < blk_cnt[b]; ++c) {
-    const double* slot = partial + static_cast<int64_t>(blk_first[b] + c) * 3 * kTB;
+    const double* slot = partial + static_cast<int64_t>(blk_first[b] + c) * 3 * tb;
     d0 += slot[l];
-    d1 += slot[kTB + l];
-    d2 += slot[2 * kTB + l];
+    d1 += slot[tb + l];
+    d2 += slot[2 * tb + l];
   }
   const double ia = inv_a[k];
   const double px = x[i] * ia, py = y[i] * ia, pz = z[i] * ia;
@@ -249,6 +270,9 @@ struct lpm_ensemble {
   Item* items = nullptr;
   int* queue = nullptr;
   int n_items = 0;
+  int shape = 0;                     // kEnsShapes index of the persistent sweep
+  std::vector<Queue> queues;         // host copies of every shape's work queue
+  std::vector<float> tuned_ms;       // the chosen shape's time for one evaluation
   int* head = nullptr;
   int32_t *blk_off = nullptr, *blk_first = nullptr, *blk_cnt = nullptr;
   double* partial = nullptr;
@@ -310,9 +334,14 @@ struct lpm_ensemble {
     }
     LPM_CUDA_TRY(cudaMemsetAsync(head, 0, sizeof(int), stream));
     EnsArgs a{items, queue, n_items, head, rec, org, px, py, pz, inv_a, partial, status};
-    ensemble_sweep_kernel<<<grid, kThreads, 0, stream>>>(a);
+    if (shape == 0) {
+      ensemble_sweep_kernel<128, 4, 4><<<grid, 128, 0, stream>>>(a);
+    } else {
+      ensemble_sweep_kernel<128, 8, 2><<<grid, 128, 0, stream>>>(a);
+    }
+    const int tb = kEnsShapes[shape].threads * kEnsShapes[shape].tpt;
     ensemble_finish_kernel<<<static_cast<unsigned>(ceil_div(n, 256)), 256, 0, stream>>>(
-        n, pinst, d_off, blk_off, blk_first, blk_cnt, partial, px, py, pz, inv_a, o0, o1, o2);
+        n, tb, pinst, d_off, blk_off, blk_first, blk_cnt, partial, px, py, pz, inv_a, o0, o1, o2);
     LPM_CUDA_TRY(cudaGetLastError());
     return LPM_OK;
   }
@@ -399,7 +428,72 @@ struct lpm_ensemble {
     return LPM_OK;
   }
 
-  // Builds the source layout and the flattened work queue of the FP32C sweep.
+  Queue make_queue(int sh, const std::vector<int64_t>& tile_off) const {
+    const int tb = kEnsShapes[sh].threads * kEnsShapes[sh].tpt;
+    Queue Q;
+    // item size: aim at ~8 items per resident CTA slot
+    double units = 0.0;
+    for (int k = 0; k < K; ++k)
+      units += static_cast<double>(ceil_div(off[k + 1] - off[k], tb)) * static_cast<double>(tile_off[k + 1] - tile_off[k]);
+    const int slots = ctx->sm_count * kEnsShapes[sh].minb;
+    const int64_t chunk_tiles = std::max<int64_t>(1, static_cast<int64_t>(std::ceil(units / (8.0 * slots))));
+    Q.boff.assign(K + 1, 0);
+    for (int k = 0; k < K; ++k) {
+      const int64_t nk = off[k + 1] - off[k];
+      const int64_t tiles = tile_off[k + 1] - tile_off[k];
+      const int64_t nblk = ceil_div(nk, tb);
+      Q.boff[k + 1] = Q.boff[k] + static_cast<int32_t>(nblk);
+      const int64_t nch = tiles > 0 ? ceil_div(tiles, chunk_tiles) : 0;
+      const int64_t per = nch > 0 ? ceil_div(tiles, nch) : 0;
+      for (int64_t b = 0; b < nblk; ++b) {
+        Q.bfirst.push_back(static_cast<int32_t>(Q.items.size()));
+        int cnt = 0;
+        for (int64_t t = 0; t < tiles; t += per) {
+          Item m;
+          m.inst = k;
+          m.t0 = off[k] + b * tb;
+          m.nt = static_cast<int>(std::min<int64_t>(tb, nk - b * tb));
+          m.tile0 = tile_off[k] + t;
+          m.ntiles = static_cast<int>(std::min<int64_t>(per, tiles - t));
+          m.pad = 0;
+          m.slot = static_cast<long long>(Q.items.size());
+          Q.items.push_back(m);
+          ++cnt;
+        }
+        Q.bcnt.push_back(cnt);
+      }
+    }
+    Q.order.resize(Q.items.size());
+    std::iota(Q.order.begin(), Q.order.end(), 0);
+    std::stable_sort(Q.order.begin(), Q.order.end(), [&](int p, int q) {
+      return static_cast<int64_t>(Q.items[p].nt) * Q.items[p].ntiles >
+             static_cast<int64_t>(Q.items[q].nt) * Q.items[q].ntiles;
+    });
+    Q.grid = std::max(1, std::min(static_cast<int>(Q.items.size()), slots));
+    return Q;
+  }
+
+  template <class T>
+  int upload_into(T* dst, const std::vector<T>& h) {
+    if (!h.empty()) LPM_CUDA_TRY(cudaMemcpyAsync(dst, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, stream));
+    return LPM_OK;
+  }
+
+  // Makes shape `sh` current: its queue into the (shared, largest-size) device buffers.
+  int use_queue(int sh) {
+    const Queue& Q = queues[sh];
+    LPM_TRY(upload_into(items, Q.items));
+    LPM_TRY(upload_into(queue, Q.order));
+    LPM_TRY(upload_into(blk_off, Q.boff));
+    LPM_TRY(upload_into(blk_first, Q.bfirst));
+    LPM_TRY(upload_into(blk_cnt, Q.bcnt));
+    n_items = static_cast<int>(Q.items.size());
+    grid = Q.grid;
+    shape = sh;
+    return LPM_OK;
+  }
+
+  // Builds the source layout and the work queues of every sweep shape (FP32C).
   int build_queue(const int32_t* active) {
     std::vector<int32_t> aidx, agrp, tinst;
     std::vector<int64_t> tile_off(K + 1, 0), src_start(K + 1, 0);
@@ -417,45 +511,16 @@ struct lpm_ensemble {
     }
     ns_total = static_cast<int64_t>(aidx.size());
     n_tiles = tile_off[K];
-    // item size: aim at ~8 items per resident CTA slot
-    double units = 0.0;
-    for (int k = 0; k < K; ++k)
-      units += static_cast<double>(ceil_div(off[k + 1] - off[k], kTB)) * static_cast<double>(tile_off[k + 1] - tile_off[k]);
-    const int slots = ctx->sm_count * kMinB;
-    const int64_t chunk_tiles = std::max<int64_t>(1, static_cast<int64_t>(std::ceil(units / (8.0 * slots))));
-    std::vector<Item> it;
-    std::vector<int32_t> boff(K + 1, 0), bfirst, bcnt;
-    for (int k = 0; k < K; ++k) {
-      const int64_t nk = off[k + 1] - off[k];
-      const int64_t tiles = tile_off[k + 1] - tile_off[k];
-      const int64_t nblk = ceil_div(nk, kTB);
-      boff[k + 1] = boff[k] + static_cast<int32_t>(nblk);
-      const int64_t nch = tiles > 0 ? ceil_div(tiles, chunk_tiles) : 0;
-      const int64_t per = nch > 0 ? ceil_div(tiles, nch) : 0;
-      for (int64_t b = 0; b < nblk; ++b) {
-        bfirst.push_back(static_cast<int32_t>(it.size()));
-        int cnt = 0;
-        for (int64_t t = 0; t < tiles; t += per) {
-          Item m;
-          m.inst = k;
-          m.t0 = off[k] + b * kTB;
-          m.nt = static_cast<int>(std::min<int64_t>(kTB, nk - b * kTB));
-          m.tile0 = tile_off[k] + t;
-          m.ntiles = static_cast<int>(std::min<int64_t>(per, tiles - t));
-          m.pad = 0;
-          m.slot = static_cast<long long>(it.size());
-          it.push_back(m);
-          ++cnt;
-        }
-        bcnt.push_back(cnt);
-      }
+    size_t n_it = 1, n_blk = 1, n_part = 1;
+    queues.clear();
+    for (int sh = 0; sh < kEnsShapeCount; ++sh) {
+      queues.push_back(make_queue(sh, tile_off));
+      const Queue& Q = queues.back();
+      const size_t tb = static_cast<size_t>(kEnsShapes[sh].threads) * kEnsShapes[sh].tpt;
+      n_it = std::max(n_it, Q.items.size());
+      n_blk = std::max(n_blk, Q.bcnt.size());
+      n_part = std::max(n_part, Q.items.size() * 3 * tb);
     }
-    n_items = static_cast<int>(it.size());
-    std::vector<int> order(it.size());
-    std::iota(order.begin(), order.end(), 0);
-    std::stable_sort(order.begin(), order.end(), [&](int p, int q) {
-      return static_cast<int64_t>(it[p].nt) * it[p].ntiles > static_cast<int64_t>(it[q].nt) * it[q].ntiles;
-    });
     LPM_TRY(upload_vec(&act_idx, aidx));
     LPM_TRY(upload_vec(&act_grp, agrp));
     LPM_TRY(upload_vec(&tile_inst, tinst));
@@ -467,15 +532,44 @@ struct lpm_ensemble {
     LPM_TRY(arena.alloc(sort_bytes, &sort_scratch));
     LPM_TRY(dev_array(&rec, std::max<int64_t>(n_tiles * kTile, 1)));
     LPM_TRY(dev_array(&org, std::max<int64_t>(n_tiles * (kTile / BveRel::kGroup), 1)));
-    LPM_TRY(upload_vec(&items, it));
-    LPM_TRY(upload_vec(&queue, order));
-    LPM_TRY(upload_vec(&blk_off, boff));
-    LPM_TRY(upload_vec(&blk_first, bfirst));
-    LPM_TRY(upload_vec(&blk_cnt, bcnt));
+    LPM_TRY(dev_array(&items, n_it));
+    LPM_TRY(dev_array(&queue, n_it));
+    LPM_TRY(dev_array(&blk_off, static_cast<size_t>(K) + 1));
+    LPM_TRY(dev_array(&blk_first, n_blk));
+    LPM_TRY(dev_array(&blk_cnt, n_blk));
     LPM_TRY(dev_array(&head, 1));
-    LPM_TRY(dev_array(&partial, std::max<size_t>(1, static_cast<size_t>(n_items) * 3 * kTB)));
-    grid = std::max(1, std::min(n_items, slots));
-    return LPM_OK;
+    LPM_TRY(dev_array(&partial, n_part));
+    return use_queue(0);
+  }
+
+  // Times one velocity evaluation of all instances with each sweep shape (after an untimed
+  // one) and keeps the fastest.  The results land in the stage-velocity scratch arrays.
+  int tune_shape() {
+    if (n_tiles == 0) return LPM_OK;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    LPM_CUDA_TRY(cudaEventCreate(&e0));
+    LPM_CUDA_TRY(cudaEventCreate(&e1));
+    int best = 0, rc = LPM_OK;
+    float best_ms = 3.4e38f;
+    for (int sh = 0; sh < kEnsShapeCount && rc == LPM_OK; ++sh) {
+      rc = use_queue(sh);
+      if (rc == LPM_OK) rc = velocity(x, y, z, q, us, vs, ws);
+      if (rc == LPM_OK && cudaEventRecord(e0, stream) != cudaSuccess) rc = set_error(LPM_ERR_CUDA, "event record");
+      if (rc == LPM_OK) rc = velocity(x, y, z, q, us, vs, ws);
+      if (rc == LPM_OK && cudaEventRecord(e1, stream) != cudaSuccess) rc = set_error(LPM_ERR_CUDA, "event record");
+      if (rc == LPM_OK) rc = check_status("ensemble autotune");
+      float ms = 0.f;
+      if (rc == LPM_OK && cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) rc = set_error(LPM_ERR_CUDA, "event time");
+      if (rc == LPM_OK && ms < best_ms) {
+        best_ms = ms;
+        best = sh;
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc != LPM_OK) return rc;
+    tuned_ms.assign(1, best_ms);
+    return use_queue(best);
   }
 };
 
@@ -532,6 +626,7 @@ int ens_create(lpm_ensemble* E, int K, const int64_t* offsets, const double* x, 
     }
   } else {
     LPM_TRY(E->build_queue(active));
+    LPM_TRY(E->tune_shape());
   }
   // initial velocity: setVelocityFromVorticity (SphereBVE.f90:489-531)
   LPM_TRY(E->velocity(E->x, E->y, E->z, E->q, E->u, E->v, E->w, kSumBveMesh));

@@ -69,6 +69,22 @@ enum WorkSlot : int {
   kWsCount
 };
 
+// Limits of the bounded waits of one sweep.  skip_tile >= 0 is a test hook: the copy of that
+// source tile (an index into the record array) is never issued, so the waits for it run out
+// and the sweep reports LPM_ERR_TIMEOUT without any fault.
+struct WaitCfg {
+  uint64_t ns;
+  int64_t skip_tile;
+};
+__host__ __device__ constexpr WaitCfg default_wait() { return WaitCfg{1000000000ull, -1}; }
+
+// Every device allocation of the library goes through here (cudaMalloc, or the failure that
+// lpm_debug_fail_device_alloc armed).  Returns LPM_OK or LPM_ERR_ALLOC with the message set.
+int device_alloc(void** p, size_t bytes);
+// The wait limits for the next host-buffer sphere-BVE FP32C sweep: the ones that
+// lpm_debug_inject_wait_timeout armed (once), else default_wait().
+WaitCfg take_injected_wait();
+
 // Returns the process context (initialising the device on first use).
 int get_context(Context** ctx);
 // Ensures workspace slot `slot` holds at least `bytes`; returns its pointer in *p.
@@ -153,14 +169,24 @@ __device__ __forceinline__ uint64_t global_ns() {
   return t;
 }
 
-// Waits for `phase` of the mbarrier for at most ~1 s of wall time.  Returns false (after
-// recording kDevTimeout in *status) when the limit is reached, so no wait can hang.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t phase, int* status) {
+// One arrival on an mbarrier (release semantics at CTA scope).
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// Default limit of a bounded wait: 1 s of wall time.
+constexpr uint64_t kWaitNs = 1000000000ull;
+
+// Waits for `phase` of the mbarrier for at most `budget_ns` of wall time (and 2^30 polls).
+// Returns false (after recording kDevTimeout in *status) when the limit is reached, so no
+// wait can hang.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t phase, int* status,
+                                                  uint64_t budget_ns = kWaitNs) {
   if (mbar_try_wait(bar, phase)) return true;
   const uint64_t t0 = global_ns();
   for (uint32_t it = 1;; ++it) {
     if (mbar_try_wait(bar, phase)) return true;
-    if ((it & 255u) == 0u && global_ns() - t0 > 1000000000ull) break;
+    if ((it & 255u) == 0u && global_ns() - t0 > budget_ns) break;
     if (it > (1u << 30)) break;
   }
   atomicExch(status, kDevTimeout);

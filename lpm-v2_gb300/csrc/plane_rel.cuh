@@ -13,7 +13,8 @@
 // that the self weight is finite).  Per target pair and source, far:
 //   d (2 FADD2), q = d.d + delta^2 (2 FFMA2), w = S rcp(q) (FMUL2 + 2 MUFU),
 //   U += w dy, V += w dx (2 FFMA2);
-// near: 4 more FADD2.  Each tile's FP32 partial goes into compensated (hi, lo) pairs; the
+// near: 4 more FADD2.  Each group's terms are summed in FP32 on their own and added to the
+// tile's FP32 partial (2 FADD2 per group), which goes into compensated (hi, lo) pairs; the
 // FP64 finish reduces the split-K chunks and sets u = -U, v = V.
 #pragma once
 
@@ -112,6 +113,12 @@ __global__ void __launch_bounds__(THREADS, MINB) plane_rel_sweep_kernel(PlaneRel
         const float2 n2 = __ffma2_rn(ty[p], ty[p], __fmul2_rn(tx[p], tx[p]));
         near |= (n2.x < lim) | (n2.y < lim);
       }
+      // the group's terms are summed on their own and then added to the tile's: a running
+      // FP32 sum of a whole tile's terms (both signs, e.g. the two lobes of a dipole) rounds
+      // at the size of the tile's partial sum 256 times, a group sum only 64 times
+      float2 gu[NP], gv[NP];
+#pragma unroll
+      for (int p = 0; p < NP; ++p) gu[p] = gv[p] = make_float2(0.f, 0.f);
       if (!__any_sync(0xffffffffu, near)) {
         // far group: d = t_hi - s_hi
 #pragma unroll 4
@@ -125,8 +132,8 @@ __global__ void __launch_bounds__(THREADS, MINB) plane_rel_sweep_kernel(PlaneRel
             float2 q = __ffma2_rn(dx, dx, d2);
             q = __ffma2_rn(dy, dy, q);
             const float2 w = __fmul2_rn(s2, make_float2(rcp_approx(q.x), rcp_approx(q.y)));
-            au[p] = __ffma2_rn(w, dy, au[p]);
-            av[p] = __ffma2_rn(w, dx, av[p]);
+            gu[p] = __ffma2_rn(w, dy, gu[p]);
+            gv[p] = __ffma2_rn(w, dx, gv[p]);
           }
         }
       } else {
@@ -147,10 +154,15 @@ __global__ void __launch_bounds__(THREADS, MINB) plane_rel_sweep_kernel(PlaneRel
             float2 q = __ffma2_rn(dx, dx, d2);
             q = __ffma2_rn(dy, dy, q);
             const float2 w = __fmul2_rn(s2, make_float2(rcp_approx(q.x), rcp_approx(q.y)));
-            au[p] = __ffma2_rn(w, dy, au[p]);
-            av[p] = __ffma2_rn(w, dx, av[p]);
+            gu[p] = __ffma2_rn(w, dy, gu[p]);
+            gv[p] = __ffma2_rn(w, dx, gv[p]);
           }
         }
+      }
+#pragma unroll
+      for (int p = 0; p < NP; ++p) {
+        au[p] = __fadd2_rn(au[p], gu[p]);
+        av[p] = __fadd2_rn(av[p], gv[p]);
       }
     }
     ++tile;
@@ -299,15 +311,16 @@ __device__ __forceinline__ void plane_pse_pair(float2 dx, float2 dy, float2 ks2,
   acc = __ffma2_rn(df, __fmul2_rn(lo2(rb), k), acc);
 }
 
-template <bool K8, int THREADS, int TPT, int TILE, int MINB>
+// On the warp-decoupled pipeline (S stages of TILE records), like the sphere PSE sweep: a warp
+// whose targets reach none of a tile's groups moves on without waiting for the others.
+template <bool K8, int THREADS, int TPT, int TILE, int MINB, int S>
 __global__ void __launch_bounds__(THREADS, MINB) plane_pse_rel_sweep_kernel(PlanePseRelArgs a) {
   static_assert(TPT % 2 == 0, "targets come in pairs");
   constexpr int NP = TPT / 2;
   constexpr int G = PlaneRel::kGroup;
   constexpr int GPT = TILE / G;
   using Rec = PlanePseRel::Rec;
-  __shared__ __align__(128) Rec stage[2][TILE];
-  __shared__ __align__(8) uint64_t bars[2];
+  __shared__ TilePipe<Rec, TILE, S> pipe;
 
   const int64_t chunk = blockIdx.y;
   const int64_t tile0 = chunk * a.tiles_per_chunk;
@@ -341,10 +354,10 @@ __global__ void __launch_bounds__(THREADS, MINB) plane_pse_rel_sweep_kernel(Plan
   }
   const float2 ks2 = make_float2(a.ks2, a.ks2);
 
-  pipe_init(bars);
+  tile_pipe_init(pipe);
   uint32_t g = 0;
   int64_t tile = tile0;
-  staged_sweep<Rec, TILE>(a.src, tile0, ntl, stage[0], stage[1], bars, g, a.status, [&](const Rec* tl) {
+  warp_sweep<Rec, TILE, S>(a.src, tile0, ntl, pipe, g, a.status, default_wait(), [&](const Rec* tl) {
     float2 acc[NP];
 #pragma unroll
     for (int p = 0; p < NP; ++p) acc[p] = make_float2(0.f, 0.f);

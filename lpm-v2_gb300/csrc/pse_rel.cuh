@@ -141,7 +141,10 @@ __device__ __forceinline__ void pse_pair(float2 dx, float2 dy, float2 dz, float2
   }
 }
 
-template <int OP, int ANG, int THREADS, int TPT, int TILE, int MINB>
+// The sweep runs on the warp-decoupled pipeline (S stages of TILE records): most groups are
+// out of reach of most warps, and a warp that skips a tile's groups moves on to the next
+// tile instead of waiting at a block barrier for the warps that evaluate it.
+template <int OP, int ANG, int THREADS, int TPT, int TILE, int MINB, int S>
 __global__ void __launch_bounds__(THREADS, MINB) pse_rel_sweep_kernel(PseRelArgs a) {
   static_assert(TPT % 2 == 0, "targets come in pairs");
   constexpr int NP = TPT / 2;
@@ -149,8 +152,7 @@ __global__ void __launch_bounds__(THREADS, MINB) pse_rel_sweep_kernel(PseRelArgs
   constexpr int G = BveRel::kGroup;
   constexpr int GPT = TILE / G;
   using Rec = PseRel::Rec;
-  __shared__ __align__(128) Rec stage[2][TILE];
-  __shared__ __align__(8) uint64_t bars[2];
+  __shared__ TilePipe<Rec, TILE, S> pipe;
 
   const int64_t chunk = blockIdx.y;
   const int64_t tile0 = chunk * a.tiles_per_chunk;
@@ -198,10 +200,10 @@ __global__ void __launch_bounds__(THREADS, MINB) pse_rel_sweep_kernel(PseRelArgs
   }
   const float2 ks2 = make_float2(a.ks2, a.ks2);
 
-  pipe_init(bars);
+  tile_pipe_init(pipe);
   uint32_t g = 0;
   int64_t tile = tile0;
-  staged_sweep<Rec, TILE>(a.src, tile0, ntl, stage[0], stage[1], bars, g, a.status, [&](const Rec* tl) {
+  warp_sweep<Rec, TILE, S>(a.src, tile0, ntl, pipe, g, a.status, default_wait(), [&](const Rec* tl) {
     float2 acc[NP][NC];
 #pragma unroll
     for (int p = 0; p < NP; ++p)

@@ -203,10 +203,7 @@ constexpr int kDiagBlocks = 256;
 // ------------------------------------------------------------------ DeviceArena / SumScratch
 int DeviceArena::alloc(size_t bytes, void** p) {
   void* q = nullptr;
-  cudaError_t e = cudaMalloc(&q, bytes > 0 ? bytes : 16);
-  if (e != cudaSuccess) {
-    return set_error(LPM_ERR_ALLOC, "device allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
-  }
+  LPM_TRY(device_alloc(&q, bytes));
   ptrs.push_back(q);
   *p = q;
   return LPM_OK;

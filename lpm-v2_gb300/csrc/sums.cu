@@ -34,7 +34,7 @@ struct BveShape {
 constexpr BveShape kBveShapes[] = {{128, 4, 4}, {256, 4, 2}, {128, 6, 2}, {128, 8, 2}};
 constexpr int kBveShapeCount = sizeof(kBveShapes) / sizeof(kBveShapes[0]);
 constexpr int kPlaneThreads = 128, kPlaneTpt = 4, kPlaneTile = 256, kPlaneMinB = 4;
-constexpr int kPseThreads = 128, kPseTpt = 4, kPseTile = 256, kPseMinB = 4;
+constexpr int kPseThreads = 128, kPseTpt = 4, kPseTile = 128, kPseMinB = 4, kPseStages = 4;
 constexpr int kStreamThreads = 128, kStreamTpt = 4, kStreamTile = 256, kStreamMinB = 4;
 constexpr int kBetaThreads = 128, kBetaTpt = 4, kBetaTile = 256, kBetaMinB = 4;
 constexpr int kSweMinB = 3;        // planar SWE velocity sweep: 128 x 4 targets, 3 CTAs per SM
@@ -632,7 +632,8 @@ void pse_rel_launch(const SumJob& job, const SumPlan& plan, const int32_t* src_l
       job.x, job.y, job.z, job.s1, job.s2, job.s3, job.area, src_list, job.ns, a.inv_a,
       const_cast<PseRel::Rec*>(a.src), const_cast<BveRel::Origin*>(a.org));
   const dim3 grid(static_cast<unsigned>(ceil_div(job.nt, kPseThreads * kPseTpt)), static_cast<unsigned>(plan.nsplit));
-  pse_rel_sweep_kernel<OP, ANG, kPseThreads, kPseTpt, kPseTile, kPseMinB><<<grid, kPseThreads, 0, job.stream>>>(a);
+  pse_rel_sweep_kernel<OP, ANG, kPseThreads, kPseTpt, kPseTile, kPseMinB, kPseStages>
+      <<<grid, kPseThreads, 0, job.stream>>>(a);
 }
 
 int launch_pse_rel(const SumJob& job, const SumPlan& plan, int64_t npad) {
@@ -714,9 +715,11 @@ int launch_plane_pse_rel(const SumJob& job, const SumPlan& plan, int64_t npad) {
       const_cast<PlaneRel::Origin*>(a.org));
   const dim3 grid(static_cast<unsigned>(ceil_div(job.nt, kPseThreads * kPseTpt)), static_cast<unsigned>(plan.nsplit));
   if (job.kind == kSumPseK8Chord) {
-    plane_pse_rel_sweep_kernel<true, kPseThreads, kPseTpt, kPseTile, kPseMinB><<<grid, kPseThreads, 0, job.stream>>>(a);
+    plane_pse_rel_sweep_kernel<true, kPseThreads, kPseTpt, kPseTile, kPseMinB, kPseStages>
+        <<<grid, kPseThreads, 0, job.stream>>>(a);
   } else {
-    plane_pse_rel_sweep_kernel<false, kPseThreads, kPseTpt, kPseTile, kPseMinB><<<grid, kPseThreads, 0, job.stream>>>(a);
+    plane_pse_rel_sweep_kernel<false, kPseThreads, kPseTpt, kPseTile, kPseMinB, kPseStages>
+        <<<grid, kPseThreads, 0, job.stream>>>(a);
   }
   return LPM_OK;
 }
@@ -955,6 +958,7 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
       a.nt = job.nt;
       a.partial = job.partial;
       a.status = job.status;
+      a.wait = job.wait;
       const BveShape sh = kBveShapes[plan.shape];
       const dim3 grid(static_cast<unsigned>(ceil_div(job.nt, sh.threads * sh.tpt)), static_cast<unsigned>(plan.nsplit));
       switch (plan.shape) {
@@ -1475,14 +1479,17 @@ int run_host(const HostArgs& a, int nout) {
     int shape = 0;
     LPM_TRY(autotune_bve_shape(job, ctx->sm_count, &shape));
     plan = plan_sum(a.kind, prec, ns, nt, ctx->sm_count, shape);
+    if (prec == LPM_MODE_FP32C && (a.kind == kSumBve || a.kind == kSumBveMesh)) job.wait = take_injected_wait();
     LPM_TRY(launch_sum(job, plan));
   }
+  // the caller's outputs are written only when every bounded wait of the sum succeeded
+  LPM_TRY(sync_and_check(ctx, "direct sum"));
   double* outs[4] = {a.out0, a.out1, a.out2, a.out3};
   for (int c = 0; c < nout; ++c) {
     LPM_CUDA_TRY(cudaMemcpyAsync(outs[c] + ib, dout + c * nt, static_cast<size_t>(nt) * sizeof(double),
                                  cudaMemcpyDeviceToHost, s));
   }
-  LPM_TRY(sync_and_check(ctx, "direct sum"));
+  LPM_CUDA_TRY(cudaStreamSynchronize(s));
   if (a.mode & LPM_FLAG_CHECK_FINITE) {
     for (int c = 0; c < nout; ++c) {
       for (int64_t i = ib; i < ib + nt; ++i) {

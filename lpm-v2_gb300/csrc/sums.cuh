@@ -84,6 +84,7 @@ struct SumJob {
   double* partial = nullptr;
   int* status = nullptr;
   cudaStream_t stream = nullptr;
+  WaitCfg wait = default_wait();  // limits of the sweep's bounded waits (sphere BVE FP32C)
 };
 
 // Split-K factor for a sweep of `blocks` target blocks over `tiles` source tiles on `slots`

@@ -114,6 +114,9 @@ _SIGNATURES = {
     "lpm_mesh_get_particles": [_vp, _D, _D, _D, _D, _I],
     "lpm_mesh_max_edge_length": [_vp],
     "lpm_mesh_avg_edge_length": [_vp],
+    "lpm_release_workspace": [],
+    "lpm_debug_fail_device_alloc": [_i64],
+    "lpm_debug_inject_wait_timeout": [_i64, _i64],
 }
 _RESTYPES = {
     "lpm_last_error_string": ctypes.c_char_p,
@@ -606,6 +609,22 @@ class Ensemble:
             self.close()
         except Exception:
             pass
+
+
+def release_workspace() -> None:
+    """Frees the device workspace the host-buffer calls keep between calls."""
+    _check(lib().lpm_release_workspace())
+
+
+def debug_fail_device_alloc(k: int) -> None:
+    """Test hook: the k-th device allocation from now on fails (0 disarms)."""
+    _check(lib().lpm_debug_fail_device_alloc(int(k)))
+
+
+def debug_inject_wait_timeout(skip_tile: int, budget_ns: int) -> None:
+    """Test hook: the next host-buffer sphere-BVE FP32C sum skips the copy of one source tile
+    and bounds its waits by budget_ns, so it returns LPM_ERR_TIMEOUT (one-shot)."""
+    _check(lib().lpm_debug_inject_wait_timeout(int(skip_tile), int(budget_ns)))
 
 
 def measure_fp32_peak(ms_target: float = 200.0) -> float:

@@ -290,6 +290,36 @@ def test_beta_plane_fp32c_distant_clusters(lg, oracle_mod):
     assert max(rel(pr, rr), rel(pa, ra)) <= FP32C_TOL
 
 
+@pytest.mark.parametrize("radius", [0.03, 0.08])
+def test_beta_plane_fp32c_targets_just_beyond_near_limit(lg, oracle_mod, radius):
+    """Targets in the band 4.05R-4.95R of one compact group of 64 sources: every warp takes the
+    complex far form there (the near limit is max(4R, 0.02)), where its cancellation is the
+    largest.  Velocity and stream functions against the oracle to 1e-6 of their max."""
+    rng = np.random.default_rng(int(radius * 1000))
+    ns, nt = 64, 4096
+    sx = 0.5 + radius * 0.5 * rng.uniform(-1, 1, ns)
+    sy = radius * 0.5 * rng.uniform(-1, 1, ns)
+    o = np.array([sx.mean(), sy.mean()])
+    R = np.sqrt((sx - o[0]) ** 2 + (sy - o[1]) ** 2).max()
+    rho = R * rng.uniform(4.05, 4.95, nt)
+    th = rng.uniform(0.0, 2.0 * np.pi, nt)
+    x = np.concatenate([sx, o[0] + rho * np.cos(th)])
+    y = np.concatenate([sy, o[1] + rho * np.sin(th)])
+    area = np.concatenate([rng.uniform(0.5, 1.5, ns) * 1e-3, np.zeros(nt)])
+    zeta = np.concatenate([rng.uniform(-1.0, 1.0, ns) + 0.3, np.zeros(nt)])
+    absv = zeta + 2.0 * y
+    act = np.concatenate([np.ones(ns), np.zeros(nt)]).astype(np.int32)
+    ib, ie = ns + 1, ns + nt
+    s = slice(ib - 1, ie)
+    u, v = lg.beta_plane_velocity(x, y, zeta, area, act, ib, ie, mode="fp32c")
+    ru, rv = oracle_mod.beta_plane_velocity(x, y, zeta, area, act, ib - 1, ie)
+    scale = max(np.abs(ru).max(), np.abs(rv).max())
+    assert max(np.abs(u[s] - ru).max(), np.abs(v[s] - rv).max()) <= FP32C_TOL * scale
+    pr, pa = lg.beta_plane_stream_functions(x, y, zeta, absv, area, act, ib, ie, mode="fp32c")
+    rr, ra = oracle_mod.beta_plane_stream(x, y, zeta, absv, area, act, ib - 1, ie)
+    assert max(rel(pr[s], rr), rel(pa[s], ra)) <= FP32C_TOL
+
+
 @pytest.mark.parametrize("n", [1, 2, 63, 65, 257, 1031])
 def test_beta_plane_fp32c_ragged_and_empty(lg, oracle_mod, n):
     """Ragged sizes (partial groups and tiles, inert records) and a set with no active source

@@ -272,7 +272,7 @@ def test_beta_complex_far_form_identity(oracle_mod):
         ej = np.exp(2j * np.pi * ((pts[:, 0] - zo[0]) + 1j * (pts[:, 1] - zo[1])))
         dx = tx - zo[0]
         dx -= np.rint(dx)
-        far = dx * dx + (ty - zo[1]) ** 2 > (5.0 * R) ** 2
+        far = dx * dx + (ty - zo[1]) ** 2 > (4.0 * R) ** 2  # the kernels' near limit, 4R
         ei = np.exp(2j * np.pi * (dx + 1j * (ty - zo[1])))
         G = (S[None, :] * ej[None, :] / (ei[:, None] - ej[None, :])).sum(1)
         u = S.sum() + 2.0 * G.real
