@@ -436,6 +436,7 @@ def measure_ensemble(torch, lg, wl, n_instances, steps, warmup, dt, inst=None, c
         inst = wl.config_ensemble(n_instances=n_instances, seed=0)
     inter_eval = sum(int(d["x"].size) * int(d["active"].sum()) - int(d["active"].sum()) for d in inst)
     ens = lg.Ensemble(inst, mode="fp32c")
+    shape = ens.sweep_shape()
     ens.timestep(dt, max(warmup, 3), renormalize=True)
     torch.cuda.synchronize()
     k0 = ens.kernel_timing()
@@ -480,6 +481,8 @@ def measure_ensemble(torch, lg, wl, n_instances, steps, warmup, dt, inst=None, c
             "sequential": {"value": total / t_seq / 1e9, "unit": UNIT, "ms_per_step": 1e3 * t_seq / steps,
                            "how": "one BVESolver per instance, each replaying its step graph back to back"},
             "speedup_vs_sequential": t_seq / t_batch,
+            "sweep_shape": {"threads": shape[0], "targets_per_thread": shape[1], "ctas_per_sm": shape[2],
+                            "items_per_cta_slot": shape[3]},
             "sum_kernel_ms_per_step": (k1[0] - k0[0]) / steps,
             "gpu_launches": k1[1] - k0[1],
             "velocity_rel_linf_vs_fp64_max": max(errs), "instances_checked": len(errs),
@@ -506,7 +509,7 @@ def run_ensemble(args):
         sub = [d for d in inst if d["nest"] == nest]
         q = measure_ensemble(torch, lg, wl, len(sub), max(2, steps // 5), args.warmup, args.dt, inst=sub, check=2)
         classes[str(nest)] = {"instances": len(sub), "batched": q["value"], "sequential": q["sequential"]["value"],
-                              "speedup_vs_sequential": q["speedup_vs_sequential"],
+                              "speedup_vs_sequential": q["speedup_vs_sequential"], "sweep_shape": q["sweep_shape"],
                               "interactions_per_eval": q["interactions_per_eval"], "steps": q["steps"]}
     line = {
         "metric": "BVE ensemble Ginteractions/s (64 uneven instances, batched persistent launch)", "value": r["value"],
@@ -520,6 +523,7 @@ def run_ensemble(args):
         "sequential": r["sequential"],
         "speedup_vs_sequential": r["speedup_vs_sequential"],
         "sum_kernel_ms_per_step": r["sum_kernel_ms_per_step"],
+        "sweep_shape": r["sweep_shape"],
         "gpu_launches": r["gpu_launches"],
         "accuracy": {"velocity_rel_linf_vs_fp64_max": r["velocity_rel_linf_vs_fp64_max"],
                      "instances_checked": r["instances_checked"]},

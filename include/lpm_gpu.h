@@ -321,6 +321,11 @@ int lpm_ensemble_velocity(lpm_ensemble* ens);
 int lpm_ensemble_get_state(lpm_ensemble* ens, double* x, double* y, double* z,
                            double* relvort, double* u, double* v, double* w);
 int lpm_ensemble_kernel_timing(lpm_ensemble* ens, double* total_ms, int64_t* launches);
+/* The persistent sweep's configuration the autotuner chose at creation (LPM_MODE_FP32C; all
+ * zero in LPM_MODE_FP64): CTA threads, targets per thread, CTAs per SM, and the work items
+ * per resident CTA the source ranges were cut for.  Any pointer may be NULL. */
+int lpm_ensemble_sweep_shape(lpm_ensemble* ens, int* threads, int* targets_per_thread,
+                             int* ctas_per_sm, int* items_per_slot);
 int lpm_ensemble_destroy(lpm_ensemble* ens);
 
 /* ------------------------------------------------------------------ allocation-free call */

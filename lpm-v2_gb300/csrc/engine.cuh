@@ -89,16 +89,19 @@ __device__ __forceinline__ bool staged_sweep(const Rec* __restrict__ src, int64_
                                  static_cast<Body&&>(body));
 }
 
-// Shared memory of an S-stage warp-decoupled pipeline.
-template <class Rec, int TILE, int S>
+// Shared memory of an S-stage warp-decoupled pipeline.  With NSIDE > 0 each stage also holds
+// the tile's NSIDE side records (e.g. its group origins), copied with the tile, so that a warp
+// reads them from shared memory rather than waiting on a global load per group.
+template <class Rec, int TILE, int S, class Side = Rec, int NSIDE = 0>
 struct __align__(128) TilePipe {
   Rec stage[S][TILE];
-  uint64_t full[S];   // completes when tile data has landed (1 arrival + the copy's bytes)
+  Side side[S][NSIDE > 0 ? NSIDE : 1];
+  uint64_t full[S];   // completes when tile data has landed (1 arrival + the copies' bytes)
   uint64_t empty[S];  // completes when every warp is done with the stage (one arrival per warp)
 };
 
-template <class Rec, int TILE, int S>
-__device__ __forceinline__ void tile_pipe_init(TilePipe<Rec, TILE, S>& pp) {
+template <class Rec, int TILE, int S, class Side, int NSIDE>
+__device__ __forceinline__ void tile_pipe_init(TilePipe<Rec, TILE, S, Side, NSIDE>& pp) {
   if (threadIdx.x == 0) {
     for (int s = 0; s < S; ++s) {
       mbar_init(&pp.full[s], 1);
@@ -117,12 +120,15 @@ __device__ __forceinline__ void tile_pipe_init(TilePipe<Rec, TILE, S>& pp) {
 // issues the copies: before each of its tiles it refills every stage already released,
 // keeping up to S tiles in flight, and it blocks (bounded) on a release only when the tile
 // it needs next has not been issued.  Returns false in every thread when any wait gave up.
-template <class Rec, int TILE, int S, class Body>
+// With NSIDE > 0 the side records of tile t are side_src[t * NSIDE .. (t + 1) * NSIDE) and
+// body(const Rec*, const Side*) gets both; otherwise body(const Rec*).
+template <class Rec, int TILE, int S, class Side, int NSIDE, class Body>
 __device__ __forceinline__ bool warp_sweep(const Rec* __restrict__ src, int64_t tile0, int64_t ntl,
-                                           TilePipe<Rec, TILE, S>& pp, uint32_t& g, int* status,
-                                           const WaitCfg& w, Body&& body) {
+                                           TilePipe<Rec, TILE, S, Side, NSIDE>& pp, uint32_t& g, int* status,
+                                           const WaitCfg& w, const Side* __restrict__ side_src, Body&& body) {
   constexpr uint32_t kBytes = TILE * sizeof(Rec);
-  static_assert(kBytes % 16 == 0, "tile bytes must be a multiple of 16");
+  constexpr uint32_t kSideBytes = NSIDE * sizeof(Side);
+  static_assert(kBytes % 16 == 0 && kSideBytes % 16 == 0, "copies must be multiples of 16 bytes");
   static_assert(S >= 2, "at least two stages");
   const bool producer = threadIdx.x == 0;
   int64_t next = 0;  // next tile to issue (thread 0)
@@ -141,8 +147,9 @@ __device__ __forceinline__ bool warp_sweep(const Rec* __restrict__ src, int64_t 
       }
     }
     if (tile0 + kk != w.skip_tile) {
-      mbar_arrive_expect_tx(&pp.full[s], kBytes);
+      mbar_arrive_expect_tx(&pp.full[s], kBytes + kSideBytes);
       tma_load_1d(pp.stage[s], src + (tile0 + kk) * TILE, kBytes, &pp.full[s]);
+      if constexpr (NSIDE > 0) tma_load_1d(pp.side[s], side_src + (tile0 + kk) * NSIDE, kSideBytes, &pp.full[s]);
     }
     return 1;
   };
@@ -160,7 +167,11 @@ __device__ __forceinline__ bool warp_sweep(const Rec* __restrict__ src, int64_t 
     const uint32_t s = q % S;
     const bool mine = ok && mbar_wait_bounded(&pp.full[s], (q / S) & 1u, status, w.ns);
     if (!__all_sync(0xffffffffu, mine)) break;
-    body(pp.stage[s]);
+    if constexpr (NSIDE > 0) {
+      body(pp.stage[s], pp.side[s]);
+    } else {
+      body(pp.stage[s]);
+    }
     __syncwarp();
     if ((threadIdx.x & 31u) == 0u) mbar_arrive(&pp.empty[s]);
   }

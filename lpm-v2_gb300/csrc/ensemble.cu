@@ -19,8 +19,10 @@
 //
 // Autotuner: the persistent kernel comes in the CTA shapes the single-instance tuner picks
 // from (128 threads x 4 targets at 4 CTAs per SM: 512 targets per item; 128 x 8 at 2 per SM:
-// 1024).  At creation each shape's work queue is built and one velocity evaluation of all
-// instances is timed; the faster shape is kept for the ensemble's life.
+// 1024), and the source ranges are cut for about 4, 8 or 16 items per resident CTA (fewer,
+// longer items cost less per item; more, shorter ones leave a shorter tail).  At creation
+// the work queue of each of the six choices is built and one velocity evaluation of all
+// instances is timed; the fastest is kept for the ensemble's life.
 //
 // FP64 mode (parity) runs the bit-exact sequential sweep per instance instead.
 #include <algorithm>
@@ -43,7 +45,6 @@ struct EnsShape {
   int threads, tpt, minb;
 };
 constexpr EnsShape kEnsShapes[] = {{128, 4, 4}, {128, 8, 2}};
-constexpr int kEnsShapeCount = sizeof(kEnsShapes) / sizeof(kEnsShapes[0]);
 constexpr double kPi = 3.1415926535897932384626433832795027975;
 constexpr int kStage = 256;
 
@@ -56,6 +57,13 @@ struct Item {
   int pad;
   long long slot;  // partial slot (item id in block order)
 };
+
+// Queue choices of the autotuner: (sweep shape, items per resident CTA slot).
+struct QueueChoice {
+  int shape, per_slot;
+};
+constexpr QueueChoice kQueueChoices[] = {{0, 4}, {0, 8}, {0, 16}, {1, 4}, {1, 8}, {1, 16}};
+constexpr int kQueueChoiceCount = sizeof(kQueueChoices) / sizeof(kQueueChoices[0]);
 
 // The flattened work queue of one sweep shape, on the host.
 struct Queue {
@@ -271,7 +279,8 @@ struct lpm_ensemble {
   int* queue = nullptr;
   int n_items = 0;
   int shape = 0;                     // kEnsShapes index of the persistent sweep
-  std::vector<Queue> queues;         // host copies of every shape's work queue
+  int choice = 0;                    // kQueueChoices index in use
+  std::vector<Queue> queues;         // host copies of every choice's work queue
   std::vector<float> tuned_ms;       // the chosen shape's time for one evaluation
   int* head = nullptr;
   int32_t *blk_off = nullptr, *blk_first = nullptr, *blk_cnt = nullptr;
@@ -428,15 +437,16 @@ struct lpm_ensemble {
     return LPM_OK;
   }
 
-  Queue make_queue(int sh, const std::vector<int64_t>& tile_off) const {
+  Queue make_queue(int sh, int per_slot, const std::vector<int64_t>& tile_off) const {
     const int tb = kEnsShapes[sh].threads * kEnsShapes[sh].tpt;
     Queue Q;
-    // item size: aim at ~8 items per resident CTA slot
+    // item size: aim at ~per_slot items per resident CTA slot
     double units = 0.0;
     for (int k = 0; k < K; ++k)
       units += static_cast<double>(ceil_div(off[k + 1] - off[k], tb)) * static_cast<double>(tile_off[k + 1] - tile_off[k]);
     const int slots = ctx->sm_count * kEnsShapes[sh].minb;
-    const int64_t chunk_tiles = std::max<int64_t>(1, static_cast<int64_t>(std::ceil(units / (8.0 * slots))));
+    const int64_t chunk_tiles =
+        std::max<int64_t>(1, static_cast<int64_t>(std::ceil(units / (static_cast<double>(per_slot) * slots))));
     Q.boff.assign(K + 1, 0);
     for (int k = 0; k < K; ++k) {
       const int64_t nk = off[k + 1] - off[k];
@@ -479,9 +489,9 @@ struct lpm_ensemble {
     return LPM_OK;
   }
 
-  // Makes shape `sh` current: its queue into the (shared, largest-size) device buffers.
-  int use_queue(int sh) {
-    const Queue& Q = queues[sh];
+  // Makes queue choice `ch` current: its queue into the (shared, largest-size) device buffers.
+  int use_queue(int ch) {
+    const Queue& Q = queues[ch];
     LPM_TRY(upload_into(items, Q.items));
     LPM_TRY(upload_into(queue, Q.order));
     LPM_TRY(upload_into(blk_off, Q.boff));
@@ -489,7 +499,8 @@ struct lpm_ensemble {
     LPM_TRY(upload_into(blk_cnt, Q.bcnt));
     n_items = static_cast<int>(Q.items.size());
     grid = Q.grid;
-    shape = sh;
+    shape = kQueueChoices[ch].shape;
+    choice = ch;
     return LPM_OK;
   }
 
@@ -513,8 +524,9 @@ struct lpm_ensemble {
     n_tiles = tile_off[K];
     size_t n_it = 1, n_blk = 1, n_part = 1;
     queues.clear();
-    for (int sh = 0; sh < kEnsShapeCount; ++sh) {
-      queues.push_back(make_queue(sh, tile_off));
+    for (int ch = 0; ch < kQueueChoiceCount; ++ch) {
+      const int sh = kQueueChoices[ch].shape;
+      queues.push_back(make_queue(sh, kQueueChoices[ch].per_slot, tile_off));
       const Queue& Q = queues.back();
       const size_t tb = static_cast<size_t>(kEnsShapes[sh].threads) * kEnsShapes[sh].tpt;
       n_it = std::max(n_it, Q.items.size());
@@ -542,7 +554,7 @@ struct lpm_ensemble {
     return use_queue(0);
   }
 
-  // Times one velocity evaluation of all instances with each sweep shape (after an untimed
+  // Times one velocity evaluation of all instances with each queue choice (after an untimed
   // one) and keeps the fastest.  The results land in the stage-velocity scratch arrays.
   int tune_shape() {
     if (n_tiles == 0) return LPM_OK;
@@ -551,7 +563,7 @@ struct lpm_ensemble {
     LPM_CUDA_TRY(cudaEventCreate(&e1));
     int best = 0, rc = LPM_OK;
     float best_ms = 3.4e38f;
-    for (int sh = 0; sh < kEnsShapeCount && rc == LPM_OK; ++sh) {
+    for (int sh = 0; sh < kQueueChoiceCount && rc == LPM_OK; ++sh) {
       rc = use_queue(sh);
       if (rc == LPM_OK) rc = velocity(x, y, z, q, us, vs, ws);
       if (rc == LPM_OK && cudaEventRecord(e0, stream) != cudaSuccess) rc = set_error(LPM_ERR_CUDA, "event record");
@@ -701,6 +713,18 @@ extern "C" int lpm_ensemble_kernel_timing(lpm_ensemble* E, double* total_ms, int
   if (!E) return set_error(LPM_ERR_ARG, "null ensemble");
   if (total_ms) *total_ms = E->kernel_ms;
   if (launches) *launches = E->launches;
+  return LPM_OK;
+}
+
+extern "C" int lpm_ensemble_sweep_shape(lpm_ensemble* E, int* threads, int* targets_per_thread, int* ctas_per_sm,
+                                        int* items_per_slot) {
+  if (!E) return set_error(LPM_ERR_ARG, "null ensemble");
+  const bool fp32c = E->mode == LPM_MODE_FP32C;
+  const EnsShape& sh = kEnsShapes[E->shape];
+  if (threads) *threads = fp32c ? sh.threads : 0;
+  if (targets_per_thread) *targets_per_thread = fp32c ? sh.tpt : 0;
+  if (ctas_per_sm) *ctas_per_sm = fp32c ? sh.minb : 0;
+  if (items_per_slot) *items_per_slot = fp32c ? kQueueChoices[E->choice].per_slot : 0;
   return LPM_OK;
 }
 

@@ -291,6 +291,9 @@ struct PlanePseRelArgs {
   const PlanePseRel::Rec* src;
   const PlaneRel::Origin* org;
   int64_t n_tiles, tiles_per_chunk, ib, nt;
+  // targets in curve order: position k of the sweep is particle tperm[k] (nullptr: ib + k);
+  // partial sums are stored at the particle's own place, (tperm[k] - ib)
+  const int32_t* tperm;
   double* partial;  // [chunk][nt]
   int* status;
 };
@@ -320,7 +323,7 @@ __global__ void __launch_bounds__(THREADS, MINB) plane_pse_rel_sweep_kernel(Plan
   constexpr int G = PlaneRel::kGroup;
   constexpr int GPT = TILE / G;
   using Rec = PlanePseRel::Rec;
-  __shared__ TilePipe<Rec, TILE, S> pipe;
+  __shared__ TilePipe<Rec, TILE, S, PlaneRel::Origin, GPT> pipe;
 
   const int64_t chunk = blockIdx.y;
   const int64_t tile0 = chunk * a.tiles_per_chunk;
@@ -332,14 +335,19 @@ __global__ void __launch_bounds__(THREADS, MINB) plane_pse_rel_sweep_kernel(Plan
   float2 fh[NP], fl[NP], hs[NP], ls[NP];
   const int64_t first = static_cast<int64_t>(blockIdx.x) * (THREADS * TPT);
   const int64_t count = a.nt - first < THREADS * TPT ? a.nt - first : THREADS * TPT;
+  // each warp takes 32 x TPT consecutive targets of the (curve-ordered) block
+  const int64_t wbase = static_cast<int64_t>(threadIdx.x >> 5) * (32 * TPT) + (threadIdx.x & 31);
+  int64_t tgt[NP][2];
 #pragma unroll
   for (int p = 0; p < NP; ++p) {
     float vh[2][3], vl[2][3];
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
-      int64_t il = (2 * p + h) * THREADS + threadIdx.x;
+      int64_t il = wbase + (2 * p + h) * 32;
+      tgt[p][h] = il < count ? first + il : -1;
       if (il >= count) il = count - 1;  // duplicates of a valid target; results not stored
-      const int64_t i = a.ib + first + il;
+      const int64_t i = a.tperm ? static_cast<int64_t>(a.tperm[first + il]) : a.ib + first + il;
+      if (tgt[p][h] >= 0) tgt[p][h] = i - a.ib;
       split2(a.x[i], vh[h][0], vl[h][0]);
       split2(a.y[i], vh[h][1], vl[h][1]);
       split2(a.f[i], vh[h][2], vl[h][2]);
@@ -356,12 +364,11 @@ __global__ void __launch_bounds__(THREADS, MINB) plane_pse_rel_sweep_kernel(Plan
 
   tile_pipe_init(pipe);
   uint32_t g = 0;
-  int64_t tile = tile0;
-  warp_sweep<Rec, TILE, S>(a.src, tile0, ntl, pipe, g, a.status, default_wait(), [&](const Rec* tl) {
+  warp_sweep(a.src, tile0, ntl, pipe, g, a.status, default_wait(), a.org,
+             [&](const Rec* tl, const PlaneRel::Origin* og) {
     float2 acc[NP];
 #pragma unroll
     for (int p = 0; p < NP; ++p) acc[p] = make_float2(0.f, 0.f);
-    const PlaneRel::Origin* og = a.org + tile * GPT;
 #pragma unroll 1
     for (int g0 = 0; g0 < TILE; g0 += G) {
       const PlaneRel::Origin o = og[g0 / G];
@@ -406,7 +413,6 @@ __global__ void __launch_bounds__(THREADS, MINB) plane_pse_rel_sweep_kernel(Plan
         }
       }
     }
-    ++tile;
 #pragma unroll
     for (int p = 0; p < NP; ++p) {
       comp_add(hs[p].x, ls[p].x, acc[p].x);
@@ -418,8 +424,8 @@ __global__ void __launch_bounds__(THREADS, MINB) plane_pse_rel_sweep_kernel(Plan
   for (int p = 0; p < NP; ++p) {
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
-      const int64_t il = first + (2 * p + h) * THREADS + threadIdx.x;
-      if (il < a.nt)
+      const int64_t il = tgt[p][h];
+      if (il >= 0)
         a.partial[chunk * a.nt + il] = static_cast<double>(h ? hs[p].y : hs[p].x) + static_cast<double>(h ? ls[p].y : ls[p].x);
     }
   }

@@ -61,6 +61,9 @@ struct PseRelArgs {
   const PseRel::Rec* src;
   const BveRel::Origin* org;  // hi.w: near radius (0 for a compact group), lo.w: group radius
   int64_t n_tiles, tiles_per_chunk, ib, nt;
+  // targets in curve order: position k of the sweep is particle tperm[k] (nullptr: ib + k);
+  // partial sums are stored at the particle's own place, (tperm[k] - ib)
+  const int32_t* tperm;
   double* partial;  // [chunk][comps][nt]
   int* status;
 };
@@ -152,7 +155,7 @@ __global__ void __launch_bounds__(THREADS, MINB) pse_rel_sweep_kernel(PseRelArgs
   constexpr int G = BveRel::kGroup;
   constexpr int GPT = TILE / G;
   using Rec = PseRel::Rec;
-  __shared__ TilePipe<Rec, TILE, S> pipe;
+  __shared__ TilePipe<Rec, TILE, S, BveRel::Origin, GPT> pipe;
 
   const int64_t chunk = blockIdx.y;
   const int64_t tile0 = chunk * a.tiles_per_chunk;
@@ -164,14 +167,20 @@ __global__ void __launch_bounds__(THREADS, MINB) pse_rel_sweep_kernel(PseRelArgs
   float2 hs[NP][NC], ls[NP][NC];
   const int64_t first = static_cast<int64_t>(blockIdx.x) * (THREADS * TPT);
   const int64_t count = a.nt - first < THREADS * TPT ? a.nt - first : THREADS * TPT;
+  // each warp takes 32 x TPT consecutive targets of the (curve-ordered) block, so that its
+  // targets are close together and the group cutoff passes over as many groups as it can
+  const int64_t wbase = static_cast<int64_t>(threadIdx.x >> 5) * (32 * TPT) + (threadIdx.x & 31);
+  int64_t tgt[NP][2];
 #pragma unroll
   for (int p = 0; p < NP; ++p) {
     float vh[2][3], vl[2][3], ex[2][3];
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
-      int64_t il = (2 * p + h) * THREADS + threadIdx.x;
+      int64_t il = wbase + (2 * p + h) * 32;
+      tgt[p][h] = il < count ? first + il : -1;
       if (il >= count) il = count - 1;  // duplicates of a valid target; results not stored
-      const int64_t i = a.ib + first + il;
+      const int64_t i = a.tperm ? static_cast<int64_t>(a.tperm[first + il]) : a.ib + first + il;
+      if (tgt[p][h] >= 0) tgt[p][h] = i - a.ib;
       double px, py, pz;
       pse_position<ANG>(a.x, a.y, a.z, i, a.inv_a, px, py, pz);
       split2(px, vh[h][0], vl[h][0]);
@@ -202,14 +211,13 @@ __global__ void __launch_bounds__(THREADS, MINB) pse_rel_sweep_kernel(PseRelArgs
 
   tile_pipe_init(pipe);
   uint32_t g = 0;
-  int64_t tile = tile0;
-  warp_sweep<Rec, TILE, S>(a.src, tile0, ntl, pipe, g, a.status, default_wait(), [&](const Rec* tl) {
+  warp_sweep(a.src, tile0, ntl, pipe, g, a.status, default_wait(), a.org,
+             [&](const Rec* tl, const BveRel::Origin* og) {
     float2 acc[NP][NC];
 #pragma unroll
     for (int p = 0; p < NP; ++p)
 #pragma unroll
       for (int c = 0; c < NC; ++c) acc[p][c] = make_float2(0.f, 0.f);
-    const BveRel::Origin* og = a.org + tile * GPT;
 #pragma unroll 1
     for (int g0 = 0; g0 < TILE; g0 += G) {
       const BveRel::Origin o = og[g0 / G];
@@ -260,7 +268,6 @@ __global__ void __launch_bounds__(THREADS, MINB) pse_rel_sweep_kernel(PseRelArgs
         }
       }
     }
-    ++tile;
 #pragma unroll
     for (int p = 0; p < NP; ++p)
 #pragma unroll
@@ -274,8 +281,8 @@ __global__ void __launch_bounds__(THREADS, MINB) pse_rel_sweep_kernel(PseRelArgs
   for (int p = 0; p < NP; ++p) {
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
-      const int64_t il = first + (2 * p + h) * THREADS + threadIdx.x;
-      if (il < a.nt) {
+      const int64_t il = tgt[p][h];
+      if (il >= 0) {
 #pragma unroll
         for (int c = 0; c < NC; ++c)
           a.partial[(chunk * NC + c) * a.nt + il] =

@@ -34,7 +34,10 @@ struct BveShape {
 constexpr BveShape kBveShapes[] = {{128, 4, 4}, {256, 4, 2}, {128, 6, 2}, {128, 8, 2}};
 constexpr int kBveShapeCount = sizeof(kBveShapes) / sizeof(kBveShapes[0]);
 constexpr int kPlaneThreads = 128, kPlaneTpt = 4, kPlaneTile = 256, kPlaneMinB = 4;
-constexpr int kPseThreads = 128, kPseTpt = 4, kPseTile = 128, kPseMinB = 4, kPseStages = 4;
+// PSE sweeps (warp-decoupled pipeline): 256-source tiles in two stages; the divergence, whose
+// sweep holds more per-target state (128 registers), runs faster on 128-source tiles in four
+constexpr int kPseThreads = 128, kPseTpt = 4, kPseTile = 256, kPseMinB = 4, kPseStages = 2;
+constexpr int kPseDivTile = 128, kPseDivStages = 4;
 constexpr int kStreamThreads = 128, kStreamTpt = 4, kStreamTile = 256, kStreamMinB = 4;
 constexpr int kBetaThreads = 128, kBetaTpt = 4, kBetaTile = 256, kBetaMinB = 4;
 constexpr int kSweMinB = 3;        // planar SWE velocity sweep: 128 x 4 targets, 3 CTAs per SM
@@ -430,8 +433,9 @@ int tile_of(int kind, int mode) {
     case kSumSwePlane:
       return kPlaneTile;
     case kSumPseGrad:
-    case kSumPseDiv:
       return kPseTile;
+    case kSumPseDiv:
+      return kPseDivTile;
     case kSumSphereStream:
     case kSumPlaneStream:
     case kSumSweSphere:
@@ -550,13 +554,22 @@ bool sum_uses_sorted_sources(int kind, int mode) {
                                     kind == kSumBetaPlane || kind == kSumBetaStream);
 }
 
-size_t sort_scratch_bytes(int kind, int64_t ns) {
+namespace {
+// The FP32C PSE kinds also sort their targets (nt of them) with the same scratch.
+bool pse_sorts_targets(int kind) {
+  return kind == kSumPseK8Geo || kind == kSumPseGaussChord || kind == kSumPseK8Chord || kind == kSumPseGrad ||
+         kind == kSumPseDiv;
+}
+}  // namespace
+
+size_t sort_scratch_bytes(int kind, int64_t ns, int64_t nt) {
+  const int64_t m = pse_sorts_targets(kind) && nt > ns ? nt : ns;
   // planar kinds sort in 2-D; the Gaussian-chord Laplacian serves the plane and the sphere
   if (kind == kSumPlane || kind == kSumPseK8Chord || kind == kSumPlaneStream || kind == kSumSwePlane ||
       kind == kSumBetaPlane || kind == kSumBetaStream)
-    return curve_sort2d_bytes(ns);
-  if (kind == kSumPseGaussChord) return std::max(curve_sort_bytes(ns), curve_sort2d_bytes(ns));
-  return curve_sort_bytes(ns);
+    return curve_sort2d_bytes(m);
+  if (kind == kSumPseGaussChord) return std::max(curve_sort_bytes(m), curve_sort2d_bytes(m));
+  return curve_sort_bytes(m);
 }
 
 int bve_shape_count() { return kBveShapeCount; }
@@ -577,6 +590,10 @@ SumPlan plan_sum(int kind, int mode, int64_t ns, int64_t nt, int sm_count, int s
                   "one origin layout size");
     pl.src_bytes = align_up(pl.src_bytes, 256) +
                    static_cast<size_t>(pl.n_tiles) * (tile / BveRel::kGroup) * sizeof(BveRel::Origin);
+  }
+  if (mode == LPM_MODE_FP32C && pse_sorts_targets(kind)) {
+    pl.tperm_offset = align_up(pl.src_bytes, 256);
+    pl.src_bytes = pl.tperm_offset + 2 * align_up(static_cast<size_t>(nt) * sizeof(int32_t), 256);
   }
   if (mode == LPM_MODE_FP32C && kind == kSumSphereStream) {
     // the sources' own zeta A (2 x nt) and the two totals follow the group origins
@@ -628,12 +645,35 @@ namespace {
 // The sphere PSE sums on the group-relative layout (pse_rel.cuh): sort, prep and sweep.
 template <int OP, int ANG>
 void pse_rel_launch(const SumJob& job, const SumPlan& plan, const int32_t* src_list, const PseRelArgs& a) {
-  pse_rel_prep_kernel<OP, ANG, kPseTile><<<static_cast<unsigned>(plan.n_tiles), kPseTile, 0, job.stream>>>(
+  constexpr int TILE = OP == kPseOpDiv ? kPseDivTile : kPseTile;
+  constexpr int S = OP == kPseOpDiv ? kPseDivStages : kPseStages;
+  pse_rel_prep_kernel<OP, ANG, TILE><<<static_cast<unsigned>(plan.n_tiles), TILE, 0, job.stream>>>(
       job.x, job.y, job.z, job.s1, job.s2, job.s3, job.area, src_list, job.ns, a.inv_a,
       const_cast<PseRel::Rec*>(a.src), const_cast<BveRel::Origin*>(a.org));
   const dim3 grid(static_cast<unsigned>(ceil_div(job.nt, kPseThreads * kPseTpt)), static_cast<unsigned>(plan.nsplit));
-  pse_rel_sweep_kernel<OP, ANG, kPseThreads, kPseTpt, kPseTile, kPseMinB, kPseStages>
-      <<<grid, kPseThreads, 0, job.stream>>>(a);
+  pse_rel_sweep_kernel<OP, ANG, kPseThreads, kPseTpt, TILE, kPseMinB, S><<<grid, kPseThreads, 0, job.stream>>>(a);
+}
+
+// The list ib, ib + 1, ..., ib + n - 1.
+__global__ void iota_kernel(int64_t n, int64_t ib, int32_t* out) {
+  const int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k < n) out[k] = static_cast<int32_t>(ib + k);
+}
+
+// The targets of a PSE sweep in curve order, when the plan has room for them and the job
+// brings sort scratch (nullptr otherwise: the sweep takes targets in index order).  The sort
+// scratch is reused after the sources' sort (stream order).
+template <class SortFn>
+int sorted_targets(const SumJob& job, const SumPlan& plan, SortFn&& sort, const int32_t** tperm) {
+  *tperm = nullptr;
+  if (!job.sort_scratch || plan.tperm_offset == 0 || job.nt < 2) return LPM_OK;
+  int32_t* in = reinterpret_cast<int32_t*>(static_cast<char*>(job.src_buf) + plan.tperm_offset);
+  int32_t* out = reinterpret_cast<int32_t*>(reinterpret_cast<char*>(in) +
+                                            align_up(static_cast<size_t>(job.nt) * sizeof(int32_t), 256));
+  iota_kernel<<<static_cast<unsigned>(ceil_div(job.nt, 256)), 256, 0, job.stream>>>(job.nt, job.ib, in);
+  LPM_TRY(sort(in, out));
+  *tperm = out;
+  return LPM_OK;
 }
 
 int launch_pse_rel(const SumJob& job, const SumPlan& plan, int64_t npad) {
@@ -644,7 +684,12 @@ int launch_pse_rel(const SumJob& job, const SumPlan& plan, int64_t npad) {
                        job.sort_bytes, job.sorted));
     src_list = job.sorted;
   }
+  const int32_t* tperm = nullptr;
+  LPM_TRY(sorted_targets(job, plan, [&](const int32_t* in, int32_t* out) {
+    return curve_sort(job.stream, job.nt, in, job.x, job.y, job.z, inv_a, job.sort_scratch, job.sort_bytes, out);
+  }, &tperm));
   PseRelArgs a;
+  a.tperm = tperm;
   a.x = job.x;
   a.y = job.y;
   a.z = job.z;
@@ -695,7 +740,12 @@ int launch_plane_pse_rel(const SumJob& job, const SumPlan& plan, int64_t npad) {
                          job.sorted));
     src_list = job.sorted;
   }
+  const int32_t* tperm = nullptr;
+  LPM_TRY(sorted_targets(job, plan, [&](const int32_t* in, int32_t* out) {
+    return curve_sort2d(job.stream, job.nt, in, job.x, job.y, job.sort_scratch, job.sort_bytes, out);
+  }, &tperm));
   PlanePseRelArgs a;
+  a.tperm = tperm;
   a.x = job.x;
   a.y = job.y;
   a.f = job.s1;
@@ -1462,7 +1512,7 @@ int run_host(const HostArgs& a, int nout) {
     LPM_TRY(workspace(ctx, kWsSources, plan.src_bytes, &job.src_buf));
     if (sum_uses_sorted_sources(a.kind, prec)) {
       void* ps = nullptr;
-      const size_t sb = sort_scratch_bytes(a.kind, ns);
+      const size_t sb = sort_scratch_bytes(a.kind, ns, nt);
       const size_t sorted_off = align_up(sb, 256);
       LPM_TRY(workspace(ctx, kWsScan, sorted_off + static_cast<size_t>(ns) * sizeof(int32_t), &ps));
       job.sort_scratch = ps;

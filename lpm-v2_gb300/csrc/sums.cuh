@@ -21,6 +21,9 @@ struct SumPlan {
   // split, its source records at src_buf + aux_src_offset; it reuses the partials
   int64_t aux_n_tiles = 0, aux_tiles_per_chunk = 0, aux_nsplit = 0;
   size_t aux_src_offset = 0;
+  // FP32C PSE sums: the targets' curve order (two lists of nt int32: [ib, ib + nt) and its
+  // sorted permutation) at src_buf + tperm_offset; 0 when the sweep takes targets in order
+  size_t tperm_offset = 0;
 };
 
 enum SumKind : int {
@@ -114,6 +117,6 @@ int launch_sum(const SumJob& job, const SumPlan& plan);
 // Whether the FP32C form of `kind` runs on curve-sorted, group-relative sources, and the
 // scratch bytes of that sort for ns sources.
 bool sum_uses_sorted_sources(int kind, int mode);
-size_t sort_scratch_bytes(int kind, int64_t ns);
+size_t sort_scratch_bytes(int kind, int64_t ns, int64_t nt);
 
 }  // namespace lpm

@@ -102,6 +102,7 @@ _SIGNATURES = {
     "lpm_ensemble_velocity": [_vp],
     "lpm_ensemble_get_state": [_vp, _D, _D, _D, _D, _D, _D, _D],
     "lpm_ensemble_kernel_timing": [_vp, _D, _L],
+    "lpm_ensemble_sweep_shape": [_vp, _I, _I, _I, _I],
     "lpm_ensemble_destroy": [_vp],
     "lpm_mesh_create": [_pvp, _int, _int, _dbl],
     "lpm_mesh_destroy": [_vp],
@@ -598,6 +599,12 @@ class Ensemble:
         ms, n = _dbl(), _i64()
         _check(lib().lpm_ensemble_kernel_timing(self._h, ctypes.byref(ms), ctypes.byref(n)))
         return ms.value, n.value
+
+    def sweep_shape(self):
+        """(threads, targets per thread, CTAs per SM, items per CTA slot) the tuner chose."""
+        v = [ctypes.c_int32() for _ in range(4)]
+        _check(lib().lpm_ensemble_sweep_shape(self._h, *(ctypes.byref(q) for q in v)))
+        return tuple(q.value for q in v)
 
     def close(self):
         if getattr(self, "_h", None):

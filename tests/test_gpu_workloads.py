@@ -1,25 +1,24 @@
-"""GPU parity at the benchmark configurations themselves, against the oracle.
+"""GPU parity at the benchmark workloads themselves, against the oracle.
 
-The other GPU tests pin each sum on small and ragged inputs.  These run the configurations
-the benchmarks are quoted on, at their own sizes (or, where the FP64 oracle would take
-minutes, on bounded target blocks of the full-size problem):
+The other GPU tests pin each sum on small and ragged inputs.  These run the workloads the
+benchmarks are quoted on, at their own sizes (or, where the FP64 oracle would take minutes,
+on bounded target blocks of the full-size problem):
 
-  config 1  sphere BVE single Gaussian vortex, icos nest 4 (7,682 targets, 5,120 sources),
-            100 RK4 steps of dt = 0.01 in FP64: bit-identical to the oracle's timestepPrivate
-            (src/SphereBVESolver.f90:219-353; examples/BVESingleGaussianVortex.f90:216-270 with
-            remesh off).
-  config 2  planar colliding dipoles, quad nest 7 on [-4,4]^2 (131,585 targets, 65,536
-            sources), delta = 0 and 0.02: FP64 bit-identical and FP32C within 1e-6 on target
-            blocks against planarIncompressibleVelocity (src/PlaneIncompressibleSolver.f90:
-            278-316); 200 RK4 steps of dt = 0.005 (at quad nest 5, where the FP64 oracle
-            finishes in seconds) FP64 bit-identical to the oracle, with the FP32C solver
-            tracking the FP64 one.
-  config 4  sphere BVE at icos nest 8 (1,966,082 targets, 1,310,720 sources), RH4 + Gaussian
-            vortex: the FP32C sum on target blocks against the oracle, before and after one
-            RK4 step of the renormalising solver the benchmark times.
-  config 5  the 64-instance ensemble at icos nests 3-6: every instance's FP32C velocity on a
-            target block against the oracle, before and after two RK4 steps; and one
-            instance per nest 3-6 advanced one FP64 step, bit-identical to the oracle.
+  single Gaussian vortex on the sphere, icos nest 4 (7,682 targets, 5,120 sources): 100 RK4
+      steps of dt = 0.01 in FP64, bit-identical to the oracle's timestepPrivate
+      (src/SphereBVESolver.f90:219-353; examples/BVESingleGaussianVortex.f90:216-270 with
+      remesh off).
+  planar colliding dipoles, quad nest 7 on [-4,4]^2 (131,585 targets, 65,536 sources),
+      delta = 0 and 0.02: FP64 bit-identical and FP32C within 1e-6 on target blocks against
+      planarIncompressibleVelocity (src/PlaneIncompressibleSolver.f90:278-316); 200 RK4 steps
+      of dt = 0.005 (at quad nest 5, where the FP64 oracle finishes in seconds) FP64
+      bit-identical to the oracle, with the FP32C solver tracking the FP64 one.
+  Rossby-Haurwitz wave 4 + Gaussian vortex at icos nest 8 (1,966,082 targets, 1,310,720
+      sources): the FP32C sum on target blocks against the oracle, before and after one RK4
+      step of the renormalising solver the headline benchmark times.
+  the 64-instance ensemble at icos nests 3-6: every instance's FP32C velocity on a target
+      block against the oracle, before and after two RK4 steps; and one instance per nest
+      3-6 advanced one FP64 step, bit-identical to the oracle.
 """
 import numpy as np
 import pytest
@@ -45,8 +44,8 @@ def _rel_linf(got, ref):
     return float(np.abs(got - ref).max() / np.abs(ref).max())
 
 
-# ------------------------------------------------------------------ config 1
-def test_config1_icos4_100_steps_fp64_bit_exact(lg, wl, oracle_mod):
+# ------------------------------------------------------------------ Gaussian vortex, icos nest 4
+def test_gauss_vortex_icos4_100_steps_fp64_bit_exact(lg, wl, oracle_mod):
     c = wl.config_gauss_vortex_icos(4)
     assert c["x"].size == 7682 and int(c["active"].sum()) == 5120
     a = (c["x"], c["y"], c["z"], c["zeta"], c["area"], c["active"])
@@ -60,7 +59,7 @@ def test_config1_icos4_100_steps_fp64_bit_exact(lg, wl, oracle_mod):
         assert np.array_equal(st[k], r), k
 
 
-# ------------------------------------------------------------------ config 2
+# ------------------------------------------------------------------ colliding dipoles
 @pytest.fixture(scope="module")
 def dipoles7(wl):
     c = wl.config_colliding_dipoles(7)
@@ -69,9 +68,9 @@ def dipoles7(wl):
 
 
 @pytest.mark.parametrize("delta", [0.0, 0.02])
-def test_config2_quad7_velocity_blocks(lg, oracle_mod, dipoles7, delta):
+def test_dipoles_quad7_velocity_blocks(lg, oracle_mod, dipoles7, delta):
     """FP64 bit-identical to the oracle on three target blocks; FP32C within 1e-6 of the
-    largest velocity of the whole set (the relative L-infinity error the benchmark spec bounds).
+    largest velocity of the whole set (the relative L-infinity error of the velocity).
     Normalised by each block's own largest velocity instead, the block in the slow corner of
     the domain, where the two dipoles' fields cancel, would read 1.3e-6 at delta = 0."""
     c = dipoles7
@@ -80,6 +79,7 @@ def test_config2_quad7_velocity_blocks(lg, oracle_mod, dipoles7, delta):
     full32 = np.stack(lg.planar_incompressible_velocity(*a, delta, mode="fp32c"))
     full64 = np.stack(lg.planar_incompressible_velocity(*a, delta, mode="fp64"))
     umax = np.abs(full64).max()
+    print(f"quad nest 7, delta {delta}: FP32C relative Linf error {np.abs(full32 - full64).max() / umax:.3e}")
     for ib in (1, n // 2 - 2047, n - 4095):
         ie = ib + 4095
         ref = np.stack(oracle_mod.plane_velocity(*a, delta, ib=ib - 1, ie=ie))
@@ -91,7 +91,7 @@ def test_config2_quad7_velocity_blocks(lg, oracle_mod, dipoles7, delta):
     assert np.abs(full32 - full64).max() / umax <= FP32C_TOL
 
 
-def test_config2_200_steps_fp64_bit_exact_and_fp32c_track(lg, wl, oracle_mod):
+def test_dipoles_quad5_200_steps_fp64_bit_exact_and_fp32c_track(lg, wl, oracle_mod):
     """200 RK4 steps of dt = 0.005 with delta = 0.02 (quad nest 5): the FP64 solver is
     bit-identical to the oracle's timestepPrivate (src/PlaneIncompressibleSolver.f90:171-259),
     and the FP32C solver tracks it.  Over the first 20 steps (t = 0.1) the positions agree
@@ -125,7 +125,7 @@ def test_config2_200_steps_fp64_bit_exact_and_fp32c_track(lg, wl, oracle_mod):
     assert d32["circulation"] == d64["circulation"]  # omega is carried unchanged
 
 
-# ------------------------------------------------------------------ config 4
+# ------------------------------------------------------------------ RH4 + vortex, icos nest 8
 @pytest.fixture(scope="module")
 def rh54_icos8(wl):
     c = wl.config_rh54_icos(8, seed=0)
@@ -137,7 +137,7 @@ def _blocks(n, m=4096):
     return [(n // 4, n // 4 + m - 1), (3 * n // 4, 3 * n // 4 + m - 1)]
 
 
-def test_config4_icos8_fp32c_blocks_vs_oracle(lg, oracle_mod, rh54_icos8):
+def test_rh4_icos8_fp32c_blocks_vs_oracle(lg, oracle_mod, rh54_icos8):
     c = rh54_icos8
     a = (c["x"], c["y"], c["z"], c["zeta"], c["area"], c["active"])
     got = lg.bve_sphere_velocity(*a, 1.0, mode="fp32c")
@@ -146,7 +146,7 @@ def test_config4_icos8_fp32c_blocks_vs_oracle(lg, oracle_mod, rh54_icos8):
         assert _rel_linf([q[ib - 1:ie] for q in got], ref) <= FP32C_TOL
 
 
-def test_config4_icos8_rk4_step_vs_oracle(lg, oracle_mod, rh54_icos8):
+def test_rh4_icos8_rk4_step_vs_oracle(lg, oracle_mod, rh54_icos8):
     """One RK4 step of the renormalising FP32C solver (the benchmark's step): the velocity it
     leaves at the new positions, on target blocks, against the oracle at that state."""
     c = rh54_icos8
@@ -160,7 +160,7 @@ def test_config4_icos8_rk4_step_vs_oracle(lg, oracle_mod, rh54_icos8):
         assert _rel_linf([st[k][ib - 1:ie] for k in ("u", "v", "w")], ref) <= FP32C_TOL
 
 
-# ------------------------------------------------------------------ config 5
+# ------------------------------------------------------------------ ensemble of 64, nests 3-6
 def _check_instances_vs_oracle(oracle_mod, inst, st, offs, m=512):
     worst = 0.0
     for k, d in enumerate(inst):
@@ -177,7 +177,7 @@ def _check_instances_vs_oracle(oracle_mod, inst, st, offs, m=512):
     return worst
 
 
-def test_config5_ensemble_64_fp32c_vs_oracle(lg, wl, oracle_mod):
+def test_ensemble_64_nests3to6_fp32c_vs_oracle(lg, wl, oracle_mod):
     inst = wl.config_ensemble(n_instances=64, seed=0)
     assert sorted({d["nest"] for d in inst}) == [3, 4, 5, 6]
     ens = lg.Ensemble(inst, mode="fp32c")
@@ -187,7 +187,7 @@ def test_config5_ensemble_64_fp32c_vs_oracle(lg, wl, oracle_mod):
     ens.close()
 
 
-def test_config5_ensemble_one_per_nest_fp64_step_bit_exact(lg, wl, oracle_mod):
+def test_ensemble_one_per_nest_fp64_step_bit_exact(lg, wl, oracle_mod):
     inst = []
     for nest in (3, 4, 5, 6):
         inst += [d for d in wl.config_ensemble(n_instances=1, seed=nest, nests=(nest,))]
