@@ -88,6 +88,8 @@ def parse_args():
     p.add_argument("--no-fp64", action="store_true", help="skip the FP64 parity-mode rate at the headline size")
     p.add_argument("--no-ensemble", action="store_true", help="skip the 64-instance ensemble object")
     p.add_argument("--ensemble-steps", type=int, default=10, help="RK4 steps of the ensemble object")
+    p.add_argument("--no-size-classes", action="store_true",
+                   help="--workload ensemble: skip the per-refinement-level measurements")
     p.add_argument("--workload", choices=["rk4", "ensemble", "stream", "configs", "sum", "remesh"], default="rk4",
                    help="rk4: the headline single-instance step; ensemble: the 64-instance batch")
     p.add_argument("--instances", type=int, default=64)
@@ -505,7 +507,7 @@ def run_ensemble(args):
     r = measure_ensemble(torch, lg, wl, args.instances, steps, args.warmup, args.dt, inst=inst)
     clocks = sampler.stop()
     classes = {}
-    for nest in sorted({d["nest"] for d in inst}):
+    for nest in ([] if args.no_size_classes else sorted({d["nest"] for d in inst})):
         sub = [d for d in inst if d["nest"] == nest]
         q = measure_ensemble(torch, lg, wl, len(sub), max(2, steps // 5), args.warmup, args.dt, inst=sub, check=2)
         classes[str(nest)] = {"instances": len(sub), "batched": q["value"], "sequential": q["sequential"]["value"],

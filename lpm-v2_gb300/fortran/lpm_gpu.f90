@@ -33,6 +33,7 @@ public :: lpm_plane_solver_create, lpm_plane_timestep, lpm_plane_get_state, lpm_
 public :: lpm_plane_solver_destroy
 public :: lpm_ensemble_create, lpm_ensemble_timestep, lpm_ensemble_velocity, lpm_ensemble_get_state
 public :: lpm_ensemble_destroy, lpm_bve_kernel_timing, lpm_bve_solver_set_timing, lpm_version
+public :: lpm_ensemble_sweep_shape, lpm_release_workspace
 
 integer(c_int), parameter :: LPM_MODE_FP64 = 0
 integer(c_int), parameter :: LPM_MODE_FP32C = 1
@@ -413,6 +414,18 @@ interface
 	integer(c_int) function lpm_ensemble_destroy(ens) bind(C, name="lpm_ensemble_destroy")
 		import :: c_int, c_ptr
 		type(c_ptr), value :: ens
+	end function
+
+	integer(c_int) function lpm_ensemble_sweep_shape(ens, threads, targetsPerThread, ctasPerSM, itemsPerSlot) &
+			bind(C, name="lpm_ensemble_sweep_shape")
+		import :: c_int, c_ptr
+		type(c_ptr), value :: ens
+		integer(c_int), intent(out) :: threads, targetsPerThread, ctasPerSM, itemsPerSlot
+	end function
+
+	! ---- workspace
+	integer(c_int) function lpm_release_workspace() bind(C, name="lpm_release_workspace")
+		import :: c_int
 	end function
 
 	! ---- timing and version
