@@ -326,6 +326,11 @@ int lpm_ensemble_kernel_timing(lpm_ensemble* ens, double* total_ms, int64_t* lau
  * per resident CTA the source ranges were cut for.  Any pointer may be NULL. */
 int lpm_ensemble_sweep_shape(lpm_ensemble* ens, int* threads, int* targets_per_thread,
                              int* ctas_per_sm, int* items_per_slot);
+/* Replaces the autotuner's choice with a given one (LPM_MODE_FP32C): threads x
+ * targets_per_thread must be 128 x 4 or 128 x 8, items_per_slot 4, 8 or 16; anything else
+ * fails with LPM_ERR_ARG.  For reproducible timings, or to test every shape. */
+int lpm_ensemble_select_sweep(lpm_ensemble* ens, int threads, int targets_per_thread,
+                              int items_per_slot);
 int lpm_ensemble_destroy(lpm_ensemble* ens);
 
 /* ------------------------------------------------------------------ allocation-free call */

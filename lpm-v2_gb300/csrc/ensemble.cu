@@ -728,6 +728,26 @@ extern "C" int lpm_ensemble_sweep_shape(lpm_ensemble* E, int* threads, int* targ
   return LPM_OK;
 }
 
+extern "C" int lpm_ensemble_select_sweep(lpm_ensemble* E, int threads, int targets_per_thread, int items_per_slot) {
+  if (!E) return set_error(LPM_ERR_ARG, "null ensemble");
+  if (E->mode != LPM_MODE_FP32C) return set_error(LPM_ERR_STATE, "the FP64 ensemble has no sweep shape to select");
+  for (int ch = 0; ch < kQueueChoiceCount; ++ch) {
+    const EnsShape& sh = kEnsShapes[kQueueChoices[ch].shape];
+    if (sh.threads == threads && sh.tpt == targets_per_thread && kQueueChoices[ch].per_slot == items_per_slot) {
+      LPM_CUDA_TRY(cudaStreamSynchronize(E->stream));
+      LPM_TRY(E->use_queue(ch));
+      // the captured step graph holds the previous shape's kernel and grid: capture again
+      if (E->exec) cudaGraphExecDestroy(E->exec);
+      if (E->graph) cudaGraphDestroy(E->graph);
+      E->exec = nullptr;
+      E->graph = nullptr;
+      return E->check_status("lpm_ensemble_select_sweep");
+    }
+  }
+  return set_error(LPM_ERR_ARG, "no sweep shape %d threads x %d targets with %d items per CTA slot", threads,
+                   targets_per_thread, items_per_slot);
+}
+
 extern "C" int lpm_ensemble_destroy(lpm_ensemble* E) {
   if (!E) return LPM_OK;
   E->destroy();

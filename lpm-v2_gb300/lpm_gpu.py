@@ -103,6 +103,7 @@ _SIGNATURES = {
     "lpm_ensemble_get_state": [_vp, _D, _D, _D, _D, _D, _D, _D],
     "lpm_ensemble_kernel_timing": [_vp, _D, _L],
     "lpm_ensemble_sweep_shape": [_vp, _I, _I, _I, _I],
+    "lpm_ensemble_select_sweep": [_vp, _int, _int, _int],
     "lpm_ensemble_destroy": [_vp],
     "lpm_mesh_create": [_pvp, _int, _int, _dbl],
     "lpm_mesh_destroy": [_vp],
@@ -605,6 +606,10 @@ class Ensemble:
         v = [ctypes.c_int32() for _ in range(4)]
         _check(lib().lpm_ensemble_sweep_shape(self._h, *(ctypes.byref(q) for q in v)))
         return tuple(q.value for q in v)
+
+    def select_sweep(self, threads, targets_per_thread, items_per_slot):
+        """Replaces the autotuner's choice of the persistent sweep's configuration."""
+        _check(lib().lpm_ensemble_select_sweep(self._h, int(threads), int(targets_per_thread), int(items_per_slot)))
 
     def close(self):
         if getattr(self, "_h", None):

@@ -120,3 +120,27 @@ def test_ensemble_mixed_radii_and_rotation(lg, wl):
         assert np.abs(u32 - u64).max() <= 1e-6 * np.abs(u64).max()
     e64.close()
     e32.close()
+
+
+@pytest.mark.parametrize("tpt", [4, 8])
+@pytest.mark.parametrize("per_slot", [4, 8, 16])
+def test_ensemble_every_sweep_shape(lg, instances, tpt, per_slot):
+    """Each of the persistent sweep's six configurations (the autotuner's choices), selected
+    by hand: the velocity of every instance within 1e-6 of its FP64 sum, before and after two
+    RK4 steps (the step graph is captured again for the selected shape)."""
+    ens = lg.Ensemble(instances, mode="fp32c")
+    ens.select_sweep(128, tpt, per_slot)
+    assert ens.sweep_shape() == (128, tpt, 4 if tpt == 4 else 2, per_slot)
+    ens.velocity()
+    for steps in (0, 2):
+        if steps:
+            ens.timestep(0.01, steps)
+        parts = _split(ens.get_state(), ens.sizes)
+        for d, got in zip(instances, parts):
+            ref = lg.bve_sphere_velocity(got["x"], got["y"], got["z"], got["rel_vort"], d["area"], d["active"],
+                                         d["radius"], mode="fp64")
+            err = np.abs(np.stack([got["u"], got["v"], got["w"]]) - np.stack(ref)).max() / np.abs(np.stack(ref)).max()
+            assert err <= 1e-6
+    with pytest.raises(lg.LpmError):
+        ens.select_sweep(256, 4, 8)
+    ens.close()
