@@ -374,10 +374,11 @@ int lpm_release_workspace(void);
  * LPM_ERR_ALLOC; k = 0 disarms.  Every handle or workspace allocated before the failure is
  * released or kept consistent, so the next call succeeds.
  *
- * lpm_debug_inject_wait_timeout(skip_tile, budget_ns): the next host-buffer sphere-BVE
- * LPM_MODE_FP32C sum (lpm_bve_velocity or lpm_bve_set_velocity_from_vorticity) does not issue
- * the copy of source tile `skip_tile` and bounds its waits by budget_ns (0 < budget_ns <= 1e9)
- * instead of 1 s.  The waits for that tile run out, the call returns LPM_ERR_TIMEOUT with the
+ * lpm_debug_inject_wait_timeout(skip_tile, budget_ns): the next host-buffer LPM_MODE_FP32C
+ * sphere-BVE sum (lpm_bve_velocity, lpm_bve_set_velocity_from_vorticity; block-synchronous
+ * tile pipeline) or sphere PSE sum (lpm_pse_sphere_laplacian, _gradient, _divergence;
+ * warp-decoupled pipeline) does not issue the copy of source tile `skip_tile` and bounds its
+ * waits by budget_ns (0 < budget_ns <= 1e9) instead of 1 s.  The waits for that tile run out, the call returns LPM_ERR_TIMEOUT with the
  * caller's outputs untouched, and the context stays usable.  Nothing faults: no copy is in
  * flight for the skipped tile.  One-shot. */
 int lpm_debug_fail_device_alloc(int64_t k);

@@ -66,6 +66,7 @@ struct PseRelArgs {
   const int32_t* tperm;
   double* partial;  // [chunk][comps][nt]
   int* status;
+  WaitCfg wait;  // limits of the bounded waits (the test hook may shorten them and skip a tile)
 };
 
 template <int OP>
@@ -211,7 +212,7 @@ __global__ void __launch_bounds__(THREADS, MINB) pse_rel_sweep_kernel(PseRelArgs
 
   tile_pipe_init(pipe);
   uint32_t g = 0;
-  warp_sweep(a.src, tile0, ntl, pipe, g, a.status, default_wait(), a.org,
+  warp_sweep(a.src, tile0, ntl, pipe, g, a.status, a.wait, a.org,
              [&](const Rec* tl, const BveRel::Origin* og) {
     float2 acc[NP][NC];
 #pragma unroll

@@ -710,6 +710,7 @@ int launch_pse_rel(const SumJob& job, const SumPlan& plan, int64_t npad) {
   a.nt = job.nt;
   a.partial = job.partial;
   a.status = job.status;
+  a.wait = job.wait;
   const bool series = job.eps <= 0.06 * job.radius;  // the asin^2 series angle (pse_rel.cuh)
   switch (job.kind) {
     case kSumPseK8Geo:
@@ -1529,7 +1530,10 @@ int run_host(const HostArgs& a, int nout) {
     int shape = 0;
     LPM_TRY(autotune_bve_shape(job, ctx->sm_count, &shape));
     plan = plan_sum(a.kind, prec, ns, nt, ctx->sm_count, shape);
-    if (prec == LPM_MODE_FP32C && (a.kind == kSumBve || a.kind == kSumBveMesh)) job.wait = take_injected_wait();
+    if (prec == LPM_MODE_FP32C && (a.kind == kSumBve || a.kind == kSumBveMesh || a.kind == kSumPseK8Geo ||
+                                   (a.kind == kSumPseGaussChord && job.z) || a.kind == kSumPseGrad ||
+                                   a.kind == kSumPseDiv))
+      job.wait = take_injected_wait();
     LPM_TRY(launch_sum(job, plan));
   }
   // the caller's outputs are written only when every bounded wait of the sum succeeded

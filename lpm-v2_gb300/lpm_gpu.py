@@ -634,8 +634,8 @@ def debug_fail_device_alloc(k: int) -> None:
 
 
 def debug_inject_wait_timeout(skip_tile: int, budget_ns: int) -> None:
-    """Test hook: the next host-buffer sphere-BVE FP32C sum skips the copy of one source tile
-    and bounds its waits by budget_ns, so it returns LPM_ERR_TIMEOUT (one-shot)."""
+    """Test hook: the next host-buffer sphere-BVE or sphere PSE FP32C sum skips the copy of one
+    source tile and bounds its waits by budget_ns, so it returns LPM_ERR_TIMEOUT (one-shot)."""
     _check(lib().lpm_debug_inject_wait_timeout(int(skip_tile), int(budget_ns)))
 
 

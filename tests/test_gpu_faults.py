@@ -5,7 +5,8 @@ src/Logger.f90:159), which the Fortran shim calls on any non-zero status.  These
 the library's two kinds of failure happen without faulting, trapping or hanging a GPU:
 
 * A bounded device wait that runs out: lpm_debug_inject_wait_timeout makes the next
-  host-buffer sphere-BVE FP32C sum skip the copy of one source tile and bounds its waits by
+  host-buffer sphere-BVE or sphere PSE FP32C sum (the block-synchronous and the
+  warp-decoupled tile pipelines) skip the copy of one source tile and bounds its waits by
   1 ms.  The waits for that tile give up, the call returns LPM_ERR_TIMEOUT with the caller's
   outputs untouched, and the next call on the same context is correct.  No copy is ever in
   flight for the skipped tile, so nothing is left to land after the CTA has gone.
@@ -67,6 +68,31 @@ def test_bounded_wait_runs_out_and_context_survives(lg, wl, oracle_mod):
     got64 = lg.bve_sphere_velocity(*a, 1.0, mode="fp64")
     for g, r in zip(got64, ref):
         assert np.array_equal(g, r)
+
+
+@pytest.mark.parametrize("skip_tile", [0, 3])
+def test_bounded_wait_runs_out_warp_decoupled_pipeline(lg, wl, oracle_mod, skip_tile):
+    """The same on the warp-decoupled pipeline of the PSE sweeps: every warp of the CTAs that
+    own the skipped tile gives up on it, thread 0's bounded waits for the stages end, the copies
+    of the other stages are waited for, and the call returns LPM_ERR_TIMEOUT with the output
+    untouched; the next call is within the PSE FP32C bound of the oracle."""
+    c = wl.config_pse_cubed(4)
+    a = (c["x"], c["y"], c["z"], c["f"], c["area"], c["active"])
+    ref = oracle_mod.pse_laplacian(*a, c["eps_k8"], 1.0, oracle_mod.PSE_K8_GEODESIC)
+    lg.pse_sphere_laplacian_at_particles(*a, c["eps_k8"], 1.0, lg.PSE_K8_GEODESIC, mode="fp32c")
+    n = c["x"].size
+    x, y, z, f, area = (np.ascontiguousarray(q, dtype=np.float64) for q in a[:5])
+    act = np.ascontiguousarray(c["active"], dtype=np.int32)
+    out = np.full(n, 7.0)
+    P = ctypes.POINTER(ctypes.c_double)
+    lg.debug_inject_wait_timeout(skip_tile, 1_000_000)
+    rc = lg.lib().lpm_pse_sphere_laplacian(n, *(q.ctypes.data_as(P) for q in (x, y, z, f, area)),
+                                           act.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), c["eps_k8"], 1.0,
+                                           lg.PSE_K8_GEODESIC, 1, n, out.ctypes.data_as(P), LPM_MODE_FP32C)
+    assert rc == LPM_ERR_TIMEOUT, lg.lib().lpm_last_error_string().decode()
+    assert np.all(out == 7.0)
+    got = lg.pse_sphere_laplacian_at_particles(*a, c["eps_k8"], 1.0, lg.PSE_K8_GEODESIC, mode="fp32c")
+    assert np.abs(got - ref).max() <= 1e-4 * np.abs(ref).max()
 
 
 def test_inject_wait_timeout_rejects_bad_arguments(lg):
