@@ -137,6 +137,7 @@ extern "C" int lpm_release_workspace(void) {
     b.ptr = nullptr;
     b.bytes = 0;
   }
+  std::vector<int32_t>().swap(ctx->h_idx);
   return LPM_OK;
 }
 

@@ -56,6 +56,7 @@ struct Context {
   int* d_status = nullptr;     // device status word (kDev*)
   int* h_status = nullptr;     // pinned mirror
   std::vector<DevBuf> bufs;    // workspace slots, indexed by WorkSlot
+  std::vector<int32_t> h_idx;  // host buffer of the active list of a host-buffer call
   std::mutex mu;               // one direct-sum call at a time per process
 };
 

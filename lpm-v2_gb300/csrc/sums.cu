@@ -130,10 +130,10 @@ __global__ void __launch_bounds__(k64Threads) seq_fp64_kernel(P p, const Rec* __
 // one term to each accumulator component (a = a + X, or a = a - X, which is a + (-X)), so the
 // sums stay bit-identical up to the sign of an exact zero.  S times as many warps share the
 // FP64 work.
-template <class Op, class Rec, class P, int S>
-__global__ void __launch_bounds__(k64Threads) seq_fp64_split_kernel(P p, const Rec* __restrict__ src,
-                                                                    int64_t ns, int64_t ib, int64_t nt,
-                                                                    int* status) {
+template <class Op, class Rec, class P, int S, int THREADS>
+__global__ void __launch_bounds__(THREADS) seq_fp64_split_kernel(P p, const Rec* __restrict__ src,
+                                                                 int64_t ns, int64_t ib, int64_t nt,
+                                                                 int* status) {
   static_assert(32 % S == 0, "a target's lanes stay in one warp");
   using Acc = typename Op::Acc;
   static_assert(sizeof(Acc) % sizeof(double) == 0, "accumulators are doubles");
@@ -142,7 +142,7 @@ __global__ void __launch_bounds__(k64Threads) seq_fp64_split_kernel(P p, const R
   __shared__ __align__(8) uint64_t bars[2];
   const int k = static_cast<int>(threadIdx.x) % S;
   const int lane0 = static_cast<int>(threadIdx.x & 31u) - k;  // the group's first lane in the warp
-  const int64_t il = static_cast<int64_t>(blockIdx.x) * (k64Threads / S) + threadIdx.x / S;
+  const int64_t il = static_cast<int64_t>(blockIdx.x) * (THREADS / S) + threadIdx.x / S;
   const bool valid = il < nt;
   const int64_t i = ib + (valid ? il : nt - 1);
   const typename Op::Tgt t = Op::load(p, i);
@@ -174,6 +174,20 @@ __global__ void __launch_bounds__(k64Threads) seq_fp64_split_kernel(P p, const R
     ++tile;
   });
   if (valid && k == 0) Op::store(p, i, il, acc);
+}
+
+// The split sweep at a CTA size of 128, 64 or 32 threads.
+template <class Op, class Rec, class P>
+void launch_split64(int threads, unsigned grid, cudaStream_t stream, const P& p, const Rec* src, int64_t ns,
+                    int64_t ib, int64_t nt, int* status) {
+  if (threads == 32) {
+    seq_fp64_split_kernel<Op, Rec, P, kSplit64, 32><<<grid, 32, 0, stream>>>(p, src, ns, ib, nt, status);
+  } else if (threads == 64) {
+    seq_fp64_split_kernel<Op, Rec, P, kSplit64, 64><<<grid, 64, 0, stream>>>(p, src, ns, ib, nt, status);
+  } else {
+    seq_fp64_split_kernel<Op, Rec, P, kSplit64, k64Threads><<<grid, k64Threads, 0, stream>>>(p, src, ns, ib, nt,
+                                                                                             status);
+  }
 }
 
 // The bounding ball (centre, radius) of each FP64 source tile (k64Tile consecutive active
@@ -527,6 +541,25 @@ int targets_per_cta(int kind, int shape) {
 
 }  // namespace
 
+// CTA size of an FP64 sweep over `lanes` threads (one per target, or kSplit64 per target):
+// every CTA does the same work and all of them are resident at once, so an SM's time is its
+// CTA count times the CTA size, and the sweep takes the longest SM's.  Of 128, 64 and 32
+// threads, the size that minimises ceil(CTAs / SMs) x size (the larger on a tie): e.g. at
+// 7,682 targets x 4 lanes, 961 CTAs of 32 threads put at most 7 on an SM (224 thread-slots)
+// where 241 CTAs of 128 put 2 (256).
+static int fp64_block_threads(int64_t lanes, int64_t sms) {
+  int best = k64Threads;
+  int64_t best_cost = ceil_div(ceil_div(lanes, k64Threads), sms) * k64Threads;
+  for (int t : {64, 32}) {
+    const int64_t cost = ceil_div(ceil_div(lanes, t), sms) * t;
+    if (cost < best_cost) {
+      best_cost = cost;
+      best = t;
+    }
+  }
+  return best;
+}
+
 int64_t choose_split(int64_t blocks, int64_t tiles, int64_t slots, int64_t max_split) {
   if (blocks < 1) blocks = 1;
   if (slots < 1) slots = 1;
@@ -611,7 +644,9 @@ SumPlan plan_sum(int kind, int mode, int64_t ns, int64_t nt, int sm_count, int s
     // planar velocity, the split sweep) so that more SMs share the FP64 work.  At one CTA
     // per SM and above the sequential sweep keeps the FP64 pipe busy (85 % at icos nest 5).
     const int64_t sms = sm_count > 0 ? sm_count : 152;
-    pl.fp64_threads = ceil_div(nt, k64Threads) < sms ? 32 : k64Threads;
+    pl.fp64_small = ceil_div(nt, k64Threads) < sms;
+    pl.fp64_threads = fp64_block_threads(nt, sms);
+    pl.fp64_split_threads = fp64_block_threads(nt * kSplit64, sms);
     pl.nsplit = 1;
     pl.tiles_per_chunk = pl.n_tiles;
     pl.partial_bytes = 0;
@@ -785,9 +820,10 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
   const unsigned prep_grid_pad = static_cast<unsigned>(ceil_div(npad, pb));
 
   if (job.mode == LPM_MODE_FP64) {
-    const int t64 = plan.fp64_threads == 32 ? 32 : k64Threads;
+    const int t64 = plan.fp64_threads;
     const unsigned g = static_cast<unsigned>(ceil_div(job.nt, t64));
-    const unsigned gs = static_cast<unsigned>(ceil_div(job.nt, k64Threads / kSplit64));  // the split sweep's grid
+    const int ts = plan.fp64_split_threads;
+    const unsigned gs = static_cast<unsigned>(ceil_div(job.nt, ts / kSplit64));  // the split sweep's grid
     Fp64Cut cut;
     if (fp64_cutoff(job.kind, &cut.unit)) {
       TileBall* bounds = reinterpret_cast<TileBall*>(
@@ -810,14 +846,12 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
         BveF64Params p{job.x, job.y, job.z, job.radius * job.radius, (4.0 * kPi) * job.radius,
                        job.out0, job.out1, job.out2};
         const Rec64* src = static_cast<const Rec64*>(job.src_buf);
-        if (t64 == 32) {
+        if (plan.fp64_small) {
           // a small target set: kSplit64 lanes per target (the terms in parallel, the sum in order)
           if (job.kind == kSumBve) {
-            seq_fp64_split_kernel<BveF64<0>, Rec64, BveF64Params, kSplit64><<<gs, k64Threads, 0, job.stream>>>(
-                p, src, job.ns, job.ib, job.nt, job.status);
+            launch_split64<BveF64<0>, Rec64>(ts, gs, job.stream, p, src, job.ns, job.ib, job.nt, job.status);
           } else {
-            seq_fp64_split_kernel<BveF64<1>, Rec64, BveF64Params, kSplit64><<<gs, k64Threads, 0, job.stream>>>(
-                p, src, job.ns, job.ib, job.nt, job.status);
+            launch_split64<BveF64<1>, Rec64>(ts, gs, job.stream, p, src, job.ns, job.ib, job.nt, job.status);
           }
         } else if (job.kind == kSumBve) {
           seq_fp64_kernel<BveF64<0>, Rec64><<<g, t64, 0, job.stream>>>(p, src, job.ns, job.ib, job.nt, job.status);
@@ -831,9 +865,8 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
                                                                  job.ns, static_cast<RecPlane64*>(job.src_buf));
         PlaneF64Params p{job.x, job.y, 2.0 * kPi, job.delta * job.delta, job.out0, job.out1};
         const RecPlane64* src = static_cast<const RecPlane64*>(job.src_buf);
-        if (t64 == 32) {
-          seq_fp64_split_kernel<PlaneF64, RecPlane64, PlaneF64Params, kSplit64><<<gs, k64Threads, 0, job.stream>>>(
-              p, src, job.ns, job.ib, job.nt, job.status);
+        if (plan.fp64_small) {
+          launch_split64<PlaneF64, RecPlane64>(ts, gs, job.stream, p, src, job.ns, job.ib, job.nt, job.status);
         } else {
           seq_fp64_kernel<PlaneF64, RecPlane64><<<g, t64, 0, job.stream>>>(p, src, job.ns, job.ib, job.nt,
                                                                            job.status);
@@ -1445,11 +1478,15 @@ int run_host(const HostArgs& a, int nout) {
   const int64_t ib = a.i_begin - 1;
   const int64_t nt = a.i_end - a.i_begin + 1;
 
-  std::vector<int32_t> idx;
-  idx.reserve(static_cast<size_t>(n));
-  for (int64_t j = 0; j < n; ++j)
-    if (a.active[j]) idx.push_back(static_cast<int32_t>(j));
-  const int64_t ns = static_cast<int64_t>(idx.size());
+  // the active list, in a host buffer the context keeps between calls (no page faults on a
+  // fresh allocation per call), filled without a branch per particle
+  std::vector<int32_t>& idx = ctx->h_idx;
+  if (idx.size() < static_cast<size_t>(n)) idx.resize(static_cast<size_t>(n));
+  int64_t ns = 0;
+  for (int64_t j = 0; j < n; ++j) {
+    idx[static_cast<size_t>(ns)] = static_cast<int32_t>(j);
+    ns += a.active[j] != 0 ? 1 : 0;
+  }
 
   const bool has_z = a.z != nullptr;
   const bool has_s2 = a.s2 != nullptr;

@@ -16,7 +16,9 @@ struct SumPlan {
   size_t src_bytes = 0;      // bytes of the padded source-record array
   size_t partial_bytes = 0;  // bytes of the FP64 partial sums
   int shape = 0;             // sweep shape (sphere BVE FP32C; see bve_shape_count)
-  int fp64_threads = 128;    // FP64 sweep CTA size: 32 when there are fewer CTAs of 128 than SMs
+  int fp64_threads = 128;    // FP64 sequential sweep CTA size (32, 64 or 128: the best-balanced)
+  bool fp64_small = false;   // fewer 128-thread CTAs than SMs: the split sweep where there is one
+  int fp64_split_threads = 128;  // the split sweep's CTA size (32, 64 or 128)
   // a second sweep of the same job (the planar SWE surface-height Laplacian): its tiles and
   // split, its source records at src_buf + aux_src_offset; it reuses the partials
   int64_t aux_n_tiles = 0, aux_tiles_per_chunk = 0, aux_nsplit = 0;
