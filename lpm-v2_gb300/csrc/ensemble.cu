@@ -116,7 +116,7 @@ __global__ void __launch_bounds__(THREADS, MINB) ensemble_sweep_kernel(EnsArgs a
       float2 ax[NP], ay[NP], az[NP];
 #pragma unroll
       for (int p = 0; p < NP; ++p) ax[p] = ay[p] = az[p] = make_float2(0.f, 0.f);
-      bve_rel_tile<NP, kTile>(tl, a.org + tile * GPT, pr, ax, ay, az);
+      bve_rel_tile<NP, kTile, (NP >= 4 ? 4 : 2)>(tl, a.org + tile * GPT, pr, ax, ay, az);  // no spills at 128 x 4
       ++tile;
       bve_merge_pairs<NP>(ax, ay, az, hx, hy, hz, lx, ly, lz);
     });
