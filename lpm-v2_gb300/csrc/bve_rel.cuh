@@ -60,7 +60,9 @@ struct BveRel {
     float4 hi;  // o_hi.x, o_hi.y, o_hi.z, R (the group radius about o; -R for a compact group)
     float4 lo;  // o_lo.x, o_lo.y, o_lo.z, 1 if every c_j of the group is negligible
   };
-  static constexpr int kGroup = 64;           // sources per origin
+  // sources per origin: 128 measured 4.4 % faster than 64 for the BVE sweep (half the per-group
+  // work per source) at the same accuracy; the stream-function sweeps share the layout
+  static constexpr int kGroup = 128;
   static constexpr float kNearFactor = 3.0f;  // near: |t - o| < kNearFactor R
   static constexpr float kCompactRadius = 0.5f;  // compact: R <= kCompactRadius (unit sphere)
   static constexpr float kCompactRatio = 64.0f;  // and R <= kCompactRatio h
@@ -344,7 +346,7 @@ __global__ void __launch_bounds__(THREADS, MINB) bve_rel_sweep_kernel(SweepArgs<
   }
 }
 
-// The frame of the thread's group of kGroup sources within a tile of TILE (one CTA of TILE
+// The frame of the thread's group of G sources within a tile of TILE (one CTA of TILE
 // threads, every thread one source): the centroid o as hi/lo floats, the radius R about o,
 // whether the group is compact (R <= a/2 and R <= 64 x the smallest distance h between
 // consecutive sources) and whether every |c_j| <= 2^-30 h^2 (c_j negligible in q).  (px, py,
@@ -355,9 +357,8 @@ struct GroupFrame {
   bool compact, on_sphere;
 };
 
-template <int TILE>
+template <int TILE, int G>
 __device__ __forceinline__ GroupFrame sphere_group_frame(bool valid, double px, double py, double pz, double cj) {
-  constexpr int G = BveRel::kGroup;
   __shared__ double sp[3][TILE];
   __shared__ double red[3][TILE];
   __shared__ float fmax_[TILE], fmin_[TILE], cmax_[TILE], cntf[TILE];
@@ -459,7 +460,7 @@ __device__ __forceinline__ void bve_rel_prep_tile(const double* x, const double*
     pz = z[j] * inv_a;
     cj = fma(px, px, fma(py, py, fma(pz, pz, -1.0)));
   }
-  const GroupFrame f = sphere_group_frame<TILE>(valid, px, py, pz, cj);
+  const GroupFrame f = sphere_group_frame<TILE, BveRel::kGroup>(valid, px, py, pz, cj);
   BveRel::Rec r;
   if (valid) {
     float hi[3], lo[3];

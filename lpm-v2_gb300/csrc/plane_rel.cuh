@@ -38,7 +38,9 @@ struct PlaneRel {
   struct Pair {
     float2 xh, yh, xl, yl;
   };
-  static constexpr int kGroup = 64;
+  // sources per origin: 128 (the planar velocity, stream-function and SWE sweeps measured 0.2-2 %
+  // faster than with 64)
+  static constexpr int kGroup = 128;
   static constexpr float kNearFactor = 3.0f;  // near: |t - o| < kNearFactor R
 };
 
@@ -282,6 +284,7 @@ struct PlanePseRel {
     float4 c;  // -sx_lo, -sx_lo, -sy_lo, -sy_lo
     float4 d;  // f_lo, f_lo, 0, 0
   };
+  static constexpr int kGroup = 64;  // sources per origin: the group cutoff's granularity
 };
 
 struct PlanePseRelArgs {
@@ -320,7 +323,7 @@ template <bool K8, int THREADS, int TPT, int TILE, int MINB, int S>
 __global__ void __launch_bounds__(THREADS, MINB) plane_pse_rel_sweep_kernel(PlanePseRelArgs a) {
   static_assert(TPT % 2 == 0, "targets come in pairs");
   constexpr int NP = TPT / 2;
-  constexpr int G = PlaneRel::kGroup;
+  constexpr int G = PlanePseRel::kGroup;
   constexpr int GPT = TILE / G;
   using Rec = PlanePseRel::Rec;
   __shared__ TilePipe<Rec, TILE, S, PlaneRel::Origin, GPT> pipe;
@@ -438,7 +441,7 @@ __global__ void __launch_bounds__(TILE) plane_pse_rel_prep_kernel(const double* 
                                                                   const double* area, const int32_t* sorted,
                                                                   int64_t ns, PlanePseRel::Rec* out,
                                                                   PlaneRel::Origin* org) {
-  constexpr int G = PlaneRel::kGroup;
+  constexpr int G = PlanePseRel::kGroup;
   __shared__ double red[2][TILE];
   __shared__ float fmax_[TILE], cntf[TILE];
   const int64_t t = blockIdx.x;

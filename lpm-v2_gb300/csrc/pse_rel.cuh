@@ -50,6 +50,8 @@ struct PseRel {
     float2 xh, yh, zh, xl, yl, zl, e0, e1, e2;
   };
   static constexpr float kCutR2 = 100.0f;  // r^2 beyond which a pair is negligible
+  // sources per origin: the group cutoff's granularity (larger groups reach farther)
+  static constexpr int kGroup = 64;
 };
 
 struct PseRelArgs {
@@ -153,7 +155,7 @@ __global__ void __launch_bounds__(THREADS, MINB) pse_rel_sweep_kernel(PseRelArgs
   static_assert(TPT % 2 == 0, "targets come in pairs");
   constexpr int NP = TPT / 2;
   constexpr int NC = PseRelComps<OP>::value;
-  constexpr int G = BveRel::kGroup;
+  constexpr int G = PseRel::kGroup;
   constexpr int GPT = TILE / G;
   using Rec = PseRel::Rec;
   __shared__ TilePipe<Rec, TILE, S, BveRel::Origin, GPT> pipe;
@@ -306,7 +308,7 @@ __global__ void __launch_bounds__(TILE) pse_rel_prep_kernel(const double* x, con
   const int32_t j = valid ? sorted[k] : 0;
   double px = 0.0, py = 0.0, pz = 0.0;
   if (valid) pse_position<ANG>(x, y, z, j, inv_a, px, py, pz);
-  const GroupFrame fr = sphere_group_frame<TILE>(valid, px, py, pz, 0.0);
+  const GroupFrame fr = sphere_group_frame<TILE, PseRel::kGroup>(valid, px, py, pz, 0.0);
   PseRel::Rec r;
   if (valid) {
     float hi[3], lo[3];
@@ -329,10 +331,10 @@ __global__ void __launch_bounds__(TILE) pse_rel_prep_kernel(const double* x, con
     r.a = r.b = r.c = r.d = r.e = make_float4(0.f, 0.f, 0.f, 0.f);  // zero area: no contribution
   }
   out[k] = r;
-  if (threadIdx.x % BveRel::kGroup == 0) {
+  if (threadIdx.x % PseRel::kGroup == 0) {
     BveRel::Origin o = group_origin(fr);
     o.lo.w = fr.radius;  // the cutoff test needs the radius of every group
-    org[t * (TILE / BveRel::kGroup) + threadIdx.x / BveRel::kGroup] = o;
+    org[t * (TILE / PseRel::kGroup) + threadIdx.x / PseRel::kGroup] = o;
   }
 }
 

@@ -276,7 +276,7 @@ __global__ void __launch_bounds__(TILE) stream_rel_prep_kernel(const double* x, 
     pz = z[j] * inv_a;
     cj = fma(px, px, fma(py, py, fma(pz, pz, -1.0)));
   }
-  const GroupFrame f = sphere_group_frame<TILE>(valid, px, py, pz, cj);
+  const GroupFrame f = sphere_group_frame<TILE, BveRel::kGroup>(valid, px, py, pz, cj);
   StreamRel::Rec r;
   if (valid) {
     float hi[3], lo[3];

@@ -462,6 +462,33 @@ int tile_of(int kind, int mode) {
   }
 }
 
+// Sources per group origin of a group-relative FP32C layout: 128 for the sphere BVE sweep and
+// the sweeps that share its layout, 64 for the PSE sweeps (their cutoff's granularity) and
+// the planar and beta-plane ones.
+int origin_group(int kind) {
+  static_assert(PseRel::kGroup == PlanePseRel::kGroup, "the Gaussian-chord kind serves the sphere and the plane");
+  switch (kind) {
+    case kSumBve:
+    case kSumBveMesh:
+    case kSumSphereStream:
+    case kSumSweSphere:
+      return BveRel::kGroup;
+    case kSumPseK8Geo:
+    case kSumPseGaussChord:
+    case kSumPseGrad:
+    case kSumPseDiv:
+      return PseRel::kGroup;
+    case kSumPseK8Chord:
+      return PlanePseRel::kGroup;
+    case kSumBetaPlane:
+      return BetaRel::kGroup;
+    case kSumBetaStream:
+      return BetaStreamRel::kGroup;
+    default:
+      return PlaneRel::kGroup;
+  }
+}
+
 size_t rec_bytes(int kind, int mode) {
   if (mode == LPM_MODE_FP64) {
     if (kind == kSumPlane) return sizeof(RecPlane64);
@@ -616,13 +643,12 @@ SumPlan plan_sum(int kind, int mode, int64_t ns, int64_t nt, int sm_count, int s
   pl.src_bytes = static_cast<size_t>(pl.n_tiles) * tile * rec_bytes(kind, mode);
   if (sum_uses_sorted_sources(kind, mode)) {
     // the group origins follow the records
-    static_assert(sizeof(BveRel::Origin) == sizeof(PlaneRel::Origin) && BveRel::kGroup == PlaneRel::kGroup &&
-                      sizeof(BveRel::Origin) == sizeof(BetaRel::Origin) && BveRel::kGroup == BetaRel::kGroup &&
-                      sizeof(BveRel::Origin) == sizeof(BetaStreamRel::Origin) &&
-                      BveRel::kGroup == BetaStreamRel::kGroup,
+    static_assert(sizeof(BveRel::Origin) == sizeof(PlaneRel::Origin) &&
+                      sizeof(BveRel::Origin) == sizeof(BetaRel::Origin) &&
+                      sizeof(BveRel::Origin) == sizeof(BetaStreamRel::Origin),
                   "one origin layout size");
     pl.src_bytes = align_up(pl.src_bytes, 256) +
-                   static_cast<size_t>(pl.n_tiles) * (tile / BveRel::kGroup) * sizeof(BveRel::Origin);
+                   static_cast<size_t>(pl.n_tiles) * (tile / origin_group(kind)) * sizeof(BveRel::Origin);
   }
   if (mode == LPM_MODE_FP32C && pse_sorts_targets(kind)) {
     pl.tperm_offset = align_up(pl.src_bytes, 256);
