@@ -59,11 +59,11 @@ L2_FLUSH_BYTES = 256 << 20
 # DRAM bytes (ncu dram__bytes_read.sum + dram__bytes_write.sum) of one full-size icos nest 8
 # sweep launch, from a single-pass ncu capture of this benchmark's own step (ncu cannot run
 # inside the timed region, so this is a recorded constant, not a figure of this run)
-SWEEP_TRAFFIC_ICOS8 = 270_783_744 + 127_093_760
-# Pipe utilisation of the same sweep kernel (ncu --set full of bve_rel_sweep_kernel<128,8,256,2>
-# on this workload at icos nest 7, one launch): the pipe-level counterpart of the flop-contract
-# fraction; recorded constants, not figures of this run
-SWEEP_PIPES_ICOS7 = {"fma_pipe_active": 0.6608, "xu_pipe_active": 0.6144, "issue_active": 0.4797}
+SWEEP_TRAFFIC_ICOS8 = 264_474_880 + 126_703_360
+# Pipe utilisation of the same sweep kernel (ncu --set full of bve_rel_sweep_kernel<128,4,256,4>,
+# the autotuner's shape, on this workload at icos nest 7, one launch): the pipe-level counterpart
+# of the flop-contract fraction; recorded constants, not figures of this run
+SWEEP_PIPES_ICOS7 = {"fma_pipe_active": 0.6801, "xu_pipe_active": 0.6448, "issue_active": 0.5366}
 # FP32 CUDA-core nominal peak: 152 SMs x 128 lanes x 2 flops per FMA, per MHz of SM clock
 FP32_NOMINAL_TFLOPS_PER_MHZ = 152 * 128 * 2 / 1e6
 # FP64: 2 DFMA per clock per SM (4 flops), per MHz
