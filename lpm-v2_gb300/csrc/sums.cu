@@ -125,9 +125,13 @@ __global__ void __launch_bounds__(k64Threads) seq_fp64_kernel(P p, const Rec* __
 
 // The FP64 sweep for a small target set, S lanes per target.  Lane k of a target's group
 // evaluates sources j = j0 + k of each run of S, on an accumulator of zero, so it holds the
-// term itself (0 + X = X).  The group's first lane adds the S terms in ascending j, with the
-// same rounding as the sequential sweep.  This is for operators whose interact adds exactly
-// one term to each accumulator component (a = a + X, or a = a - X, which is a + (-X)), so the
+// term itself (0 + X = X).  The S terms of a run are then added in ascending j, with the same
+// rounding as the sequential sweep, each accumulator component by one lane of the group:
+// lane k keeps components k, k + S, ...  (one FP64 add per lane and term instead of one per
+// component: on GB300's 2 FP64 lanes per clock per SM the adds of all components in every
+// lane cost a quarter of the pipe at S = 4 and three components).  The group's first lane
+// collects the components at the end.  This is for operators whose interact adds exactly one
+// term to each accumulator component (a = a + X, or a = a - X, which is a + (-X)), so the
 // sums stay bit-identical up to the sign of an exact zero.  S times as many warps share the
 // FP64 work.
 template <class Op, class Rec, class P, int S, int THREADS>
@@ -138,6 +142,7 @@ __global__ void __launch_bounds__(THREADS) seq_fp64_split_kernel(P p, const Rec*
   using Acc = typename Op::Acc;
   static_assert(sizeof(Acc) % sizeof(double) == 0, "accumulators are doubles");
   constexpr int NA = static_cast<int>(sizeof(Acc) / sizeof(double));
+  constexpr int NSLOT = (NA + S - 1) / S;  // components per lane
   __shared__ __align__(128) Rec stage[2][k64Tile];
   __shared__ __align__(8) uint64_t bars[2];
   const int k = static_cast<int>(threadIdx.x) % S;
@@ -146,8 +151,9 @@ __global__ void __launch_bounds__(THREADS) seq_fp64_split_kernel(P p, const Rec*
   const bool valid = il < nt;
   const int64_t i = ib + (valid ? il : nt - 1);
   const typename Op::Tgt t = Op::load(p, i);
-  Acc acc{};
-  double* av = reinterpret_cast<double*>(&acc);
+  double slot[NSLOT];  // slot m: component k + m S of the target's sum
+#pragma unroll
+  for (int m = 0; m < NSLOT; ++m) slot[m] = 0.0;
   const int64_t n_tiles = ceil_div(ns, k64Tile);
   int64_t tile = 0;
   pipe_init(bars);
@@ -164,15 +170,25 @@ __global__ void __launch_bounds__(THREADS) seq_fp64_split_kernel(P p, const Rec*
 #pragma unroll
       for (int q = 0; q < S; ++q) {
         const bool hq = __shfl_sync(0xffffffffu, has, lane0 + q);
+        double x[NA];
 #pragma unroll
-        for (int c = 0; c < NA; ++c) {
-          const double x = __shfl_sync(0xffffffffu, dv[c], lane0 + q);
-          if (hq) av[c] = __dadd_rn(av[c], x);
+        for (int c = 0; c < NA; ++c) x[c] = __shfl_sync(0xffffffffu, dv[c], lane0 + q);
+#pragma unroll
+        for (int m = 0; m < NSLOT; ++m) {
+          const int c = k + m * S;
+          double xc = x[0];
+#pragma unroll
+          for (int cc = 1; cc < NA; ++cc) xc = c == cc ? x[cc] : xc;
+          if (hq && c < NA) slot[m] = __dadd_rn(slot[m], xc);
         }
       }
     }
     ++tile;
   });
+  Acc acc{};
+  double* av = reinterpret_cast<double*>(&acc);
+#pragma unroll
+  for (int c = 0; c < NA; ++c) av[c] = __shfl_sync(0xffffffffu, slot[c / S], lane0 + c % S);
   if (valid && k == 0) Op::store(p, i, il, acc);
 }
 
