@@ -112,20 +112,21 @@ __device__ __forceinline__ void tile_pipe_init(TilePipe<Rec, TILE, S, Side, NSID
   __syncthreads();
 }
 
-// S-stage warp-decoupled sweep over tiles [tile0, tile0 + ntl) of `src`: body(const Rec*)
-// runs once per tile in every warp, each warp at its own pace.  `g` counts the tiles this CTA
-// has pushed through the pipeline (identical in every thread): tile number q uses stage
-// q % S, whose full barrier completes phase (q / S) & 1 for it and whose empty barrier
-// completes phase (q / S) & 1 when every warp has released it.  Thread 0 (a consumer too)
-// issues the copies: before each of its tiles it refills every stage already released,
+// S-stage warp-decoupled sweep over ntl tiles of `src`, the k-th being tile tile_of(k):
+// body(const Rec*) runs once per tile in every warp, each warp at its own pace.  `g` counts
+// the tiles this CTA has pushed through the pipeline (identical in every thread): tile number
+// q uses stage q % S, whose full barrier completes phase (q / S) & 1 for it and whose empty
+// barrier completes phase (q / S) & 1 when every warp has released it.  Thread 0 (a consumer
+// too) issues the copies: before each of its tiles it refills every stage already released,
 // keeping up to S tiles in flight, and it blocks (bounded) on a release only when the tile
-// it needs next has not been issued.  Returns false in every thread when any wait gave up.
-// With NSIDE > 0 the side records of tile t are side_src[t * NSIDE .. (t + 1) * NSIDE) and
-// body(const Rec*, const Side*) gets both; otherwise body(const Rec*).
-template <class Rec, int TILE, int S, class Side, int NSIDE, class Body>
-__device__ __forceinline__ bool warp_sweep(const Rec* __restrict__ src, int64_t tile0, int64_t ntl,
-                                           TilePipe<Rec, TILE, S, Side, NSIDE>& pp, uint32_t& g, int* status,
-                                           const WaitCfg& w, const Side* __restrict__ side_src, Body&& body) {
+// it needs next has not been issued.  Returns false in every thread when any wait gave up;
+// the stages' barrier phases are then no longer in step with `g`, so the CTA must not sweep
+// again.  With NSIDE > 0 the side records of tile t are side_src[t * NSIDE .. (t + 1) *
+// NSIDE) and body(const Rec*, const Side*) gets both; otherwise body(const Rec*).
+template <class Rec, int TILE, int S, class Side, int NSIDE, class TileOf, class Body>
+__device__ __forceinline__ bool warp_sweep_tiles(const Rec* __restrict__ src, TileOf&& tile_of, int64_t ntl,
+                                                 TilePipe<Rec, TILE, S, Side, NSIDE>& pp, uint32_t& g, int* status,
+                                                 const WaitCfg& w, const Side* __restrict__ side_src, Body&& body) {
   constexpr uint32_t kBytes = TILE * sizeof(Rec);
   constexpr uint32_t kSideBytes = NSIDE * sizeof(Side);
   static_assert(kBytes % 16 == 0 && kSideBytes % 16 == 0, "copies must be multiples of 16 bytes");
@@ -146,10 +147,11 @@ __device__ __forceinline__ bool warp_sweep(const Rec* __restrict__ src, int64_t 
         return 0;
       }
     }
-    if (tile0 + kk != w.skip_tile) {
+    const int64_t t = tile_of(kk);
+    if (t != w.skip_tile) {
       mbar_arrive_expect_tx(&pp.full[s], kBytes + kSideBytes);
-      tma_load_1d(pp.stage[s], src + (tile0 + kk) * TILE, kBytes, &pp.full[s]);
-      if constexpr (NSIDE > 0) tma_load_1d(pp.side[s], side_src + (tile0 + kk) * NSIDE, kSideBytes, &pp.full[s]);
+      tma_load_1d(pp.stage[s], src + t * TILE, kBytes, &pp.full[s]);
+      if constexpr (NSIDE > 0) tma_load_1d(pp.side[s], side_src + t * NSIDE, kSideBytes, &pp.full[s]);
     }
     return 1;
   };
@@ -180,13 +182,126 @@ __device__ __forceinline__ bool warp_sweep(const Rec* __restrict__ src, int64_t 
     // copies issued for tiles this warp did not wait for must land before the CTA moves on
     // (bounded again); tiles below k completed, every stage before them too
     for (int64_t kk = k; kk < next; ++kk) {
-      if (tile0 + kk == w.skip_tile) continue;  // never issued
+      if (tile_of(kk) == w.skip_tile) continue;  // never issued
       const uint32_t q = g + static_cast<uint32_t>(kk);
       mbar_wait_bounded(&pp.full[q % S], (q / S) & 1u, status, w.ns);
     }
   }
   g += static_cast<uint32_t>(ntl);
   return all;
+}
+
+// The sweep over the contiguous tiles [tile0, tile0 + ntl).
+template <class Rec, int TILE, int S, class Side, int NSIDE, class Body>
+__device__ __forceinline__ bool warp_sweep(const Rec* __restrict__ src, int64_t tile0, int64_t ntl,
+                                           TilePipe<Rec, TILE, S, Side, NSIDE>& pp, uint32_t& g, int* status,
+                                           const WaitCfg& w, const Side* __restrict__ side_src, Body&& body) {
+  return warp_sweep_tiles(src, [tile0](int64_t k) { return tile0 + k; }, ntl, pp, g, status, w, side_src,
+                          static_cast<Body&&>(body));
+}
+
+// ---------------------------------------------------------------- tile culling (cutoff sums)
+// For the sums with a distance cutoff a CTA first lists the tiles of its chunk that hold a
+// group within reach of any of its targets and sweeps only those (warp_sweep_tiles over the
+// list), a window of kCullWindow tiles at a time.  The test is conservative against the
+// warps' own per-group test, so the tiles left out are exactly tiles every warp would have
+// skipped: the sums are unchanged, the copies and the per-group tests of those tiles saved.
+
+constexpr int kCullWindow = 128;
+
+// A ball around a CTA's targets: the centroid of the points and the largest distance to it.
+struct TargetBall {
+  float cx, cy, cz, r;
+};
+
+// Every thread passes its NPT points (hi parts of the positions the warps test with); the
+// ball is written to `out` (shared memory, so that it holds no registers during the sweep),
+// visible to every thread on return.
+template <int THREADS, int NPT>
+__device__ __forceinline__ void cta_target_ball(const float (&px)[NPT], const float (&py)[NPT], const float (&pz)[NPT],
+                                                TargetBall& out) {
+  static_assert(THREADS % 32 == 0 && THREADS <= 1024, "whole warps");
+  constexpr int NW = THREADS / 32;
+  __shared__ float red[4][NW];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  float sx = 0.f, sy = 0.f, sz = 0.f;
+#pragma unroll
+  for (int k = 0; k < NPT; ++k) {
+    sx += px[k];
+    sy += py[k];
+    sz += pz[k];
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    sx += __shfl_xor_sync(0xffffffffu, sx, o);
+    sy += __shfl_xor_sync(0xffffffffu, sy, o);
+    sz += __shfl_xor_sync(0xffffffffu, sz, o);
+  }
+  if (lane == 0) {
+    red[0][wid] = sx;
+    red[1][wid] = sy;
+    red[2][wid] = sz;
+  }
+  __syncthreads();
+  TargetBall b;
+  sx = sy = sz = 0.f;
+#pragma unroll
+  for (int k = 0; k < NW; ++k) {
+    sx += red[0][k];
+    sy += red[1][k];
+    sz += red[2][k];
+  }
+  constexpr float inv = 1.f / static_cast<float>(THREADS * NPT);
+  b.cx = sx * inv;
+  b.cy = sy * inv;
+  b.cz = sz * inv;
+  float m = 0.f;
+#pragma unroll
+  for (int k = 0; k < NPT; ++k) {
+    const float dx = px[k] - b.cx, dy = py[k] - b.cy, dz = pz[k] - b.cz;
+    const float d2 = dx * dx + dy * dy + dz * dz;
+    m = d2 > m ? d2 : (d2 == d2 ? m : __int_as_float(0x7f800000));  // a NaN point: infinite ball
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if (lane == 0) red[3][wid] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    m = 0.f;
+#pragma unroll
+    for (int k = 0; k < NW; ++k) m = fmaxf(m, red[3][k]);
+    b.r = sqrtf(m);
+    out = b;
+  }
+  __syncthreads();
+}
+
+// Lists (in tile order, into list[0..count)) the tiles t0 .. t0 + n - 1 (n <= kCullWindow)
+// holding a group gi (GPT per tile, gi = t * GPT + g) for which in_reach(gi) is true; returns
+// the count in every thread.  flags and count_out are shared scratch.
+template <int THREADS, int GPT, class InReach>
+__device__ __forceinline__ int cull_tiles(int64_t t0, int n, InReach&& in_reach, int32_t* list, int* flags,
+                                          int* count_out) {
+  for (int i = threadIdx.x; i < n; i += THREADS) flags[i] = 0;
+  __syncthreads();
+  for (int i = threadIdx.x; i < n * GPT; i += THREADS) {
+    if (in_reach((t0 + i / GPT) * GPT + i % GPT)) flags[i / GPT] = 1;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    int base = 0;
+    for (int i0 = 0; i0 < n; i0 += 32) {
+      const int i = i0 + lane;
+      const bool f = i < n && flags[i] != 0;
+      const unsigned m = __ballot_sync(0xffffffffu, f);
+      if (f) list[base + __popc(m & ((1u << lane) - 1u))] = static_cast<int32_t>(t0 + i);
+      base += __popc(m);
+    }
+    if (lane == 0) *count_out = base;
+  }
+  __syncthreads();
+  return *count_out;
 }
 
 // Arguments of a compensated FP32 sweep (targets, records, split-K partials).

@@ -273,8 +273,8 @@ namespace lpm {
 // PSEPlaneLaplacianAtParticles (src/PSEDirectSum.f90:467-500, K8 of the chord distance) and
 // the Gaussian 4 exp(-r^2)/pi of the chord, on the planar group-relative layout with the
 // group cutoff of the sphere's PSE sweep (pse_rel.cuh): a warp skips a group when every one
-// of its targets is farther than R + 10 eps from its centroid, where r^2 >= 100 and a term
-// is below FP32 resolution of the sum.  Per target pair and evaluated source (far form):
+// of its targets is farther than R + 7 eps from its centroid, where r^2 >= 49 and a term is
+// below 1e-17 of the kernel's peak, far below FP32 resolution of the sum.  Per target pair and evaluated source (far form):
 // d (2 FADD2), r^2 (2), exp(-r^2) (1 FMUL2 + 2 MUFU ex2), the K8 polynomial and product
 // (3 + 1), f_j - f_i from hi/lo parts (3), the accumulation (2).
 struct PlanePseRel {
@@ -290,7 +290,7 @@ struct PlanePseRel {
 struct PlanePseRelArgs {
   const double *x, *y, *f;
   float ks2;    // eps^-2
-  float c_cut;  // 10 eps
+  float c_cut;  // 7 eps: r^2 = PseRel::kCutR2
   const PlanePseRel::Rec* src;
   const PlaneRel::Origin* org;
   int64_t n_tiles, tiles_per_chunk, ib, nt;
@@ -365,10 +365,24 @@ __global__ void __launch_bounds__(THREADS, MINB) plane_pse_rel_sweep_kernel(Plan
   }
   const float2 ks2 = make_float2(a.ks2, a.ks2);
 
+  // the CTA's targets (hi parts) for the tile culling (engine.cuh)
+  __shared__ TargetBall ball;
+  {
+    float bx[2 * NP], by[2 * NP], bz[2 * NP];
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+      bx[2 * p] = pr[p].xh.x;
+      bx[2 * p + 1] = pr[p].xh.y;
+      by[2 * p] = pr[p].yh.x;
+      by[2 * p + 1] = pr[p].yh.y;
+      bz[2 * p] = bz[2 * p + 1] = 0.f;
+    }
+    cta_target_ball<THREADS, 2 * NP>(bx, by, bz, ball);
+  }
+
   tile_pipe_init(pipe);
   uint32_t g = 0;
-  warp_sweep(a.src, tile0, ntl, pipe, g, a.status, default_wait(), a.org,
-             [&](const Rec* tl, const PlaneRel::Origin* og) {
+  auto tile_body = [&](const Rec* tl, const PlaneRel::Origin* og) {
     float2 acc[NP];
 #pragma unroll
     for (int p = 0; p < NP; ++p) acc[p] = make_float2(0.f, 0.f);
@@ -388,7 +402,7 @@ __global__ void __launch_bounds__(THREADS, MINB) plane_pse_rel_sweep_kernel(Plan
         in_reach |= (n2.x < reach * reach) | (n2.y < reach * reach);
         near |= (n2.x < lim) | (n2.y < lim);
       }
-      if (!__any_sync(0xffffffffu, in_reach)) continue;  // every pair has r^2 > 100
+      if (!__any_sync(0xffffffffu, in_reach)) continue;  // every pair has r^2 > PseRel::kCutR2
       if (!__any_sync(0xffffffffu, near)) {
 #pragma unroll 4
         for (int j = 0; j < G; ++j) {
@@ -421,7 +435,29 @@ __global__ void __launch_bounds__(THREADS, MINB) plane_pse_rel_sweep_kernel(Plan
       comp_add(hs[p].x, ls[p].x, acc[p].x);
       comp_add(hs[p].y, ls[p].y, acc[p].y);
     }
-  });
+  };
+  // Only the chunk's tiles with a group within reach of the CTA's ball, a window at a time:
+  // the warps' own test with the ball's radius added, widened by 1e-4 of itself and by 1e-5
+  // of the coordinates' size for the rounding of the hi parts and of the ball.
+  __shared__ int32_t tlist[kCullWindow];
+  __shared__ int tflag[kCullWindow];
+  __shared__ int tcount;
+  const WaitCfg wait = default_wait();
+  for (int64_t w0 = 0; w0 < ntl; w0 += kCullWindow) {
+    const int nw = static_cast<int>(ntl - w0 < kCullWindow ? ntl - w0 : kCullWindow);
+    const int cnt = cull_tiles<THREADS, GPT>(
+        tile0 + w0, nw,
+        [&](int64_t gi) {
+          const PlaneRel::Origin o = a.org[gi];
+          const float dx = o.o.x - ball.cx, dy = o.o.y - ball.cy;
+          const float lim = (ball.r + o.f.x + a.c_cut) * 1.0001f + 1e-5f * (1.f + fabsf(ball.cx) + fabsf(ball.cy));
+          return !(dx * dx + dy * dy >= lim * lim);
+        },
+        tlist, tflag, &tcount);
+    if (!warp_sweep_tiles(a.src, [&](int64_t k) { return static_cast<int64_t>(tlist[k]); }, cnt, pipe, g, a.status,
+                          wait, a.org, tile_body))
+      break;  // a wait gave up: the stages are out of step, sweep no more
+  }
 
 #pragma unroll
   for (int p = 0; p < NP; ++p) {

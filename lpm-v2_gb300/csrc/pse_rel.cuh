@@ -8,12 +8,13 @@
 //   PSESphereGradientAtParticles  (:220-267)  G_i = eps^-4 P_i sum_j (f_j + f_i) (x_i - x_j) A_j K1(r)
 //   PSESphereDivergenceAtParticles (:537-579) D_i = eps^-4 sum_j (P_i (x_i - x_j)) . (V_j + V_i) A_j K1(r)
 // with r = distance / eps and P_i = I - x_i x_i^T (SphereProjection).  Every kernel carries
-// exp(-r^2): a pair with r^2 >= 100 adds less than 1e-37 of a near pair's term, below FP32
-// resolution of any sum it enters.  A warp therefore skips a whole group of 64 sources when
-// every one of its targets is farther than R + c_cut from the group's centroid (R the group
-// radius, c_cut = 10 eps / a the chord at which r^2 = 100; the great-circle distance is
-// never shorter than the chord).  The result equals the all-pairs sum to FP32 rounding; the
-// skipped pairs are counted as done.
+// exp(-r^2): at r^2 >= 49 every kernel (K8, K1 times r, the Gaussian) is below 1e-17 of its
+// peak (K8: |40 - 40 r^2 + 10 r^4 - 2/3 r^6| e^-49 / 40 = 7e-19), far below FP32 -- and
+// FP64 -- resolution of any sum it enters.  A warp therefore skips a whole group of 64
+// sources when every one of its targets is farther than R + c_cut from the group's centroid
+// (R the group radius, c_cut = 7 eps / a the chord at which r^2 = 49; the great-circle
+// distance is never shorter than the chord).  The result equals the all-pairs sum to FP32
+// rounding; the skipped pairs are counted as done.
 //
 // Positions are unit directions p / |p| for the great-circle kernels (the angle between them
 // is what SphereDistance's atan2 measures; then x_i - x_j = a d and x_i . d = |d|^2 / 2 on
@@ -49,7 +50,7 @@ struct PseRel {
   struct Pair {
     float2 xh, yh, zh, xl, yl, zl, e0, e1, e2;
   };
-  static constexpr float kCutR2 = 100.0f;  // r^2 beyond which a pair is negligible
+  static constexpr float kCutR2 = 49.0f;  // r^2 beyond which a pair is negligible
   // sources per origin: the group cutoff's granularity (larger groups reach farther)
   static constexpr int kGroup = 64;
 };
@@ -212,10 +213,29 @@ __global__ void __launch_bounds__(THREADS, MINB) pse_rel_sweep_kernel(PseRelArgs
   }
   const float2 ks2 = make_float2(a.ks2, a.ks2);
 
+  // Tile culling for the Laplacians (measured: Gaussian chord +13 %, K8 +3 % at cubed nest
+  // 7).  The gradient and divergence sweeps, already at 128 registers, spill more with it and
+  // ran 6 % slower and unchanged, so they sweep every tile of their chunk.
+  constexpr bool kCull = OP == kPseOpLapK8 || OP == kPseOpLapGauss;
+  // the CTA's targets (unit-scaled hi parts) for the tile culling
+  __shared__ TargetBall ball;
+  if constexpr (kCull) {
+    float bx[2 * NP], by[2 * NP], bz[2 * NP];
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+      bx[2 * p] = pr[p].xh.x;
+      bx[2 * p + 1] = pr[p].xh.y;
+      by[2 * p] = pr[p].yh.x;
+      by[2 * p + 1] = pr[p].yh.y;
+      bz[2 * p] = pr[p].zh.x;
+      bz[2 * p + 1] = pr[p].zh.y;
+    }
+    cta_target_ball<THREADS, 2 * NP>(bx, by, bz, ball);
+  }
+
   tile_pipe_init(pipe);
   uint32_t g = 0;
-  warp_sweep(a.src, tile0, ntl, pipe, g, a.status, a.wait, a.org,
-             [&](const Rec* tl, const BveRel::Origin* og) {
+  auto tile_body = [&](const Rec* tl, const BveRel::Origin* og) {
     float2 acc[NP][NC];
 #pragma unroll
     for (int p = 0; p < NP; ++p)
@@ -236,7 +256,7 @@ __global__ void __launch_bounds__(THREADS, MINB) pse_rel_sweep_kernel(PseRelArgs
         const float2 n2 = __ffma2_rn(tz[p], tz[p], __ffma2_rn(ty[p], ty[p], __fmul2_rn(tx[p], tx[p])));
         in_reach |= (n2.x < reach * reach) | (n2.y < reach * reach);
       }
-      if (!__any_sync(0xffffffffu, in_reach)) continue;  // every pair has r^2 > 100
+      if (!__any_sync(0xffffffffu, in_reach)) continue;  // every pair has r^2 > kCutR2
       if (o.hi.w == 0.f || !warp_near<NP>(tx, ty, tz, o.hi.w)) {
         // compact or far group: d = t_hi - s_hi
 #pragma unroll 4
@@ -278,7 +298,33 @@ __global__ void __launch_bounds__(THREADS, MINB) pse_rel_sweep_kernel(PseRelArgs
         comp_add(hs[p][c].x, ls[p][c].x, acc[p][c].x);
         comp_add(hs[p][c].y, ls[p][c].y, acc[p][c].y);
       }
-  });
+  };
+  if constexpr (!kCull) {
+    warp_sweep(a.src, tile0, ntl, pipe, g, a.status, a.wait, a.org, tile_body);
+  } else {
+    // The chunk's tiles with a group within reach of the CTA's ball (the warps' test with the
+    // ball's radius added, widened by 1e-4 of itself and by 1e-5 of the coordinates' size for
+    // the rounding of the hi parts and of the ball), a window at a time.
+    __shared__ int32_t tlist[kCullWindow];
+    __shared__ int tflag[kCullWindow];
+    __shared__ int tcount;
+    for (int64_t w0 = 0; w0 < ntl; w0 += kCullWindow) {
+      const int nw = static_cast<int>(ntl - w0 < kCullWindow ? ntl - w0 : kCullWindow);
+      const int cnt = cull_tiles<THREADS, GPT>(
+          tile0 + w0, nw,
+          [&](int64_t gi) {
+            const BveRel::Origin o = a.org[gi];
+            const float dx = o.hi.x - ball.cx, dy = o.hi.y - ball.cy, dz = o.hi.z - ball.cz;
+            const float lim = (ball.r + o.lo.w + a.c_cut) * 1.0001f +
+                              1e-5f * (1.f + fabsf(ball.cx) + fabsf(ball.cy) + fabsf(ball.cz));
+            return !(dx * dx + dy * dy + dz * dz >= lim * lim);
+          },
+          tlist, tflag, &tcount);
+      if (!warp_sweep_tiles(a.src, [&](int64_t k) { return static_cast<int64_t>(tlist[k]); }, cnt, pipe, g,
+                            a.status, a.wait, a.org, tile_body))
+        break;  // a wait gave up: the stages are out of step, sweep no more
+    }
+  }
 
 #pragma unroll
   for (int p = 0; p < NP; ++p) {

@@ -1142,7 +1142,7 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
       const double e4 = (job.eps * job.eps) * (job.eps * job.eps);
       const double cscale = (job.kind == kSumPseGaussChord ? 4.0 : 1.0) / kPi / e4;
       if (job.z && (job.kind == kSumPseK8Geo || job.kind == kSumPseGaussChord)) {
-        // sphere: group-relative sweep with the r^2 >= 100 group cutoff (pse_rel.cuh)
+        // sphere: group-relative sweep with the r^2 >= 49 group cutoff (pse_rel.cuh)
         LPM_TRY(launch_pse_rel(job, plan, npad));
       } else {
         // plane: the 2-D group-relative sweep with the same cutoff (plane_rel.cuh)
