@@ -50,15 +50,17 @@ constexpr int kSplit64 = 4;  // lanes per target of the split FP64 sweep (small 
 // One thread per target, sources in ascending particle order, one accumulator: the same
 // summation order as the Fortran j loop, hence bit-identical sums.
 //
-// The PSE kernels all carry exp(-r^2), r = distance / eps: a pair with r >= 10 adds less than
-// 1e-37 of a near pair's term, far below the FP64 sums' 1e-12 agreement with the reference
-// (whose exp is not CUDA's anyway).  For those a warp skips a whole source tile when every one
-// of its targets is farther than the tile's radius plus `reach` from the tile's centre, in the
-// space the distance is measured in:
-//   - unit directions for the great-circle kernels (reach 10 eps / radius; the angle is never
+// The PSE kernels all carry exp(-r^2), r = distance / eps: at r >= 7 each kernel (its
+// polynomial times e^-49) is below 1e-14 of its peak, far below the FP64 sums' 1e-12
+// agreement with the reference (whose exp is not CUDA's anyway; the all-pairs oracle tests
+// hold that bound with the cutoff).  For those a warp skips a whole source tile when every one of its
+// targets is farther than the tile's radius plus `reach` from the tile's centre, in the space
+// the distance is measured in:
+//   - unit directions for the great-circle kernels (reach 7 eps / radius; the angle is never
 //     shorter than the chord of the unit directions);
-//   - raw positions for the chord and planar ones (reach 10 eps).
-// The pairs it keeps are summed in the reference's order.
+//   - raw positions for the chord and planar ones (reach 7 eps).
+// The pairs it keeps are summed in the reference's order.  The FP32C sweeps cut at the same
+// r^2 = 49 (PseRel::kCutR2).
 struct __align__(32) TileBall {
   double x, y, z, r;  // centre and radius in the test space
 };
@@ -877,7 +879,7 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
       cut.x = job.x;
       cut.y = job.y;
       cut.z = job.z;
-      cut.reach = 10.0 * job.eps / (cut.unit ? job.radius : 1.0);
+      cut.reach = std::sqrt(static_cast<double>(PseRel::kCutR2)) * job.eps / (cut.unit ? job.radius : 1.0);
     }
     switch (job.kind) {
       case kSumBve:

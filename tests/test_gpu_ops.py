@@ -346,9 +346,10 @@ def test_beta_plane_fp32c_ragged_and_empty(lg, oracle_mod, n):
 
 
 def test_pse_fp64_tile_cutoff_plane(lg, oracle_mod):
-    """The FP64 PSE sweeps skip source tiles beyond r = 10 (exp(-r^2) < 1e-43): at quad nest 6
-    on [-4,4]^2 with eps = 2h = 0.25 (reach 2.5) most tiles are out of a warp's reach, and every
-    planar operator stays within 1e-12 of the all-pairs oracle, on a block of targets too."""
+    """The FP64 PSE sweeps skip source tiles beyond r = 7 (every kernel below 1e-14 of its peak):
+    at quad nest 6 on [-4,4]^2 with eps = 2h = 0.25 (reach 1.75) most tiles are out of a warp's
+    reach, and every planar operator stays within 1e-12 of the all-pairs oracle, on a block of
+    targets too."""
     m, act, eps = _plane(lg, 6, 21)
     f = np.exp(-0.3 * (m.x ** 2 + m.y ** 2)) * np.cos(m.x) + 0.2
     u, v = np.cos(0.5 * m.y), 0.3 * np.sin(m.x)
@@ -377,7 +378,7 @@ def test_pse_fp64_tile_cutoff_plane(lg, oracle_mod):
 
 @pytest.mark.parametrize("radius", [1.0, 6.37122e6])
 def test_pse_fp64_tile_cutoff_sphere(lg, oracle_mod, radius):
-    """The great-circle FP64 PSE sweeps with the tile cutoff (reach 10 eps / radius on unit
+    """The great-circle FP64 PSE sweeps with the tile cutoff (reach 7 eps / radius on unit
     directions) at cubed nest 5 with eps = 0.06 radius: Laplacian (K8 geodesic and Gaussian
     chord), gradient, divergence and double dot within 1e-12 of the all-pairs oracle."""
     m = lg.PolyMesh2d(lg.CUBED_SPHERE_SEED, 5, 1.0)
