@@ -201,13 +201,14 @@ __device__ __forceinline__ bool warp_sweep(const Rec* __restrict__ src, int64_t 
 }
 
 // ---------------------------------------------------------------- tile culling (cutoff sums)
-// For the sums with a distance cutoff a CTA first lists the tiles of its chunk that hold a
-// group within reach of any of its targets and sweeps only those (warp_sweep_tiles over the
-// list), a window of kCullWindow tiles at a time.  The test is conservative against the
-// warps' own per-group test, so the tiles left out are exactly tiles every warp would have
-// skipped: the sums are unchanged, the copies and the per-group tests of those tiles saved.
-
-constexpr int kCullWindow = 128;
+// For the sums with a distance cutoff every CTA of a target block lists the tiles of the whole
+// source range that lie within reach of its targets -- one test per tile, of the tile's ball
+// (written by the prep kernel) against the ball around the CTA's targets -- and CTA (block, c)
+// sweeps the c-th of gridDim.y equal shares of that list (warp_sweep_tiles over it), so the
+// work of a block is split evenly among its CTAs wherever its tiles lie.  The test is
+// conservative against the warps' own per-group test, so every tile left out is one every
+// warp would have skipped: the sums are unchanged, the copies and per-group tests of those
+// tiles saved.
 
 // A ball around a CTA's targets: the centroid of the points and the largest distance to it.
 struct TargetBall {
@@ -276,32 +277,103 @@ __device__ __forceinline__ void cta_target_ball(const float (&px)[NPT], const fl
   __syncthreads();
 }
 
-// Lists (in tile order, into list[0..count)) the tiles t0 .. t0 + n - 1 (n <= kCullWindow)
-// holding a group gi (GPT per tile, gi = t * GPT + g) for which in_reach(gi) is true; returns
-// the count in every thread.  flags and count_out are shared scratch.
-template <int THREADS, int GPT, class InReach>
-__device__ __forceinline__ int cull_tiles(int64_t t0, int n, InReach&& in_reach, int32_t* list, int* flags,
-                                          int* count_out) {
-  for (int i = threadIdx.x; i < n; i += THREADS) flags[i] = 0;
-  __syncthreads();
-  for (int i = threadIdx.x; i < n * GPT; i += THREADS) {
-    if (in_reach((t0 + i / GPT) * GPT + i % GPT)) flags[i / GPT] = 1;
-  }
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    const int lane = threadIdx.x;
-    int base = 0;
-    for (int i0 = 0; i0 < n; i0 += 32) {
-      const int i = i0 + lane;
-      const bool f = i < n && flags[i] != 0;
-      const unsigned m = __ballot_sync(0xffffffffu, f);
-      if (f) list[base + __popc(m & ((1u << lane) - 1u))] = static_cast<int32_t>(t0 + i);
-      base += __popc(m);
+// The ball of a tile from its GPT groups' balls (centre hi parts, radius; w < 0 marks an empty
+// group): centre the mean of the groups' centres, radius the largest distance to a group's
+// centre plus that group's radius, widened by 1e-5 of itself and 1e-6 of the centre's size for
+// the rounding of the hi parts.  Every source of the tile lies in it.
+template <int GPT>
+__device__ __forceinline__ float4 tile_ball_from_groups(const float4 (&grp)[GPT]) {
+  float cx = 0.f, cy = 0.f, cz = 0.f, n = 0.f;
+#pragma unroll
+  for (int g = 0; g < GPT; ++g) {
+    if (grp[g].w >= 0.f) {
+      cx += grp[g].x;
+      cy += grp[g].y;
+      cz += grp[g].z;
+      n += 1.f;
     }
-    if (lane == 0) *count_out = base;
   }
+  if (n > 0.f) {
+    cx /= n;
+    cy /= n;
+    cz /= n;
+  }
+  float r = 0.f;
+#pragma unroll
+  for (int g = 0; g < GPT; ++g) {
+    if (grp[g].w >= 0.f) {
+      const float dx = grp[g].x - cx, dy = grp[g].y - cy, dz = grp[g].z - cz;
+      const float e = sqrtf(dx * dx + dy * dy + dz * dz) + grp[g].w;
+      r = e > r ? e : (e == e ? r : __int_as_float(0x7f800000));  // NaN: an infinite ball
+    }
+  }
+  r = r * 1.00001f + 1e-6f * (1.f + fabsf(cx) + fabsf(cy) + fabsf(cz));
+  return make_float4(cx, cy, cz, r);
+}
+
+// Whether a tile's ball is within reach of a CTA's ball: the distance of the centres is below
+// the two radii plus c_cut, widened by 1e-4 of that and by 1e-5 of the coordinates' size for
+// the rounding of the hi parts (NaN reads as in reach).
+__device__ __forceinline__ bool tile_in_reach(const float4& tb, const TargetBall& b, float c_cut) {
+  const float dx = tb.x - b.cx, dy = tb.y - b.cy, dz = tb.z - b.cz;
+  const float lim = (b.r + tb.w + c_cut) * 1.0001f + 1e-5f * (1.f + fabsf(b.cx) + fabsf(b.cy) + fabsf(b.cz));
+  return !(dx * dx + dy * dy + dz * dz >= lim * lim);
+}
+
+// One window of THREADS tiles, t0 .. t0 + n - 1 (n <= THREADS), one per thread: counts the
+// tiles in reach, and lists (in tile order, into list[0..kept)) those whose rank in the whole
+// in-reach list -- rank0 for the window's first -- is in [lo, hi).  wcount is shared scratch
+// of THREADS / 32 ints.  Every thread gets the same counts.
+struct CullCount {
+  int in_reach, kept;
+};
+
+template <int THREADS, class InReach>
+__device__ __forceinline__ CullCount cull_window(int64_t t0, int n, InReach&& in_reach, int64_t rank0, int64_t lo,
+                                                 int64_t hi, int32_t* list, int* wcount) {
+  static_assert(THREADS % 32 == 0 && THREADS <= 1024, "whole warps");
+  constexpr int NW = THREADS / 32;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const bool f = static_cast<int>(threadIdx.x) < n && in_reach(t0 + threadIdx.x);
+  const unsigned m = __ballot_sync(0xffffffffu, f);
+  if (lane == 0) wcount[wid] = __popc(m);
   __syncthreads();
-  return *count_out;
+  int before = 0, total = 0;
+#pragma unroll
+  for (int w = 0; w < NW; ++w) {
+    const int c = wcount[w];
+    before += w < wid ? c : 0;
+    total += c;
+  }
+  const int64_t rank = rank0 + before + __popc(m & ((1u << lane) - 1u));
+  const int64_t first = rank0 > lo ? rank0 : lo;
+  if (f && rank >= lo && rank < hi) list[rank - first] = static_cast<int32_t>(t0 + threadIdx.x);
+  const int64_t end = rank0 + total < hi ? rank0 + total : hi;
+  __syncthreads();  // the list is complete and wcount free for the next window
+  return CullCount{total, end > first ? static_cast<int>(end - first) : 0};
+}
+
+// The balanced share of the in-reach tiles for CTA (blockIdx.x, blockIdx.y): lists them a
+// window at a time and calls sweep(list, count) for each non-empty window; stops early when
+// sweep returns false (a wait gave up).  in_reach(t) tests tile t.
+template <int THREADS, class InReach, class Sweep>
+__device__ __forceinline__ void sweep_culled_share(int64_t n_tiles, InReach&& in_reach, Sweep&& sweep) {
+  __shared__ int32_t list[THREADS];
+  __shared__ int wcount[THREADS / 32];
+  int64_t total = 0;
+  for (int64_t w0 = 0; w0 < n_tiles; w0 += THREADS) {
+    const int n = static_cast<int>(n_tiles - w0 < THREADS ? n_tiles - w0 : THREADS);
+    total += cull_window<THREADS>(w0, n, in_reach, total, 0, 0, list, wcount).in_reach;
+  }
+  const int64_t shares = gridDim.y, c = blockIdx.y;
+  const int64_t lo = total * c / shares, hi = total * (c + 1) / shares;
+  int64_t rank0 = 0;
+  for (int64_t w0 = 0; w0 < n_tiles && rank0 < hi; w0 += THREADS) {
+    const int n = static_cast<int>(n_tiles - w0 < THREADS ? n_tiles - w0 : THREADS);
+    const CullCount cc = cull_window<THREADS>(w0, n, in_reach, rank0, lo, hi, list, wcount);
+    rank0 += cc.in_reach;
+    if (cc.kept > 0 && !sweep(static_cast<const int32_t*>(list), cc.kept)) break;
+  }
 }
 
 // Arguments of a compensated FP32 sweep (targets, records, split-K partials).

@@ -291,6 +291,7 @@ struct PlanePseRelArgs {
   const double *x, *y, *f;
   float ks2;    // eps^-2
   float c_cut;  // 7 eps: r^2 = PseRel::kCutR2
+  const float4* tball;  // per source tile: centre (hi parts, z = 0) and radius
   const PlanePseRel::Rec* src;
   const PlaneRel::Origin* org;
   int64_t n_tiles, tiles_per_chunk, ib, nt;
@@ -328,11 +329,7 @@ __global__ void __launch_bounds__(THREADS, MINB) plane_pse_rel_sweep_kernel(Plan
   using Rec = PlanePseRel::Rec;
   __shared__ TilePipe<Rec, TILE, S, PlaneRel::Origin, GPT> pipe;
 
-  const int64_t chunk = blockIdx.y;
-  const int64_t tile0 = chunk * a.tiles_per_chunk;
-  int64_t ntl = a.n_tiles - tile0;
-  if (ntl > a.tiles_per_chunk) ntl = a.tiles_per_chunk;
-  if (ntl < 0) ntl = 0;
+  const int64_t chunk = blockIdx.y;  // this CTA's share of the target block's in-reach tiles
 
   PlaneRel::Pair pr[NP];
   float2 fh[NP], fl[NP], hs[NP], ls[NP];
@@ -436,28 +433,15 @@ __global__ void __launch_bounds__(THREADS, MINB) plane_pse_rel_sweep_kernel(Plan
       comp_add(hs[p].y, ls[p].y, acc[p].y);
     }
   };
-  // Only the chunk's tiles with a group within reach of the CTA's ball, a window at a time:
-  // the warps' own test with the ball's radius added, widened by 1e-4 of itself and by 1e-5
-  // of the coordinates' size for the rounding of the hi parts and of the ball.
-  __shared__ int32_t tlist[kCullWindow];
-  __shared__ int tflag[kCullWindow];
-  __shared__ int tcount;
+  // this CTA's balanced share of the in-reach tiles of the whole source range (engine.cuh);
+  // gridDim.y CTAs share a target block
   const WaitCfg wait = default_wait();
-  for (int64_t w0 = 0; w0 < ntl; w0 += kCullWindow) {
-    const int nw = static_cast<int>(ntl - w0 < kCullWindow ? ntl - w0 : kCullWindow);
-    const int cnt = cull_tiles<THREADS, GPT>(
-        tile0 + w0, nw,
-        [&](int64_t gi) {
-          const PlaneRel::Origin o = a.org[gi];
-          const float dx = o.o.x - ball.cx, dy = o.o.y - ball.cy;
-          const float lim = (ball.r + o.f.x + a.c_cut) * 1.0001f + 1e-5f * (1.f + fabsf(ball.cx) + fabsf(ball.cy));
-          return !(dx * dx + dy * dy >= lim * lim);
-        },
-        tlist, tflag, &tcount);
-    if (!warp_sweep_tiles(a.src, [&](int64_t k) { return static_cast<int64_t>(tlist[k]); }, cnt, pipe, g, a.status,
-                          wait, a.org, tile_body))
-      break;  // a wait gave up: the stages are out of step, sweep no more
-  }
+  sweep_culled_share<THREADS>(
+      a.n_tiles, [&](int64_t t) { return tile_in_reach(a.tball[t], ball, a.c_cut); },
+      [&](const int32_t* list, int cnt) {
+        return warp_sweep_tiles(a.src, [list](int64_t k) { return static_cast<int64_t>(list[k]); }, cnt, pipe, g,
+                                a.status, wait, a.org, tile_body);
+      });
 
 #pragma unroll
   for (int p = 0; p < NP; ++p) {
@@ -476,7 +460,7 @@ template <int TILE>
 __global__ void __launch_bounds__(TILE) plane_pse_rel_prep_kernel(const double* x, const double* y, const double* f,
                                                                   const double* area, const int32_t* sorted,
                                                                   int64_t ns, PlanePseRel::Rec* out,
-                                                                  PlaneRel::Origin* org) {
+                                                                  PlaneRel::Origin* org, float4* tball) {
   constexpr int G = PlanePseRel::kGroup;
   __shared__ double red[2][TILE];
   __shared__ float fmax_[TILE], cntf[TILE];
@@ -528,12 +512,17 @@ __global__ void __launch_bounds__(TILE) plane_pse_rel_prep_kernel(const double* 
     r.a = r.b = r.c = r.d = make_float4(0.f, 0.f, 0.f, 0.f);  // zero area: no contribution
   }
   out[k] = r;
+  constexpr int GPT = TILE / G;
+  __shared__ float4 grp[GPT];  // the groups' balls for the tile's ball (w < 0: empty group)
   if (lane == 0) {
     PlaneRel::Origin o;
     o.o = make_float4(oxh, oyh, oxl, oyl);
     o.f = make_float4(fmax_[g0], 0.f, 0.f, 0.f);
-    org[t * (TILE / G) + tid / G] = o;
+    org[t * GPT + tid / G] = o;
+    grp[tid / G] = valid ? make_float4(oxh, oyh, 0.f, fmax_[g0]) : make_float4(0.f, 0.f, 0.f, -1.f);
   }
+  __syncthreads();
+  if (tid == 0) tball[t] = tile_ball_from_groups<GPT>(grp);
 }
 
 // ====================================================================== planar SWE integrals

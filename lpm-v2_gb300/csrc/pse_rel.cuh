@@ -60,6 +60,7 @@ struct PseRelArgs {
   double inv_a;
   float ks2;      // (a / eps)^2
   float c_cut;    // chord at which r^2 = kCutR2
+  const float4* tball;  // per source tile: centre (unit-scaled hi parts) and radius (Laplacians)
   float half_a2;  // a^2 / 2 (divergence: P d = d - (a^2 |d|^2 / 2) p_i)
   const PseRel::Rec* src;
   const BveRel::Origin* org;  // hi.w: near radius (0 for a compact group), lo.w: group radius
@@ -302,28 +303,14 @@ __global__ void __launch_bounds__(THREADS, MINB) pse_rel_sweep_kernel(PseRelArgs
   if constexpr (!kCull) {
     warp_sweep(a.src, tile0, ntl, pipe, g, a.status, a.wait, a.org, tile_body);
   } else {
-    // The chunk's tiles with a group within reach of the CTA's ball (the warps' test with the
-    // ball's radius added, widened by 1e-4 of itself and by 1e-5 of the coordinates' size for
-    // the rounding of the hi parts and of the ball), a window at a time.
-    __shared__ int32_t tlist[kCullWindow];
-    __shared__ int tflag[kCullWindow];
-    __shared__ int tcount;
-    for (int64_t w0 = 0; w0 < ntl; w0 += kCullWindow) {
-      const int nw = static_cast<int>(ntl - w0 < kCullWindow ? ntl - w0 : kCullWindow);
-      const int cnt = cull_tiles<THREADS, GPT>(
-          tile0 + w0, nw,
-          [&](int64_t gi) {
-            const BveRel::Origin o = a.org[gi];
-            const float dx = o.hi.x - ball.cx, dy = o.hi.y - ball.cy, dz = o.hi.z - ball.cz;
-            const float lim = (ball.r + o.lo.w + a.c_cut) * 1.0001f +
-                              1e-5f * (1.f + fabsf(ball.cx) + fabsf(ball.cy) + fabsf(ball.cz));
-            return !(dx * dx + dy * dy + dz * dz >= lim * lim);
-          },
-          tlist, tflag, &tcount);
-      if (!warp_sweep_tiles(a.src, [&](int64_t k) { return static_cast<int64_t>(tlist[k]); }, cnt, pipe, g,
-                            a.status, a.wait, a.org, tile_body))
-        break;  // a wait gave up: the stages are out of step, sweep no more
-    }
+    // this CTA's balanced share of the in-reach tiles of the whole source range (engine.cuh);
+    // gridDim.y CTAs share a target block
+    sweep_culled_share<THREADS>(
+        a.n_tiles, [&](int64_t t) { return tile_in_reach(a.tball[t], ball, a.c_cut); },
+        [&](const int32_t* list, int cnt) {
+          return warp_sweep_tiles(a.src, [list](int64_t k) { return static_cast<int64_t>(list[k]); }, cnt, pipe, g,
+                                  a.status, a.wait, a.org, tile_body);
+        });
   }
 
 #pragma unroll
@@ -347,7 +334,8 @@ template <int OP, int ANG, int TILE>
 __global__ void __launch_bounds__(TILE) pse_rel_prep_kernel(const double* x, const double* y, const double* z,
                                                             const double* f, const double* vy, const double* vz,
                                                             const double* area, const int32_t* sorted, int64_t ns,
-                                                            double inv_a, PseRel::Rec* out, BveRel::Origin* org) {
+                                                            double inv_a, PseRel::Rec* out, BveRel::Origin* org,
+                                                            float4* tball) {
   const int64_t t = blockIdx.x;
   const int64_t k = t * TILE + threadIdx.x;
   const bool valid = k < ns;
@@ -377,10 +365,18 @@ __global__ void __launch_bounds__(TILE) pse_rel_prep_kernel(const double* x, con
     r.a = r.b = r.c = r.d = r.e = make_float4(0.f, 0.f, 0.f, 0.f);  // zero area: no contribution
   }
   out[k] = r;
+  constexpr int GPT = TILE / PseRel::kGroup;
+  __shared__ float4 grp[GPT];  // the groups' balls for the tile's ball (w < 0: empty group)
   if (threadIdx.x % PseRel::kGroup == 0) {
     BveRel::Origin o = group_origin(fr);
     o.lo.w = fr.radius;  // the cutoff test needs the radius of every group
-    org[t * (TILE / PseRel::kGroup) + threadIdx.x / PseRel::kGroup] = o;
+    org[t * GPT + threadIdx.x / PseRel::kGroup] = o;
+    grp[threadIdx.x / PseRel::kGroup] = valid ? make_float4(o.hi.x, o.hi.y, o.hi.z, fr.radius)
+                                              : make_float4(0.f, 0.f, 0.f, -1.f);
+  }
+  if (tball) {  // uniform over the CTA
+    __syncthreads();
+    if (threadIdx.x == 0) tball[t] = tile_ball_from_groups<GPT>(grp);
   }
 }
 

@@ -633,6 +633,24 @@ bool sum_uses_sorted_sources(int kind, int mode) {
 }
 
 namespace {
+// The FP32C PSE Laplacians sweep only the tiles within reach of each CTA's targets, in
+// balanced shares (engine.cuh); their prep kernels write a ball per tile.
+bool pse_culls_tiles(int kind) {
+  return kind == kSumPseK8Geo || kind == kSumPseGaussChord || kind == kSumPseK8Chord;
+}
+
+// Shares per target block of a culled sweep: about six waves of CTAs in all, at most 32 per
+// block.  A block's in-reach work is split evenly, but tiles differ in cost (near and partly
+// reached groups), so finer CTAs balance the SMs better until the per-CTA scan of the tile
+// balls (every CTA of a block scans them all) starts to count.  Measured on GB300 (K8 and
+// Gaussian at cubed nests 6-8, planar K8 at quad nests 7-8, 1 to 32 shares): within 3 % of
+// the best count at every size, where a fixed 3 was up to 2x slower (cubed nest 6).
+int64_t cull_shares(int64_t blocks, int64_t slots) {
+  if (blocks < 1) blocks = 1;
+  const int64_t m = ceil_div(6 * (slots > 0 ? slots : 1), blocks);
+  return m < 1 ? 1 : (m > 32 ? 32 : m);
+}
+
 // The FP32C PSE kinds also sort their targets (nt of them) with the same scratch.
 bool pse_sorts_targets(int kind) {
   return kind == kSumPseK8Geo || kind == kSumPseGaussChord || kind == kSumPseK8Chord || kind == kSumPseGrad ||
@@ -667,6 +685,10 @@ SumPlan plan_sum(int kind, int mode, int64_t ns, int64_t nt, int sm_count, int s
                   "one origin layout size");
     pl.src_bytes = align_up(pl.src_bytes, 256) +
                    static_cast<size_t>(pl.n_tiles) * (tile / origin_group(kind)) * sizeof(BveRel::Origin);
+  }
+  if (mode == LPM_MODE_FP32C && pse_culls_tiles(kind)) {
+    // the tiles' balls follow the group origins
+    pl.src_bytes = align_up(pl.src_bytes, 256) + static_cast<size_t>(pl.n_tiles) * sizeof(float4);
   }
   if (mode == LPM_MODE_FP32C && pse_sorts_targets(kind)) {
     pl.tperm_offset = align_up(pl.src_bytes, 256);
@@ -703,9 +725,16 @@ SumPlan plan_sum(int kind, int mode, int64_t ns, int64_t nt, int sm_count, int s
                    : kind == kSumSweSphere                           ? kSweSphereMinB
                                                                      : 4;
   const int64_t slots = static_cast<int64_t>(sm_count > 0 ? sm_count : 152) * minb;
-  const int64_t nsplit = choose_split(tblocks, pl.n_tiles, slots, 65535);
-  pl.tiles_per_chunk = ceil_div(pl.n_tiles, nsplit);
-  pl.nsplit = ceil_div(pl.n_tiles, pl.tiles_per_chunk);
+  if (mode == LPM_MODE_FP32C && pse_culls_tiles(kind)) {
+    // every CTA scans the whole source range for its in-reach tiles and takes one of nsplit
+    // equal shares of them
+    pl.tiles_per_chunk = pl.n_tiles;
+    pl.nsplit = cull_shares(tblocks, slots);
+  } else {
+    const int64_t nsplit = choose_split(tblocks, pl.n_tiles, slots, 65535);
+    pl.tiles_per_chunk = ceil_div(pl.n_tiles, nsplit);
+    pl.nsplit = ceil_div(pl.n_tiles, pl.tiles_per_chunk);
+  }
   pl.partial_bytes = static_cast<size_t>(pl.nsplit) * comps_of(kind) * nt * sizeof(double);
   if (kind == kSumSwePlane || kind == kSumSweSphere) {
     // the surface-height Laplacian: the K8 PSE sweep (planar or geodesic), after the velocity sweep
@@ -728,7 +757,7 @@ void pse_rel_launch(const SumJob& job, const SumPlan& plan, const int32_t* src_l
   constexpr int S = OP == kPseOpDiv ? kPseDivStages : kPseStages;
   pse_rel_prep_kernel<OP, ANG, TILE><<<static_cast<unsigned>(plan.n_tiles), TILE, 0, job.stream>>>(
       job.x, job.y, job.z, job.s1, job.s2, job.s3, job.area, src_list, job.ns, a.inv_a,
-      const_cast<PseRel::Rec*>(a.src), const_cast<BveRel::Origin*>(a.org));
+      const_cast<PseRel::Rec*>(a.src), const_cast<BveRel::Origin*>(a.org), const_cast<float4*>(a.tball));
   const dim3 grid(static_cast<unsigned>(ceil_div(job.nt, kPseThreads * kPseTpt)), static_cast<unsigned>(plan.nsplit));
   pse_rel_sweep_kernel<OP, ANG, kPseThreads, kPseTpt, TILE, kPseMinB, S><<<grid, kPseThreads, 0, job.stream>>>(a);
 }
@@ -783,6 +812,13 @@ int launch_pse_rel(const SumJob& job, const SumPlan& plan, int64_t npad) {
   a.src = static_cast<PseRel::Rec*>(job.src_buf);
   a.org = reinterpret_cast<BveRel::Origin*>(static_cast<char*>(job.src_buf) +
                                             align_up(static_cast<size_t>(npad) * sizeof(PseRel::Rec), 256));
+  // the Laplacians' tile balls follow the origins (plan_sum)
+  a.tball = job.kind == kSumPseK8Geo || job.kind == kSumPseGaussChord
+                ? reinterpret_cast<const float4*>(
+                      reinterpret_cast<const char*>(a.org) +
+                      align_up(static_cast<size_t>(plan.n_tiles) * (kPseTile / PseRel::kGroup) * sizeof(BveRel::Origin),
+                               256))
+                : nullptr;
   a.n_tiles = plan.n_tiles;
   a.tiles_per_chunk = plan.tiles_per_chunk;
   a.ib = job.ib;
@@ -834,6 +870,10 @@ int launch_plane_pse_rel(const SumJob& job, const SumPlan& plan, int64_t npad) {
   a.src = static_cast<PlanePseRel::Rec*>(job.src_buf);
   a.org = reinterpret_cast<PlaneRel::Origin*>(static_cast<char*>(job.src_buf) +
                                               align_up(static_cast<size_t>(npad) * sizeof(PlanePseRel::Rec), 256));
+  // the tile balls follow the origins (plan_sum)
+  a.tball = reinterpret_cast<const float4*>(
+      reinterpret_cast<const char*>(a.org) +
+      align_up(static_cast<size_t>(plan.n_tiles) * (kPseTile / PlanePseRel::kGroup) * sizeof(PlaneRel::Origin), 256));
   a.n_tiles = plan.n_tiles;
   a.tiles_per_chunk = plan.tiles_per_chunk;
   a.ib = job.ib;
@@ -842,7 +882,7 @@ int launch_plane_pse_rel(const SumJob& job, const SumPlan& plan, int64_t npad) {
   a.status = job.status;
   plane_pse_rel_prep_kernel<kPseTile><<<static_cast<unsigned>(plan.n_tiles), kPseTile, 0, job.stream>>>(
       job.x, job.y, job.s1, job.area, src_list, job.ns, const_cast<PlanePseRel::Rec*>(a.src),
-      const_cast<PlaneRel::Origin*>(a.org));
+      const_cast<PlaneRel::Origin*>(a.org), const_cast<float4*>(a.tball));
   const dim3 grid(static_cast<unsigned>(ceil_div(job.nt, kPseThreads * kPseTpt)), static_cast<unsigned>(plan.nsplit));
   if (job.kind == kSumPseK8Chord) {
     plane_pse_rel_sweep_kernel<true, kPseThreads, kPseTpt, kPseTile, kPseMinB, kPseStages>
