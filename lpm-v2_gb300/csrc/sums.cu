@@ -70,6 +70,9 @@ struct Fp64Cut {
   const double *x = nullptr, *y = nullptr, *z = nullptr;  // target positions (z may be null)
   double reach = 0.0;
   int unit = 0;  // 1: the test space is unit directions
+  // the targets in curve order (nt global indices), or nullptr for index order: a warp then
+  // holds 32 targets close together and skips more tiles; each target's own sum is unchanged
+  const int32_t* tperm = nullptr;
 };
 
 // The point of particle i in the test space.  A point at the origin has no direction (and
@@ -92,9 +95,10 @@ __global__ void __launch_bounds__(k64Threads) seq_fp64_kernel(P p, const Rec* __
                                                               int* status, Fp64Cut cut = Fp64Cut{}) {
   __shared__ __align__(128) Rec stage[2][k64Tile];
   __shared__ __align__(8) uint64_t bars[2];
-  const int64_t il = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  const bool valid = il < nt;
-  const int64_t i = ib + (valid ? il : nt - 1);
+  const int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  const bool valid = k < nt;
+  const int64_t i = cut.tperm ? static_cast<int64_t>(cut.tperm[valid ? k : nt - 1]) : ib + (valid ? k : nt - 1);
+  const int64_t il = i - ib;  // the target's place in the outputs
   const typename Op::Tgt t = Op::load(p, i);
   typename Op::Acc acc{};
   const int64_t n_tiles = ceil_div(ns, k64Tile);
@@ -659,10 +663,13 @@ bool pse_sorts_targets(int kind) {
 }  // namespace
 
 size_t sort_scratch_bytes(int kind, int64_t ns, int64_t nt) {
-  const int64_t m = pse_sorts_targets(kind) && nt > ns ? nt : ns;
+  int unit = 0;
+  const bool targets = pse_sorts_targets(kind) || fp64_cutoff(kind, &unit);  // FP64 cut sums sort targets only
+  const int64_t m = targets && nt > ns ? nt : ns;
   // planar kinds sort in 2-D; the Gaussian-chord Laplacian serves the plane and the sphere
   if (kind == kSumPlane || kind == kSumPseK8Chord || kind == kSumPlaneStream || kind == kSumSwePlane ||
-      kind == kSumBetaPlane || kind == kSumBetaStream)
+      kind == kSumBetaPlane || kind == kSumBetaStream || kind == kSumPsePlaneGrad || kind == kSumPsePlaneSecond ||
+      kind == kSumPsePlaneDdot || kind == kSumPseInterpPlane)
     return curve_sort2d_bytes(m);
   if (kind == kSumPseGaussChord) return std::max(curve_sort_bytes(m), curve_sort2d_bytes(m));
   return curve_sort_bytes(m);
@@ -702,8 +709,11 @@ SumPlan plan_sum(int kind, int mode, int64_t ns, int64_t nt, int sm_count, int s
   if (mode == LPM_MODE_FP64) {
     int unit = 0;
     if (fp64_cutoff(kind, &unit)) {
-      // the tiles' bounding balls follow the records
+      // the tiles' bounding balls follow the records, then the targets' curve order (two
+      // lists of nt int32, as for the FP32C PSE sums)
       pl.src_bytes = align_up(pl.src_bytes, 256) + static_cast<size_t>(pl.n_tiles) * sizeof(TileBall);
+      pl.tperm_offset = align_up(pl.src_bytes, 256);
+      pl.src_bytes = pl.tperm_offset + 2 * align_up(static_cast<size_t>(nt) * sizeof(int32_t), 256);
     }
     // one target per thread and no split (the sum is sequential per target): a target set
     // too small for one 128-thread CTA per SM takes CTAs of one warp (and, for the BVE and
@@ -920,6 +930,13 @@ int launch_sum(const SumJob& job, const SumPlan& plan) {
       cut.y = job.y;
       cut.z = job.z;
       cut.reach = std::sqrt(static_cast<double>(PseRel::kCutR2)) * job.eps / (cut.unit ? job.radius : 1.0);
+      // targets in curve order when the job brings sort scratch (the host-buffer calls)
+      const bool sphere = cut.unit || (job.kind == kSumPseGaussChord && job.z);
+      LPM_TRY(sorted_targets(job, plan, [&](const int32_t* in, int32_t* out) {
+        return sphere ? curve_sort(job.stream, job.nt, in, job.x, job.y, job.z, 1.0 / job.radius, job.sort_scratch,
+                                   job.sort_bytes, out)
+                      : curve_sort2d(job.stream, job.nt, in, job.x, job.y, job.sort_scratch, job.sort_bytes, out);
+      }, &cut.tperm));
     }
     switch (job.kind) {
       case kSumBve:
@@ -1632,7 +1649,8 @@ int run_host(const HostArgs& a, int nout) {
     job.out2 = nout > 2 ? dout + 2 * nt : nullptr;
     job.out3 = nout > 3 ? dout + 3 * nt : nullptr;
     LPM_TRY(workspace(ctx, kWsSources, plan.src_bytes, &job.src_buf));
-    if (sum_uses_sorted_sources(a.kind, prec)) {
+    int unit = 0;
+    if (sum_uses_sorted_sources(a.kind, prec) || (prec == LPM_MODE_FP64 && fp64_cutoff(a.kind, &unit))) {
       void* ps = nullptr;
       const size_t sb = sort_scratch_bytes(a.kind, ns, nt);
       const size_t sorted_off = align_up(sb, 256);
