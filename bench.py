@@ -674,7 +674,7 @@ def run_configs(args):
         mc = 2048
         t = _best_time(lambda: orc.pse_laplacian(*a, eps, 1.0, kern, ib=n // 3, ie=n // 3 + mc), reps=1)
         row[f"cpu_oracle_{name}"] = mc * ns / t / 1e9
-    row["gpu_fp64_sample"] = "every target; source tiles beyond r = 10 skipped (all-pairs equivalent)"
+    row["gpu_fp64_sample"] = "every target, in curve order; source tiles beyond r = 7 skipped (all-pairs equivalent)"
     row["cpu_sample"] = "2048 targets against all sources"
     out["C3_pse_laplacian"] = row
     line = {"metric": "direct-sum Ginteractions/s per configuration (GPU FP64 / FP32C, CPU oracle)",
