@@ -60,7 +60,7 @@ struct PseRelArgs {
   double inv_a;
   float ks2;      // (a / eps)^2
   float c_cut;    // chord at which r^2 = kCutR2
-  const float4* tball;  // per source tile: centre (unit-scaled hi parts) and radius (Laplacians)
+  const float4* tball;  // per source tile: centre (unit-scaled hi parts) and radius
   float half_a2;  // a^2 / 2 (divergence: P d = d - (a^2 |d|^2 / 2) p_i)
   const PseRel::Rec* src;
   const BveRel::Origin* org;  // hi.w: near radius (0 for a compact group), lo.w: group radius
@@ -162,11 +162,7 @@ __global__ void __launch_bounds__(THREADS, MINB) pse_rel_sweep_kernel(PseRelArgs
   using Rec = PseRel::Rec;
   __shared__ TilePipe<Rec, TILE, S, BveRel::Origin, GPT> pipe;
 
-  const int64_t chunk = blockIdx.y;
-  const int64_t tile0 = chunk * a.tiles_per_chunk;
-  int64_t ntl = a.n_tiles - tile0;
-  if (ntl > a.tiles_per_chunk) ntl = a.tiles_per_chunk;
-  if (ntl < 0) ntl = 0;
+  const int64_t chunk = blockIdx.y;  // this CTA's share of the target block's in-reach tiles
 
   PseRel::Pair pr[NP];
   float2 hs[NP][NC], ls[NP][NC];
@@ -214,13 +210,9 @@ __global__ void __launch_bounds__(THREADS, MINB) pse_rel_sweep_kernel(PseRelArgs
   }
   const float2 ks2 = make_float2(a.ks2, a.ks2);
 
-  // Tile culling for the Laplacians (measured: Gaussian chord +13 %, K8 +3 % at cubed nest
-  // 7).  The gradient and divergence sweeps, already at 128 registers, spill more with it and
-  // ran 6 % slower and unchanged, so they sweep every tile of their chunk.
-  constexpr bool kCull = OP == kPseOpLapK8 || OP == kPseOpLapGauss;
-  // the CTA's targets (unit-scaled hi parts) for the tile culling
+  // the ball around the CTA's targets (unit-scaled hi parts) for the tile culling
   __shared__ TargetBall ball;
-  if constexpr (kCull) {
+  {
     float bx[2 * NP], by[2 * NP], bz[2 * NP];
 #pragma unroll
     for (int p = 0; p < NP; ++p) {
@@ -300,18 +292,16 @@ __global__ void __launch_bounds__(THREADS, MINB) pse_rel_sweep_kernel(PseRelArgs
         comp_add(hs[p][c].y, ls[p][c].y, acc[p][c].y);
       }
   };
-  if constexpr (!kCull) {
-    warp_sweep(a.src, tile0, ntl, pipe, g, a.status, a.wait, a.org, tile_body);
-  } else {
-    // this CTA's balanced share of the in-reach tiles of the whole source range (engine.cuh);
-    // gridDim.y CTAs share a target block
-    sweep_culled_share<THREADS>(
-        a.n_tiles, [&](int64_t t) { return tile_in_reach(a.tball[t], ball, a.c_cut); },
-        [&](const int32_t* list, int cnt) {
-          return warp_sweep_tiles(a.src, [list](int64_t k) { return static_cast<int64_t>(list[k]); }, cnt, pipe, g,
-                                  a.status, a.wait, a.org, tile_body);
-        });
-  }
+  // this CTA's balanced share of the in-reach tiles of the whole source range (engine.cuh);
+  // gridDim.y CTAs share a target block.  (The gradient and divergence sweeps spill 64-144
+  // bytes with it, at 128 registers, and still run 1.4-2x faster than over every tile of a
+  // chunk.)
+  sweep_culled_share<THREADS>(
+      a.n_tiles, [&](int64_t t) { return tile_in_reach(a.tball[t], ball, a.c_cut); },
+      [&](const int32_t* list, int cnt) {
+        return warp_sweep_tiles(a.src, [list](int64_t k) { return static_cast<int64_t>(list[k]); }, cnt, pipe, g,
+                                a.status, a.wait, a.org, tile_body);
+      });
 
 #pragma unroll
   for (int p = 0; p < NP; ++p) {
@@ -374,10 +364,8 @@ __global__ void __launch_bounds__(TILE) pse_rel_prep_kernel(const double* x, con
     grp[threadIdx.x / PseRel::kGroup] = valid ? make_float4(o.hi.x, o.hi.y, o.hi.z, fr.radius)
                                               : make_float4(0.f, 0.f, 0.f, -1.f);
   }
-  if (tball) {  // uniform over the CTA
-    __syncthreads();
-    if (threadIdx.x == 0) tball[t] = tile_ball_from_groups<GPT>(grp);
-  }
+  __syncthreads();
+  if (threadIdx.x == 0) tball[t] = tile_ball_from_groups<GPT>(grp);
 }
 
 // Gradient finish: chunk sums of sum_j (f_j + f_i) A_j K1 d, projected with P_i = I - x_i x_i^T

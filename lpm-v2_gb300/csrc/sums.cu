@@ -637,10 +637,11 @@ bool sum_uses_sorted_sources(int kind, int mode) {
 }
 
 namespace {
-// The FP32C PSE Laplacians sweep only the tiles within reach of each CTA's targets, in
-// balanced shares (engine.cuh); their prep kernels write a ball per tile.
+// The FP32C PSE sums sweep only the tiles within reach of each CTA's targets, in balanced
+// shares (engine.cuh); their prep kernels write a ball per tile.
 bool pse_culls_tiles(int kind) {
-  return kind == kSumPseK8Geo || kind == kSumPseGaussChord || kind == kSumPseK8Chord;
+  return kind == kSumPseK8Geo || kind == kSumPseGaussChord || kind == kSumPseK8Chord || kind == kSumPseGrad ||
+         kind == kSumPseDiv;
 }
 
 // Shares per target block of a culled sweep: about six waves of CTAs in all, at most 32 per
@@ -823,12 +824,10 @@ int launch_pse_rel(const SumJob& job, const SumPlan& plan, int64_t npad) {
   a.org = reinterpret_cast<BveRel::Origin*>(static_cast<char*>(job.src_buf) +
                                             align_up(static_cast<size_t>(npad) * sizeof(PseRel::Rec), 256));
   // the Laplacians' tile balls follow the origins (plan_sum)
-  a.tball = job.kind == kSumPseK8Geo || job.kind == kSumPseGaussChord
-                ? reinterpret_cast<const float4*>(
-                      reinterpret_cast<const char*>(a.org) +
-                      align_up(static_cast<size_t>(plan.n_tiles) * (kPseTile / PseRel::kGroup) * sizeof(BveRel::Origin),
-                               256))
-                : nullptr;
+  const int tile = job.kind == kSumPseDiv ? kPseDivTile : kPseTile;
+  a.tball = reinterpret_cast<const float4*>(
+      reinterpret_cast<const char*>(a.org) +
+      align_up(static_cast<size_t>(plan.n_tiles) * (tile / PseRel::kGroup) * sizeof(BveRel::Origin), 256));
   a.n_tiles = plan.n_tiles;
   a.tiles_per_chunk = plan.tiles_per_chunk;
   a.ib = job.ib;
