@@ -9,6 +9,7 @@
 // affects rounding (the FP32C sum is order-independent to its error bound); FP64 sums keep
 // the reference's ascending order.
 #include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_select.cuh>
 
 #include "lpm_common.cuh"
 #include "hilbert.cuh"
@@ -230,6 +231,50 @@ int curve_sort2d(cudaStream_t stream, int64_t ns, const int32_t* idx, const doub
   LPM_CUDA_TRY(cudaGetLastError());
   LPM_CUDA_TRY(cub::DeviceRadixSort::SortPairs(d_temp, temp, keys_in, keys_out, vals_in, sorted,
                                                static_cast<int>(ns), 0, 32, stream));
+  return LPM_OK;
+}
+
+namespace {
+__global__ void mark_kernel(int64_t ns, const int32_t* idx, uint8_t* mask) {
+  const int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k < ns) mask[idx[k]] = 1;
+}
+
+__global__ void gather_flags_kernel(int64_t n, const int32_t* order, const uint8_t* mask, uint8_t* flags) {
+  const int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k < n) flags[k] = mask[order[k]];
+}
+
+size_t select_temp_bytes(int64_t n) {
+  size_t temp = 0;
+  cub::DeviceSelect::Flagged(nullptr, temp, static_cast<const int32_t*>(nullptr), static_cast<const uint8_t*>(nullptr),
+                             static_cast<int32_t*>(nullptr), static_cast<int64_t*>(nullptr), static_cast<int>(n));
+  return temp;
+}
+}  // namespace
+
+size_t select_in_order_bytes(int64_t n) {
+  // mask and flags (n bytes each), the selected count, then the CUB temporary
+  return 2 * align_up(static_cast<size_t>(n), 256) + 256 + align_up(select_temp_bytes(n), 256);
+}
+
+int select_in_order(cudaStream_t stream, int64_t n, const int32_t* order, int64_t ns, const int32_t* idx,
+                    void* scratch, size_t scratch_bytes, int32_t* out) {
+  if (n <= 0 || ns <= 0) return LPM_OK;
+  const size_t temp = select_temp_bytes(n);
+  const size_t nb = align_up(static_cast<size_t>(n), 256);
+  if (scratch_bytes < 2 * nb + 256 + align_up(temp, 256)) return set_error(LPM_ERR_STATE, "select scratch too small");
+  char* base = static_cast<char*>(scratch);
+  uint8_t* mask = reinterpret_cast<uint8_t*>(base);
+  uint8_t* flags = reinterpret_cast<uint8_t*>(base + nb);
+  int64_t* count = reinterpret_cast<int64_t*>(base + 2 * nb);
+  void* d_temp = base + 2 * nb + 256;
+  LPM_CUDA_TRY(cudaMemsetAsync(mask, 0, static_cast<size_t>(n), stream));
+  mark_kernel<<<static_cast<unsigned>(ceil_div(ns, 256)), 256, 0, stream>>>(ns, idx, mask);
+  gather_flags_kernel<<<static_cast<unsigned>(ceil_div(n, 256)), 256, 0, stream>>>(n, order, mask, flags);
+  LPM_CUDA_TRY(cudaGetLastError());
+  size_t tb = temp;
+  LPM_CUDA_TRY(cub::DeviceSelect::Flagged(d_temp, tb, order, flags, out, count, static_cast<int>(n), stream));
   return LPM_OK;
 }
 

@@ -27,4 +27,12 @@ size_t curve_sort2d_bytes(int64_t ns);
 int curve_sort2d(cudaStream_t stream, int64_t ns, const int32_t* idx, const double* x, const double* y,
                  void* scratch, size_t scratch_bytes, int32_t* sorted);
 
+// out[0..ns) = the entries of order[0..n) (a permutation of the particles 0..n-1) that are
+// listed in idx[0..ns) (the active particles, distinct), in the order of `order`: the active
+// particles in the curve order of all of them, without a second sort.  Scratch:
+// select_in_order_bytes(n) bytes.
+size_t select_in_order_bytes(int64_t n);
+int select_in_order(cudaStream_t stream, int64_t n, const int32_t* order, int64_t ns, const int32_t* idx,
+                    void* scratch, size_t scratch_bytes, int32_t* out);
+
 }  // namespace lpm

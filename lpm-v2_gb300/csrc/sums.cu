@@ -1,6 +1,7 @@
 // sums.cu -- direct-sum kernels (prep, sweep, finish), their launchers and the host-buffer
 // C-ABI entry points lpm_bve_velocity, lpm_plane_velocity, lpm_pse_*_laplacian and the
 // stream functions.
+#include <algorithm>
 #include <cmath>
 #include <map>
 #include <mutex>
@@ -671,9 +672,9 @@ size_t sort_scratch_bytes(int kind, int64_t ns, int64_t nt) {
   if (kind == kSumPlane || kind == kSumPseK8Chord || kind == kSumPlaneStream || kind == kSumSwePlane ||
       kind == kSumBetaPlane || kind == kSumBetaStream || kind == kSumPsePlaneGrad || kind == kSumPsePlaneSecond ||
       kind == kSumPsePlaneDdot || kind == kSumPseInterpPlane)
-    return curve_sort2d_bytes(m);
-  if (kind == kSumPseGaussChord) return std::max(curve_sort_bytes(m), curve_sort2d_bytes(m));
-  return curve_sort_bytes(m);
+    return std::max(curve_sort2d_bytes(m), pse_sorts_targets(kind) ? select_in_order_bytes(m) : size_t{0});
+  if (kind == kSumPseGaussChord) return std::max({curve_sort_bytes(m), curve_sort2d_bytes(m), select_in_order_bytes(m)});
+  return std::max(curve_sort_bytes(m), pse_sorts_targets(kind) ? select_in_order_bytes(m) : size_t{0});
 }
 
 int bve_shape_count() { return kBveShapeCount; }
@@ -795,18 +796,34 @@ int sorted_targets(const SumJob& job, const SumPlan& plan, SortFn&& sort, const 
   return LPM_OK;
 }
 
+// Whether a PSE job's targets are every particle, so that its sources (the active ones) can take
+// the targets' curve order instead of a sort of their own.
+bool targets_cover_sources(const SumJob& job, const SumPlan& plan) {
+  return job.sort_scratch && plan.tperm_offset != 0 && job.ib == 0 && job.nt == job.n && job.nt >= 2;
+}
+
 int launch_pse_rel(const SumJob& job, const SumPlan& plan, int64_t npad) {
   const double inv_a = 1.0 / job.radius;
   const int32_t* src_list = job.src_idx;
-  if (job.sort_scratch) {
-    LPM_TRY(curve_sort(job.stream, job.ns, job.src_idx, job.x, job.y, job.z, inv_a, job.sort_scratch,
-                       job.sort_bytes, job.sorted));
-    src_list = job.sorted;
-  }
   const int32_t* tperm = nullptr;
-  LPM_TRY(sorted_targets(job, plan, [&](const int32_t* in, int32_t* out) {
+  auto sort3 = [&](const int32_t* in, int32_t* out) {
     return curve_sort(job.stream, job.nt, in, job.x, job.y, job.z, inv_a, job.sort_scratch, job.sort_bytes, out);
-  }, &tperm));
+  };
+  if (targets_cover_sources(job, plan)) {
+    // one sort: every particle in curve order, the sources picked out of it in that order
+    // (the same order as a sort of their own, whose keys are the same function of position)
+    LPM_TRY(sorted_targets(job, plan, sort3, &tperm));
+    LPM_TRY(select_in_order(job.stream, job.n, tperm, job.ns, job.src_idx, job.sort_scratch, job.sort_bytes,
+                            job.sorted));
+    src_list = job.sorted;
+  } else {
+    if (job.sort_scratch) {
+      LPM_TRY(curve_sort(job.stream, job.ns, job.src_idx, job.x, job.y, job.z, inv_a, job.sort_scratch,
+                         job.sort_bytes, job.sorted));
+      src_list = job.sorted;
+    }
+    LPM_TRY(sorted_targets(job, plan, sort3, &tperm));
+  }
   PseRelArgs a;
   a.tperm = tperm;
   a.x = job.x;
@@ -860,15 +877,25 @@ int launch_pse_rel(const SumJob& job, const SumPlan& plan, int64_t npad) {
 namespace {
 int launch_plane_pse_rel(const SumJob& job, const SumPlan& plan, int64_t npad) {
   const int32_t* src_list = job.src_idx;
-  if (job.sort_scratch) {
-    LPM_TRY(curve_sort2d(job.stream, job.ns, job.src_idx, job.x, job.y, job.sort_scratch, job.sort_bytes,
-                         job.sorted));
-    src_list = job.sorted;
-  }
   const int32_t* tperm = nullptr;
-  LPM_TRY(sorted_targets(job, plan, [&](const int32_t* in, int32_t* out) {
+  auto sort2 = [&](const int32_t* in, int32_t* out) {
     return curve_sort2d(job.stream, job.nt, in, job.x, job.y, job.sort_scratch, job.sort_bytes, out);
-  }, &tperm));
+  };
+  if (targets_cover_sources(job, plan)) {
+    // one sort: every particle along the curve over their bounding box, the sources picked
+    // out of it in that order
+    LPM_TRY(sorted_targets(job, plan, sort2, &tperm));
+    LPM_TRY(select_in_order(job.stream, job.n, tperm, job.ns, job.src_idx, job.sort_scratch, job.sort_bytes,
+                            job.sorted));
+    src_list = job.sorted;
+  } else {
+    if (job.sort_scratch) {
+      LPM_TRY(curve_sort2d(job.stream, job.ns, job.src_idx, job.x, job.y, job.sort_scratch, job.sort_bytes,
+                           job.sorted));
+      src_list = job.sorted;
+    }
+    LPM_TRY(sorted_targets(job, plan, sort2, &tperm));
+  }
   PlanePseRelArgs a;
   a.tperm = tperm;
   a.x = job.x;
