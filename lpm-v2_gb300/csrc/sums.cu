@@ -54,9 +54,9 @@ constexpr int kSplit64 = 4;  // lanes per target of the split FP64 sweep (small 
 // The PSE kernels all carry exp(-r^2), r = distance / eps: at r >= 7 each kernel (its
 // polynomial times e^-49) is below 1e-14 of its peak, far below the FP64 sums' 1e-12
 // agreement with the reference (whose exp is not CUDA's anyway; the all-pairs oracle tests
-// hold that bound with the cutoff).  For those a warp skips a whole source tile when every one of its
-// targets is farther than the tile's radius plus `reach` from the tile's centre, in the space
-// the distance is measured in:
+// hold that bound with the cutoff).  For those a warp skips a whole source tile when every
+// one of its targets is farther than the tile's radius plus `reach` from the tile's centre,
+// in the space the distance is measured in:
 //   - unit directions for the great-circle kernels (reach 7 eps / radius; the angle is never
 //     shorter than the chord of the unit directions);
 //   - raw positions for the chord and planar ones (reach 7 eps).
