@@ -650,14 +650,35 @@ def run_configs(args):
     per = n * ns - ns
     row = {"size": f"quad nest 7 on [-4,4]^2: {n} targets, {ns} sources", "interactions_per_eval": per}
     a = (c["x"], c["y"], c["omega"], c["area"], c["active"])
+    m = 4096
+    blk = (n // 3, n // 3 + m)
     for delta in (0.0, 0.02):
         for mode in ("fp64", "fp32c"):
             t = _best_time(lambda: lg.planar_incompressible_velocity(*a, delta, mode=mode))
             row[f"gpu_{mode}_delta{delta}"] = per / t / 1e9
-    m = 4096
-    t = _best_time(lambda: orc.plane_velocity(*a, 0.0, ib=n // 3, ie=n // 3 + m), reps=1)
+        # FP32C velocity error against the oracle on a block of targets, relative to the
+        # block's largest velocity
+        u, v = lg.planar_incompressible_velocity(*a, delta, i_begin=blk[0] + 1, i_end=blk[1], mode="fp32c")
+        ru, rv = orc.plane_velocity(*a, delta, ib=blk[0], ie=blk[1])
+        err = max(np.abs(u[blk[0]:blk[1]] - ru).max(), np.abs(v[blk[0]:blk[1]] - rv).max())
+        row[f"fp32c_velocity_rel_linf_delta{delta}"] = err / max(np.abs(ru).max(), np.abs(rv).max())
+    t = _best_time(lambda: orc.plane_velocity(*a, 0.0, ib=blk[0], ie=blk[1]), reps=1)
     row["cpu_oracle"] = m * ns / t / 1e9
     row["cpu_sample"] = f"delta 0, {m} targets against all sources"
+    # the configuration's run: RK4, dt 0.005, 200 steps, delta 0.02, FP32C, through the solver
+    s_ = lg.PlaneSolver(*a, delta=0.02, mode="fp32c")
+    d0 = s_.diagnostics()
+    s_.timestep(0.005, 2)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s_.timestep(0.005, 198)
+    torch.cuda.synchronize()
+    row["gpu_fp32c_rk4_200_steps"] = 198 * 4 * per / (time.perf_counter() - t0) / 1e9
+    d1 = s_.diagnostics()
+    s_.close()
+    row["rk4_circulation_drift"] = d1["circulation"] - d0["circulation"]
+    row["rk4_kinetic_energy_rel_drift"] = (d1["kinetic_energy"] - d0["kinetic_energy"]) / d0["kinetic_energy"]
+    row["rk4"] = "200 RK4 steps of dt 0.005 (delta 0.02, FP32C solver): rate over the last 198, drifts over all 200"
     out["C2_planar_velocity"] = row
     # C3
     c = wl.config_pse_cubed(7)
@@ -665,16 +686,27 @@ def run_configs(args):
     per = n * ns
     row = {"size": f"cubed sphere nest 7: {n} targets, {ns} sources", "interactions_per_eval": per}
     a = (c["x"], c["y"], c["z"], c["f"], c["area"], c["active"])
+    exact = -30.0 * wl.y54(c["x"], c["y"], c["z"])  # the Laplacian of the smooth part of f
     for name, kern, eps in (("k8_geodesic", lg.PSE_K8_GEODESIC, c["eps_k8"]),
                             ("gauss_chord", lg.PSE_GAUSS_CHORD, c["eps_gauss"])):
         t = _best_time(lambda: lg.pse_sphere_laplacian_at_particles(*a, eps, 1.0, kern, mode="fp32c"))
         row[f"gpu_fp32c_{name}"] = per / t / 1e9
         t = _best_time(lambda: lg.pse_sphere_laplacian_at_particles(*a, eps, 1.0, kern, mode="fp64"), reps=1)
         row[f"gpu_fp64_{name}"] = per / t / 1e9
+        l32 = lg.pse_sphere_laplacian_at_particles(*a, eps, 1.0, kern, mode="fp32c")
+        l64 = lg.pse_sphere_laplacian_at_particles(*a, eps, 1.0, kern, mode="fp64")
+        row[f"fp32c_rel_linf_vs_fp64_{name}"] = float(np.abs(l32 - l64).max() / np.abs(l64).max())
+        row[f"fp64_rel_linf_vs_exact_{name}"] = float(np.abs(l64 - exact).max() / np.abs(exact).max())
+        # the same sum on Y54 alone: the PSE discretisation error against the exact Laplacian
+        y = (c["x"], c["y"], c["z"], wl.y54(c["x"], c["y"], c["z"]), c["area"], c["active"])
+        ly = lg.pse_sphere_laplacian_at_particles(*y, eps, 1.0, kern, mode="fp32c")
+        row[f"fp32c_rel_linf_vs_exact_noise_free_{name}"] = float(np.abs(ly - exact).max() / np.abs(exact).max())
         mc = 2048
         t = _best_time(lambda: orc.pse_laplacian(*a, eps, 1.0, kern, ib=n // 3, ie=n // 3 + mc), reps=1)
         row[f"cpu_oracle_{name}"] = mc * ns / t / 1e9
     row["gpu_fp64_sample"] = "every target, in curve order; source tiles beyond r = 7 skipped (all-pairs equivalent)"
+    row["exact"] = ("-30 Y54 (the 1e-3 noise in f has no closed-form Laplacian, so the error against it includes "
+                    "the PSE estimate of the noise's)")
     row["cpu_sample"] = "2048 targets against all sources"
     out["C3_pse_laplacian"] = row
     line = {"metric": "direct-sum Ginteractions/s per configuration (GPU FP64 / FP32C, CPU oracle)",

@@ -322,15 +322,15 @@ __device__ __forceinline__ bool tile_in_reach(const float4& tb, const TargetBall
 
 // One window of THREADS tiles, t0 .. t0 + n - 1 (n <= THREADS), one per thread: counts the
 // tiles in reach, and lists (in tile order, into list[0..kept)) those whose rank in the whole
-// in-reach list -- rank0 for the window's first -- is in [lo, hi).  wcount is shared scratch
-// of THREADS / 32 ints.  Every thread gets the same counts.
+// in-reach list -- rank0 for the window's first -- is share modulo shares.  wcount is shared
+// scratch of THREADS / 32 ints.  Every thread gets the same counts.
 struct CullCount {
   int in_reach, kept;
 };
 
 template <int THREADS, class InReach>
-__device__ __forceinline__ CullCount cull_window(int64_t t0, int n, InReach&& in_reach, int64_t rank0, int64_t lo,
-                                                 int64_t hi, int32_t* list, int* wcount) {
+__device__ __forceinline__ CullCount cull_window(int64_t t0, int n, InReach&& in_reach, int64_t rank0, int64_t shares,
+                                                 int64_t share, int32_t* list, int* wcount) {
   static_assert(THREADS % 32 == 0 && THREADS <= 1024, "whole warps");
   constexpr int NW = THREADS / 32;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -346,31 +346,28 @@ __device__ __forceinline__ CullCount cull_window(int64_t t0, int n, InReach&& in
     total += c;
   }
   const int64_t rank = rank0 + before + __popc(m & ((1u << lane) - 1u));
-  const int64_t first = rank0 > lo ? rank0 : lo;
-  if (f && rank >= lo && rank < hi) list[rank - first] = static_cast<int32_t>(t0 + threadIdx.x);
-  const int64_t end = rank0 + total < hi ? rank0 + total : hi;
+  // the first rank >= rank0 of this share; the share's ranks follow every `shares`
+  const int64_t first = rank0 + ((share - rank0 % shares) % shares + shares) % shares;
+  if (f && rank % shares == share) list[(rank - first) / shares] = static_cast<int32_t>(t0 + threadIdx.x);
+  const int64_t end = rank0 + total;
   __syncthreads();  // the list is complete and wcount free for the next window
-  return CullCount{total, end > first ? static_cast<int>(end - first) : 0};
+  return CullCount{total, end > first ? static_cast<int>((end - 1 - first) / shares + 1) : 0};
 }
 
-// The balanced share of the in-reach tiles for CTA (blockIdx.x, blockIdx.y): lists them a
-// window at a time and calls sweep(list, count) for each non-empty window; stops early when
-// sweep returns false (a wait gave up).  in_reach(t) tests tile t.
+// The share of the in-reach tiles for CTA (blockIdx.x, blockIdx.y): every gridDim.y-th tile
+// of the block's in-reach list, starting at the blockIdx.y-th (equal counts to within one,
+// in one scan of the tile balls).  Lists them a window at a time and calls sweep(list,
+// count) for each non-empty window; stops early when sweep returns false (a wait gave up).
+// in_reach(t) tests tile t.
 template <int THREADS, class InReach, class Sweep>
 __device__ __forceinline__ void sweep_culled_share(int64_t n_tiles, InReach&& in_reach, Sweep&& sweep) {
   __shared__ int32_t list[THREADS];
   __shared__ int wcount[THREADS / 32];
-  int64_t total = 0;
+  const int64_t shares = gridDim.y, share = blockIdx.y;
+  int64_t rank0 = 0;
   for (int64_t w0 = 0; w0 < n_tiles; w0 += THREADS) {
     const int n = static_cast<int>(n_tiles - w0 < THREADS ? n_tiles - w0 : THREADS);
-    total += cull_window<THREADS>(w0, n, in_reach, total, 0, 0, list, wcount).in_reach;
-  }
-  const int64_t shares = gridDim.y, c = blockIdx.y;
-  const int64_t lo = total * c / shares, hi = total * (c + 1) / shares;
-  int64_t rank0 = 0;
-  for (int64_t w0 = 0; w0 < n_tiles && rank0 < hi; w0 += THREADS) {
-    const int n = static_cast<int>(n_tiles - w0 < THREADS ? n_tiles - w0 : THREADS);
-    const CullCount cc = cull_window<THREADS>(w0, n, in_reach, rank0, lo, hi, list, wcount);
+    const CullCount cc = cull_window<THREADS>(w0, n, in_reach, rank0, shares, share, list, wcount);
     rank0 += cc.in_reach;
     if (cc.kept > 0 && !sweep(static_cast<const int32_t*>(list), cc.kept)) break;
   }

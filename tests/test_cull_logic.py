@@ -6,7 +6,9 @@ group (centroid o, radius R) when |c - o| >= (R_ball + R + c_cut) (1 + 1e-4) + 1
 The culling must be conservative against the warps' own test, which skips a group when every
 target of the warp has |t - o| >= R + c_cut: then the sums are the same with and without it.
 Here every target of a CTA that culls a group must be at least R + c_cut from its centroid,
-with room for the float rounding of the warps' test."""
+with room for the float rounding of the warps' test.  The CTAs of a block then split its
+in-reach tiles round robin (cull_window's pick, restated at the end): each tile goes to one CTA.
+"""
 import numpy as np
 
 GROUP = 64
@@ -103,3 +105,35 @@ def test_nan_target_culls_nothing():
     T[5, 1] = np.nan
     c, rb = _ball(T)
     assert not any(_culled(c, rb, o, R, 0.1) for o, R in _groups(S))
+
+
+def _share_listing(rank0, total, shares, share):
+    """cull_window's pick for one window, restated: the kept count and each kept rank's place."""
+    first = rank0 + ((share - rank0 % shares) % shares + shares) % shares
+    end = rank0 + total
+    kept = (end - 1 - first) // shares + 1 if end > first else 0
+    places = {r: (r - first) // shares for r in range(rank0, end) if r % shares == share}
+    return kept, places
+
+
+def test_round_robin_shares_list_every_tile_once():
+    """Every in-reach tile of a block goes to exactly one of its CTAs, each CTA's list is dense
+    (places 0..kept-1 in rank order) and the shares' counts differ by at most one."""
+    rng = np.random.default_rng(25)
+    for _ in range(200):
+        shares = int(rng.integers(1, 33))
+        windows = [int(rng.integers(0, 129)) for _ in range(int(rng.integers(1, 6)))]
+        owner = {}
+        counts = [0] * shares
+        for share in range(shares):
+            rank0 = 0
+            for total in windows:
+                kept, places = _share_listing(rank0, total, shares, share)
+                assert sorted(places.values()) == list(range(kept))
+                for r in places:
+                    assert r not in owner
+                    owner[r] = share
+                counts[share] += kept
+                rank0 += total
+        assert sorted(owner) == list(range(sum(windows)))
+        assert max(counts) - min(counts) <= 1
