@@ -1,10 +1,10 @@
 // sort.cu -- spatial (Hilbert-curve) ordering of the source particles on the device.
 //
-// The FP32C sphere sweep stores every source relative to the origin of its group of 64, so
-// groups must be spatially compact: sources are ordered by the 30-bit index, along a 3-D
+// The FP32C sweeps store every source relative to the origin of its group (64 or 128
+// consecutive sources), so groups must be spatially compact: sources are ordered by the 30-bit index, along a 3-D
 // Hilbert curve over a 2^10 grid per axis, of the cell holding their unit-scaled position,
-// with a device radix sort (CUB).  Consecutive Hilbert cells are face neighbours, so 64
-// consecutive sources form one connected patch (a Hilbert-curve order jumps across the grid at
+// with a device radix sort (CUB).  Consecutive Hilbert cells are face neighbours, so a group
+// of consecutive sources forms one connected patch (a Hilbert-curve order jumps across the grid at
 // its octant boundaries, which leaves some groups in two distant pieces).  The order only
 // affects rounding (the FP32C sum is order-independent to its error bound); FP64 sums keep
 // the reference's ascending order.
