@@ -284,7 +284,7 @@ struct PlanePseRel {
     float4 c;  // -sx_lo, -sx_lo, -sy_lo, -sy_lo
     float4 d;  // f_lo, f_lo, 0, 0
   };
-  static constexpr int kGroup = 64;  // sources per origin: the group cutoff's granularity
+  static constexpr int kGroup = 32;  // sources per origin: the group cutoff's granularity
 };
 
 struct PlanePseRelArgs {

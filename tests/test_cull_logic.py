@@ -11,7 +11,7 @@ in-reach tiles round robin (cull_window's pick, restated at the end): each tile 
 """
 import numpy as np
 
-GROUP = 64
+GROUP = 32  # PseRel::kGroup, PlanePseRel::kGroup
 CTA_TARGETS = 512
 
 
