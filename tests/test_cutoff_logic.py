@@ -1,12 +1,12 @@
 """The FP64 PSE sweeps' tile cutoff (seq_fp64_kernel with tile_bounds64_kernel) restated in
-numpy: a warp skips a 128-source tile when every target is farther than the tile's radius plus
+numpy: a warp skips a 64-source tile when every target is farther than the tile's radius plus
 the reach from its centre, in unit directions (reach 7 eps / radius, great-circle kernels) or
 raw positions (reach 7 eps).  Every pair of a skipped tile must then have r = distance / eps
 >= 7 -- the great-circle distance is never shorter than the chord of the unit directions --
 so each kernel (a polynomial times exp(-r^2)) is below 1e-14 of its peak there."""
 import numpy as np
 
-TILE = 128
+TILE = 64
 
 
 def _balls(P):
