@@ -2,12 +2,15 @@
 //
 // Layout: sources are compacted (active particles only) into an array of fixed-size
 // records, padded with inert records to a multiple of the tile size.  A CTA owns a block of
-// targets (held in registers) and a contiguous range of source tiles (one split-K chunk).
+// targets (held in registers) and a contiguous range of source tiles (one split-K chunk) --
+// or, for the sums with a distance cutoff, a round-robin share of the tiles within reach of
+// its targets (sweep_culled_share, at the end of this file).
 // Tiles are staged into shared memory by 1-D TMA bulk copies (cp.async.bulk), and every
 // thread then sweeps a tile with broadcast shared-memory reads.  Two pipelines:
 //  - staged_sweep: two stages, block-synchronous (every warp finishes a tile before its stage
 //    is refilled; two block barriers per tile);
-//  - warp_sweep: S stages, warp-decoupled.  Each stage has a "full" mbarrier (the copy's
+//  - warp_sweep / warp_sweep_tiles: S stages, warp-decoupled, over a contiguous range or a
+//    list of tiles.  Each stage has a "full" mbarrier (the copy's
 //    transaction count) and an "empty" one (one arrival per warp when it is done with the
 //    tile).  Thread 0 refills a stage as soon as every warp has released it, so warps that
 //    skip a tile's work run ahead by up to S - 1 tiles instead of waiting at a barrier.
