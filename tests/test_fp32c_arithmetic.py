@@ -341,3 +341,30 @@ def test_plane_fp32c_arithmetic_meets_the_bar(built_lib, oracle_mod, delta, shif
         wgt = np.where(own, F(0), Sf[None, :] / np.where(own, F(1), q))
         plain = np.stack([-(wgt * d[:, :, 1]).sum(1, dtype=F), (wgt * d[:, :, 0]).sum(1, dtype=F)], 1)
         assert np.sqrt(((plain.astype(D) - ref) ** 2).sum(1)).max() / full.max() > 1e-5
+
+
+def test_hilbert_keys_match_the_library(tmp_path):
+    """The numpy curve keys above are the library's (csrc/hilbert.cuh, compiled here for the
+    host) on random cells of both grids."""
+    import shutil
+    import subprocess
+    from pathlib import Path
+    if shutil.which("g++") is None:
+        pytest.skip("no g++")
+    hdr = Path(__file__).resolve().parents[1] / "lpm-v2_gb300" / "csrc" / "hilbert.cuh"
+    src = tmp_path / "keys.cpp"
+    src.write_text('#include <cstdio>\n#define __host__\n#define __device__\n#include "%s"\n'
+                   "int main() {\n  unsigned a, b, c, u, v;\n"
+                   "  while (scanf(\"%%u %%u %%u %%u %%u\", &a, &b, &c, &u, &v) == 5)\n"
+                   "    printf(\"%%u %%u\\n\", lpm::hilbert_index30(a, b, c), lpm::hilbert_index2d(u, v));\n"
+                   "}\n" % hdr)
+    exe = tmp_path / "keys"
+    subprocess.run(["g++", "-O1", "-o", str(exe), str(src)], check=True)
+    rng = np.random.default_rng(8)
+    cells = np.stack([rng.integers(0, 1024, 4000), rng.integers(0, 1024, 4000), rng.integers(0, 1024, 4000),
+                      rng.integers(0, 65536, 4000), rng.integers(0, 65536, 4000)], 1)
+    out = subprocess.run([str(exe)], input="\n".join(" ".join(map(str, r)) for r in cells), capture_output=True,
+                         text=True, check=True).stdout
+    want = np.array(out.split(), dtype=np.uint64).reshape(-1, 2)
+    assert np.array_equal(_hilbert([cells[:, 0], cells[:, 1], cells[:, 2]], 10), want[:, 0])
+    assert np.array_equal(_hilbert([cells[:, 3], cells[:, 4]], 16), want[:, 1])
