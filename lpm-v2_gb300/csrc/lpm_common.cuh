@@ -112,13 +112,6 @@ __device__ __forceinline__ float ex2_approx(float x) {
   return r;
 }
 
-// log2 on the MUFU unit (PTX lg2.approx, flush-to-zero): absolute error ~2^-22.
-__device__ __forceinline__ float lg2_approx(float x) {
-  float r;
-  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-  return r;
-}
-
 // TwoSum (Knuth): s + e == a + b exactly, with s = fl(a + b).
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   s = __fadd_rn(a, b);

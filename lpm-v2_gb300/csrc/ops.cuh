@@ -17,12 +17,6 @@ __device__ __forceinline__ void split2(double v, float& hi, float& lo) {
   lo = __double2float_rn(v - static_cast<double>(hi));
 }
 
-// difference of two hi/lo numbers: (ah - bh) + (al - bl).  For nearby values ah - bh is
-// exact (Sterbenz), so near pairs keep ~48-bit differences.
-__device__ __forceinline__ float diff2(float ah, float al, float bh, float bl) {
-  return __fadd_rn(__fsub_rn(ah, bh), __fsub_rn(al, bl));
-}
-
 // ============================================================ sphere BVE velocity
 // Reference: BVESphereVelocity, src/SphereBVESolver.f90:395-420.
 //
