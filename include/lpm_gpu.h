@@ -9,7 +9,8 @@
  *
  * Conventions shared by every entry point
  *  - Arrays are contiguous, length n, in particle order (Fortran 1-based array base
- *    pointers pass straight through).
+ *    pointers pass straight through); 1 <= n <= 2^31 - 1, the range of the 32-bit particle
+ *    indices the library keeps.
  *  - active[j] is 1 for active (panel-centre) particles and 0 for passive (vertex)
  *    particles: the Fortran logical(klog) mask converted once with merge(1,0,mask).
  *  - i_begin/i_end are 1-based and inclusive, the MPISetup indexStart/indexEnd of the
@@ -36,7 +37,7 @@ extern "C" {
 
 enum {
   LPM_OK = 0,
-  LPM_ERR_ARG = -1,       /* bad argument (null pointer, n <= 0, bad range or mode) */
+  LPM_ERR_ARG = -1,       /* bad argument (null pointer, n out of range, bad range or mode) */
   LPM_ERR_CUDA = -2,      /* a CUDA runtime call failed */
   LPM_ERR_TIMEOUT = -3,   /* a bounded device-side wait gave up */
   LPM_ERR_NONFINITE = -4, /* LPM_FLAG_CHECK_FINITE found a NaN/Inf output */

@@ -42,6 +42,19 @@ void clear_error();
 // device status word values (set by kernels, read by the host after a synchronize)
 enum : int { kDevOk = 0, kDevTimeout = 1, kDevBadIndex = 2 };
 
+// Largest particle count of a call: source lists, sort values and curve orders hold 32-bit
+// particle indices.
+constexpr int64_t kMaxParticles = 2147483647;
+
+// LPM_ERR_ARG unless 0 < n <= kMaxParticles.
+inline int check_count(int64_t n) {
+  if (n <= 0) return set_error(LPM_ERR_ARG, "n must be positive (got %lld)", static_cast<long long>(n));
+  if (n > kMaxParticles)
+    return set_error(LPM_ERR_ARG, "n = %lld is above the %lld particles that 32-bit indices address",
+                     static_cast<long long>(n), static_cast<long long>(kMaxParticles));
+  return LPM_OK;
+}
+
 // ------------------------------------------------------------------ context / workspace
 // A device buffer that only grows.  Growth synchronises the context stream first.
 struct DevBuf {

@@ -551,7 +551,7 @@ extern "C" int lpm_bve_solver_create(lpm_bve_solver** out, int64_t n, const doub
                                      double radius, double rotation_rate, int mode) {
   if (!out) return set_error(LPM_ERR_ARG, "null solver handle pointer");
   *out = nullptr;
-  if (n <= 0) return set_error(LPM_ERR_ARG, "n must be positive");
+  LPM_TRY(check_count(n));
   if (!x || !y || !z || !relvort || !area || !active) return set_error(LPM_ERR_ARG, "null input array");
   if (!(radius > 0.0)) return set_error(LPM_ERR_ARG, "radius must be positive");
   if (mode != LPM_MODE_FP64 && mode != LPM_MODE_FP32C) return set_error(LPM_ERR_ARG, "unknown mode %d", mode);
@@ -620,7 +620,7 @@ extern "C" int lpm_bve_solver_remesh(lpm_bve_solver* S, int64_t n, const double*
                                      const double* relvort, const double* area, const int32_t* active, const double* u,
                                      const double* v, const double* w) {
   if (!S) return set_error(LPM_ERR_ARG, "null solver");
-  if (n <= 0) return set_error(LPM_ERR_ARG, "n must be positive");
+  LPM_TRY(check_count(n));
   if (!x || !y || !z || !relvort || !area || !active) return set_error(LPM_ERR_ARG, "null input array");
   if ((u == nullptr) != (v == nullptr) || (u == nullptr) != (w == nullptr))
     return set_error(LPM_ERR_ARG, "u, v, w must be all given or all NULL");
@@ -958,7 +958,7 @@ extern "C" int lpm_plane_solver_create(lpm_plane_solver** out, int64_t n, const 
                                        const double* u, const double* v, double delta, int mode) {
   if (!out) return set_error(LPM_ERR_ARG, "null solver handle pointer");
   *out = nullptr;
-  if (n <= 0) return set_error(LPM_ERR_ARG, "n must be positive");
+  LPM_TRY(check_count(n));
   if (!x || !y || !omega || !area || !active) return set_error(LPM_ERR_ARG, "null input array");
   if (!(delta >= 0.0)) return set_error(LPM_ERR_ARG, "delta must be >= 0");
   if (mode != LPM_MODE_FP64 && mode != LPM_MODE_FP32C) return set_error(LPM_ERR_ARG, "unknown mode %d", mode);
@@ -997,7 +997,7 @@ extern "C" int lpm_plane_solver_remesh(lpm_plane_solver* S, int64_t n, const dou
                                        const double* omega, const double* area, const int32_t* active,
                                        const double* u, const double* v) {
   if (!S) return set_error(LPM_ERR_ARG, "null solver");
-  if (n <= 0) return set_error(LPM_ERR_ARG, "n must be positive");
+  LPM_TRY(check_count(n));
   if (!x || !y || !omega || !area || !active) return set_error(LPM_ERR_ARG, "null input array");
   if ((u == nullptr) != (v == nullptr)) return set_error(LPM_ERR_ARG, "u and v must be both given or both NULL");
   LPM_CUDA_TRY(cudaStreamSynchronize(S->stream));

@@ -1579,7 +1579,7 @@ struct HostArgs {
 };
 
 int check_common(const HostArgs& a, int nout) {
-  if (a.n <= 0) return set_error(LPM_ERR_ARG, "n must be positive (got %lld)", (long long)a.n);
+  LPM_TRY(check_count(a.n));
   if (!a.x || !a.y || !a.s1 || !a.area || !a.active)
     return set_error(LPM_ERR_ARG, "null input array");
   if (!a.out0 || (nout > 1 && !a.out1) || (nout > 2 && !a.out2) || (nout > 3 && !a.out3))
@@ -1885,7 +1885,9 @@ extern "C" int lpm_pse_interpolate_scalar(int64_t n, const double* x, const doub
   if (geometry == LPM_GEOMETRY_SPHERE && (!z || !qz))
     return lpm::set_error(LPM_ERR_ARG, "the sphere needs z and qz");
   if (!(eps > 0.0) || !(radius > 0.0)) return lpm::set_error(LPM_ERR_ARG, "eps and radius must be positive");
-  if (n <= 0 || !x || !y || !f || !area || !active) return lpm::set_error(LPM_ERR_ARG, "null input array");
+  LPM_TRY(lpm::check_count(n));
+  if (m > lpm::kMaxParticles - n) return lpm::set_error(LPM_ERR_ARG, "n + m is above 2^31 - 1 particles");
+  if (!x || !y || !f || !area || !active) return lpm::set_error(LPM_ERR_ARG, "null input array");
   // The query points become passive particles n .. n+m-1 (area 0, inactive), the targets.
   const int64_t nn = n + m;
   std::vector<double> cx(nn), cy(nn), cz(nn), cf(nn, 0.0), ca(nn, 0.0), co(nn, 0.0);

@@ -123,3 +123,28 @@ def test_operator_argument_checks(built_lib, call):
         fn()
     if isinstance(e.value, lg.LpmError):
         assert e.value.code == -1
+
+
+def test_particle_count_above_32_bit_indices_rejected(built_lib):
+    """n above 2^31 - 1 is refused before any array is read or any device is touched: the
+    source lists, sort values and curve orders hold 32-bit particle indices."""
+    L = built_lib.lib()
+    dp, ip = built_lib._dp, built_lib._ip
+    x, y, z, zeta, area, act = _tiny()
+    out = np.zeros(3)
+    big = 2 ** 31
+    rc = L.lpm_bve_velocity(big, dp(x), dp(y), dp(z), dp(zeta), dp(area), ip(act), 1.0, 1, 1, dp(out), dp(out),
+                            dp(out), 0)
+    assert rc == -1 and "32-bit" in L.lpm_last_error_string().decode()
+    rc = L.lpm_plane_velocity(big, dp(x), dp(y), dp(zeta), dp(area), ip(act), 0.0, 1, 1, dp(out), dp(out), 0)
+    assert rc == -1
+    h = ctypes.c_void_p()
+    rc = L.lpm_bve_solver_create(ctypes.byref(h), big, dp(x), dp(y), dp(z), dp(zeta), dp(area), ip(act), None, None,
+                                 None, 1.0, 0.0, 0)
+    assert rc == -1 and not h.value
+    rc = L.lpm_plane_solver_create(ctypes.byref(h), big, dp(x), dp(y), dp(zeta), dp(area), ip(act), None, None, 0.0,
+                                   0)
+    assert rc == -1 and not h.value
+    rc = L.lpm_pse_interpolate_scalar(3, dp(x), dp(y), dp(z), dp(zeta), dp(area), ip(act), 0.1, 1.0, 1, big - 2,
+                                      dp(x), dp(y), dp(z), dp(out), 0)
+    assert rc == -1
