@@ -3,7 +3,8 @@ numpy: a warp skips a 64-source tile when every target is farther than the tile'
 the reach from its centre, in unit directions (reach 7 eps / radius, great-circle kernels) or
 raw positions (reach 7 eps).  Every pair of a skipped tile must then have r = distance / eps
 >= 7 -- the great-circle distance is never shorter than the chord of the unit directions --
-so each kernel (a polynomial times exp(-r^2)) is below 1e-14 of its peak there."""
+so each kernel (a polynomial times exp(-r^2)) is below 1e-14 of its peak there.  Also the
+FP32C sweeps' angle series for eps <= 0.06 a, up to and beyond the same cutoff."""
 import numpy as np
 
 TILE = 64
@@ -57,3 +58,24 @@ def test_plane_cutoff_is_conservative():
         assert (d / eps).min() >= 7.0
         skipped += far.sum()
     assert skipped > 0
+
+
+def test_fp32c_angle_series_up_to_the_cutoff():
+    """The FP32C great-circle kernels take theta^2 = 4 asin^2(c/2) from the chord c by its
+    series in v = c^2 (pse_r2 with kPseAngleSeries, coefficients 1, 1/12, 1/90, 1/560, 1/3150
+    as the float constants the kernel holds) when eps <= 0.06 a.  Up to the cutoff r = 7 the
+    truncation stays below 1e-8 relative, under an FP32 ulp.  The series grows with v, so a
+    pair beyond the cutoff still has r^2 >= 49 (1 - 1e-8): its kernel stays negligible when a
+    warp evaluates it anyway."""
+    coef = np.array([3.1746032e-4, 1.7857143e-3, 1.1111111e-2, 8.3333336e-2, 1.0], dtype=np.float32).astype(np.float64)
+
+    def theta2(v):
+        return v * np.polyval(coef, v)
+
+    for eps_a in (0.005, 0.02, 0.04, 0.06):
+        v_cut = (2.0 * np.sin(3.5 * eps_a)) ** 2
+        v = np.linspace(v_cut * 1e-6, v_cut, 20001)
+        exact = 4.0 * np.arcsin(np.sqrt(v) / 2.0) ** 2
+        assert np.abs(theta2(v) / exact - 1.0).max() <= 1e-8
+        beyond = np.linspace(v_cut, 4.0, 20001)
+        assert (theta2(beyond) / eps_a ** 2).min() >= 49.0 * (1.0 - 1e-8)
