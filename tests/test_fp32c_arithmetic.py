@@ -368,3 +368,26 @@ def test_hilbert_keys_match_the_library(tmp_path):
     want = np.array(out.split(), dtype=np.uint64).reshape(-1, 2)
     assert np.array_equal(_hilbert([cells[:, 0], cells[:, 1], cells[:, 2]], 10), want[:, 0])
     assert np.array_equal(_hilbert([cells[:, 3], cells[:, 4]], 16), want[:, 1])
+
+
+def test_pse_kernel_constants_match_the_reference(oracle_mod):
+    """The FP32C PSE pair kernels (pse_pair): exp(-r^2) as 2^(r^2 x -1.4426950) (the
+    approximate 2^x modelled as the rounded value times 1 + delta, |delta| <= 2^-22), times the
+    K8 polynomial 40 - 40 r^2 + 10 r^4 - 2/3 r^6 or the K1 polynomial -20 + 20 r^2 - 5 r^4 +
+    r^6 / 3 in Horner form with the kernel's float constants.  Over 0 <= r <= 7.5 both are
+    within 1e-6 of their peak (3.1e-7 measured) of the oracle's bivariateLaplacianKernel8 and
+    bivariateFirstDerivativeKernel8 (src/PSEDirectSum.f90:622-634) times pi (the 1/pi is in
+    the finish kernel's scale)."""
+    rng = np.random.default_rng(9)
+    r = np.linspace(0.0, 7.5, 3001)
+    r2 = (r * r).astype(F)
+    ea = r2 * F(-1.4426950)
+    k = (np.exp2(ea.astype(D)) * (1.0 + rng.uniform(-1.0, 1.0, r.size) * 2.0 ** -22)).astype(F)
+    k8 = _fma(_fma(_fma(np.full(r.size, F(-0.6666666666666666)), r2, np.full(r.size, F(10))), r2,
+                   np.full(r.size, F(-40))), r2, np.full(r.size, F(40))) * k
+    k1 = _fma(_fma(_fma(np.full(r.size, F(0.33333334)), r2, np.full(r.size, F(-5))), r2, np.full(r.size, F(20))), r2,
+              np.full(r.size, F(-20))) * k
+    ref8 = np.array([oracle_mod.k8(float(v)) for v in r]) * np.pi
+    ref1 = np.array([oracle_mod.lib().lpmo_k1(float(v)) for v in r]) * np.pi
+    assert np.abs(k8.astype(D) - ref8).max() <= 1e-6 * 40.0
+    assert np.abs(k1.astype(D) - ref1).max() <= 1e-6 * 20.0
