@@ -1,8 +1,8 @@
 """The Fortran binding module (lpm-v2_gb300/fortran/lpm_gpu.f90) against the C header: every
 `bind(C, name=...)` interface names a function that include/lpm_gpu.h declares, with the same
 number of arguments, each of the C parameter's kind and passing.  The image has no Fortran
-compiler, so this is the check that the shim a
-maintainer adds to the reference still matches the library."""
+compiler, so this is the check that the shim a maintainer adds to the reference still
+matches the library."""
 import re
 from pathlib import Path
 
