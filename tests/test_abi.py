@@ -148,3 +148,54 @@ def test_particle_count_above_32_bit_indices_rejected(built_lib):
     rc = L.lpm_pse_interpolate_scalar(3, dp(x), dp(y), dp(z), dp(zeta), dp(area), ip(act), 0.1, 1.0, 1, big - 2,
                                       dp(x), dp(y), dp(z), dp(out), 0)
     assert rc == -1
+
+
+def _c_prototypes():
+    """name -> (return type, [(base type, pointer depth)]) for every function include/*.h declares."""
+    out = {}
+    for h in sorted(INCLUDE.glob("*.h")):
+        text = re.sub(r"/\*.*?\*/", " ", h.read_text(), flags=re.S)
+        text = re.sub(r"^\s*#.*$", " ", text, flags=re.M)
+        for m in re.finditer(r"([\w\s\*]+?)\b(lpm_\w+)\s*\(([^;{]*?)\)\s*;", text, re.S):
+            params = m.group(3).strip()
+            plist = []
+            if params not in ("", "void"):
+                for p in params.split(","):
+                    p = p.replace("const", " ").strip()
+                    plist.append((p.replace("*", " ").split()[0], p.count("*")))
+            ret = " ".join(m.group(1).split()[-2:]) if "*" in m.group(1) else m.group(1).split()[-1]
+            out[m.group(2)] = (ret.replace("const", "").strip(), plist)
+    return out
+
+
+def test_ctypes_signatures_match_the_headers(built_lib):
+    """The Python binding's argtypes and restypes against the C prototypes, parameter by
+    parameter: int64_t <-> c_int64, int <-> c_int, double <-> c_double, double* / int32_t* /
+    int64_t* <-> POINTER of the same, a handle or void* <-> c_void_p, a handle** <->
+    POINTER(c_void_p).  ctypes converts whatever it is told, so a wrong entry here would pass
+    a wrong value rather than fail."""
+    lg = built_lib
+    scalar = {"int64_t": ctypes.c_int64, "int": ctypes.c_int, "double": ctypes.c_double}
+    pointee = {"double": ctypes.c_double, "int32_t": ctypes.c_int32, "int64_t": ctypes.c_int64, "int": ctypes.c_int}
+    protos = _c_prototypes()
+    assert set(lg._SIGNATURES) <= set(protos), set(lg._SIGNATURES) - set(protos)
+    checked = 0
+    for name, argtypes in lg._SIGNATURES.items():
+        ret, params = protos[name]
+        assert len(argtypes) == len(params), name
+        for k, (t, (base, depth)) in enumerate(zip(argtypes, params)):
+            if depth == 0:
+                want = scalar[base]
+            elif depth == 1 and (base.startswith("lpm_") or base == "void"):
+                want = ctypes.c_void_p
+            elif depth == 1:
+                want = ctypes.POINTER(pointee[base])
+            else:
+                want = ctypes.POINTER(ctypes.c_void_p)
+            assert t is want, f"{name} argument {k + 1}: {t} for C {base}{'*' * depth}"
+            checked += 1
+        rt = lg._RESTYPES.get(name, ctypes.c_int)
+        want_rt = {"int": ctypes.c_int, "int64_t": ctypes.c_int64, "double": ctypes.c_double, "void": None,
+                   "char*": ctypes.c_char_p}[ret.replace(" ", "")]
+        assert rt is want_rt, f"{name} returns {ret}, bound as {rt}"
+    assert checked > 300
