@@ -399,16 +399,17 @@ def test_pse_kernel_constants_match_the_reference(oracle_mod):
 _SERIES = [F(3.1746032e-4), F(1.7857143e-3), F(1.1111111e-2), F(8.3333336e-2), F(1.0)]
 
 
-def _pse_fp32c_block(T, fT, P, fP, A, eps_a, ang, kernel, rng):
+def _pse_fp32c_block(T, fT, P, fP, A, eps_a, ang, kernel, rng, op="lap"):
     """The sphere PSE Laplacian sweep (pse_rel_prep_kernel, pse_rel_sweep_kernel with 128
     threads x 4 targets, each warp 128 consecutive curve-ordered targets) for one CTA: groups
     of 32 sources in curve order with the compact / far / near choice of the BVE sweep; a warp
     skips a group when every target is farther than R + 7 eps / a from its centroid; the angle
     from the chord by the asin^2 series ("series"), by 4 asin^2(c/2) ("asin") or the chord
     itself ("chord"); exp(-r^2) as 2^x; the K8 polynomial or the Gaussian; (f_j - f_i) from
-    hi/lo parts; FP32 sums per 256-source tile merged by TwoSum.  The tile culling is left out:
-    it only skips tiles whose every group the warps skip as well.  Returns the FP64 sums
-    (before the 1 / (pi eps^4) scale) and the branch counts."""
+    hi/lo parts; FP32 sums per 256-source tile merged by TwoSum.  op "grad" is the gradient
+    sweep instead: the K1 polynomial and (f_j + f_i) A_j K1 d summed per component.  The tile
+    culling is left out: it only skips tiles whose every group the warps skip as well.
+    Returns the FP64 sums (before the finish kernel's scale) and the branch counts."""
     tgroup, tile = 32, 256
     nt = len(T)
     th, tl = zip(*(_split2(T[:, k]) for k in range(3)))
@@ -417,9 +418,10 @@ def _pse_fp32c_block(T, fT, P, fP, A, eps_a, ang, kernel, rng):
     c_cut = F(7.0 * eps_a)
     warps = [np.arange(w, min(w + 128, nt)) for w in range(0, nt, 128)]
     stats = dict(skipped=0, far=0, near=0)
-    hi, lo = np.zeros(nt, F), np.zeros(nt, F)
+    nc = 3 if op == "grad" else 1
+    hi, lo = np.zeros((nt, nc), F), np.zeros((nt, nc), F)
     for t0 in range(0, len(P), tile):
-        acc = np.zeros(nt, F)
+        acc = np.zeros((nt, nc), F)
         for g0 in range(t0, min(t0 + tile, len(P)), tgroup):
             Q = P[g0:g0 + tgroup]
             o = Q.mean(0)
@@ -459,17 +461,29 @@ def _pse_fp32c_block(T, fT, P, fP, A, eps_a, ang, kernel, rng):
                 else:
                     r2 = v * ks2
                 ex = (np.exp2((r2 * F(-1.4426950)).astype(D)) * (1.0 + rng.uniform(-1, 1, r2.shape) * 2.0 ** -22)).astype(F)
-                if kernel == "k8":
+                if op == "grad":
+                    poly = _fma(_fma(_fma(np.full(r2.shape, F(0.33333334)), r2, np.full(r2.shape, F(-5))), r2,
+                                     np.full(r2.shape, F(20))), r2, np.full(r2.shape, F(-20)))
+                    ex = poly * ex
+                elif kernel == "k8":
                     poly = _fma(_fma(_fma(np.full(r2.shape, F(-0.6666666666666666)), r2, np.full(r2.shape, F(10))), r2,
                                      np.full(r2.shape, F(-40))), r2, np.full(r2.shape, F(40)))
                     ex = poly * ex
                 wk = ar[None, :] * ex
+                if op == "grad":
+                    wf = (fh[None, :] + fth[w][:, None]) * wk
+                    for j in range(d.shape[1]):
+                        for k in range(3):
+                            acc[w, k] = _fma(wf[:, j], d[:, j, k], acc[w, k])
+                    continue
                 df = (fh[None, :] - fth[w][:, None]) + (fl[None, :] - ftl[w][:, None])
                 for j in range(d.shape[1]):
-                    acc[w] = _fma(df[:, j], wk[:, j], acc[w])
-        hi, e = _two_sum(hi, acc)
-        lo = lo + e
-    return hi.astype(D) + lo.astype(D), stats
+                    acc[w, 0] = _fma(df[:, j], wk[:, j], acc[w, 0])
+        for k in range(nc):
+            hi[:, k], e = _two_sum(hi[:, k], acc[:, k])
+            lo[:, k] = lo[:, k] + e
+    out = hi.astype(D) + lo.astype(D)
+    return (out if op == "grad" else out[:, 0]), stats
 
 
 @pytest.mark.parametrize("kernel,ang,eps", [("k8", "asin", None), ("k8", "series", 0.05), ("gauss", "chord", None)])
@@ -500,4 +514,30 @@ def test_pse_fp32c_arithmetic_meets_the_bar(built_lib, oracle_mod, kernel, ang, 
     oker = oracle_mod.PSE_K8_GEODESIC if kernel == "k8" else oracle_mod.PSE_GAUSS_CHORD
     ref = oracle_mod.pse_laplacian(x, y, z, f, area, active, eps, 1.0, kernel=oker)
     err = np.abs(got - ref[tg]).max() / np.abs(ref).max()
+    assert err <= 1e-4, err
+
+
+def test_pse_gradient_fp32c_arithmetic_meets_the_bar(built_lib, oracle_mod):
+    """The sphere PSE gradient (PSESphereGradientAtParticles, PSEDirectSum.f90:220-267) the
+    same way at cubed nest 5 with eps = h^0.5 (0.22: the asin angle), f = Y54 + 1e-3 noise:
+    the sums of (f_j + f_i) A_j K1 d projected with I - x_i x_i^T and scaled by
+    a / (pi eps^4), as pse_grad_finish_kernel does, are within 1e-4 of max|grad f| of the
+    oracle (1.6e-6 measured)."""
+    import workloads
+    c = workloads.config_pse_cubed(5)
+    x, y, z, f, area, active = c["x"], c["y"], c["z"], c["f"], c["area"], c["active"]
+    eps = c["mesh"].max_edge_length ** 0.5
+    P = np.stack([x, y, z], 1)
+    U = P / np.linalg.norm(P, axis=1)[:, None]
+    order = np.argsort(_hilbert30(P), kind="stable")
+    src = order[active[order] != 0]
+    mid = (len(order) // 2) // 512 * 512
+    tg = order[mid:mid + 512]
+    s, stats = _pse_fp32c_block(U[tg], f[tg], U[src], f[src], area[src], eps, "asin", "k1",
+                                np.random.default_rng(11), op="grad")
+    assert min(stats.values()) > 0, stats
+    xt = P[tg]
+    g = (s - xt * (xt * s).sum(1)[:, None]) / (np.pi * eps ** 4)
+    ref = np.stack(oracle_mod.pse_sphere_gradient(x, y, z, f, area, active, eps, 1.0), 1)
+    err = np.abs(g - ref[tg]).max() / np.abs(ref).max()
     assert err <= 1e-4, err
