@@ -407,13 +407,18 @@ def _pse_fp32c_block(T, fT, P, fP, A, eps_a, ang, kernel, rng, op="lap"):
     from the chord by the asin^2 series ("series"), by 4 asin^2(c/2) ("asin") or the chord
     itself ("chord"); exp(-r^2) as 2^x; the K8 polynomial or the Gaussian; (f_j - f_i) from
     hi/lo parts; FP32 sums per 256-source tile merged by TwoSum.  op "grad" is the gradient
-    sweep instead: the K1 polynomial and (f_j + f_i) A_j K1 d summed per component.  The tile
+    sweep instead: the K1 polynomial and (f_j + f_i) A_j K1 d summed per component; op "div"
+    the divergence sweep on 128-source tiles: fT and fP hold the vector fields, and
+    (P_i d).(V_j + V_i) A_j K1 is summed with P_i d = d - (|d|^2 / 2) p_i.  The tile
     culling is left out: it only skips tiles whose every group the warps skip as well.
     Returns the FP64 sums (before the finish kernel's scale) and the branch counts."""
-    tgroup, tile = 32, 256
+    tgroup, tile = 32, (128 if op == "div" else 256)
     nt = len(T)
     th, tl = zip(*(_split2(T[:, k]) for k in range(3)))
-    fth, ftl = _split2(fT)
+    if op == "div":
+        vt = fT.astype(F)
+    else:
+        fth, ftl = _split2(fT)
     ks2 = F(1.0 / (eps_a * eps_a))
     c_cut = F(7.0 * eps_a)
     warps = [np.arange(w, min(w + 128, nt)) for w in range(0, nt, 128)]
@@ -432,7 +437,10 @@ def _pse_fp32c_block(T, fT, P, fP, A, eps_a, ang, kernel, rng, op="lap"):
             sh, sl = np.empty((len(Q), 3), F), np.empty((len(Q), 3), F)
             for k in range(3):
                 sh[:, k], sl[:, k] = (_rel2_fast if compact else _rel2)(*_split2(Q[:, k]), oh[k], ol[k])
-            fh, fl = _split2(fP[g0:g0 + tgroup])
+            if op == "div":
+                vs = fP[g0:g0 + tgroup].astype(F)
+            else:
+                fh, fl = _split2(fP[g0:g0 + tgroup])
             ar = A[g0:g0 + tgroup].astype(F)
             t = np.stack([(th[k] - oh[k]) + (tl[k] - ol[k]) for k in range(3)], 1)
             n2 = _fma(t[:, 2], t[:, 2], _fma(t[:, 1], t[:, 1], t[:, 0] * t[:, 0]))
@@ -461,7 +469,7 @@ def _pse_fp32c_block(T, fT, P, fP, A, eps_a, ang, kernel, rng, op="lap"):
                 else:
                     r2 = v * ks2
                 ex = (np.exp2((r2 * F(-1.4426950)).astype(D)) * (1.0 + rng.uniform(-1, 1, r2.shape) * 2.0 ** -22)).astype(F)
-                if op == "grad":
+                if op in ("grad", "div"):
                     poly = _fma(_fma(_fma(np.full(r2.shape, F(0.33333334)), r2, np.full(r2.shape, F(-5))), r2,
                                      np.full(r2.shape, F(20))), r2, np.full(r2.shape, F(-20)))
                     ex = poly * ex
@@ -470,6 +478,14 @@ def _pse_fp32c_block(T, fT, P, fP, A, eps_a, ang, kernel, rng, op="lap"):
                                      np.full(r2.shape, F(-40))), r2, np.full(r2.shape, F(40)))
                     ex = poly * ex
                 wk = ar[None, :] * ex
+                if op == "div":
+                    cv = v * F(-0.5)
+                    gp = [_fma(cv, np.broadcast_to(th[k][w][:, None], cv.shape), d[:, :, k]) for k in range(3)]
+                    wv = [vs[None, :, k] + vt[w][:, None, k] for k in range(3)]
+                    dot = _fma(gp[2], wv[2], _fma(gp[1], wv[1], gp[0] * wv[0]))
+                    for j in range(d.shape[1]):
+                        acc[w, 0] = _fma(dot[:, j], wk[:, j], acc[w, 0])
+                    continue
                 if op == "grad":
                     wf = (fh[None, :] + fth[w][:, None]) * wk
                     for j in range(d.shape[1]):
@@ -540,4 +556,28 @@ def test_pse_gradient_fp32c_arithmetic_meets_the_bar(built_lib, oracle_mod):
     g = (s - xt * (xt * s).sum(1)[:, None]) / (np.pi * eps ** 4)
     ref = np.stack(oracle_mod.pse_sphere_gradient(x, y, z, f, area, active, eps, 1.0), 1)
     err = np.abs(g - ref[tg]).max() / np.abs(ref).max()
+    assert err <= 1e-4, err
+
+
+def test_pse_divergence_fp32c_arithmetic_meets_the_bar(built_lib, oracle_mod):
+    """The sphere PSE divergence (PSESphereDivergenceAtParticles, PSEDirectSum.f90:537-579)
+    the same way at cubed nest 5 with eps = h^0.5, V = the surface gradient of Y54: the sums
+    scaled by a / (pi eps^4) are within 1e-4 of max|div V| of the oracle (6.2e-7 measured)."""
+    import workloads
+    c = workloads.config_pse_cubed(5)
+    x, y, z, area, active = c["x"], c["y"], c["z"], c["area"], c["active"]
+    V = np.stack(workloads.y54_surface_gradient(x, y, z), 1)
+    eps = c["mesh"].max_edge_length ** 0.5
+    P = np.stack([x, y, z], 1)
+    U = P / np.linalg.norm(P, axis=1)[:, None]
+    order = np.argsort(_hilbert30(P), kind="stable")
+    src = order[active[order] != 0]
+    mid = (len(order) // 2) // 512 * 512
+    tg = order[mid:mid + 512]
+    s, stats = _pse_fp32c_block(U[tg], V[tg], U[src], V[src], area[src], eps, "asin", "k1",
+                                np.random.default_rng(12), op="div")
+    assert min(stats.values()) > 0, stats
+    got = s / (np.pi * eps ** 4)
+    ref = oracle_mod.pse_sphere_divergence(x, y, z, V[:, 0], V[:, 1], V[:, 2], area, active, eps, 1.0)
+    err = np.abs(got - ref[tg]).max() / np.abs(ref).max()
     assert err <= 1e-4, err
