@@ -19,9 +19,9 @@ is rounded twice, which can differ from the fused result by one ulp in rare ties
 approximate reciprocal is the rounded reciprocal times 1 + delta, |delta| <= 2^-23, drawn
 from a seeded generator.
 
-The planar sweep (plane_rel_prep_kernel, plane_rel_sweep_kernel) and the sphere PSE
-Laplacian sweep (pse_rel_prep_kernel, pse_rel_sweep_kernel, with its group cutoff) are
-restated the same way, and the PSE pair kernels' constants are checked against the
+The planar sweep (plane_rel_prep_kernel, plane_rel_sweep_kernel) and the sphere PSE sweeps
+(pse_rel_prep_kernel, pse_rel_sweep_kernel with its group cutoff: Laplacian, gradient and
+divergence) are restated the same way, and the PSE pair kernels' constants are checked against the
 reference's kernel functions.
 
 This pins the precision design, not the kernels: the GPU tests check the CUDA path itself
