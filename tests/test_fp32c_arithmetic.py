@@ -21,7 +21,8 @@ from a seeded generator.
 
 The planar sweep (plane_rel_prep_kernel, plane_rel_sweep_kernel) and the sphere PSE sweeps
 (pse_rel_prep_kernel, pse_rel_sweep_kernel with its group cutoff: Laplacian, gradient and
-divergence) are restated the same way, and the PSE pair kernels' constants are checked against the
+divergence) and the sphere stream functions (stream_rel_prep_kernel, stream_rel_sweep_kernel,
+with the device logarithm) are restated the same way, and the PSE pair kernels' constants are checked against the
 reference's kernel functions.
 
 This pins the precision design, not the kernels: the GPU tests check the CUDA path itself
@@ -581,3 +582,93 @@ def test_pse_divergence_fp32c_arithmetic_meets_the_bar(built_lib, oracle_mod):
     ref = oracle_mod.pse_sphere_divergence(x, y, z, V[:, 0], V[:, 1], V[:, 2], area, active, eps, 1.0)
     err = np.abs(got - ref[tg]).max() / np.abs(ref).max()
     assert err <= 1e-4, err
+
+
+def _stream_fp32c_block(T, ct, groups, s_abs):
+    """The sphere stream-function sweep (stream_rel_prep_kernel, stream_rel_sweep_kernel with
+    128 threads x 4 targets) for one CTA: the BVE sweep's groups and records with the two
+    strengths S = -zeta A / (4 pi); per warp and group the expanded far form h = q/2 with
+    ln q = ln h + ln 2, the compact-near form or the two-float near form with q = |d|^2 -
+    c_i - c_j (a self pair: d = 0, ln 1); the device logarithm (the table sequence of
+    ln_q2_shift, emulated as in test_ln_table); FP32 partials flushed into TwoSum pairs every
+    32 sources.  Returns the FP64 sums of S ln q for both strengths."""
+    from test_ln_table import ln_q_emulated
+    nt = len(T)
+    th, tl = zip(*(_split2(T[:, k]) for k in range(3)))
+    nc = (-ct).astype(F) + F(2.0 ** -100)
+    warps = []
+    for wi in range(THREADS // 32):
+        idx = np.array([wi * 32 + lane + k * THREADS for k in range(4) for lane in range(32)])
+        warps.append(idx[idx < nt])
+    stats = dict(far=0, compact_near=0, near=0)
+    hi, lo = np.zeros((nt, 2), F), np.zeros((nt, 2), F)
+    for gi, g in enumerate(groups):
+        sa = s_abs[gi * GROUP:gi * GROUP + len(g["S"])]
+        t = np.stack([(th[k] - g["oh"][k]) + (tl[k] - g["ol"][k]) for k in range(3)], 1)
+        n2 = _fma(t[:, 2], t[:, 2], _fma(t[:, 1], t[:, 1], t[:, 0] * t[:, 0]))
+        lim = max((F(3) * g["R"]) * (F(3) * g["R"]), F(2.0 ** -100))
+        for w in warps:
+            tw, m = t[w], len(w)
+            if not (~(n2[w] > lim)).any():
+                stats["far"] += 1
+                c2 = _fma(tw[:, 2], tw[:, 2], _fma(tw[:, 1], tw[:, 1], _fma(tw[:, 0], tw[:, 0], nc[w]))) * F(0.5)
+                h = c2[:, None] + g["b"][None, :]
+                for k in range(3):
+                    h = _fma(tw[:, k:k + 1], g["nsh"][None, :, k], h)
+                lg = ln_q_emulated(h, -1)
+            else:
+                if g["compact"]:
+                    stats["compact_near"] += 1
+                    d = tw[:, None, :] + g["nsh"][None, :, :]
+                else:
+                    stats["near"] += 1
+                    tt = [_rel2(th[k][w], tl[k][w], g["oh"][k], g["ol"][k]) for k in range(3)]
+                    d = np.stack([(tt[k][0][:, None] + g["nsh"][None, :, k]) + (tt[k][1][:, None] + g["nsl"][None, :, k])
+                                  for k in range(3)], 2)
+                u = _fma(d[:, :, 2], d[:, :, 2], _fma(d[:, :, 1], d[:, :, 1], d[:, :, 0] * d[:, :, 0]))
+                q = u + (nc[w][:, None] + g["ncj"][None, :])
+                q = np.where(u != 0, np.maximum(q, F(2.0 ** -126)), F(1))
+                lg = ln_q_emulated(q)
+            ar, aa = np.zeros(m, F), np.zeros(m, F)
+            for j in range(lg.shape[1]):
+                ar = _fma(np.full(m, g["S"][j], F), lg[:, j], ar)
+                aa = _fma(np.full(m, sa[j], F), lg[:, j], aa)
+                if (j + 1) % 32 == 0 or j + 1 == lg.shape[1]:
+                    for k, acc in enumerate((ar, aa)):
+                        hi[w, k], e = _two_sum(hi[w, k], acc)
+                        lo[w, k] = lo[w, k] + e
+                    ar, aa = np.zeros(m, F), np.zeros(m, F)
+    return hi.astype(D) + lo.astype(D), stats
+
+
+def test_sphere_stream_fp32c_arithmetic_meets_the_bar(case, oracle_mod):
+    """The sphere stream functions (SetStreamFunctionsOnMesh, src/SphereBVE.f90:445-485) the
+    same way at icosahedral nest 5 (RH4 + Gaussian vortex, absolute vorticity zeta + 2 Omega z),
+    the CTA of 512 targets at the middle of the particle list: with the finish kernel's
+    constant term -ln(a^2 / 2) / (4 pi) (sum_j zeta_j A_j - the target's own) added in FP64,
+    both are within 1e-6 of max|psi| of the oracle (2.3e-7 relative, 5.4e-8 absolute
+    vorticity measured)."""
+    P = np.stack([case["x"], case["y"], case["z"]], 1)
+    n = len(P)
+    zeta, area, active = case["zeta"], case["area"], case["active"]
+    absv = zeta + 2.0 * case["omega"] * case["z"]
+    c = np.einsum("ij,ij->i", P, P) - 1.0
+    src = np.nonzero(active)[0]
+    src = src[np.argsort(_hilbert30(P[src]), kind="stable")]
+    k4 = -1.0 / (4.0 * np.pi)
+    groups = _groups(P[src], c[src], zeta[src] * area[src] * k4)
+    s_abs = (absv[src] * area[src] * k4).astype(F)
+    ib = n // 2
+    ie = ib + THREADS * 4
+    T = P[ib:ie]
+    sums, stats = _stream_fp32c_block(T, c[ib:ie], groups, s_abs)
+    assert min(stats.values()) > 0, stats
+    own = np.where(active[ib:ie] != 0, 1.0, 0.0)
+    k_const = -np.log(0.5) / (4.0 * np.pi)
+    tot = [(zeta[src] * area[src]).sum(), (absv[src] * area[src]).sum()]
+    own_w = [own * zeta[ib:ie] * area[ib:ie], own * absv[ib:ie] * area[ib:ie]]
+    got = [sums[:, k] + k_const * (tot[k] - own_w[k]) for k in range(2)]
+    ref = oracle_mod.bve_stream(case["x"], case["y"], case["z"], zeta, absv, area, active, ib=ib, ie=ie)
+    for k in range(2):
+        err = np.abs(got[k] - ref[k]).max() / np.abs(ref[k]).max()
+        assert err <= 1e-6, err
