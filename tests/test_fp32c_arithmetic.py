@@ -21,8 +21,8 @@ from a seeded generator.
 
 The planar sweep (plane_rel_prep_kernel, plane_rel_sweep_kernel) and the sphere PSE sweeps
 (pse_rel_prep_kernel, pse_rel_sweep_kernel with its group cutoff: Laplacian, gradient and
-divergence) and the sphere stream functions (stream_rel_prep_kernel, stream_rel_sweep_kernel,
-with the device logarithm) are restated the same way, and the PSE pair kernels' constants are checked against the
+divergence) and the stream functions (stream_rel_sweep_kernel and
+plane_stream_rel_sweep_kernel, with the device logarithm) are restated the same way, and the PSE pair kernels' constants are checked against the
 reference's kernel functions.
 
 This pins the precision design, not the kernels: the GPU tests check the CUDA path itself
@@ -672,3 +672,89 @@ def test_sphere_stream_fp32c_arithmetic_meets_the_bar(case, oracle_mod):
     for k in range(2):
         err = np.abs(got[k] - ref[k]).max() / np.abs(ref[k]).max()
         assert err <= 1e-6, err
+
+
+def _plane_stream_fp32c_block(T, P, S):
+    """The planar stream-function sweep (plane_rel_prep_kernel with S = omega A / (4 pi),
+    plane_stream_rel_sweep_kernel with 128 threads x 4 targets): per target and group the
+    centring shift k, the exponent of max(|t - o|^2, R^2) clamped to [2^-100, 2^100], with
+    k S_g carried exactly in its own TwoSum pair (S_g the group's total of the float
+    strengths, as a hi/lo pair); the terms S_j (ln u_j - k ln 2) by the device logarithm,
+    far groups summed whole, near groups (the two-float form; a self pair takes u -> 1)
+    flushed every 16 sources.  Returns sum_j S_j ln u_j in FP64, as the sweep writes it."""
+    from test_ln_table import ln_q_emulated
+    nt = len(T)
+    (txh, txl), (tyh, tyl) = _split2(T[:, 0]), _split2(T[:, 1])
+    warps = []
+    for wi in range(THREADS // 32):
+        idx = np.array([wi * 32 + lane + k * THREADS for k in range(4) for lane in range(32)])
+        warps.append(idx[idx < nt])
+    stats = dict(far=0, near=0)
+    hs, ls, hk, lk = (np.zeros(nt, F) for _ in range(4))
+    tiny, huge = F(2.0 ** -100), F(2.0 ** 100)
+    for g0 in range(0, len(P), GROUP):
+        Q = P[g0:g0 + GROUP]
+        s = S[g0:g0 + GROUP].astype(F)
+        o = Q.mean(0)
+        R = np.sqrt(((Q - o) ** 2).sum(1)).astype(F).max()
+        sgh, sgl = _split2(np.array([s.astype(D).sum()]))
+        (oxh, oxl), (oyh, oyl) = _split2(o[:1]), _split2(o[1:])
+        sxh, sxl = _rel2(*_split2(Q[:, 0]), oxh, oxl)
+        syh, syl = _rel2(*_split2(Q[:, 1]), oyh, oyl)
+        tx, ty = (txh - oxh) + (txl - oxl), (tyh - oyh) + (tyl - oyl)
+        n2 = _fma(ty, ty, tx * tx)
+        r2 = R * R
+        lim = max(F(9) * r2, tiny)
+        cen = np.minimum(np.maximum(np.maximum(n2, r2), tiny), huge)
+        k = ((cen.view(np.int32).astype(np.int64) - 0x3F3504F3) >> 23).astype(F)
+        ph = sgh * k
+        pe = _fma(np.full(nt, sgh[0]), k, -ph)
+        hk, e = _two_sum(hk, ph)
+        lk = _fma(np.full(nt, sgl[0]), k, (lk + e) + pe)
+        for w in warps:
+            sh = k[w][:, None].astype(D)
+            if not (~(n2[w] > lim)).any():
+                stats["far"] += 1
+                dx = tx[w][:, None] - sxh[None, :]
+                dy = ty[w][:, None] - syh[None, :]
+                lg = ln_q_emulated(_fma(dy, dy, dx * dx), sh)
+                flush = GROUP
+            else:
+                stats["near"] += 1
+                ax, bx = _rel2(txh[w], txl[w], oxh, oxl)
+                ay, by = _rel2(tyh[w], tyl[w], oyh, oyl)
+                dx = (ax[:, None] - sxh[None, :]) + (bx[:, None] - sxl[None, :])
+                dy = (ay[:, None] - syh[None, :]) + (by[:, None] - syl[None, :])
+                u = _fma(dy, dy, dx * dx)
+                lg = ln_q_emulated(np.where(u != 0, np.maximum(u, F(2.0 ** -126)), F(1)), sh)
+                flush = 16
+            acc = np.zeros(len(w), F)
+            for j in range(lg.shape[1]):
+                acc = _fma(np.full(len(w), s[j], F), lg[:, j], acc)
+                if (j + 1) % flush == 0 or j + 1 == lg.shape[1]:
+                    hs[w], e = _two_sum(hs[w], acc)
+                    ls[w] = ls[w] + e
+                    acc = np.zeros(len(w), F)
+    return (hs.astype(D) + ls.astype(D)) + np.log(2.0) * (hk.astype(D) + lk.astype(D)), stats
+
+
+def test_plane_stream_fp32c_arithmetic_meets_the_bar(built_lib, oracle_mod):
+    """The planar stream function (SetStreamFunctionOnMesh, src/PlanarIncompressible.f90:
+    470-505) the same way at quad nest 6 on [-4, 4]^2 (colliding dipoles), the 512 targets of
+    the CTA at the middle of the particle list: within 1e-6 of max|psi| over every target of
+    the oracle (7.9e-8 measured; 1.7e-6 of that block's own max|psi|, a tenth of the
+    largest)."""
+    import workloads
+    c = workloads.config_colliding_dipoles(6)
+    x, y, omega, area, active = c["x"], c["y"], c["omega"], c["area"], c["active"]
+    n = len(x)
+    src = np.nonzero(active)[0]
+    src = src[np.argsort(_hilbert2d(x[src], y[src]), kind="stable")]
+    ib = n // 2
+    ie = ib + THREADS * 4
+    got, stats = _plane_stream_fp32c_block(np.stack([x[ib:ie], y[ib:ie]], 1), np.stack([x[src], y[src]], 1),
+                                           (omega[src] * area[src] / (4.0 * np.pi)).astype(F))
+    assert min(stats.values()) > 0, stats
+    full = oracle_mod.plane_stream(x, y, omega, area, active)
+    err = np.abs(got - full[ib:ie]).max() / np.abs(full).max()
+    assert err <= 1e-6, err
