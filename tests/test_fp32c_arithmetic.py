@@ -19,7 +19,7 @@ is rounded twice, which can differ from the fused result by one ulp in rare ties
 approximate reciprocal is the rounded reciprocal times 1 + delta, |delta| <= 2^-23, drawn
 from a seeded generator.
 
-The planar sweep (plane_rel_prep_kernel, plane_rel_sweep_kernel) and the sphere PSE sweeps
+The planar sweeps (plane_rel_sweep_kernel, plane_pse_rel_sweep_kernel) and the sphere PSE sweeps
 (pse_rel_prep_kernel, pse_rel_sweep_kernel with its group cutoff: Laplacian, gradient and
 divergence) and the stream functions (stream_rel_sweep_kernel and
 plane_stream_rel_sweep_kernel, with the device logarithm) are restated the same way, and the PSE pair kernels' constants are checked against the
@@ -758,3 +758,85 @@ def test_plane_stream_fp32c_arithmetic_meets_the_bar(built_lib, oracle_mod):
     full = oracle_mod.plane_stream(x, y, omega, area, active)
     err = np.abs(got - full[ib:ie]).max() / np.abs(full).max()
     assert err <= 1e-6, err
+
+
+def _plane_pse_fp32c_block(T, fT, P, fP, A, eps, kernel, rng):
+    """The planar PSE Laplacian sweep (plane_pse_rel_prep_kernel, plane_pse_rel_sweep_kernel
+    with 128 threads x 4 targets, each warp 128 consecutive curve-ordered targets): groups of
+    32 sources; a warp skips a group beyond R + 7 eps, takes the far form d = t_hi - s_hi
+    when every target is beyond 3R and the two-float form otherwise; r^2 = |d|^2 / eps^2,
+    exp(-r^2) as 2^x, the K8 polynomial or the Gaussian, (f_j - f_i) from hi/lo parts; FP32
+    sums per 256-source tile merged by TwoSum (the tile culling left out, as for the sphere).
+    Returns the FP64 sums before the 1 / (pi eps^4) scale."""
+    nt = len(T)
+    (txh, txl), (tyh, tyl) = _split2(T[:, 0]), _split2(T[:, 1])
+    fth, ftl = _split2(fT)
+    ks2, c_cut = F(1.0 / (eps * eps)), F(7.0 * eps)
+    warps = [np.arange(w, min(w + 128, nt)) for w in range(0, nt, 128)]
+    stats = dict(skipped=0, far=0, near=0)
+    hi, lo = np.zeros(nt, F), np.zeros(nt, F)
+    for t0 in range(0, len(P), 256):
+        acc = np.zeros(nt, F)
+        for g0 in range(t0, min(t0 + 256, len(P)), 32):
+            Q = P[g0:g0 + 32]
+            o = Q.mean(0)
+            R = np.sqrt(((Q - o) ** 2).sum(1)).astype(F).max()
+            (oxh, oxl), (oyh, oyl) = _split2(o[:1]), _split2(o[1:])
+            sxh, sxl = _rel2(*_split2(Q[:, 0]), oxh, oxl)
+            syh, syl = _rel2(*_split2(Q[:, 1]), oyh, oyl)
+            fh, fl = _split2(fP[g0:g0 + 32])
+            ar = A[g0:g0 + 32].astype(F)
+            tx, ty = (txh - oxh) + (txl - oxl), (tyh - oyh) + (tyl - oyl)
+            n2 = _fma(ty, ty, tx * tx)
+            reach = R + c_cut
+            for w in warps:
+                if not (n2[w] < reach * reach).any():
+                    stats["skipped"] += 1
+                    continue
+                if not (n2[w] < (F(3) * R) * (F(3) * R)).any():
+                    stats["far"] += 1
+                    dx = tx[w][:, None] - sxh[None, :]
+                    dy = ty[w][:, None] - syh[None, :]
+                else:
+                    stats["near"] += 1
+                    ax, bx = _rel2(txh[w], txl[w], oxh, oxl)
+                    ay, by = _rel2(tyh[w], tyl[w], oyh, oyl)
+                    dx = (ax[:, None] - sxh[None, :]) + (bx[:, None] - sxl[None, :])
+                    dy = (ay[:, None] - syh[None, :]) + (by[:, None] - syl[None, :])
+                r2 = _fma(dy, dy, dx * dx) * ks2
+                ex = (np.exp2((r2 * F(-1.4426950)).astype(D)) * (1.0 + rng.uniform(-1, 1, r2.shape) * 2.0 ** -22)).astype(F)
+                if kernel == "k8":
+                    ex = _fma(_fma(_fma(np.full(r2.shape, F(-0.6666666666666666)), r2, np.full(r2.shape, F(10))), r2,
+                                   np.full(r2.shape, F(-40))), r2, np.full(r2.shape, F(40))) * ex
+                df = (fh[None, :] - fth[w][:, None]) + (fl[None, :] - ftl[w][:, None])
+                wk = ar[None, :] * ex
+                for j in range(dx.shape[1]):
+                    acc[w] = _fma(df[:, j], wk[:, j], acc[w])
+        hi, e = _two_sum(hi, acc)
+        lo = lo + e
+    return hi.astype(D) + lo.astype(D), stats
+
+
+@pytest.mark.parametrize("kernel", ["k8", "gauss"])
+def test_plane_pse_fp32c_arithmetic_meets_the_bar(built_lib, oracle_mod, kernel):
+    """The planar PSE Laplacian (PSEPlaneLaplacianAtParticles, PSEDirectSum.f90:467-500, and
+    the Gaussian of the chord) the same way on the quad mesh of [-4, 4]^2 at nest 5 with
+    eps = h^0.75, f = exp(-|x|^2) cos 2x + 1e-3 noise, the 512 curve-ordered targets at the
+    middle: within 1e-4 of max|L| of the oracle, with groups skipped, far and near (1.0e-6
+    K8, 4.9e-7 Gaussian measured)."""
+    mesh = built_lib.PolyMesh2d(built_lib.QUAD_RECT_SEED, 5, 4.0)
+    x, y, area, active = mesh.x, mesh.y, mesh.area, mesh.active
+    f = np.exp(-(x * x + y * y)) * np.cos(2.0 * x) + 1e-3 * np.random.default_rng(5).random(mesh.n)
+    eps = mesh.max_edge_length ** 0.75
+    order = np.argsort(_hilbert2d(x, y), kind="stable")
+    src = order[active[order] != 0]
+    mid = (len(order) // 2) // 512 * 512
+    tg = order[mid:mid + 512]
+    sums, stats = _plane_pse_fp32c_block(np.stack([x[tg], y[tg]], 1), f[tg], np.stack([x[src], y[src]], 1), f[src],
+                                         area[src], eps, kernel, np.random.default_rng(13))
+    assert min(stats.values()) > 0, stats
+    got = sums * ((4.0 if kernel == "gauss" else 1.0) / np.pi / eps ** 4)
+    oker = oracle_mod.PSE_K8_CHORD if kernel == "k8" else oracle_mod.PSE_GAUSS_CHORD
+    ref = oracle_mod.pse_laplacian(x, y, None, f, area, active, eps, 1.0, oker)
+    err = np.abs(got - ref[tg]).max() / np.abs(ref).max()
+    assert err <= 1e-4, err
