@@ -397,6 +397,17 @@ def test_pse_kernel_constants_match_the_reference(oracle_mod):
     assert np.abs(k1.astype(D) - ref1).max() <= 1e-6 * 20.0
 
 
+def _ln_emulation():
+    """The float32 emulation of the sweeps' logarithm, from tests/test_ln_table.py (loaded by
+    path, whatever the import mode)."""
+    import importlib.util
+    from pathlib import Path
+    spec = importlib.util.spec_from_file_location("_ln_table_emulation", Path(__file__).with_name("test_ln_table.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.ln_q_emulated
+
+
 _SERIES = [F(3.1746032e-4), F(1.7857143e-3), F(1.1111111e-2), F(8.3333336e-2), F(1.0)]
 
 
@@ -592,7 +603,7 @@ def _stream_fp32c_block(T, ct, groups, s_abs):
     c_i - c_j (a self pair: d = 0, ln 1); the device logarithm (the table sequence of
     ln_q2_shift, emulated as in test_ln_table); FP32 partials flushed into TwoSum pairs every
     32 sources.  Returns the FP64 sums of S ln q for both strengths."""
-    from test_ln_table import ln_q_emulated
+    ln_q_emulated = _ln_emulation()
     nt = len(T)
     th, tl = zip(*(_split2(T[:, k]) for k in range(3)))
     nc = (-ct).astype(F) + F(2.0 ** -100)
@@ -682,7 +693,7 @@ def _plane_stream_fp32c_block(T, P, S):
     strengths, as a hi/lo pair); the terms S_j (ln u_j - k ln 2) by the device logarithm,
     far groups summed whole, near groups (the two-float form; a self pair takes u -> 1)
     flushed every 16 sources.  Returns sum_j S_j ln u_j in FP64, as the sweep writes it."""
-    from test_ln_table import ln_q_emulated
+    ln_q_emulated = _ln_emulation()
     nt = len(T)
     (txh, txl), (tyh, tyl) = _split2(T[:, 0]), _split2(T[:, 1])
     warps = []
