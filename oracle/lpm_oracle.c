@@ -3,7 +3,9 @@
  *
  * The checker for the CUDA library: the tests compare the GPU results against these
  * loops, and the benchmark's CPU-baseline leg times them on the host cores.  Nothing in
- * the shipped library calls this file.  See lpm_oracle.h for what pins each routine.
+ * the shipped library calls this file.  See lpm_oracle.h for what pins each routine
+ * (the PSE Laplacian: the reference's regression thresholds; the BVE and planar sums:
+ * parity unpinned beyond known answers, as the reference ships no golden vectors).
  *
  * Build: -O3 -fopenmp -ffp-contract=off (no fused multiply-add, so every product and
  * sum is rounded exactly where the Fortran source rounds it).

@@ -15,8 +15,8 @@
  * solid-body known answer of examples/BVESolidBody.f90:231-243; the mesh inputs
  * by the counts and area invariants of tests/IcosTriMeshTester.f90:72-89.  The
  * reference ships no golden vectors for the BVE or planar sums and cannot be
- * built here (Fortran + MPI), so those two sums are parity-unpinned beyond the
- * known answers.
+ * built here (Fortran + MPI).  Parity unpinned: beyond the known answers, the BVE
+ * and planar sums rest on this restatement alone.
  */
 #ifndef LPM_ORACLE_H
 #define LPM_ORACLE_H
