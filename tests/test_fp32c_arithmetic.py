@@ -1,5 +1,5 @@
-"""The FP32C sphere-BVE arithmetic restated in float32 numpy and checked on the CPU against
-the oracle's FP64 sum (the reference loop src/SphereBVESolver.f90:395-420).
+"""The FP32C arithmetic of the GPU sweeps restated in float32 numpy and checked on the CPU
+against the oracle's FP64 sums, first the sphere BVE (src/SphereBVESolver.f90:395-420).
 
 The restatement follows the three kernels of one FP32C velocity sum, operation for operation:
 - bve_rel_prep_kernel: sources in Hilbert-curve order (the 30-bit key of the cell of a
@@ -19,12 +19,12 @@ is rounded twice, which can differ from the fused result by one ulp in rare ties
 approximate reciprocal is the rounded reciprocal times 1 + delta, |delta| <= 2^-23, drawn
 from a seeded generator.
 
-The planar sweeps (plane_rel_sweep_kernel, plane_pse_rel_sweep_kernel,
-plane_swe_rel_sweep_kernel) and the sphere PSE sweeps
-(pse_rel_prep_kernel, pse_rel_sweep_kernel with its group cutoff: Laplacian, gradient and
-divergence) and the stream functions (stream_rel_sweep_kernel and
-plane_stream_rel_sweep_kernel, with the device logarithm) are restated the same way, and the PSE pair kernels' constants are checked against the
-reference's kernel functions.
+The other FP32C sweeps are restated the same way: the planar velocity, PSE and SWE sweeps
+(plane_rel_sweep_kernel, plane_pse_rel_sweep_kernel, plane_swe_rel_sweep_kernel), the sphere
+PSE sweeps with their group cutoff (pse_rel_sweep_kernel: Laplacian, gradient, divergence),
+the sphere SWE velocity sweep and both stream-function sweeps (stream_rel_sweep_kernel,
+plane_stream_rel_sweep_kernel, with the device logarithm).  The PSE pair kernels' constants
+are checked against the reference's kernel functions.
 
 This pins the precision design, not the kernels: the GPU tests check the CUDA path itself
 against the oracle.  The same data in plain FP32 (1 - p_i.p_j and FP32 sums) misses the 1e-6
@@ -939,3 +939,80 @@ def test_plane_swe_fp32c_arithmetic_meets_the_bar(built_lib, oracle_mod):
     err_u = max(np.abs(s[:, 0] - ref[0][ib:ie]).max(), np.abs(s[:, 1] - ref[1][ib:ie]).max()) / vel
     err_dd = np.abs(ddot - ref[2][ib:ie]).max() / np.abs(ref[2]).max()
     assert err_u <= 1e-6 and err_dd <= 2e-6, (err_u, err_dd)
+
+
+def _sphere_swe_fp32c_block(T, ct, groups, s_p, rng):
+    """The sphere SWE velocity sweep (stream_rel_prep_kernel with S_r = -zeta A / (2 pi a^2)
+    and S_p = div A / (2 pi a^2), sphere_swe_rel_sweep_kernel with 128 threads x 4 targets):
+    compact and far groups take d = t_hi - s_hi, other near groups the two-float form; with
+    q = |d|^2 - c_i - c_j and 1/q = 0 for the self pair, the seven sums Dr = sum (S_r/q) d,
+    Dp = sum (S_p/q) d and W = sum S_p/q, FP32 per 256-source tile, merged by TwoSum."""
+    nt = len(T)
+    th, tl = zip(*(_split2(T[:, k]) for k in range(3)))
+    nc = (-ct).astype(F) + F(2.0 ** -100)
+    warps = []
+    for wi in range(THREADS // 32):
+        idx = np.array([wi * 32 + lane + k * THREADS for k in range(4) for lane in range(32)])
+        warps.append(idx[idx < nt])
+    stats = dict(far=0, near=0)
+    hi, lo = np.zeros((nt, 7), F), np.zeros((nt, 7), F)
+    for g0 in range(0, len(groups), TILE // GROUP):
+        acc = np.zeros((nt, 7), F)
+        for gi in range(g0, min(g0 + TILE // GROUP, len(groups))):
+            g = groups[gi]
+            sp = s_p[gi * GROUP:gi * GROUP + len(g["S"])]
+            t = np.stack([(th[k] - g["oh"][k]) + (tl[k] - g["ol"][k]) for k in range(3)], 1)
+            n2 = _fma(t[:, 2], t[:, 2], _fma(t[:, 1], t[:, 1], t[:, 0] * t[:, 0]))
+            for w in warps:
+                tw = t[w]
+                if g["compact"] or not (n2[w] < (F(3) * g["R"]) * (F(3) * g["R"])).any():
+                    stats["far"] += 1
+                    d = tw[:, None, :] + g["nsh"][None, :, :]
+                else:
+                    stats["near"] += 1
+                    tt = [_rel2(th[k][w], tl[k][w], g["oh"][k], g["ol"][k]) for k in range(3)]
+                    d = np.stack([(tt[k][0][:, None] + g["nsh"][None, :, k]) + (tt[k][1][:, None] + g["nsl"][None, :, k])
+                                  for k in range(3)], 2)
+                u = _fma(d[:, :, 2], d[:, :, 2], _fma(d[:, :, 1], d[:, :, 1], d[:, :, 0] * d[:, :, 0]))
+                q = u + (nc[w][:, None] + g["ncj"][None, :])
+                inv = np.where(u != 0, _rcp(np.where(u != 0, q, F(1)), rng), F(0))
+                wr, wp = g["S"][None, :] * inv, sp[None, :] * inv
+                for j in range(d.shape[1]):
+                    for k in range(3):
+                        acc[w, k] = _fma(wr[:, j], d[:, j, k], acc[w, k])
+                        acc[w, 3 + k] = _fma(wp[:, j], d[:, j, k], acc[w, 3 + k])
+                    acc[w, 6] = wp[:, j] + acc[w, 6]
+        for c in range(7):
+            hi[:, c], e = _two_sum(hi[:, c], acc[:, c])
+            lo[:, c] = lo[:, c] + e
+    return hi.astype(D) + lo.astype(D), stats
+
+
+def test_sphere_swe_fp32c_arithmetic_meets_the_bar(case, oracle_mod):
+    """The sphere SWE integrals' velocity (SWESphereRHSIntegrals, src/SphereSWESolver.f90:
+    299-372) the same way at icosahedral nest 5 (the RH4 + Gaussian vorticity, a divergence
+    0.1 cos 3z), the CTA of 512 targets at the middle of the particle list: with the finish
+    kernel's u = Dr x p_i + Dp - p_i W in FP64, within 1e-6 of max|(u, v, w)| of the oracle
+    (3.9e-7 measured)."""
+    P = np.stack([case["x"], case["y"], case["z"]], 1)
+    n = len(P)
+    zeta, area, active = case["zeta"], case["area"], case["active"]
+    div = 0.1 * np.cos(3.0 * case["z"])
+    sh = 1.0 + 0.2 * case["z"]
+    c = np.einsum("ij,ij->i", P, P) - 1.0
+    src = np.nonzero(active)[0]
+    src = src[np.argsort(_hilbert30(P[src]), kind="stable")]
+    k2 = 1.0 / (2.0 * np.pi)
+    groups = _groups(P[src], c[src], -zeta[src] * area[src] * k2)
+    s_p = (div[src] * area[src] * k2).astype(F)
+    ib = n // 2
+    ie = ib + THREADS * 4
+    T = P[ib:ie]
+    s, stats = _sphere_swe_fp32c_block(T, c[ib:ie], groups, s_p, np.random.default_rng(15))
+    assert min(stats.values()) > 0, stats
+    vel = np.cross(s[:, 0:3], T) + s[:, 3:6] - T * s[:, 6:7]
+    ref = oracle_mod.swe_sphere_rhs(case["x"], case["y"], case["z"], zeta, div, sh, area, active, 1.0, 1.0, 0.25,
+                                    ib=ib, ie=ie)
+    ref_v = np.stack(ref[:3], 1)
+    err = np.abs(vel - ref_v).max() / np.abs(ref_v).max()
+    assert err <= 1e-6, err
