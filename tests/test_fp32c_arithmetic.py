@@ -22,8 +22,10 @@ from a seeded generator.
 The other FP32C sweeps are restated the same way: the planar velocity, PSE and SWE sweeps
 (plane_rel_sweep_kernel, plane_pse_rel_sweep_kernel, plane_swe_rel_sweep_kernel), the sphere
 PSE sweeps with their group cutoff (pse_rel_sweep_kernel: Laplacian, gradient, divergence),
-the sphere SWE velocity sweep and both stream-function sweeps (stream_rel_sweep_kernel,
-plane_stream_rel_sweep_kernel, with the device logarithm).  The PSE pair kernels' constants
+the sphere SWE velocity sweep, both stream-function sweeps (stream_rel_sweep_kernel,
+plane_stream_rel_sweep_kernel, with the device logarithm) and the beta-plane velocity sweep
+(beta_rel_sweep_kernel: the complex far form and the direct form with the library's own
+sin, cos, sinh and cosh reductions).  The PSE pair kernels' constants
 are checked against the reference's kernel functions.
 
 This pins the precision design, not the kernels: the GPU tests check the CUDA path itself
@@ -1015,4 +1017,150 @@ def test_sphere_swe_fp32c_arithmetic_meets_the_bar(case, oracle_mod):
                                     ib=ib, ie=ie)
     ref_v = np.stack(ref[:3], 1)
     err = np.abs(vel - ref_v).max() / np.abs(ref_v).max()
+    assert err <= 1e-6, err
+
+
+_KM = F(12582912.0)
+
+
+def _perturb(v, rng):
+    """A float64 value rounded to float32 and moved by a relative 2^-22 at most: a model of a
+    library function accurate to an ulp or two (expf, sincospif)."""
+    return (v.astype(F).astype(D) * (1.0 + rng.uniform(-1, 1, v.shape) * 2.0 ** -22)).astype(F)
+
+
+def _beta_deltas(txh, txl, tyh, tyl, sxh, sxl, syh, syl):
+    """beta_deltas2: the x offset wrapped into [-1/2, 1/2] keeping the rounding of its hi
+    difference (TwoSum), and dy from the hi/lo parts."""
+    nxh = -sxh
+    dh = txh + nxh
+    bb = dh - txh
+    dv = dh - bb
+    e = (txh - dv) + (nxh - bb)
+    nn = (dh + _KM) - _KM
+    lo = e + (txl - sxl)
+    return (dh - nn) + lo, (tyh - syh) + (tyl - syl)
+
+
+def _beta_direct(tt, dy, S, rng):
+    """BetaF32::interact2's terms (-S sinh(2 pi dy), S sin(2 pi dx)) / (cosh - cos) by half
+    angles: sin(pi t), cos(pi t) and sinh, cosh of a = pi |dy| reduced by k ln 2, with the
+    library's polynomial coefficients; returns the (u, v) terms."""
+    t2 = tt * tt
+    ps = _fma(np.full(tt.shape, F(-0.00737043097615242)), t2, np.full(tt.shape, F(0.08214588463306427)))
+    for cf in (-0.5992645025253296, 2.550163984298706, -5.167712688446045, 3.1415927410125732):
+        ps = _fma(ps, t2, np.full(tt.shape, F(cf)))
+    sn = ps * tt
+    pc = _fma(np.full(tt.shape, F(0.001929574296809733)), t2, np.full(tt.shape, F(-0.025806890800595284)))
+    for cf in (0.23533062636852264, -1.3352627754211426, 4.058712005615234, -4.934802055358887, 1.0):
+        pc = _fma(pc, t2, np.full(tt.shape, F(cf)))
+    cs = pc
+    a = np.minimum(F(3.1415927) * np.abs(dy), F(87))
+    kb = _fma(a, np.full(a.shape, F(1.442695)), np.full(a.shape, _KM))
+    kf = kb - _KM
+    rr = _fma(-kf, np.full(a.shape, F(0.69314575)), a)
+    rr = _fma(-kf, np.full(a.shape, F(1.4286068e-06)), rr)
+    r2 = rr * rr
+    shr = _fma(rr * r2, _fma(_fma(r2, np.full(a.shape, F(1.9841270e-4)), np.full(a.shape, F(8.3333333e-3))), r2,
+                             np.full(a.shape, F(0.16666667))), rr)
+    chr_ = _fma(_fma(_fma(_fma(r2, np.full(a.shape, F(2.4801587e-5)), np.full(a.shape, F(1.3888889e-3))), r2,
+                          np.full(a.shape, F(4.1666667e-2))), r2, np.full(a.shape, F(0.5))), r2, np.full(a.shape, F(1)))
+    pk = ((np.uint32(0x3F800000) - (kb.view(np.uint32) << np.uint32(23))).astype(np.uint32)).view(F)
+    sc = pk + pk
+    q = pk * pk
+    om, op = F(1) - q, F(1) + q
+    shp = np.copysign(_fma(om, chr_, op * shr), dy)
+    chp = _fma(op, chr_, om * shr)
+    snp, csp = sn * sc, cs * sc
+    den = _fma(shp, shp, _fma(snp, snp, np.full(a.shape, F(2.0 ** -100))))
+    w = S * _rcp(den, rng)
+    return -(w * shp), chp, w * snp, csp
+
+
+def _beta_fp32c_block(T, P, S, rng):
+    """The beta-plane velocity sweep (beta_rel_prep_kernel, beta_rel_sweep_kernel with 128
+    threads x 4 targets): groups of 64 sources in curve order with e_j = exp(2 pi i (z_j - z_o))
+    and S_j e_j from FP64; per warp and group the complex far form v + i u = i (S_g + 2 G),
+    G = sum S_j e_j / (e_i - e_j), when every target is beyond max(4 R, 0.02) of z_o in the
+    periodic distance, and the direct form otherwise; FP32 sums per 256-source tile merged by
+    TwoSum.  expf and sincospif of e_i are modelled as the rounded values times 1 + delta,
+    |delta| <= 2^-22.  Returns (u, v) in FP64."""
+    nt = len(T)
+    (txh, txl), (tyh, tyl) = _split2(T[:, 0]), _split2(T[:, 1])
+    warps = []
+    for wi in range(THREADS // 32):
+        idx = np.array([wi * 32 + lane + k * THREADS for k in range(4) for lane in range(32)])
+        warps.append(idx[idx < nt])
+    stats = dict(far=0, near=0)
+    hi, lo = np.zeros((nt, 2), F), np.zeros((nt, 2), F)
+    for t0 in range(0, len(P), 256):
+        acc = np.zeros((nt, 2), F)
+        for g0 in range(t0, min(t0 + 256, len(P)), 64):
+            Q, s64 = P[g0:g0 + 64], S[g0:g0 + 64]
+            s = s64.astype(F)
+            o = Q.mean(0)
+            R = np.sqrt(((Q - o) ** 2).sum(1)).astype(F).max()
+            rg = R if R <= F(2) else F(3e37)
+            sg = F(s.astype(D).sum())
+            (oxh, oxl), (oyh, oyl) = _split2(o[:1]), _split2(o[1:])
+            ang = 2.0 * np.pi * (Q[:, 0] - o[0])
+            mag = np.exp(-2.0 * np.pi * (Q[:, 1] - o[1]))
+            ere, eim = mag * np.cos(ang), mag * np.sin(ang)
+            fre, fim = ere.astype(F), eim.astype(F)
+            sre, sim = (s.astype(D) * ere).astype(F), (s.astype(D) * eim).astype(F)
+            dx, dy = _beta_deltas(txh, txl, tyh, tyl, oxh[0], oxl[0], oyh[0], oyl[0])
+            n2 = _fma(dy, dy, dx * dx)
+            lim = max((F(4) * rg) * (F(4) * rg), F(4e-4))
+            (sxh, sxl), (syh, syl) = _split2(Q[:, 0]), _split2(Q[:, 1])
+            for w in warps:
+                m = len(w)
+                if not (~(n2[w] > lim)).any():
+                    stats["far"] += 1
+                    a2 = (F(2) * dx[w]).astype(D) * np.pi
+                    sn_, cs_ = _perturb(np.sin(a2), rng), _perturb(np.cos(a2), rng)
+                    mm_ = _perturb(np.exp((F(-6.2831853) * np.clip(dy[w], F(-6), F(6))).astype(D)), rng)
+                    er, ei = mm_ * cs_, mm_ * sn_
+                    br = er[:, None] - fre[None, :]
+                    bi = ei[:, None] - fim[None, :]
+                    inv = _rcp(_fma(bi, bi, br * br), rng)
+                    nr = _fma(np.broadcast_to(sim[None, :], bi.shape), bi, sre[None, :] * br)
+                    ni = _fma(np.broadcast_to(-sre[None, :], bi.shape), bi, sim[None, :] * br)
+                    gre, gim = np.zeros(m, F), np.zeros(m, F)
+                    for j in range(br.shape[1]):
+                        gre = _fma(nr[:, j], inv[:, j], gre)
+                        gim = _fma(ni[:, j], inv[:, j], gim)
+                    acc[w, 0] = acc[w, 0] + (sg + F(2) * gre)
+                    acc[w, 1] = acc[w, 1] - F(2) * gim
+                else:
+                    stats["near"] += 1
+                    tt, dyy = _beta_deltas(txh[w][:, None], txl[w][:, None], tyh[w][:, None], tyl[w][:, None],
+                                           sxh[None, :], sxl[None, :], syh[None, :], syl[None, :])
+                    nwsh, chp, wsn, csp = _beta_direct(tt, dyy, s[None, :], rng)
+                    for j in range(tt.shape[1]):
+                        acc[w, 0] = _fma(nwsh[:, j], chp[:, j], acc[w, 0])
+                        acc[w, 1] = _fma(wsn[:, j], csp[:, j], acc[w, 1])
+        for c in range(2):
+            hi[:, c], e = _two_sum(hi[:, c], acc[:, c])
+            lo[:, c] = lo[:, c] + e
+    return hi.astype(D) + lo.astype(D), stats
+
+
+def test_beta_fp32c_arithmetic_meets_the_bar(built_lib, oracle_mod):
+    """The beta-plane velocity (BetaPlaneVelocity, src/BetaPlaneSolver.f90:227-268) the same
+    way on the beta plane's quad refinement of [0, 1] x [-1/2, 1/2] at nest 5 (a Rossby wave
+    plus a zonal jet), the CTA of 512 targets at the middle of the particle list: within
+    1e-6 of max|(u, v)| of the oracle, with far and near groups (1.3e-7 measured)."""
+    import workloads
+    c = workloads.config_beta_plane(5)
+    x, y, zeta, area, active = c["x"], c["y"], c["zeta"], c["area"], c["active"]
+    n = len(x)
+    src = np.nonzero(active)[0]
+    src = src[np.argsort(_hilbert2d(x[src], y[src]), kind="stable")]
+    ib = n // 2
+    ie = ib + THREADS * 4
+    uv, stats = _beta_fp32c_block(np.stack([x[ib:ie], y[ib:ie]], 1), np.stack([x[src], y[src]], 1),
+                                  0.5 * zeta[src] * area[src], np.random.default_rng(16))
+    assert min(stats.values()) > 0, stats
+    ref = np.stack(oracle_mod.beta_plane_velocity(x, y, zeta, area, active, ib, ie), 1)
+    err = np.abs(uv - ref).max() / np.abs(ref).max()
     assert err <= 1e-6, err
