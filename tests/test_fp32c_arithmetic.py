@@ -23,9 +23,9 @@ The other FP32C sweeps are restated the same way: the planar velocity, PSE and S
 (plane_rel_sweep_kernel, plane_pse_rel_sweep_kernel, plane_swe_rel_sweep_kernel), the sphere
 PSE sweeps with their group cutoff (pse_rel_sweep_kernel: Laplacian, gradient, divergence),
 the sphere SWE velocity sweep, both stream-function sweeps (stream_rel_sweep_kernel,
-plane_stream_rel_sweep_kernel, with the device logarithm) and the beta-plane velocity sweep
-(beta_rel_sweep_kernel: the complex far form and the direct form with the library's own
-sin, cos, sinh and cosh reductions).  The PSE pair kernels' constants
+plane_stream_rel_sweep_kernel, with the device logarithm) and both beta-plane sweeps
+(beta_rel_sweep_kernel, beta_stream_rel_sweep_kernel: the complex far forms and the direct
+forms with the library's own sin, cos, sinh and cosh reductions).  The PSE pair kernels' constants
 are checked against the reference's kernel functions.
 
 This pins the precision design, not the kernels: the GPU tests check the CUDA path itself
@@ -1164,3 +1164,165 @@ def test_beta_fp32c_arithmetic_meets_the_bar(built_lib, oracle_mod):
     ref = np.stack(oracle_mod.beta_plane_velocity(x, y, zeta, area, active, ib, ie), 1)
     err = np.abs(uv - ref).max() / np.abs(ref).max()
     assert err <= 1e-6, err
+
+
+def _beta_offsets_ff(txh, txl, tyh, tyl, xo, yo):
+    """beta_offsets_ff: offsets from a float origin as float-float pairs, x wrapped into
+    [-1/2, 1/2], each hi part carrying the rounding of its difference."""
+    nxo, nyo = -xo, -yo
+    dx, dy = txh + nxo, tyh + nyo
+    bx, by = dx - txh, dy - tyh
+    ex = (txh - (dx - bx)) + (nxo - bx)
+    ey = (tyh - (dy - by)) + (nyo - by)
+    nn = (dx + _KM) - _KM
+    th = dx - nn
+    tl_, ul = ex + txl, ey + tyl
+    xh = th + tl_
+    yh = dy + ul
+    return xh, tl_ - (xh - th), yh, ul - (yh - dy)
+
+
+def _beta_stream_direct(tt, dy, ln_q):
+    """BetaStreamF32::interact2's ln(cosh 2 pi dy - cos 2 pi dx) by half angles, the exponent
+    of the sinh / cosh reduction taken out of the logarithm; 0 for the self pair."""
+    t2 = tt * tt
+    ps = _fma(np.full(tt.shape, F(-0.00737043097615242)), t2, np.full(tt.shape, F(0.08214588463306427)))
+    for cf in (-0.5992645025253296, 2.550163984298706, -5.167712688446045, 3.1415927410125732):
+        ps = _fma(ps, t2, np.full(tt.shape, F(cf)))
+    sn = ps * tt
+    a = F(3.1415927) * np.abs(dy)
+    kb = _fma(a, np.full(a.shape, F(1.442695)), np.full(a.shape, _KM))
+    kf = kb - _KM
+    rr = _fma(-kf, np.full(a.shape, F(0.69314575)), a)
+    rr = _fma(-kf, np.full(a.shape, F(1.4286068e-06)), rr)
+    r2 = rr * rr
+    shr = _fma(rr * r2, _fma(_fma(r2, np.full(a.shape, F(1.9841270e-4)), np.full(a.shape, F(8.3333333e-3))), r2,
+                             np.full(a.shape, F(0.16666667))), rr)
+    chr_ = _fma(_fma(_fma(_fma(r2, np.full(a.shape, F(2.4801587e-5)), np.full(a.shape, F(1.3888889e-3))), r2,
+                          np.full(a.shape, F(4.1666667e-2))), r2, np.full(a.shape, F(0.5))), r2, np.full(a.shape, F(1)))
+    k = kb.view(np.uint32).astype(np.int64) - 0x4B400000
+    c = np.minimum(k, 126).astype(np.uint32)
+    pk = (np.uint32(0x3F800000) - (c << np.uint32(23))).astype(np.uint32).view(F)
+    sc, q = pk + pk, pk * pk
+    shp = _fma(F(1) - q, chr_, (F(1) + q) * shr)
+    snp = sn * sc
+    x = _fma(shp, shp, snp * snp)
+    lg = ln_q(np.where(x > 0, x, F(1)), (1 - 2 * k).astype(D))
+    return np.where(x > 0, lg, F(0))
+
+
+def _beta_stream_fp32c_block(T, P, wr_, wa_, rng):
+    """The beta-plane stream-function sweep (beta_stream_rel_prep_kernel,
+    beta_stream_rel_sweep_kernel with 128 threads x 4 targets): groups of 64 about their
+    centroid rounded to float, with W and C per group; a warp whose targets are all beyond
+    max(4 R, 0.02) and within |dy| <= 6 of the origin adds sum_j w_j ln|e_i - e_j|^2 (less
+    s ln 2, s the exponent of |e_i - 1|^2), W (s ln 2 + 2 pi dy) and C, every part
+    compensated; other warps take the direct form flushed every 8 sources.  e_i's expf and
+    sincospif are modelled as for the velocity.  Returns (psi_rel, psi_abs) in FP64."""
+    ln_q = _ln_emulation()
+    k2h, k2l = F(6.2831854820251465), F(-1.7484556025237907e-07)
+    kl2h, kl2l = F(0.693145751953125), F(1.4286068202862268e-06)
+    nt = len(T)
+    (txh, txl), (tyh, tyl) = _split2(T[:, 0]), _split2(T[:, 1])
+    warps = []
+    for wi in range(THREADS // 32):
+        idx = np.array([wi * 32 + lane + k * THREADS for k in range(4) for lane in range(32)])
+        warps.append(idx[idx < nt])
+    stats = dict(far=0, near=0)
+    hi, lo = np.zeros((nt, 2), F), np.zeros((nt, 2), F)
+
+    def comp(c, w, v):
+        hi[w, c], e = _two_sum(hi[w, c], v)
+        lo[w, c] = lo[w, c] + e
+
+    for g0 in range(0, len(P), 64):
+        Q = P[g0:g0 + 64]
+        wr, wa = wr_[g0:g0 + 64].astype(F), wa_[g0:g0 + 64].astype(F)
+        o = Q.mean(0).astype(F)
+        cx, cy = D(o[0]), D(o[1])
+        R = np.sqrt(((Q - [cx, cy]) ** 2).sum(1)).astype(F).max()
+        rg = R if R <= F(2) else F(3e37)
+        carg = 2.0 * np.pi * (Q[:, 1] - cy) - np.log(2.0)
+        Wr, Wa = F(wr.astype(D).sum()), F(wa.astype(D).sum())
+        Cr, Ca = F((wr.astype(D) * carg).sum()), F((wa.astype(D) * carg).sum())
+        mag = np.exp(-2.0 * np.pi * (Q[:, 1] - cy))
+        fre = (mag * np.cos(2.0 * np.pi * (Q[:, 0] - cx))).astype(F)
+        fim = (mag * np.sin(2.0 * np.pi * (Q[:, 0] - cx))).astype(F)
+        dx, dxl, dy, dyl = _beta_offsets_ff(txh, txl, tyh, tyl, o[0], o[1])
+        n2 = _fma(dy, dy, dx * dx)
+        lim = max((F(4) * rg) * (F(4) * rg), F(4e-4))
+        near_t = ~(n2 > lim) | ~(np.abs(dy) <= F(6))
+        (sxh, sxl), (syh, syl) = _split2(Q[:, 0]), _split2(Q[:, 1])
+        for w in warps:
+            m = len(w)
+            if not near_t[w].any():
+                stats["far"] += 1
+                a2 = (F(2) * dx[w]).astype(D) * np.pi
+                s_, c_ = _perturb(np.sin(a2), rng), _perturb(np.cos(a2), rng)
+                dl = k2h * dxl[w]
+                cc = _fma(-s_, dl, c_)
+                ss = _fma(c_, dl, s_)
+                ah = k2h * dy[w]
+                al = _fma(np.full(m, k2h), dy[w], -ah) + _fma(np.full(m, k2h), dyl[w], k2l * dy[w])
+                mm_ = _perturb(np.exp((-ah).astype(D)), rng) * (F(1) - al)
+                er, ei = mm_ * cc, mm_ * ss
+                d1 = er - F(1)
+                m2 = _fma(ei, ei, d1 * d1)
+                ex = (m2.view(np.uint32) >> np.uint32(23)).astype(np.int64) - 127
+                exf = ex.astype(F)
+                sl = exf * kl2h
+                kh = sl + ah
+                bb = kh - sl
+                te = (sl - (kh - bb)) + (ah - bb)
+                kl = (te + al) + exf * kl2l
+                br = er[:, None] - fre[None, :]
+                bi = ei[:, None] - fim[None, :]
+                lg = ln_q(_fma(bi, bi, br * br), ex[:, None].astype(D))
+                ar, aa = np.zeros(m, F), np.zeros(m, F)
+                for j in range(lg.shape[1]):
+                    ar = _fma(np.full(m, wr[j]), lg[:, j], ar)
+                    aa = _fma(np.full(m, wa[j]), lg[:, j], aa)
+                for c, (W, C, acc) in enumerate(((Wr, Cr, ar), (Wa, Ca, aa))):
+                    pr = W * kh
+                    comp(c, w, pr)
+                    comp(c, w, np.full(m, C))
+                    comp(c, w, _fma(np.full(m, W), kl, _fma(np.full(m, W), kh, -pr)) + acc)
+            else:
+                stats["near"] += 1
+                tt, dyy = _beta_deltas(txh[w][:, None], txl[w][:, None], tyh[w][:, None], tyl[w][:, None],
+                                       sxh[None, :], sxl[None, :], syh[None, :], syl[None, :])
+                g = _beta_stream_direct(tt, dyy, ln_q)
+                ar, aa = np.zeros(m, F), np.zeros(m, F)
+                for j in range(g.shape[1]):
+                    ar = _fma(np.full(m, wr[j]), g[:, j], ar)
+                    aa = _fma(np.full(m, wa[j]), g[:, j], aa)
+                    if (j + 1) % 8 == 0 or j + 1 == g.shape[1]:
+                        comp(0, w, ar)
+                        comp(1, w, aa)
+                        ar, aa = np.zeros(m, F), np.zeros(m, F)
+    return hi.astype(D) + lo.astype(D), stats
+
+
+def test_beta_stream_fp32c_arithmetic_meets_the_bar(built_lib, oracle_mod):
+    """The beta plane's stream functions (SetStreamFunctionsOnMesh, src/BetaPlane.f90:399-442)
+    the same way on the beta plane's quad nest 5 (absolute vorticity zeta + 3 y), the CTA of
+    512 targets at the middle of the particle list: both within 1e-6 of max|psi| of the
+    oracle, with far and near groups (1.3e-7 and 1.2e-7 measured)."""
+    import workloads
+    c = workloads.config_beta_plane(5)
+    x, y, zeta, area, active = c["x"], c["y"], c["zeta"], c["area"], c["active"]
+    absv = zeta + 3.0 * y
+    n = len(x)
+    src = np.nonzero(active)[0]
+    src = src[np.argsort(_hilbert2d(x[src], y[src]), kind="stable")]
+    ib = n // 2
+    ie = ib + THREADS * 4
+    k4 = 1.0 / (4.0 * np.pi)
+    psi, stats = _beta_stream_fp32c_block(np.stack([x[ib:ie], y[ib:ie]], 1), np.stack([x[src], y[src]], 1),
+                                          zeta[src] * area[src] * k4, absv[src] * area[src] * k4,
+                                          np.random.default_rng(17))
+    assert min(stats.values()) > 0, stats
+    ref = oracle_mod.beta_plane_stream(x, y, zeta, absv, area, active, ib, ie)
+    for k in range(2):
+        err = np.abs(psi[:, k] - ref[k]).max() / np.abs(ref[k]).max()
+        assert err <= 1e-6, err
