@@ -25,7 +25,9 @@ PSE sweeps with their group cutoff (pse_rel_sweep_kernel: Laplacian, gradient, d
 the sphere SWE velocity sweep, both stream-function sweeps (stream_rel_sweep_kernel,
 plane_stream_rel_sweep_kernel, with the device logarithm) and both beta-plane sweeps
 (beta_rel_sweep_kernel, beta_stream_rel_sweep_kernel: the complex far forms and the direct
-forms with the library's own sin, cos, sinh and cosh reductions).  The PSE pair kernels' constants
+forms with the library's own sin, cos, sinh and cosh reductions), and the allocation-free
+entry point's sweep (bve_sweep_x2_kernel).  The ensemble sweep runs the BVE tile of
+bve_rel_sweep_kernel.  The PSE pair kernels' constants
 are checked against the reference's kernel functions.
 
 This pins the precision design, not the kernels: the GPU tests check the CUDA path itself
@@ -1326,3 +1328,46 @@ def test_beta_stream_fp32c_arithmetic_meets_the_bar(built_lib, oracle_mod):
     for k in range(2):
         err = np.abs(psi[:, k] - ref[k]).max() / np.abs(ref[k]).max()
         assert err <= 1e-6, err
+
+
+def test_noalloc_x2_fp32c_arithmetic_meets_the_bar(built_lib, oracle_mod):
+    """The allocation-free entry point's sweep (noalloc_prep_kernel, bve_sweep_x2_kernel with
+    128 threads x 4 targets, 256-source tiles) the same way: every particle a source in its own
+    order (a passive one with S = 0), d = (t_hi - s_hi) + (t_lo - s_lo) from absolute hi/lo
+    positions, q = |d|^2 - c_i - c_j, FP32 sums per tile merged by TwoSum, u = D x p in FP64.
+    At icosahedral nest 4 (RH4 + Gaussian vortex) the 512 targets at the middle are within 1e-6
+    of max|u| of the oracle (3.0e-7 measured)."""
+    import workloads
+    c = workloads.config_rh54_icos(4)
+    P = np.stack([c["x"], c["y"], c["z"]], 1)
+    zeta, area, active = c["zeta"], c["area"], c["active"]
+    n = len(P)
+    cc = np.einsum("ij,ij->i", P, P) - 1.0
+    sh, sl = zip(*(_split2(P[:, k]) for k in range(3)))
+    ncs = (-cc).astype(F)
+    S = np.where(active != 0, zeta * area * (-1.0 / (2.0 * np.pi)), 0.0).astype(F)
+    ib = n // 2
+    ie = ib + 512
+    T = P[ib:ie]
+    th, tl = zip(*(_split2(T[:, k]) for k in range(3)))
+    nct = (-cc[ib:ie]).astype(F) + F(2.0 ** -100)
+    rng = np.random.default_rng(18)
+    hi, lo = np.zeros((512, 3), F), np.zeros((512, 3), F)
+    for t0 in range(0, n, 256):
+        j = slice(t0, min(t0 + 256, n))
+        d = np.stack([(th[k][:, None] - sh[k][None, j]) + (tl[k][:, None] - sl[k][None, j]) for k in range(3)], 2)
+        q = nct[:, None] + ncs[None, j]
+        for k in range(3):
+            q = _fma(d[:, :, k], d[:, :, k], q)
+        wgt = S[None, j] * _rcp(q, rng)
+        acc = np.zeros((512, 3), F)
+        for jj in range(d.shape[1]):
+            for k in range(3):
+                acc[:, k] = _fma(wgt[:, jj], d[:, jj, k], acc[:, k])
+        for k in range(3):
+            hi[:, k], e = _two_sum(hi[:, k], acc[:, k])
+            lo[:, k] = lo[:, k] + e
+    u = np.cross(hi.astype(D) + lo.astype(D), T)
+    ref = np.stack(oracle_mod.bve_velocity(c["x"], c["y"], c["z"], zeta, area, active, ib=ib, ie=ie), 1)
+    err = _rel_linf(u, ref)
+    assert err <= 1e-6, err
