@@ -43,7 +43,7 @@ enum {
   LPM_ERR_NONFINITE = -4, /* LPM_FLAG_CHECK_FINITE found a NaN/Inf output */
   LPM_ERR_ALLOC = -5,     /* device or host allocation failed */
   LPM_ERR_NO_DEVICE = -6, /* no usable CUDA device */
-  LPM_ERR_STATE = -7      /* handle used in a wrong state */
+  LPM_ERR_STATE = -7      /* call in a wrong state (another device current, wrong handle mode) */
 };
 
 enum { LPM_MODE_FP64 = 0, LPM_MODE_FP32C = 1 };
