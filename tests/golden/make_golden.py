@@ -1,4 +1,5 @@
-"""Generates the golden fixtures under tests/golden/ (run: python tests/golden/make_golden.py).
+"""Generates the golden fixtures under tests/golden/ (run: python tests/golden/make_golden.py,
+or with the argument `operators` for ops_small.npz alone).
 
 The reference (Fortran + MPI) cannot be built in this environment, so the expected outputs
 are produced by the CPU oracle (oracle/lpm_oracle.c), itself pinned by the reference's PSE
@@ -78,5 +79,60 @@ def main():
     print("wrote", sorted(p.name for p in HERE.glob("*.npz")))
 
 
+def operators():
+    """ops_small.npz: the other PSE operators, the SWE integrals and the beta plane, small."""
+    out = {}
+    # sphere: icos nest 2
+    m, zeta = sphere_case(2, 2)
+    x, y, z, a, act = m.x, m.y, m.z, m.area, m.active
+    f = wl.y54(x, y, z)
+    gx, gy, gz = wl.y54_surface_gradient(x, y, z)
+    eps = m.max_edge_length ** 0.5
+    out.update(sx=x, sy=y, sz=z, sa=a, sact=act, szeta=zeta, sf=f, sgx=gx, sgy=gy, sgz=gz, seps=eps)
+    out["grad"] = np.stack(orc.pse_sphere_gradient(x, y, z, f, a, act, eps, 1.0))
+    out["div"] = orc.pse_sphere_divergence(x, y, z, gx, gy, gz, a, act, eps, 1.0)
+    out["sddot"] = orc.pse_sphere_double_dot(x, y, z, gx, gy, gz, a, act, eps, 1.0)
+    q = np.stack([np.cos(np.linspace(0, 6, 16)), np.sin(np.linspace(0, 6, 16)), np.zeros(16)])
+    out["sq"] = q
+    out["sinterp"] = orc.pse_interpolate(x, y, z, f, a, act, eps, q[0], q[1], q[2], 1, 1.0)
+    div = 0.1 * np.cos(3.0 * z)
+    sh = 1.0 + 0.2 * z
+    out.update(sdivv=div, ssh=sh)
+    out["sswe"] = np.stack(orc.swe_sphere_rhs(x, y, z, zeta, div, sh, a, act, 1.0, 1.0, 0.25))
+    # plane: quad nest 3 on [-4, 4]^2
+    mp = lg.PolyMesh2d(lg.QUAD_RECT_SEED, 3, 4.0)
+    px, py, pa, pact = mp.x, mp.y, mp.area, mp.active
+    pf = np.sin(px) * np.cos(0.5 * py)
+    peps = 2.0 * np.sqrt(pa[pact == 1].max())
+    out.update(px=px, py=py, pa=pa, pact=pact, pf=pf, peps=peps)
+    pg = orc.pse_plane_gradient(px, py, pf, pa, pact, peps)
+    out["pgrad"] = np.stack(pg)
+    out["psecond"] = np.stack(orc.pse_plane_second_partials(px, py, pg[0], pg[1], pa, pact, peps))
+    out["pddot"] = orc.pse_plane_double_dot(px, py, pg[0], pg[1], pa, pact, peps)
+    pq = np.stack([np.linspace(-3, 3, 16), np.linspace(2, -2, 16), np.zeros(16)])
+    out["pq"] = pq
+    out["pinterp"] = orc.pse_interpolate(px, py, None, pf, pa, pact, peps, pq[0], pq[1], None, 0, 1.0)
+    vort = np.exp(-(px ** 2 + py ** 2))
+    pdiv = 0.3 * np.exp(-((px - 1) ** 2 + py ** 2))
+    psh = 1.0 + 0.1 * np.cos(px)
+    out.update(pvort=vort, pdivv=pdiv, psh=psh)
+    out["pswe"] = np.stack(orc.swe_plane_rhs(px, py, vort, pdiv, psh, pa, pact, peps))
+    # beta plane: 300 random points on the strip
+    rng = np.random.default_rng(3)
+    bx, by = rng.random(300), rng.uniform(-0.5, 0.5, 300)
+    ba = rng.uniform(0.5, 1.5, 300) / 300
+    bz = np.sin(2 * PI * bx) * np.exp(-8 * by * by)
+    bact = (rng.random(300) < 0.8).astype(np.int32)
+    out.update(bx=bx, by=by, ba=ba, bzeta=bz, bact=bact)
+    out["bvel"] = np.stack(orc.beta_plane_velocity(bx, by, bz, ba, bact))
+    out["bstream"] = np.stack(orc.beta_plane_stream(bx, by, bz, bz + 3.0 * by, ba, bact))
+    np.savez_compressed(HERE / "ops_small.npz", **out)
+    print("wrote ops_small.npz")
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["operators"]:
+        operators()
+    else:
+        main()
+        operators()

@@ -220,3 +220,33 @@ def test_golden_pse(oracle_mod):
                                   2)
     for a, b in ((lk, g["lap_k8"]), (lgs, g["lap_gauss"]), (lp, g["plap"])):
         assert np.abs(a - b).max() <= 1e-12 * np.abs(b).max()
+
+
+def test_golden_operators(oracle_mod):
+    """The other PSE operators, the SWE integrals and the beta plane against ops_small.npz
+    (1e-13 of each result's max: exp, atan2, log and cosh may differ by an ulp between C
+    libraries)."""
+    g = _load("ops_small.npz")
+    o = oracle_mod
+    sx, sy, sz, sa, sact, seps = g["sx"], g["sy"], g["sz"], g["sa"], g["sact"], float(g["seps"])
+    px, py, pa, pact, peps = g["px"], g["py"], g["pa"], g["pact"], float(g["peps"])
+    pg = o.pse_plane_gradient(px, py, g["pf"], pa, pact, peps)
+    got = {
+        "grad": np.stack(o.pse_sphere_gradient(sx, sy, sz, g["sf"], sa, sact, seps, 1.0)),
+        "div": o.pse_sphere_divergence(sx, sy, sz, g["sgx"], g["sgy"], g["sgz"], sa, sact, seps, 1.0),
+        "sddot": o.pse_sphere_double_dot(sx, sy, sz, g["sgx"], g["sgy"], g["sgz"], sa, sact, seps, 1.0),
+        "sinterp": o.pse_interpolate(sx, sy, sz, g["sf"], sa, sact, seps, g["sq"][0], g["sq"][1], g["sq"][2], 1, 1.0),
+        "sswe": np.stack(o.swe_sphere_rhs(sx, sy, sz, g["szeta"], g["sdivv"], g["ssh"], sa, sact, 1.0, 1.0, 0.25)),
+        "pgrad": np.stack(pg),
+        "psecond": np.stack(o.pse_plane_second_partials(px, py, pg[0], pg[1], pa, pact, peps)),
+        "pddot": o.pse_plane_double_dot(px, py, pg[0], pg[1], pa, pact, peps),
+        "pinterp": o.pse_interpolate(px, py, None, g["pf"], pa, pact, peps, g["pq"][0], g["pq"][1], None, 0, 1.0),
+        "pswe": np.stack(o.swe_plane_rhs(px, py, g["pvort"], g["pdivv"], g["psh"], pa, pact, peps)),
+        "bvel": np.stack(o.beta_plane_velocity(g["bx"], g["by"], g["bzeta"], g["ba"], g["bact"])),
+        "bstream": np.stack(o.beta_plane_stream(g["bx"], g["by"], g["bzeta"], g["bzeta"] + 3.0 * g["by"], g["ba"],
+                                                g["bact"])),
+    }
+    for k, v in got.items():
+        ref = g[k]
+        assert v.shape == ref.shape, k
+        assert np.abs(v - ref).max() <= 1e-13 * max(np.abs(ref).max(), 1e-300), k
